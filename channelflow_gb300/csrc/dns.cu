@@ -1,0 +1,1213 @@
+// Host runtime of the GB300 DNS step and the C ABI declared in include/cfgpu.h.
+//
+// A cfgpu_dns owns, on one CUDA device and stream:
+//   * the multistep history ring (u, q and the nonlinear term N per slot),
+//     or the CNAB / CNRK2 state, in the solved-mode layout of common.cuh;
+//   * the per-substep tau tables of the main and of the initialisation
+//     scheme (TauSolver constructor work, done once by k_tau_setup);
+//   * FFT plans/twiddles and the Chebyshev transform matrices;
+//   * work arrays of the nonlinear-term pipeline.
+// Scheme logic follows channelflow/dnsalgo.cpp (MultistepDNS, CNABstyleDNS,
+// RungeKuttaDNS) and the DNS facade channelflow/dns.cpp:22-163.
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/cfgpu.h"
+#include "kernels.h"
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CK(x)                                                                                  \
+  do {                                                                                         \
+    cudaError_t e_ = (x);                                                                      \
+    if (e_ != cudaSuccess) return fail(CFGPU_ECUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+#define CKS(x)                 \
+  do {                         \
+    int s_ = (x);              \
+    if (s_ != CFGPU_OK) return s_; \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// Host-side Chebyshev helpers (chebyshev.cpp) for base flows and constraints
+// ---------------------------------------------------------------------------
+std::vector<double> cheb_diff_h(const std::vector<double>& u, double L) {
+  const int N = (int)u.size();
+  std::vector<double> d(N, 0.0);
+  if (N < 2) return d;
+  const int Nb = N - 1;
+  const double scale = 4.0 / L;
+  d[Nb] = 0.0;
+  d[Nb - 1] = scale * Nb * u[Nb];
+  for (int n = Nb - 2; n >= 0; --n) d[n] = d[n + 2] + scale * (n + 1) * u[n + 1];
+  d[0] *= 0.5;
+  return d;
+}
+double eval_b_h(const std::vector<double>& u) {
+  double s = 0.0;
+  for (int n = (int)u.size() - 1; n >= 0; --n) s += u[n];
+  return s;
+}
+double eval_a_h(const std::vector<double>& u) {
+  double s = 0.0;
+  for (int n = (int)u.size() - 1; n >= 0; --n) s += u[n] * ((n % 2 == 0) ? 1 : -1);
+  return s;
+}
+double mean_h(const std::vector<double>& u) {
+  double s = u[0];
+  for (size_t n = 2; n < u.size(); n += 2) s -= u[n] / (double)(n * n - 1);
+  return s;
+}
+// cos(pi m / d) with the argument reduced exactly first
+long double cospi_ratio(long long m, long long d) {
+  long long r = m % (2 * d);
+  if (r < 0) r += 2 * d;
+  return cosl(3.14159265358979323846264338327950288L * (long double)r / (long double)d);
+}
+// Values at Gauss-Lobatto points -> Chebyshev coefficients (chebyfft, chebyshev.cpp:262-284), direct sum.
+std::vector<double> chebyfft_h(const std::vector<double>& x) {
+  const int N = (int)x.size();
+  std::vector<double> a(N);
+  for (int n = 0; n < N; ++n) {
+    long double Y = (long double)x[0] + ((n % 2 == 0) ? 1.0L : -1.0L) * x[N - 1];
+    for (int j = 1; j < N - 1; ++j) Y += 2.0L * x[j] * cospi_ratio((long long)n * j, N - 1);
+    long double c = Y / (N - 1);
+    if (n == 0 || n == N - 1) c *= 0.5L;
+    a[n] = (double)c;
+  }
+  return a;
+}
+
+// laminarProfile (channelflow/nse.cpp:823-943)
+std::vector<double> laminar_profile(double nu, int constraint, double dPdx, double Ubulk, double Vsuck, double a,
+                                    double b, double ua, double ub, int Ny) {
+  std::vector<double> u(Ny, 0.0);
+  const double H = b - a;
+  double mu = Vsuck * H / nu;
+  if (std::fabs(mu) == 0.0) {
+    if (constraint == CFGPU_BulkVelocity) {
+      u[0] = 0.125 * (ub + ua) + 0.75 * Ubulk;
+      u[1] = 0.5 * (ub - ua);
+      u[2] = 0.375 * (ub + ua) - 0.75 * Ubulk;
+    } else {
+      dPdx *= ((b - a) / 2) * ((b - a) / 2);
+      u[0] = 0.5 * (ub + ua) - 0.25 * dPdx / nu;
+      u[1] = 0.5 * (ub - ua);
+      u[2] = 0.25 * dPdx / nu;
+    }
+    return u;
+  }
+  mu = H * Vsuck / nu;
+  const double ub_ua = ub - ua;
+  const double expm1_mu = std::expm1(-mu);
+  double dPdx_HH_nu = dPdx * H * H / nu;
+  std::vector<double> phys(Ny);
+  const double piN = M_PI / (Ny - 1), radius = (b - a) / 2, center = (b + a) / 2;
+  if (std::fabs(mu) > 1e-01) {
+    if (constraint == CFGPU_BulkVelocity) {
+      const double k = -1.0 / expm1_mu - 1 / mu;
+      dPdx_HH_nu = mu * (Ubulk - ua - ub_ua * k) / (0.5 - k);
+    }
+    for (int i = 0; i < Ny; ++i) {
+      const double y = center + radius * std::cos(i * piN);
+      const double yhat = (y - a) / H;
+      const double e = std::expm1(-mu * yhat);
+      phys[i] = ua + ub_ua * e / expm1_mu + dPdx_HH_nu * (yhat - e / expm1_mu) / mu;
+    }
+  } else {
+    if (constraint == CFGPU_BulkVelocity) {
+      const double mu2 = mu * mu, A = ub - ua, B = ua + ub - 2 * Ubulk;
+      dPdx_HH_nu = 6 * B + mu * (A + mu * (B / 10 + mu2 * (-B / 1400 + mu2 * B / 126000)));
+    }
+    const double one_2 = 1.0 / 2, one_12 = 1.0 / 12, one_24 = 1.0 / 24, one_720 = 1.0 / 720, one_1440 = 1.0 / 1440,
+                 one_30240 = 1.0 / 30240, one_120960 = 1.0 / 120960;
+    for (int i = 0; i < Ny; ++i) {
+      const double y = center + radius * std::cos(i * piN);
+      const double yh = (y - a) / H, yh2 = yh * yh, yh3 = yh2 * yh, yh4 = yh3 * yh, yh_1 = yh - 1;
+      const double sq = (yh * yh_1) * (yh * yh_1);
+      const double t1 =
+          yh + mu * (-one_2 * yh * yh_1 +
+                     mu * (one_12 * yh * yh_1 * (2 * yh - 1) +
+                           mu * (-one_24 * sq + mu * (one_720 * yh * yh_1 * (2 * yh - 1) * (3 * yh2 - 3 * yh - 1) +
+                                                      mu * (-one_1440 * sq * (2 * yh2 - 2 * yh - 1) +
+                                                            mu * (one_30240 * yh * yh_1 * (2 * yh - 1) *
+                                                                  (3 * yh4 - 6 * yh3 + 3 * yh + 1)))))));
+      const double t2 =
+          one_2 * yh * yh_1 +
+          mu * (-one_12 * yh * yh_1 * (2 * yh - 1) +
+                mu * (one_24 * sq +
+                      mu * (-one_720 * yh * yh_1 * (2 * yh - 1) * (3 * yh2 - 3 * yh - 1) +
+                            mu * (one_1440 * sq * (2 * yh2 - 2 * yh - 1) +
+                                  mu * (-one_30240 * yh * yh_1 * (2 * yh - 1) * (3 * yh4 - 6 * yh3 + 3 * yh + 1) +
+                                        mu * (one_120960 * sq * (3 * yh4 - 6 * yh3 + 4 * yh + 2)))))));
+      phys[i] = ua + ub_ua * t1 + dPdx_HH_nu * t2;
+    }
+  }
+  return chebyfft_h(phys);
+}
+
+// ---------------------------------------------------------------------------
+// FFT plans and Chebyshev matrices
+// ---------------------------------------------------------------------------
+bool make_fft_plan(int L, FftPlan& p, std::vector<std::complex<long double>>& tw) {
+  std::vector<int> rs;
+  int n = L;
+  while (n % 4 == 0) { rs.push_back(4); n /= 4; }
+  while (n % 2 == 0) { rs.push_back(2); n /= 2; }
+  while (n % 3 == 0) { rs.push_back(3); n /= 3; }
+  while (n % 5 == 0) { rs.push_back(5); n /= 5; }
+  if (n != 1 || rs.empty() || (int)rs.size() > FFT_MAX_STAGES) return false;
+  memset(&p, 0, sizeof(p));
+  p.L = L;
+  p.nst = (int)rs.size();
+  int Ns = 1, off = 0;
+  tw.clear();
+  const long double PI_L = 3.14159265358979323846264338327950288L;
+  for (int s = 0; s < p.nst; ++s) {
+    const int R = rs[s];
+    p.radix[s] = R;
+    p.Ns[s] = Ns;
+    p.twoff[s] = off;
+    for (int k = 0; k < Ns; ++k)
+      for (int r = 1; r < R; ++r) {
+        // exp(-2 pi i r k / (Ns R)), argument reduced over the integer r*k
+        const long long num = (long long)r * k, den = (long long)Ns * R;
+        const long double ang = -2.0L * PI_L * (long double)(num % den) / (long double)den;
+        tw.emplace_back(cosl(ang), sinl(ang));
+      }
+    off += Ns * (R - 1);
+    Ns *= R;
+  }
+  p.twlen = off;
+  return true;
+}
+
+struct ChebMats {
+  std::vector<double> invA, invB, fwdA, fwdB;  // P x KA, P x KB (row-major)
+};
+
+ChebMats make_cheb_mats(int N) {
+  ChebMats M;
+  const int P = (N + 1) / 2, KA = (N + 1) / 2, KB = (N - 1) / 2, J = (N - 1) / 2;
+  M.invA.assign((size_t)P * KA, 0.0);
+  M.invB.assign((size_t)P * KB, 0.0);
+  M.fwdA.assign((size_t)P * KA, 0.0);
+  M.fwdB.assign((size_t)P * KB, 0.0);
+  for (int j = 0; j < P; ++j) {
+    for (int k = 0; k < KA; ++k) M.invA[j * KA + k] = (double)cospi_ratio(2LL * k * j, N - 1);
+    for (int k = 0; k < KB; ++k) M.invB[j * KB + k] = (double)cospi_ratio((2LL * k + 1) * j, N - 1);
+  }
+  for (int k = 0; k < P; ++k) {
+    const int n = 2 * k;
+    const long double cn = (n == 0 || n == N - 1) ? 0.5L : 1.0L;
+    for (int j = 0; j <= J; ++j) {
+      const long double w = (j == 0) ? 1.0L : 2.0L;
+      M.fwdA[k * KA + j] = (double)(w * cospi_ratio((long long)n * j, N - 1) * cn / (N - 1));
+    }
+    const int no = 2 * k + 1;
+    if (no < N)
+      for (int j = 0; j < J; ++j) {
+        const long double w = (j == 0) ? 1.0L : 2.0L;
+        M.fwdB[k * KB + j] = (double)(w * cospi_ratio((long long)no * j, N - 1) / (N - 1));
+      }
+  }
+  return M;
+}
+
+// Be/Bo rows packed by Chebyshev index (helmholtz.cpp:35-70)
+void make_helm_b(int N, std::vector<double>& lo, std::vector<double>& di, std::vector<double>& up) {
+  const int N_ = N - 1;
+  lo.assign(N, 0.0);
+  di.assign(N, 0.0);
+  up.assign(N, 0.0);
+  auto beta = [&](int n) { return (n > N_ - 2) ? 0 : 1; };
+  auto c = [&](int n) { return (n == 0 || n == N_) ? 2 : 1; };
+  for (int n = 2; n < N; ++n) {
+    const int nn = n * n;
+    lo[n] = ((double)c(n - 2)) / (4 * n * (n - 1));
+    di[n] = -((double)beta(n)) / (2 * (nn - 1));
+    if (beta(n + 2)) up[n] = 1.0 / (4 * n * (n + 1));
+  }
+  di[0] = di[1] = 1.0;
+}
+
+template <typename T>
+int dalloc(T** p, size_t n, long long& bytes) {
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+  if (e != cudaSuccess) return fail(CFGPU_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  bytes += (long long)(n * sizeof(T));
+  return CFGPU_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// The DNS object
+// ---------------------------------------------------------------------------
+struct Scheme {
+  int method = CFGPU_SBDF3;
+  int family = 0;  // 0 multistep, 1 CNAB-style, 2 RK
+  int order = 0, nsub = 1, ninit = 0;
+  double eta = 1;
+  double alpha[4] = {0}, beta[4] = {0};          // multistep
+  double ca[3] = {0}, cb[3] = {0}, cg[3] = {0}, cz[3] = {0};  // CNAB-style
+  double rA[3] = {0}, rB[3] = {0}, rC[3] = {0};  // RK
+  std::vector<double> lambda_t;
+  int countdown = 0;
+  bool full = true;
+  double t = 0;
+  std::vector<TauTable> tau;
+};
+
+static int setup_scheme(Scheme& s, int method, double dt) {
+  s.method = method;
+  switch (method) {
+    case CFGPU_CNFE1:
+    case CFGPU_SBDF1:
+      s.family = 0; s.order = 1; s.eta = 1.0; s.alpha[0] = -1.0; s.beta[0] = 1.0; break;
+    case CFGPU_SBDF2:
+      s.family = 0; s.order = 2; s.eta = 1.5; s.alpha[0] = -2.0; s.alpha[1] = 0.5; s.beta[0] = 2.0; s.beta[1] = -1.0;
+      break;
+    case CFGPU_SBDF3:
+      s.family = 0; s.order = 3; s.eta = 11.0 / 6.0;
+      s.alpha[0] = -3.0; s.alpha[1] = 1.5; s.alpha[2] = -1.0 / 3.0;
+      s.beta[0] = 3.0; s.beta[1] = -3.0; s.beta[2] = 1.0;
+      break;
+    case CFGPU_SBDF4:
+      s.family = 0; s.order = 4; s.eta = 25.0 / 12.0;
+      s.alpha[0] = -4.0; s.alpha[1] = 3.0; s.alpha[2] = -4.0 / 3.0; s.alpha[3] = 0.25;
+      s.beta[0] = 4.0; s.beta[1] = -6.0; s.beta[2] = 4.0; s.beta[3] = -1.0;
+      break;
+    case CFGPU_CNAB2:
+      s.family = 1; s.order = 2; s.nsub = 1; s.ninit = 1;
+      s.ca[0] = 0.5; s.cb[0] = 0.5; s.cg[0] = 1.5; s.cz[0] = -0.5;
+      break;
+    case CFGPU_SMRK2:
+      s.family = 1; s.order = 2; s.nsub = 3; s.ninit = 0;
+      s.ca[0] = 29.0 / 96.0; s.ca[1] = -3.0 / 40.0; s.ca[2] = 1.0 / 6.0;
+      s.cb[0] = 37.0 / 160.0; s.cb[1] = 5.0 / 24.0; s.cb[2] = 1.0 / 6.0;
+      s.cg[0] = 8.0 / 15.0; s.cg[1] = 5.0 / 12.0; s.cg[2] = 3.0 / 4.0;
+      s.cz[0] = 0.0; s.cz[1] = -17.0 / 60.0; s.cz[2] = -5.0 / 12.0;
+      break;
+    case CFGPU_CNRK2:
+      s.family = 2; s.order = 2; s.nsub = 3; s.ninit = 0;
+      s.rA[0] = 0.0; s.rA[1] = -5.0 / 9.0; s.rA[2] = -153.0 / 128.0;
+      s.rB[0] = 1.0 / 3.0; s.rB[1] = 15.0 / 16.0; s.rB[2] = 8.0 / 15.0;
+      s.rC[0] = 1.0 / 6.0; s.rC[1] = 5.0 / 24.0; s.rC[2] = 1.0 / 8.0;
+      break;
+    default:
+      return fail(CFGPU_EINVAL, "unknown time-stepping method");
+  }
+  s.lambda_t.clear();
+  if (s.family == 0) {
+    s.ninit = s.order - 1;
+    s.lambda_t.push_back(s.eta / dt);
+    s.countdown = s.ninit;
+    s.full = (s.countdown == 0);
+  } else if (s.family == 1) {
+    for (int j = 0; j < s.nsub; ++j) s.lambda_t.push_back(1.0 / (s.cb[j] * dt));
+    s.full = (method == CFGPU_SMRK2);
+  } else {
+    for (int j = 0; j < s.nsub; ++j) s.lambda_t.push_back(1.0 / (s.rC[j] * dt));
+    s.full = true;
+  }
+  return CFGPU_OK;
+}
+
+struct cfgpu_dns_s {
+  int device = 0;
+  cudaStream_t st = nullptr;
+  GridDev g{};
+  int N = 0;  // Ny
+  int precision = CFGPU_FP64;
+  cfgpu_flags fl{};
+  long long bytes = 0;
+  long long launches = 0;
+  // base flow and constraint (NSE::initCFConstraint)
+  std::vector<double> Ubase, Wbase, Ubaseyy, Wbaseyy;
+  double UbulkBase = 0, WbulkBase = 0, dPdxRef = 0, dPdzRef = 0, UbulkRef = 0, WbulkRef = 0;
+  double dPdxAct = 0, dPdzAct = 0;
+  double baseShear[2] = {0, 0};
+  double *dUbase = nullptr, *dWbase = nullptr, *dUbaseyy = nullptr, *dWbaseyy = nullptr;
+  double* ddPdx = nullptr;  // [2]
+  // Helmholtz B rows
+  double *hb_lo = nullptr, *hb_di = nullptr, *hb_up = nullptr;
+  // transforms
+  FftPlan px{}, pz{};
+  void *twx = nullptr, *twz = nullptr;  // R-typed complex
+  void *cinvA = nullptr, *cinvB = nullptr, *cfwdA = nullptr, *cfwdB = nullptr;
+  // state: current fields
+  double *Ucur = nullptr, *Qcur = nullptr;
+  // multistep ring
+  double *Uh[4] = {nullptr}, *Qh[4] = {nullptr};
+  void* Nh[4] = {nullptr};
+  int perm[4] = {0, 1, 2, 3};
+  // CNAB-style (main or init): fj, fj1 per scheme; RK accumulator
+  void *fj[2] = {nullptr, nullptr}, *fj1[2] = {nullptr, nullptr};
+  void* rkQ[2] = {nullptr, nullptr};
+  void* rkN = nullptr;
+  // NL work
+  void *C6 = nullptr, *W6 = nullptr, *X6 = nullptr, *Z3 = nullptr, *F3 = nullptr;
+  double* scratch = nullptr;
+  int RP = 8;
+  // schemes
+  Scheme main, init;
+  bool has_init = false;
+  // host staging (pinned)
+  double* stage = nullptr;
+  size_t stage_elems = 0;
+  // phase profiling: event pairs recorded around NL passes (0) and tau solves (1)
+  bool profiling = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_used;
+
+  size_t rowc() const { return 2 * (size_t)g.Md; }           // doubles per row
+  size_t compc() const { return rowc() * (size_t)N; }         // doubles per component
+  size_t rsz() const { return precision == CFGPU_FP64 ? 8 : 4; }
+};
+
+namespace {
+
+cudaEvent_t take_event(cfgpu_dns d) {
+  if (d->ev_pool.empty()) {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+  }
+  cudaEvent_t e = d->ev_pool.back();
+  d->ev_pool.pop_back();
+  return e;
+}
+
+struct PhaseScope {
+  cfgpu_dns d;
+  int phase;
+  cudaEvent_t a = nullptr;
+  PhaseScope(cfgpu_dns d_, int p) : d(d_), phase(p) {
+    if (d->profiling) {
+      a = take_event(d);
+      cudaEventRecord(a, d->st);
+    }
+  }
+  ~PhaseScope() {
+    if (d->profiling) {
+      cudaEvent_t b = take_event(d);
+      cudaEventRecord(b, d->st);
+      d->ev_used.push_back({phase, {a, b}});
+    }
+  }
+};
+
+int build_tables(cfgpu_dns d, Scheme& s) {
+  const size_t FN = (size_t)d->N * d->g.Md;
+  HelmB hb{d->hb_lo, d->hb_di, d->hb_up};
+  for (auto& t : s.tau) {
+    cudaFree(t.f);
+    cudaFree(t.s);
+  }
+  s.tau.clear();
+  for (double lt : s.lambda_t) {
+    TauTable t{};
+    CKS(dalloc(&t.f, FN * TF_NFIELDS, d->bytes));
+    CKS(dalloc(&t.s, (size_t)d->g.Md * TS_NSCALARS, d->bytes));
+    CK(launch_tau_setup(d->g, d->N, lt, d->fl.nu, hb, t, d->scratch, d->st));
+    d->launches++;
+    s.tau.push_back(t);
+  }
+  return CFGPU_OK;
+}
+
+// Nonlinear term N(u) of the fields in U (solved-mode layout) into Nout (R-typed).
+template <typename R>
+int nonlinear_impl(cfgpu_dns d, const double* U, void* Nout) {
+  const GridDev& g = d->g;
+  const int N = d->N;
+  R* C6 = (R*)d->C6;
+  R* W6 = (R*)d->W6;
+  const size_t row = d->rowc(), comp = d->compc();
+  CK(launch_curl_base<R>(g, U, C6, d->dUbase, d->dWbase, d->fl.Vsuck, d->st));
+  CK((launch_cheb<R, R, R>(N, true, (int)row, 6, C6, row, comp, W6, row, comp, (const R*)d->cinvA,
+                           (const R*)d->cinvB, d->st)));
+  CK(launch_xinv<R>(g, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)W6, (cpx<R>*)d->X6, 6, d->st));
+  CK(launch_zcross<R>(g, d->pz, (const cpx<R>*)d->twz, d->RP, (const cpx<R>*)d->X6, (cpx<R>*)d->Z3, d->st));
+  CK(launch_xfwd<R>(g, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)d->Z3, (cpx<R>*)d->F3, 3, d->st));
+  CK((launch_cheb<R, R, R>(N, false, (int)row, 3, (const R*)d->F3, row, comp, (R*)Nout, row, comp,
+                           (const R*)d->cfwdA, (const R*)d->cfwdB, d->st)));
+  d->launches += 6;
+  return CFGPU_OK;
+}
+
+int nonlinear(cfgpu_dns d, const double* U, void* Nout) {
+  PhaseScope ps(d, 0);
+  if (d->precision == CFGPU_FP64) return nonlinear_impl<double>(d, U, Nout);
+  return nonlinear_impl<float>(d, U, Nout);
+}
+
+SolveParams base_params(cfgpu_dns d) {
+  SolveParams sp{};
+  sp.nu = d->fl.nu;
+  sp.constraint = d->fl.constraint;
+  sp.dPdxRef = d->dPdxRef;
+  sp.dPdzRef = d->dPdzRef;
+  sp.umean = d->UbulkRef - d->UbulkBase;
+  sp.wmean = d->WbulkRef - d->WbulkBase;
+  sp.baseShear[0] = d->baseShear[0];
+  sp.baseShear[1] = d->baseShear[1];
+  sp.taucorrection = d->fl.taucorrection;
+  sp.force_real00 = 1;
+  return sp;
+}
+
+SolvePtrs base_ptrs(cfgpu_dns d) {
+  SolvePtrs p{};
+  p.Ubaseyy = d->dUbaseyy;
+  p.Wbaseyy = d->dWbaseyy;
+  p.Ubase = d->dUbase;
+  p.Wbase = d->dWbase;
+  p.scratch = d->scratch;
+  p.dPdx_out = d->ddPdx;
+  return p;
+}
+
+int tau_solve(cfgpu_dns d, const SolveParams& sp, const SolvePtrs& p, const TauTable& tt) {
+  PhaseScope ps(d, 1);
+  HelmB hb{d->hb_lo, d->hb_di, d->hb_up};
+  if (d->precision == CFGPU_FP64) {
+    CK(launch_tau_solve<double>(d->g, d->N, sp, p, hb, tt, d->st));
+  } else {
+    CK(launch_tau_solve<float>(d->g, d->N, sp, p, hb, tt, d->st));
+  }
+  d->launches++;
+  return CFGPU_OK;
+}
+
+size_t state_bytes(cfgpu_dns d) { return d->compc() * sizeof(double); }
+
+// ---- multistep (dnsalgo.cpp:202-315) ---------------------------------------
+void ms_shift(cfgpu_dns d) {
+  const int K = d->main.order;
+  const int last = d->perm[K - 1];
+  for (int j = K - 1; j > 0; --j) d->perm[j] = d->perm[j - 1];
+  d->perm[0] = last;
+}
+
+int ms_push(cfgpu_dns d) {
+  ms_shift(d);
+  if (d->main.order > 1) {
+    const int s1 = d->perm[1];
+    CK(cudaMemcpyAsync(d->Uh[s1], d->Ucur, 3 * state_bytes(d), cudaMemcpyDeviceToDevice, d->st));
+    CK(cudaMemcpyAsync(d->Qh[s1], d->Qcur, state_bytes(d), cudaMemcpyDeviceToDevice, d->st));
+    CKS(nonlinear(d, d->Uh[s1], d->Nh[s1]));
+  }
+  d->main.t += d->fl.dt;
+  d->main.countdown--;
+  d->main.full = (d->main.countdown == 0);
+  return CFGPU_OK;
+}
+
+int ms_advance(cfgpu_dns d, int nsteps) {
+  Scheme& s = d->main;
+  const int K = s.order, J = K - 1;
+  const double dt = d->fl.dt;
+  if (nsteps <= 0) return CFGPU_OK;
+  CK(cudaMemcpyAsync(d->Uh[d->perm[0]], d->Ucur, 3 * state_bytes(d), cudaMemcpyDeviceToDevice, d->st));
+  CK(cudaMemcpyAsync(d->Qh[d->perm[0]], d->Qcur, state_bytes(d), cudaMemcpyDeviceToDevice, d->st));
+  for (int step = 0; step < nsteps; ++step) {
+    CKS(nonlinear(d, d->Uh[d->perm[0]], d->Nh[d->perm[0]]));
+    SolveParams sp = base_params(d);
+    sp.kind = 0;
+    sp.order = K;
+    SolvePtrs p = base_ptrs(d);
+    for (int j = 0; j < K; ++j) {
+      sp.a[j] = -s.alpha[j] / dt;
+      sp.b[j] = -s.beta[j];
+      p.uin[j] = d->Uh[d->perm[j]];
+      p.nin[j] = d->Nh[d->perm[j]];
+    }
+    p.uout = d->Uh[d->perm[J]];
+    p.qout = d->Qh[d->perm[J]];
+    CKS(tau_solve(d, sp, p, s.tau[0]));
+    ms_shift(d);
+    s.t += dt;
+  }
+  CK(cudaMemcpyAsync(d->Ucur, d->Uh[d->perm[0]], 3 * state_bytes(d), cudaMemcpyDeviceToDevice, d->st));
+  CK(cudaMemcpyAsync(d->Qcur, d->Qh[d->perm[0]], state_bytes(d), cudaMemcpyDeviceToDevice, d->st));
+  return CFGPU_OK;
+}
+
+// ---- CNAB-style (dnsalgo.cpp:608-697); which = 0 main, 1 init --------------
+int cnab_push(cfgpu_dns d, int which) {
+  std::swap(d->fj[which], d->fj1[which]);
+  CKS(nonlinear(d, d->Ucur, d->fj[which]));
+  Scheme& s = which == 0 ? d->main : d->init;
+  s.t += d->fl.dt;
+  s.full = true;
+  return CFGPU_OK;
+}
+
+int cnab_advance(cfgpu_dns d, int which, int nsteps) {
+  Scheme& s = which == 0 ? d->main : d->init;
+  for (int n = 0; n < nsteps; ++n) {
+    for (int j = 0; j < s.nsub; ++j) {
+      std::swap(d->fj[which], d->fj1[which]);
+      CKS(nonlinear(d, d->Ucur, d->fj[which]));
+      SolveParams sp = base_params(d);
+      sp.kind = 1;
+      sp.lam = s.lambda_t[j];
+      sp.a_b = s.ca[j] / s.cb[j];
+      sp.g_b = s.cg[j] / s.cb[j];
+      sp.z_b = s.cz[j] / s.cb[j];
+      SolvePtrs p = base_ptrs(d);
+      p.uin[0] = d->Ucur;
+      p.nin[0] = d->fj[which];
+      p.nin[1] = d->fj1[which];
+      p.qin = d->Qcur;
+      p.uout = d->Ucur;
+      p.qout = d->Qcur;
+      CKS(tau_solve(d, sp, p, s.tau[j]));
+    }
+    s.t += d->fl.dt;
+  }
+  return CFGPU_OK;
+}
+
+// ---- CNRK2 (dnsalgo.cpp:419-470) -------------------------------------------
+int rk_advance(cfgpu_dns d, int which, int nsteps) {
+  Scheme& s = which == 0 ? d->main : d->init;
+  for (int n = 0; n < nsteps; ++n) {
+    for (int j = 0; j < s.nsub; ++j) {
+      CKS(nonlinear(d, d->Ucur, d->rkN));
+      SolveParams sp = base_params(d);
+      sp.kind = 2;
+      sp.lam = s.lambda_t[j];
+      sp.rkA = s.rA[j];
+      sp.B_C = s.rB[j] / s.rC[j];
+      SolvePtrs p = base_ptrs(d);
+      p.uin[0] = d->Ucur;
+      p.nin[0] = d->rkN;
+      p.Q = d->rkQ[which];
+      p.qin = d->Qcur;
+      p.uout = d->Ucur;
+      p.qout = d->Qcur;
+      CKS(tau_solve(d, sp, p, s.tau[j]));
+    }
+    s.t += d->fl.dt;
+  }
+  return CFGPU_OK;
+}
+
+int scheme_advance(cfgpu_dns d, int which, int nsteps) {
+  Scheme& s = which == 0 ? d->main : d->init;
+  if (s.family == 0) return ms_advance(d, nsteps);
+  if (s.family == 1) return cnab_advance(d, which, nsteps);
+  return rk_advance(d, which, nsteps);
+}
+
+int scheme_push(cfgpu_dns d) {
+  if (d->main.family == 0) return ms_push(d);
+  if (d->main.family == 1) return cnab_push(d, 0);
+  return CFGPU_OK;
+}
+
+// DNS::advance (dns.cpp:135-163)
+int dns_advance_device(cfgpu_dns d, int nsteps) {
+  int n = 0;
+  while (!d->main.full && n < nsteps) {
+    if (!d->has_init) return fail(CFGPU_EINVAL, "main algorithm uninitialized and no init algorithm");
+    CKS(scheme_push(d));
+    CKS(scheme_advance(d, 1, 1));
+    ++n;
+  }
+  return scheme_advance(d, 0, nsteps - n);
+}
+
+// host serial layout <-> solved-mode layout
+void gather_modes(cfgpu_dns d, const double* h, int Nd, double* out) {
+  const GridDev& g = d->g;
+  const int Mz = g.Nz / 2 + 1;
+  for (int i = 0; i < Nd; ++i)
+    for (int my = 0; my < g.Ny; ++my)
+      for (int m = 0; m < g.Md; ++m) {
+        const int kx = mode_kx(g, m), kz = mode_kz(g, m);
+        const int mx = kx >= 0 ? kx : kx + g.Nx;
+        const size_t src = 2 * ((((size_t)i * g.Ny + my) * g.Nx + mx) * Mz + kz);
+        const size_t dst = 2 * (((size_t)i * g.Ny + my) * g.Md + m);
+        out[dst] = h[src];
+        out[dst + 1] = h[src + 1];
+      }
+}
+void scatter_modes(cfgpu_dns d, const double* in, int Nd, double* h) {
+  const GridDev& g = d->g;
+  const int Mz = g.Nz / 2 + 1;
+  for (int i = 0; i < Nd; ++i)
+    for (int my = 0; my < g.Ny; ++my)
+      for (int m = 0; m < g.Md; ++m) {
+        const int kx = mode_kx(g, m), kz = mode_kz(g, m);
+        const int mx = kx >= 0 ? kx : kx + g.Nx;
+        const size_t dst = 2 * ((((size_t)i * g.Ny + my) * g.Nx + mx) * Mz + kz);
+        const size_t src = 2 * (((size_t)i * g.Ny + my) * g.Md + m);
+        h[dst] = in[src];
+        h[dst + 1] = in[src + 1];
+      }
+}
+
+int set_fields(cfgpu_dns d, const double* u, const double* q) {
+  const size_t cd = d->compc();
+  if (u) {
+    gather_modes(d, u, 3, d->stage);
+    CK(cudaMemcpyAsync(d->Ucur, d->stage, 3 * cd * sizeof(double), cudaMemcpyHostToDevice, d->st));
+  }
+  if (q) {
+    gather_modes(d, q, 1, d->stage + 3 * cd);
+    CK(cudaMemcpyAsync(d->Qcur, d->stage + 3 * cd, cd * sizeof(double), cudaMemcpyHostToDevice, d->st));
+  }
+  return CFGPU_OK;
+}
+
+int get_fields(cfgpu_dns d, double* u, double* q) {
+  const size_t cd = d->compc();
+  CK(cudaMemcpyAsync(d->stage, d->Ucur, 3 * cd * sizeof(double), cudaMemcpyDeviceToHost, d->st));
+  CK(cudaMemcpyAsync(d->stage + 3 * cd, d->Qcur, cd * sizeof(double), cudaMemcpyDeviceToHost, d->st));
+  CK(cudaStreamSynchronize(d->st));
+  if (u) scatter_modes(d, d->stage, 3, u);
+  if (q) scatter_modes(d, d->stage + 3 * cd, 1, q);
+  return CFGPU_OK;
+}
+
+template <typename R>
+int upload_as(const std::vector<double>& v, void** dst, long long& bytes) {
+  std::vector<R> t(v.begin(), v.end());
+  R* p;
+  CKS(dalloc(&p, t.size(), bytes));
+  CK(cudaMemcpy(p, t.data(), t.size() * sizeof(R), cudaMemcpyHostToDevice));
+  *dst = p;
+  return CFGPU_OK;
+}
+
+template <typename R>
+int upload_tw(const std::vector<std::complex<long double>>& tw, void** dst, long long& bytes) {
+  std::vector<cpx<R>> t(tw.size() ? tw.size() : 1);
+  for (size_t i = 0; i < tw.size(); ++i) t[i] = cmk<R>((R)tw[i].real(), (R)tw[i].imag());
+  cpx<R>* p;
+  CKS(dalloc(&p, t.size(), bytes));
+  CK(cudaMemcpy(p, t.data(), t.size() * sizeof(cpx<R>), cudaMemcpyHostToDevice));
+  *dst = p;
+  return CFGPU_OK;
+}
+
+int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flags, const double* Ub, const double* Wb,
+                    const double* u0) {
+  d->fl = *flags;
+  const cfgpu_flags& f = d->fl;
+  const int Nx = grid->Nx, Ny = grid->Ny, Nz = grid->Nz;
+  if (Nx < 4 || Nz < 4 || Nx % 2 || Nz % 2) return fail(CFGPU_EINVAL, "Nx and Nz must be even and >= 4");
+  if (Ny < 5 || Ny % 2 == 0) return fail(CFGPU_EINVAL, "Ny must be odd and >= 5 (HelmholtzSolver asserts odd N)");
+  if ((Ny + 1) / 2 > 72) return fail(CFGPU_ENOTSUP, "Ny > 143 not supported by the Chebyshev transform kernel");
+  if (!(grid->b > grid->a) || grid->Lx <= 0 || grid->Lz <= 0) return fail(CFGPU_EINVAL, "bad box");
+  if (f.dt <= 0 || f.nu <= 0) return fail(CFGPU_EINVAL, "dt and nu must be positive");
+  if (f.nonlinearity != CFGPU_Rotational)
+    return fail(CFGPU_ENOTSUP, "only Rotational nonlinearity is implemented on the device path");
+  if (f.dealiasing == CFGPU_DealiasY || f.dealiasing == CFGPU_DealiasXYZ)
+    return fail(CFGPU_ENOTSUP, "DealiasY is not implemented on the device path");
+  const bool dxz = (f.dealiasing == CFGPU_DealiasXZ);
+  GridDev& g = d->g;
+  g.Nx = Nx;
+  g.Ny = Ny;
+  g.Nz = Nz;
+  g.kxmax = Nx / 2;
+  g.kzmax = Nz / 2;
+  g.Kx = dxz ? Nx / 3 - 1 : Nx / 2 - 1;
+  g.Kz = dxz ? Nz / 3 - 1 : Nz / 2 - 1;
+  g.NKx = 2 * g.Kx + 1;
+  g.NKz = g.Kz + 1;
+  g.Md = g.NKx * g.NKz;
+  g.Lx = grid->Lx;
+  g.Lz = grid->Lz;
+  g.a = grid->a;
+  g.b = grid->b;
+  g.kxs = g.kzs = nullptr;
+  d->N = Ny;
+  CK(cudaGetDevice(&d->device));
+  CK(cudaStreamCreateWithFlags(&d->st, cudaStreamNonBlocking));
+
+  // base flow (NSE::createCFBaseFlow, nse.cpp:589-632)
+  const double a = g.a, b = g.b;
+  if (Ub && Wb) {
+    d->Ubase.assign(Ub, Ub + Ny);
+    d->Wbase.assign(Wb, Wb + Ny);
+  } else {
+    d->Ubase.assign(Ny, 0.0);
+    d->Wbase.assign(Ny, 0.0);
+    switch (f.baseflow) {
+      case CFGPU_ZeroBase: break;
+      case CFGPU_LinearBase: d->Ubase[1] = 1; break;
+      case CFGPU_ParabolicBase: d->Ubase[0] = 0.5; d->Ubase[2] = -0.5; break;
+      case CFGPU_SuctionBase:
+        d->Ubase = laminar_profile(f.nu, CFGPU_PressureGradient, 0, f.Ubulk, f.Vsuck, a, b, -0.5, 0.5, Ny);
+        break;
+      case CFGPU_LaminarBase:
+        d->Ubase = laminar_profile(f.nu, f.constraint, f.dPdx, f.Ubulk, f.Vsuck, a, b, f.ulowerwall, f.uupperwall, Ny);
+        d->Wbase = laminar_profile(f.nu, f.constraint, f.dPdz, f.Wbulk, f.Vsuck, a, b, f.wlowerwall, f.wupperwall, Ny);
+        break;
+      default:
+        return fail(CFGPU_EINVAL, "ArbitraryBase requires Ubase and Wbase");
+    }
+  }
+  // NSE::initCFConstraint (nse.cpp:634-671)
+  const double L = b - a;
+  d->UbulkBase = mean_h(d->Ubase);
+  d->Ubaseyy = cheb_diff_h(cheb_diff_h(d->Ubase, L), L);
+  d->WbulkBase = mean_h(d->Wbase);
+  d->Wbaseyy = cheb_diff_h(cheb_diff_h(d->Wbase, L), L);
+  {
+    std::vector<double> Uy = cheb_diff_h(d->Ubase, L), Wy = cheb_diff_h(d->Wbase, L);
+    d->baseShear[0] = f.nu * (eval_b_h(Uy) - eval_a_h(Uy)) / L;
+    d->baseShear[1] = f.nu * (eval_b_h(Wy) - eval_a_h(Wy)) / L;
+  }
+  if (f.constraint == CFGPU_BulkVelocity) {
+    d->UbulkRef = f.Ubulk;
+    d->WbulkRef = f.Wbulk;
+  } else {
+    d->dPdxAct = d->dPdxRef = f.dPdx;
+    d->dPdzAct = d->dPdzRef = f.dPdz;
+  }
+  (void)u0;
+  long long& B = d->bytes;
+  CKS(dalloc(&d->dUbase, Ny, B));
+  CKS(dalloc(&d->dWbase, Ny, B));
+  CKS(dalloc(&d->dUbaseyy, Ny, B));
+  CKS(dalloc(&d->dWbaseyy, Ny, B));
+  CKS(dalloc(&d->ddPdx, 2, B));
+  CK(cudaMemcpy(d->dUbase, d->Ubase.data(), Ny * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d->dWbase, d->Wbase.data(), Ny * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d->dUbaseyy, d->Ubaseyy.data(), Ny * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d->dWbaseyy, d->Wbaseyy.data(), Ny * sizeof(double), cudaMemcpyHostToDevice));
+  {
+    double init[2] = {d->dPdxAct, d->dPdzAct};
+    CK(cudaMemcpy(d->ddPdx, init, sizeof(init), cudaMemcpyHostToDevice));
+  }
+  // Helmholtz B rows
+  {
+    std::vector<double> lo, di, up;
+    make_helm_b(Ny, lo, di, up);
+    CKS(dalloc(&d->hb_lo, Ny, B));
+    CKS(dalloc(&d->hb_di, Ny, B));
+    CKS(dalloc(&d->hb_up, Ny, B));
+    CK(cudaMemcpy(d->hb_lo, lo.data(), Ny * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d->hb_di, di.data(), Ny * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d->hb_up, up.data(), Ny * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  // FFT plans, twiddles, Chebyshev matrices
+  std::vector<std::complex<long double>> twx, twz;
+  if (!make_fft_plan(Nx, d->px, twx) || !make_fft_plan(Nz, d->pz, twz))
+    return fail(CFGPU_ENOTSUP, "Nx and Nz must factor into 2, 3 and 5");
+  ChebMats cm = make_cheb_mats(Ny);
+  const bool fp64 = d->precision == CFGPU_FP64;
+  if (fp64) {
+    CKS(upload_tw<double>(twx, &d->twx, B));
+    CKS(upload_tw<double>(twz, &d->twz, B));
+    CKS(upload_as<double>(cm.invA, &d->cinvA, B));
+    CKS(upload_as<double>(cm.invB, &d->cinvB, B));
+    CKS(upload_as<double>(cm.fwdA, &d->cfwdA, B));
+    CKS(upload_as<double>(cm.fwdB, &d->cfwdB, B));
+  } else {
+    CKS(upload_tw<float>(twx, &d->twx, B));
+    CKS(upload_tw<float>(twz, &d->twz, B));
+    CKS(upload_as<float>(cm.invA, &d->cinvA, B));
+    CKS(upload_as<float>(cm.invB, &d->cinvB, B));
+    CKS(upload_as<float>(cm.fwdA, &d->cfwdA, B));
+    CKS(upload_as<float>(cm.fwdB, &d->cfwdB, B));
+  }
+  // state and work arrays
+  const size_t cd = d->compc();
+  const size_t rs = d->rsz();
+  CKS(dalloc(&d->Ucur, 3 * cd, B));
+  CKS(dalloc(&d->Qcur, cd, B));
+  CK(cudaMemset(d->Ucur, 0, 3 * cd * sizeof(double)));
+  CK(cudaMemset(d->Qcur, 0, cd * sizeof(double)));
+  unsigned char* tmp;
+  CKS(dalloc(&tmp, 6 * cd * rs, B));
+  d->C6 = tmp;
+  CKS(dalloc(&tmp, 6 * cd * rs, B));
+  d->W6 = tmp;
+  const size_t plane = (size_t)Nx * g.NKz * 2;  // reals per plane per component
+  CKS(dalloc(&tmp, 6 * plane * Ny * rs, B));
+  d->X6 = tmp;
+  CKS(dalloc(&tmp, 3 * plane * Ny * rs, B));
+  d->Z3 = tmp;
+  CKS(dalloc(&tmp, 3 * cd * rs, B));
+  d->F3 = tmp;
+  CKS(dalloc(&d->scratch, 8 * cd, B));
+  d->RP = fp64 ? 8 : 16;
+  while (d->RP > 2 && (fp64 ? zcross_smem_bytes<double>(g, d->RP) : zcross_smem_bytes<float>(g, d->RP)) > 200 * 1024)
+    d->RP -= 2;
+  if ((fp64 ? xfft_smem_bytes<double>(g) : xfft_smem_bytes<float>(g)) > 227 * 1024 ||
+      (fp64 ? zcross_smem_bytes<double>(g, d->RP) : zcross_smem_bytes<float>(g, d->RP)) > 227 * 1024)
+    return fail(CFGPU_ENOTSUP, "grid too large for the shared-memory FFT passes");
+  if (cheb_smem_bytes(Ny, rs) > 200 * 1024) return fail(CFGPU_ENOTSUP, "Ny too large for the Chebyshev kernel");
+
+  // schemes (DNS::DNS, dns.cpp:22-39)
+  CKS(setup_scheme(d->main, f.timestepping, f.dt));
+  d->main.t = f.t0;
+  d->has_init = false;
+  if (!d->main.full && f.initstepping != f.timestepping) {
+    CKS(setup_scheme(d->init, f.initstepping, f.dt));
+    d->init.t = f.t0;
+    if (d->init.ninit != 0 && d->init.family == 0)
+      return fail(CFGPU_EINVAL, "init scheme needs initialization itself");
+    d->has_init = true;
+  }
+  auto alloc_scheme = [&](Scheme& s, int which) -> int {
+    if (s.family == 0) {
+      for (int j = 0; j < s.order; ++j) {
+        CKS(dalloc(&d->Uh[j], 3 * cd, B));
+        CKS(dalloc(&d->Qh[j], cd, B));
+        CKS(dalloc(&tmp, 3 * cd * rs, B));
+        d->Nh[j] = tmp;
+        CK(cudaMemset(d->Uh[j], 0, 3 * cd * sizeof(double)));
+        CK(cudaMemset(d->Qh[j], 0, cd * sizeof(double)));
+        CK(cudaMemset(d->Nh[j], 0, 3 * cd * rs));
+      }
+    } else if (s.family == 1) {
+      CKS(dalloc(&tmp, 3 * cd * rs, B));
+      d->fj[which] = tmp;
+      CKS(dalloc(&tmp, 3 * cd * rs, B));
+      d->fj1[which] = tmp;
+      CK(cudaMemset(d->fj[which], 0, 3 * cd * rs));
+      CK(cudaMemset(d->fj1[which], 0, 3 * cd * rs));
+    } else {
+      CKS(dalloc(&tmp, 3 * cd * rs, B));
+      d->rkQ[which] = tmp;
+      CK(cudaMemset(d->rkQ[which], 0, 3 * cd * rs));
+      if (!d->rkN) {
+        CKS(dalloc(&tmp, 3 * cd * rs, B));
+        d->rkN = tmp;
+      }
+    }
+    return CFGPU_OK;
+  };
+  CKS(alloc_scheme(d->main, 0));
+  if (d->has_init) CKS(alloc_scheme(d->init, 1));
+  CKS(build_tables(d, d->main));
+  if (d->has_init) CKS(build_tables(d, d->init));
+  d->stage_elems = 4 * cd;
+  CK(cudaMallocHost((void**)&d->stage, d->stage_elems * sizeof(double)));
+  CK(cudaStreamSynchronize(d->st));
+  return CFGPU_OK;
+}
+
+void dns_free(cfgpu_dns d) {
+  if (!d) return;
+  auto F = [](void* p) {
+    if (p) cudaFree(p);
+  };
+  F(d->dUbase); F(d->dWbase); F(d->dUbaseyy); F(d->dWbaseyy); F(d->ddPdx);
+  F(d->hb_lo); F(d->hb_di); F(d->hb_up);
+  F(d->twx); F(d->twz); F(d->cinvA); F(d->cinvB); F(d->cfwdA); F(d->cfwdB);
+  F(d->Ucur); F(d->Qcur);
+  for (int j = 0; j < 4; ++j) { F(d->Uh[j]); F(d->Qh[j]); F(d->Nh[j]); }
+  for (int w = 0; w < 2; ++w) { F(d->fj[w]); F(d->fj1[w]); F(d->rkQ[w]); }
+  F(d->rkN);
+  F(d->C6); F(d->W6); F(d->X6); F(d->Z3); F(d->F3); F(d->scratch);
+  for (Scheme* s : {&d->main, &d->init})
+    for (auto& t : s->tau) { F(t.f); F(t.s); }
+  if (d->stage) cudaFreeHost(d->stage);
+  for (auto& e : d->ev_pool) cudaEventDestroy(e);
+  for (auto& u : d->ev_used) {
+    cudaEventDestroy(u.second.first);
+    cudaEventDestroy(u.second.second);
+  }
+  if (d->st) cudaStreamDestroy(d->st);
+  delete d;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+const char* cfgpu_version(void) { return "cfgpu 0.1 (sm_103a)"; }
+const char* cfgpu_last_error(void) { return g_err.c_str(); }
+
+cfgpu_status cfgpu_flags_default(cfgpu_flags* f) {
+  if (!f) return fail(CFGPU_EINVAL, "null flags");
+  memset(f, 0, sizeof(*f));
+  f->nu = 0.0025;
+  f->dt = 0.03125;
+  f->baseflow = CFGPU_LaminarBase;
+  f->constraint = CFGPU_PressureGradient;
+  f->timestepping = CFGPU_SBDF3;
+  f->initstepping = CFGPU_SMRK2;
+  f->nonlinearity = CFGPU_Rotational;
+  f->dealiasing = CFGPU_DealiasXZ;
+  f->taucorrection = 1;
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_dns_create(const cfgpu_grid* grid, const cfgpu_flags* flags, const double* Ubase,
+                              const double* Wbase, const double* u, int precision, cfgpu_dns* out) {
+  if (!grid || !flags || !out) return fail(CFGPU_EINVAL, "null argument");
+  if (precision != CFGPU_FP64 && precision != CFGPU_MIXED) return fail(CFGPU_EINVAL, "bad precision");
+  if ((Ubase == nullptr) != (Wbase == nullptr)) return fail(CFGPU_EINVAL, "Ubase and Wbase must both be given");
+  *out = nullptr;
+  cfgpu_dns d = new cfgpu_dns_s();
+  d->precision = precision;
+  int s = dns_create_impl(d, grid, flags, Ubase, Wbase, u);
+  if (s != CFGPU_OK) {
+    std::string keep = g_err;
+    dns_free(d);
+    g_err = keep;
+    return s;
+  }
+  *out = d;
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_dns_set_fields(cfgpu_dns d, const double* u, const double* q) {
+  if (!d) return fail(CFGPU_EINVAL, "null dns");
+  CKS(set_fields(d, u, q));
+  CK(cudaStreamSynchronize(d->st));
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_dns_get_fields(cfgpu_dns d, double* u, double* q) {
+  if (!d) return fail(CFGPU_EINVAL, "null dns");
+  return get_fields(d, u, q);
+}
+
+cfgpu_status cfgpu_dns_advance_resident(cfgpu_dns d, int nsteps) {
+  if (!d || nsteps < 0) return fail(CFGPU_EINVAL, "bad argument");
+  CKS(dns_advance_device(d, nsteps));
+  CK(cudaStreamSynchronize(d->st));
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_dns_advance(cfgpu_dns d, double* u, double* q, int nsteps) {
+  if (!d || !u || !q || nsteps < 0) return fail(CFGPU_EINVAL, "bad argument");
+  CKS(set_fields(d, u, q));
+  CKS(dns_advance_device(d, nsteps));
+  return get_fields(d, u, q);
+}
+
+cfgpu_status cfgpu_dns_reset_dt(cfgpu_dns d, double dt) {
+  if (!d || dt <= 0) return fail(CFGPU_EINVAL, "bad argument");
+  d->fl.dt = dt;
+  // MultistepDNS/CNABstyleDNS/RungeKuttaDNS::reset_dt (dnsalgo.cpp:191-200, 404-413, 589-606)
+  for (Scheme* s : {&d->main, &d->init}) {
+    if (s == &d->init && !d->has_init) continue;
+    const double t = s->t;
+    std::vector<TauTable> keep = s->tau;
+    CKS(setup_scheme(*s, s->method, dt));
+    s->t = t;
+    s->tau = keep;
+    CKS(build_tables(d, *s));
+  }
+  CK(cudaStreamSynchronize(d->st));
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_dns_time(cfgpu_dns d, double* t) {
+  if (!d || !t) return fail(CFGPU_EINVAL, "bad argument");
+  *t = d->main.t;
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_dns_dPdx(cfgpu_dns d, double* dPdx) {
+  if (!d || !dPdx) return fail(CFGPU_EINVAL, "bad argument");
+  double v[2];
+  CK(cudaMemcpyAsync(v, d->ddPdx, sizeof(v), cudaMemcpyDeviceToHost, d->st));
+  CK(cudaStreamSynchronize(d->st));
+  *dPdx = v[0];
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_dns_base(cfgpu_dns d, double* Ubase, double* Wbase) {
+  if (!d) return fail(CFGPU_EINVAL, "null dns");
+  if (Ubase) memcpy(Ubase, d->Ubase.data(), d->N * sizeof(double));
+  if (Wbase) memcpy(Wbase, d->Wbase.data(), d->N * sizeof(double));
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_dns_num_modes(cfgpu_dns d, int* n) {
+  if (!d || !n) return fail(CFGPU_EINVAL, "bad argument");
+  *n = d->g.Md;
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_dns_device_bytes(cfgpu_dns d, long long* b) {
+  if (!d || !b) return fail(CFGPU_EINVAL, "bad argument");
+  *b = d->bytes;
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_dns_kernel_launches(cfgpu_dns d, long long* n) {
+  if (!d || !n) return fail(CFGPU_EINVAL, "bad argument");
+  *n = d->launches;
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_dns_advance_timed(cfgpu_dns d, int nsteps, double* ms) {
+  if (!d || nsteps < 0 || !ms) return fail(CFGPU_EINVAL, "bad argument");
+  cudaEvent_t a = take_event(d), b = take_event(d);
+  CK(cudaEventRecord(a, d->st));
+  CKS(dns_advance_device(d, nsteps));
+  CK(cudaEventRecord(b, d->st));
+  CK(cudaEventSynchronize(b));
+  float t = 0;
+  CK(cudaEventElapsedTime(&t, a, b));
+  *ms = t;
+  d->ev_pool.push_back(a);
+  d->ev_pool.push_back(b);
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_dns_set_profiling(cfgpu_dns d, int enable) {
+  if (!d) return fail(CFGPU_EINVAL, "null dns");
+  d->profiling = enable != 0;
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_dns_phase_times(cfgpu_dns d, double* nl_ms, long long* nl_count, double* tau_ms,
+                                   long long* tau_count) {
+  if (!d) return fail(CFGPU_EINVAL, "null dns");
+  CK(cudaStreamSynchronize(d->st));
+  double t[2] = {0, 0};
+  long long n[2] = {0, 0};
+  for (auto& u : d->ev_used) {
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, u.second.first, u.second.second));
+    t[u.first] += ms;
+    n[u.first] += 1;
+    d->ev_pool.push_back(u.second.first);
+    d->ev_pool.push_back(u.second.second);
+  }
+  d->ev_used.clear();
+  if (nl_ms) *nl_ms = t[0];
+  if (nl_count) *nl_count = n[0];
+  if (tau_ms) *tau_ms = t[1];
+  if (tau_count) *tau_count = n[1];
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_dns_destroy(cfgpu_dns d) {
+  if (!d) return CFGPU_OK;
+  cudaStreamSynchronize(d->st);
+  dns_free(d);
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_tau_solve_batched(int N, int nmodes, const int* kx, const int* kz, double Lx, double Lz, double a,
+                                     double b, double lambda_t, double nu, int taucorrection, const double* Rx,
+                                     const double* Ry, const double* Rz, double* u, double* v, double* w, double* P) {
+  if (N < 5 || N % 2 == 0 || nmodes <= 0 || !kx || !kz || !Rx || !Ry || !Rz || !u || !v || !w || !P)
+    return fail(CFGPU_EINVAL, "bad argument");
+  if (!(b > a) || Lx <= 0 || Lz <= 0) return fail(CFGPU_EINVAL, "bad geometry");
+  GridDev g{};
+  g.Nx = g.Nz = 4;
+  g.Ny = N;
+  g.Md = nmodes;
+  g.NKx = nmodes;
+  g.NKz = 1;
+  g.kxmax = g.kzmax = 1 << 30;  // no Nyquist zeroing for explicit lists
+  g.Lx = Lx;
+  g.Lz = Lz;
+  g.a = a;
+  g.b = b;
+  long long bytes = 0;
+  int *dkx = nullptr, *dkz = nullptr;
+  double *R3 = nullptr, *U3 = nullptr, *Q1 = nullptr, *scr = nullptr, *zero = nullptr, *hlo = nullptr,
+         *hdi = nullptr, *hup = nullptr;
+  TauTable t{};
+  cudaStream_t st = nullptr;
+  int status = CFGPU_OK;
+  const size_t row = 2 * (size_t)nmodes, comp = row * N;
+  std::vector<double> h(3 * comp), hq(comp);
+  auto body = [&]() -> int {
+    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    CKS(dalloc(&dkx, nmodes, bytes));
+    CKS(dalloc(&dkz, nmodes, bytes));
+    CK(cudaMemcpy(dkx, kx, nmodes * sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(dkz, kz, nmodes * sizeof(int), cudaMemcpyHostToDevice));
+    g.kxs = dkx;
+    g.kzs = dkz;
+    CKS(dalloc(&R3, 3 * comp, bytes));
+    CKS(dalloc(&U3, 3 * comp, bytes));
+    CKS(dalloc(&Q1, comp, bytes));
+    CKS(dalloc(&scr, 8 * comp, bytes));
+    CKS(dalloc(&zero, N, bytes));
+    CK(cudaMemset(zero, 0, N * sizeof(double)));
+    std::vector<double> lo, di, up;
+    make_helm_b(N, lo, di, up);
+    CKS(dalloc(&hlo, N, bytes));
+    CKS(dalloc(&hdi, N, bytes));
+    CKS(dalloc(&hup, N, bytes));
+    CK(cudaMemcpy(hlo, lo.data(), N * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(hdi, di.data(), N * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(hup, up.data(), N * sizeof(double), cudaMemcpyHostToDevice));
+    HelmB hb{hlo, hdi, hup};
+    CKS(dalloc(&t.f, (size_t)N * nmodes * TF_NFIELDS, bytes));
+    CKS(dalloc(&t.s, (size_t)nmodes * TS_NSCALARS, bytes));
+    CK(launch_tau_setup(g, N, lambda_t, nu, hb, t, scr, st));
+    const double* Rs[3] = {Rx, Ry, Rz};
+    for (int c = 0; c < 3; ++c)
+      for (int k = 0; k < nmodes; ++k)
+        for (int n = 0; n < N; ++n) {
+          h[c * comp + n * row + 2 * k] = Rs[c][2 * ((size_t)k * N + n)];
+          h[c * comp + n * row + 2 * k + 1] = Rs[c][2 * ((size_t)k * N + n) + 1];
+        }
+    CK(cudaMemcpyAsync(R3, h.data(), 3 * comp * sizeof(double), cudaMemcpyHostToDevice, st));
+    SolveParams sp{};
+    sp.kind = 0;
+    sp.order = 1;
+    sp.a[0] = 1.0;
+    sp.b[0] = 0.0;
+    sp.nu = nu;
+    sp.constraint = CFGPU_PressureGradient;
+    sp.taucorrection = taucorrection;
+    sp.force_real00 = 0;
+    SolvePtrs p{};
+    p.uin[0] = R3;
+    p.nin[0] = R3;
+    p.uout = U3;
+    p.qout = Q1;
+    p.Ubaseyy = zero;
+    p.Wbaseyy = zero;
+    p.scratch = scr;
+    CK(launch_tau_solve<double>(g, N, sp, p, hb, t, st));
+    CK(cudaMemcpyAsync(h.data(), U3, 3 * comp * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(hq.data(), Q1, comp * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    double* outs[4] = {u, v, w, P};
+    for (int c = 0; c < 4; ++c)
+      for (int k = 0; k < nmodes; ++k)
+        for (int n = 0; n < N; ++n) {
+          const double* src = c < 3 ? &h[c * comp] : hq.data();
+          outs[c][2 * ((size_t)k * N + n)] = src[n * row + 2 * k];
+          outs[c][2 * ((size_t)k * N + n) + 1] = src[n * row + 2 * k + 1];
+        }
+    return CFGPU_OK;
+  };
+  status = body();
+  for (void* p : {(void*)dkx, (void*)dkz, (void*)R3, (void*)U3, (void*)Q1, (void*)scr, (void*)zero, (void*)hlo,
+                  (void*)hdi, (void*)hup, (void*)t.f, (void*)t.s})
+    if (p) cudaFree(p);
+  if (st) cudaStreamDestroy(st);
+  return status;
+}
+
+}  // extern "C"

@@ -1,0 +1,94 @@
+// Internal launcher declarations shared by the kernel translation units and
+// the host runtime (not part of the public C ABI).
+#pragma once
+
+#include "fft.cuh"
+
+template <typename R>
+cudaError_t launch_curl_base(const GridDev& g, const double* U, R* C6, const double* Ub, const double* Wb, double Vsuck,
+                             cudaStream_t st);
+
+size_t cheb_smem_bytes(int N, size_t rsize);
+
+template <typename TI, typename R, typename TO>
+cudaError_t launch_cheb(int N, bool inverse, int nlines, int ncomp, const TI* in, size_t ld_in, size_t cs_in, TO* out,
+                        size_t ld_out, size_t cs_out, const R* A, const R* B, cudaStream_t st);
+
+template <typename R>
+size_t xfft_smem_bytes(const GridDev& g);
+template <typename R>
+size_t zcross_smem_bytes(const GridDev& g, int RP);
+
+template <typename R>
+cudaError_t launch_xinv(const GridDev& g, const FftPlan& px, const cpx<R>* twx, const cpx<R>* W, cpx<R>* X, int ncomp,
+                        cudaStream_t st);
+template <typename R>
+cudaError_t launch_zcross(const GridDev& g, const FftPlan& pz, const cpx<R>* twz, int RP, const cpx<R>* X, cpx<R>* Z,
+                          cudaStream_t st);
+template <typename R>
+cudaError_t launch_xfwd(const GridDev& g, const FftPlan& px, const cpx<R>* twx, const cpx<R>* Z, cpx<R>* F, int ncomp,
+                        cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// Tau / Helmholtz per-mode tables (FP64), layout [field][n][m] with m the
+// compact mode index (stride Md), plus per-mode scalars [s][m].
+// ---------------------------------------------------------------------------
+enum TauField {
+  TF_PBAND = 0, TF_PUP, TF_PLO, TF_PINV,  // pressure Helmholtz UL factors (lambda = kappa^2, nu = 1)
+  TF_VBAND, TF_VUP, TF_VLO, TF_VINV,      // velocity Helmholtz UL factors (lambda, nu)
+  TF_PP, TF_VP, TF_PM, TF_VM, TF_P0, TF_V0,
+  TF_NFIELDS
+};
+enum TauScalar { TS_I00 = 0, TS_I01, TS_I10, TS_I11, TS_S0NB1, TS_S0NB, TS_UCMEAN, TS_LAMBDA, TS_NSCALARS };
+
+struct TauTable {
+  double* f;  // [TF_NFIELDS][N][Md]
+  double* s;  // [TS_NSCALARS][Md]
+};
+
+// Mode-independent Helmholtz right-hand-side matrices Be/Bo, packed by n:
+// brow[n] holds the row of B that produces u[n]: lo, diag, up; row 0 is e0.
+struct HelmB {
+  const double* lo;
+  const double* di;
+  const double* up;
+};
+
+cudaError_t launch_tau_setup(const GridDev& g, int N, double lambda_t, double nu, const HelmB& hb, TauTable tt,
+                             double* scratch, cudaStream_t st);
+
+// Per-mode solve parameters for one substep.
+struct SolveParams {
+  int kind;          // 0 = multistep (SBDF/CNFE), 1 = CNAB-style substep, 2 = CNRK2 substep
+  int order;         // multistep order
+  double a[4], b[4]; // multistep: rhs = sum_j a_j u_j + b_j N_j
+  // CNAB: rhs = lambda u + a_b L(u,q) - g_b N_j - z_b N_{j-1}
+  double lam, a_b, g_b, z_b;
+  // CNRK2: Q = A_j Q - N(u);  rhs = L(u,q) + lam u + B_C Q
+  double rkA, B_C;
+  double nu;
+  int constraint;    // 0 = PressureGradient, 1 = BulkVelocity
+  double dPdxRef, dPdzRef, umean, wmean;
+  double baseShear[2];  // nu (U'(b) - U'(a)) / Ly and the same for W (bulk-velocity linear term)
+  int taucorrection;
+  int force_real00;  // NSE::solve keeps only the real part of the (0,0) mode
+};
+
+struct SolvePtrs {
+  const double* uin[4];  // multistep history u_j (3 comps each, complex [3][N][Md])
+  const void* nin[4];    // N_j (R-typed, [3][N][Md] complex)
+  const double* qin;     // pressure q (CNAB/RK linear term)
+  double* uout;          // solution u (may alias uin[0] for CNAB/RK)
+  double* qout;          // solution q
+  void* Q;               // CNRK2 accumulator (R-typed)
+  const double* Ubaseyy;
+  const double* Wbaseyy;
+  const double* Ubase;   // for the bulk-velocity linear term
+  const double* Wbase;
+  double* scratch;       // [8][N][2Md]
+  double* dPdx_out;      // device scalars: actual dPdx, dPdz after solve
+};
+
+template <typename R>
+cudaError_t launch_tau_solve(const GridDev& g, int N, const SolveParams& sp, const SolvePtrs& p, const HelmB& hb,
+                             TauTable tt, cudaStream_t st);

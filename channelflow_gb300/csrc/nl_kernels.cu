@@ -1,0 +1,450 @@
+// Nonlinear-term kernels of the DNS step: spectral curl, Chebyshev (y)
+// transforms and the x/z FFT passes with the physical-space cross product.
+//
+// Reference functions restated (channelflow project paths):
+//   curl               channelflow/diffops.cpp:2229-2334
+//   cross              channelflow/diffops.cpp:2560-2611
+//   rotationalNL       channelflow/diffops.cpp:2852-2881
+//   navierstokesNL     channelflow/nse.cpp:12-91 (base flow added to (0,0))
+//   makePhysical_y / makeSpectral_y   channelflow/flowfield.cpp:1888-1987
+//   makePhysical_xz / makeSpectral_xz channelflow/flowfield.cpp:1850-1886
+//   zeroPaddedModes    channelflow/flowfield.cpp:2235-2255 (only solved modes
+//                      are ever stored, so truncation is implicit)
+#include "fft.cuh"
+#include "kernels.h"
+
+// ---------------------------------------------------------------------------
+// Spectral curl with the base flow added to the (0,0) mode.
+//   out[0..2] = u + base,  out[3..5] = curl(u + base)   (Chebyshev coeffs)
+// One thread per mode; the y-derivative is the reference's downward
+// recurrence d[n] = d[n+2] + (4/L)(n+1) u[n+1], d[0] *= 1/2.
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void k_curl_base(GridDev g, const double* __restrict__ U, R* __restrict__ C6,
+                            const double* __restrict__ Ubase, const double* __restrict__ Wbase, double Vsuck) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= g.Md) return;
+  const int Ny = g.Ny;
+  const size_t row = 2 * (size_t)g.Md;
+  const size_t comp = row * Ny;
+  const int kx = mode_kx(g, m), kz = mode_kz(g, m);
+  const double dx = 2.0 * M_PI * kx / g.Lx * (kx == g.kxmax ? 0.0 : 1.0);
+  const double dz = 2.0 * M_PI * kz / g.Lz * (kz == g.kzmax ? 0.0 : 1.0);
+  const bool m00 = (kx == 0 && kz == 0);
+  const double scale = 4.0 / (g.b - g.a);
+  const int Nb = Ny - 1;
+  // Downward recurrence d[n] = d[n+2] + (n+1)*scale*x[n+1] with d[Nb+1] =
+  // d[Nb+2] = 0; (d1, d2) hold d[n+1], d[n+2]; xn holds x[n+1].
+  cpx<double> dw1 = cmk(0.0, 0.0), dw2 = cmk(0.0, 0.0), du1 = cmk(0.0, 0.0), du2 = cmk(0.0, 0.0);
+  cpx<double> un = cmk(0.0, 0.0), wn = cmk(0.0, 0.0);
+  for (int n = Nb; n >= 0; --n) {
+    const size_t o = n * row + 2 * (size_t)m;
+    cpx<double> u = cmk(U[o], U[o + 1]);
+    cpx<double> v = cmk(U[comp + o], U[comp + o + 1]);
+    cpx<double> w = cmk(U[2 * comp + o], U[2 * comp + o + 1]);
+    if (m00) {
+      u.x += Ubase[n];
+      w.x += Wbase[n];
+      if (n == 0) v.x -= Vsuck;
+    }
+    const double c = (n + 1) * scale;
+    const cpx<double> dwn = cmk(dw2.x + c * wn.x, dw2.y + c * wn.y);
+    const cpx<double> dun = cmk(du2.x + c * un.x, du2.y + c * un.y);
+    dw2 = dw1;
+    dw1 = dwn;
+    du2 = du1;
+    du1 = dun;
+    un = u;
+    wn = w;
+    cpx<double> Dw = dwn, Du = dun;
+    if (n == 0) {
+      Dw.x *= 0.5; Dw.y *= 0.5;
+      Du.x *= 0.5; Du.y *= 0.5;
+    }
+    // omega_x = Dw - i dz v ; omega_y = i dz u - i dx w ; omega_z = i dx v - Du
+    cpx<double> ox = cmk(Dw.x + dz * v.y, Dw.y - dz * v.x);
+    cpx<double> oy = cmk(-dz * u.y + dx * w.y, dz * u.x - dx * w.x);
+    cpx<double> oz = cmk(-dx * v.y - Du.x, dx * v.x - Du.y);
+    R* out = C6 + o;
+    out[0] = (R)u.x; out[1] = (R)u.y;
+    out[comp] = (R)v.x; out[comp + 1] = (R)v.y;
+    out[2 * comp] = (R)w.x; out[2 * comp + 1] = (R)w.y;
+    out[3 * comp] = (R)ox.x; out[3 * comp + 1] = (R)ox.y;
+    out[4 * comp] = (R)oy.x; out[4 * comp + 1] = (R)oy.y;
+    out[5 * comp] = (R)oz.x; out[5 * comp + 1] = (R)oz.y;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Chebyshev transform along y of many real lines, parity split.
+// Lines are the interleaved re/im reals of a component: element (n, l) at
+// base[c*cstride + n*ld + l].  One block: 64 lines x all N rows.
+//   inverse (coefficients -> values at y_j = cos(pi j/(N-1))):
+//       E_j = sum_k a_{2k} cos(pi 2k j/(N-1)),  O_j = sum_k a_{2k+1} cos(pi (2k+1) j/(N-1))
+//       u_j = E_j + O_j,  u_{N-1-j} = E_j - O_j        (ichebyfft, chebyshev.cpp:286-303)
+//   forward (values -> coefficients, chebyfft, chebyshev.cpp:262-284):
+//       a_{2k} = sum_j Fe[k][j] (u_j + u_{N-1-j}),  a_{2k+1} = sum_j Fo[k][j] (u_j - u_{N-1-j})
+// A (P x KA) and B (P x KB) hold the two half matrices (host-built in double).
+// ---------------------------------------------------------------------------
+#define CHEB_TL 64
+#define CHEB_WARPS 8
+#define CHEB_PT 9
+
+template <typename TI, typename R, typename TO>
+__global__ void __launch_bounds__(256) k_cheb(int N, int inverse, int nlines, const TI* __restrict__ in, size_t ld_in,
+                                              size_t cs_in, TO* __restrict__ out, size_t ld_out, size_t cs_out,
+                                              const R* __restrict__ Amat, const R* __restrict__ Bmat, int P, int KA,
+                                              int KB) {
+  extern __shared__ unsigned char smem_raw[];
+  R* xa = reinterpret_cast<R*>(smem_raw);
+  R* xb = xa + (size_t)KA * CHEB_TL;
+  R* As = xb + (size_t)KB * CHEB_TL;
+  R* Bs = As + (size_t)P * KA;
+  const int tid = threadIdx.x;
+  const int l0 = blockIdx.x * CHEB_TL;
+  const int c = blockIdx.y;
+  in += c * cs_in;
+  out += c * cs_out;
+  const int J = (N - 1) / 2;
+  for (int i = tid; i < P * KA; i += blockDim.x) As[i] = Amat[i];
+  for (int i = tid; i < P * KB; i += blockDim.x) Bs[i] = Bmat[i];
+  // stage inputs
+  for (int i = tid; i < N * CHEB_TL; i += blockDim.x) {
+    const int n = i / CHEB_TL, l = i % CHEB_TL;
+    const int gl = l0 + l;
+    if (inverse) {
+      R v = gl < nlines ? (R)in[n * ld_in + gl] : (R)0;
+      if (n & 1) xb[(n >> 1) * CHEB_TL + l] = v;
+      else xa[(n >> 1) * CHEB_TL + l] = v;
+    } else if (n <= J) {
+      R v1 = gl < nlines ? (R)in[n * ld_in + gl] : (R)0;
+      R v2 = gl < nlines ? (R)in[(N - 1 - n) * ld_in + gl] : (R)0;
+      if (n < J) {
+        xa[n * CHEB_TL + l] = v1 + v2;
+        xb[n * CHEB_TL + l] = v1 - v2;
+      } else {
+        xa[n * CHEB_TL + l] = v1;  // middle point
+      }
+    }
+  }
+  __syncthreads();
+  const int lane = tid & 31, warp = tid >> 5;
+  R accA[CHEB_PT][2], accB[CHEB_PT][2];
+#pragma unroll
+  for (int i = 0; i < CHEB_PT; ++i) accA[i][0] = accA[i][1] = accB[i][0] = accB[i][1] = (R)0;
+  for (int k = 0; k < KA; ++k) {
+    const R x0 = xa[k * CHEB_TL + lane], x1 = xa[k * CHEB_TL + lane + 32];
+#pragma unroll
+    for (int i = 0; i < CHEB_PT; ++i) {
+      const int p = warp + CHEB_WARPS * i;
+      if (p < P) {
+        const R a = As[p * KA + k];
+        accA[i][0] += a * x0;
+        accA[i][1] += a * x1;
+      }
+    }
+  }
+  for (int k = 0; k < KB; ++k) {
+    const R x0 = xb[k * CHEB_TL + lane], x1 = xb[k * CHEB_TL + lane + 32];
+#pragma unroll
+    for (int i = 0; i < CHEB_PT; ++i) {
+      const int p = warp + CHEB_WARPS * i;
+      if (p < P) {
+        const R bq = Bs[p * KB + k];
+        accB[i][0] += bq * x0;
+        accB[i][1] += bq * x1;
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < CHEB_PT; ++i) {
+    const int p = warp + CHEB_WARPS * i;
+    if (p >= P) continue;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int gl = l0 + lane + 32 * h;
+      if (gl >= nlines) continue;
+      if (inverse) {
+        // p = j in [0, J]
+        out[p * ld_out + gl] = (TO)(accA[i][h] + accB[i][h]);
+        if (p < J) out[(N - 1 - p) * ld_out + gl] = (TO)(accA[i][h] - accB[i][h]);
+      } else {
+        // p = k: even coefficient 2k, odd coefficient 2k+1
+        out[(2 * p) * ld_out + gl] = (TO)accA[i][h];
+        if (2 * p + 1 < N) out[(2 * p + 1) * ld_out + gl] = (TO)accB[i][h];
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// x-direction inverse FFT of the solved (kx, kz) block of one y-plane and
+// component: column kz of the compact input is placed at x-wavenumber
+// positions (kx >= 0 -> kx, kx < 0 -> Nx + kx), zero elsewhere, and
+// transformed with exp(+2 pi i kx x/Nx).  Output X[c][ny][x][iz].
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(256) k_xinv(GridDev g, FftPlan px, const cpx<R>* __restrict__ twx,
+                                              const cpx<R>* __restrict__ W, cpx<R>* __restrict__ X, int czc) {
+  extern __shared__ unsigned char smem_raw[];
+  const int ss = g.Nx + 1;
+  const int iz0 = blockIdx.z * czc;
+  const int nc = min(czc, g.NKz - iz0);
+  cpx<R>* a = reinterpret_cast<cpx<R>*>(smem_raw);
+  cpx<R>* b = a + (size_t)czc * ss;
+  const int ny = blockIdx.x, c = blockIdx.y;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const cpx<R>* src = W + ((size_t)c * g.Ny + ny) * g.Md;
+  for (int i = tid; i < nc * ss; i += nthr) a[i] = cmk<R>(0, 0);
+  __syncthreads();
+  for (int i = tid; i < g.NKx * nc; i += nthr) {
+    const int ix = i / nc, jz = i - ix * nc;
+    const int kx = ix <= g.Kx ? ix : ix - g.NKx;
+    const int pos = kx >= 0 ? kx : g.Nx + kx;
+    a[jz * ss + pos] = src[ix * g.NKz + iz0 + jz];
+  }
+  __syncthreads();
+  fft_batch<R>(a, b, nc, ss, px, twx, +1);
+  cpx<R>* dst = X + ((size_t)c * g.Ny + ny) * (size_t)g.Nx * g.NKz;
+  for (int i = tid; i < g.Nx * nc; i += nthr) {
+    const int x = i / nc, jz = i - x * nc;
+    dst[x * g.NKz + iz0 + jz] = a[jz * ss + x];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// z-direction pass for RP x-rows of one y-plane: c2r inverse FFT of the six
+// fields (u, v, w, ox, oy, oz; two real rows packed per complex FFT), the
+// physical-space cross product f = omega x u, and the r2c forward FFT of f
+// (again two real rows per complex FFT), keeping kz in [0, Kz].
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(256) k_zcross(GridDev g, FftPlan pz, const cpx<R>* __restrict__ twz, int RP,
+                                                const cpx<R>* __restrict__ X, cpx<R>* __restrict__ Z) {
+  extern __shared__ unsigned char smem_raw[];
+  const int Nz = g.Nz, ss = Nz + 1, NKz = g.NKz;
+  const int ninv = 3 * RP;  // inverse sequences
+  cpx<R>* A = reinterpret_cast<cpx<R>*>(smem_raw);
+  cpx<R>* B = A + (size_t)ninv * ss;
+  const int ny = blockIdx.y;
+  const int x0 = blockIdx.x * RP;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const size_t plane = (size_t)g.Nx * NKz;
+  for (int i = tid; i < ninv * ss; i += nthr) A[i] = cmk<R>(0, 0);
+  __syncthreads();
+  // pack: sequence (r, p) = comps (2p, 2p+1) of row x0+r
+  for (int i = tid; i < RP * 3 * NKz; i += nthr) {
+    const int iz = i % NKz;
+    const int rp = i / NKz;
+    const int p = rp % 3, r = rp / 3;
+    const int x = x0 + r;
+    if (x >= g.Nx) continue;
+    const size_t o = ((size_t)(2 * p) * g.Ny + ny) * plane + (size_t)x * NKz + iz;
+    cpx<R> ca = X[o];
+    cpx<R> cb = X[o + (size_t)g.Ny * plane];
+    cpx<R>* s = A + (size_t)(r * 3 + p) * ss;
+    if (iz == 0) {
+      s[0] = cmk<R>(ca.x, cb.x);
+    } else {
+      s[iz] = cmk<R>(ca.x - cb.y, ca.y + cb.x);           // A_k + i B_k
+      s[Nz - iz] = cmk<R>(ca.x + cb.y, -ca.y + cb.x);     // conj(A_k) + i conj(B_k)
+    }
+  }
+  __syncthreads();
+  fft_batch<R>(A, B, ninv, ss, pz, twz, +1);
+  // cross product into B: forward sequences per row pair (r0 = 2q, r1 = 2q+1):
+  //   s0 = f0(r0) + i f1(r0), s1 = f2(r0) + i f2(r1), s2 = f0(r1) + i f1(r1)
+  const int npair = RP / 2;
+  for (int i = tid; i < RP * Nz; i += nthr) {
+    const int z = i % Nz, r = i / Nz;
+    const cpx<R> s0 = A[(size_t)(r * 3 + 0) * ss + z];  // u, v
+    const cpx<R> s1 = A[(size_t)(r * 3 + 1) * ss + z];  // w, ox
+    const cpx<R> s2 = A[(size_t)(r * 3 + 2) * ss + z];  // oy, oz
+    const R u = s0.x, v = s0.y, w = s1.x, ox = s1.y, oy = s2.x, oz = s2.y;
+    const R f0 = oy * w - oz * v;
+    const R f1 = oz * u - ox * w;
+    const R f2 = ox * v - oy * u;
+    const int q = r >> 1;
+    cpx<R>* base = B + (size_t)(q * 3) * ss;
+    if ((r & 1) == 0) {
+      base[z] = cmk<R>(f0, f1);
+      base[ss + z].x = f2;
+    } else {
+      base[2 * ss + z] = cmk<R>(f0, f1);
+      base[ss + z].y = f2;
+    }
+  }
+  __syncthreads();
+  fft_batch<R>(B, A, 3 * npair, ss, pz, twz, -1);
+  // unpack P_k = (Z_k + conj(Z_-k))/2, Q_k = (Z_k - conj(Z_-k))/(2i)
+  for (int i = tid; i < npair * 3 * NKz; i += nthr) {
+    const int iz = i % NKz;
+    const int t = i / NKz;
+    const int sidx = t % 3, q = t / 3;
+    const cpx<R>* s = B + (size_t)(q * 3 + sidx) * ss;
+    const cpx<R> zk = s[iz];
+    const cpx<R> zm = s[iz == 0 ? 0 : Nz - iz];
+    const cpx<R> Pk = cmk<R>((R)0.5 * (zk.x + zm.x), (R)0.5 * (zk.y - zm.y));
+    const cpx<R> Qk = cmk<R>((R)0.5 * (zk.y + zm.y), (R)0.5 * (zm.x - zk.x));
+    const int r0 = x0 + 2 * q, r1 = r0 + 1;
+    // sidx 0: (f0, f1) of r0; 1: (f2 r0, f2 r1); 2: (f0, f1) of r1
+    int cP, cQ, xP, xQ;
+    if (sidx == 0) { cP = 0; cQ = 1; xP = r0; xQ = r0; }
+    else if (sidx == 1) { cP = 2; cQ = 2; xP = r0; xQ = r1; }
+    else { cP = 0; cQ = 1; xP = r1; xQ = r1; }
+    if (xP < g.Nx) Z[((size_t)cP * g.Ny + ny) * plane + (size_t)xP * NKz + iz] = Pk;
+    if (xQ < g.Nx) Z[((size_t)cQ * g.Ny + ny) * plane + (size_t)xQ * NKz + iz] = Qk;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// x-direction forward FFT of the kz columns of one plane/component, keeping
+// the solved kx and applying the 1/(Nx Nz) scale of makeSpectral_xz.
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(256) k_xfwd(GridDev g, FftPlan px, const cpx<R>* __restrict__ twx,
+                                              const cpx<R>* __restrict__ Z, cpx<R>* __restrict__ F, R scale, int czc) {
+  extern __shared__ unsigned char smem_raw[];
+  const int ss = g.Nx + 1;
+  const int iz0 = blockIdx.z * czc;
+  const int nc = min(czc, g.NKz - iz0);
+  cpx<R>* a = reinterpret_cast<cpx<R>*>(smem_raw);
+  cpx<R>* b = a + (size_t)czc * ss;
+  const int ny = blockIdx.x, c = blockIdx.y;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const cpx<R>* src = Z + ((size_t)c * g.Ny + ny) * (size_t)g.Nx * g.NKz;
+  for (int i = tid; i < g.Nx * nc; i += nthr) {
+    const int x = i / nc, jz = i - x * nc;
+    a[jz * ss + x] = src[x * g.NKz + iz0 + jz];
+  }
+  __syncthreads();
+  fft_batch<R>(a, b, nc, ss, px, twx, -1);
+  cpx<R>* dst = F + ((size_t)c * g.Ny + ny) * g.Md;
+  for (int i = tid; i < g.NKx * nc; i += nthr) {
+    const int ix = i / nc, jz = i - ix * nc;
+    const int kx = ix <= g.Kx ? ix : ix - g.NKx;
+    const int pos = kx >= 0 ? kx : g.Nx + kx;
+    dst[ix * g.NKz + iz0 + jz] = cscale(a[jz * ss + pos], scale);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host launchers
+// ---------------------------------------------------------------------------
+template <typename R>
+cudaError_t launch_curl_base(const GridDev& g, const double* U, R* C6, const double* Ub, const double* Wb, double Vsuck,
+                             cudaStream_t st) {
+  const int T = 128;
+  k_curl_base<R><<<(g.Md + T - 1) / T, T, 0, st>>>(g, U, C6, Ub, Wb, Vsuck);
+  return cudaGetLastError();
+}
+
+size_t cheb_smem_bytes(int N, size_t rsize) {
+  const int KA = (N + 1) / 2, KB = (N - 1) / 2, P = (N + 1) / 2;
+  return rsize * ((size_t)(KA + KB) * CHEB_TL + (size_t)P * (KA + KB));
+}
+
+template <typename TI, typename R, typename TO>
+cudaError_t launch_cheb(int N, bool inverse, int nlines, int ncomp, const TI* in, size_t ld_in, size_t cs_in, TO* out,
+                        size_t ld_out, size_t cs_out, const R* A, const R* B, cudaStream_t st) {
+  if ((N + 1) / 2 > CHEB_WARPS * CHEB_PT) return cudaErrorInvalidValue;
+  const int P = (N + 1) / 2;
+  int KA, KB;
+  if (inverse) {
+    KA = (N + 1) / 2;
+    KB = (N - 1) / 2;
+  } else {
+    KA = (N + 1) / 2;
+    KB = (N - 1) / 2;
+  }
+  const size_t sm = cheb_smem_bytes(N, sizeof(R));
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_cheb<TI, R, TO>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr_set = true;
+  }
+  dim3 grid((nlines + CHEB_TL - 1) / CHEB_TL, ncomp);
+  k_cheb<TI, R, TO><<<grid, 32 * CHEB_WARPS, sm, st>>>(N, inverse ? 1 : 0, nlines, in, ld_in, cs_in, out, ld_out,
+                                                       cs_out, A, B, P, KA, KB);
+  return cudaGetLastError();
+}
+
+// Columns per block of the x passes: all NKz when they fit in shared memory.
+template <typename R>
+int xfft_cols(const GridDev& g) {
+  const size_t per = 2 * sizeof(cpx<R>) * (size_t)(g.Nx + 1);
+  int c = (int)((200 * 1024) / per);
+  if (c > g.NKz) c = g.NKz;
+  if (c < 1) c = 1;
+  return c;
+}
+template <typename R>
+size_t xfft_smem_bytes(const GridDev& g) {
+  return 2 * sizeof(cpx<R>) * (size_t)xfft_cols<R>(g) * (g.Nx + 1);
+}
+template <typename R>
+size_t zcross_smem_bytes(const GridDev& g, int RP) {
+  return 2 * sizeof(cpx<R>) * (size_t)(3 * RP) * (g.Nz + 1);
+}
+
+template <typename R>
+cudaError_t launch_xinv(const GridDev& g, const FftPlan& px, const cpx<R>* twx, const cpx<R>* W, cpx<R>* X, int ncomp,
+                        cudaStream_t st) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_xinv<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    attr_set = true;
+  }
+  const int czc = xfft_cols<R>(g);
+  k_xinv<R><<<dim3(g.Ny, ncomp, (g.NKz + czc - 1) / czc), 256, xfft_smem_bytes<R>(g), st>>>(g, px, twx, W, X, czc);
+  return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_zcross(const GridDev& g, const FftPlan& pz, const cpx<R>* twz, int RP, const cpx<R>* X, cpx<R>* Z,
+                          cudaStream_t st) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_zcross<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    attr_set = true;
+  }
+  k_zcross<R><<<dim3((g.Nx + RP - 1) / RP, g.Ny), 256, zcross_smem_bytes<R>(g, RP), st>>>(g, pz, twz, RP, X, Z);
+  return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_xfwd(const GridDev& g, const FftPlan& px, const cpx<R>* twx, const cpx<R>* Z, cpx<R>* F, int ncomp,
+                        cudaStream_t st) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_xfwd<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    attr_set = true;
+  }
+  const R scale = (R)(1.0 / ((double)g.Nx * (double)g.Nz));
+  const int czc = xfft_cols<R>(g);
+  k_xfwd<R><<<dim3(g.Ny, ncomp, (g.NKz + czc - 1) / czc), 256, xfft_smem_bytes<R>(g), st>>>(g, px, twx, Z, F, scale,
+                                                                                          czc);
+  return cudaGetLastError();
+}
+
+#define INST_R(R)                                                                                                   \
+  template cudaError_t launch_curl_base<R>(const GridDev&, const double*, R*, const double*, const double*, double, \
+                                           cudaStream_t);                                                           \
+  template cudaError_t launch_xinv<R>(const GridDev&, const FftPlan&, const cpx<R>*, const cpx<R>*, cpx<R>*, int,   \
+                                      cudaStream_t);                                                                \
+  template cudaError_t launch_zcross<R>(const GridDev&, const FftPlan&, const cpx<R>*, int, const cpx<R>*, cpx<R>*, \
+                                        cudaStream_t);                                                              \
+  template cudaError_t launch_xfwd<R>(const GridDev&, const FftPlan&, const cpx<R>*, const cpx<R>*, cpx<R>*, int,   \
+                                      cudaStream_t);                                                                \
+  template size_t xfft_smem_bytes<R>(const GridDev&);                                                               \
+  template size_t zcross_smem_bytes<R>(const GridDev&, int);
+
+INST_R(float)
+INST_R(double)
+
+template cudaError_t launch_cheb<double, double, double>(int, bool, int, int, const double*, size_t, size_t, double*,
+                                                         size_t, size_t, const double*, const double*, cudaStream_t);
+template cudaError_t launch_cheb<float, float, float>(int, bool, int, int, const float*, size_t, size_t, float*, size_t,
+                                                      size_t, const float*, const float*, cudaStream_t);
+template cudaError_t launch_cheb<float, float, double>(int, bool, int, int, const float*, size_t, size_t, double*,
+                                                       size_t, size_t, const float*, const float*, cudaStream_t);

@@ -1,0 +1,205 @@
+"""Python mirror of the reference's DNS / DNSFlags API over the C ABI.
+
+Mirrors channelflow's ``DNS`` (channelflow/dns.h:30-97) and ``DNSFlags``
+(channelflow/dnsflags.h:81-198): same field names, same enum values, and
+``DNS.advance(u, q, nsteps)`` overwrites the fields in place like
+``DNS::advance(fields, nSteps)``.  Fields are NumPy complex128 arrays shaped
+(Nd, Ny, Nx, Nz//2+1) -- byte-identical to the reference's serial spectral
+FlowField layout.  All arithmetic runs in libcfgpu.so on the GPU; errors
+raise ``CfgpuError`` (the reference exits via cferror instead).
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, fields as dc_fields
+
+import numpy as np
+
+from . import _lib as L
+
+# Enumerations (channelflow/dnsflags.h:24-38)
+ZeroBase, LinearBase, ParabolicBase, LaminarBase, SuctionBase, ArbitraryBase = range(6)
+PressureGradient, BulkVelocity = range(2)
+CNFE1, CNAB2, CNRK2, SMRK2, SBDF1, SBDF2, SBDF3, SBDF4 = range(8)
+Rotational, Convection, Divergence, SkewSymmetric, Alternating, Alternating_, LinearAboutProfile = range(7)
+NoDealiasing, DealiasXZ, DealiasY, DealiasXYZ = range(4)
+
+
+@dataclass
+class DNSFlags:
+    """DNSFlags members used by the time step, with the reference's defaults (dnsflags.h:84-92)."""
+    nu: float = 0.0025
+    dPdx: float = 0.0
+    dPdz: float = 0.0
+    Ubulk: float = 0.0
+    Wbulk: float = 0.0
+    ulowerwall: float = 0.0
+    uupperwall: float = 0.0
+    wlowerwall: float = 0.0
+    wupperwall: float = 0.0
+    Vsuck: float = 0.0
+    t0: float = 0.0
+    dt: float = 0.03125
+    baseflow: int = LaminarBase
+    constraint: int = PressureGradient
+    timestepping: int = SBDF3
+    initstepping: int = SMRK2
+    nonlinearity: int = Rotational
+    dealiasing: int = DealiasXZ
+    taucorrection: bool = True
+
+    def to_c(self) -> L.Flags:
+        f = L.Flags()
+        for fld in dc_fields(self):
+            setattr(f, fld.name, int(getattr(self, fld.name)) if fld.name in (
+                "baseflow", "constraint", "timestepping", "initstepping", "nonlinearity", "dealiasing",
+                "taucorrection") else float(getattr(self, fld.name)))
+        return f
+
+
+@dataclass
+class Grid:
+    Nx: int
+    Ny: int
+    Nz: int
+    Lx: float
+    Lz: float
+    a: float = -1.0
+    b: float = 1.0
+
+    def to_c(self) -> L.Grid:
+        return L.Grid(self.Nx, self.Ny, self.Nz, self.Lx, self.Lz, self.a, self.b)
+
+    @property
+    def Mz(self):
+        return self.Nz // 2 + 1
+
+    def field(self, Nd: int) -> np.ndarray:
+        """Zero spectral FlowField buffer (Nd, Ny, Nx, Mz) complex128."""
+        return np.zeros((Nd, self.Ny, self.Nx, self.Mz), dtype=np.complex128)
+
+
+def _as_field(a: np.ndarray, g: Grid, Nd: int) -> np.ndarray:
+    if a.dtype != np.complex128 or not a.flags["C_CONTIGUOUS"] or a.shape != (Nd, g.Ny, g.Nx, g.Mz):
+        raise ValueError("field must be C-contiguous complex128 of shape %s" % ((Nd, g.Ny, g.Nx, g.Mz),))
+    return a
+
+
+class DNS:
+    """GPU DNS with the reference's DNS interface (channelflow/dns.h:30-97).
+
+    ``precision`` is "fp64" (plain path) or "mixed" (FP32 transforms and
+    nonlinear term, FP64 state and tau solves).
+    """
+
+    def __init__(self, u: np.ndarray, grid: Grid, flags: DNSFlags, base=None, precision: str = "fp64"):
+        lib = L.load()
+        self.grid, self.flags = grid, flags
+        _as_field(u, grid, 3)
+        prec = {"fp64": L.CFGPU_FP64, "mixed": L.CFGPU_MIXED}[precision]
+        h = C.c_void_p()
+        Ub = Wb = None
+        if base is not None:
+            Ub = np.ascontiguousarray(base[0], dtype=np.float64)
+            Wb = np.ascontiguousarray(base[1], dtype=np.float64)
+        gc, fc = grid.to_c(), flags.to_c()
+        L.check(lib.cfgpu_dns_create(C.byref(gc), C.byref(fc), L.dptr(Ub), L.dptr(Wb), L.dptr(u), prec,
+                                     C.byref(h)))
+        self._h = h
+        self._lib = lib
+
+    def advance(self, u: np.ndarray, q: np.ndarray, nsteps: int):
+        """DNS::advance(fields, nSteps): u (3,...) and q (1,...) updated in place."""
+        _as_field(u, self.grid, 3)
+        _as_field(q, self.grid, 1)
+        L.check(self._lib.cfgpu_dns_advance(self._h, L.dptr(u), L.dptr(q), int(nsteps)))
+
+    def set_fields(self, u, q):
+        L.check(self._lib.cfgpu_dns_set_fields(self._h, L.dptr(_as_field(u, self.grid, 3)),
+                                               L.dptr(_as_field(q, self.grid, 1))))
+
+    def advance_resident(self, nsteps: int):
+        L.check(self._lib.cfgpu_dns_advance_resident(self._h, int(nsteps)))
+
+    def get_fields(self, u, q):
+        L.check(self._lib.cfgpu_dns_get_fields(self._h, L.dptr(_as_field(u, self.grid, 3)),
+                                               L.dptr(_as_field(q, self.grid, 1))))
+
+    def advance_timed(self, nsteps: int) -> float:
+        """Resident advance bracketed by CUDA events on the library's stream; device milliseconds."""
+        ms = C.c_double()
+        L.check(self._lib.cfgpu_dns_advance_timed(self._h, int(nsteps), C.byref(ms)))
+        return ms.value
+
+    def set_profiling(self, enable: bool):
+        L.check(self._lib.cfgpu_dns_set_profiling(self._h, int(bool(enable))))
+
+    def phase_times(self):
+        """(nl_ms, nl_count, tau_ms, tau_count) accumulated since the last call."""
+        a, c = C.c_double(), C.c_double()
+        b, d = C.c_longlong(), C.c_longlong()
+        L.check(self._lib.cfgpu_dns_phase_times(self._h, C.byref(a), C.byref(b), C.byref(c), C.byref(d)))
+        return a.value, b.value, c.value, d.value
+
+    def reset_dt(self, dt: float):
+        L.check(self._lib.cfgpu_dns_reset_dt(self._h, float(dt)))
+        self.flags.dt = dt
+
+    def time(self) -> float:
+        t = C.c_double()
+        L.check(self._lib.cfgpu_dns_time(self._h, C.byref(t)))
+        return t.value
+
+    def dPdx(self) -> float:
+        v = C.c_double()
+        L.check(self._lib.cfgpu_dns_dPdx(self._h, C.byref(v)))
+        return v.value
+
+    def base(self):
+        U = np.zeros(self.grid.Ny)
+        W = np.zeros(self.grid.Ny)
+        L.check(self._lib.cfgpu_dns_base(self._h, L.dptr(U), L.dptr(W)))
+        return U, W
+
+    def num_modes(self) -> int:
+        n = C.c_int()
+        L.check(self._lib.cfgpu_dns_num_modes(self._h, C.byref(n)))
+        return n.value
+
+    def device_bytes(self) -> int:
+        n = C.c_longlong()
+        L.check(self._lib.cfgpu_dns_device_bytes(self._h, C.byref(n)))
+        return n.value
+
+    def kernel_launches(self) -> int:
+        n = C.c_longlong()
+        L.check(self._lib.cfgpu_dns_kernel_launches(self._h, C.byref(n)))
+        return n.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.cfgpu_dns_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def tau_solve_batched(N, kx, kz, Lx, Lz, a, b, lambda_t, nu, Rx, Ry, Rz, taucorrection=True):
+    """Batched TauSolver solve; R* complex arrays shaped (nmodes, N). Returns (u, v, w, P)."""
+    lib = L.load()
+    kx = np.ascontiguousarray(kx, dtype=np.int32)
+    kz = np.ascontiguousarray(kz, dtype=np.int32)
+    nm = kx.shape[0]
+    Rs = [np.ascontiguousarray(r, dtype=np.complex128) for r in (Rx, Ry, Rz)]
+    for r in Rs:
+        assert r.shape == (nm, N)
+    outs = [np.zeros((nm, N), dtype=np.complex128) for _ in range(4)]
+    L.check(lib.cfgpu_tau_solve_batched(int(N), int(nm), L.iptr(kx), L.iptr(kz), float(Lx), float(Lz), float(a),
+                                        float(b), float(lambda_t), float(nu), int(bool(taucorrection)),
+                                        *[L.dptr(r) for r in Rs], *[L.dptr(o) for o in outs]))
+    return tuple(outs)

@@ -1,0 +1,158 @@
+/*
+ * cfgpu.h -- C ABI of the GB300-native channelflow DNS time step.
+ *
+ * The library replaces the hot path of channelflow's C++ API: the DNS time
+ * step (DNS / DNSFlags / NSE / TauSolver / HelmholtzSolver) with hand-written
+ * sm_103a CUDA kernels.  Plain C types only: pointers, sizes, doubles.
+ *
+ * Field buffers exchanged with the host use the reference's serial
+ * FlowField spectral layout (channelflow/flowfield.h:383-402): complex
+ * values (re, im interleaved doubles) indexed [i][my][mx][mz], with
+ * Mz = Nz/2+1, my the Chebyshev index, i the vector component.  Velocity
+ * has Nd = 3, pressure q has Nd = 1.
+ *
+ * Only the (kx, kz) modes that the reference's NSE::solve updates (its
+ * "solved set": |kx| <= Nx/3-1, kz <= Nz/3-1 with DealiasXZ; all but the
+ * Nyquist modes without dealiasing) are held on the device.  Those modes are
+ * read from the input buffers and written back; every other mode of the
+ * caller's buffers is left untouched.  The nonlinear term is evaluated from
+ * the solved modes only (the reference also uses any nonzero unsolved modes
+ * of the input; they are zero for every field the reference's own DNS
+ * produces from a padded field).
+ *
+ * Errors: every entry point returns a cfgpu_status; the reference's
+ * cferror() exits the process instead (cfbasics/cfbasics.h:272-278).
+ * cfgpu_last_error() returns a message for the last failure on the calling
+ * thread.
+ */
+#ifndef CFGPU_H
+#define CFGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int cfgpu_status;
+enum {
+  CFGPU_OK = 0,
+  CFGPU_EINVAL = 1,    /* invalid argument (bad grid, flags, null pointer) */
+  CFGPU_ENOMEM = 2,    /* device allocation failed */
+  CFGPU_ECUDA = 3,     /* CUDA runtime error */
+  CFGPU_ENOTSUP = 4,   /* option not implemented on the device path */
+  CFGPU_ENONFINITE = 5 /* NaN or Inf detected in the state */
+};
+
+/* Arithmetic of the nonlinear term and transforms. */
+enum { CFGPU_FP64 = 0, CFGPU_MIXED = 1 };
+
+/* Enumerations with the reference's values (channelflow/dnsflags.h:24-38). */
+enum { CFGPU_ZeroBase = 0, CFGPU_LinearBase, CFGPU_ParabolicBase, CFGPU_LaminarBase, CFGPU_SuctionBase,
+       CFGPU_ArbitraryBase };
+enum { CFGPU_PressureGradient = 0, CFGPU_BulkVelocity };
+enum { CFGPU_CNFE1 = 0, CFGPU_CNAB2, CFGPU_CNRK2, CFGPU_SMRK2, CFGPU_SBDF1, CFGPU_SBDF2, CFGPU_SBDF3, CFGPU_SBDF4 };
+enum { CFGPU_Rotational = 0, CFGPU_Convection, CFGPU_Divergence, CFGPU_SkewSymmetric, CFGPU_Alternating,
+       CFGPU_Alternating_, CFGPU_LinearAboutProfile };
+enum { CFGPU_NoDealiasing = 0, CFGPU_DealiasXZ, CFGPU_DealiasY, CFGPU_DealiasXYZ };
+
+/* Geometry of a FlowField (FlowField(Nx,Ny,Nz,Nd,Lx,Lz,a,b), flowfield.h:60-70). */
+typedef struct cfgpu_grid {
+  int Nx, Ny, Nz;
+  double Lx, Lz, a, b;
+} cfgpu_grid;
+
+/* The DNSFlags members used by the time step (channelflow/dnsflags.h:84-140). */
+typedef struct cfgpu_flags {
+  double nu, dPdx, dPdz, Ubulk, Wbulk;
+  double ulowerwall, uupperwall, wlowerwall, wupperwall;
+  double Vsuck, t0, dt;
+  int baseflow, constraint, timestepping, initstepping, nonlinearity, dealiasing, taucorrection;
+} cfgpu_flags;
+
+typedef struct cfgpu_dns_s* cfgpu_dns;
+
+/* DNSFlags() defaults (channelflow/dnsflags.h:84-92, dnsflags.cpp:110-158). */
+cfgpu_status cfgpu_flags_default(cfgpu_flags* flags);
+
+/*
+ * Builds a DNS on the current CUDA device: base flow, mean constraint,
+ * per-mode tau tables for the main and the initialisation scheme.
+ * Replaces DNS::DNS(fields, flags) (channelflow/dns.cpp:22-39) and, when
+ * Ubase/Wbase are non-null (Ny Chebyshev coefficients each),
+ * DNS::DNS(fields, base, flags) (channelflow/dns.cpp:41-62).  `u` is the
+ * initial velocity in the layout above; it fixes the initial bulk velocity
+ * and dPdx (NSE::initCFConstraint, channelflow/nse.cpp:634-671) but is not
+ * stored: every advance call passes the fields.
+ */
+cfgpu_status cfgpu_dns_create(const cfgpu_grid* grid, const cfgpu_flags* flags, const double* Ubase,
+                              const double* Wbase, const double* u, int precision, cfgpu_dns* out);
+
+/*
+ * DNS::advance(fields, nSteps) (channelflow/dns.cpp:135-163): copies u and q
+ * (host buffers) to the device, takes nsteps steps (initialisation steps of
+ * the init scheme first while the multistep history is not full), and
+ * copies the new u and q back into the same buffers.
+ */
+cfgpu_status cfgpu_dns_advance(cfgpu_dns dns, double* u, double* q, int nsteps);
+
+/* Device-resident variant: set the fields once, advance without host copies, read them back. */
+cfgpu_status cfgpu_dns_set_fields(cfgpu_dns dns, const double* u, const double* q);
+cfgpu_status cfgpu_dns_advance_resident(cfgpu_dns dns, int nsteps);
+cfgpu_status cfgpu_dns_get_fields(cfgpu_dns dns, double* u, double* q);
+
+/* DNS::reset_dt (channelflow/dns.cpp:191-196): rebuilds tau tables, restarts initialisation. */
+cfgpu_status cfgpu_dns_reset_dt(cfgpu_dns dns, double dt);
+
+/* DNS::time(), DNS::dPdx(), DNS::Ubulk() style queries (channelflow/dns.h:55-75). */
+cfgpu_status cfgpu_dns_time(cfgpu_dns dns, double* t);
+cfgpu_status cfgpu_dns_dPdx(cfgpu_dns dns, double* dPdx);
+
+/* Base flow Chebyshev coefficients (NSE::Ubase/Wbase, channelflow/nse.cpp:766-767); Ny doubles each. */
+cfgpu_status cfgpu_dns_base(cfgpu_dns dns, double* Ubase, double* Wbase);
+
+/* Number of solved (kx, kz) modes held on the device. */
+cfgpu_status cfgpu_dns_num_modes(cfgpu_dns dns, int* nmodes);
+
+/* Device bytes held by this DNS. */
+cfgpu_status cfgpu_dns_device_bytes(cfgpu_dns dns, long long* bytes);
+
+/* Launch count of the library's kernels since create (diagnostics). */
+cfgpu_status cfgpu_dns_kernel_launches(cfgpu_dns dns, long long* launches);
+
+cfgpu_status cfgpu_dns_destroy(cfgpu_dns dns);
+
+/*
+ * Timing (no reference counterpart; the reference times dns.advance with
+ * gettimeofday, tools/benchmark.cpp:122-149).  cfgpu_dns_advance_timed runs
+ * cfgpu_dns_advance_resident bracketed by CUDA events on the DNS's stream and
+ * returns the device time in milliseconds.  With profiling enabled, every
+ * nonlinear-term pass and every tau solve is bracketed by events too;
+ * cfgpu_dns_phase_times returns their accumulated milliseconds and counts
+ * since the last reset (and resets them).
+ */
+cfgpu_status cfgpu_dns_advance_timed(cfgpu_dns dns, int nsteps, double* ms);
+cfgpu_status cfgpu_dns_set_profiling(cfgpu_dns dns, int enable);
+cfgpu_status cfgpu_dns_phase_times(cfgpu_dns dns, double* nl_ms, long long* nl_count, double* tau_ms,
+                                   long long* tau_count);
+
+/*
+ * Batched TauSolver (channelflow/tausolver.cpp:81-176 constructor and
+ * 347-402 solve): for nmodes modes (kx[k], kz[k]) of one geometry, solves
+ *   nu (u'' - kappa^2 u) - lambda u - grad P = -R,  div u = 0,  u(a)=u(b)=0
+ * with lambda = lambda_t + nu kappa^2 (NSE::reset_lambda, nse.cpp:683-700).
+ * Profiles are complex Chebyshev coefficients [k][n] (re, im interleaved),
+ * N odd.  The (0,0) mode uses the reference's degenerate branch (v = 0).
+ */
+cfgpu_status cfgpu_tau_solve_batched(int N, int nmodes, const int* kx, const int* kz, double Lx, double Lz, double a,
+                                     double b, double lambda_t, double nu, int taucorrection, const double* Rx,
+                                     const double* Ry, const double* Rz, double* u, double* v, double* w, double* P);
+
+/* Library version string. */
+const char* cfgpu_version(void);
+
+/* Message for the last error on the calling thread. */
+const char* cfgpu_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CFGPU_H */

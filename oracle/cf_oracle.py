@@ -428,9 +428,10 @@ class TauSolver:
     def verify(self, u, v, w, P, Rx, Ry, Rz):
         """Residual of the discrete Stokes problem (after TauSolver::verify, tausolver.cpp:452-629).
 
-        Returns, per mode, the sum of: L2 residual of nu u'' - kappa2 nu u -
-        lambda u - grad P + R over the first N-2 Chebyshev equations of each
-        momentum component, the divergence, and the four boundary values.
+        Returns, per mode, the sum of: L2 residual of nu u'' - lambda u -
+        grad P + R (lambda includes nu kappa^2) over the first N-2 Chebyshev
+        equations of each momentum component, the divergence, and the
+        boundary values of u, v, w and v'.
         """
         L, nu, lam = self.L, self.nu, self.lam
         k2 = self.kappa2
@@ -438,10 +439,10 @@ class TauSolver:
         Dz = 1j * self.two_pi_kzLz
         err = np.zeros(u.shape[1])
         for f, Rf, grad in ((u, Rx, Dx * P), (w, Rz, Dz * P)):
-            res = nu * (cdiff2(f.real, L) + 1j * cdiff2(f.imag, L)) - (nu * k2 + lam) * f - grad + Rf
+            res = nu * (cdiff2(f.real, L) + 1j * cdiff2(f.imag, L)) - lam * f - grad + Rf
             err += np.sqrt(cheb_l2norm2(res[: self.N - 2]))
         Py = cdiff(P.real, L) + 1j * cdiff(P.imag, L)
-        res = nu * (cdiff2(v.real, L) + 1j * cdiff2(v.imag, L)) - (nu * k2 + lam) * v - Py + Ry
+        res = nu * (cdiff2(v.real, L) + 1j * cdiff2(v.imag, L)) - lam * v - Py + Ry
         err += np.sqrt(cheb_l2norm2(res[: self.N - 2]))
         vy = cdiff(v.real, L) + 1j * cdiff(v.imag, L)
         div = Dx * u + vy + Dz * w

@@ -1,0 +1,141 @@
+"""GPU parity: libcfgpu.so (through its C ABI) against the oracle and the reference's golden data."""
+
+import math
+import os
+
+import numpy as np
+import pytest
+
+from oracle import cf_oracle as O
+from tests.helpers import COUETTE_BOX, POISEUILLE_BOX, oracle_run, rel_l2, solved_mask, to_cflags, to_cgrid
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+FP64_TOL = 1e-10     # relative L2 after the run, plain FP64 path (Chebyshev-weighted norm)
+MIXED_TOL = 1e-5     # relative L2, FP32 transforms/nonlinear term + FP64 tau solves
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from channelflow_gb300 import build
+    build.build()
+
+
+def gpu_run(u0, g, fl, nsteps, precision="fp64", base=None, chunks=None):
+    from channelflow_gb300 import DNS
+    u = np.ascontiguousarray(u0.copy())
+    q = np.zeros((1,) + u.shape[1:], complex)
+    dns = DNS(u, to_cgrid(g), to_cflags(fl), base=base, precision=precision)
+    for n in (chunks or [nsteps]):
+        dns.advance(u, q, n)
+    return u, q, dns
+
+
+def test_tau_batched_matches_oracle():
+    from channelflow_gb300 import tau_solve_batched
+    from tests.test_oracle_golden import tau_case
+    rng = np.random.default_rng(11)
+    for _ in range(10):
+        c = tau_case(rng)
+        kxs = np.array([c["kx"], 0, 1, 3])
+        kzs = np.array([c["kz"], 0, 0, 2])
+        R = [np.stack([c[k]] * 4) for k in ("Rx", "Ry", "Rz")]
+        u, v, w, P = tau_solve_batched(c["N"], kxs, kzs, c["Lx"], c["Lz"], c["a"], c["b"], c["lam_t"], c["nu"], *R)
+        lam = c["lam_t"] + 4 * math.pi ** 2 * c["nu"] * ((kxs / c["Lx"]) ** 2 + (kzs / c["Lz"]) ** 2)
+        ts = O.TauSolver(kxs, kzs, c["Lx"], c["Lz"], c["a"], c["b"], lam, c["nu"], c["N"])
+        ou, ov, ow, oP = ts.solve(*[r.T.copy() for r in R])
+        for got, ref in ((u, ou), (v, ov), (w, ow), (P, oP)):
+            scale = np.abs(ref).max()
+            assert np.abs(got - ref.T).max() <= 1e-12 * scale
+        # the first mode reproduces the analytic solution
+        assert np.abs(u[0] - c["u"]).max() < 1e-9 and np.abs(v[0] - c["v"]).max() < 1e-9
+
+
+CASES = [
+    # name, grid, flags kwargs, steps
+    ("couette_sbdf3", (16, 17, 16, *COUETTE_BOX),
+     dict(nu=1 / 400, dt=0.02, timestepping=O.SBDF3, initstepping=O.SMRK2, baseflow=O.LaminarBase,
+          ulowerwall=-1.0, uupperwall=1.0), 30),
+    ("poiseuille_cnab2_bulk", (24, 33, 24, *POISEUILLE_BOX),
+     dict(nu=1 / 4000, dt=0.01, timestepping=O.CNAB2, initstepping=O.SMRK2, baseflow=O.LaminarBase,
+          constraint=O.BulkVelocity, Ubulk=2.0 / 3.0), 30),
+    ("couette_cnrk2_gradp", (12, 17, 12, *COUETTE_BOX),
+     dict(nu=1 / 400, dt=0.02, timestepping=O.CNRK2, baseflow=O.LaminarBase, ulowerwall=-1.0, uupperwall=1.0), 10),
+    ("poiseuille_sbdf4_bulk", (12, 17, 12, *POISEUILLE_BOX),
+     dict(nu=1 / 2000, dt=0.01, timestepping=O.SBDF4, initstepping=O.SMRK2, baseflow=O.LaminarBase,
+          constraint=O.BulkVelocity, Ubulk=2.0 / 3.0), 12),
+    ("couette_sbdf2", (12, 17, 12, *COUETTE_BOX),
+     dict(nu=1 / 400, dt=0.02, timestepping=O.SBDF2, initstepping=O.SMRK2, baseflow=O.LaminarBase,
+          ulowerwall=-1.0, uupperwall=1.0), 10),
+    ("couette_cnfe1", (12, 17, 12, *COUETTE_BOX),
+     dict(nu=1 / 400, dt=0.02, timestepping=O.CNFE1, baseflow=O.LaminarBase, ulowerwall=-1.0, uupperwall=1.0), 10),
+    ("couette_smrk2_nodealias", (8, 17, 8, *COUETTE_BOX),
+     dict(nu=1 / 400, dt=0.02, timestepping=O.SMRK2, baseflow=O.LaminarBase, ulowerwall=-1.0, uupperwall=1.0,
+          dealiasing=O.NoDealiasing), 10),
+    ("suction_sbdf1_gradp", (12, 17, 12, *COUETTE_BOX),
+     dict(nu=1 / 400, dt=0.02, timestepping=O.SBDF1, baseflow=O.SuctionBase, Vsuck=1 / 400), 10),
+    ("poiseuille_48_cnab2", (48, 49, 48, *POISEUILLE_BOX),
+     dict(nu=1 / 4000, dt=0.01, timestepping=O.CNAB2, initstepping=O.SMRK2, baseflow=O.LaminarBase,
+          constraint=O.BulkVelocity, Ubulk=2.0 / 3.0), 5),
+]
+
+
+@pytest.mark.parametrize("name,grid,fk,nsteps", CASES, ids=[c[0] for c in CASES])
+def test_dns_fp64_matches_oracle(name, grid, fk, nsteps):
+    g = O.Grid(*grid)
+    fl = O.DNSFlags(**fk)
+    dealias = fl.dealiasing == O.DealiasXZ
+    u0 = O.random_divfree_field(g, seed=hash(name) % 1000, norm=0.1,
+                                zero_mean_u=fl.constraint == O.BulkVelocity)
+    if not dealias:
+        u0[:, :, ~solved_mask(g, dealias)] = 0.0
+    ou, oq, _ = oracle_run(u0, g, fl, nsteps, chunks=[nsteps // 2, nsteps - nsteps // 2])
+    gu, gq, dns = gpu_run(u0, g, fl, nsteps, chunks=[nsteps // 2, nsteps - nsteps // 2])
+    m = solved_mask(g, dealias)
+    ou[:, :, ~m] = 0
+    oq[:, :, ~m] = 0
+    assert rel_l2(gu, ou, g) <= FP64_TOL
+    assert rel_l2(gq, oq, g) <= 1e-9
+    assert abs(dns.time() - (fl.t0 + nsteps * fl.dt)) < 1e-12
+
+
+def test_time_integration_golden_gpu():
+    """The reference's golden regression on the GPU: uinit -> 440 SBDF3 steps -> ufinal."""
+    z = np.load(os.path.join(GOLD, "timeintegration.npz"))
+    g = O.Grid(int(z["uinit_Nx"]), int(z["uinit_Ny"]), int(z["uinit_Nz"]), float(z["uinit_Lx"]),
+               float(z["uinit_Lz"]), float(z["uinit_a"]), float(z["uinit_b"]))
+    u0 = O.load_io_field(z["uinit"], g.Nx, g.Nz)
+    uf = O.load_io_field(z["ufinal"], g.Nx, g.Nz)
+    fl = O.DNSFlags(baseflow=O.SuctionBase, timestepping=O.SBDF3, initstepping=O.SMRK2, dt=1.0 / 40,
+                    nu=1.0 / 400, Vsuck=1.0 / 400)
+    gu, _, _ = gpu_run(u0, g, fl, 440, chunks=[40] * 11)
+    m = solved_mask(g)
+    uf[:, :, ~m] = 0
+    gu[:, :, ~m] = 0
+    assert O.L2Dist(gu, uf, g) <= 1e-13
+
+
+def test_dns_mixed_matches_oracle():
+    g = O.Grid(32, 33, 32, *COUETTE_BOX)
+    fl = O.DNSFlags(nu=1 / 400, dt=0.02, timestepping=O.SBDF3, initstepping=O.SMRK2, baseflow=O.LaminarBase,
+                    ulowerwall=-1.0, uupperwall=1.0)
+    u0 = O.random_divfree_field(g, seed=5, norm=0.1)
+    ou, _, _ = oracle_run(u0, g, fl, 50)
+    gu, _, _ = gpu_run(u0, g, fl, 50, precision="mixed")
+    ou[:, :, ~solved_mask(g)] = 0
+    assert rel_l2(gu, ou, g) <= MIXED_TOL
+
+
+def test_resident_path_equals_host_path():
+    g = O.Grid(16, 17, 16, *COUETTE_BOX)
+    fl = O.DNSFlags(nu=1 / 400, dt=0.02, baseflow=O.LaminarBase, ulowerwall=-1.0, uupperwall=1.0)
+    u0 = O.random_divfree_field(g, seed=3, norm=0.1)
+    a, _, _ = gpu_run(u0, g, fl, 12)
+    from channelflow_gb300 import DNS
+    u = u0.copy()
+    q = np.zeros((1,) + u.shape[1:], complex)
+    dns = DNS(u, to_cgrid(g), to_cflags(fl))
+    dns.set_fields(u, q)
+    dns.advance_resident(12)
+    dns.get_fields(u, q)
+    assert np.array_equal(u, a)
