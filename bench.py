@@ -1,0 +1,330 @@
+"""Benchmark of the GB300 DNS time step (one JSON line on stdout).
+
+Workload: plane Poiseuille flow at constant bulk velocity (Ubulk = 2/3,
+Re_centreline = 4000, nu = 1/4000), box Lx = 4 pi, Lz = 2 pi, grid
+128 x 97 x 128, CNAB2 with SMRK2 start-up, dt = 0.01, rotational
+nonlinearity with 2/3-rule dealiasing; initial field = laminar profile plus a
+seeded divergence-free perturbation of L2 norm 0.3 (synthetic, see
+channelflow_gb300/fields.py).  A "step" is one CNAB2 time step of that field.
+
+GPU arm (default):  value = steps/s of the mixed-precision path (FP32
+transforms and nonlinear term, FP64 state and tau solves) with the fields
+resident in HBM, device-timed with CUDA events on the library's stream.
+The plain FP64 path is timed the same way ("fp64" block), the end-to-end
+number goes through cfgpu_dns_advance with host buffers every step ("e2e"),
+and the mixed-vs-FP64 relative L2 difference after T = 10 is reported
+("accuracy").  With torchrun, every rank runs an independent replica on its
+own GPU (the DNS of one field does not shard); value aggregates all ranks.
+
+Reference arm (--impl reference): the reference's algorithm restated on the
+CPU (oracle/cf_oracle.py, NumPy, one core) on the same workload; each timed
+step is one full CNAB2 step of the 128 x 97 x 128 field.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DNS steps/s 128x97x128: FP32-mixed vs FP64 at stated L2 err; serve p50/p99"
+NX, NY, NZ = 128, 97, 128
+LX, LZ = 4 * math.pi, 2 * math.pi
+NU, DT, UBULK = 1.0 / 4000.0, 0.01, 2.0 / 3.0
+WORKLOAD = ("plane Poiseuille 128x97x128 (Lx=4pi, Lz=2pi), CNAB2 + SMRK2 start-up, dt=0.01, bulk velocity "
+            "Ubulk=2/3, Re_c=4000, rotational NL, 2/3 dealiasing, seeded perturbation L2=0.3")
+CNAB2, SMRK2, LaminarBase, BulkVelocity = 1, 3, 3, 1
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if not self.path or not os.path.exists(self.path):
+            return out
+        sm, smax, reasons = [], [], set()
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"),
+                                 f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        os.unlink(self.path)
+        if sm:
+            out.update(sm_mhz=statistics.median(sm), sm_max_mhz=max(smax), reasons=sorted(reasons),
+                       samples=len(sm))
+        return out
+
+
+def make_flags():
+    from channelflow_gb300 import DNSFlags
+    return DNSFlags(nu=NU, dt=DT, timestepping=CNAB2, initstepping=SMRK2, baseflow=LaminarBase,
+                    constraint=BulkVelocity, Ubulk=UBULK)
+
+
+def initial_field(seed=1):
+    from channelflow_gb300.fields import random_divfree_field
+    return random_divfree_field(NX, NY, NZ, LX, LZ, seed=seed, norm=0.3, zero_mean_u=True)
+
+
+def bytes_per_step(Md, prec):
+    """Algorithmic HBM bytes of one CNAB2 step (fixed by formula, independent of the implementation).
+
+    A = Ny*Md complex values per component.  Nonlinear pass (read u, write
+    y-physical u and omega; read 6, write f; read 3, write N):
+        B_NL = 2A (6*8 + 18*s_w)
+    Tau pass (read u, q (FP64), N_j, N_j-1 (s_w), per-mode tables 14 Ny
+    doubles; write u, q):  B_tau = 2A (4*8 + 6*s_w + 4*8) + 14*8*A
+    """
+    A = NY * Md
+    sw = 4 if prec == "mixed" else 8
+    bnl = 2 * A * (6 * 8 + 18 * sw)
+    btau = 2 * A * (4 * 8 + 6 * sw + 4 * 8) + 14 * 8 * A
+    return bnl, btau
+
+
+def run_gpu(args, rank, world):
+    import ctypes  # noqa: F401
+    from channelflow_gb300 import DNS, Grid
+    from channelflow_gb300 import build as b
+    from channelflow_gb300.fields import l2norm
+
+    b.build()
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist_
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", rank)))
+        dist_.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        dist = dist_
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if not dist:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    grid = Grid(NX, NY, NZ, LX, LZ)
+    u0 = initial_field(seed=1 + rank)
+    q0 = np.zeros((1,) + u0.shape[1:], dtype=np.complex128)
+    results = {}
+    hbm, peak_kind = peaks()
+    for prec in ("mixed", "fp64"):
+        u, q = u0.copy(), q0.copy()
+        dns = DNS(u, grid, make_flags(), precision=prec)
+        dns.set_fields(u, q)
+        dns.advance_resident(args.warmup)
+        K = args.steps if prec == "mixed" else max(3, args.steps // 4)
+        dns.set_profiling(True)
+        dns.phase_times()
+        l0 = dns.kernel_launches()
+        barrier()
+        with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as cs:
+            ms = dns.advance_timed(K)
+        ms = max_over_ranks(ms)
+        launches = dns.kernel_launches() - l0
+        nl_ms, nl_n, tau_ms, tau_n = dns.phase_times()
+        dns.set_profiling(False)
+        results[prec] = dict(ms=ms, K=K, launches=launches, clocks=cs.summary(), nl_ms=nl_ms, nl_n=nl_n,
+                             tau_ms=tau_ms, tau_n=tau_n, Md=dns.num_modes(), bytes=dns.device_bytes())
+        if prec == "mixed":
+            # end-to-end through the public API: host buffers in, host buffers out, every step
+            Ke = max(3, min(args.steps, 50))
+            ue, qe = u0.copy(), q0.copy()
+            dns_e = DNS(ue, grid, make_flags(), precision=prec)
+            dns_e.advance(ue, qe, args.warmup)
+            barrier()
+            t0 = time.perf_counter()
+            for _ in range(Ke):
+                dns_e.advance(ue, qe, 1)
+            te = max_over_ranks(time.perf_counter() - t0)
+            Md = dns_e.num_modes()
+            results["e2e"] = dict(s=te, K=Ke, h2d=4 * NY * Md * 16, d2h=4 * NY * Md * 16)
+            dns_e.close()
+        dns.close()
+    acc = None
+    if args.accuracy_steps > 0 and rank == 0:
+        outs = {}
+        for prec in ("mixed", "fp64"):
+            u, q = u0.copy(), q0.copy()
+            d = DNS(u, grid, make_flags(), precision=prec)
+            d.set_fields(u, q)
+            d.advance_resident(args.accuracy_steps)
+            d.get_fields(u, q)
+            d.close()
+            outs[prec] = u
+        diff = l2norm(outs["mixed"] - outs["fp64"], NX, NZ) / l2norm(outs["fp64"], NX, NZ)
+        acc = {"T": args.accuracy_steps * DT, "rel_l2_mixed_vs_fp64": diff,
+               "norm": "Chebyshev-weighted L2 over all modes (diffops.cpp:415-487)"}
+    return results, acc, hbm, peak_kind
+
+
+def cpu_sample(nsteps):
+    """The oracle (reference algorithm restated in NumPy) on the same workload: nsteps CNAB2 steps."""
+    from oracle import cf_oracle as O
+    g = O.Grid(NX, NY, NZ, LX, LZ)
+    fl = O.DNSFlags(nu=NU, dt=DT, timestepping=O.CNAB2, initstepping=O.SMRK2, baseflow=O.LaminarBase,
+                    constraint=O.BulkVelocity, Ubulk=UBULK)
+    u = initial_field()
+    q = np.zeros((1,) + u.shape[1:], dtype=np.complex128)
+    dns = O.DNS(u, q, g, fl)
+    u, q = dns.advance(u, q, 1)  # SMRK2 start-up step (untimed)
+    t0 = time.perf_counter()
+    for _ in range(nsteps):
+        u, q = dns.advance(u, q, 1)
+    dt = time.perf_counter() - t0
+    return nsteps / dt, dt
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--accuracy-steps", type=int, default=1000, help="steps for the mixed-vs-FP64 error (T=10)")
+    ap.add_argument("--cpu-steps", type=int, default=3, help="oracle steps in the cpu_baseline sample")
+    ap.add_argument("--grid", default=None, help="Nx,Ny,Nz override for small profiling cases (not a bench line)")
+    args = ap.parse_args()
+    if args.grid:
+        global NX, NY, NZ
+        NX, NY, NZ = (int(v) for v in args.grid.split(","))
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        warm = max(0, min(args.warmup, 3))
+        from oracle import cf_oracle as O  # noqa: F401
+        n = max(1, min(args.steps, 20))
+        sps, secs = cpu_sample(n)
+        line = {"metric": METRIC, "impl": "reference", "value": sps, "unit": "steps/s", "n_gpus": args.gpus,
+                "steps": n, "warmup": warm, "ms_per_step": 1000.0 / sps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": WORKLOAD, "grid": [NX, NY, NZ]},
+                "cpu_baseline": {"value": sps, "unit": "steps/s", "cores": 1, "kind": "port",
+                                 "sample": "%d full CNAB2 steps of the 128x97x128 field after 1 SMRK2 start-up "
+                                           "step (NumPy restatement of the reference, one core)" % n},
+                "e2e": {"value": sps, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    res, acc, hbm, peak_kind = run_gpu(args, rank, world)
+    if rank != 0:
+        return
+    m = res["mixed"]
+    Md = m["Md"]
+    sps = world * m["K"] / (m["ms"] / 1000.0)
+    f = res["fp64"]
+    sps64 = world * f["K"] / (f["ms"] / 1000.0)
+    bnl, btau = bytes_per_step(Md, "mixed")
+    nl_avg = m["nl_ms"] / max(1, m["nl_n"])
+    tau_avg = m["tau_ms"] / max(1, m["tau_n"])
+    phases = {"nonlinear_pass": (nl_avg, bnl, m["nl_ms"]), "tau_solve": (tau_avg, btau, m["tau_ms"])}
+    dom = max(phases, key=lambda k: phases[k][2])
+    t_avg, bts, _ = phases[dom]
+    ach = bts / (t_avg / 1000.0) / 1e9
+    e = res["e2e"]
+    cpu = None
+    if world == 1 and args.cpu_steps > 0:
+        cps, csecs = cpu_sample(args.cpu_steps)
+        cpu = {"value": cps, "unit": "steps/s", "cores": 1, "kind": "port",
+               "sample": "%d full CNAB2 steps of the 128x97x128 field (after 1 untimed SMRK2 start-up step), "
+                         "NumPy restatement of the reference on one host core, %.1f s" % (args.cpu_steps, csecs)}
+    bnl64, btau64 = bytes_per_step(Md, "fp64")
+    line = {
+        "metric": METRIC, "value": sps, "unit": "steps/s", "n_gpus": world, "steps": m["K"],
+        "warmup": args.warmup, "ms_per_step": m["ms"] / m["K"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64 (FP32 transforms/NL, FP64 state and tau solves)",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "precision": "mixed", "grid": [NX, NY, NZ], "solved_modes": Md,
+                   "grid_point_steps_per_s": sps * NX * NY * NZ,
+                   "l2": "no flush: per-step working set %.0f MB > 129 MB L2" % (m["bytes"] / 1e6),
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm, "unit": "GB/s",
+                     "frac": ach / hbm, "peak_source": peak_kind, "traffic": None,
+                     "algorithmic_bytes": bts, "avg_launch_ms": t_avg},
+        "phases": {"nonlinear_pass": {"avg_ms": nl_avg, "launches": m["nl_n"], "alg_bytes": bnl,
+                                      "achieved_gbs": bnl / (nl_avg / 1e3) / 1e9 if nl_avg else None,
+                                      "frac": (bnl / (nl_avg / 1e3) / 1e9) / hbm if nl_avg else None},
+                   "tau_solve": {"avg_ms": tau_avg, "launches": m["tau_n"], "alg_bytes": btau,
+                                 "achieved_gbs": btau / (tau_avg / 1e3) / 1e9 if tau_avg else None}},
+        "fp64": {"value": sps64, "unit": "steps/s", "ms_per_step": f["ms"] / f["K"], "steps": f["K"],
+                 "nl_avg_ms": f["nl_ms"] / max(1, f["nl_n"]), "tau_avg_ms": f["tau_ms"] / max(1, f["tau_n"]),
+                 "nl_alg_bytes": bnl64, "tau_alg_bytes": btau64},
+        "accuracy": acc,
+        "e2e": {"value": world * e["K"] / e["s"], "unit": "steps/s", "h2d_bytes_per_step": e["h2d"],
+                "d2h_bytes_per_step": e["d2h"],
+                "path": "cfgpu_dns_advance(u, q, 1) per step with host FlowField buffers"},
+        "gpu_launches": m["launches"],
+        "clocks": m["clocks"],
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

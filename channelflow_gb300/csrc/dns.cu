@@ -196,7 +196,21 @@ bool make_fft_plan(int L, FftPlan& p, std::vector<std::complex<long double>>& tw
 
 struct ChebMats {
   std::vector<double> invA, invB, fwdA, fwdB;  // P x KA, P x KB (row-major)
+  std::vector<double> derA, derB;              // (2/L) T'_n at y_j for even / odd n
 };
+
+long double sinpi_ratio(long long m, long long d) {
+  long long r = m % (2 * d);
+  if (r < 0) r += 2 * d;
+  return sinl(3.14159265358979323846264338327950288L * (long double)r / (long double)d);
+}
+
+// T'_n(y_j) at y_j = cos(pi j/(N-1)): n sin(n theta)/sin(theta), n^2 at j = 0
+long double cheb_deriv_at(int n, int j, int N) {
+  if (j == 0) return (long double)n * n;
+  if (2 * j == 2 * (N - 1)) return (n % 2 ? 1.0L : -1.0L) * n * n;
+  return n * sinpi_ratio((long long)n * j, N - 1) / sinpi_ratio(j, N - 1);
+}
 
 ChebMats make_cheb_mats(int N) {
   ChebMats M;
@@ -208,6 +222,12 @@ ChebMats make_cheb_mats(int N) {
   for (int j = 0; j < P; ++j) {
     for (int k = 0; k < KA; ++k) M.invA[j * KA + k] = (double)cospi_ratio(2LL * k * j, N - 1);
     for (int k = 0; k < KB; ++k) M.invB[j * KB + k] = (double)cospi_ratio((2LL * k + 1) * j, N - 1);
+  }
+  M.derA.assign((size_t)P * KA, 0.0);
+  M.derB.assign((size_t)P * KB, 0.0);
+  for (int j = 0; j < P; ++j) {
+    for (int k = 0; k < KA; ++k) M.derA[j * KA + k] = (double)(cheb_deriv_at(2 * k, j, N));
+    for (int k = 0; k < KB; ++k) M.derB[j * KB + k] = (double)(cheb_deriv_at(2 * k + 1, j, N));
   }
   for (int k = 0; k < P; ++k) {
     const int n = 2 * k;
@@ -349,6 +369,7 @@ struct cfgpu_dns_s {
   FftPlan px{}, pz{};
   void *twx = nullptr, *twz = nullptr;  // R-typed complex
   void *cinvA = nullptr, *cinvB = nullptr, *cfwdA = nullptr, *cfwdB = nullptr;
+  void *cderA = nullptr, *cderB = nullptr, *basey = nullptr;  // fused curl: (2/L) T'_n(y_j); U, U', W, W' at y_j
   // state: current fields
   double *Ucur = nullptr, *Qcur = nullptr;
   // multistep ring
@@ -438,9 +459,15 @@ int nonlinear_impl(cfgpu_dns d, const double* U, void* Nout) {
   R* C6 = (R*)d->C6;
   R* W6 = (R*)d->W6;
   const size_t row = d->rowc(), comp = d->compc();
-  CK(launch_curl_base<R>(g, U, C6, d->dUbase, d->dWbase, d->fl.Vsuck, d->st));
-  CK((launch_cheb<R, R, R>(N, true, (int)row, 6, C6, row, comp, W6, row, comp, (const R*)d->cinvA,
-                           (const R*)d->cinvB, d->st)));
+  if ((N + 1) / 2 <= 56) {
+    CK(launch_curl_cheb<R>(g, N, U, W6, (const R*)d->cinvA, (const R*)d->cinvB, (const R*)d->cderA,
+                           (const R*)d->cderB, (const R*)d->basey, d->fl.Vsuck, d->st));
+    d->launches -= 1;
+  } else {
+    CK(launch_curl_base<R>(g, U, C6, d->dUbase, d->dWbase, d->fl.Vsuck, d->st));
+    CK((launch_cheb<R, R, R>(N, true, (int)row, 6, C6, row, comp, W6, row, comp, (const R*)d->cinvA,
+                             (const R*)d->cinvB, d->st)));
+  }
   CK(launch_xinv<R>(g, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)W6, (cpx<R>*)d->X6, 6, d->st));
   CK(launch_zcross<R>(g, d->pz, (const cpx<R>*)d->twz, d->RP, (const cpx<R>*)d->X6, (cpx<R>*)d->Z3, d->st));
   CK(launch_xfwd<R>(g, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)d->Z3, (cpx<R>*)d->F3, 3, d->st));
@@ -815,6 +842,24 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
   if (!make_fft_plan(Nx, d->px, twx) || !make_fft_plan(Nz, d->pz, twz))
     return fail(CFGPU_ENOTSUP, "Nx and Nz must factor into 2, 3 and 5");
   ChebMats cm = make_cheb_mats(Ny);
+  for (auto& v : cm.derA) v *= 2.0 / (b - a);
+  for (auto& v : cm.derB) v *= 2.0 / (b - a);
+  std::vector<double> basey(4 * (size_t)Ny, 0.0);
+  for (int j = 0; j < Ny; ++j) {
+    long double U = 0, Uy = 0, W = 0, Wy = 0;
+    for (int n = 0; n < Ny; ++n) {
+      const long double c = cospi_ratio((long long)n * j, Ny - 1);
+      const long double dd = cheb_deriv_at(n, j, Ny) * (2.0L / (b - a));
+      U += d->Ubase[n] * c;
+      Uy += d->Ubase[n] * dd;
+      W += d->Wbase[n] * c;
+      Wy += d->Wbase[n] * dd;
+    }
+    basey[j] = (double)U;
+    basey[Ny + j] = (double)Uy;
+    basey[2 * Ny + j] = (double)W;
+    basey[3 * Ny + j] = (double)Wy;
+  }
   const bool fp64 = d->precision == CFGPU_FP64;
   if (fp64) {
     CKS(upload_tw<double>(twx, &d->twx, B));
@@ -823,6 +868,9 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
     CKS(upload_as<double>(cm.invB, &d->cinvB, B));
     CKS(upload_as<double>(cm.fwdA, &d->cfwdA, B));
     CKS(upload_as<double>(cm.fwdB, &d->cfwdB, B));
+    CKS(upload_as<double>(cm.derA, &d->cderA, B));
+    CKS(upload_as<double>(cm.derB, &d->cderB, B));
+    CKS(upload_as<double>(basey, &d->basey, B));
   } else {
     CKS(upload_tw<float>(twx, &d->twx, B));
     CKS(upload_tw<float>(twz, &d->twz, B));
@@ -830,6 +878,9 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
     CKS(upload_as<float>(cm.invB, &d->cinvB, B));
     CKS(upload_as<float>(cm.fwdA, &d->cfwdA, B));
     CKS(upload_as<float>(cm.fwdB, &d->cfwdB, B));
+    CKS(upload_as<float>(cm.derA, &d->cderA, B));
+    CKS(upload_as<float>(cm.derB, &d->cderB, B));
+    CKS(upload_as<float>(basey, &d->basey, B));
   }
   // state and work arrays
   const size_t cd = d->compc();
@@ -917,6 +968,7 @@ void dns_free(cfgpu_dns d) {
   F(d->dUbase); F(d->dWbase); F(d->dUbaseyy); F(d->dWbaseyy); F(d->ddPdx);
   F(d->hb_lo); F(d->hb_di); F(d->hb_up);
   F(d->twx); F(d->twz); F(d->cinvA); F(d->cinvB); F(d->cfwdA); F(d->cfwdB);
+  F(d->cderA); F(d->cderB); F(d->basey);
   F(d->Ucur); F(d->Qcur);
   for (int j = 0; j < 4; ++j) { F(d->Uh[j]); F(d->Qh[j]); F(d->Nh[j]); }
   for (int w = 0; w < 2; ++w) { F(d->fj[w]); F(d->fj1[w]); F(d->rkQ[w]); }

@@ -88,7 +88,7 @@ __device__ __forceinline__ void dft5(cpx<R>* x, int sign) {
 // stride) in place; the result is left in `a` (the routine copies back after
 // an odd number of stages).  Must be called by all threads of the block.
 template <typename R>
-__device__ void fft_batch(cpx<R>* a, cpx<R>* b, int nseq, int ss, const FftPlan& p, const cpx<R>* __restrict__ tw,
+__device__ void fft_batch_generic(cpx<R>* a, cpx<R>* b, int nseq, int ss, const FftPlan& p, const cpx<R>* __restrict__ tw,
                           int sign) {
   const int L = p.L;
   const int nthr = blockDim.x * blockDim.y * blockDim.z;
@@ -132,4 +132,91 @@ __device__ void fft_batch(cpx<R>* a, cpx<R>* b, int nseq, int ss, const FftPlan&
     for (int idx = tid; idx < total; idx += nthr) a[idx] = src[idx];
     __syncthreads();
   }
+}
+
+// ---------------------------------------------------------------------------
+// Compile-time-length variant.  The radix of each stage is chosen as the host
+// plan does (all 4s, then one 2, then 3s, then 5s), so the twiddle offsets
+// TWOFF accumulate exactly like FftPlan::twoff.
+// ---------------------------------------------------------------------------
+template <int REM>
+struct RadixOf {
+  static constexpr int v = REM % 4 == 0 ? 4 : (REM % 2 == 0 ? 2 : (REM % 3 == 0 ? 3 : 5));
+};
+
+template <typename R, int RAD>
+__device__ __forceinline__ void dft_fixed(cpx<R>* x, int sign) {
+  if constexpr (RAD == 2) dft2(x);
+  else if constexpr (RAD == 3) dft3(x, sign);
+  else if constexpr (RAD == 4) dft4(x, sign);
+  else dft5(x, sign);
+}
+
+template <typename R, int L, int Ns, int TWOFF, int PARITY>
+__device__ __forceinline__ void fft_fixed_stages(cpx<R>* src, cpx<R>* dst, cpx<R>* a, int nseq, int ss,
+                                                 const cpx<R>* __restrict__ tw, int sign, int tid, int nthr) {
+  if constexpr (Ns >= L) {
+    if constexpr (PARITY == 1) {
+      // result is in src (== b); copy back to a
+      const int total = nseq * ss;
+      for (int idx = tid; idx < total; idx += nthr) a[idx] = src[idx];
+      __syncthreads();
+    }
+  } else {
+    constexpr int RAD = RadixOf<L / Ns>::v;
+    constexpr int LR = L / RAD;
+    const int total = nseq * LR;
+    for (int idx = tid; idx < total; idx += nthr) {
+      const int qq = idx / LR;
+      const int j = idx - qq * LR;
+      const int k = j % Ns;
+      const cpx<R>* sp = src + qq * ss + j;
+      cpx<R> x[RAD];
+#pragma unroll
+      for (int r = 0; r < RAD; ++r) x[r] = sp[r * LR];
+      if constexpr (Ns > 1) {
+#pragma unroll
+        for (int r = 1; r < RAD; ++r) {
+          cpx<R> w = tw[TWOFF + k * (RAD - 1) + (r - 1)];
+          if (sign > 0) w.y = -w.y;
+          x[r] = cmul(x[r], w);
+        }
+      }
+      dft_fixed<R, RAD>(x, sign);
+      cpx<R>* dp = dst + qq * ss + (j - k) * RAD + k;
+#pragma unroll
+      for (int r = 0; r < RAD; ++r) dp[r * Ns] = x[r];
+    }
+    __syncthreads();
+    fft_fixed_stages<R, L, Ns * RAD, TWOFF + Ns * (RAD - 1), 1 - PARITY>(dst, src, a, nseq, ss, tw, sign, tid, nthr);
+  }
+}
+
+// Dispatch to a compile-time length when the plan length is one of the common grid sizes.
+template <typename R>
+__device__ void fft_batch(cpx<R>* a, cpx<R>* b, int nseq, int ss, const FftPlan& p, const cpx<R>* __restrict__ tw,
+                          int sign) {
+  const int nthr = blockDim.x * blockDim.y * blockDim.z;
+  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+#define FFT_CASE(LL)                                                              \
+  case LL:                                                                        \
+    fft_fixed_stages<R, LL, 1, 0, 0>(a, b, a, nseq, ss, tw, sign, tid, nthr);      \
+    return;
+  switch (p.L) {
+    FFT_CASE(4)
+    FFT_CASE(8)
+    FFT_CASE(12)
+    FFT_CASE(16)
+    FFT_CASE(24)
+    FFT_CASE(32)
+    FFT_CASE(48)
+    FFT_CASE(64)
+    FFT_CASE(96)
+    FFT_CASE(128)
+    FFT_CASE(192)
+    FFT_CASE(256)
+    default:
+      fft_batch_generic<R>(a, b, nseq, ss, p, tw, sign);
+  }
+#undef FFT_CASE
 }

@@ -10,6 +10,12 @@ cudaError_t launch_curl_base(const GridDev& g, const double* U, R* C6, const dou
 
 size_t cheb_smem_bytes(int N, size_t rsize);
 
+template <typename R>
+size_t curl_cheb_smem_bytes(int N);
+template <typename R>
+cudaError_t launch_curl_cheb(const GridDev& g, int N, const double* U, R* W6, const R* CA, const R* CB, const R* DA,
+                             const R* DB, const R* basey, double Vsuck, cudaStream_t st);
+
 template <typename TI, typename R, typename TO>
 cudaError_t launch_cheb(int N, bool inverse, int nlines, int ncomp, const TI* in, size_t ld_in, size_t cs_in, TO* out,
                         size_t ld_out, size_t cs_out, const R* A, const R* B, cudaStream_t st);

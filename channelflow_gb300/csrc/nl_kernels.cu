@@ -178,6 +178,165 @@ __global__ void __launch_bounds__(256) k_cheb(int N, int inverse, int nlines, co
 }
 
 // ---------------------------------------------------------------------------
+// Fused spectral curl + inverse Chebyshev transform (rotationalNL's curl and
+// makePhysical_y, diffops.cpp:2229-2334, flowfield.cpp:1939-1987).
+// For each real line (re or im part of one mode) the kernel evaluates, at the
+// Gauss-Lobatto points y_j and y_{N-1-j}:
+//   u, v, w                  from  CA (even n) / CB (odd n):  u_j = E_j + O_j, u_{N-1-j} = E_j - O_j
+//   du/dy, dw/dy             from  DA (even n) / DB (odd n) with DA[j][k] = (2/L) T'_{2k}(y_j),
+//                                  DB[j][k] = (2/L) T'_{2k+1}(y_j): d_j = DB.x_odd + DA.x_even,
+//                                  d_{N-1-j} = DB.x_odd - DA.x_even
+// adds the base flow (U, U', W, W' at y_j; -Vsuck on v) to the (0,0) mode and
+// forms omega = curl(u) pointwise in y, pairing the re/im lines of a mode
+// through a lane shuffle.  Output: W6[c][j][line], c = u, v, w, ox, oy, oz.
+// Block: 256 threads (8 warps) x 32 lines; warp w handles j = w, w+8, ...
+// ---------------------------------------------------------------------------
+#define CC_TL 32
+#define CC_PT 7
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_curl_cheb(GridDev g, int N, const double* __restrict__ U, R* __restrict__ W6,
+                                                   const R* __restrict__ CA, const R* __restrict__ CB,
+                                                   const R* __restrict__ DA, const R* __restrict__ DB,
+                                                   const R* __restrict__ basey, R Vsuck) {
+  extern __shared__ unsigned char smem_raw[];
+  const int P = (N + 1) / 2, KA = (N + 1) / 2, KB = (N - 1) / 2, J = (N - 1) / 2;
+  R* xs = reinterpret_cast<R*>(smem_raw);           // [3][N][CC_TL]: even coefs rows 0..KA-1, odd KA..N-1
+  R* sCA = xs + 3 * N * CC_TL;
+  R* sCB = sCA + P * KA;
+  R* sDA = sCB + P * KB;
+  R* sDB = sDA + P * KA;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nlines = 2 * g.Md;
+  const int l0 = blockIdx.x * CC_TL;
+  const size_t row = (size_t)nlines, comp = row * N;
+  for (int i = tid; i < P * KA; i += blockDim.x) {
+    sCA[i] = CA[i];
+    sDA[i] = DA[i];
+  }
+  for (int i = tid; i < P * KB; i += blockDim.x) {
+    sCB[i] = CB[i];
+    sDB[i] = DB[i];
+  }
+  for (int i = tid; i < 3 * N * CC_TL; i += blockDim.x) {
+    const int l = i % CC_TL, n = (i / CC_TL) % N, c = i / (CC_TL * N);
+    const int gl = l0 + l;
+    const R v = gl < nlines ? (R)U[c * comp + (size_t)n * row + gl] : (R)0;
+    const int r = (n & 1) ? KA + (n >> 1) : (n >> 1);
+    xs[(c * N + r) * CC_TL + l] = v;
+  }
+  __syncthreads();
+  R aCu[CC_PT], aCv[CC_PT], aCw[CC_PT], aDu[CC_PT], aDw[CC_PT];   // even-coefficient sums
+  R bCu[CC_PT], bCv[CC_PT], bCw[CC_PT], bDu[CC_PT], bDw[CC_PT];   // odd-coefficient sums
+#pragma unroll
+  for (int i = 0; i < CC_PT; ++i) aCu[i] = aCv[i] = aCw[i] = aDu[i] = aDw[i] = bCu[i] = bCv[i] = bCw[i] = bDu[i] = bDw[i] = 0;
+  const R* xu = xs + lane;
+  const R* xv = xs + N * CC_TL + lane;
+  const R* xw = xs + 2 * N * CC_TL + lane;
+  for (int k = 0; k < KA; ++k) {
+    const R u = xu[k * CC_TL], v = xv[k * CC_TL], w = xw[k * CC_TL];
+#pragma unroll
+    for (int i = 0; i < CC_PT; ++i) {
+      const int p = warp + 8 * i;
+      if (p < P) {
+        const R c = sCA[p * KA + k], d = sDA[p * KA + k];
+        aCu[i] += c * u; aCv[i] += c * v; aCw[i] += c * w;
+        aDu[i] += d * u; aDw[i] += d * w;
+      }
+    }
+  }
+  for (int k = 0; k < KB; ++k) {
+    const R u = xu[(KA + k) * CC_TL], v = xv[(KA + k) * CC_TL], w = xw[(KA + k) * CC_TL];
+#pragma unroll
+    for (int i = 0; i < CC_PT; ++i) {
+      const int p = warp + 8 * i;
+      if (p < P) {
+        const R c = sCB[p * KB + k], d = sDB[p * KB + k];
+        bCu[i] += c * u; bCv[i] += c * v; bCw[i] += c * w;
+        bDu[i] += d * u; bDw[i] += d * w;
+      }
+    }
+  }
+  const int gl = l0 + lane;
+  const int m = min(gl, nlines - 1) >> 1;
+  const int part = gl & 1;
+  const int kx = mode_kx(g, m), kz = mode_kz(g, m);
+  const R dx = (R)(2.0 * M_PI * kx / g.Lx * (kx == g.kxmax ? 0.0 : 1.0));
+  const R dz = (R)(2.0 * M_PI * kz / g.Lz * (kz == g.kzmax ? 0.0 : 1.0));
+  const bool base = (kx == 0 && kz == 0 && part == 0);
+#pragma unroll
+  for (int i = 0; i < CC_PT; ++i) {
+    const int p = warp + 8 * i;
+    if (p >= P) continue;  // uniform per warp
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      if (h == 1 && p >= J) continue;  // middle point written once
+      const int j = h == 0 ? p : N - 1 - p;
+      const R sg = h == 0 ? (R)1 : (R)-1;
+      R u = aCu[i] + sg * bCu[i], v = aCv[i] + sg * bCv[i], w = aCw[i] + sg * bCw[i];
+      R du = bDu[i] + sg * aDu[i], dw = bDw[i] + sg * aDw[i];
+      if (base) {
+        u += basey[j];
+        du += basey[N + j];
+        w += basey[2 * N + j];
+        dw += basey[3 * N + j];
+        v -= Vsuck;
+      }
+      const R ou = __shfl_xor_sync(0xffffffffu, u, 1);
+      const R ov = __shfl_xor_sync(0xffffffffu, v, 1);
+      const R ow = __shfl_xor_sync(0xffffffffu, w, 1);
+      R ox, oy, oz;
+      if (part == 0) {
+        ox = dw + dz * ov;
+        oy = -dz * ou + dx * ow;
+        oz = -dx * ov - du;
+      } else {
+        ox = dw - dz * ov;
+        oy = dz * ou - dx * ow;
+        oz = dx * ov - du;
+      }
+      if (gl < nlines) {
+        R* o = W6 + (size_t)j * row + gl;
+        o[0] = u;
+        o[comp] = v;
+        o[2 * comp] = w;
+        o[3 * comp] = ox;
+        o[4 * comp] = oy;
+        o[5 * comp] = oz;
+      }
+    }
+  }
+}
+
+template <typename R>
+size_t curl_cheb_smem_bytes(int N) {
+  const int P = (N + 1) / 2, KA = (N + 1) / 2, KB = (N - 1) / 2;
+  return sizeof(R) * ((size_t)3 * N * CC_TL + 2 * (size_t)P * (KA + KB));
+}
+
+template <typename R>
+cudaError_t launch_curl_cheb(const GridDev& g, int N, const double* U, R* W6, const R* CA, const R* CB, const R* DA,
+                             const R* DB, const R* basey, double Vsuck, cudaStream_t st) {
+  if ((N + 1) / 2 > 8 * CC_PT) return cudaErrorInvalidValue;
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_curl_cheb<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    attr_set = true;
+  }
+  const int nlines = 2 * g.Md;
+  k_curl_cheb<R><<<(nlines + CC_TL - 1) / CC_TL, 256, curl_cheb_smem_bytes<R>(N), st>>>(g, N, U, W6, CA, CB, DA, DB,
+                                                                                         basey, (R)Vsuck);
+  return cudaGetLastError();
+}
+template cudaError_t launch_curl_cheb<float>(const GridDev&, int, const double*, float*, const float*, const float*,
+                                             const float*, const float*, const float*, double, cudaStream_t);
+template cudaError_t launch_curl_cheb<double>(const GridDev&, int, const double*, double*, const double*,
+                                              const double*, const double*, const double*, const double*, double,
+                                              cudaStream_t);
+template size_t curl_cheb_smem_bytes<float>(int);
+template size_t curl_cheb_smem_bytes<double>(int);
+
+// ---------------------------------------------------------------------------
 // x-direction inverse FFT of the solved (kx, kz) block of one y-plane and
 // component: column kz of the compact input is placed at x-wavenumber
 // positions (kx >= 0 -> kx, kx < 0 -> Nx + kx), zero elsewhere, and

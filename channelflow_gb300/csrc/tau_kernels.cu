@@ -235,195 +235,341 @@ cudaError_t launch_tau_setup(const GridDev& g, int N, double lambda_t, double nu
 }
 
 // ---------------------------------------------------------------------------
-// Step solve: thread (m, part) with part 0 = real, 1 = imaginary.  Builds the
-// scheme's right-hand side, solves the tau problem, writes u and q.
+// Step solve.  Four threads per mode: (part, q) = (real/imaginary part,
+// Chebyshev parity).  Even and odd Chebyshev coefficients decouple in every
+// Helmholtz solve (helmholtz.cpp:79-95: Ae/Ao, Be/Bo), so thread q owns the
+// coefficients n = 2i + q of every line.  Derivative recurrences read the
+// other parity (written by the neighbour lane before a group barrier);
+// boundary sums are combined with a shuffle.  Lines live in global memory in
+// the [n][2*Md] layout; every loop prefetches a chunk of independent loads
+// before the dependent arithmetic so no load sits on a recurrence chain.
 // ---------------------------------------------------------------------------
+#define TCH 4
+
+// parity-local line: element i <-> Chebyshev index n = 2i + q
+struct PLn {
+  double* p;
+  int s;  // elements between i and i+1 (= 2 * full-line stride)
+  __device__ __forceinline__ double& operator[](int i) const { return p[(size_t)i * s]; }
+};
+
+// u = A^{-1} B f for one parity system of M rows (row 0 of the system carries the boundary value bc).
+// Descending pass: B-multiply on the fly, back-substitution, row-0 accumulation; ascending pass: L solve.
+__device__ void helm_par(int M, int q, const double* __restrict__ hlo, const double* __restrict__ hdi,
+                         const double* __restrict__ hup, PLn band, PLn up, PLn lo, PLn inv, PLn f, PLn u,
+                         double bc) {
+  const int nM = 2 * (M - 1) + q;
+  double fi = f[M - 1], fm = f[M - 2];
+  double unext = __ldg(hlo + nM) * fm + __ldg(hdi + nM) * fi;
+  u[M - 1] = unext;
+  double acc = bc - band[M - 1] * unext;
+  double fi1 = fi;
+  fi = fm;
+  for (int i = M - 2; i >= 1; i -= TCH) {
+    double fp[TCH], upv[TCH], bv[TCH];
+#pragma unroll
+    for (int k = 0; k < TCH; ++k)
+      if (i - k >= 1) {
+        fp[k] = f[i - k - 1];
+        upv[k] = up[i - k];
+        bv[k] = band[i - k];
+      }
+#pragma unroll
+    for (int k = 0; k < TCH; ++k)
+      if (i - k >= 1) {
+        const int n = 2 * (i - k) + q;
+        const double bf = (__ldg(hlo + n) * fp[k] + __ldg(hdi + n) * fi) + __ldg(hup + n) * fi1;
+        const double ui = bf - upv[k] * unext;
+        u[i - k] = ui;
+        unext = ui;
+        acc -= bv[k] * ui;
+        fi1 = fi;
+        fi = fp[k];
+      }
+  }
+  double prev = acc / band[0];
+  u[0] = prev;
+  for (int i = 1; i < M; i += TCH) {
+    double uv[TCH], lv[TCH], iv[TCH];
+#pragma unroll
+    for (int k = 0; k < TCH; ++k)
+      if (i + k < M) {
+        uv[k] = u[i + k];
+        lv[k] = lo[i + k];
+        iv[k] = inv[i + k];
+      }
+#pragma unroll
+    for (int k = 0; k < TCH; ++k)
+      if (i + k < M) {
+        prev = (uv[k] - lv[k] * prev) * iv[k];
+        u[i + k] = prev;
+      }
+  }
+}
+
+// Parity q of d = diff(x) (chebyshev.cpp:672-697): d[n] = d[n+2] + (scale (n+1)) x[n+1], descending,
+// d[0] *= 1/2.  xo is the other parity of x.  Optionally stores d (dst) and returns the partial sum of
+// d over this parity (for boundary values).
+__device__ double diff_par(int M, int q, int N, double scale, PLn xo, PLn* dst) {
+  double dn2 = 0.0, sum = 0.0;
+  int i = M - 1;
+  if (q == 0) {
+    // top even index n = N-1: x[N] = 0
+    const double v = dn2 + (scale * N) * 0.0;
+    if (dst) (*dst)[i] = v;
+    sum += v;
+    dn2 = v;
+    i--;
+  }
+  for (; i >= 0; i -= TCH) {
+    double xv[TCH];
+#pragma unroll
+    for (int k = 0; k < TCH; ++k)
+      if (i - k >= 0) xv[k] = xo[i - k + q];
+#pragma unroll
+    for (int k = 0; k < TCH; ++k)
+      if (i - k >= 0) {
+        const int n = 2 * (i - k) + q;
+        double v = dn2 + (scale * (n + 1)) * xv[k];
+        dn2 = v;
+        if (n == 0) v *= 0.5;
+        if (dst) (*dst)[i - k] = v;
+        sum += v;
+      }
+  }
+  return sum;
+}
+
 template <typename R>
 __global__ void __launch_bounds__(128) k_tau_solve(GridDev g, int N, SolveParams sp, SolvePtrs P, HelmB hb,
                                                    TauTable tt) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int Md = g.Md;
-  const bool active = t < 2 * Md;
-  const int m = active ? t >> 1 : 0;
-  const int part = t & 1;
-  const size_t row = 2 * (size_t)Md;       // state / scratch row stride
-  const size_t comp = row * N;              // component stride
-  const size_t off = 2 * (size_t)m + part;  // my element in a row
-  const size_t poff = 2 * (size_t)m + (1 - part);
+  const bool act = (t >> 2) < Md;
+  const int m = act ? (t >> 2) : Md - 1;
+  const int part = (t >> 1) & 1, q = t & 1;
+  const int lane = threadIdx.x & 31;
+  const unsigned gmask = 0xFu << (lane & 28);
+  const int row = 2 * Md;
+  const size_t comp = (size_t)row * N;
+  const int off = 2 * m + part, poff = 2 * m + (1 - part);
   const size_t FN = (size_t)N * Md;
-  auto T = [&](int f) { return Ln{tt.f + f * FN + m, (size_t)Md}; };
-  auto SC = [&](int k) { return Ln{P.scratch + k * comp + off, row}; };
-  auto SCp = [&](int k) { return Ln{P.scratch + k * comp + poff, row}; };
+  const int M = q ? (N - 1) / 2 : (N - 1) / 2 + 1;
+  const int Nb = N - 1;
+  // full-line base (n = 0) of component/array at my element; parity views
+  auto mine = [&](double* base) { return PLn{base + off + q * row, 2 * row}; };
+  auto other = [&](double* base) { return PLn{base + off + (1 - q) * row, 2 * row}; };
+  auto ppart = [&](double* base) { return PLn{base + poff + q * row, 2 * row}; };
+  auto TB = [&](int f) { return PLn{tt.f + f * FN + m + q * Md, 2 * Md}; };
+  double* SC[6];
+  for (int k = 0; k < 6; ++k) SC[k] = P.scratch + k * comp;
   const int kx = mode_kx(g, m), kz = mode_kz(g, m);
   const bool m00 = (kx == 0 && kz == 0);
   const double kxL = 2 * M_PI * kx / g.Lx;
   const double kzL = 2 * M_PI * kz / g.Lz;
   const double scale = 4.0 / (g.b - g.a);
   const double nu = sp.nu;
-  const int Nb = N - 1;
   const double lambda = tt.s[TS_LAMBDA * Md + m];
-  HelmFac PH{T(TF_PBAND), T(TF_PUP), T(TF_PLO), T(TF_PINV)};
-  HelmFac VH{T(TF_VBAND), T(TF_VUP), T(TF_VLO), T(TF_VINV)};
-  Ln Rx = SC(0), Ry = SC(1), Rz = SC(2);
+  const double* __restrict__ hlo = hb.lo;
+  const double* __restrict__ hdi = hb.di;
+  const double* __restrict__ hup = hb.up;
 
-  // ---- A: right-hand side (my part) --------------------------------------
-  if (active) {
-    if (sp.kind == 0) {
-      for (int n = 0; n < N; ++n) {
-        const size_t o = n * row + off;
-        for (int c = 0; c < 3; ++c) {
-          double acc = 0.0;
-          for (int j = 0; j < sp.order; ++j) {
-            const double uj = P.uin[j][c * comp + o];
-            const double Nj = (double)static_cast<const R*>(P.nin[j])[c * comp + o];
-            acc += sp.a[j] * uj + sp.b[j] * Nj;
-          }
-          SC(c)[n] = acc;
-        }
-      }
-    } else {
-      // linear term L = nu u'' - kappa^2 nu u - grad q  (NSE::linear)
-      const double kappa2 = 4 * M_PI * M_PI * ((kx / g.Lx) * (kx / g.Lx) + (kz / g.Lz) * (kz / g.Lz));
-      const double Dx = 2 * M_PI * kx / g.Lx * (kx == g.kxmax ? 0.0 : 1.0);
-      const double Dz = 2 * M_PI * kz / g.Lz * (kz == g.kzmax ? 0.0 : 1.0);
-      Ln uk = SC(3), d1 = SC(4), d2 = SC(5);
-      Ln qm{const_cast<double*>(P.qin) + off, row};
-      Ln qp{const_cast<double*>(P.qin) + poff, row};
+  // ---- A: right-hand side (my part, my parity) ----------------------------
+  if (sp.kind == 0) {
+    for (int i = 0; i < M; ++i) {
+      const size_t o = (size_t)(2 * i + q) * row + off;
       for (int c = 0; c < 3; ++c) {
-        Ln uc{const_cast<double*>(P.uin[0]) + c * comp + off, row};
-        for (int n = 0; n < N; ++n) uk[n] = nu * uc[n];
-        cheb_diff(N, scale, uk, d1);
-        cheb_diff(N, scale, d1, d2);
-        double wall = 0.0;
-        if (m00 && part == 0 && sp.constraint == 1 && c != 1) {
-          // actual dPdx from wall shear of nu*u (nse.cpp:452-466), first term
-          const double Ly = g.b - g.a;
-          wall = (eval_b(N, d1) - eval_a(N, d1)) / Ly;
+        double acc = 0.0;
+        for (int j = 0; j < sp.order; ++j)
+          acc += sp.a[j] * P.uin[j][c * comp + o] + sp.b[j] * (double)static_cast<const R*>(P.nin[j])[c * comp + o];
+        if (m00 && part == 0 && c != 1) {
+          acc += nu * (c == 0 ? P.Ubaseyy[2 * i + q] : P.Wbaseyy[2 * i + q]);
+          if (2 * i + q == 0 && sp.constraint == 0) acc -= (c == 0 ? sp.dPdxRef : sp.dPdzRef);
         }
-        if (c == 1) cheb_diff(N, scale, qm, d1);  // q' for the y component
-        for (int n = 0; n < N; ++n) {
-          double gq;
-          if (c == 0) gq = part == 0 ? -(Dx * qp[n]) : Dx * qp[n];
-          else if (c == 2) gq = part == 0 ? -(Dz * qp[n]) : Dz * qp[n];
-          else gq = d1[n];
-          double L = d2[n] - kappa2 * uk[n] - gq;
-          if (m00 && part == 0 && c != 1) {
-            L += nu * (c == 0 ? P.Ubaseyy[n] : P.Wbaseyy[n]);
-            if (n == 0) {
-              if (sp.constraint == 0) L -= (c == 0 ? sp.dPdxRef : sp.dPdzRef);
-              else L -= wall + sp.baseShear[c == 0 ? 0 : 1];
-            }
-          }
-          const double u0 = uc[n];
-          double Nj = (double)static_cast<const R*>(P.nin[0])[c * comp + n * row + off];
-          double rhs;
-          if (sp.kind == 1) {
-            const double Nj1 = (double)static_cast<const R*>(P.nin[1])[c * comp + n * row + off];
-            rhs = (u0 * sp.lam + sp.a_b * L) + ((-sp.g_b) * Nj + (-sp.z_b) * Nj1);
-          } else {
-            R* Q = static_cast<R*>(P.Q) + c * comp + n * row + off;
-            const double Qn = (double)(*Q) * sp.rkA - Nj;
-            *Q = (R)Qn;
-            rhs = L + (sp.lam * u0 + sp.B_C * Qn);
-          }
-          SC(c)[n] = rhs;
-        }
+        if (act) SC[c][o] = acc;
       }
     }
-    if (m00 && part == 0) {
-      // (0,0): NSE::solve adds nu Ubase'' (and the pressure gradient) to the RHS
-      for (int n = 0; n < N; ++n) {
-        Rx[n] += nu * P.Ubaseyy[n];
-        Rz[n] += nu * P.Wbaseyy[n];
+  } else {
+    const double kappa2 = 4 * M_PI * M_PI * ((kx / g.Lx) * (kx / g.Lx) + (kz / g.Lz) * (kz / g.Lz));
+    const double Dx = 2 * M_PI * kx / g.Lx * (kx == g.kxmax ? 0.0 : 1.0);
+    const double Dz = 2 * M_PI * kz / g.Lz * (kz == g.kzmax ? 0.0 : 1.0);
+    double* uin0 = const_cast<double*>(P.uin[0]);
+    double* qin = const_cast<double*>(P.qin);
+    for (int c = 0; c < 3; ++c) {
+      __syncwarp(gmask);
+      PLn uc = mine(uin0 + c * comp);
+      PLn uk = mine(SC[3]);
+      for (int i = 0; i < M; ++i)
+        if (act) uk[i] = nu * uc[i];
+      __syncwarp(gmask);
+      PLn d1 = mine(SC[4]);
+      const double s = diff_par(M, q, N, scale, other(SC[3]), act ? &d1 : nullptr);
+      const double so = __shfl_xor_sync(gmask, s, 1);
+      double wall = 0.0;
+      if (m00 && part == 0 && sp.constraint == 1 && c != 1) {
+        // actual dPdx from the wall shear of nu*u (nse.cpp:452-466): (eval_b - eval_a)/Ly
+        const double s0 = q == 0 ? s : so, s1 = q == 0 ? so : s;
+        wall = ((s0 + s1) - (s0 - s1)) / (g.b - g.a);
       }
-      if (sp.constraint == 0) {
-        Rx[0] -= sp.dPdxRef;
-        Rz[0] -= sp.dPdzRef;
+      __syncwarp(gmask);
+      // descending: d2 = D(d1), dq = D(q) (c == 1), L and the scheme's rhs
+      PLn d1o = other(SC[4]);
+      PLn qo = other(qin);
+      PLn qp = ppart(qin);
+      PLn out = mine(SC[c]);
+      const R* Nj = static_cast<const R*>(P.nin[0]) + c * comp + off + q * row;
+      const R* Nj1 = sp.kind == 1 ? static_cast<const R*>(P.nin[1]) + c * comp + off + q * row : nullptr;
+      R* Q = sp.kind == 2 ? static_cast<R*>(P.Q) + c * comp + off + q * row : nullptr;
+      double d2n2 = 0.0, dqn2 = 0.0;
+      for (int i = M - 1; i >= 0; --i) {
+        const int n = 2 * i + q;
+        const double x1 = (n + 1 <= Nb) ? d1o[i + q] : 0.0;
+        double d2 = d2n2 + (scale * (n + 1)) * x1;
+        d2n2 = d2;
+        if (n == 0) d2 *= 0.5;
+        double gq;
+        if (c == 1) {
+          const double y1 = (n + 1 <= Nb) ? qo[i + q] : 0.0;
+          double dq = dqn2 + (scale * (n + 1)) * y1;
+          dqn2 = dq;
+          if (n == 0) dq *= 0.5;
+          gq = dq;
+        } else {
+          const double kD = c == 0 ? Dx : Dz;
+          gq = part == 0 ? -(kD * qp[i]) : kD * qp[i];
+        }
+        double L = d2 - kappa2 * uk[i] - gq;
+        if (m00 && part == 0 && c != 1) {
+          L += nu * (c == 0 ? P.Ubaseyy[n] : P.Wbaseyy[n]);
+          if (n == 0) L -= sp.constraint == 0 ? (c == 0 ? sp.dPdxRef : sp.dPdzRef)
+                                              : wall + sp.baseShear[c == 0 ? 0 : 1];
+        }
+        const double u0 = uc[i];
+        const double nj = (double)Nj[(size_t)i * 2 * row];
+        double rhs;
+        if (sp.kind == 1) {
+          const double nj1 = (double)Nj1[(size_t)i * 2 * row];
+          rhs = (u0 * sp.lam + sp.a_b * L) + ((-sp.g_b) * nj + (-sp.z_b) * nj1);
+        } else {
+          const double Qn = (double)Q[(size_t)i * 2 * row] * sp.rkA - nj;
+          if (act) Q[(size_t)i * 2 * row] = (R)Qn;
+          rhs = L + (sp.lam * u0 + sp.B_C * Qn);
+        }
+        if (m00 && part == 0 && c != 1) {
+          rhs += nu * (c == 0 ? P.Ubaseyy[n] : P.Wbaseyy[n]);
+          if (n == 0 && sp.constraint == 0) rhs -= (c == 0 ? sp.dPdxRef : sp.dPdzRef);
+        }
+        if (act) out[i] = rhs;
       }
     }
   }
-  __syncwarp();
-  // ---- B/C: pressure and wall-normal velocity (solve_P_and_v) -----------
-  Ln rr = SC(3), t1 = SC(4), t2 = SC(5);
-  Ln Pl{P.qout + off, row};
-  Ln Vl{P.uout + comp + off, row};
-  if (active) {
-    cheb_diff(N, scale, Ry, rr);
-    Ln Rxp = SCp(0), Rzp = SCp(2);
-    for (int n = 0; n < N; ++n) {
-      if (part == 0) rr[n] = rr[n] - (kxL * Rxp[n] + kzL * Rzp[n]);
-      else rr[n] = rr[n] + (kxL * Rxp[n] + kzL * Rzp[n]);
-    }
-    helm_solve(PH, hb, N, rr, Pl, 0.0, 0.0);
-    if (m00) {
-      for (int n = 0; n < N; ++n) Vl[n] = 0.0;
-    } else {
-      cheb_diff(N, scale, Pl, t1);
-      for (int n = 0; n < N; ++n) t1[n] -= Ry[n];
-      helm_solve(VH, hb, N, t1, Vl, 0.0, 0.0);
-      // influence correction
-      cheb_diff(N, scale, Vl, t2);
-      const double plus = eval_b(N, t2), minus = eval_a(N, t2);
-      const double* s = tt.s + m;
-      const double i00 = s[TS_I00 * Md], i01 = s[TS_I01 * Md], i10 = s[TS_I10 * Md], i11 = s[TS_I11 * Md];
-      const double dp = -i00 * plus - i01 * minus;
-      const double dm = -i10 * plus - i11 * minus;
-      Ln Pp = T(TF_PP), Vp = T(TF_VP), Pm = T(TF_PM), Vm = T(TF_VM);
-      for (int n = 0; n < N; ++n) {
-        Pl[n] += dp * Pp[n] + dm * Pm[n];
-        Vl[n] += dp * Vp[n] + dm * Vm[n];
-      }
-      if (sp.taucorrection) {
-        // nu v''[Nb], nu v''[Nb-1] and P'[Nb] vanish identically; P'[Nb-1] = scale*Nb*P[Nb]
-        double s1Nb = lambda * Vl[Nb] - nu * 0.0 - Ry[Nb];
-        double s1Nb1 = lambda * Vl[Nb - 1] - nu * 0.0 - Ry[Nb - 1];
-        s1Nb += 0.0;
-        s1Nb1 += (scale * Nb) * Pl[Nb];
-        const double sNb = s1Nb / (1.0 - s[TS_S0NB * Md]);
-        const double sNb1 = s1Nb1 / (1.0 - s[TS_S0NB1 * Md]);
-        Ln P0 = T(TF_P0), V0 = T(TF_V0);
-        for (int n = 0; n <= Nb; ++n) {
-          Pl[n] += ((n % 2 == 0) ? sNb1 : sNb) * P0[n];
-          Vl[n] += ((n % 2 == 0) ? sNb : sNb1) * V0[n];
-        }
-      }
+  __syncwarp(gmask);
+
+  // ---- B/C: pressure and wall-normal velocity (solve_P_and_v) ------------
+  PLn Ry = mine(SC[1]);
+  PLn rr = mine(SC[3]);
+  {
+    // rr = D(Ry) -/+ (kx Rx' + kz Rz') with ' the other part
+    PLn Rxp = ppart(SC[0]), Rzp = ppart(SC[2]);
+    PLn* dst = act ? &rr : nullptr;
+    diff_par(M, q, N, scale, other(SC[1]), dst);
+    for (int i = 0; i < M; ++i) {
+      const double x = kxL * Rxp[i] + kzL * Rzp[i];
+      if (act) rr[i] = part == 0 ? rr[i] - x : rr[i] + x;
     }
   }
-  __syncwarp();
+  PLn Pl = mine(P.qout);
+  PLn Vl = mine(P.uout + comp);
+  PLn PH_band = TB(TF_PBAND), PH_up = TB(TF_PUP), PH_lo = TB(TF_PLO), PH_inv = TB(TF_PINV);
+  PLn VH_band = TB(TF_VBAND), VH_up = TB(TF_VUP), VH_lo = TB(TF_VLO), VH_inv = TB(TF_VINV);
+  // dummy sink for inactive lanes (never stored)
+  if (act) helm_par(M, q, hlo, hdi, hup, PH_band, PH_up, PH_lo, PH_inv, rr, Pl, 0.0);
+  __syncwarp(gmask);
+  if (m00) {
+    if (act)
+      for (int i = 0; i < M; ++i) Vl[i] = 0.0;
+  } else {
+    PLn tmp = mine(SC[4]);
+    diff_par(M, q, N, scale, other(P.qout), act ? &tmp : nullptr);
+    if (act) {
+      for (int i = 0; i < M; ++i) tmp[i] -= Ry[i];
+      helm_par(M, q, hlo, hdi, hup, VH_band, VH_up, VH_lo, VH_inv, tmp, Vl, 0.0);
+    }
+  }
+  __syncwarp(gmask);
+  {
+    // influence correction (tausolver.cpp:178-191) and tau correction (tausolver.cpp:221-247)
+    const double s = m00 ? 0.0 : diff_par(M, q, N, scale, other(P.uout + comp), nullptr);
+    const double so = __shfl_xor_sync(gmask, s, 1);
+    const double s0 = q == 0 ? s : so, s1 = q == 0 ? so : s;
+    const double plus = s0 + s1, minus = s0 - s1;
+    const double* sc = tt.s + m;
+    const double i00 = sc[TS_I00 * Md], i01 = sc[TS_I01 * Md], i10 = sc[TS_I10 * Md], i11 = sc[TS_I11 * Md];
+    const double dp = -i00 * plus - i01 * minus;
+    const double dm = -i10 * plus - i11 * minus;
+    PLn Pp = TB(TF_PP), Vp = TB(TF_VP), Pm = TB(TF_PM), Vm = TB(TF_VM);
+    if (!m00 && act)
+      for (int i = 0; i < M; ++i) {
+        Pl[i] += dp * Pp[i] + dm * Pm[i];
+        Vl[i] += dp * Vp[i] + dm * Vm[i];
+      }
+    // Nb = N-1 is even (q = 0 holds v[Nb], P[Nb]); Nb-1 is odd (q = 1)
+    const int itop = M - 1;
+    double x0 = 0.0, y0 = 0.0;
+    if (!m00) {
+      x0 = lambda * Vl[itop] - nu * 0.0 - Ry[itop];
+      y0 = q == 0 ? (scale * Nb) * Pl[itop] : 0.0;
+    }
+    const double ox = __shfl_xor_sync(gmask, x0, 1);
+    const double oy = __shfl_xor_sync(gmask, y0, 1);
+    if (!m00 && sp.taucorrection) {
+      const double s1Nb = (q == 0 ? x0 : ox) + 0.0;
+      const double s1Nb1 = q == 0 ? ox + y0 : x0 + oy;
+      const double sNb = s1Nb / (1.0 - sc[TS_S0NB * Md]);
+      const double sNb1 = s1Nb1 / (1.0 - sc[TS_S0NB1 * Md]);
+      PLn P0 = TB(TF_P0), V0 = TB(TF_V0);
+      const double fP = q == 0 ? sNb1 : sNb, fV = q == 0 ? sNb : sNb1;
+      if (act)
+        for (int i = 0; i < M; ++i) {
+          Pl[i] += fP * P0[i];
+          Vl[i] += fV * V0[i];
+        }
+    }
+  }
+  __syncwarp(gmask);
+
   // ---- D: streamwise and spanwise velocity -------------------------------
-  if (active) {
-    Ln Pp{P.qout + poff, row};  // partner's pressure part
-    Ln Ul{P.uout + off, row};
-    Ln Wl{P.uout + 2 * comp + off, row};
-    for (int c = 0; c < 2; ++c) {
-      const double kL = c == 0 ? kxL : kzL;
-      Ln Rc = c == 0 ? Rx : Rz;
-      Ln out = c == 0 ? Ul : Wl;
-      for (int n = 0; n < N; ++n) rr[n] = part == 0 ? -(kL * Pp[n]) - Rc[n] : kL * Pp[n] - Rc[n];
-      if (m00 && part == 0 && sp.constraint == 1) {
-        // mean-constrained solve (helmholtz.cpp:158-213): returns mu = dPdx
-        helm_solve(VH, hb, N, rr, out, 0.0, 0.0);
-        const double amean = cheb_mean(N, out);
-        const double ucmean = tt.s[TS_UCMEAN * Md + m];
-        const double target = c == 0 ? sp.umean : sp.wmean;
-        const double mu = nu * (target - amean) / ucmean;
-        rr[0] = rr[0] + mu;
-        helm_solve(VH, hb, N, rr, out, 0.0, 0.0);
+  PLn Ppt = ppart(P.qout);
+  for (int c = 0; c < 2; ++c) {
+    const double kL = c == 0 ? kxL : kzL;
+    PLn Rc = mine(SC[c == 0 ? 0 : 2]);
+    PLn out = mine(P.uout + (c == 0 ? 0 : 2) * comp);
+    PLn r = mine(SC[3]);
+    if (act) {
+      for (int i = 0; i < M; ++i) r[i] = part == 0 ? -(kL * Ppt[i]) - Rc[i] : kL * Ppt[i] - Rc[i];
+      helm_par(M, q, hlo, hdi, hup, VH_band, VH_up, VH_lo, VH_inv, r, out, 0.0);
+    }
+    if (m00 && sp.constraint == 1) {
+      // mean-constrained solve of the real part (helmholtz.cpp:158-213); the mean involves even n only
+      double amean = 0.0;
+      if (q == 0) {
+        amean = out[0];
+        for (int i = 1; i < M; ++i) amean -= out[i] / (double)((2 * i) * (2 * i) - 1);
+      }
+      const double ucmean = tt.s[TS_UCMEAN * Md + m];
+      const double target = c == 0 ? sp.umean : sp.wmean;
+      const double mu = nu * (target - amean) / ucmean;
+      if (part == 0 && q == 0 && act) {
+        r[0] = r[0] + mu;
+        helm_par(M, q, hlo, hdi, hup, VH_band, VH_up, VH_lo, VH_inv, r, out, 0.0);
         if (P.dPdx_out) P.dPdx_out[c] = mu;
-      } else {
-        helm_solve(VH, hb, N, rr, out, 0.0, 0.0);
       }
     }
   }
-  __syncwarp();
-  if (active && m00 && part == 1 && sp.force_real00) {
-    // (0,0) must be real (nse.cpp:555-564)
-    for (int n = 0; n < N; ++n) {
-      P.uout[n * row + off] = 0.0;
-      P.uout[comp + n * row + off] = 0.0;
-      P.uout[2 * comp + n * row + off] = 0.0;
-      P.qout[n * row + off] = 0.0;
-    }
+  __syncwarp(gmask);
+  if (act && m00 && part == 1 && sp.force_real00) {
+    PLn u0 = mine(P.uout), v0 = mine(P.uout + comp), w0 = mine(P.uout + 2 * comp), p0 = mine(P.qout);
+    for (int i = 0; i < M; ++i) u0[i] = v0[i] = w0[i] = p0[i] = 0.0;
   }
 }
 
@@ -431,7 +577,7 @@ template <typename R>
 cudaError_t launch_tau_solve(const GridDev& g, int N, const SolveParams& sp, const SolvePtrs& p, const HelmB& hb,
                              TauTable tt, cudaStream_t st) {
   const int T = 64;
-  k_tau_solve<R><<<(2 * g.Md + T - 1) / T, T, 0, st>>>(g, N, sp, p, hb, tt);
+  k_tau_solve<R><<<(4 * g.Md + T - 1) / T, T, 0, st>>>(g, N, sp, p, hb, tt);
   return cudaGetLastError();
 }
 
