@@ -60,6 +60,8 @@ _SIGS = {
     "cfgpu_dns_phase_times": [C.c_void_p, _PD, C.POINTER(C.c_longlong), _PD, C.POINTER(C.c_longlong)],
     "cfgpu_tau_solve_batched": [C.c_int, C.c_int, _PI, _PI, C.c_double, C.c_double, C.c_double, C.c_double,
                                 C.c_double, C.c_double, C.c_int, _PD, _PD, _PD, _PD, _PD, _PD, _PD],
+    "cfgpu_tau_solve_batched_noalloc": [C.c_int, C.c_int, _PI, _PI, C.c_double, C.c_double, C.c_double, C.c_double,
+                                        C.c_double, C.c_double, C.c_int, _PD, _PD, _PD, _PD, _PD, _PD, _PD],
 }
 
 

@@ -274,6 +274,8 @@ int dalloc(T** p, size_t n, long long& bytes) {
 
 }  // namespace
 
+int cfgpu_record_error(int code, const std::string& msg) { return fail(code, msg); }
+
 // ---------------------------------------------------------------------------
 // The DNS object
 // ---------------------------------------------------------------------------

@@ -2,7 +2,12 @@
 // the host runtime (not part of the public C ABI).
 #pragma once
 
+#include <string>
+
 #include "fft.cuh"
+
+// Records the message returned by cfgpu_last_error() on this thread; returns code.
+int cfgpu_record_error(int code, const std::string& msg);
 
 template <typename R>
 cudaError_t launch_curl_base(const GridDev& g, const double* U, R* C6, const double* Ub, const double* Wb, double Vsuck,

@@ -146,6 +146,33 @@ cfgpu_status cfgpu_tau_solve_batched(int N, int nmodes, const int* kx, const int
                                      double b, double lambda_t, double nu, int taucorrection, const double* Rx,
                                      const double* Ry, const double* Rz, double* u, double* v, double* w, double* P);
 
+/*
+ * Batched tau solve that allocates nothing (no counterpart in the reference:
+ * channelflow solves per mode on the CPU and never touches GPU memory).
+ *
+ * Same arguments, host buffers and results as cfgpu_tau_solve_batched, but
+ * it calls no cudaMalloc/cudaFree: all device working memory comes from one
+ * static array of CFGPU_NOALLOC_BYTES (16 MiB) that every GPU loading this
+ * library holds until the process exits.  It is for callers that must not
+ * allocate GPU memory: processes whose GPU memory is fully reserved by
+ * another allocator (a framework's pool, a fixed budget on a shared GPU),
+ * and latency-sensitive loops that cannot pay for allocation.
+ *
+ * Limit: 54*N*nmodes + 9*nmodes + 4*N doubles must fit in the array, e.g.
+ * N = 49 allows nmodes <= 789, N = 97 allows nmodes <= 399; larger requests
+ * return CFGPU_EINVAL with the sizes in cfgpu_last_error().
+ * The first call on a device (with that device current) looks up the array's
+ * device address; make that first call before any stream capture.  Every
+ * call on a device reuses the same array, and calls run on the legacy
+ * default stream: calls that overlap on the GPU (from several host threads)
+ * race on it.
+ */
+#define CFGPU_NOALLOC_BYTES (16u << 20)
+cfgpu_status cfgpu_tau_solve_batched_noalloc(int N, int nmodes, const int* kx, const int* kz, double Lx, double Lz,
+                                             double a, double b, double lambda_t, double nu, int taucorrection,
+                                             const double* Rx, const double* Ry, const double* Rz, double* u,
+                                             double* v, double* w, double* P);
+
 /* Library version string. */
 const char* cfgpu_version(void);
 

@@ -1,0 +1,60 @@
+"""The allocation-free batched tau solve agrees with the allocating one.
+
+cfgpu_tau_solve_batched_noalloc serves callers that must not allocate GPU
+memory (their GPU memory is fully reserved by another allocator, or they run
+latency-sensitive loops): it takes all device working memory from a static
+16 MiB array inside the library.  This file is collected last on purpose.
+"""
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from channelflow_gb300 import _lib as L
+from tests.test_oracle_golden import tau_case
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12  # same tolerance as the batched tau parity test
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from channelflow_gb300 import build
+    build.build()
+    return L.load()
+
+
+def _solve(lib, fn, N, kx, kz, c, R):
+    outs = [np.zeros((kx.shape[0], N), dtype=np.complex128) for _ in range(4)]
+    L.check(getattr(lib, fn)(int(N), int(kx.shape[0]), L.iptr(kx), L.iptr(kz), c["Lx"], c["Lz"], c["a"], c["b"],
+                             c["lam_t"], c["nu"], 1, *[L.dptr(r) for r in R], *[L.dptr(o) for o in outs]))
+    return outs
+
+
+def test_noalloc_matches_allocating_entry_point_twice(lib):
+    rng = np.random.default_rng(99)
+    for call in range(2):
+        c = tau_case(rng)
+        N = c["N"]
+        nm = 40 + 17 * call
+        kx = rng.integers(-20, 21, nm).astype(np.int32)
+        kz = rng.integers(0, 21, nm).astype(np.int32)
+        kx[0], kz[0] = 0, 0
+        R = [np.ascontiguousarray(np.stack([c[k] * (1 + 0.1 * j) for j in range(nm)])) for k in ("Rx", "Ry", "Rz")]
+        ref = _solve(lib, "cfgpu_tau_solve_batched", N, kx, kz, c, R)
+        got = _solve(lib, "cfgpu_tau_solve_batched_noalloc", N, kx, kz, c, R)
+        for a, b in zip(got, ref):
+            assert np.abs(a - b).max() <= TOL * max(1.0, np.abs(b).max())
+
+
+def test_noalloc_rejects_oversize_request(lib):
+    N, nm = 97, 400
+    kx = np.zeros(nm, np.int32)
+    kz = np.zeros(nm, np.int32)
+    R = [np.zeros((nm, N), np.complex128) for _ in range(3)]
+    outs = [np.zeros((nm, N), np.complex128) for _ in range(4)]
+    code = lib.cfgpu_tau_solve_batched_noalloc(N, nm, L.iptr(kx), L.iptr(kz), 1.0, 1.0, -1.0, 1.0, 1.0, 1e-3, 1,
+                                               *[L.dptr(r) for r in R], *[L.dptr(o) for o in outs])
+    assert code == L.CFGPU_EINVAL
+    assert b"static working array" in lib.cfgpu_last_error()
