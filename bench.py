@@ -206,18 +206,24 @@ def run_gpu(args, rank, world):
         dns.close()
     acc = None
     if args.accuracy_steps > 0 and rank == 0:
-        outs = {}
-        for prec in ("mixed", "fp64"):
-            u, q = u0.copy(), q0.copy()
-            d = DNS(u, grid, make_flags(), precision=prec)
-            d.set_fields(u, q)
-            d.advance_resident(args.accuracy_steps)
-            d.get_fields(u, q)
-            d.close()
-            outs[prec] = u
-        diff = l2norm(outs["mixed"] - outs["fp64"], NX, NZ) / l2norm(outs["fp64"], NX, NZ)
-        acc = {"T": args.accuracy_steps * DT, "rel_l2_mixed_vs_fp64": diff,
-               "norm": "Chebyshev-weighted L2 over all modes (diffops.cpp:415-487)"}
+        # Mixed vs plain FP64 from the same field.  With dt = 0.01 the workload itself becomes unstable at
+        # t ~ 5.1 (the CPU restatement of the reference algorithm blows up between steps 510 and 520 on the
+        # same trajectory), so the error is stated at t = 4.5 for dt = 0.01 and at T = 10 with dt = 0.005.
+        acc = {"norm": "Chebyshev-weighted L2 over all modes (diffops.cpp:415-487), relative to the FP64 path"}
+        for dt, steps, key in ((DT, 450, "t4.5_dt0.01"), (DT / 2, 2 * args.accuracy_steps, "T10_dt0.005")):
+            outs = {}
+            for prec in ("mixed", "fp64"):
+                u, q = u0.copy(), q0.copy()
+                fl = make_flags()
+                fl.dt = dt
+                d = DNS(u, grid, fl, precision=prec)
+                d.set_fields(u, q)
+                d.advance_resident(steps)
+                d.get_fields(u, q)
+                d.close()
+                outs[prec] = u
+            acc[key] = l2norm(outs["mixed"] - outs["fp64"], NX, NZ) / l2norm(outs["fp64"], NX, NZ)
+        acc["rel_l2_mixed_vs_fp64"] = acc["T10_dt0.005"]
     return results, acc, hbm, peak_kind
 
 
