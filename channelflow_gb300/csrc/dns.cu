@@ -197,6 +197,7 @@ bool make_fft_plan(int L, FftPlan& p, std::vector<std::complex<long double>>& tw
 struct ChebMats {
   std::vector<double> invA, invB, fwdA, fwdB;  // P x KA, P x KB (row-major)
   std::vector<double> derA, derB;              // (2/L) T'_n at y_j for even / odd n
+  std::vector<double> dfA, dfB;                // diff o chebyfft: even coefs from d (P x KB), odd from s (P x KA)
 };
 
 long double sinpi_ratio(long long m, long long d) {
@@ -228,6 +229,33 @@ ChebMats make_cheb_mats(int N) {
   for (int j = 0; j < P; ++j) {
     for (int k = 0; k < KA; ++k) M.derA[j * KA + k] = (double)(cheb_deriv_at(2 * k, j, N));
     for (int k = 0; k < KB; ++k) M.derB[j * KB + k] = (double)(cheb_deriv_at(2 * k + 1, j, N));
+  }
+  {
+    // full forward matrix F[n][j] and coefficient derivative D (diff, chebyshev.cpp:672-697, L = 2 here;
+    // the 2/L factor is applied by the caller), DF = D F split by parity
+    std::vector<long double> F((size_t)N * N), D((size_t)N * N, 0.0L), DF((size_t)N * N, 0.0L);
+    for (int n = 0; n < N; ++n) {
+      const long double cn = (n == 0 || n == N - 1) ? 0.5L : 1.0L;
+      for (int j = 0; j < N; ++j) {
+        const long double w = (j == 0 || j == N - 1) ? 1.0L : 2.0L;
+        F[(size_t)n * N + j] = w * cospi_ratio((long long)n * j, N - 1) * cn / (N - 1);
+      }
+    }
+    for (int n = 0; n < N; ++n)
+      for (int m2 = n + 1; m2 < N; m2 += 2) D[(size_t)n * N + m2] = (n == 0 ? 1.0L : 2.0L) * m2;
+    for (int n = 0; n < N; ++n)
+      for (int mm = 0; mm < N; ++mm) {
+        const long double dv = D[(size_t)n * N + mm];
+        if (dv == 0.0L) continue;
+        for (int j = 0; j < N; ++j) DF[(size_t)n * N + j] += dv * F[(size_t)mm * N + j];
+      }
+    M.dfA.assign((size_t)P * KB, 0.0);
+    M.dfB.assign((size_t)P * KA, 0.0);
+    for (int k = 0; k < P; ++k) {
+      for (int j = 0; j < KB; ++j) M.dfA[k * KB + j] = (double)DF[(size_t)(2 * k) * N + j];
+      if (2 * k + 1 < N)
+        for (int j = 0; j <= J; ++j) M.dfB[k * KA + j] = (double)DF[(size_t)(2 * k + 1) * N + j];
+    }
   }
   for (int k = 0; k < P; ++k) {
     const int n = 2 * k;
@@ -372,6 +400,8 @@ struct cfgpu_dns_s {
   void *twx = nullptr, *twz = nullptr;  // R-typed complex
   void *cinvA = nullptr, *cinvB = nullptr, *cfwdA = nullptr, *cfwdB = nullptr;
   void *cderA = nullptr, *cderB = nullptr, *basey = nullptr;  // fused curl: (2/L) T'_n(y_j); U, U', W, W' at y_j
+  void *cdfA = nullptr, *cdfB = nullptr;                       // (2/L) diff o chebyfft, parity split
+  int alt[2] = {0, 0};  // Alternating state of the main (0) and init (1) NSE: 0 = next is divergence
   // state: current fields
   double *Ucur = nullptr, *Qcur = nullptr;
   // multistep ring
@@ -453,36 +483,73 @@ int build_tables(cfgpu_dns d, Scheme& s) {
   return CFGPU_OK;
 }
 
-// Nonlinear term N(u) of the fields in U (solved-mode layout) into Nout (R-typed).
+// Nonlinear term N(u) of the fields in U (solved-mode layout) into Nout (R-typed):
+// navierstokesNL (nse.cpp:12-91) for the form selected by the flags; `which`
+// selects the NSE (0 main, 1 init) whose Alternating state is advanced.
 template <typename R>
-int nonlinear_impl(cfgpu_dns d, const double* U, void* Nout) {
+int nonlinear_impl(cfgpu_dns d, const double* U, void* Nout, int form) {
   const GridDev& g = d->g;
   const int N = d->N;
   R* C6 = (R*)d->C6;
-  R* W6 = (R*)d->W6;
+  R* W = (R*)d->W6;
   const size_t row = d->rowc(), comp = d->compc();
-  if ((N + 1) / 2 <= 56) {
-    CK(launch_curl_cheb<R>(g, N, U, W6, (const R*)d->cinvA, (const R*)d->cinvB, (const R*)d->cderA,
-                           (const R*)d->cderB, (const R*)d->basey, d->fl.Vsuck, d->st));
-    d->launches -= 1;
+  int nin = 6, nout = 3;
+  if (form == NL_ROTATIONAL) {
+    if ((N + 1) / 2 <= 56) {
+      CK(launch_curl_cheb<R>(g, N, U, W, (const R*)d->cinvA, (const R*)d->cinvB, (const R*)d->cderA,
+                             (const R*)d->cderB, (const R*)d->basey, d->fl.Vsuck, d->st));
+      d->launches += 1;
+    } else {
+      CK(launch_curl_base<R>(g, U, C6, d->dUbase, d->dWbase, d->fl.Vsuck, d->st));
+      CK((launch_cheb<R, R, R>(N, true, (int)row, 6, C6, row, comp, W, row, comp, (const R*)d->cinvA,
+                               (const R*)d->cinvB, d->st)));
+      d->launches += 2;
+    }
   } else {
-    CK(launch_curl_base<R>(g, U, C6, d->dUbase, d->dWbase, d->fl.Vsuck, d->st));
-    CK((launch_cheb<R, R, R>(N, true, (int)row, 6, C6, row, comp, W6, row, comp, (const R*)d->cinvA,
-                             (const R*)d->cinvB, d->st)));
+    if ((N + 1) / 2 > 56) return fail(CFGPU_ENOTSUP, "Ny > 111 with a gradient nonlinear form");
+    const bool gradient = form != NL_DIVERGENCE;
+    CK(launch_grad_cheb<R>(g, N, gradient, U, W, (const R*)d->cinvA, (const R*)d->cinvB, (const R*)d->cderA,
+                           (const R*)d->cderB, (const R*)d->basey, d->fl.Vsuck, d->st));
+    d->launches += 1;
+    nin = gradient ? 12 : 3;
+    nout = form == NL_CONVECTION ? 3 : (form == NL_DIVERGENCE ? 6 : 9);
   }
-  CK(launch_xinv<R>(g, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)W6, (cpx<R>*)d->X6, 6, d->st));
-  CK(launch_zcross<R>(g, d->pz, (const cpx<R>*)d->twz, d->RP, (const cpx<R>*)d->X6, (cpx<R>*)d->Z3, d->st));
-  CK(launch_xfwd<R>(g, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)d->Z3, (cpx<R>*)d->F3, 3, d->st));
-  CK((launch_cheb<R, R, R>(N, false, (int)row, 3, (const R*)d->F3, row, comp, (R*)Nout, row, comp,
-                           (const R*)d->cfwdA, (const R*)d->cfwdB, d->st)));
-  d->launches += 6;
+  CK(launch_xinv<R>(g, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)W, (cpx<R>*)d->X6, nin, d->st));
+  CK(launch_zphys<R>(g, form, d->pz, (const cpx<R>*)d->twz, d->RP, (const cpx<R>*)d->X6, (cpx<R>*)d->Z3, d->st));
+  CK(launch_xfwd<R>(g, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)d->Z3, (cpx<R>*)d->F3, nout, d->st));
+  d->launches += 3;
+  const R* F = (const R*)d->F3;
+  if (form == NL_ROTATIONAL || form == NL_CONVECTION) {
+    CK((launch_cheb<R, R, R>(N, false, (int)row, 3, F, row, comp, (R*)Nout, row, comp, (const R*)d->cfwdA,
+                             (const R*)d->cfwdB, d->st)));
+    d->launches += 1;
+  } else {
+    // products p_ij (ij = uu, uv, uw, vv, vw, ww) follow the convection term for the skew form
+    const R* p = form == NL_SKEW ? F + 3 * comp : F;
+    const int pij[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+    const R half = (R)0.5;
+    for (int i = 0; i < 3; ++i) {
+      const R* pF = form == NL_SKEW ? F + i * comp : nullptr;
+      const R wF = form == NL_SKEW ? half : (R)0, w = form == NL_SKEW ? half : (R)1;
+      CK(launch_cheb_fwd_div<R>(g, N, pF, p + pij[i][0] * comp, p + pij[i][2] * comp, p + pij[i][1] * comp, wF, w,
+                                w, (R*)Nout + i * comp, (const R*)d->cfwdA, (const R*)d->cfwdB,
+                                (const R*)d->cdfA, (const R*)d->cdfB, d->st));
+    }
+    d->launches += 3;
+  }
   return CFGPU_OK;
 }
 
-int nonlinear(cfgpu_dns d, const double* U, void* Nout) {
+int nonlinear(cfgpu_dns d, const double* U, void* Nout, int which = 0) {
   PhaseScope ps(d, 0);
-  if (d->precision == CFGPU_FP64) return nonlinear_impl<double>(d, U, Nout);
-  return nonlinear_impl<float>(d, U, Nout);
+  int form = d->fl.nonlinearity;
+  if (form == CFGPU_Alternating || form == CFGPU_Alternating_) {
+    // navierstokesNL flips the NSE's flag on every call (nse.cpp:50-57): divergence, then convection, ...
+    form = d->alt[which] == 0 ? NL_DIVERGENCE : NL_CONVECTION;
+    d->alt[which] ^= 1;
+  }
+  if (d->precision == CFGPU_FP64) return nonlinear_impl<double>(d, U, Nout, form);
+  return nonlinear_impl<float>(d, U, Nout, form);
 }
 
 SolveParams base_params(cfgpu_dns d) {
@@ -580,7 +647,7 @@ int ms_advance(cfgpu_dns d, int nsteps) {
 // ---- CNAB-style (dnsalgo.cpp:608-697); which = 0 main, 1 init --------------
 int cnab_push(cfgpu_dns d, int which) {
   std::swap(d->fj[which], d->fj1[which]);
-  CKS(nonlinear(d, d->Ucur, d->fj[which]));
+  CKS(nonlinear(d, d->Ucur, d->fj[which], which));
   Scheme& s = which == 0 ? d->main : d->init;
   s.t += d->fl.dt;
   s.full = true;
@@ -592,7 +659,7 @@ int cnab_advance(cfgpu_dns d, int which, int nsteps) {
   for (int n = 0; n < nsteps; ++n) {
     for (int j = 0; j < s.nsub; ++j) {
       std::swap(d->fj[which], d->fj1[which]);
-      CKS(nonlinear(d, d->Ucur, d->fj[which]));
+      CKS(nonlinear(d, d->Ucur, d->fj[which], which));
       SolveParams sp = base_params(d);
       sp.kind = 1;
       sp.lam = s.lambda_t[j];
@@ -618,7 +685,7 @@ int rk_advance(cfgpu_dns d, int which, int nsteps) {
   Scheme& s = which == 0 ? d->main : d->init;
   for (int n = 0; n < nsteps; ++n) {
     for (int j = 0; j < s.nsub; ++j) {
-      CKS(nonlinear(d, d->Ucur, d->rkN));
+      CKS(nonlinear(d, d->Ucur, d->rkN, which));
       SolveParams sp = base_params(d);
       sp.kind = 2;
       sp.lam = s.lambda_t[j];
@@ -747,8 +814,10 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
   if ((Ny + 1) / 2 > 72) return fail(CFGPU_ENOTSUP, "Ny > 143 not supported by the Chebyshev transform kernel");
   if (!(grid->b > grid->a) || grid->Lx <= 0 || grid->Lz <= 0) return fail(CFGPU_EINVAL, "bad box");
   if (f.dt <= 0 || f.nu <= 0) return fail(CFGPU_EINVAL, "dt and nu must be positive");
-  if (f.nonlinearity != CFGPU_Rotational)
-    return fail(CFGPU_ENOTSUP, "only Rotational nonlinearity is implemented on the device path");
+  if (f.nonlinearity == CFGPU_LinearAboutProfile)
+    return fail(CFGPU_ENOTSUP, "LinearAboutProfile is not implemented on the device path");
+  if (f.nonlinearity < CFGPU_Rotational || f.nonlinearity > CFGPU_Alternating_)
+    return fail(CFGPU_EINVAL, "unknown nonlinearity");
   if (f.dealiasing == CFGPU_DealiasY || f.dealiasing == CFGPU_DealiasXYZ)
     return fail(CFGPU_ENOTSUP, "DealiasY is not implemented on the device path");
   const bool dxz = (f.dealiasing == CFGPU_DealiasXZ);
@@ -769,6 +838,7 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
   g.b = grid->b;
   g.kxs = g.kzs = nullptr;
   d->N = Ny;
+  d->alt[0] = d->alt[1] = (f.nonlinearity == CFGPU_Alternating_) ? 1 : 0;
   CK(cudaGetDevice(&d->device));
   CK(cudaStreamCreateWithFlags(&d->st, cudaStreamNonBlocking));
 
@@ -846,6 +916,8 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
   ChebMats cm = make_cheb_mats(Ny);
   for (auto& v : cm.derA) v *= 2.0 / (b - a);
   for (auto& v : cm.derB) v *= 2.0 / (b - a);
+  for (auto& v : cm.dfA) v *= 2.0 / (b - a);
+  for (auto& v : cm.dfB) v *= 2.0 / (b - a);
   std::vector<double> basey(4 * (size_t)Ny, 0.0);
   for (int j = 0; j < Ny; ++j) {
     long double U = 0, Uy = 0, W = 0, Wy = 0;
@@ -873,6 +945,8 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
     CKS(upload_as<double>(cm.derA, &d->cderA, B));
     CKS(upload_as<double>(cm.derB, &d->cderB, B));
     CKS(upload_as<double>(basey, &d->basey, B));
+    CKS(upload_as<double>(cm.dfA, &d->cdfA, B));
+    CKS(upload_as<double>(cm.dfB, &d->cdfB, B));
   } else {
     CKS(upload_tw<float>(twx, &d->twx, B));
     CKS(upload_tw<float>(twz, &d->twz, B));
@@ -883,6 +957,8 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
     CKS(upload_as<float>(cm.derA, &d->cderA, B));
     CKS(upload_as<float>(cm.derB, &d->cderB, B));
     CKS(upload_as<float>(basey, &d->basey, B));
+    CKS(upload_as<float>(cm.dfA, &d->cdfA, B));
+    CKS(upload_as<float>(cm.dfB, &d->cdfB, B));
   }
   // state and work arrays
   const size_t cd = d->compc();
@@ -894,21 +970,25 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
   unsigned char* tmp;
   CKS(dalloc(&tmp, 6 * cd * rs, B));
   d->C6 = tmp;
-  CKS(dalloc(&tmp, 6 * cd * rs, B));
+  const bool rot = (f.nonlinearity == CFGPU_Rotational);
+  const int nin = rot ? 6 : 12, nout = rot ? 3 : 9;  // y-physical components in / physical outputs
+  CKS(dalloc(&tmp, nin * cd * rs, B));
   d->W6 = tmp;
   const size_t plane = (size_t)Nx * g.NKz * 2;  // reals per plane per component
-  CKS(dalloc(&tmp, 6 * plane * Ny * rs, B));
+  CKS(dalloc(&tmp, nin * plane * Ny * rs, B));
   d->X6 = tmp;
-  CKS(dalloc(&tmp, 3 * plane * Ny * rs, B));
+  CKS(dalloc(&tmp, nout * plane * Ny * rs, B));
   d->Z3 = tmp;
-  CKS(dalloc(&tmp, 3 * cd * rs, B));
+  CKS(dalloc(&tmp, nout * cd * rs, B));
   d->F3 = tmp;
   CKS(dalloc(&d->scratch, 8 * cd, B));
   d->RP = fp64 ? 8 : 16;
-  while (d->RP > 2 && (fp64 ? zcross_smem_bytes<double>(g, d->RP) : zcross_smem_bytes<float>(g, d->RP)) > 200 * 1024)
-    d->RP -= 2;
-  if ((fp64 ? xfft_smem_bytes<double>(g) : xfft_smem_bytes<float>(g)) > 227 * 1024 ||
-      (fp64 ? zcross_smem_bytes<double>(g, d->RP) : zcross_smem_bytes<float>(g, d->RP)) > 227 * 1024)
+  auto zbytes = [&](int form, int rp) {
+    return fp64 ? zphys_smem_bytes<double>(g, form, rp) : zphys_smem_bytes<float>(g, form, rp);
+  };
+  const int zform = rot ? NL_ROTATIONAL : NL_SKEW;  // skew needs the most shared memory of the gradient forms
+  while (d->RP > 2 && zbytes(zform, d->RP) > 200 * 1024) d->RP -= 2;
+  if ((fp64 ? xfft_smem_bytes<double>(g) : xfft_smem_bytes<float>(g)) > 227 * 1024 || zbytes(zform, d->RP) > 227 * 1024)
     return fail(CFGPU_ENOTSUP, "grid too large for the shared-memory FFT passes");
   if (cheb_smem_bytes(Ny, rs) > 200 * 1024) return fail(CFGPU_ENOTSUP, "Ny too large for the Chebyshev kernel");
 
@@ -970,7 +1050,7 @@ void dns_free(cfgpu_dns d) {
   F(d->dUbase); F(d->dWbase); F(d->dUbaseyy); F(d->dWbaseyy); F(d->ddPdx);
   F(d->hb_lo); F(d->hb_di); F(d->hb_up);
   F(d->twx); F(d->twz); F(d->cinvA); F(d->cinvB); F(d->cfwdA); F(d->cfwdB);
-  F(d->cderA); F(d->cderB); F(d->basey);
+  F(d->cderA); F(d->cderB); F(d->basey); F(d->cdfA); F(d->cdfB);
   F(d->Ucur); F(d->Qcur);
   for (int j = 0; j < 4; ++j) { F(d->Uh[j]); F(d->Qh[j]); F(d->Nh[j]); }
   for (int w = 0; w < 2; ++w) { F(d->fj[w]); F(d->fj1[w]); F(d->rkQ[w]); }

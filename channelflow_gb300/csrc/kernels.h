@@ -25,6 +25,26 @@ template <typename TI, typename R, typename TO>
 cudaError_t launch_cheb(int N, bool inverse, int nlines, int ncomp, const TI* in, size_t ld_in, size_t cs_in, TO* out,
                         size_t ld_out, size_t cs_out, const R* A, const R* B, cudaStream_t st);
 
+// Nonlinear forms (values of the reference's NonlinearMethod enum, dnsflags.h:28-35)
+enum { NL_ROTATIONAL = 0, NL_CONVECTION = 1, NL_DIVERGENCE = 2, NL_SKEW = 3 };
+
+template <typename R>
+size_t grad_cheb_smem_bytes(int N);
+template <typename R>
+cudaError_t launch_grad_cheb(const GridDev& g, int N, bool gradient, const double* U, R* W, const R* CA, const R* CB,
+                             const R* DA, const R* DB, const R* basey, double Vsuck, cudaStream_t st);
+template <typename R>
+size_t zphys_smem_bytes(const GridDev& g, int form, int RP);
+template <typename R>
+cudaError_t launch_zphys(const GridDev& g, int form, const FftPlan& pz, const cpx<R>* twz, int RP, const cpx<R>* X,
+                         cpx<R>* Z, cudaStream_t st);
+template <typename R>
+size_t cheb_fwd_div_smem_bytes(int N);
+template <typename R>
+cudaError_t launch_cheb_fwd_div(const GridDev& g, int N, const R* pF, const R* pKx, const R* pKz, const R* pD, R wF,
+                                R wK, R wD, R* out, const R* FA, const R* FB, const R* DFA, const R* DFB,
+                                cudaStream_t st);
+
 template <typename R>
 size_t xfft_smem_bytes(const GridDev& g);
 template <typename R>

@@ -1,0 +1,490 @@
+// Nonlinear-term forms beyond the fused rotational kernel: the velocity
+// gradient (convection, skew-symmetric) and velocity-only (divergence) inverse
+// Chebyshev kernels, a physical-space z pass for any form, and the forward
+// Chebyshev transform with the divergence combination.
+//
+// Reference functions restated (channelflow project paths):
+//   convectionNL -> dotgrad        channelflow/diffops.cpp:2883-2885, 3586-3643
+//   divergenceNL                   channelflow/diffops.cpp:3110-3134 (outer + div)
+//   skewsymmetricNL                channelflow/diffops.cpp:3142-3286
+//   grad (d/dx_j u_i, index 3i+j)  channelflow/diffops.cpp:1784-1941
+// Forms (NL_*): rotational (omega x u), convection (u.grad u), divergence
+// (div(u u)), skew-symmetric (1/2 (u.grad u + div(u u))).
+#include "fft.cuh"
+#include "kernels.h"
+
+#define GC_TL 32
+#define GC_PT 7
+
+// ---------------------------------------------------------------------------
+// Inverse Chebyshev of u, v, w (+ base flow) with, for MODE = 1, the nine
+// gradient components G[3i+j] = d u_i / d x_j (d/dx, d/dz spectral, d/dy via
+// the (2/L) T'_n half-matrices).  MODE = 2 outputs u, v, w only.
+// Output W[c][j][line]: c = 0..2 velocity, 3 + 3i + j gradient.
+// ---------------------------------------------------------------------------
+template <typename R, int MODE>
+__global__ void __launch_bounds__(256) k_grad_cheb(GridDev g, int N, const double* __restrict__ U, R* __restrict__ W,
+                                                   const R* __restrict__ CA, const R* __restrict__ CB,
+                                                   const R* __restrict__ DA, const R* __restrict__ DB,
+                                                   const R* __restrict__ basey, R Vsuck) {
+  extern __shared__ unsigned char smem_raw[];
+  const int P = (N + 1) / 2, KA = (N + 1) / 2, KB = (N - 1) / 2, J = (N - 1) / 2;
+  R* xs = reinterpret_cast<R*>(smem_raw);  // [3][N][TL]: even coefs rows 0..KA-1, odd KA..N-1
+  R* sCA = xs + 3 * N * GC_TL;
+  R* sCB = sCA + P * KA;
+  R* sDA = sCB + P * KB;
+  R* sDB = sDA + P * KA;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nlines = 2 * g.Md;
+  const int l0 = blockIdx.x * GC_TL;
+  const size_t row = (size_t)nlines, comp = row * N;
+  for (int i = tid; i < P * KA; i += blockDim.x) {
+    sCA[i] = CA[i];
+    if (MODE == 1) sDA[i] = DA[i];
+  }
+  for (int i = tid; i < P * KB; i += blockDim.x) {
+    sCB[i] = CB[i];
+    if (MODE == 1) sDB[i] = DB[i];
+  }
+  for (int i = tid; i < 3 * N * GC_TL; i += blockDim.x) {
+    const int l = i % GC_TL, n = (i / GC_TL) % N, c = i / (GC_TL * N);
+    const int gl = l0 + l;
+    const R v = gl < nlines ? (R)U[c * comp + (size_t)n * row + gl] : (R)0;
+    const int r = (n & 1) ? KA + (n >> 1) : (n >> 1);
+    xs[(c * N + r) * GC_TL + l] = v;
+  }
+  __syncthreads();
+  constexpr int NT = MODE == 1 ? 6 : 3;  // transforms: C u_c (3) and, for the gradient, CD u_c (3)
+  R ae[NT][GC_PT], bo[NT][GC_PT];        // even-coefficient and odd-coefficient partial sums
+#pragma unroll
+  for (int t = 0; t < NT; ++t)
+#pragma unroll
+    for (int i = 0; i < GC_PT; ++i) ae[t][i] = bo[t][i] = 0;
+  for (int k = 0; k < KA; ++k) {
+    R x[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) x[c] = xs[(c * N + k) * GC_TL + lane];
+#pragma unroll
+    for (int i = 0; i < GC_PT; ++i) {
+      const int p = warp + 8 * i;
+      if (p < P) {
+        const R cc = sCA[p * KA + k];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) ae[c][i] += cc * x[c];
+        if (MODE == 1) {
+          const R d = sDA[p * KA + k];
+#pragma unroll
+          for (int c = 0; c < 3; ++c) ae[3 + c][i] += d * x[c];
+        }
+      }
+    }
+  }
+  for (int k = 0; k < KB; ++k) {
+    R x[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) x[c] = xs[(c * N + KA + k) * GC_TL + lane];
+#pragma unroll
+    for (int i = 0; i < GC_PT; ++i) {
+      const int p = warp + 8 * i;
+      if (p < P) {
+        const R cc = sCB[p * KB + k];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) bo[c][i] += cc * x[c];
+        if (MODE == 1) {
+          const R d = sDB[p * KB + k];
+#pragma unroll
+          for (int c = 0; c < 3; ++c) bo[3 + c][i] += d * x[c];
+        }
+      }
+    }
+  }
+  const int gl = l0 + lane;
+  const int m = min(gl, nlines - 1) >> 1;
+  const int part = gl & 1;
+  const int kx = mode_kx(g, m), kz = mode_kz(g, m);
+  const R dx = (R)(2.0 * M_PI * kx / g.Lx * (kx == g.kxmax ? 0.0 : 1.0));
+  const R dz = (R)(2.0 * M_PI * kz / g.Lz * (kz == g.kzmax ? 0.0 : 1.0));
+  const bool base = (kx == 0 && kz == 0 && part == 0);
+#pragma unroll
+  for (int i = 0; i < GC_PT; ++i) {
+    const int p = warp + 8 * i;
+    if (p >= P) continue;  // uniform per warp
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      if (h == 1 && p >= J) continue;
+      const int j = h == 0 ? p : N - 1 - p;
+      const R sg = h == 0 ? (R)1 : (R)-1;
+      R u[3], dy[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) u[c] = ae[c][i] + sg * bo[c][i];
+      if (MODE == 1) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) dy[c] = bo[3 + c][i] + sg * ae[3 + c][i];
+      }
+      if (base) {
+        u[0] += basey[j];
+        u[2] += basey[2 * N + j];
+        u[1] -= Vsuck;
+        if (MODE == 1) {
+          dy[0] += basey[N + j];
+          dy[2] += basey[3 * N + j];
+        }
+      }
+      R* o = W + (size_t)j * row + gl;
+      if (MODE == 1) {
+        R ou[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) ou[c] = __shfl_xor_sync(0xffffffffu, u[c], 1);
+        if (gl < nlines) {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            // (i k) f: re = -k f_im, im = k f_re
+            const R gx = part == 0 ? -dx * ou[c] : dx * ou[c];
+            const R gz = part == 0 ? -dz * ou[c] : dz * ou[c];
+            o[(size_t)c * comp] = u[c];
+            o[(size_t)(3 + 3 * c + 0) * comp] = gx;
+            o[(size_t)(3 + 3 * c + 1) * comp] = dy[c];
+            o[(size_t)(3 + 3 * c + 2) * comp] = gz;
+          }
+        }
+      } else if (gl < nlines) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) o[(size_t)c * comp] = u[c];
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// z pass for any form.  Real sequence k of the block (row r = k / NC,
+// component c = k % NC) is half of complex sequence k/2 (real part for even
+// k, imaginary for odd k): one complex FFT transforms two real rows.
+// ---------------------------------------------------------------------------
+template <int FORM>
+struct FormIO;
+template <>
+struct FormIO<NL_ROTATIONAL> { static constexpr int NC = 6, NO = 3; };
+template <>
+struct FormIO<NL_CONVECTION> { static constexpr int NC = 12, NO = 3; };
+template <>
+struct FormIO<NL_DIVERGENCE> { static constexpr int NC = 3, NO = 6; };
+template <>
+struct FormIO<NL_SKEW> { static constexpr int NC = 12, NO = 9; };
+
+template <typename R, int FORM>
+__device__ __forceinline__ void phys_products(const R* c, R* f) {
+  if constexpr (FORM == NL_ROTATIONAL) {
+    // c = u, v, w, ox, oy, oz ; f = omega x u
+    f[0] = c[4] * c[2] - c[5] * c[1];
+    f[1] = c[5] * c[0] - c[3] * c[2];
+    f[2] = c[3] * c[1] - c[4] * c[0];
+  } else if constexpr (FORM == NL_DIVERGENCE) {
+    f[0] = c[0] * c[0];
+    f[1] = c[0] * c[1];
+    f[2] = c[0] * c[2];
+    f[3] = c[1] * c[1];
+    f[4] = c[1] * c[2];
+    f[5] = c[2] * c[2];
+  } else {
+    // u_j d u_i / d x_j
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      R s = 0;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) s += c[j] * c[3 + 3 * i + j];
+      f[i] = s;
+    }
+    if constexpr (FORM == NL_SKEW) {
+      f[3] = c[0] * c[0];
+      f[4] = c[0] * c[1];
+      f[5] = c[0] * c[2];
+      f[6] = c[1] * c[1];
+      f[7] = c[1] * c[2];
+      f[8] = c[2] * c[2];
+    }
+  }
+}
+
+template <typename R, int FORM>
+__global__ void __launch_bounds__(256) k_zphys(GridDev g, FftPlan pz, const cpx<R>* __restrict__ twz, int RP,
+                                               const cpx<R>* __restrict__ X, cpx<R>* __restrict__ Z) {
+  constexpr int NC = FormIO<FORM>::NC, NO = FormIO<FORM>::NO;
+  extern __shared__ unsigned char smem_raw[];
+  const int Nz = g.Nz, ss = Nz + 1, NKz = g.NKz;
+  const int nseq = ((NC > NO ? NC : NO) * RP) / 2;
+  const int ninv = NC * RP / 2, nfwd = NO * RP / 2;
+  cpx<R>* A = reinterpret_cast<cpx<R>*>(smem_raw);
+  cpx<R>* B = A + (size_t)nseq * ss;
+  const int ny = blockIdx.y;
+  const int x0 = blockIdx.x * RP;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const size_t plane = (size_t)g.Nx * NKz;
+  for (int i = tid; i < ninv * ss; i += nthr) A[i] = cmk<R>(0, 0);
+  __syncthreads();
+  for (int i = tid; i < ninv * NKz; i += nthr) {
+    const int iz = i % NKz, s = i / NKz;
+    const int k0 = 2 * s, k1 = 2 * s + 1;
+    const int r0 = k0 / NC, c0 = k0 % NC, r1 = k1 / NC, c1 = k1 % NC;
+    cpx<R> ca = cmk<R>(0, 0), cb = cmk<R>(0, 0);
+    if (x0 + r0 < g.Nx) ca = X[((size_t)c0 * g.Ny + ny) * plane + (size_t)(x0 + r0) * NKz + iz];
+    if (x0 + r1 < g.Nx) cb = X[((size_t)c1 * g.Ny + ny) * plane + (size_t)(x0 + r1) * NKz + iz];
+    cpx<R>* sq = A + (size_t)s * ss;
+    if (iz == 0) {
+      sq[0] = cmk<R>(ca.x, cb.x);
+    } else {
+      sq[iz] = cmk<R>(ca.x - cb.y, ca.y + cb.x);        // A_k + i B_k
+      sq[Nz - iz] = cmk<R>(ca.x + cb.y, -ca.y + cb.x);  // conj(A_k) + i conj(B_k)
+    }
+  }
+  __syncthreads();
+  fft_batch<R>(A, B, ninv, ss, pz, twz, +1);
+  R* Br = reinterpret_cast<R*>(B);
+  for (int i = tid; i < RP * Nz; i += nthr) {
+    const int z = i % Nz, r = i / Nz;
+    R c[NC], f[NO];
+#pragma unroll
+    for (int q = 0; q < NC; ++q) {
+      const int k = r * NC + q;
+      const cpx<R> v = A[(size_t)(k >> 1) * ss + z];
+      c[q] = (k & 1) ? v.y : v.x;
+    }
+    phys_products<R, FORM>(c, f);
+#pragma unroll
+    for (int o = 0; o < NO; ++o) {
+      const int k = r * NO + o;
+      Br[2 * ((size_t)(k >> 1) * ss + z) + (k & 1)] = f[o];
+    }
+  }
+  __syncthreads();
+  fft_batch<R>(B, A, nfwd, ss, pz, twz, -1);
+  for (int i = tid; i < nfwd * NKz; i += nthr) {
+    const int iz = i % NKz, s = i / NKz;
+    const cpx<R>* sq = B + (size_t)s * ss;
+    const cpx<R> zk = sq[iz];
+    const cpx<R> zm = sq[iz == 0 ? 0 : Nz - iz];
+    const cpx<R> Pk = cmk<R>((R)0.5 * (zk.x + zm.x), (R)0.5 * (zk.y - zm.y));
+    const cpx<R> Qk = cmk<R>((R)0.5 * (zk.y + zm.y), (R)0.5 * (zm.x - zk.x));
+    const int k0 = 2 * s, k1 = 2 * s + 1;
+    const int r0 = k0 / NO, o0 = k0 % NO, r1 = k1 / NO, o1 = k1 % NO;
+    if (x0 + r0 < g.Nx) Z[((size_t)o0 * g.Ny + ny) * plane + (size_t)(x0 + r0) * NKz + iz] = Pk;
+    if (x0 + r1 < g.Nx) Z[((size_t)o1 * g.Ny + ny) * plane + (size_t)(x0 + r1) * NKz + iz] = Qk;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Forward Chebyshev transform with the divergence combination for one output
+// component i:  N_i = wF F(pF) + wK (i kx F(pKx) + i kz F(pKz)) + wD DF(pD)
+// where F maps values at the Gauss-Lobatto points to Chebyshev coefficients
+// (chebyfft) and DF = diff o F.  Parity split: with s_j = x_j + x_{N-1-j},
+// d_j = x_j - x_{N-1-j}: F even = FA s, F odd = FB d, DF even = DFA d,
+// DF odd = DFB s.  pF may be null (divergence form).
+// ---------------------------------------------------------------------------
+#define CF_TL 32
+#define CF_PT 9
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_cheb_fwd_div(GridDev g, int N, const R* __restrict__ pF,
+                                                      const R* __restrict__ pKx, const R* __restrict__ pKz,
+                                                      const R* __restrict__ pD, R wF, R wK, R wD, R* __restrict__ out,
+                                                      const R* __restrict__ FA, const R* __restrict__ FB,
+                                                      const R* __restrict__ DFA, const R* __restrict__ DFB) {
+  extern __shared__ unsigned char smem_raw[];
+  const int P = (N + 1) / 2, J = (N - 1) / 2, KA = J + 1, KB = J;
+  R* xs = reinterpret_cast<R*>(smem_raw);  // [4 inputs][KA s-rows + KB d-rows][TL]
+  R* sFA = xs + 4 * N * CF_TL;
+  R* sFB = sFA + P * KA;
+  R* sDA = sFB + P * KB;  // P x KB (acts on d)
+  R* sDB = sDA + P * KB;  // P x KA (acts on s)
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nlines = 2 * g.Md;
+  const int l0 = blockIdx.x * CF_TL;
+  const size_t row = (size_t)nlines;
+  for (int i = tid; i < P * KA; i += blockDim.x) {
+    sFA[i] = FA[i];
+    sDB[i] = DFB[i];
+  }
+  for (int i = tid; i < P * KB; i += blockDim.x) {
+    sFB[i] = FB[i];
+    sDA[i] = DFA[i];
+  }
+  const R* ins[4] = {pF, pKx, pKz, pD};
+  for (int i = tid; i < 4 * KA * CF_TL; i += blockDim.x) {
+    const int l = i % CF_TL, j = (i / CF_TL) % KA, c = i / (CF_TL * KA);
+    const int gl = l0 + l;
+    const R* src = ins[c];
+    R v1 = 0, v2 = 0;
+    if (src && gl < nlines) {
+      v1 = src[(size_t)j * row + gl];
+      v2 = src[(size_t)(N - 1 - j) * row + gl];
+    }
+    if (j < J) {
+      xs[(c * N + j) * CF_TL + l] = v1 + v2;
+      xs[(c * N + KA + j) * CF_TL + l] = v1 - v2;
+    } else {
+      xs[(c * N + j) * CF_TL + l] = v1;  // middle point
+    }
+  }
+  __syncthreads();
+  R fe[3][CF_PT], fo[3][CF_PT], de[CF_PT], dd[CF_PT];
+#pragma unroll
+  for (int i = 0; i < CF_PT; ++i) {
+    de[i] = dd[i] = 0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) fe[c][i] = fo[c][i] = 0;
+  }
+  // s rows: F even (inputs 0..2) and DF odd (input 3)
+  for (int k = 0; k < KA; ++k) {
+    R x[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) x[c] = xs[(c * N + k) * CF_TL + lane];
+#pragma unroll
+    for (int i = 0; i < CF_PT; ++i) {
+      const int p = warp + 8 * i;
+      if (p < P) {
+        const R a = sFA[p * KA + k];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) fe[c][i] += a * x[c];
+        dd[i] += sDB[p * KA + k] * x[3];
+      }
+    }
+  }
+  // d rows: F odd (inputs 0..2) and DF even (input 3)
+  for (int k = 0; k < KB; ++k) {
+    R x[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) x[c] = xs[(c * N + KA + k) * CF_TL + lane];
+#pragma unroll
+    for (int i = 0; i < CF_PT; ++i) {
+      const int p = warp + 8 * i;
+      if (p < P) {
+        const R b = sFB[p * KB + k];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) fo[c][i] += b * x[c];
+        de[i] += sDA[p * KB + k] * x[3];
+      }
+    }
+  }
+  const int gl = l0 + lane;
+  const int m = min(gl, nlines - 1) >> 1;
+  const int part = gl & 1;
+  const int kx = mode_kx(g, m), kz = mode_kz(g, m);
+  const R dx = (R)(2.0 * M_PI * kx / g.Lx * (kx == g.kxmax ? 0.0 : 1.0));
+  const R dz = (R)(2.0 * M_PI * kz / g.Lz * (kz == g.kzmax ? 0.0 : 1.0));
+#pragma unroll
+  for (int i = 0; i < CF_PT; ++i) {
+    const int p = warp + 8 * i;
+    if (p >= P) continue;  // uniform per warp
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int n = 2 * p + h;
+      if (n >= N) continue;  // uniform per warp
+      const R vF = h == 0 ? fe[0][i] : fo[0][i];
+      const R vX = h == 0 ? fe[1][i] : fo[1][i];
+      const R vZ = h == 0 ? fe[2][i] : fo[2][i];
+      const R vD = h == 0 ? de[i] : dd[i];
+      const R t = dx * vX + dz * vZ;                    // (kx F(pKx) + kz F(pKz)) of my part
+      const R tp = __shfl_xor_sync(0xffffffffu, t, 1);  // same of the other part
+      const R ik = part == 0 ? -tp : tp;                // i * (...)
+      const R val = wF * vF + wK * ik + wD * vD;
+      if (gl < nlines) out[(size_t)n * row + gl] = val;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+template <typename R>
+size_t grad_cheb_smem_bytes(int N) {
+  const int P = (N + 1) / 2, KA = (N + 1) / 2, KB = (N - 1) / 2;
+  return sizeof(R) * ((size_t)3 * N * GC_TL + 2 * (size_t)P * (KA + KB));
+}
+
+template <typename R>
+cudaError_t launch_grad_cheb(const GridDev& g, int N, bool gradient, const double* U, R* W, const R* CA, const R* CB,
+                             const R* DA, const R* DB, const R* basey, double Vsuck, cudaStream_t st) {
+  if ((N + 1) / 2 > 8 * GC_PT) return cudaErrorInvalidValue;
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_grad_cheb<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(k_grad_cheb<R, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    attr_set = true;
+  }
+  const int nlines = 2 * g.Md;
+  const dim3 grid((nlines + GC_TL - 1) / GC_TL);
+  if (gradient)
+    k_grad_cheb<R, 1><<<grid, 256, grad_cheb_smem_bytes<R>(N), st>>>(g, N, U, W, CA, CB, DA, DB, basey, (R)Vsuck);
+  else
+    k_grad_cheb<R, 2><<<grid, 256, grad_cheb_smem_bytes<R>(N), st>>>(g, N, U, W, CA, CB, DA, DB, basey, (R)Vsuck);
+  return cudaGetLastError();
+}
+
+template <typename R>
+size_t zphys_smem_bytes(const GridDev& g, int form, int RP) {
+  int nc = 6, no = 3;
+  if (form == NL_CONVECTION) { nc = 12; no = 3; }
+  if (form == NL_DIVERGENCE) { nc = 3; no = 6; }
+  if (form == NL_SKEW) { nc = 12; no = 9; }
+  const int nseq = ((nc > no ? nc : no) * RP) / 2;
+  return 2 * sizeof(cpx<R>) * (size_t)nseq * (g.Nz + 1);
+}
+
+template <typename R, int FORM>
+static cudaError_t launch_zphys_t(const GridDev& g, const FftPlan& pz, const cpx<R>* twz, int RP, const cpx<R>* X,
+                                  cpx<R>* Z, cudaStream_t st) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_zphys<R, FORM>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    attr_set = true;
+  }
+  k_zphys<R, FORM><<<dim3((g.Nx + RP - 1) / RP, g.Ny), 256, zphys_smem_bytes<R>(g, FORM, RP), st>>>(g, pz, twz, RP,
+                                                                                                    X, Z);
+  return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_zphys(const GridDev& g, int form, const FftPlan& pz, const cpx<R>* twz, int RP, const cpx<R>* X,
+                         cpx<R>* Z, cudaStream_t st) {
+  switch (form) {
+    case NL_ROTATIONAL: return launch_zphys_t<R, NL_ROTATIONAL>(g, pz, twz, RP, X, Z, st);
+    case NL_CONVECTION: return launch_zphys_t<R, NL_CONVECTION>(g, pz, twz, RP, X, Z, st);
+    case NL_DIVERGENCE: return launch_zphys_t<R, NL_DIVERGENCE>(g, pz, twz, RP, X, Z, st);
+    default: return launch_zphys_t<R, NL_SKEW>(g, pz, twz, RP, X, Z, st);
+  }
+}
+
+template <typename R>
+size_t cheb_fwd_div_smem_bytes(int N) {
+  const int P = (N + 1) / 2, J = (N - 1) / 2;
+  return sizeof(R) * ((size_t)4 * N * CF_TL + (size_t)P * (J + 1) * 2 + (size_t)P * J * 2);
+}
+
+template <typename R>
+cudaError_t launch_cheb_fwd_div(const GridDev& g, int N, const R* pF, const R* pKx, const R* pKz, const R* pD, R wF,
+                                R wK, R wD, R* out, const R* FA, const R* FB, const R* DFA, const R* DFB,
+                                cudaStream_t st) {
+  if ((N + 1) / 2 > 8 * CF_PT) return cudaErrorInvalidValue;
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_cheb_fwd_div<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    attr_set = true;
+  }
+  const int nlines = 2 * g.Md;
+  k_cheb_fwd_div<R><<<(nlines + CF_TL - 1) / CF_TL, 256, cheb_fwd_div_smem_bytes<R>(N), st>>>(
+      g, N, pF, pKx, pKz, pD, wF, wK, wD, out, FA, FB, DFA, DFB);
+  return cudaGetLastError();
+}
+
+#define INST_FORMS(R)                                                                                              \
+  template size_t grad_cheb_smem_bytes<R>(int);                                                                    \
+  template cudaError_t launch_grad_cheb<R>(const GridDev&, int, bool, const double*, R*, const R*, const R*,      \
+                                           const R*, const R*, const R*, double, cudaStream_t);                    \
+  template size_t zphys_smem_bytes<R>(const GridDev&, int, int);                                                   \
+  template cudaError_t launch_zphys<R>(const GridDev&, int, const FftPlan&, const cpx<R>*, int, const cpx<R>*,      \
+                                       cpx<R>*, cudaStream_t);                                                     \
+  template size_t cheb_fwd_div_smem_bytes<R>(int);                                                                 \
+  template cudaError_t launch_cheb_fwd_div<R>(const GridDev&, int, const R*, const R*, const R*, const R*, R, R, R, \
+                                              R*, const R*, const R*, const R*, const R*, cudaStream_t);
+
+INST_FORMS(float)
+INST_FORMS(double)

@@ -775,8 +775,12 @@ class NSE:
         u[2, :, 0, 0] += self.Wbase
         u[1, 0, 0, 0] -= fl.Vsuck
         nl = fl.nonlinearity
-        if nl in (Alternating, Alternating_):
-            raise NotImplementedError("Alternating nonlinearity")
+        if nl == Alternating:  # nse.cpp:50-57: the flag flips on every call
+            nl = Divergence
+            fl.nonlinearity = Alternating_
+        elif nl == Alternating_:
+            nl = Convection
+            fl.nonlinearity = Alternating
         if nl == Rotational:
             om = curl(u, g)
             up = make_physical(u, g)

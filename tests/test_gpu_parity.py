@@ -74,6 +74,21 @@ CASES = [
           dealiasing=O.NoDealiasing), 10),
     ("suction_sbdf1_gradp", (12, 17, 12, *COUETTE_BOX),
      dict(nu=1 / 400, dt=0.02, timestepping=O.SBDF1, baseflow=O.SuctionBase, Vsuck=1 / 400), 10),
+    ("couette_sbdf3_convection", (12, 17, 12, *COUETTE_BOX),
+     dict(nu=1 / 400, dt=0.02, timestepping=O.SBDF3, initstepping=O.SMRK2, baseflow=O.LaminarBase,
+          ulowerwall=-1.0, uupperwall=1.0, nonlinearity=O.Convection), 10),
+    ("couette_cnab2_skew_bulk", (12, 17, 12, *POISEUILLE_BOX),
+     dict(nu=1 / 2000, dt=0.01, timestepping=O.CNAB2, initstepping=O.SMRK2, baseflow=O.LaminarBase,
+          constraint=O.BulkVelocity, Ubulk=2.0 / 3.0, nonlinearity=O.SkewSymmetric), 10),
+    ("couette_sbdf2_divergence", (12, 17, 12, *COUETTE_BOX),
+     dict(nu=1 / 400, dt=0.02, timestepping=O.SBDF2, initstepping=O.SMRK2, baseflow=O.LaminarBase,
+          ulowerwall=-1.0, uupperwall=1.0, nonlinearity=O.Divergence), 10),
+    ("couette_sbdf3_alternating", (12, 17, 12, *COUETTE_BOX),
+     dict(nu=1 / 400, dt=0.02, timestepping=O.SBDF3, initstepping=O.SMRK2, baseflow=O.LaminarBase,
+          ulowerwall=-1.0, uupperwall=1.0, nonlinearity=O.Alternating), 11),
+    ("suction_cnrk2_skew_nodealias", (8, 17, 8, *COUETTE_BOX),
+     dict(nu=1 / 400, dt=0.02, timestepping=O.CNRK2, baseflow=O.SuctionBase, Vsuck=1 / 400,
+          nonlinearity=O.SkewSymmetric, dealiasing=O.NoDealiasing), 6),
     ("poiseuille_48_cnab2", (48, 49, 48, *POISEUILLE_BOX),
      dict(nu=1 / 4000, dt=0.01, timestepping=O.CNAB2, initstepping=O.SMRK2, baseflow=O.LaminarBase,
           constraint=O.BulkVelocity, Ubulk=2.0 / 3.0), 5),
@@ -122,6 +137,18 @@ def test_dns_mixed_matches_oracle():
     u0 = O.random_divfree_field(g, seed=5, norm=0.1)
     ou, _, _ = oracle_run(u0, g, fl, 50)
     gu, _, _ = gpu_run(u0, g, fl, 50, precision="mixed")
+    ou[:, :, ~solved_mask(g)] = 0
+    assert rel_l2(gu, ou, g) <= MIXED_TOL
+
+
+@pytest.mark.parametrize("nl", [O.Convection, O.SkewSymmetric, O.Divergence])
+def test_dns_mixed_gradient_forms(nl):
+    g = O.Grid(24, 25, 24, *COUETTE_BOX)
+    fl = O.DNSFlags(nu=1 / 400, dt=0.02, timestepping=O.SBDF3, initstepping=O.SMRK2, baseflow=O.LaminarBase,
+                    ulowerwall=-1.0, uupperwall=1.0, nonlinearity=nl)
+    u0 = O.random_divfree_field(g, seed=7, norm=0.1)
+    ou, _, _ = oracle_run(u0, g, fl, 20)
+    gu, _, _ = gpu_run(u0, g, fl, 20, precision="mixed")
     ou[:, :, ~solved_mask(g)] = 0
     assert rel_l2(gu, ou, g) <= MIXED_TOL
 
