@@ -55,6 +55,9 @@ _SIGS = {
     "cfgpu_dns_device_bytes": [C.c_void_p, C.POINTER(C.c_longlong)],
     "cfgpu_dns_kernel_launches": [C.c_void_p, C.POINTER(C.c_longlong)],
     "cfgpu_dns_destroy": [C.c_void_p],
+    "cfgpu_dns_cfl": [C.c_void_p, _PD],
+    "cfgpu_measure_fp64": [_PD, _PD],
+    "cfgpu_dns_l2norm": [C.c_void_p, C.c_int, _PD],
     "cfgpu_dns_advance_timed": [C.c_void_p, C.c_int, _PD],
     "cfgpu_dns_set_profiling": [C.c_void_p, C.c_int],
     "cfgpu_dns_phase_times": [C.c_void_p, _PD, C.POINTER(C.c_longlong), _PD, C.POINTER(C.c_longlong)],

@@ -1,0 +1,186 @@
+// Diagnostics computed on the device: the CFL factor and the L2 norm.
+//
+// Reference functions restated (channelflow project paths):
+//   FlowField::CFLfactor(Ubase, Wbase)   channelflow/flowfield.cpp:4035-4068
+//       max over points and components of (u_i + U_i)/dx_i -- a signed maximum,
+//       dx = Lx/Nx, Lz/Nz, and in y (y[ny-1]-y[ny+1])/2 ((y0-y1) at the walls)
+//   DNSAlgorithm::CFL                     channelflow/dnsalgo.cpp:63-67
+//   L2Norm2(FlowField, normalize=true)    channelflow/diffops.cpp:417-487 with the
+//       Chebyshev quadratic form of L2Norm2(ChebyCoeff), chebyshev.cpp:758-773
+#include "fft.cuh"
+#include "kernels.h"
+
+// Order-preserving map of doubles onto unsigned 64-bit integers (for atomicMax).
+__device__ __forceinline__ unsigned long long dbl_key(double v) {
+  const unsigned long long b = __double_as_longlong(v);
+  return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+__host__ __device__ inline double key_dbl(unsigned long long k) {
+  const unsigned long long b = (k & 0x8000000000000000ull) ? (k & ~0x8000000000000000ull) : ~k;
+  double d;
+  memcpy(&d, &b, sizeof(d));
+  return d;
+}
+
+// z pass for the CFL factor: c2r along z of u, v, w (x-transformed planes,
+// two real rows per complex FFT) and the signed maximum of u_i/dx_i.
+template <typename R>
+__global__ void __launch_bounds__(256) k_zcfl(GridDev g, FftPlan pz, const cpx<R>* __restrict__ twz, int RP,
+                                              const cpx<R>* __restrict__ X, const double* __restrict__ dyc, double dx,
+                                              double dz, unsigned long long* __restrict__ out) {
+  extern __shared__ unsigned char smem_raw[];
+  const int Nz = g.Nz, ss = Nz + 1, NKz = g.NKz;
+  const int nseq = 3 * RP / 2;
+  cpx<R>* A = reinterpret_cast<cpx<R>*>(smem_raw);
+  cpx<R>* B = A + (size_t)nseq * ss;
+  __shared__ unsigned long long bmax;
+  const int ny = blockIdx.y, x0 = blockIdx.x * RP;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const size_t plane = (size_t)g.Nx * NKz;
+  if (tid == 0) bmax = 0ull;
+  for (int i = tid; i < nseq * ss; i += nthr) A[i] = cmk<R>(0, 0);
+  __syncthreads();
+  for (int i = tid; i < nseq * NKz; i += nthr) {
+    const int iz = i % NKz, s = i / NKz;
+    const int k0 = 2 * s, k1 = 2 * s + 1;
+    const int r0 = k0 / 3, c0 = k0 % 3, r1 = k1 / 3, c1 = k1 % 3;
+    cpx<R> ca = cmk<R>(0, 0), cb = cmk<R>(0, 0);
+    if (x0 + r0 < g.Nx) ca = X[((size_t)c0 * g.Ny + ny) * plane + (size_t)(x0 + r0) * NKz + iz];
+    if (x0 + r1 < g.Nx) cb = X[((size_t)c1 * g.Ny + ny) * plane + (size_t)(x0 + r1) * NKz + iz];
+    cpx<R>* sq = A + (size_t)s * ss;
+    if (iz == 0) {
+      sq[0] = cmk<R>(ca.x, cb.x);
+    } else {
+      sq[iz] = cmk<R>(ca.x - cb.y, ca.y + cb.x);
+      sq[Nz - iz] = cmk<R>(ca.x + cb.y, -ca.y + cb.x);
+    }
+  }
+  __syncthreads();
+  fft_batch<R>(A, B, nseq, ss, pz, twz, +1);
+  const double inv[3] = {1.0 / dx, 1.0 / dyc[ny], 1.0 / dz};
+  double m = -1e300;
+  for (int i = tid; i < RP * Nz; i += nthr) {
+    const int z = i % Nz, r = i / Nz;
+    if (x0 + r >= g.Nx) continue;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const int k = r * 3 + c;
+      const cpx<R> v = A[(size_t)(k >> 1) * ss + z];
+      const double val = (double)((k & 1) ? v.y : v.x);
+      m = fmax(m, val * inv[c]);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((tid & 31) == 0) atomicMax(&bmax, dbl_key(m));
+  __syncthreads();
+  if (tid == 0) atomicMax(out, bmax);
+}
+
+// L2Norm2 over the solved modes: one thread per (component, mode, part) line.
+__global__ void k_l2norm2(GridDev g, int N, int ncomp, const double* __restrict__ U, double* __restrict__ out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lines = 2 * g.Md;
+  double s = 0.0;
+  if (t < ncomp * lines) {
+    const int c = t / lines, l = t % lines;
+    const int m = l >> 1;
+    const size_t row = (size_t)lines;
+    const double* u = U + (size_t)c * row * N + l;
+    for (int a = 0; a < N; ++a) {
+      const double ua = u[(size_t)a * row];
+      double ps = 0.0;
+      for (int b = a % 2; b < N; b += 2) {
+        const double w = (double)(1 - a * a - b * b) /
+                         ((double)(1 + a - b) * (double)(1 - a + b) * (double)(1 + a + b) * (double)(1 - a - b));
+        ps += u[(size_t)b * row] * w;
+      }
+      s += ua * ps;
+    }
+    s *= (mode_kz(g, m) == 0) ? 1.0 : 2.0;
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0 && s != 0.0) atomicAdd(out, s);
+}
+
+template <typename R>
+cudaError_t launch_zcfl(const GridDev& g, const FftPlan& pz, const cpx<R>* twz, int RP, const cpx<R>* X,
+                        const double* dyc, double dx, double dz, unsigned long long* out, cudaStream_t st) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_zcfl<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaGetLastError();
+    attr_set = true;
+  }
+  const size_t smem = 2 * sizeof(cpx<R>) * (size_t)(3 * RP / 2) * (g.Nz + 1);
+  k_zcfl<R><<<dim3((g.Nx + RP - 1) / RP, g.Ny), 256, smem, st>>>(g, pz, twz, RP, X, dyc, dx, dz, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_l2norm2(const GridDev& g, int N, int ncomp, const double* U, double* out, cudaStream_t st) {
+  const int T = 128, total = ncomp * 2 * g.Md;
+  k_l2norm2<<<(total + T - 1) / T, T, 0, st>>>(g, N, ncomp, U, out);
+  return cudaGetLastError();
+}
+
+double cfl_key_to_double(unsigned long long k) { return key_dbl(k); }
+
+template cudaError_t launch_zcfl<float>(const GridDev&, const FftPlan&, const cpx<float>*, int, const cpx<float>*,
+                                        const double*, double, double, unsigned long long*, cudaStream_t);
+template cudaError_t launch_zcfl<double>(const GridDev&, const FftPlan&, const cpx<double>*, int,
+                                         const cpx<double>*, const double*, double, double, unsigned long long*,
+                                         cudaStream_t);
+
+// ---------------------------------------------------------------------------
+// FP64 pipe microbenchmark: the roofline denominator of the FP64 kernels.
+// k_dfma_tput: every thread runs 8 independent FMA chains (a*x + b with |a| < 1,
+// so values stay bounded); k_dfma_chain: one thread, one dependent chain.
+// ---------------------------------------------------------------------------
+__global__ void k_dfma_tput(int iters, double a, double b, double* out) {
+  double x[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) x[k] = threadIdx.x * 1e-3 + k;
+  for (int it = 0; it < iters; ++it)
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = fma(a, x[k], b);
+  double s = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += x[k];
+  if (s == 12345.678) out[0] = s;  // keeps the chains alive
+}
+
+__global__ void k_dfma_chain(int iters, double a, double b, double* out, long long* cycles) {
+  double x = threadIdx.x * 1e-3;
+  const long long t0 = clock64();
+  for (int it = 0; it < iters; ++it) x = fma(a, x, b);
+  const long long t1 = clock64();
+  out[0] = x;
+  cycles[0] = t1 - t0;
+}
+
+int measure_fp64(int device_sms, double* tflops, double* cycles_per_fma) {
+  double* d = nullptr;
+  long long* c = nullptr;
+  if (cudaMalloc(&d, sizeof(double)) != cudaSuccess) return 1;
+  if (cudaMalloc(&c, sizeof(long long)) != cudaSuccess) { cudaFree(d); return 1; }
+  const int iters = 4096, blocks = device_sms * 8, threads = 256;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  k_dfma_tput<<<blocks, threads>>>(64, 0.999, 1e-3, d);  // warm-up
+  cudaEventRecord(e0);
+  k_dfma_tput<<<blocks, threads>>>(iters, 0.999, 1e-3, d);
+  cudaEventRecord(e1);
+  cudaEventSynchronize(e1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (ms * 1e-3) / 1e12;
+  k_dfma_chain<<<1, 1>>>(iters, 0.999, 1e-3, d, c);
+  long long cyc = 0;
+  cudaMemcpy(&cyc, c, sizeof(cyc), cudaMemcpyDeviceToHost);
+  *cycles_per_fma = (double)cyc / iters;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(d);
+  cudaFree(c);
+  return cudaGetLastError() == cudaSuccess ? 0 : 1;
+}

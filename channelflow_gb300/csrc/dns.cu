@@ -401,6 +401,8 @@ struct cfgpu_dns_s {
   void *cinvA = nullptr, *cinvB = nullptr, *cfwdA = nullptr, *cfwdB = nullptr;
   void *cderA = nullptr, *cderB = nullptr, *basey = nullptr;  // fused curl: (2/L) T'_n(y_j); U, U', W, W' at y_j
   void *cdfA = nullptr, *cdfB = nullptr;                       // (2/L) diff o chebyfft, parity split
+  double* dyc = nullptr;           // CFL grid spacing in y per Gauss-Lobatto point
+  unsigned long long* dred = nullptr;  // reduction scratch (CFL key, L2 sum)
   int alt[2] = {0, 0};  // Alternating state of the main (0) and init (1) NSE: 0 = next is divergence
   // state: current fields
   double *Ucur = nullptr, *Qcur = nullptr;
@@ -890,6 +892,15 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
   CKS(dalloc(&d->dUbaseyy, Ny, B));
   CKS(dalloc(&d->dWbaseyy, Ny, B));
   CKS(dalloc(&d->ddPdx, 2, B));
+  CKS(dalloc(&d->dred, 2, B));
+  {
+    // FlowField::CFLfactor spacing (flowfield.cpp:4046-4052)
+    std::vector<double> y(Ny), dy(Ny);
+    for (int j = 0; j < Ny; ++j) y[j] = (b + a) / 2 + (b - a) / 2 * std::cos(j * M_PI / (Ny - 1));
+    for (int j = 0; j < Ny; ++j) dy[j] = (j == 0 || j == Ny - 1) ? y[0] - y[1] : (y[j - 1] - y[j + 1]) / 2.0;
+    CKS(dalloc(&d->dyc, Ny, B));
+    CK(cudaMemcpy(d->dyc, dy.data(), Ny * sizeof(double), cudaMemcpyHostToDevice));
+  }
   CK(cudaMemcpy(d->dUbase, d->Ubase.data(), Ny * sizeof(double), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(d->dWbase, d->Wbase.data(), Ny * sizeof(double), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(d->dUbaseyy, d->Ubaseyy.data(), Ny * sizeof(double), cudaMemcpyHostToDevice));
@@ -1050,7 +1061,7 @@ void dns_free(cfgpu_dns d) {
   F(d->dUbase); F(d->dWbase); F(d->dUbaseyy); F(d->dWbaseyy); F(d->ddPdx);
   F(d->hb_lo); F(d->hb_di); F(d->hb_up);
   F(d->twx); F(d->twz); F(d->cinvA); F(d->cinvB); F(d->cfwdA); F(d->cfwdB);
-  F(d->cderA); F(d->cderB); F(d->basey); F(d->cdfA); F(d->cdfB);
+  F(d->cderA); F(d->cderB); F(d->basey); F(d->cdfA); F(d->cdfB); F(d->dyc); F(d->dred);
   F(d->Ucur); F(d->Qcur);
   for (int j = 0; j < 4; ++j) { F(d->Uh[j]); F(d->Qh[j]); F(d->Nh[j]); }
   for (int w = 0; w < 2; ++w) { F(d->fj[w]); F(d->fj1[w]); F(d->rkQ[w]); }
@@ -1070,12 +1081,44 @@ void dns_free(cfgpu_dns d) {
 
 }  // namespace
 
+namespace {
+template <typename R>
+int cfl_impl(cfgpu_dns d, double* cfl) {
+  const GridDev& g = d->g;
+  if ((d->N + 1) / 2 > 56) return fail(CFGPU_ENOTSUP, "CFL needs Ny <= 111");
+  R* W = (R*)d->W6;
+  CK(launch_grad_cheb<R>(g, d->N, false, d->Ucur, W, (const R*)d->cinvA, (const R*)d->cinvB, (const R*)d->cderA,
+                         (const R*)d->cderB, (const R*)d->basey, 0.0, d->st));
+  CK(launch_xinv<R>(g, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)W, (cpx<R>*)d->X6, 3, d->st));
+  CK(cudaMemsetAsync(d->dred, 0, sizeof(unsigned long long), d->st));
+  CK(launch_zcfl<R>(g, d->pz, (const cpx<R>*)d->twz, d->RP, (const cpx<R>*)d->X6, d->dyc, g.Lx / g.Nx, g.Lz / g.Nz,
+                    d->dred, d->st));
+  d->launches += 3;
+  unsigned long long key = 0;
+  CK(cudaMemcpyAsync(&key, d->dred, sizeof(key), cudaMemcpyDeviceToHost, d->st));
+  CK(cudaStreamSynchronize(d->st));
+  const double factor = cfl_key_to_double(key);
+  const bool dxz = d->fl.dealiasing == CFGPU_DealiasXZ || d->fl.dealiasing == CFGPU_DealiasXYZ;
+  *cfl = factor * (dxz ? 2.0 * M_PI / 3.0 * d->fl.dt : M_PI * d->fl.dt);
+  return CFGPU_OK;
+}
+}  // namespace
+
 // ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------
 extern "C" {
 
 const char* cfgpu_version(void) { return "cfgpu 0.1 (sm_103a)"; }
+
+cfgpu_status cfgpu_measure_fp64(double* tflops, double* cycles_per_fma) {
+  if (!tflops || !cycles_per_fma) return fail(CFGPU_EINVAL, "null argument");
+  int dev = 0, sms = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  if (measure_fp64(sms, tflops, cycles_per_fma) != 0) return fail(CFGPU_ECUDA, "FP64 microbenchmark failed");
+  return CFGPU_OK;
+}
 const char* cfgpu_last_error(void) { return g_err.c_str(); }
 
 cfgpu_status cfgpu_flags_default(cfgpu_flags* f) {
@@ -1192,6 +1235,26 @@ cfgpu_status cfgpu_dns_device_bytes(cfgpu_dns d, long long* b) {
 cfgpu_status cfgpu_dns_kernel_launches(cfgpu_dns d, long long* n) {
   if (!d || !n) return fail(CFGPU_EINVAL, "bad argument");
   *n = d->launches;
+  return CFGPU_OK;
+}
+
+
+cfgpu_status cfgpu_dns_cfl(cfgpu_dns d, double* cfl) {
+  if (!d || !cfl) return fail(CFGPU_EINVAL, "bad argument");
+  if (d->precision == CFGPU_FP64) return cfl_impl<double>(d, cfl);
+  return cfl_impl<float>(d, cfl);
+}
+
+cfgpu_status cfgpu_dns_l2norm(cfgpu_dns d, int field, double* l2) {
+  if (!d || !l2 || (field != 0 && field != 1)) return fail(CFGPU_EINVAL, "bad argument");
+  double* out = reinterpret_cast<double*>(d->dred) + 1;
+  CK(cudaMemsetAsync(out, 0, sizeof(double), d->st));
+  CK(launch_l2norm2(d->g, d->N, field == 0 ? 3 : 1, field == 0 ? d->Ucur : d->Qcur, out, d->st));
+  d->launches++;
+  double s = 0;
+  CK(cudaMemcpyAsync(&s, out, sizeof(s), cudaMemcpyDeviceToHost, d->st));
+  CK(cudaStreamSynchronize(d->st));
+  *l2 = std::sqrt(s);
   return CFGPU_OK;
 }
 

@@ -244,7 +244,7 @@ cudaError_t launch_tau_setup(const GridDev& g, int N, double lambda_t, double nu
 // the [n][2*Md] layout; every loop prefetches a chunk of independent loads
 // before the dependent arithmetic so no load sits on a recurrence chain.
 // ---------------------------------------------------------------------------
-#define TCH 4
+#define TCH 8
 
 // parity-local line: element i <-> Chebyshev index n = 2i + q
 struct PLn {
@@ -914,18 +914,422 @@ __global__ void __launch_bounds__(32) k_tau_solve_s(GridDev g, int N, SolveParam
   }
 }
 
+// ---------------------------------------------------------------------------
+// Table-staged variant (the one launched).  As k_tau_solve_s, but before each
+// Helmholtz solve the warp copies the four UL-factor lines of its 8 modes into
+// shared memory with one burst of independent coalesced loads, so the
+// dependent sweeps read factors at shared-memory latency.  Rx and Rz, which
+// are only streamed, live in global scratch.  Shared memory per warp:
+// recurrence constants, 4 working lines per lane, 4 staged factor lines.
+// Slots: 0 = Ry then v, 1 = P, 2 and 3 = scratch.
+// ---------------------------------------------------------------------------
+struct TLn {
+  const double* p;
+  __device__ __forceinline__ double operator[](int i) const { return p[i * 16]; }
+};
+
+__device__ void helm_t(int M, int q, const double* __restrict__ hlo, const double* __restrict__ hdi,
+                       const double* __restrict__ hup, TLn band, TLn up, TLn lo, TLn inv, SLn f, SLn u, double bc) {
+  const int nM = 2 * (M - 1) + q;
+  double fi = f[M - 1], fm = f[M - 2];
+  double unext = __ldg(hlo + nM) * fm + __ldg(hdi + nM) * fi;
+  u[M - 1] = unext;
+  double acc = bc - band[M - 1] * unext;
+  double fi1 = fi;
+  fi = fm;
+  for (int i = M - 2; i >= 1; --i) {
+    const int n = 2 * i + q;
+    const double fm1 = f[i - 1];
+    const double bf = (__ldg(hlo + n) * fm1 + __ldg(hdi + n) * fi) + __ldg(hup + n) * fi1;
+    const double ui = bf - up[i] * unext;
+    u[i] = ui;
+    unext = ui;
+    acc -= band[i] * ui;
+    fi1 = fi;
+    fi = fm1;
+  }
+  double prev = acc / band[0];
+  u[0] = prev;
+  for (int i = 1; i < M; ++i) {
+    prev = (u[i] - lo[i] * prev) * inv[i];
+    u[i] = prev;
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(32) k_tau_solve_t(GridDev g, int N, SolveParams sp, SolvePtrs P, HelmB hb,
+                                                    TauTable tt) {
+  extern __shared__ double sm[];
+  const int lane = threadIdx.x;
+  const int t = blockIdx.x * 32 + lane;
+  const int Md = g.Md;
+  const bool act = (t >> 2) < Md;
+  const int m = act ? (t >> 2) : Md - 1;
+  const int mi = lane >> 2;  // mode within the warp
+  const int mbase = blockIdx.x * 8;
+  const int part = (t >> 1) & 1, q = t & 1;
+  const unsigned gmask = 0xFu << (lane & 28);
+  const int row = 2 * Md;
+  const size_t comp = (size_t)row * N;
+  const int off = 2 * m + part, poff = 2 * m + (1 - part);
+  const size_t FN = (size_t)N * Md;
+  const int M0 = (N - 1) / 2 + 1;
+  const int M = q ? (N - 1) / 2 : M0;
+  const int Nb = N - 1;
+  const double scale = 4.0 / (g.b - g.a);
+  double* ct = sm;
+  double* lines = sm + ((N + 1) & ~1);
+  double* tab = lines + (size_t)4 * M0 * 32;  // [4][N][8]
+  for (int n = lane; n < N; n += 32) ct[n] = scale * (n + 1);
+  __syncwarp();
+  auto S = [&](int slot) { return SLn{lines + (size_t)slot * M0 * 32 + lane}; };
+  auto So = [&](int slot) { return SLn{lines + (size_t)slot * M0 * 32 + (lane ^ 1)}; };
+  auto Sp = [&](int slot) { return SLn{lines + (size_t)slot * M0 * 32 + (lane ^ 2)}; };
+  auto G = [&](const double* base) { return PLn{const_cast<double*>(base) + off + q * row, 2 * row}; };
+  auto Go = [&](const double* base) { return PLn{const_cast<double*>(base) + off + (1 - q) * row, 2 * row}; };
+  auto Gp = [&](const double* base) { return PLn{const_cast<double*>(base) + poff + q * row, 2 * row}; };
+  auto TB = [&](int f) { return PLn{tt.f + f * FN + m + q * Md, 2 * Md}; };
+  auto TS = [&](int k) { return TLn{tab + ((size_t)k * N + q) * 8 + mi}; };
+  // stage factor fields f0..f3 of this warp's 8 modes into tab
+  auto stage = [&](int f0) {
+    __syncwarp();
+    const int total = 4 * N * 8;
+    for (int b0 = lane; b0 < total; b0 += 32 * 16) {
+      double v[16];
+#pragma unroll
+      for (int k2 = 0; k2 < 16; ++k2) {
+        const int idx = b0 + 32 * k2;
+        v[k2] = 0.0;
+        if (idx < total) {
+          const int k = idx / (N * 8), rem = idx - k * N * 8;
+          const int n = rem >> 3, mm = mbase + (rem & 7);
+          if (mm < Md) v[k2] = __ldg(&tt.f[(size_t)(f0 + k) * FN + (size_t)n * Md + mm]);
+        }
+      }
+#pragma unroll
+      for (int k2 = 0; k2 < 16; ++k2)
+        if (b0 + 32 * k2 < total) tab[b0 + 32 * k2] = v[k2];
+    }
+    __syncwarp();
+  };
+  double* Rxg = P.scratch;          // global scratch lines for Rx and Rz
+  double* Rzg = P.scratch + comp;
+  const int kx = mode_kx(g, m), kz = mode_kz(g, m);
+  const bool m00 = (kx == 0 && kz == 0);
+  const double kxL = 2 * M_PI * kx / g.Lx;
+  const double kzL = 2 * M_PI * kz / g.Lz;
+  const double nu = sp.nu;
+  const double lambda = tt.s[TS_LAMBDA * Md + m];
+  const double* __restrict__ hlo = hb.lo;
+  const double* __restrict__ hdi = hb.di;
+  const double* __restrict__ hup = hb.up;
+
+  // ---- A: right-hand side -------------------------------------------------
+  if (sp.kind == 0) {
+    PLn outx = G(Rxg), outz = G(Rzg);
+    SLn outy = S(0);
+    for (int c = 0; c < 3; ++c) {
+      for (int i0 = 0; i0 < M; i0 += TCH) {
+        double acc[TCH];
+#pragma unroll
+        for (int k = 0; k < TCH; ++k) acc[k] = 0.0;
+        for (int j = 0; j < sp.order; ++j) {
+          const double* uj = P.uin[j] + c * comp;
+          const R* nj = static_cast<const R*>(P.nin[j]) + c * comp;
+          double uv[TCH], nv[TCH];
+#pragma unroll
+          for (int k = 0; k < TCH; ++k)
+            if (i0 + k < M) {
+              const size_t o = (size_t)(2 * (i0 + k) + q) * row + off;
+              uv[k] = __ldg(uj + o);
+              nv[k] = (double)__ldg(nj + o);
+            }
+#pragma unroll
+          for (int k = 0; k < TCH; ++k)
+            if (i0 + k < M) acc[k] += sp.a[j] * uv[k] + sp.b[j] * nv[k];
+        }
+#pragma unroll
+        for (int k = 0; k < TCH; ++k)
+          if (i0 + k < M) {
+            const int i = i0 + k, n = 2 * i + q;
+            double a = acc[k];
+            if (m00 && part == 0 && c != 1) {
+              a += nu * (c == 0 ? P.Ubaseyy[n] : P.Wbaseyy[n]);
+              if (n == 0 && sp.constraint == 0) a -= (c == 0 ? sp.dPdxRef : sp.dPdzRef);
+            }
+            if (c == 1) outy[i] = a;
+            else if (act) (c == 0 ? outx : outz)[i] = a;
+          }
+      }
+    }
+  } else {
+    const double kappa2 = 4 * M_PI * M_PI * ((kx / g.Lx) * (kx / g.Lx) + (kz / g.Lz) * (kz / g.Lz));
+    const double Dx = 2 * M_PI * kx / g.Lx * (kx == g.kxmax ? 0.0 : 1.0);
+    const double Dz = 2 * M_PI * kz / g.Lz * (kz == g.kzmax ? 0.0 : 1.0);
+    for (int c = 0; c < 3; ++c) {
+      PLn uc = G(P.uin[0] + c * comp);
+      PLn uo = Go(P.uin[0] + c * comp);
+      SLn d1 = S(2);
+      __syncwarp(gmask);
+      double s = 0.0;
+      {
+        double dn2 = 0.0;
+        int i = M - 1;
+        if (q == 0) {
+          const double v = dn2 + ct[2 * i] * 0.0;
+          d1[i] = v;
+          s += v;
+          dn2 = v;
+          i--;
+        }
+        for (; i >= 0; i -= TCH) {
+          double xv[TCH];
+#pragma unroll
+          for (int k = 0; k < TCH; ++k)
+            if (i - k >= 0) xv[k] = uo[i - k + q];
+#pragma unroll
+          for (int k = 0; k < TCH; ++k)
+            if (i - k >= 0) {
+              const int n = 2 * (i - k) + q;
+              double v = dn2 + ct[n] * (nu * xv[k]);
+              dn2 = v;
+              if (n == 0) v *= 0.5;
+              d1[i - k] = v;
+              s += v;
+            }
+        }
+      }
+      const double so = __shfl_xor_sync(gmask, s, 1);
+      double wall = 0.0;
+      if (m00 && part == 0 && sp.constraint == 1 && c != 1) {
+        const double s0 = q == 0 ? s : so, s1 = q == 0 ? so : s;
+        wall = ((s0 + s1) - (s0 - s1)) / (g.b - g.a);
+      }
+      __syncwarp(gmask);
+      SLn d1o = So(2);
+      PLn qo = Go(P.qin);
+      PLn qp = Gp(P.qin);
+      PLn outg = G(c == 0 ? Rxg : Rzg);
+      SLn outs = S(0);
+      const R* Nj = static_cast<const R*>(P.nin[0]) + c * comp + off + q * row;
+      const R* Nj1 = sp.kind == 1 ? static_cast<const R*>(P.nin[1]) + c * comp + off + q * row : nullptr;
+      R* Q = sp.kind == 2 ? static_cast<R*>(P.Q) + c * comp + off + q * row : nullptr;
+      const double kD = c == 0 ? Dx : Dz;
+      double d2n2 = 0.0, dqn2 = 0.0;
+      for (int i0 = M - 1; i0 >= 0; i0 -= TCH) {
+        // prefetch the streamed inputs of TCH consecutive (descending) elements
+        double uv[TCH], qv[TCH], nv[TCH], n1v[TCH];
+#pragma unroll
+        for (int k = 0; k < TCH; ++k) {
+          const int i = i0 - k;
+          if (i >= 0) {
+            const int n = 2 * i + q;
+            uv[k] = uc[i];
+            qv[k] = c == 1 ? ((n + 1 <= Nb) ? qo[i + q] : 0.0) : qp[i];
+            nv[k] = (double)Nj[(size_t)i * 2 * row];
+            n1v[k] = sp.kind == 1 ? (double)Nj1[(size_t)i * 2 * row] : (double)Q[(size_t)i * 2 * row];
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < TCH; ++k) {
+          const int i = i0 - k;
+          if (i < 0) break;
+          const int n = 2 * i + q;
+          const double x1 = (n + 1 <= Nb) ? d1o[i + q] : 0.0;
+          double d2 = d2n2 + ct[n] * x1;
+          d2n2 = d2;
+          if (n == 0) d2 *= 0.5;
+          double gq;
+          if (c == 1) {
+            double dq = dqn2 + ct[n] * qv[k];
+            dqn2 = dq;
+            if (n == 0) dq *= 0.5;
+            gq = dq;
+          } else {
+            gq = part == 0 ? -(kD * qv[k]) : kD * qv[k];
+          }
+          const double u0 = uv[k];
+          double L = d2 - kappa2 * (nu * u0) - gq;
+          if (m00 && part == 0 && c != 1) {
+            L += nu * (c == 0 ? P.Ubaseyy[n] : P.Wbaseyy[n]);
+            if (n == 0) L -= sp.constraint == 0 ? (c == 0 ? sp.dPdxRef : sp.dPdzRef)
+                                                : wall + sp.baseShear[c == 0 ? 0 : 1];
+          }
+          const double nj = nv[k];
+          double rhs;
+          if (sp.kind == 1) {
+            rhs = (u0 * sp.lam + sp.a_b * L) + ((-sp.g_b) * nj + (-sp.z_b) * n1v[k]);
+          } else {
+            const double Qn = n1v[k] * sp.rkA - nj;
+            if (act) Q[(size_t)i * 2 * row] = (R)Qn;
+            rhs = L + (sp.lam * u0 + sp.B_C * Qn);
+          }
+          if (m00 && part == 0 && c != 1) {
+            rhs += nu * (c == 0 ? P.Ubaseyy[n] : P.Wbaseyy[n]);
+            if (n == 0 && sp.constraint == 0) rhs -= (c == 0 ? sp.dPdxRef : sp.dPdzRef);
+          }
+          if (c == 1) outs[i] = rhs;
+          else if (act) outg[i] = rhs;
+        }
+      }
+    }
+  }
+  __syncwarp(gmask);
+  __threadfence_block();
+
+  // ---- B: pressure ---------------------------------------------------------
+  stage(TF_PBAND);
+  {
+    SLn rr = S(2);
+    diff_s(M, q, ct, So(0), &rr);
+    PLn Rxp = Gp(Rxg), Rzp = Gp(Rzg);
+    for (int i = 0; i < M; i += TCH) {
+      double xa[TCH], za[TCH];
+#pragma unroll
+      for (int k = 0; k < TCH; ++k)
+        if (i + k < M) {
+          xa[k] = Rxp[i + k];
+          za[k] = Rzp[i + k];
+        }
+#pragma unroll
+      for (int k = 0; k < TCH; ++k)
+        if (i + k < M) {
+          const double x = kxL * xa[k] + kzL * za[k];
+          rr[i + k] = part == 0 ? rr[i + k] - x : rr[i + k] + x;
+        }
+    }
+    helm_t(M, q, hlo, hdi, hup, TS(0), TS(1), TS(2), TS(3), rr, S(1), 0.0);
+  }
+  stage(TF_VBAND);
+  // ---- C: wall-normal velocity, influence and tau corrections -------------
+  SLn Pl = S(1), Vl = S(0);
+  const double RyTop = S(0)[M - 1];
+  if (m00) {
+    for (int i = 0; i < M; ++i) Vl[i] = 0.0;
+  } else {
+    SLn tmp = S(3);
+    diff_s(M, q, ct, So(1), &tmp);
+    SLn Ry = S(0);
+    for (int i = 0; i < M; ++i) tmp[i] -= Ry[i];
+    helm_t(M, q, hlo, hdi, hup, TS(0), TS(1), TS(2), TS(3), tmp, Vl, 0.0);
+  }
+  __syncwarp(gmask);
+  {
+    const double s = m00 ? 0.0 : diff_s(M, q, ct, So(0), nullptr);
+    const double so = __shfl_xor_sync(gmask, s, 1);
+    const double s0 = q == 0 ? s : so, s1 = q == 0 ? so : s;
+    const double plus = s0 + s1, minus = s0 - s1;
+    const double* sc = tt.s + m;
+    const double i00 = sc[TS_I00 * Md], i01 = sc[TS_I01 * Md], i10 = sc[TS_I10 * Md], i11 = sc[TS_I11 * Md];
+    const double dp = -i00 * plus - i01 * minus;
+    const double dm = -i10 * plus - i11 * minus;
+    PLn Pp = TB(TF_PP), Vp = TB(TF_VP), Pm = TB(TF_PM), Vm = TB(TF_VM);
+    if (!m00)
+      for (int i = 0; i < M; i += TCH) {
+        double a[TCH], b[TCH], c2[TCH], d[TCH];
+#pragma unroll
+        for (int k = 0; k < TCH; ++k)
+          if (i + k < M) {
+            a[k] = Pp[i + k];
+            b[k] = Pm[i + k];
+            c2[k] = Vp[i + k];
+            d[k] = Vm[i + k];
+          }
+#pragma unroll
+        for (int k = 0; k < TCH; ++k)
+          if (i + k < M) {
+            Pl[i + k] += dp * a[k] + dm * b[k];
+            Vl[i + k] += dp * c2[k] + dm * d[k];
+          }
+      }
+    const int itop = M - 1;
+    double x0 = 0.0, y0 = 0.0;
+    if (!m00) {
+      x0 = lambda * Vl[itop] - nu * 0.0 - RyTop;
+      y0 = q == 0 ? ct[Nb - 1] * Pl[itop] : 0.0;
+    }
+    const double ox = __shfl_xor_sync(gmask, x0, 1);
+    const double oy = __shfl_xor_sync(gmask, y0, 1);
+    if (!m00 && sp.taucorrection) {
+      const double s1Nb = (q == 0 ? x0 : ox) + 0.0;
+      const double s1Nb1 = q == 0 ? ox + y0 : x0 + oy;
+      const double sNb = s1Nb / (1.0 - sc[TS_S0NB * Md]);
+      const double sNb1 = s1Nb1 / (1.0 - sc[TS_S0NB1 * Md]);
+      PLn P0 = TB(TF_P0), V0 = TB(TF_V0);
+      const double fP = q == 0 ? sNb1 : sNb, fV = q == 0 ? sNb : sNb1;
+      for (int i = 0; i < M; i += TCH) {
+        double a[TCH], b[TCH];
+#pragma unroll
+        for (int k = 0; k < TCH; ++k)
+          if (i + k < M) {
+            a[k] = P0[i + k];
+            b[k] = V0[i + k];
+          }
+#pragma unroll
+        for (int k = 0; k < TCH; ++k)
+          if (i + k < M) {
+            Pl[i + k] += fP * a[k];
+            Vl[i + k] += fV * b[k];
+          }
+      }
+    }
+  }
+  __syncwarp(gmask);
+  // ---- D: streamwise and spanwise velocity -------------------------------
+  SLn Ppt = Sp(1);
+  const bool zero_im = m00 && part == 1 && sp.force_real00;
+  for (int c = 0; c < 2; ++c) {
+    const double kL = c == 0 ? kxL : kzL;
+    PLn Rc = G(c == 0 ? Rxg : Rzg);
+    SLn r = S(2), o = S(3);
+    for (int i = 0; i < M; i += TCH) {
+      double rv[TCH];
+#pragma unroll
+      for (int k = 0; k < TCH; ++k)
+        if (i + k < M) rv[k] = Rc[i + k];
+#pragma unroll
+      for (int k = 0; k < TCH; ++k)
+        if (i + k < M) r[i + k] = part == 0 ? -(kL * Ppt[i + k]) - rv[k] : kL * Ppt[i + k] - rv[k];
+    }
+    helm_t(M, q, hlo, hdi, hup, TS(0), TS(1), TS(2), TS(3), r, o, 0.0);
+    if (m00 && sp.constraint == 1 && part == 0) {
+      if (q == 0) {
+        double amean = o[0];
+        for (int i = 1; i < M; ++i) amean -= o[i] / (double)((2 * i) * (2 * i) - 1);
+        const double ucmean = tt.s[TS_UCMEAN * Md + m];
+        const double target = c == 0 ? sp.umean : sp.wmean;
+        const double mu = nu * (target - amean) / ucmean;
+        r[0] = r[0] + mu;
+        helm_t(M, q, hlo, hdi, hup, TS(0), TS(1), TS(2), TS(3), r, o, 0.0);
+        if (act && P.dPdx_out) P.dPdx_out[c] = mu;
+      }
+    }
+    if (act) {
+      PLn gout = G(P.uout + (c == 0 ? 0 : 2) * comp);
+      for (int i = 0; i < M; ++i) gout[i] = zero_im ? 0.0 : o[i];
+    }
+  }
+  if (act) {
+    PLn gq = G(P.qout), gv = G(P.uout + comp);
+    for (int i = 0; i < M; ++i) {
+      gq[i] = zero_im ? 0.0 : Pl[i];
+      gv[i] = zero_im ? 0.0 : Vl[i];
+    }
+  }
+}
+
 template <typename R>
 cudaError_t launch_tau_solve(const GridDev& g, int N, const SolveParams& sp, const SolvePtrs& p, const HelmB& hb,
                              TauTable tt, cudaStream_t st) {
   const int M0 = (N - 1) / 2 + 1;
-  const size_t smem = sizeof(double) * (((N + 1) & ~1) + (size_t)6 * M0 * 32);
-  if (smem <= 227 * 1024) {
+  const size_t smem_t = sizeof(double) * (((N + 1) & ~1) + (size_t)4 * M0 * 32 + (size_t)4 * N * 8);
+  if (smem_t <= 227 * 1024) {
     static bool attr = false;
     if (!attr) {
-      cudaFuncSetAttribute(k_tau_solve_s<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+      cudaFuncSetAttribute(k_tau_solve_t<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
       attr = true;
     }
-    k_tau_solve_s<R><<<(4 * g.Md + 31) / 32, 32, smem, st>>>(g, N, sp, p, hb, tt);
+    k_tau_solve_t<R><<<(4 * g.Md + 31) / 32, 32, smem_t, st>>>(g, N, sp, p, hb, tt);
     return cudaGetLastError();
   }
   const int T = 64;

@@ -156,6 +156,18 @@ class DNS:
         L.check(self._lib.cfgpu_dns_dPdx(self._h, C.byref(v)))
         return v.value
 
+    def CFL(self) -> float:
+        """DNS::CFL of the current velocity (dnsalgo.cpp:63-67)."""
+        v = C.c_double()
+        L.check(self._lib.cfgpu_dns_cfl(self._h, C.byref(v)))
+        return v.value
+
+    def l2norm(self, field: int = 0) -> float:
+        """L2Norm (normalize=true) of the current u (field 0) or q (field 1)."""
+        v = C.c_double()
+        L.check(self._lib.cfgpu_dns_l2norm(self._h, int(field), C.byref(v)))
+        return v.value
+
     def base(self):
         U = np.zeros(self.grid.Ny)
         W = np.zeros(self.grid.Ny)

@@ -106,6 +106,17 @@ cfgpu_status cfgpu_dns_reset_dt(cfgpu_dns dns, double dt);
 cfgpu_status cfgpu_dns_time(cfgpu_dns dns, double* t);
 cfgpu_status cfgpu_dns_dPdx(cfgpu_dns dns, double* dPdx);
 
+/*
+ * DNS::CFL(u) (channelflow/dnsalgo.cpp:63-67 with FlowField::CFLfactor,
+ * flowfield.cpp:4035-4068) of the current velocity: the signed maximum over
+ * grid points and components of (u_i + U_i)/dx_i, times 2 pi/3 dt with
+ * DealiasXZ (pi dt otherwise).  Needs Ny <= 111.
+ */
+cfgpu_status cfgpu_dns_cfl(cfgpu_dns dns, double* cfl);
+
+/* L2Norm(field, normalize=true) (channelflow/diffops.cpp:415-487) of the current u (field 0) or q (field 1). */
+cfgpu_status cfgpu_dns_l2norm(cfgpu_dns dns, int field, double* l2);
+
 /* Base flow Chebyshev coefficients (NSE::Ubase/Wbase, channelflow/nse.cpp:766-767); Ny doubles each. */
 cfgpu_status cfgpu_dns_base(cfgpu_dns dns, double* Ubase, double* Wbase);
 
@@ -172,6 +183,14 @@ cfgpu_status cfgpu_tau_solve_batched_noalloc(int N, int nmodes, const int* kx, c
                                              double a, double b, double lambda_t, double nu, int taucorrection,
                                              const double* Rx, const double* Ry, const double* Rz, double* u,
                                              double* v, double* w, double* P);
+
+/*
+ * FP64 microbenchmark of the current device (no reference counterpart):
+ * sustained FMA throughput in TFLOP/s (8 independent chains per thread, 8
+ * blocks per SM) and the latency of one dependent FMA chain in cycles.  The
+ * FP64 kernels' roofline denominator.
+ */
+cfgpu_status cfgpu_measure_fp64(double* tflops, double* cycles_per_fma);
 
 /* Library version string. */
 const char* cfgpu_version(void);

@@ -1218,3 +1218,19 @@ def load_io_field(phys_io: np.ndarray, Nx: int, Nz: int) -> np.ndarray:
     out[:, :, Nx_io // 2 + 1 + (Nx - Nx_io): Nx, :Mz_io] = c[:, :, Nx_io // 2 + 1:, :]
     out *= 1.0 / (Nx_io * Nz_io)
     return chebyfft(out, axis=1)
+
+
+def cfl_factor(u: np.ndarray, g: Grid, Ubase: np.ndarray, Wbase: np.ndarray) -> float:
+    """FlowField::CFLfactor(Ubase, Wbase) (flowfield.cpp:4035-4068): signed max of (u_i + U_i)/dx_i."""
+    up = make_physical(u, g)
+    Ub = ichebyfft(Ubase)
+    Wb = ichebyfft(Wbase)
+    y = chebypoints(g.Ny, g.a, g.b)
+    dx = [g.Lx / g.Nx, None, g.Lz / g.Nz]
+    cfl = 0.0
+    for i in range(3):
+        for ny in range(g.Ny):
+            d = dx[i] if i != 1 else ((y[0] - y[1]) if ny in (0, g.Ny - 1) else (y[ny - 1] - y[ny + 1]) / 2.0)
+            Ui = Ub[ny] if i == 0 else (Wb[ny] if i == 2 else 0.0)
+            cfl = max(cfl, float(np.max((up[i, ny] + Ui) / d)))
+    return cfl

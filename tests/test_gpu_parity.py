@@ -166,3 +166,16 @@ def test_resident_path_equals_host_path():
     dns.advance_resident(12)
     dns.get_fields(u, q)
     assert np.array_equal(u, a)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed", 1e-5)])
+def test_cfl_and_l2norm_match_oracle(precision, tol):
+    g = O.Grid(24, 33, 24, *COUETTE_BOX)
+    fl = O.DNSFlags(nu=1 / 400, dt=0.02, baseflow=O.LaminarBase, ulowerwall=-1.0, uupperwall=1.0)
+    u0 = O.random_divfree_field(g, seed=21, norm=0.2)
+    gu, gq, dns = gpu_run(u0, g, fl, 3, precision=precision)
+    nse = O.NSE(g, fl)
+    ref = O.cfl_factor(gu, g, nse.Ubase, nse.Wbase) * (2 * math.pi / 3 * fl.dt)
+    assert abs(dns.CFL() - ref) <= tol * ref
+    assert abs(dns.l2norm(0) - O.L2Norm(gu, g)) <= 1e-12 * O.L2Norm(gu, g)
+    assert abs(dns.l2norm(1) - O.L2Norm(gq, g)) <= 1e-12 * max(O.L2Norm(gq, g), 1e-300)
