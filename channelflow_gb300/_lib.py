@@ -30,6 +30,10 @@ class Flags(C.Structure):
                                        "dealiasing", "taucorrection")]
 
 
+class TimeStepC(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("dt", "dtmin", "dtmax", "dT", "CFLmin", "CFLmax")] + [("variable", C.c_int)]
+
+
 class CfgpuError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__("cfgpu error %d: %s" % (code, msg))
@@ -57,6 +61,9 @@ _SIGS = {
     "cfgpu_dns_destroy": [C.c_void_p],
     "cfgpu_dns_cfl": [C.c_void_p, _PD],
     "cfgpu_measure_fp64": [_PD, _PD],
+    "cfgpu_timestep_adjust_for_T": [C.c_void_p, C.c_double, _PI, _PI, _PD],
+    "cfgpu_timestep_adjust": [C.c_void_p, C.c_double, _PI, _PI],
+    "cfgpu_ft": [C.POINTER(Grid), C.POINTER(Flags), C.POINTER(TimeStepC), C.c_double, _PD, _PD, _PD, C.c_int],
     "cfgpu_dns_l2norm": [C.c_void_p, C.c_int, _PD],
     "cfgpu_dns_advance_timed": [C.c_void_p, C.c_int, _PD],
     "cfgpu_dns_set_profiling": [C.c_void_p, C.c_int],

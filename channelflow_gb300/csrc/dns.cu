@@ -9,6 +9,7 @@
 //   * work arrays of the nonlinear-term pipeline.
 // Scheme logic follows channelflow/dnsalgo.cpp (MultistepDNS, CNABstyleDNS,
 // RungeKuttaDNS) and the DNS facade channelflow/dns.cpp:22-163.
+#include <climits>
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -1105,6 +1106,73 @@ int cfl_impl(cfgpu_dns d, double* cfl) {
 }  // namespace
 
 // ---------------------------------------------------------------------------
+// TimeStep (channelflow/dnsflags.cpp:736-972): dt within [dtmin, dtmax] with
+// dT = n dt, CFL kept within [CFLmin, CFLmax] by adjust(); same arithmetic.
+// ---------------------------------------------------------------------------
+namespace {
+inline int iround_h(double x) { return int(x > 0.0 ? x + 0.5 : x - 0.5); }
+
+struct TimeStepH {
+  int n = 0, N = 0;
+  double dt = 0, dtmin = 0, dtmax = 0, dT = 0, T = 0, CFLmin = 0, CFL = 0, CFLmax = 0;
+  bool variable = false;
+  double value() const { return dT / n; }  // TimeStep::operator Real
+
+  int init(const cfgpu_timestep& t) {
+    dt = t.dt; dtmin = t.dtmin; dtmax = t.dtmax; dT = t.dT; CFLmin = t.CFLmin; CFLmax = t.CFLmax;
+    variable = t.variable != 0;
+    CFL = (CFLmax + CFLmin) / 2;
+    if (dtmin < 0 || dt < dtmin || dtmax < dt) return fail(CFGPU_EINVAL, "TimeStep: 0 <= dtmin <= dt <= dtmax");
+    if (CFLmin < 0 || CFLmax < CFLmin) return fail(CFGPU_EINVAL, "TimeStep: 0 <= CFLmin <= CFLmax");
+    if (dT < dtmin) return fail(CFGPU_EINVAL, "TimeStep: dT < dtmin");
+    n = std::max(iround_h(dT / dt), 1);
+    dt = dT / n;
+    while (dt < dtmin && n >= 2 && dT != 0) dt = dT / --n;
+    while (dt > dtmax && n <= INT_MAX && dT != 0) dt = dT / ++n;
+    return CFGPU_OK;
+  }
+  bool adjust(double c) {
+    CFL = c;
+    if (variable && (c <= CFLmin || c >= CFLmax)) return adjust_to_middle(c);
+    return false;
+  }
+  bool adjust_to_middle(double c) {
+    if (dtmin == dtmax || dT == 0.0) return false;
+    int nn = std::max(iround_h(2 * n * c / (CFLmax + CFLmin)), 1);
+    double d = dT / nn;
+    while (d < dtmin && d < dT) d = dT / --nn;
+    while (d > dtmax && nn <= INT_MAX) d = dT / ++nn;
+    c *= d / dt;
+    const bool adj = nn != n;
+    if (adj) {
+      n = nn;
+      dt = d;
+      CFL = c;
+    }
+    return adj;
+  }
+  bool adjust_for_T(double TT) {
+    T = TT;
+    if (TT == 0) {
+      const bool adj = dt != 0;
+      dt = 0; n = 0; dT = 0; T = 0;
+      return adj;
+    }
+    const int NN = std::max(iround_h(TT / dT), 1);
+    const double dTT = TT / NN;
+    int nn = std::max(iround_h(dTT / dt), 1);
+    double d = dTT / nn;
+    while (d < dtmin && nn > 2 && dTT != 0) d = dTT / --nn;
+    while (d > dtmax && nn <= INT_MAX && dTT != 0) d = dTT / ++nn;
+    const double c = d * CFL / dt;
+    const bool adj = d != dt;
+    n = nn; N = NN; dt = d; dT = dTT; CFL = c;
+    return adj;
+  }
+};
+}  // namespace
+
+// ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------
 extern "C" {
@@ -1298,6 +1366,82 @@ cfgpu_status cfgpu_dns_phase_times(cfgpu_dns d, double* nl_ms, long long* nl_cou
   if (nl_count) *nl_count = n[0];
   if (tau_ms) *tau_ms = t[1];
   if (tau_count) *tau_count = n[1];
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_timestep_adjust_for_T(cfgpu_timestep* ts, double T, int* n, int* N, double* dt) {
+  if (!ts || T < 0) return fail(CFGPU_EINVAL, "bad argument");
+  TimeStepH h;
+  CKS(h.init(*ts));
+  h.adjust_for_T(T);
+  ts->dt = h.dt;
+  ts->dT = h.dT;
+  if (n) *n = h.n;
+  if (N) *N = h.N;
+  if (dt) *dt = h.value();
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_timestep_adjust(cfgpu_timestep* ts, double cfl, int* n, int* adjusted) {
+  if (!ts) return fail(CFGPU_EINVAL, "bad argument");
+  TimeStepH h;
+  CKS(h.init(*ts));
+  const int adj = h.adjust(cfl) ? 1 : 0;
+  ts->dt = h.dt;
+  if (n) *n = h.n;
+  if (adjusted) *adjusted = adj;
+  return CFGPU_OK;
+}
+
+// f^T(u): cfDSI's f(u, T, ...) without a Poincare section (channelflow/cfdsi.cpp:705-775).
+cfgpu_status cfgpu_ft(const cfgpu_grid* grid, const cfgpu_flags* flags, const cfgpu_timestep* timestep, double T,
+                      const double* u, double* fu, double* cfl_out, int precision) {
+  if (!grid || !flags || !timestep || !u || !fu) return fail(CFGPU_EINVAL, "null argument");
+  const size_t ncplx = 3 * (size_t)grid->Ny * grid->Nx * (grid->Nz / 2 + 1);
+  for (size_t i = 0; i < 2 * ncplx; ++i)
+    if (!std::isfinite(u[i])) return fail(CFGPU_ENONFINITE, "f: u is not finite");
+  memcpy(fu, u, 2 * ncplx * sizeof(double));
+  if (T < 0) {
+    for (size_t i = 0; i < 2 * ncplx; ++i) fu[i] *= 1 + std::fabs(T);
+    return CFGPU_OK;
+  }
+  if (T == 0) return CFGPU_OK;
+  TimeStepH dt;
+  CKS(dt.init(*timestep));
+  dt.adjust_for_T(T);
+  cfgpu_flags fl = *flags;
+  fl.dt = dt.value();
+  std::vector<double> q((size_t)2 * grid->Ny * grid->Nx * (grid->Nz / 2 + 1), 0.0);
+  cfgpu_dns d = nullptr;
+  CKS(cfgpu_dns_create(grid, &fl, nullptr, nullptr, u, precision, &d));
+  int st = CFGPU_OK;
+  double cfl = 0;
+  do {
+    if ((st = set_fields(d, fu, q.data())) != CFGPU_OK) break;
+    if (dt.variable) {
+      // one step to measure the CFL number, then restart from u with the adjusted dt
+      if ((st = dns_advance_device(d, 1)) != CFGPU_OK) break;
+      if ((st = cfgpu_dns_cfl(d, &cfl)) != CFGPU_OK) break;
+      dt.adjust(cfl);
+      if ((st = cfgpu_dns_reset_dt(d, dt.value())) != CFGPU_OK) break;
+      if ((st = set_fields(d, u, nullptr)) != CFGPU_OK) break;
+    }
+    for (int s = 1; s <= dt.N; ++s) {
+      if ((st = cfgpu_dns_cfl(d, &cfl)) != CFGPU_OK) break;
+      if ((st = dns_advance_device(d, dt.n)) != CFGPU_OK) break;
+      if (dt.variable && dt.adjust(cfl))
+        if ((st = cfgpu_dns_reset_dt(d, dt.value())) != CFGPU_OK) break;
+    }
+    if (st != CFGPU_OK) break;
+    st = get_fields(d, fu, q.data());
+  } while (false);
+  std::string keep = g_err;
+  cfgpu_dns_destroy(d);
+  g_err = keep;
+  if (st != CFGPU_OK) return st;
+  for (size_t i = 0; i < 2 * ncplx; ++i)
+    if (!std::isfinite(fu[i])) return fail(CFGPU_ENONFINITE, "f: f^T(u) is not finite");
+  if (cfl_out) *cfl_out = cfl;
   return CFGPU_OK;
 }
 

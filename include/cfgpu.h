@@ -70,6 +70,13 @@ typedef struct cfgpu_flags {
 
 typedef struct cfgpu_dns_s* cfgpu_dns;
 
+/* TimeStep parameters (channelflow/dnsflags.h:166-198): dt within [dtmin, dtmax], dT = n dt the CFL-check
+ * interval, CFL kept within [CFLmin, CFLmax] when variable != 0. */
+typedef struct cfgpu_timestep {
+  double dt, dtmin, dtmax, dT, CFLmin, CFLmax;
+  int variable;
+} cfgpu_timestep;
+
 /* DNSFlags() defaults (channelflow/dnsflags.h:84-92, dnsflags.cpp:110-158). */
 cfgpu_status cfgpu_flags_default(cfgpu_flags* flags);
 
@@ -144,6 +151,31 @@ cfgpu_status cfgpu_dns_advance_timed(cfgpu_dns dns, int nsteps, double* ms);
 cfgpu_status cfgpu_dns_set_profiling(cfgpu_dns dns, int enable);
 cfgpu_status cfgpu_dns_phase_times(cfgpu_dns dns, double* nl_ms, long long* nl_count, double* tau_ms,
                                    long long* tau_count);
+
+/*
+ * TimeStep::adjust_for_T (channelflow/dnsflags.cpp:912-965): fits dT and dt to the horizon T; returns
+ * n (steps per dT), N (dT intervals) and dt = dT/n, and updates ts->dt, ts->dT.
+ */
+cfgpu_status cfgpu_timestep_adjust_for_T(cfgpu_timestep* ts, double T, int* n, int* N, double* dt);
+
+/*
+ * TimeStep::adjust(CFL) (channelflow/dnsflags.cpp:811-859): when variable and CFL is outside
+ * [CFLmin, CFLmax], moves dt = dT/n so that the CFL number returns to the middle of the range;
+ * updates ts->dt, returns n and whether it changed.
+ */
+cfgpu_status cfgpu_timestep_adjust(cfgpu_timestep* ts, double cfl, int* n, int* adjusted);
+
+/*
+ * f^T(u): the time-T map used by the Newton-Krylov, Arnoldi and continuation
+ * drivers, cfDSI's f(u, T, ...) without a Poincare section
+ * (channelflow/cfdsi.cpp:705-775): adjust dt to T, build a DNS, optionally
+ * probe the CFL number with one step and restart from u with the adjusted dt,
+ * then advance N intervals of n steps, adjusting dt from the CFL number of
+ * each interval when timestep->variable.  u and fu are velocity buffers in
+ * the FlowField layout; the final CFL number is returned in *cfl (may be null).
+ */
+cfgpu_status cfgpu_ft(const cfgpu_grid* grid, const cfgpu_flags* flags, const cfgpu_timestep* timestep, double T,
+                      const double* u, double* fu, double* cfl, int precision);
 
 /*
  * Batched TauSolver (channelflow/tausolver.cpp:81-176 constructor and

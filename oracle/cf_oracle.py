@@ -947,6 +947,12 @@ class MultistepDNS:
     def full(self):
         return self.countdown == 0
 
+    def reset_dt(self, dt):
+        """MultistepDNS::reset_dt (dnsalgo.cpp:191-200): new lambda, initialisation starts over."""
+        self.flags.dt = dt
+        self.nse.reset_lambda([self.eta / dt])
+        self.countdown = self.Ninitsteps
+
     def _shift(self):
         for j in range(self.order - 1, 0, -1):
             self.nonlf[j], self.nonlf[j - 1] = self.nonlf[j - 1], self.nonlf[j]
@@ -1007,6 +1013,14 @@ class CNABstyleDNS:
     def full(self):
         return self._full
 
+    def reset_dt(self, dt):
+        """CNABstyleDNS::reset_dt (dnsalgo.cpp:588-606): CNAB2 re-takes its forward-Euler start."""
+        self.flags.dt = dt
+        self.lambda_t = [1.0 / (b * dt) for b in self.beta]
+        self.nse.reset_lambda(self.lambda_t)
+        if self.flags.timestepping == CNAB2:
+            self._full = False
+
     def push(self, u, q):
         """Returns the caller's u after the in-place transform round trip of nonlinear()."""
         self.fj, self.fj1 = self.fj1, self.fj
@@ -1050,6 +1064,12 @@ class RungeKuttaDNS:
 
     def full(self):
         return True
+
+    def reset_dt(self, dt):
+        """RungeKuttaDNS::reset_dt (dnsalgo.cpp:407-417)."""
+        self.flags.dt = dt
+        self.lambda_t = [1.0 / (c * dt) for c in self.C]
+        self.nse.reset_lambda(self.lambda_t)
 
     def push(self, u, q):
         return u
@@ -1104,6 +1124,189 @@ class DNS:
             u, q = self.init.advance(u, q, 1)
             n += 1
         return self.main.advance(u, q, nsteps - n)
+
+    def reset_dt(self, dt):
+        """DNS::reset_dt (dns.cpp:191-196)."""
+        self.main.reset_dt(dt)
+        if self.init is not None:
+            self.init.reset_dt(dt)
+
+    def CFL(self, u):
+        """DNSAlgorithm::CFL (dnsalgo.cpp:62-66)."""
+        c = cfl_factor(u, self.g, self.main_nse.Ubase, self.main_nse.Wbase)
+        f = self.main.flags
+        return c * (2.0 * PI / 3.0 * f.dt if f.dealiasing in (DealiasXZ, DealiasXYZ) else PI * f.dt)
+
+
+# ---------------------------------------------------------------------------
+# Pressure conversions of the rotational form and single-mode fields
+# ---------------------------------------------------------------------------
+
+def up2q(u, p, g: Grid, Ubase, Wbase, nonlinearity, as_reference: bool = True):
+    """DNS::up2q (dns.cpp:408-440): q = p + 1/2 |u + U|^2 for the rotational form, else q = p.
+
+    With as_reference=True it is restated as the reference computes it: U is
+    read without leaving its spectral state and the w shift uses U as well
+    (dns.cpp:421-434), so the added profile is U's Chebyshev coefficients, for
+    both u and w.  That corrupts q (its (0,0) mode at O(1)); schemes whose linear term
+    reads q (CNRK2, and CNAB2 through its CNRK2 start) carry the error on.
+    as_reference=False uses the physical U and W (the inverse of uq2p).
+    """
+    if nonlinearity != Rotational:
+        return p.copy()
+    up = make_physical(u, g)
+    pp = make_physical(p, g)
+    if as_reference:
+        U = W = np.asarray(Ubase, float)[:, None, None]
+    else:
+        U = ichebyfft(np.asarray(Ubase, float))[:, None, None]
+        W = ichebyfft(np.asarray(Wbase, float))[:, None, None]
+    pp[0] += 0.5 * ((up[0] + U) ** 2 + up[1] ** 2 + (up[2] + W) ** 2)
+    return make_spectral(pp, g)
+
+
+def uq2p(u, q, g: Grid, Ubase, Wbase, nonlinearity):
+    """DNS::uq2p (dns.cpp:372-406): p = q - 1/2 |u + U|^2 for the rotational form, else p = q."""
+    if nonlinearity != Rotational:
+        return q.copy()
+    up = make_physical(u, g)
+    qp = make_physical(q, g)
+    U = ichebyfft(np.asarray(Ubase, float))[:, None, None]
+    W = ichebyfft(np.asarray(Wbase, float))[:, None, None]
+    qp[0] -= 0.5 * ((up[0] + U) ** 2 + up[1] ** 2 + (up[2] + W) ** 2)
+    return make_spectral(qp, g)
+
+
+def basisfunc_field(profiles, kx: int, kz: int, g: Grid) -> np.ndarray:
+    """FlowField += BasisFunc and += conjugate(BasisFunc) (basisfunc.cpp:43-73, flowfield.cpp operator+=).
+
+    ``profiles`` are the BasisFunc's complex y-profiles [ny, i] at the
+    Chebyshev points (state P); the field gets their Chebyshev coefficients at
+    (kx, kz) and the conjugates at (-kx, -kz), i.e. 2 Re(f(y) e^{i(alpha x + beta z)}).
+    """
+    prof = np.asarray(profiles, complex)
+    Nd = prof.shape[1]
+    c = chebyfft(prof.T, axis=1)  # [i, ny]
+    out = np.zeros((Nd, g.Ny, g.Nx, g.Mz), complex)
+    mx = kx % g.Nx
+    out[:, :, mx, kz] += c
+    out[:, :, (-kx) % g.Nx, kz] += np.conj(c)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# TimeStep (dnsflags.cpp:736-972) and f^T(u) (cfdsi.cpp:705-775)
+# ---------------------------------------------------------------------------
+
+def iround(x: float) -> int:
+    """iround (cfbasics/mathdefs.h): round half away from zero."""
+    return int(x + 0.5) if x > 0 else int(x - 0.5)
+
+
+class TimeStep:
+    """TimeStep(dt, dtmin, dtmax, dT, CFLmin, CFLmax, variable) (dnsflags.cpp:752-801, 811-972)."""
+
+    def __init__(self, dt, dtmin, dtmax, dT, CFLmin, CFLmax, variable):
+        if dtmin < 0 or dt < dtmin or dtmax < dt:
+            raise ValueError("condition 0 <= dtmin <= dt <= dtmax does not hold")
+        if CFLmin < 0 or CFLmax < CFLmin:
+            raise ValueError("condition 0 <= CFLmin <= CFLmax does not hold")
+        if dT < dtmin:
+            raise ValueError("dT < dtmin")
+        self.dtmin, self.dtmax, self.dT, self.T = dtmin, dtmax, dT, 0.0
+        self.CFLmin, self.CFLmax, self.CFL = CFLmin, CFLmax, (CFLmax + CFLmin) / 2
+        self.variable = bool(variable)
+        self.N = 0
+        self.n = max(iround(dT / dt), 1)
+        self.dt = dT / self.n
+        while self.dt < dtmin and self.n >= 2 and dT != 0:
+            self.n -= 1
+            self.dt = dT / self.n
+        while self.dt > dtmax and dT != 0:
+            self.n += 1
+            self.dt = dT / self.n
+
+    def value(self):
+        """TimeStep::operator Real: dT / n."""
+        return self.dT / self.n
+
+    def adjust(self, CFL):
+        self.CFL = CFL
+        if self.variable and (CFL <= self.CFLmin or CFL >= self.CFLmax):
+            return self.adjust_to_middle(CFL)
+        return False
+
+    def adjust_to_middle(self, CFL):
+        if self.dtmin == self.dtmax or self.dT == 0.0:
+            return False
+        n = max(iround(2 * self.n * CFL / (self.CFLmax + self.CFLmin)), 1)
+        dt = self.dT / n
+        while dt < self.dtmin and dt < self.dT:
+            n -= 1
+            dt = self.dT / n
+        while dt > self.dtmax:
+            n += 1
+            dt = self.dT / n
+        CFL *= dt / self.dt
+        adj = n != self.n
+        if adj:
+            self.n, self.dt, self.CFL = n, dt, CFL
+        return adj
+
+    def adjust_for_T(self, T):
+        self.T = T
+        if T < 0:
+            raise ValueError("can't integrate backwards in time")
+        if T == 0:
+            adj = self.dt != 0
+            self.dt, self.n, self.dT, self.T = 0.0, 0, 0.0, 0.0
+            return adj
+        N = max(iround(T / self.dT), 1)
+        dT = T / N
+        n = max(iround(dT / self.dt), 1)
+        dt = dT / n
+        while dt < self.dtmin and n > 2 and dT != 0:
+            n -= 1
+            dt = dT / n
+        while dt > self.dtmax and dT != 0:
+            n += 1
+            dt = dT / n
+        CFL = dt * self.CFL / self.dt
+        adj = dt != self.dt
+        self.n, self.N, self.dt, self.dT, self.CFL = n, N, dt, dT, CFL
+        return adj
+
+
+def ft(u, g: Grid, flags: DNSFlags, timestep: TimeStep, T: float):
+    """f(u, T, h=0, ...) of cfdsi.cpp:705-775: returns (f^T(u), last CFL number)."""
+    import copy
+    if not np.all(np.isfinite(u)):
+        raise FloatingPointError("f: u is not finite")
+    if T < 0:
+        return u * (1 + abs(T)), 0.0
+    if T == 0:
+        return u.copy(), 0.0
+    dt = copy.copy(timestep)
+    dt.adjust_for_T(T)
+    fl = copy.copy(flags)
+    fl.dt = dt.value()
+    q = np.zeros((1,) + u.shape[1:], dtype=complex)
+    dns = DNS(u, q, g, fl)
+    f = u.copy()
+    cfl = 0.0
+    if dt.variable:
+        f, q = dns.advance(f, q, 1)
+        dt.adjust(dns.CFL(f))
+        dns.reset_dt(dt.value())
+        f = u.copy()
+    for _ in range(1, dt.N + 1):
+        cfl = dns.CFL(f)
+        f, q = dns.advance(f, q, dt.n)
+        if dt.variable and dt.adjust(cfl):
+            dns.reset_dt(dt.value())
+    if not np.all(np.isfinite(f)):
+        raise FloatingPointError("f: f^T(u) is not finite")
+    return f, cfl
 
 
 # ---------------------------------------------------------------------------
