@@ -63,6 +63,10 @@ _SIGS = {
     "cfgpu_measure_fp64": [_PD, _PD],
     "cfgpu_timestep_adjust_for_T": [C.c_void_p, C.c_double, _PI, _PI, _PD],
     "cfgpu_timestep_adjust": [C.c_void_p, C.c_double, _PI, _PI],
+    "cfgpu_ff_write": [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                       C.c_double, C.c_int, _PD],
+    "cfgpu_ff_read_header": [C.c_char_p, _PI, _PD, _PI, C.c_char_p],
+    "cfgpu_ff_read": [C.c_char_p, _PD, C.c_size_t],
     "cfgpu_ft": [C.POINTER(Grid), C.POINTER(Flags), C.POINTER(TimeStepC), C.c_double, _PD, _PD, _PD, C.c_int],
     "cfgpu_dns_l2norm": [C.c_void_p, C.c_int, _PD],
     "cfgpu_dns_advance_timed": [C.c_void_p, C.c_int, _PD],

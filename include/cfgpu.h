@@ -28,6 +28,8 @@
 #ifndef CFGPU_H
 #define CFGPU_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -176,6 +178,20 @@ cfgpu_status cfgpu_timestep_adjust(cfgpu_timestep* ts, double cfl, int* n, int* 
  */
 cfgpu_status cfgpu_ft(const cfgpu_grid* grid, const cfgpu_flags* flags, const cfgpu_timestep* timestep, double T,
                       const double* u, double* fu, double* cfl, int precision);
+
+/*
+ * channelflow's binary FlowField format (.ff): FlowField::binarySave and the
+ * FlowField(filebase) constructor's binary branch (channelflow/flowfield.cpp:2642-2723, 216-356).
+ * data is the FlowField's spectral storage, complex [Nd][Ny][Nx][Nz/2+1] (2*Nd*Ny*Nx*(Nz/2+1) doubles).
+ * padded != 0 writes only the 2/3-rule modes (the caller's aliased modes must be zero).
+ * cfgpu_ff_read_header returns dims = {Nx, Ny, Nz, Nd}, geom = {Lx, Lz, a, b}, the padded flag and the
+ * two state characters ('S' spectral, 'P' physical); cfgpu_ff_read reads spectral-state files only
+ * (CFGPU_ENOTSUP otherwise) and zero-fills the modes a padded file omits.
+ */
+cfgpu_status cfgpu_ff_write(const char* path, int Nx, int Ny, int Nz, int Nd, double Lx, double Lz, double a,
+                            double b, int padded, const double* data);
+cfgpu_status cfgpu_ff_read_header(const char* path, int* dims, double* geom, int* padded, char* state);
+cfgpu_status cfgpu_ff_read(const char* path, double* data, size_t ndoubles);
 
 /*
  * Batched TauSolver (channelflow/tausolver.cpp:81-176 constructor and

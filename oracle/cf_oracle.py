@@ -1437,3 +1437,52 @@ def cfl_factor(u: np.ndarray, g: Grid, Ubase: np.ndarray, Wbase: np.ndarray) -> 
             Ui = Ub[ny] if i == 0 else (Wb[ny] if i == 2 else 0.0)
             cfl = max(cfl, float(np.max((up[i, ny] + Ui) / d)))
     return cfl
+
+
+# ---------------------------------------------------------------------------
+# Binary FlowField files (.ff): FlowField::binarySave (flowfield.cpp:2642-2723)
+# and the binary branch of FlowField(filebase) (flowfield.cpp:216-356), with
+# the big-endian primitives of cfbasics/cfbasics.h:368-470.
+# ---------------------------------------------------------------------------
+
+def ff_write(path, u: np.ndarray, g: Grid, padded: bool):
+    """Write a spectral FlowField [Nd, Ny, Nx, Mz] the way binarySave does (version 2.0.9)."""
+    import struct
+    Nd = u.shape[0]
+    out = [struct.pack(">7i", 2, 0, 9, g.Nx, g.Ny, g.Nz, Nd), b"SS", struct.pack(">4d", g.Lx, g.Lz, g.a, g.b),
+           b"1" if padded else b"0"]
+    if padded:
+        Nxd, Nzd = 2 * (g.Nx // 6), 2 * (g.Nz // 3) + 1
+        xs = list(range(0, Nxd + 1)) + list(range(g.Nx - Nxd, g.Nx))
+        sel = u[:, :, xs, : Nzd // 2 + 1]
+    else:
+        sel = u
+    pairs = np.stack([sel.real, sel.imag], axis=-1).astype(">f8")
+    out.append(pairs.tobytes())
+    with open(path, "wb") as f:
+        f.write(b"".join(out))
+
+
+def ff_read(path):
+    """Read a spectral-state .ff file; returns (u [Nd, Ny, Nx, Mz], Grid, padded)."""
+    import struct
+    b = open(path, "rb").read()
+    major, minor, update, Nx, Ny, Nz, Nd = struct.unpack(">7i", b[:28])
+    xz, ys = b[28:29], b[29:30]
+    Lx, Lz, a, bb = struct.unpack(">4d", b[30:62])
+    padded = b[62:63] != b"0"
+    if xz != b"S" or ys != b"S":
+        raise ValueError("physical-state .ff files are not read here")
+    g = Grid(Nx, Ny, Nz, Lx, Lz, a, bb)
+    u = np.zeros((Nd, Ny, Nx, Nz // 2 + 1), complex)
+    data = np.frombuffer(b[63:], dtype=">f8")
+    if padded:
+        Nxd, Nzd = 2 * (Nx // 6), 2 * (Nz // 3) + 1
+        xs = list(range(0, Nxd + 1)) + list(range(Nx - Nxd, Nx))
+        nz = Nzd // 2 + 1
+        v = data[: Nd * Ny * len(xs) * nz * 2].reshape(Nd, Ny, len(xs), nz, 2)
+        u[:, :, xs, :nz] = v[..., 0] + 1j * v[..., 1]
+    else:
+        v = data[: Nd * Ny * Nx * (Nz // 2 + 1) * 2].reshape(Nd, Ny, Nx, Nz // 2 + 1, 2)
+        u[:] = v[..., 0] + 1j * v[..., 1]
+    return u, g, padded
