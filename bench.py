@@ -46,6 +46,10 @@ NU, DT, UBULK = 1.0 / 4000.0, 0.01, 2.0 / 3.0
 WORKLOAD = ("plane Poiseuille 128x97x128 (Lx=4pi, Lz=2pi), CNAB2 + SMRK2 start-up, dt=0.01, bulk velocity "
             "Ubulk=2/3, Re_c=4000, rotational NL, 2/3 dealiasing, seeded perturbation L2=0.3")
 CNAB2, SMRK2, LaminarBase, BulkVelocity = 1, 3, 3, 1
+# DRAM bytes (read + write) per launch of the mixed-path kernels from one `ncu --set full` capture of
+# this workload (profiles/ncu_full_poiseuille_128x97x128_mixed.md); None where not captured.
+NCU_TRAFFIC = {"tau_solve": 76.130048e6 + 4.475648e6,
+               "nonlinear_pass": (16.32896 + 16.315648 + 25.136128 + 12.600576 + 8.16384 + 0.003328) * 1e6}
 
 
 def peaks():
@@ -311,7 +315,8 @@ def main():
                    "l2": "no flush: per-step working set %.0f MB > 129 MB L2" % (m["bytes"] / 1e6),
                    "parallelism": "replicas" if world > 1 else "single"},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm, "unit": "GB/s",
-                     "frac": ach / hbm, "peak_source": peak_kind, "traffic": None,
+                     "frac": ach / hbm, "peak_source": peak_kind,
+                     "traffic": NCU_TRAFFIC.get(dom) if (NX, NY, NZ) == (128, 97, 128) else None,
                      "algorithmic_bytes": bts, "avg_launch_ms": t_avg},
         "phases": {"nonlinear_pass": {"avg_ms": nl_avg, "launches": m["nl_n"], "alg_bytes": bnl,
                                       "achieved_gbs": bnl / (nl_avg / 1e3) / 1e9 if nl_avg else None,

@@ -5,4 +5,4 @@ this package holds its in-tree build script and a Python mirror of the
 reference's DNS/DNSFlags API used by the tests and the benchmark.
 """
 
-from .dns import DNS, DNSFlags, Grid, tau_solve_batched  # noqa: F401
+from .dns import DNS, DNSFlags, Ensemble, Grid, tau_solve_batched  # noqa: F401

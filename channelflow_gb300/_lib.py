@@ -63,6 +63,13 @@ _SIGS = {
     "cfgpu_measure_fp64": [_PD, _PD],
     "cfgpu_timestep_adjust_for_T": [C.c_void_p, C.c_double, _PI, _PI, _PD],
     "cfgpu_timestep_adjust": [C.c_void_p, C.c_double, _PI, _PI],
+    "cfgpu_ensemble_create": [C.POINTER(Grid), C.POINTER(Flags), C.c_int, C.c_int, C.POINTER(C.c_void_p)],
+    "cfgpu_ensemble_size": [C.c_void_p, _PI],
+    "cfgpu_ensemble_set_field": [C.c_void_p, C.c_int, _PD, _PD],
+    "cfgpu_ensemble_get_field": [C.c_void_p, C.c_int, _PD, _PD],
+    "cfgpu_ensemble_cfl": [C.c_void_p, _PD],
+    "cfgpu_ensemble_l2norm": [C.c_void_p, C.c_int, _PD],
+    "cfgpu_ensemble_dPdx": [C.c_void_p, _PD],
     "cfgpu_ff_write": [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                        C.c_double, C.c_int, _PD],
     "cfgpu_ff_read_header": [C.c_char_p, _PI, _PD, _PI, C.c_char_p],

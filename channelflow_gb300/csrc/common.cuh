@@ -47,9 +47,13 @@ struct GridDev {
   int Md;          // NKx*NKz
   int kxmax, kzmax;  // Nx/2, Nz/2 (Nyquist; never in the solved set)
   double Lx, Lz, a, b;
-  const int* kxs;  // optional explicit mode list (batched tau solves); null = compact mapping
+  const int* kxs;  // optional explicit mode list (batched tau solves, field batches); null = compact mapping
   const int* kzs;
+  int Mf;          // modes per field when Md spans a batch of fields (m / Mf = field); 0 = one field
 };
+
+// Field (batch slot) that mode m belongs to.
+__host__ __device__ __forceinline__ int mode_field(const GridDev& g, int m) { return g.Mf > 0 ? m / g.Mf : 0; }
 
 __host__ __device__ __forceinline__ int mode_kx(const GridDev& g, int m) {
   if (g.kxs) return g.kxs[m];

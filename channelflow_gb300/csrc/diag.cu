@@ -23,11 +23,13 @@ __host__ __device__ inline double key_dbl(unsigned long long k) {
 }
 
 // z pass for the CFL factor: c2r along z of u, v, w (x-transformed planes,
-// two real rows per complex FFT) and the signed maximum of u_i/dx_i.
+// two real rows per complex FFT) and the signed maximum of u_i/dx_i.  With a
+// batch of nslot fields the planes are [y][field]: plane ny belongs to field
+// ny % nslot at Chebyshev point ny / nslot, and each field has its own maximum.
 template <typename R>
 __global__ void __launch_bounds__(256) k_zcfl(GridDev g, FftPlan pz, const cpx<R>* __restrict__ twz, int RP,
                                               const cpx<R>* __restrict__ X, const double* __restrict__ dyc, double dx,
-                                              double dz, unsigned long long* __restrict__ out) {
+                                              double dz, int nslot, unsigned long long* __restrict__ out) {
   extern __shared__ unsigned char smem_raw[];
   const int Nz = g.Nz, ss = Nz + 1, NKz = g.NKz;
   const int nseq = 3 * RP / 2;
@@ -57,7 +59,7 @@ __global__ void __launch_bounds__(256) k_zcfl(GridDev g, FftPlan pz, const cpx<R
   }
   __syncthreads();
   fft_batch<R>(A, B, nseq, ss, pz, twz, +1);
-  const double inv[3] = {1.0 / dx, 1.0 / dyc[ny], 1.0 / dz};
+  const double inv[3] = {1.0 / dx, 1.0 / dyc[ny / nslot], 1.0 / dz};
   double m = -1e300;
   for (int i = tid; i < RP * Nz; i += nthr) {
     const int z = i % Nz, r = i / Nz;
@@ -73,15 +75,18 @@ __global__ void __launch_bounds__(256) k_zcfl(GridDev g, FftPlan pz, const cpx<R
   for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
   if ((tid & 31) == 0) atomicMax(&bmax, dbl_key(m));
   __syncthreads();
-  if (tid == 0) atomicMax(out, bmax);
+  if (tid == 0) atomicMax(out + ny % nslot, bmax);
 }
 
-// L2Norm2 over the solved modes: one thread per (component, mode, part) line.
+// L2Norm2 over the solved modes: one thread per (component, mode, part) line;
+// out[field] for a batch of fields (mode_field).
 __global__ void k_l2norm2(GridDev g, int N, int ncomp, const double* __restrict__ U, double* __restrict__ out) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int lines = 2 * g.Md;
   double s = 0.0;
+  int field = 0;
   if (t < ncomp * lines) {
+    field = mode_field(g, (t % lines) >> 1);
     const int c = t / lines, l = t % lines;
     const int m = l >> 1;
     const size_t row = (size_t)lines;
@@ -98,13 +103,17 @@ __global__ void k_l2norm2(GridDev g, int N, int ncomp, const double* __restrict_
     }
     s *= (mode_kz(g, m) == 0) ? 1.0 : 2.0;
   }
+  if (g.Mf > 0) {
+    if (s != 0.0) atomicAdd(out + field, s);
+    return;
+  }
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   if ((threadIdx.x & 31) == 0 && s != 0.0) atomicAdd(out, s);
 }
 
 template <typename R>
 cudaError_t launch_zcfl(const GridDev& g, const FftPlan& pz, const cpx<R>* twz, int RP, const cpx<R>* X,
-                        const double* dyc, double dx, double dz, unsigned long long* out, cudaStream_t st) {
+                        const double* dyc, double dx, double dz, int nslot, unsigned long long* out, cudaStream_t st) {
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(k_zcfl<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
@@ -112,7 +121,7 @@ cudaError_t launch_zcfl(const GridDev& g, const FftPlan& pz, const cpx<R>* twz, 
     attr_set = true;
   }
   const size_t smem = 2 * sizeof(cpx<R>) * (size_t)(3 * RP / 2) * (g.Nz + 1);
-  k_zcfl<R><<<dim3((g.Nx + RP - 1) / RP, g.Ny), 256, smem, st>>>(g, pz, twz, RP, X, dyc, dx, dz, out);
+  k_zcfl<R><<<dim3((g.Nx + RP - 1) / RP, g.Ny), 256, smem, st>>>(g, pz, twz, RP, X, dyc, dx, dz, nslot, out);
   return cudaGetLastError();
 }
 
@@ -125,9 +134,9 @@ cudaError_t launch_l2norm2(const GridDev& g, int N, int ncomp, const double* U, 
 double cfl_key_to_double(unsigned long long k) { return key_dbl(k); }
 
 template cudaError_t launch_zcfl<float>(const GridDev&, const FftPlan&, const cpx<float>*, int, const cpx<float>*,
-                                        const double*, double, double, unsigned long long*, cudaStream_t);
+                                        const double*, double, double, int, unsigned long long*, cudaStream_t);
 template cudaError_t launch_zcfl<double>(const GridDev&, const FftPlan&, const cpx<double>*, int,
-                                         const cpx<double>*, const double*, double, double, unsigned long long*,
+                                         const cpx<double>*, const double*, double, double, int, unsigned long long*,
                                          cudaStream_t);
 
 // ---------------------------------------------------------------------------

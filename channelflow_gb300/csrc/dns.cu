@@ -381,7 +381,14 @@ static int setup_scheme(Scheme& s, int method, double dt) {
 struct cfgpu_dns_s {
   int device = 0;
   cudaStream_t st = nullptr;
-  GridDev g{};
+  GridDev g{};   // one field
+  // A batch of nb fields of the same grid and flags is stored interleaved,
+  // component arrays [c][ny][field][m]: the per-mode kernels see nb*Md modes
+  // (gm, explicit mode lists, Mf = Md) and the per-plane x/z kernels see nb*Ny
+  // planes (gp).  nb = 1: gm = gp = g.
+  int nb = 1;
+  GridDev gm{}, gp{};
+  int* dmodes = nullptr;  // kx then kz lists of gm
   int N = 0;  // Ny
   int precision = CFGPU_FP64;
   cfgpu_flags fl{};
@@ -430,7 +437,7 @@ struct cfgpu_dns_s {
   std::vector<cudaEvent_t> ev_pool;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_used;
 
-  size_t rowc() const { return 2 * (size_t)g.Md; }           // doubles per row
+  size_t rowc() const { return 2 * (size_t)g.Md * nb; }      // doubles per row (all fields)
   size_t compc() const { return rowc() * (size_t)N; }         // doubles per component
   size_t rsz() const { return precision == CFGPU_FP64 ? 8 : 4; }
 };
@@ -468,7 +475,7 @@ struct PhaseScope {
 };
 
 int build_tables(cfgpu_dns d, Scheme& s) {
-  const size_t FN = (size_t)d->N * d->g.Md;
+  const size_t FN = (size_t)d->N * d->gm.Md;
   HelmB hb{d->hb_lo, d->hb_di, d->hb_up};
   for (auto& t : s.tau) {
     cudaFree(t.f);
@@ -478,8 +485,8 @@ int build_tables(cfgpu_dns d, Scheme& s) {
   for (double lt : s.lambda_t) {
     TauTable t{};
     CKS(dalloc(&t.f, FN * TF_NFIELDS, d->bytes));
-    CKS(dalloc(&t.s, (size_t)d->g.Md * TS_NSCALARS, d->bytes));
-    CK(launch_tau_setup(d->g, d->N, lt, d->fl.nu, hb, t, d->scratch, d->st));
+    CKS(dalloc(&t.s, (size_t)d->gm.Md * TS_NSCALARS, d->bytes));
+    CK(launch_tau_setup(d->gm, d->N, lt, d->fl.nu, hb, t, d->scratch, d->st));
     d->launches++;
     s.tau.push_back(t);
   }
@@ -491,7 +498,8 @@ int build_tables(cfgpu_dns d, Scheme& s) {
 // selects the NSE (0 main, 1 init) whose Alternating state is advanced.
 template <typename R>
 int nonlinear_impl(cfgpu_dns d, const double* U, void* Nout, int form) {
-  const GridDev& g = d->g;
+  const GridDev& g = d->gm;   // per-mode kernels
+  const GridDev& gp = d->gp;  // per-plane x/z kernels
   const int N = d->N;
   R* C6 = (R*)d->C6;
   R* W = (R*)d->W6;
@@ -517,9 +525,9 @@ int nonlinear_impl(cfgpu_dns d, const double* U, void* Nout, int form) {
     nin = gradient ? 12 : 3;
     nout = form == NL_CONVECTION ? 3 : (form == NL_DIVERGENCE ? 6 : 9);
   }
-  CK(launch_xinv<R>(g, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)W, (cpx<R>*)d->X6, nin, d->st));
-  CK(launch_zphys<R>(g, form, d->pz, (const cpx<R>*)d->twz, d->RP, (const cpx<R>*)d->X6, (cpx<R>*)d->Z3, d->st));
-  CK(launch_xfwd<R>(g, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)d->Z3, (cpx<R>*)d->F3, nout, d->st));
+  CK(launch_xinv<R>(gp, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)W, (cpx<R>*)d->X6, nin, d->st));
+  CK(launch_zphys<R>(gp, form, d->pz, (const cpx<R>*)d->twz, d->RP, (const cpx<R>*)d->X6, (cpx<R>*)d->Z3, d->st));
+  CK(launch_xfwd<R>(gp, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)d->Z3, (cpx<R>*)d->F3, nout, d->st));
   d->launches += 3;
   const R* F = (const R*)d->F3;
   if (form == NL_ROTATIONAL || form == NL_CONVECTION) {
@@ -585,9 +593,9 @@ int tau_solve(cfgpu_dns d, const SolveParams& sp, const SolvePtrs& p, const TauT
   PhaseScope ps(d, 1);
   HelmB hb{d->hb_lo, d->hb_di, d->hb_up};
   if (d->precision == CFGPU_FP64) {
-    CK(launch_tau_solve<double>(d->g, d->N, sp, p, hb, tt, d->st));
+    CK(launch_tau_solve<double>(d->gm, d->N, sp, p, hb, tt, d->st));
   } else {
-    CK(launch_tau_solve<float>(d->g, d->N, sp, p, hb, tt, d->st));
+    CK(launch_tau_solve<float>(d->gm, d->N, sp, p, hb, tt, d->st));
   }
   d->launches++;
   return CFGPU_OK;
@@ -733,34 +741,45 @@ int dns_advance_device(cfgpu_dns d, int nsteps) {
   return scheme_advance(d, 0, nsteps - n);
 }
 
-// host serial layout <-> solved-mode layout
-void gather_modes(cfgpu_dns d, const double* h, int Nd, double* out) {
+// host serial layout <-> solved-mode layout.  The host side holds nf
+// consecutive FlowFields (Nd components each, fields f0 .. f0+nf-1 of the
+// batch); the device side is [i][my][field][m] with nb fields (fstride = nb),
+// or one field's compact [i][my][m] (fstride = 1, f0 = 0).
+void gather_modes(cfgpu_dns d, const double* h, int Nd, double* out, int f0 = 0, int nf = -1, int fstride = -1) {
   const GridDev& g = d->g;
   const int Mz = g.Nz / 2 + 1;
-  for (int i = 0; i < Nd; ++i)
-    for (int my = 0; my < g.Ny; ++my)
-      for (int m = 0; m < g.Md; ++m) {
-        const int kx = mode_kx(g, m), kz = mode_kz(g, m);
-        const int mx = kx >= 0 ? kx : kx + g.Nx;
-        const size_t src = 2 * ((((size_t)i * g.Ny + my) * g.Nx + mx) * Mz + kz);
-        const size_t dst = 2 * (((size_t)i * g.Ny + my) * g.Md + m);
-        out[dst] = h[src];
-        out[dst + 1] = h[src + 1];
-      }
+  if (nf < 0) nf = d->nb;
+  if (fstride < 0) fstride = d->nb;
+  const size_t hfield = (size_t)2 * Nd * g.Ny * g.Nx * Mz;
+  for (int f = 0; f < nf; ++f)
+    for (int i = 0; i < Nd; ++i)
+      for (int my = 0; my < g.Ny; ++my)
+        for (int m = 0; m < g.Md; ++m) {
+          const int kx = mode_kx(g, m), kz = mode_kz(g, m);
+          const int mx = kx >= 0 ? kx : kx + g.Nx;
+          const size_t src = f * hfield + 2 * ((((size_t)i * g.Ny + my) * g.Nx + mx) * Mz + kz);
+          const size_t dst = 2 * ((((size_t)i * g.Ny + my) * fstride + (f0 + f)) * g.Md + m);
+          out[dst] = h[src];
+          out[dst + 1] = h[src + 1];
+        }
 }
-void scatter_modes(cfgpu_dns d, const double* in, int Nd, double* h) {
+void scatter_modes(cfgpu_dns d, const double* in, int Nd, double* h, int f0 = 0, int nf = -1, int fstride = -1) {
   const GridDev& g = d->g;
   const int Mz = g.Nz / 2 + 1;
-  for (int i = 0; i < Nd; ++i)
-    for (int my = 0; my < g.Ny; ++my)
-      for (int m = 0; m < g.Md; ++m) {
-        const int kx = mode_kx(g, m), kz = mode_kz(g, m);
-        const int mx = kx >= 0 ? kx : kx + g.Nx;
-        const size_t dst = 2 * ((((size_t)i * g.Ny + my) * g.Nx + mx) * Mz + kz);
-        const size_t src = 2 * (((size_t)i * g.Ny + my) * g.Md + m);
-        h[dst] = in[src];
-        h[dst + 1] = in[src + 1];
-      }
+  if (nf < 0) nf = d->nb;
+  if (fstride < 0) fstride = d->nb;
+  const size_t hfield = (size_t)2 * Nd * g.Ny * g.Nx * Mz;
+  for (int f = 0; f < nf; ++f)
+    for (int i = 0; i < Nd; ++i)
+      for (int my = 0; my < g.Ny; ++my)
+        for (int m = 0; m < g.Md; ++m) {
+          const int kx = mode_kx(g, m), kz = mode_kz(g, m);
+          const int mx = kx >= 0 ? kx : kx + g.Nx;
+          const size_t dst = f * hfield + 2 * ((((size_t)i * g.Ny + my) * g.Nx + mx) * Mz + kz);
+          const size_t src = 2 * ((((size_t)i * g.Ny + my) * fstride + (f0 + f)) * g.Md + m);
+          h[dst] = in[src];
+          h[dst + 1] = in[src + 1];
+        }
 }
 
 int set_fields(cfgpu_dns d, const double* u, const double* q) {
@@ -786,6 +805,35 @@ int get_fields(cfgpu_dns d, double* u, double* q) {
   return CFGPU_OK;
 }
 
+// One field (slot) of a batch: the rows [c][ny] of that field are strided by nb*Md modes on the device.
+int set_slot(cfgpu_dns d, int slot, const double* u, const double* q) {
+  const size_t w = 2 * (size_t)d->g.Md, pitch = w * d->nb, cd1 = w * d->N;
+  if (u) {
+    gather_modes(d, u, 3, d->stage, 0, 1, 1);
+    CK(cudaMemcpy2DAsync(d->Ucur + slot * w, pitch * sizeof(double), d->stage, w * sizeof(double),
+                         w * sizeof(double), 3 * (size_t)d->N, cudaMemcpyHostToDevice, d->st));
+  }
+  if (q) {
+    gather_modes(d, q, 1, d->stage + 3 * cd1, 0, 1, 1);
+    CK(cudaMemcpy2DAsync(d->Qcur + slot * w, pitch * sizeof(double), d->stage + 3 * cd1, w * sizeof(double),
+                         w * sizeof(double), (size_t)d->N, cudaMemcpyHostToDevice, d->st));
+  }
+  CK(cudaStreamSynchronize(d->st));
+  return CFGPU_OK;
+}
+
+int get_slot(cfgpu_dns d, int slot, double* u, double* q) {
+  const size_t w = 2 * (size_t)d->g.Md, pitch = w * d->nb, cd1 = w * d->N;
+  CK(cudaMemcpy2DAsync(d->stage, w * sizeof(double), d->Ucur + slot * w, pitch * sizeof(double),
+                       w * sizeof(double), 3 * (size_t)d->N, cudaMemcpyDeviceToHost, d->st));
+  CK(cudaMemcpy2DAsync(d->stage + 3 * cd1, w * sizeof(double), d->Qcur + slot * w, pitch * sizeof(double),
+                       w * sizeof(double), (size_t)d->N, cudaMemcpyDeviceToHost, d->st));
+  CK(cudaStreamSynchronize(d->st));
+  if (u) scatter_modes(d, d->stage, 3, u, 0, 1, 1);
+  if (q) scatter_modes(d, d->stage + 3 * cd1, 1, q, 0, 1, 1);
+  return CFGPU_OK;
+}
+
 template <typename R>
 int upload_as(const std::vector<double>& v, void** dst, long long& bytes) {
   std::vector<R> t(v.begin(), v.end());
@@ -808,7 +856,7 @@ int upload_tw(const std::vector<std::complex<long double>>& tw, void** dst, long
 }
 
 int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flags, const double* Ub, const double* Wb,
-                    const double* u0) {
+                    const double* u0, int nb = 1) {
   d->fl = *flags;
   const cfgpu_flags& f = d->fl;
   const int Nx = grid->Nx, Ny = grid->Ny, Nz = grid->Nz;
@@ -840,7 +888,11 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
   g.a = grid->a;
   g.b = grid->b;
   g.kxs = g.kzs = nullptr;
+  g.Mf = 0;
   d->N = Ny;
+  d->nb = nb;
+  d->gm = g;
+  d->gp = g;
   d->alt[0] = d->alt[1] = (f.nonlinearity == CFGPU_Alternating_) ? 1 : 0;
   CK(cudaGetDevice(&d->device));
   CK(cudaStreamCreateWithFlags(&d->st, cudaStreamNonBlocking));
@@ -892,8 +944,24 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
   CKS(dalloc(&d->dWbase, Ny, B));
   CKS(dalloc(&d->dUbaseyy, Ny, B));
   CKS(dalloc(&d->dWbaseyy, Ny, B));
-  CKS(dalloc(&d->ddPdx, 2, B));
-  CKS(dalloc(&d->dred, 2, B));
+  CKS(dalloc(&d->ddPdx, 2 * (size_t)nb, B));
+  CKS(dalloc(&d->dred, 2 * (size_t)nb, B));
+  if (nb > 1) {
+    // mode lists of the batched mode view and the plane view of the x/z passes
+    std::vector<int> ml(2 * (size_t)nb * g.Md);
+    for (int f = 0; f < nb; ++f)
+      for (int m = 0; m < g.Md; ++m) {
+        ml[(size_t)f * g.Md + m] = mode_kx(g, m);
+        ml[(size_t)nb * g.Md + (size_t)f * g.Md + m] = mode_kz(g, m);
+      }
+    CKS(dalloc(&d->dmodes, ml.size(), B));
+    CK(cudaMemcpy(d->dmodes, ml.data(), ml.size() * sizeof(int), cudaMemcpyHostToDevice));
+    d->gm.Md = nb * g.Md;
+    d->gm.Mf = g.Md;
+    d->gm.kxs = d->dmodes;
+    d->gm.kzs = d->dmodes + (size_t)nb * g.Md;
+    d->gp.Ny = nb * Ny;
+  }
   {
     // FlowField::CFLfactor spacing (flowfield.cpp:4046-4052)
     std::vector<double> y(Ny), dy(Ny);
@@ -907,8 +975,12 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
   CK(cudaMemcpy(d->dUbaseyy, d->Ubaseyy.data(), Ny * sizeof(double), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(d->dWbaseyy, d->Wbaseyy.data(), Ny * sizeof(double), cudaMemcpyHostToDevice));
   {
-    double init[2] = {d->dPdxAct, d->dPdzAct};
-    CK(cudaMemcpy(d->ddPdx, init, sizeof(init), cudaMemcpyHostToDevice));
+    std::vector<double> init(2 * (size_t)nb);
+    for (int f = 0; f < nb; ++f) {
+      init[2 * f] = d->dPdxAct;
+      init[2 * f + 1] = d->dPdzAct;
+    }
+    CK(cudaMemcpy(d->ddPdx, init.data(), init.size() * sizeof(double), cudaMemcpyHostToDevice));
   }
   // Helmholtz B rows
   {
@@ -987,9 +1059,9 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
   CKS(dalloc(&tmp, nin * cd * rs, B));
   d->W6 = tmp;
   const size_t plane = (size_t)Nx * g.NKz * 2;  // reals per plane per component
-  CKS(dalloc(&tmp, nin * plane * Ny * rs, B));
+  CKS(dalloc(&tmp, nin * plane * Ny * nb * rs, B));
   d->X6 = tmp;
-  CKS(dalloc(&tmp, nout * plane * Ny * rs, B));
+  CKS(dalloc(&tmp, nout * plane * Ny * nb * rs, B));
   d->Z3 = tmp;
   CKS(dalloc(&tmp, nout * cd * rs, B));
   d->F3 = tmp;
@@ -1062,7 +1134,7 @@ void dns_free(cfgpu_dns d) {
   F(d->dUbase); F(d->dWbase); F(d->dUbaseyy); F(d->dWbaseyy); F(d->ddPdx);
   F(d->hb_lo); F(d->hb_di); F(d->hb_up);
   F(d->twx); F(d->twz); F(d->cinvA); F(d->cinvB); F(d->cfwdA); F(d->cfwdB);
-  F(d->cderA); F(d->cderB); F(d->basey); F(d->cdfA); F(d->cdfB); F(d->dyc); F(d->dred);
+  F(d->cderA); F(d->cderB); F(d->basey); F(d->cdfA); F(d->cdfB); F(d->dyc); F(d->dred); F(d->dmodes);
   F(d->Ucur); F(d->Qcur);
   for (int j = 0; j < 4; ++j) { F(d->Uh[j]); F(d->Qh[j]); F(d->Nh[j]); }
   for (int w = 0; w < 2; ++w) { F(d->fj[w]); F(d->fj1[w]); F(d->rkQ[w]); }
@@ -1083,24 +1155,37 @@ void dns_free(cfgpu_dns d) {
 }  // namespace
 
 namespace {
+// DNSAlgorithm::CFL of every field of the batch into cfl[0 .. nb).
 template <typename R>
 int cfl_impl(cfgpu_dns d, double* cfl) {
-  const GridDev& g = d->g;
+  const GridDev& g = d->gm;
   if ((d->N + 1) / 2 > 56) return fail(CFGPU_ENOTSUP, "CFL needs Ny <= 111");
   R* W = (R*)d->W6;
   CK(launch_grad_cheb<R>(g, d->N, false, d->Ucur, W, (const R*)d->cinvA, (const R*)d->cinvB, (const R*)d->cderA,
                          (const R*)d->cderB, (const R*)d->basey, 0.0, d->st));
-  CK(launch_xinv<R>(g, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)W, (cpx<R>*)d->X6, 3, d->st));
-  CK(cudaMemsetAsync(d->dred, 0, sizeof(unsigned long long), d->st));
-  CK(launch_zcfl<R>(g, d->pz, (const cpx<R>*)d->twz, d->RP, (const cpx<R>*)d->X6, d->dyc, g.Lx / g.Nx, g.Lz / g.Nz,
-                    d->dred, d->st));
+  CK(launch_xinv<R>(d->gp, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)W, (cpx<R>*)d->X6, 3, d->st));
+  CK(cudaMemsetAsync(d->dred, 0, d->nb * sizeof(unsigned long long), d->st));
+  CK(launch_zcfl<R>(d->gp, d->pz, (const cpx<R>*)d->twz, d->RP, (const cpx<R>*)d->X6, d->dyc, g.Lx / g.Nx,
+                    g.Lz / g.Nz, d->nb, d->dred, d->st));
   d->launches += 3;
-  unsigned long long key = 0;
-  CK(cudaMemcpyAsync(&key, d->dred, sizeof(key), cudaMemcpyDeviceToHost, d->st));
+  std::vector<unsigned long long> key(d->nb);
+  CK(cudaMemcpyAsync(key.data(), d->dred, d->nb * sizeof(unsigned long long), cudaMemcpyDeviceToHost, d->st));
   CK(cudaStreamSynchronize(d->st));
-  const double factor = cfl_key_to_double(key);
   const bool dxz = d->fl.dealiasing == CFGPU_DealiasXZ || d->fl.dealiasing == CFGPU_DealiasXYZ;
-  *cfl = factor * (dxz ? 2.0 * M_PI / 3.0 * d->fl.dt : M_PI * d->fl.dt);
+  for (int f = 0; f < d->nb; ++f)
+    cfl[f] = cfl_key_to_double(key[f]) * (dxz ? 2.0 * M_PI / 3.0 * d->fl.dt : M_PI * d->fl.dt);
+  return CFGPU_OK;
+}
+
+int l2norm_impl(cfgpu_dns d, int field, double* l2) {
+  double* out = reinterpret_cast<double*>(d->dred) + d->nb;
+  CK(cudaMemsetAsync(out, 0, d->nb * sizeof(double), d->st));
+  CK(launch_l2norm2(d->gm, d->N, field == 0 ? 3 : 1, field == 0 ? d->Ucur : d->Qcur, out, d->st));
+  d->launches++;
+  std::vector<double> s(d->nb);
+  CK(cudaMemcpyAsync(s.data(), out, d->nb * sizeof(double), cudaMemcpyDeviceToHost, d->st));
+  CK(cudaStreamSynchronize(d->st));
+  for (int f = 0; f < d->nb; ++f) l2[f] = std::sqrt(s[f]);
   return CFGPU_OK;
 }
 }  // namespace
@@ -1223,6 +1308,59 @@ cfgpu_status cfgpu_dns_create(const cfgpu_grid* grid, const cfgpu_flags* flags, 
   return CFGPU_OK;
 }
 
+cfgpu_status cfgpu_ensemble_create(const cfgpu_grid* grid, const cfgpu_flags* flags, int nfields, int precision,
+                                   cfgpu_dns* out) {
+  if (!grid || !flags || !out || nfields < 1) return fail(CFGPU_EINVAL, "bad argument");
+  if (precision != CFGPU_FP64 && precision != CFGPU_MIXED) return fail(CFGPU_EINVAL, "bad precision");
+  *out = nullptr;
+  cfgpu_dns d = new cfgpu_dns_s();
+  d->precision = precision;
+  int s = dns_create_impl(d, grid, flags, nullptr, nullptr, nullptr, nfields);
+  if (s != CFGPU_OK) {
+    std::string keep = g_err;
+    dns_free(d);
+    g_err = keep;
+    return s;
+  }
+  *out = d;
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_ensemble_size(cfgpu_dns d, int* nfields) {
+  if (!d || !nfields) return fail(CFGPU_EINVAL, "bad argument");
+  *nfields = d->nb;
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_ensemble_set_field(cfgpu_dns d, int slot, const double* u, const double* q) {
+  if (!d || slot < 0 || slot >= d->nb) return fail(CFGPU_EINVAL, "bad argument");
+  return set_slot(d, slot, u, q);
+}
+
+cfgpu_status cfgpu_ensemble_get_field(cfgpu_dns d, int slot, double* u, double* q) {
+  if (!d || slot < 0 || slot >= d->nb) return fail(CFGPU_EINVAL, "bad argument");
+  return get_slot(d, slot, u, q);
+}
+
+cfgpu_status cfgpu_ensemble_cfl(cfgpu_dns d, double* cfl) {
+  if (!d || !cfl) return fail(CFGPU_EINVAL, "bad argument");
+  return d->precision == CFGPU_FP64 ? cfl_impl<double>(d, cfl) : cfl_impl<float>(d, cfl);
+}
+
+cfgpu_status cfgpu_ensemble_l2norm(cfgpu_dns d, int field, double* l2) {
+  if (!d || !l2 || (field != 0 && field != 1)) return fail(CFGPU_EINVAL, "bad argument");
+  return l2norm_impl(d, field, l2);
+}
+
+cfgpu_status cfgpu_ensemble_dPdx(cfgpu_dns d, double* dPdx) {
+  if (!d || !dPdx) return fail(CFGPU_EINVAL, "bad argument");
+  std::vector<double> v(2 * (size_t)d->nb);
+  CK(cudaMemcpyAsync(v.data(), d->ddPdx, v.size() * sizeof(double), cudaMemcpyDeviceToHost, d->st));
+  CK(cudaStreamSynchronize(d->st));
+  for (int f = 0; f < d->nb; ++f) dPdx[f] = v[2 * f];
+  return CFGPU_OK;
+}
+
 cfgpu_status cfgpu_dns_set_fields(cfgpu_dns d, const double* u, const double* q) {
   if (!d) return fail(CFGPU_EINVAL, "null dns");
   CKS(set_fields(d, u, q));
@@ -1309,20 +1447,17 @@ cfgpu_status cfgpu_dns_kernel_launches(cfgpu_dns d, long long* n) {
 
 cfgpu_status cfgpu_dns_cfl(cfgpu_dns d, double* cfl) {
   if (!d || !cfl) return fail(CFGPU_EINVAL, "bad argument");
-  if (d->precision == CFGPU_FP64) return cfl_impl<double>(d, cfl);
-  return cfl_impl<float>(d, cfl);
+  std::vector<double> v(d->nb);
+  CKS(d->precision == CFGPU_FP64 ? cfl_impl<double>(d, v.data()) : cfl_impl<float>(d, v.data()));
+  *cfl = v[0];
+  return CFGPU_OK;
 }
 
 cfgpu_status cfgpu_dns_l2norm(cfgpu_dns d, int field, double* l2) {
   if (!d || !l2 || (field != 0 && field != 1)) return fail(CFGPU_EINVAL, "bad argument");
-  double* out = reinterpret_cast<double*>(d->dred) + 1;
-  CK(cudaMemsetAsync(out, 0, sizeof(double), d->st));
-  CK(launch_l2norm2(d->g, d->N, field == 0 ? 3 : 1, field == 0 ? d->Ucur : d->Qcur, out, d->st));
-  d->launches++;
-  double s = 0;
-  CK(cudaMemcpyAsync(&s, out, sizeof(s), cudaMemcpyDeviceToHost, d->st));
-  CK(cudaStreamSynchronize(d->st));
-  *l2 = std::sqrt(s);
+  std::vector<double> v(d->nb);
+  CKS(l2norm_impl(d, field, v.data()));
+  *l2 = v[0];
   return CFGPU_OK;
 }
 

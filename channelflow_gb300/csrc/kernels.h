@@ -127,7 +127,7 @@ cudaError_t launch_tau_solve(const GridDev& g, int N, const SolveParams& sp, con
 // Diagnostics (diag.cu)
 template <typename R>
 cudaError_t launch_zcfl(const GridDev& g, const FftPlan& pz, const cpx<R>* twz, int RP, const cpx<R>* X,
-                        const double* dyc, double dx, double dz, unsigned long long* out, cudaStream_t st);
+                        const double* dyc, double dx, double dz, int nslot, unsigned long long* out, cudaStream_t st);
 cudaError_t launch_l2norm2(const GridDev& g, int N, int ncomp, const double* U, double* out, cudaStream_t st);
 double cfl_key_to_double(unsigned long long k);
 int measure_fp64(int device_sms, double* tflops, double* cycles_per_fma);

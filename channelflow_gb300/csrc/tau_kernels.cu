@@ -562,7 +562,7 @@ __global__ void __launch_bounds__(128) k_tau_solve(GridDev g, int N, SolveParams
       if (part == 0 && q == 0 && act) {
         r[0] = r[0] + mu;
         helm_par(M, q, hlo, hdi, hup, VH_band, VH_up, VH_lo, VH_inv, r, out, 0.0);
-        if (P.dPdx_out) P.dPdx_out[c] = mu;
+        if (P.dPdx_out) P.dPdx_out[2 * mode_field(g, m) + c] = mu;
       }
     }
   }
@@ -897,7 +897,7 @@ __global__ void __launch_bounds__(32) k_tau_solve_s(GridDev g, int N, SolveParam
         const double mu = nu * (target - amean) / ucmean;
         r[0] = r[0] + mu;
         helm_s(M, q, hlo, hdi, hup, VH_band, VH_up, VH_lo, VH_inv, r, o, 0.0);
-        if (act && P.dPdx_out) P.dPdx_out[c] = mu;
+        if (act && P.dPdx_out) P.dPdx_out[2 * mode_field(g, m) + c] = mu;
       }
     }
     if (act) {
@@ -1301,7 +1301,7 @@ __global__ void __launch_bounds__(32) k_tau_solve_t(GridDev g, int N, SolveParam
         const double mu = nu * (target - amean) / ucmean;
         r[0] = r[0] + mu;
         helm_t(M, q, hlo, hdi, hup, TS(0), TS(1), TS(2), TS(3), r, o, 0.0);
-        if (act && P.dPdx_out) P.dPdx_out[c] = mu;
+        if (act && P.dPdx_out) P.dPdx_out[2 * mode_field(g, m) + c] = mu;
       }
     }
     if (act) {

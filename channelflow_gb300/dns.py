@@ -201,6 +201,64 @@ class DNS:
             pass
 
 
+class Ensemble(DNS):
+    """nfields fields with one grid and one set of flags, advanced by shared kernel launches.
+
+    Whole-ensemble buffers are shaped (nfields, 3, Ny, Nx, Nz//2+1) for u and
+    (nfields, 1, ...) for q; set_field/get_field address one slot.  Every
+    field's result equals a single-field DNS of that field.
+    """
+
+    def __init__(self, grid: Grid, flags: DNSFlags, nfields: int, precision: str = "fp64"):
+        lib = L.load()
+        self.grid, self.flags, self.nfields = grid, flags, int(nfields)
+        prec = {"fp64": L.CFGPU_FP64, "mixed": L.CFGPU_MIXED}[precision]
+        h = C.c_void_p()
+        gc, fc = grid.to_c(), flags.to_c()
+        L.check(lib.cfgpu_ensemble_create(C.byref(gc), C.byref(fc), self.nfields, prec, C.byref(h)))
+        self._h = h
+        self._lib = lib
+
+    def _all(self, a, Nd):
+        shape = (self.nfields, Nd, self.grid.Ny, self.grid.Nx, self.grid.Mz)
+        if a.dtype != np.complex128 or not a.flags["C_CONTIGUOUS"] or a.shape != shape:
+            raise ValueError("ensemble buffer must be C-contiguous complex128 of shape %s" % (shape,))
+        return a
+
+    def advance(self, u, q, nsteps: int):
+        L.check(self._lib.cfgpu_dns_advance(self._h, L.dptr(self._all(u, 3)), L.dptr(self._all(q, 1)),
+                                            int(nsteps)))
+
+    def set_fields(self, u, q):
+        L.check(self._lib.cfgpu_dns_set_fields(self._h, L.dptr(self._all(u, 3)), L.dptr(self._all(q, 1))))
+
+    def get_fields(self, u, q):
+        L.check(self._lib.cfgpu_dns_get_fields(self._h, L.dptr(self._all(u, 3)), L.dptr(self._all(q, 1))))
+
+    def set_field(self, slot: int, u, q=None):
+        L.check(self._lib.cfgpu_ensemble_set_field(self._h, int(slot), L.dptr(_as_field(u, self.grid, 3)),
+                                                   L.dptr(None if q is None else _as_field(q, self.grid, 1))))
+
+    def get_field(self, slot: int, u, q):
+        L.check(self._lib.cfgpu_ensemble_get_field(self._h, int(slot), L.dptr(_as_field(u, self.grid, 3)),
+                                                   L.dptr(_as_field(q, self.grid, 1))))
+
+    def CFL(self) -> np.ndarray:
+        v = np.zeros(self.nfields)
+        L.check(self._lib.cfgpu_ensemble_cfl(self._h, L.dptr(v)))
+        return v
+
+    def l2norm(self, field: int = 0) -> np.ndarray:
+        v = np.zeros(self.nfields)
+        L.check(self._lib.cfgpu_ensemble_l2norm(self._h, int(field), L.dptr(v)))
+        return v
+
+    def dPdx(self) -> np.ndarray:
+        v = np.zeros(self.nfields)
+        L.check(self._lib.cfgpu_ensemble_dPdx(self._h, L.dptr(v)))
+        return v
+
+
 def tau_solve_batched(N, kx, kz, Lx, Lz, a, b, lambda_t, nu, Rx, Ry, Rz, taucorrection=True):
     """Batched TauSolver solve; R* complex arrays shaped (nmodes, N). Returns (u, v, w, P)."""
     lib = L.load()

@@ -155,6 +155,29 @@ cfgpu_status cfgpu_dns_phase_times(cfgpu_dns dns, double* nl_ms, long long* nl_c
                                    long long* tau_count);
 
 /*
+ * Ensembles: nfields independent fields with one grid and one set of flags
+ * (the same base flow, constraint, nu and dt) advanced together, every kernel
+ * launch covering all of them (no reference counterpart; the reference runs
+ * one DNS per field, e.g. programs/edgetracking.cpp:488-525).  The handle is
+ * a cfgpu_dns: cfgpu_dns_set_fields/get_fields/advance then take nfields
+ * consecutive FlowField buffers, cfgpu_dns_advance_resident advances all of
+ * them, and cfgpu_dns_reset_dt/time apply to all.  Each field's arithmetic is
+ * the same as in a single-field DNS.  The per-field accessors below address
+ * one slot (0 <= slot < nfields); cfl, l2 and dPdx receive nfields values.
+ * Multistep schemes share one start-up phase: fields written into a slot
+ * after the first step join the running history (use the whole-ensemble
+ * setters, or a self-starting scheme, to restart them cleanly).
+ */
+cfgpu_status cfgpu_ensemble_create(const cfgpu_grid* grid, const cfgpu_flags* flags, int nfields, int precision,
+                                   cfgpu_dns* out);
+cfgpu_status cfgpu_ensemble_size(cfgpu_dns dns, int* nfields);
+cfgpu_status cfgpu_ensemble_set_field(cfgpu_dns dns, int slot, const double* u, const double* q);
+cfgpu_status cfgpu_ensemble_get_field(cfgpu_dns dns, int slot, double* u, double* q);
+cfgpu_status cfgpu_ensemble_cfl(cfgpu_dns dns, double* cfl);
+cfgpu_status cfgpu_ensemble_l2norm(cfgpu_dns dns, int field, double* l2);
+cfgpu_status cfgpu_ensemble_dPdx(cfgpu_dns dns, double* dPdx);
+
+/*
  * TimeStep::adjust_for_T (channelflow/dnsflags.cpp:912-965): fits dT and dt to the horizon T; returns
  * n (steps per dT), N (dT intervals) and dt = dT/n, and updates ts->dt, ts->dT.
  */

@@ -35,3 +35,18 @@ def test_version_and_errors(lib):
     assert lib.cfgpu_version().startswith(b"cfgpu")
     assert lib.cfgpu_flags_default(None) == L.CFGPU_EINVAL
     assert b"null" in lib.cfgpu_last_error()
+
+
+def test_argument_errors_need_no_gpu(lib):
+    """Argument checks run before any CUDA call, so they return EINVAL on a machine without a GPU."""
+    import ctypes as C
+    g = L.Grid(16, 17, 16, 1.0, 1.0, -1.0, 1.0)
+    f = L.Flags()
+    lib.cfgpu_flags_default(C.byref(f))
+    h = C.c_void_p()
+    assert lib.cfgpu_ensemble_create(C.byref(g), C.byref(f), 0, L.CFGPU_FP64, C.byref(h)) == L.CFGPU_EINVAL
+    assert lib.cfgpu_ensemble_create(C.byref(g), C.byref(f), 2, 7, C.byref(h)) == L.CFGPU_EINVAL
+    assert lib.cfgpu_ensemble_set_field(None, 0, None, None) == L.CFGPU_EINVAL
+    assert lib.cfgpu_dns_create(C.byref(g), C.byref(f), None, None, None, 9, C.byref(h)) == L.CFGPU_EINVAL
+    assert lib.cfgpu_tau_solve_batched(4, 1, None, None, 1.0, 1.0, -1.0, 1.0, 1.0, 1.0, 1,
+                                       None, None, None, None, None, None, None) == L.CFGPU_EINVAL

@@ -155,5 +155,7 @@ def test_gpu_orrsommerfeld_growth(scheme, baseflow, vs_oracle):
         return
     err_r, ur, qr = run_os(g, fl, base, lin, oracle_dns(g, fl, base))
     assert abs(err - err_r) <= 1e-6 * err_r
-    assert O.L2Dist(un, ur, g) <= 1e-10 * O.L2Norm(ur, g)
-    assert O.L2Dist(qn, qr, g) <= 1e-10 * O.L2Norm(qr, g)
+    # u is the 1e-4 perturbation of an O(1) flow: the round-off scale is set by the total flow
+    scale = max(O.L2Norm(ur, g), 1.0)
+    assert O.L2Dist(un, ur, g) <= 1e-12 * scale
+    assert O.L2Dist(qn, qr, g) <= 1e-12 * max(O.L2Norm(qr, g), 1.0)
