@@ -231,6 +231,100 @@ def run_gpu(args, rank, world):
     return results, acc, hbm, peak_kind
 
 
+def serve_requests(n, seed, horizon=(5.0, 50.0)):
+    """Mixed-grid f^T(u) requests: Nx, Nz in {32, 48, 64, 96}, Ny in {33, 49, 65}, Re U[300, 2000],
+    Couette or Poiseuille (box Lx = 2pi/1.14, Lz = 2pi/2.5), T U[horizon] at dt = 0.02 (T a multiple of
+    dt), SBDF3 with SMRK2 start-up, seeded divergence-free fields of L2 norm U[0.05, 0.3]."""
+    from channelflow_gb300 import DNSFlags, Grid
+    from channelflow_gb300.fields import random_divfree_field
+    rng = np.random.default_rng(seed)
+    lx, lz = 2 * math.pi / 1.14, 2 * math.pi / 2.5
+    out = []
+    for k in range(n):
+        nx, nz = (int(v) for v in rng.choice([32, 48, 64, 96], size=2))
+        ny = int(rng.choice([33, 49, 65]))
+        re = float(rng.uniform(300, 2000))
+        couette = bool(rng.random() < 0.5)
+        steps = int(round(float(rng.uniform(*horizon)) / 0.02))
+        if couette:
+            fl = DNSFlags(nu=1 / re, dt=0.02, baseflow=LaminarBase, ulowerwall=-1.0, uupperwall=1.0)
+        else:
+            fl = DNSFlags(nu=1 / re, dt=0.02, baseflow=LaminarBase, ulowerwall=0.0, uupperwall=0.0,
+                          constraint=BulkVelocity, Ubulk=2 / 3)
+        u = random_divfree_field(nx, ny, nz, lx, lz, seed=seed * 1000 + k, norm=float(rng.uniform(0.05, 0.3)),
+                                 zero_mean_u=not couette)
+        out.append((Grid(nx, ny, nz, lx, lz), fl, steps, np.ascontiguousarray(u)))
+    return out
+
+
+def run_alone(req, precision="fp64"):
+    """One request alone through the public single-field API (DNS::DNS + advance, as cfDSI::f runs it)."""
+    from channelflow_gb300 import DNS
+    g, fl, steps, u0 = req
+    u = u0.copy()
+    q = np.zeros((1,) + u.shape[1:], dtype=np.complex128)
+    d = DNS(u, g, fl, precision=precision)
+    d.advance(u, q, steps)
+    d.close()
+    return u
+
+
+def run_serve(args):
+    """Served stream vs one-at-a-time plain FP64 solves of the same requests."""
+    from channelflow_gb300.fields import l2norm
+    from channelflow_gb300.server import DONE, Server
+    reqs = serve_requests(args.serve_requests, seed=7)
+    total_steps = sum(r[2] for r in reqs)
+    # one at a time, plain FP64 (the reference's pattern: build a DNS per f^T(u) call)
+    run_alone(serve_requests(1, seed=99, horizon=(0.2, 0.2))[0])  # warm-up: library, context
+    t0 = time.perf_counter()
+    alone = [run_alone(r) for r in reqs]
+    t_alone = time.perf_counter() - t0
+    out = {"requests": len(reqs), "field_steps": total_steps,
+           "one_at_a_time_fp64": {"s": t_alone, "requests_per_s": len(reqs) / t_alone,
+                                  "field_steps_per_s": total_steps / t_alone}, "rates": []}
+    for rate in args.serve_rates:
+        rng = np.random.default_rng(11)
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, size=len(reqs))) if rate > 0 else np.zeros(len(reqs))
+        srv = Server(max_bytes=64 << 30, slots=args.serve_slots, precision=args.serve_precision)
+        ids = [None] * len(reqs)
+        nxt = 0
+        start = time.perf_counter()
+        while True:
+            now = time.perf_counter() - start
+            while nxt < len(reqs) and arrivals[nxt] <= now:
+                g, fl, steps, u = reqs[nxt]
+                ids[nxt] = srv.submit(g, fl, steps, u)
+                nxt += 1
+            active = srv.pump(args.serve_pump_steps)
+            if nxt == len(reqs) and active == 0:
+                break
+            if active == 0 and nxt < len(reqs):
+                time.sleep(max(0.0, arrivals[nxt] - (time.perf_counter() - start)))
+        makespan = time.perf_counter() - start
+        lat, errs = [], []
+        for k, rid in enumerate(ids):
+            st, res, t = srv.poll(rid)
+            assert st == DONE
+            lat.append(t[2] - t[0])
+            g = reqs[k][0]
+            errs.append(l2norm(res - alone[k], g.Nx, g.Nz) / l2norm(alone[k], g.Nx, g.Nz))
+        stats = srv.stats()
+        srv.close()
+        out["rates"].append({
+            "offered_per_s": rate, "makespan_s": makespan, "requests_per_s": len(reqs) / makespan,
+            "field_steps_per_s": total_steps / makespan, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+            "p99_ms": 1e3 * float(np.percentile(lat, 99)),
+            "vs_one_at_a_time_fp64": (len(reqs) / makespan) / (len(reqs) / t_alone),
+            "max_rel_l2_vs_alone_fp64": float(max(errs)), "ensembles": stats["ensembles"],
+            "ensemble_steps": stats["ensemble_steps"]})
+    out.update(precision=args.serve_precision, slots=args.serve_slots, pump_steps=args.serve_pump_steps,
+               workload="f^T(u) requests: Nx,Nz in {32,48,64,96}, Ny in {33,49,65}, Re U[300,2000], Couette or "
+                        "Poiseuille, T U[5,50] at dt=0.02, SBDF3 + SMRK2 start-up, seeded fields L2 U[0.05,0.3], "
+                        "Poisson arrivals")
+    return out
+
+
 def cpu_sample(nsteps):
     """The oracle (reference algorithm restated in NumPy) on the same workload: nsteps CNAB2 steps."""
     from oracle import cf_oracle as O
@@ -257,6 +351,12 @@ def main():
     ap.add_argument("--accuracy-steps", type=int, default=1000, help="steps for the mixed-vs-FP64 error (T=10)")
     ap.add_argument("--cpu-steps", type=int, default=3, help="oracle steps in the cpu_baseline sample")
     ap.add_argument("--grid", default=None, help="Nx,Ny,Nz override for small profiling cases (not a bench line)")
+    ap.add_argument("--serve-requests", type=int, default=48, help="requests in the serving stream (0: skip)")
+    ap.add_argument("--serve-rates", type=float, nargs="*", default=[4.0, 16.0, 0.0],
+                    help="offered request rates per second (0: all at once)")
+    ap.add_argument("--serve-slots", type=int, default=4)
+    ap.add_argument("--serve-pump-steps", type=int, default=25)
+    ap.add_argument("--serve-precision", default="mixed", choices=["fp64", "mixed"])
     args = ap.parse_args()
     if args.grid:
         global NX, NY, NZ
@@ -283,6 +383,7 @@ def main():
         return
 
     res, acc, hbm, peak_kind = run_gpu(args, rank, world)
+    serve = run_serve(args) if (args.serve_requests > 0 and rank == 0) else None
     if rank != 0:
         return
     m = res["mixed"]
@@ -333,6 +434,7 @@ def main():
         "gpu_launches": m["launches"],
         "clocks": m["clocks"],
         "cpu_baseline": cpu,
+        "serve": serve,
     }
     print(json.dumps(line))
 

@@ -70,6 +70,15 @@ _SIGS = {
     "cfgpu_ensemble_cfl": [C.c_void_p, _PD],
     "cfgpu_ensemble_l2norm": [C.c_void_p, C.c_int, _PD],
     "cfgpu_ensemble_dPdx": [C.c_void_p, _PD],
+    "cfgpu_ensemble_set_params": [C.c_void_p, C.c_int, C.POINTER(Flags), _PD, _PD],
+    "cfgpu_ensemble_load_slot": [C.c_void_p, C.c_int, C.c_void_p],
+    "cfgpu_server_create": [C.c_longlong, C.c_int, C.c_int, C.POINTER(C.c_void_p)],
+    "cfgpu_server_submit": [C.c_void_p, C.POINTER(Grid), C.POINTER(Flags), C.c_int, _PD, C.POINTER(C.c_longlong)],
+    "cfgpu_server_pump": [C.c_void_p, C.c_int, _PI],
+    "cfgpu_server_poll": [C.c_void_p, C.c_longlong, _PI, _PD, _PD],
+    "cfgpu_server_release": [C.c_void_p, C.c_longlong],
+    "cfgpu_server_stats": [C.c_void_p, C.POINTER(C.c_longlong)],
+    "cfgpu_server_destroy": [C.c_void_p],
     "cfgpu_ff_write": [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                        C.c_double, C.c_int, _PD],
     "cfgpu_ff_read_header": [C.c_char_p, _PI, _PD, _PI, C.c_char_p],

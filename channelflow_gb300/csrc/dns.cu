@@ -378,6 +378,87 @@ static int setup_scheme(Scheme& s, int method, double dt) {
   return CFGPU_OK;
 }
 
+// Base flow and constraint of one field: NSE::createCFBaseFlow (nse.cpp:589-632) and
+// NSE::initCFConstraint (nse.cpp:634-671), plus the base profiles at the Gauss-Lobatto
+// points used by the nonlinear kernels (U, U', W, W').
+struct BaseFlow {
+  std::vector<double> Ubase, Wbase, Ubaseyy, Wbaseyy, basey;
+  double UbulkBase = 0, WbulkBase = 0, dPdxRef = 0, dPdzRef = 0, UbulkRef = 0, WbulkRef = 0;
+  double dPdxAct = 0, dPdzAct = 0;
+  double baseShear[2] = {0, 0};
+};
+
+int compute_base(const cfgpu_flags& f, const double* Ub, const double* Wb, int Ny, double a, double b, BaseFlow& B) {
+  if (Ub && Wb) {
+    B.Ubase.assign(Ub, Ub + Ny);
+    B.Wbase.assign(Wb, Wb + Ny);
+  } else {
+    B.Ubase.assign(Ny, 0.0);
+    B.Wbase.assign(Ny, 0.0);
+    switch (f.baseflow) {
+      case CFGPU_ZeroBase: break;
+      case CFGPU_LinearBase: B.Ubase[1] = 1; break;
+      case CFGPU_ParabolicBase: B.Ubase[0] = 0.5; B.Ubase[2] = -0.5; break;
+      case CFGPU_SuctionBase:
+        B.Ubase = laminar_profile(f.nu, CFGPU_PressureGradient, 0, f.Ubulk, f.Vsuck, a, b, -0.5, 0.5, Ny);
+        break;
+      case CFGPU_LaminarBase:
+        B.Ubase = laminar_profile(f.nu, f.constraint, f.dPdx, f.Ubulk, f.Vsuck, a, b, f.ulowerwall, f.uupperwall, Ny);
+        B.Wbase = laminar_profile(f.nu, f.constraint, f.dPdz, f.Wbulk, f.Vsuck, a, b, f.wlowerwall, f.wupperwall, Ny);
+        break;
+      default:
+        return fail(CFGPU_EINVAL, "ArbitraryBase requires Ubase and Wbase");
+    }
+  }
+  const double L = b - a;
+  B.UbulkBase = mean_h(B.Ubase);
+  B.Ubaseyy = cheb_diff_h(cheb_diff_h(B.Ubase, L), L);
+  B.WbulkBase = mean_h(B.Wbase);
+  B.Wbaseyy = cheb_diff_h(cheb_diff_h(B.Wbase, L), L);
+  {
+    std::vector<double> Uy = cheb_diff_h(B.Ubase, L), Wy = cheb_diff_h(B.Wbase, L);
+    B.baseShear[0] = f.nu * (eval_b_h(Uy) - eval_a_h(Uy)) / L;
+    B.baseShear[1] = f.nu * (eval_b_h(Wy) - eval_a_h(Wy)) / L;
+  }
+  if (f.constraint == CFGPU_BulkVelocity) {
+    B.UbulkRef = f.Ubulk;
+    B.WbulkRef = f.Wbulk;
+  } else {
+    B.dPdxAct = B.dPdxRef = f.dPdx;
+    B.dPdzAct = B.dPdzRef = f.dPdz;
+  }
+  B.basey.assign(4 * (size_t)Ny, 0.0);
+  for (int j = 0; j < Ny; ++j) {
+    long double U = 0, Uy = 0, W = 0, Wy = 0;
+    for (int n = 0; n < Ny; ++n) {
+      const long double c = cospi_ratio((long long)n * j, Ny - 1);
+      const long double dd = cheb_deriv_at(n, j, Ny) * (2.0L / (b - a));
+      U += B.Ubase[n] * c;
+      Uy += B.Ubase[n] * dd;
+      W += B.Wbase[n] * c;
+      Wy += B.Wbase[n] * dd;
+    }
+    B.basey[j] = (double)U;
+    B.basey[Ny + j] = (double)Uy;
+    B.basey[2 * Ny + j] = (double)W;
+    B.basey[3 * Ny + j] = (double)Wy;
+  }
+  return CFGPU_OK;
+}
+
+SlotParams slot_params(const cfgpu_flags& f, const BaseFlow& B) {
+  SlotParams p{};
+  p.nu = f.nu;
+  p.constraint = f.constraint;
+  p.dPdxRef = B.dPdxRef;
+  p.dPdzRef = B.dPdzRef;
+  p.umean = B.UbulkRef - B.UbulkBase;
+  p.wmean = B.WbulkRef - B.WbulkBase;
+  p.baseShear[0] = B.baseShear[0];
+  p.baseShear[1] = B.baseShear[1];
+  return p;
+}
+
 struct cfgpu_dns_s {
   int device = 0;
   cudaStream_t st = nullptr;
@@ -389,6 +470,12 @@ struct cfgpu_dns_s {
   int nb = 1;
   GridDev gm{}, gp{};
   int* dmodes = nullptr;  // kx then kz lists of gm
+  // Heterogeneous batch: per-field nu, base flow and constraint (set by cfgpu_ensemble_set_params).
+  bool hetero = false;
+  std::vector<cfgpu_flags> sfl;      // per-field flags
+  SlotParams* dslot = nullptr;       // [nb]
+  double* dbaseS = nullptr;          // [4][nb][N]: Ubase, Wbase, Ubaseyy, Wbaseyy
+  void* baseyS = nullptr;            // R-typed [nb][4N]
   int N = 0;  // Ny
   int precision = CFGPU_FP64;
   cfgpu_flags fl{};
@@ -486,9 +573,30 @@ int build_tables(cfgpu_dns d, Scheme& s) {
     TauTable t{};
     CKS(dalloc(&t.f, FN * TF_NFIELDS, d->bytes));
     CKS(dalloc(&t.s, (size_t)d->gm.Md * TS_NSCALARS, d->bytes));
-    CK(launch_tau_setup(d->gm, d->N, lt, d->fl.nu, hb, t, d->scratch, d->st));
-    d->launches++;
+    if (d->hetero) {
+      for (int f = 0; f < d->nb; ++f) {
+        CK(launch_tau_setup(d->gm, d->N, lt, d->sfl[f].nu, hb, t, d->scratch, d->st, f * d->g.Md, d->g.Md));
+        d->launches++;
+      }
+    } else {
+      CK(launch_tau_setup(d->gm, d->N, lt, d->fl.nu, hb, t, d->scratch, d->st));
+      d->launches++;
+    }
     s.tau.push_back(t);
+  }
+  return CFGPU_OK;
+}
+
+// Rebuild one field's part of every tau table (its nu changed).
+int build_slot_tables(cfgpu_dns d, int f) {
+  HelmB hb{d->hb_lo, d->hb_di, d->hb_up};
+  for (Scheme* s : {&d->main, &d->init}) {
+    if (s == &d->init && !d->has_init) continue;
+    for (size_t j = 0; j < s->tau.size(); ++j) {
+      CK(launch_tau_setup(d->gm, d->N, s->lambda_t[j], d->sfl[f].nu, hb, s->tau[j], d->scratch, d->st,
+                          f * d->g.Md, d->g.Md));
+      d->launches++;
+    }
   }
   return CFGPU_OK;
 }
@@ -508,7 +616,8 @@ int nonlinear_impl(cfgpu_dns d, const double* U, void* Nout, int form) {
   if (form == NL_ROTATIONAL) {
     if ((N + 1) / 2 <= 56) {
       CK(launch_curl_cheb<R>(g, N, U, W, (const R*)d->cinvA, (const R*)d->cinvB, (const R*)d->cderA,
-                             (const R*)d->cderB, (const R*)d->basey, d->fl.Vsuck, d->st));
+                             (const R*)d->cderB, (const R*)(d->hetero ? d->baseyS : d->basey), d->fl.Vsuck, d->st,
+                             d->hetero ? 4 * N : 0));
       d->launches += 1;
     } else {
       CK(launch_curl_base<R>(g, U, C6, d->dUbase, d->dWbase, d->fl.Vsuck, d->st));
@@ -520,7 +629,8 @@ int nonlinear_impl(cfgpu_dns d, const double* U, void* Nout, int form) {
     if ((N + 1) / 2 > 56) return fail(CFGPU_ENOTSUP, "Ny > 111 with a gradient nonlinear form");
     const bool gradient = form != NL_DIVERGENCE;
     CK(launch_grad_cheb<R>(g, N, gradient, U, W, (const R*)d->cinvA, (const R*)d->cinvB, (const R*)d->cderA,
-                           (const R*)d->cderB, (const R*)d->basey, d->fl.Vsuck, d->st));
+                           (const R*)d->cderB, (const R*)(d->hetero ? d->baseyS : d->basey), d->fl.Vsuck, d->st,
+                           d->hetero ? 4 * N : 0));
     d->launches += 1;
     nin = gradient ? 12 : 3;
     nout = form == NL_CONVECTION ? 3 : (form == NL_DIVERGENCE ? 6 : 9);
@@ -586,6 +696,15 @@ SolvePtrs base_ptrs(cfgpu_dns d) {
   p.Wbase = d->dWbase;
   p.scratch = d->scratch;
   p.dPdx_out = d->ddPdx;
+  if (d->hetero) {
+    const size_t nN = (size_t)d->nb * d->N;
+    p.Ubase = d->dbaseS;
+    p.Wbase = d->dbaseS + nN;
+    p.Ubaseyy = d->dbaseS + 2 * nN;
+    p.Wbaseyy = d->dbaseS + 3 * nN;
+    p.slot = d->dslot;
+    p.base_stride = d->N;
+  }
   return p;
 }
 
@@ -897,47 +1016,24 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
   CK(cudaGetDevice(&d->device));
   CK(cudaStreamCreateWithFlags(&d->st, cudaStreamNonBlocking));
 
-  // base flow (NSE::createCFBaseFlow, nse.cpp:589-632)
+  // base flow and constraint (NSE::createCFBaseFlow, nse.cpp:589-632; NSE::initCFConstraint, nse.cpp:634-671)
   const double a = g.a, b = g.b;
-  if (Ub && Wb) {
-    d->Ubase.assign(Ub, Ub + Ny);
-    d->Wbase.assign(Wb, Wb + Ny);
-  } else {
-    d->Ubase.assign(Ny, 0.0);
-    d->Wbase.assign(Ny, 0.0);
-    switch (f.baseflow) {
-      case CFGPU_ZeroBase: break;
-      case CFGPU_LinearBase: d->Ubase[1] = 1; break;
-      case CFGPU_ParabolicBase: d->Ubase[0] = 0.5; d->Ubase[2] = -0.5; break;
-      case CFGPU_SuctionBase:
-        d->Ubase = laminar_profile(f.nu, CFGPU_PressureGradient, 0, f.Ubulk, f.Vsuck, a, b, -0.5, 0.5, Ny);
-        break;
-      case CFGPU_LaminarBase:
-        d->Ubase = laminar_profile(f.nu, f.constraint, f.dPdx, f.Ubulk, f.Vsuck, a, b, f.ulowerwall, f.uupperwall, Ny);
-        d->Wbase = laminar_profile(f.nu, f.constraint, f.dPdz, f.Wbulk, f.Vsuck, a, b, f.wlowerwall, f.wupperwall, Ny);
-        break;
-      default:
-        return fail(CFGPU_EINVAL, "ArbitraryBase requires Ubase and Wbase");
-    }
-  }
-  // NSE::initCFConstraint (nse.cpp:634-671)
-  const double L = b - a;
-  d->UbulkBase = mean_h(d->Ubase);
-  d->Ubaseyy = cheb_diff_h(cheb_diff_h(d->Ubase, L), L);
-  d->WbulkBase = mean_h(d->Wbase);
-  d->Wbaseyy = cheb_diff_h(cheb_diff_h(d->Wbase, L), L);
-  {
-    std::vector<double> Uy = cheb_diff_h(d->Ubase, L), Wy = cheb_diff_h(d->Wbase, L);
-    d->baseShear[0] = f.nu * (eval_b_h(Uy) - eval_a_h(Uy)) / L;
-    d->baseShear[1] = f.nu * (eval_b_h(Wy) - eval_a_h(Wy)) / L;
-  }
-  if (f.constraint == CFGPU_BulkVelocity) {
-    d->UbulkRef = f.Ubulk;
-    d->WbulkRef = f.Wbulk;
-  } else {
-    d->dPdxAct = d->dPdxRef = f.dPdx;
-    d->dPdzAct = d->dPdzRef = f.dPdz;
-  }
+  BaseFlow bf;
+  CKS(compute_base(f, Ub, Wb, Ny, a, b, bf));
+  d->Ubase = bf.Ubase;
+  d->Wbase = bf.Wbase;
+  d->Ubaseyy = bf.Ubaseyy;
+  d->Wbaseyy = bf.Wbaseyy;
+  d->UbulkBase = bf.UbulkBase;
+  d->WbulkBase = bf.WbulkBase;
+  d->baseShear[0] = bf.baseShear[0];
+  d->baseShear[1] = bf.baseShear[1];
+  d->UbulkRef = bf.UbulkRef;
+  d->WbulkRef = bf.WbulkRef;
+  d->dPdxAct = bf.dPdxAct;
+  d->dPdxRef = bf.dPdxRef;
+  d->dPdzAct = bf.dPdzAct;
+  d->dPdzRef = bf.dPdzRef;
   (void)u0;
   long long& B = d->bytes;
   CKS(dalloc(&d->dUbase, Ny, B));
@@ -1002,22 +1098,7 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
   for (auto& v : cm.derB) v *= 2.0 / (b - a);
   for (auto& v : cm.dfA) v *= 2.0 / (b - a);
   for (auto& v : cm.dfB) v *= 2.0 / (b - a);
-  std::vector<double> basey(4 * (size_t)Ny, 0.0);
-  for (int j = 0; j < Ny; ++j) {
-    long double U = 0, Uy = 0, W = 0, Wy = 0;
-    for (int n = 0; n < Ny; ++n) {
-      const long double c = cospi_ratio((long long)n * j, Ny - 1);
-      const long double dd = cheb_deriv_at(n, j, Ny) * (2.0L / (b - a));
-      U += d->Ubase[n] * c;
-      Uy += d->Ubase[n] * dd;
-      W += d->Wbase[n] * c;
-      Wy += d->Wbase[n] * dd;
-    }
-    basey[j] = (double)U;
-    basey[Ny + j] = (double)Uy;
-    basey[2 * Ny + j] = (double)W;
-    basey[3 * Ny + j] = (double)Wy;
-  }
+  const std::vector<double>& basey = bf.basey;
   const bool fp64 = d->precision == CFGPU_FP64;
   if (fp64) {
     CKS(upload_tw<double>(twx, &d->twx, B));
@@ -1135,6 +1216,7 @@ void dns_free(cfgpu_dns d) {
   F(d->hb_lo); F(d->hb_di); F(d->hb_up);
   F(d->twx); F(d->twz); F(d->cinvA); F(d->cinvB); F(d->cfwdA); F(d->cfwdB);
   F(d->cderA); F(d->cderB); F(d->basey); F(d->cdfA); F(d->cdfB); F(d->dyc); F(d->dred); F(d->dmodes);
+  F(d->dslot); F(d->dbaseS); F(d->baseyS);
   F(d->Ucur); F(d->Qcur);
   for (int j = 0; j < 4; ++j) { F(d->Uh[j]); F(d->Qh[j]); F(d->Nh[j]); }
   for (int w = 0; w < 2; ++w) { F(d->fj[w]); F(d->fj1[w]); F(d->rkQ[w]); }
@@ -1260,6 +1342,102 @@ struct TimeStepH {
 // ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------
+// Runtime hooks used by the request server (server.cu); not part of the C ABI.
+namespace cfgpu_rt {
+int advance_async(cfgpu_dns d, int nsteps) { return dns_advance_device(d, nsteps); }
+cudaStream_t stream(cfgpu_dns d) { return d->st; }
+long long bytes(cfgpu_dns d) { return d->bytes; }
+int nfields(cfgpu_dns d) { return d->nb; }
+
+// Steps DNS::advance takes with the start-up scheme before the main scheme runs alone.
+int startup_steps(cfgpu_dns d) {
+  if (d->main.full) return 0;
+  return d->main.family == 0 ? d->main.countdown : 1;
+}
+
+// Back to the state of a fresh DNS (time t0, start-up steps pending) without rebuilding tables.
+int restart(cfgpu_dns d) {
+  for (Scheme* s : {&d->main, &d->init}) {
+    if (s == &d->init && !d->has_init) continue;
+    std::vector<TauTable> keep = s->tau;
+    CKS(setup_scheme(*s, s->method, d->fl.dt));
+    s->tau = keep;
+    s->t = d->fl.t0;
+  }
+  d->alt[0] = d->alt[1] = (d->fl.nonlinearity == CFGPU_Alternating_) ? 1 : 0;
+  for (int j = 0; j < 4; ++j) d->perm[j] = j;
+  const size_t cd = d->compc(), rs = d->rsz();
+  for (int w = 0; w < 2; ++w)
+    if (d->rkQ[w]) CK(cudaMemsetAsync(d->rkQ[w], 0, 3 * cd * rs, d->st));  // 0 * stale NaN would stay NaN
+  return CFGPU_OK;
+}
+
+// Device bytes a DNS of nb fields with these flags allocates (the allocations of dns_create_impl).
+long long estimate_bytes(const cfgpu_grid& grid, const cfgpu_flags& f, int nb, int precision) {
+  const bool dxz = f.dealiasing == CFGPU_DealiasXZ;
+  const long long Kx = dxz ? grid.Nx / 3 - 1 : grid.Nx / 2 - 1, Kz = dxz ? grid.Nz / 3 - 1 : grid.Nz / 2 - 1;
+  const long long Md = (2 * Kx + 1) * (Kz + 1), N = grid.Ny;
+  const long long cd = 2 * Md * N * nb, rs = precision == CFGPU_FP64 ? 8 : 4;
+  const bool rot = f.nonlinearity == CFGPU_Rotational;
+  const long long nin = rot ? 6 : 12, nout = rot ? 3 : 9, plane = 2LL * grid.Nx * (Kz + 1) * N * nb;
+  long long b = 4 * cd * 8 + 6 * cd * rs + nin * cd * rs + nin * plane * rs + nout * plane * rs + nout * cd * rs +
+                8 * cd * 8;
+  Scheme m{}, i{};
+  if (setup_scheme(m, f.timestepping, f.dt) != CFGPU_OK) return -1;
+  int ntab = (int)m.lambda_t.size();
+  auto hist = [&](const Scheme& s) -> long long {
+    if (s.family == 0) return s.order * (4 * cd * 8 + 3 * cd * rs);
+    if (s.family == 1) return 6 * cd * rs;
+    return 6 * cd * rs;
+  };
+  b += hist(m);
+  if (!m.full && f.initstepping != f.timestepping && setup_scheme(i, f.initstepping, f.dt) == CFGPU_OK) {
+    b += hist(i);
+    ntab += (int)i.lambda_t.size();
+  }
+  b += ntab * (TF_NFIELDS * N * Md * nb + TS_NSCALARS * Md * nb) * 8;
+  return b + (1 << 20);
+}
+}  // namespace cfgpu_rt
+
+namespace {
+// Upload the per-field parameter arrays of a heterogeneous batch from d->sfl.
+template <typename R>
+int upload_slot(cfgpu_dns d, int f, const BaseFlow& B) {
+  const size_t N = d->N, nN = (size_t)d->nb * N;
+  const SlotParams sp = slot_params(d->sfl[f], B);
+  CK(cudaMemcpyAsync(d->dslot + f, &sp, sizeof(sp), cudaMemcpyHostToDevice, d->st));
+  const std::vector<double>* arrs[4] = {&B.Ubase, &B.Wbase, &B.Ubaseyy, &B.Wbaseyy};
+  for (int k = 0; k < 4; ++k)
+    CK(cudaMemcpyAsync(d->dbaseS + k * nN + f * N, arrs[k]->data(), N * sizeof(double), cudaMemcpyHostToDevice,
+                       d->st));
+  std::vector<R> by(B.basey.begin(), B.basey.end());
+  CK(cudaMemcpyAsync((R*)d->baseyS + f * 4 * N, by.data(), by.size() * sizeof(R), cudaMemcpyHostToDevice, d->st));
+  const double init[2] = {B.dPdxAct, B.dPdzAct};
+  CK(cudaMemcpyAsync(d->ddPdx + 2 * f, init, sizeof(init), cudaMemcpyHostToDevice, d->st));
+  CK(cudaStreamSynchronize(d->st));  // host sources are locals
+  return CFGPU_OK;
+}
+
+int ensure_hetero(cfgpu_dns d) {
+  if (d->hetero) return CFGPU_OK;
+  const size_t N = d->N, nb = d->nb;
+  CKS(dalloc(&d->dslot, nb, d->bytes));
+  CKS(dalloc(&d->dbaseS, 4 * nb * N, d->bytes));
+  unsigned char* tmp;
+  CKS(dalloc(&tmp, 4 * nb * N * d->rsz(), d->bytes));
+  d->baseyS = tmp;
+  d->sfl.assign(nb, d->fl);
+  BaseFlow B;
+  CKS(compute_base(d->fl, d->fl.baseflow == CFGPU_ArbitraryBase ? d->Ubase.data() : nullptr,
+                   d->fl.baseflow == CFGPU_ArbitraryBase ? d->Wbase.data() : nullptr, d->N, d->g.a, d->g.b, B));
+  d->hetero = true;
+  for (int f = 0; f < d->nb; ++f)
+    CKS(d->precision == CFGPU_FP64 ? upload_slot<double>(d, f, B) : upload_slot<float>(d, f, B));
+  return CFGPU_OK;
+}
+}  // namespace
+
 extern "C" {
 
 const char* cfgpu_version(void) { return "cfgpu 0.1 (sm_103a)"; }
@@ -1323,6 +1501,73 @@ cfgpu_status cfgpu_ensemble_create(const cfgpu_grid* grid, const cfgpu_flags* fl
     return s;
   }
   *out = d;
+  return CFGPU_OK;
+}
+
+
+cfgpu_status cfgpu_ensemble_set_params(cfgpu_dns d, int slot, const cfgpu_flags* f, const double* Ubase,
+                                       const double* Wbase) {
+  if (!d || !f || slot < 0 || slot >= d->nb) return fail(CFGPU_EINVAL, "bad argument");
+  if ((Ubase == nullptr) != (Wbase == nullptr)) return fail(CFGPU_EINVAL, "Ubase and Wbase must both be given");
+  const cfgpu_flags& e = d->fl;
+  if (f->dt != e.dt || f->timestepping != e.timestepping || f->initstepping != e.initstepping ||
+      f->nonlinearity != e.nonlinearity || f->dealiasing != e.dealiasing || f->taucorrection != e.taucorrection ||
+      f->Vsuck != e.Vsuck)
+    return fail(CFGPU_EINVAL,
+                "per-field flags may change nu, base flow, walls and constraint only (dt, schemes, nonlinearity, "
+                "dealiasing, taucorrection and Vsuck are shared)");
+  if (f->nu <= 0) return fail(CFGPU_EINVAL, "nu must be positive");
+  if ((d->N + 1) / 2 > 56) return fail(CFGPU_ENOTSUP, "per-field parameters need Ny <= 111");
+  CKS(ensure_hetero(d));
+  BaseFlow B;
+  CKS(compute_base(*f, Ubase, Wbase, d->N, d->g.a, d->g.b, B));
+  d->sfl[slot] = *f;
+  CKS(d->precision == CFGPU_FP64 ? upload_slot<double>(d, slot, B) : upload_slot<float>(d, slot, B));
+  CKS(build_slot_tables(d, slot));
+  CK(cudaStreamSynchronize(d->st));
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_ensemble_load_slot(cfgpu_dns d, int slot, cfgpu_dns src) {
+  if (!d || !src || slot < 0 || slot >= d->nb || src->nb != 1) return fail(CFGPU_EINVAL, "bad argument");
+  const GridDev &a = d->g, &b = src->g;
+  if (a.Nx != b.Nx || a.Ny != b.Ny || a.Nz != b.Nz || a.Md != b.Md || a.Lx != b.Lx || a.Lz != b.Lz ||
+      a.a != b.a || a.b != b.b || d->precision != src->precision || d->device != src->device)
+    return fail(CFGPU_EINVAL, "source DNS has another grid, precision or device");
+  if (d->fl.timestepping != src->fl.timestepping || d->fl.dt != src->fl.dt ||
+      d->fl.nonlinearity != src->fl.nonlinearity || d->alt[0] != src->alt[0])
+    return fail(CFGPU_EINVAL, "source DNS has another scheme, dt or nonlinearity state");
+  if (!src->main.full) return fail(CFGPU_EINVAL, "the source DNS must be past its start-up steps");
+  if (!d->main.full) {
+    // the ensemble's fields arrive through this call, already started: its scheme runs main steps from now on
+    d->main.countdown = 0;
+    d->main.full = true;
+  }
+  CK(cudaStreamSynchronize(src->st));
+  const size_t w = 2 * (size_t)a.Md, pitch = w * d->nb, N = d->N;
+  auto copy = [&](void* dst, const void* srcp, size_t esz, size_t rows) -> int {
+    CK(cudaMemcpy2DAsync((unsigned char*)dst + slot * w * esz, pitch * esz, srcp, w * esz, w * esz, rows,
+                         cudaMemcpyDeviceToDevice, d->st));
+    return CFGPU_OK;
+  };
+  const size_t rs = d->rsz();
+  CKS(copy(d->Ucur, src->Ucur, 8, 3 * N));
+  CKS(copy(d->Qcur, src->Qcur, 8, N));
+  const Scheme& m = d->main;
+  if (m.family == 0) {
+    for (int j = 1; j < m.order; ++j) {
+      CKS(copy(d->Uh[d->perm[j]], src->Uh[src->perm[j]], 8, 3 * N));
+      CKS(copy(d->Qh[d->perm[j]], src->Qh[src->perm[j]], 8, N));
+      CKS(copy(d->Nh[d->perm[j]], src->Nh[src->perm[j]], rs, 3 * N));
+    }
+  } else if (m.family == 1) {
+    CKS(copy(d->fj[0], src->fj[0], rs, 3 * N));
+    CKS(copy(d->fj1[0], src->fj1[0], rs, 3 * N));
+  } else {
+    CKS(copy(d->rkQ[0], src->rkQ[0], rs, 3 * N));
+  }
+  CK(cudaMemcpyAsync(d->ddPdx + 2 * slot, src->ddPdx, 2 * sizeof(double), cudaMemcpyDeviceToDevice, d->st));
+  CK(cudaStreamSynchronize(d->st));
   return CFGPU_OK;
 }
 

@@ -19,7 +19,8 @@ template <typename R>
 size_t curl_cheb_smem_bytes(int N);
 template <typename R>
 cudaError_t launch_curl_cheb(const GridDev& g, int N, const double* U, R* W6, const R* CA, const R* CB, const R* DA,
-                             const R* DB, const R* basey, double Vsuck, cudaStream_t st);
+                             const R* DB, const R* basey, double Vsuck, cudaStream_t st,
+                             int bstride = 0);
 
 template <typename TI, typename R, typename TO>
 cudaError_t launch_cheb(int N, bool inverse, int nlines, int ncomp, const TI* in, size_t ld_in, size_t cs_in, TO* out,
@@ -32,7 +33,8 @@ template <typename R>
 size_t grad_cheb_smem_bytes(int N);
 template <typename R>
 cudaError_t launch_grad_cheb(const GridDev& g, int N, bool gradient, const double* U, R* W, const R* CA, const R* CB,
-                             const R* DA, const R* DB, const R* basey, double Vsuck, cudaStream_t st);
+                             const R* DA, const R* DB, const R* basey, double Vsuck, cudaStream_t st,
+                             int bstride = 0);
 template <typename R>
 size_t zphys_smem_bytes(const GridDev& g, int form, int RP);
 template <typename R>
@@ -85,8 +87,9 @@ struct HelmB {
   const double* up;
 };
 
+// Tables of modes m0 .. m0+mcount-1 of g (mcount <= 0: all modes) for lambda_t and nu.
 cudaError_t launch_tau_setup(const GridDev& g, int N, double lambda_t, double nu, const HelmB& hb, TauTable tt,
-                             double* scratch, cudaStream_t st);
+                             double* scratch, cudaStream_t st, int m0 = 0, int mcount = 0);
 
 // Per-mode solve parameters for one substep.
 struct SolveParams {
@@ -105,6 +108,14 @@ struct SolveParams {
   int force_real00;  // NSE::solve keeps only the real part of the (0,0) mode
 };
 
+// Per-field parameters of a heterogeneous field batch (one entry per field);
+// they replace the SolveParams fields of the same names for that field's modes.
+struct SlotParams {
+  double nu, dPdxRef, dPdzRef, umean, wmean, baseShear[2];
+  int constraint;
+  int pad;
+};
+
 struct SolvePtrs {
   const double* uin[4];  // multistep history u_j (3 comps each, complex [3][N][Md])
   const void* nin[4];    // N_j (R-typed, [3][N][Md] complex)
@@ -117,7 +128,9 @@ struct SolvePtrs {
   const double* Ubase;   // for the bulk-velocity linear term
   const double* Wbase;
   double* scratch;       // [8][N][2Md]
-  double* dPdx_out;      // device scalars: actual dPdx, dPdz after solve
+  double* dPdx_out;      // device scalars: actual dPdx, dPdz after solve ([field][2] for a batch)
+  const SlotParams* slot;  // per-field parameters (null: SolveParams holds them for every field)
+  int base_stride;         // 0: one base flow for all fields; N: Ubase/Wbase/Ubaseyy/Wbaseyy are [field][N]
 };
 
 template <typename R>

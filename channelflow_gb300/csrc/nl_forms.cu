@@ -26,7 +26,8 @@ template <typename R, int MODE>
 __global__ void __launch_bounds__(256) k_grad_cheb(GridDev g, int N, const double* __restrict__ U, R* __restrict__ W,
                                                    const R* __restrict__ CA, const R* __restrict__ CB,
                                                    const R* __restrict__ DA, const R* __restrict__ DB,
-                                                   const R* __restrict__ basey, R Vsuck) {
+                                                   const R* __restrict__ basey, R Vsuck,
+                                                   int bstride) {
   extern __shared__ unsigned char smem_raw[];
   const int P = (N + 1) / 2, KA = (N + 1) / 2, KB = (N - 1) / 2, J = (N - 1) / 2;
   R* xs = reinterpret_cast<R*>(smem_raw);  // [3][N][TL]: even coefs rows 0..KA-1, odd KA..N-1
@@ -105,6 +106,7 @@ __global__ void __launch_bounds__(256) k_grad_cheb(GridDev g, int N, const doubl
   const R dx = (R)(2.0 * M_PI * kx / g.Lx * (kx == g.kxmax ? 0.0 : 1.0));
   const R dz = (R)(2.0 * M_PI * kz / g.Lz * (kz == g.kzmax ? 0.0 : 1.0));
   const bool base = (kx == 0 && kz == 0 && part == 0);
+  const R* __restrict__ by = basey + (size_t)bstride * mode_field(g, m);  // this field's base flow
 #pragma unroll
   for (int i = 0; i < GC_PT; ++i) {
     const int p = warp + 8 * i;
@@ -122,12 +124,12 @@ __global__ void __launch_bounds__(256) k_grad_cheb(GridDev g, int N, const doubl
         for (int c = 0; c < 3; ++c) dy[c] = bo[3 + c][i] + sg * ae[3 + c][i];
       }
       if (base) {
-        u[0] += basey[j];
-        u[2] += basey[2 * N + j];
+        u[0] += by[j];
+        u[2] += by[2 * N + j];
         u[1] -= Vsuck;
         if (MODE == 1) {
-          dy[0] += basey[N + j];
-          dy[2] += basey[3 * N + j];
+          dy[0] += by[N + j];
+          dy[2] += by[3 * N + j];
         }
       }
       R* o = W + (size_t)j * row + gl;
@@ -402,7 +404,8 @@ size_t grad_cheb_smem_bytes(int N) {
 
 template <typename R>
 cudaError_t launch_grad_cheb(const GridDev& g, int N, bool gradient, const double* U, R* W, const R* CA, const R* CB,
-                             const R* DA, const R* DB, const R* basey, double Vsuck, cudaStream_t st) {
+                             const R* DA, const R* DB, const R* basey, double Vsuck, cudaStream_t st,
+                             int bstride) {
   if ((N + 1) / 2 > 8 * GC_PT) return cudaErrorInvalidValue;
   static bool attr_set = false;
   if (!attr_set) {
@@ -413,9 +416,9 @@ cudaError_t launch_grad_cheb(const GridDev& g, int N, bool gradient, const doubl
   const int nlines = 2 * g.Md;
   const dim3 grid((nlines + GC_TL - 1) / GC_TL);
   if (gradient)
-    k_grad_cheb<R, 1><<<grid, 256, grad_cheb_smem_bytes<R>(N), st>>>(g, N, U, W, CA, CB, DA, DB, basey, (R)Vsuck);
+    k_grad_cheb<R, 1><<<grid, 256, grad_cheb_smem_bytes<R>(N), st>>>(g, N, U, W, CA, CB, DA, DB, basey, (R)Vsuck, bstride);
   else
-    k_grad_cheb<R, 2><<<grid, 256, grad_cheb_smem_bytes<R>(N), st>>>(g, N, U, W, CA, CB, DA, DB, basey, (R)Vsuck);
+    k_grad_cheb<R, 2><<<grid, 256, grad_cheb_smem_bytes<R>(N), st>>>(g, N, U, W, CA, CB, DA, DB, basey, (R)Vsuck, bstride);
   return cudaGetLastError();
 }
 
@@ -478,7 +481,7 @@ cudaError_t launch_cheb_fwd_div(const GridDev& g, int N, const R* pF, const R* p
 #define INST_FORMS(R)                                                                                              \
   template size_t grad_cheb_smem_bytes<R>(int);                                                                    \
   template cudaError_t launch_grad_cheb<R>(const GridDev&, int, bool, const double*, R*, const R*, const R*,      \
-                                           const R*, const R*, const R*, double, cudaStream_t);                    \
+                                           const R*, const R*, const R*, double, cudaStream_t, int);               \
   template size_t zphys_smem_bytes<R>(const GridDev&, int, int);                                                   \
   template cudaError_t launch_zphys<R>(const GridDev&, int, const FftPlan&, const cpx<R>*, int, const cpx<R>*,      \
                                        cpx<R>*, cudaStream_t);                                                     \

@@ -198,7 +198,8 @@ template <typename R>
 __global__ void __launch_bounds__(256) k_curl_cheb(GridDev g, int N, const double* __restrict__ U, R* __restrict__ W6,
                                                    const R* __restrict__ CA, const R* __restrict__ CB,
                                                    const R* __restrict__ DA, const R* __restrict__ DB,
-                                                   const R* __restrict__ basey, R Vsuck) {
+                                                   const R* __restrict__ basey, R Vsuck,
+                                                   int bstride) {
   extern __shared__ unsigned char smem_raw[];
   const int P = (N + 1) / 2, KA = (N + 1) / 2, KB = (N - 1) / 2, J = (N - 1) / 2;
   R* xs = reinterpret_cast<R*>(smem_raw);           // [3][N][CC_TL]: even coefs rows 0..KA-1, odd KA..N-1
@@ -264,6 +265,7 @@ __global__ void __launch_bounds__(256) k_curl_cheb(GridDev g, int N, const doubl
   const R dx = (R)(2.0 * M_PI * kx / g.Lx * (kx == g.kxmax ? 0.0 : 1.0));
   const R dz = (R)(2.0 * M_PI * kz / g.Lz * (kz == g.kzmax ? 0.0 : 1.0));
   const bool base = (kx == 0 && kz == 0 && part == 0);
+  const R* __restrict__ by = basey + (size_t)bstride * mode_field(g, m);  // this field's base flow
 #pragma unroll
   for (int i = 0; i < CC_PT; ++i) {
     const int p = warp + 8 * i;
@@ -276,10 +278,10 @@ __global__ void __launch_bounds__(256) k_curl_cheb(GridDev g, int N, const doubl
       R u = aCu[i] + sg * bCu[i], v = aCv[i] + sg * bCv[i], w = aCw[i] + sg * bCw[i];
       R du = bDu[i] + sg * aDu[i], dw = bDw[i] + sg * aDw[i];
       if (base) {
-        u += basey[j];
-        du += basey[N + j];
-        w += basey[2 * N + j];
-        dw += basey[3 * N + j];
+        u += by[j];
+        du += by[N + j];
+        w += by[2 * N + j];
+        dw += by[3 * N + j];
         v -= Vsuck;
       }
       const R ou = __shfl_xor_sync(0xffffffffu, u, 1);
@@ -316,7 +318,8 @@ size_t curl_cheb_smem_bytes(int N) {
 
 template <typename R>
 cudaError_t launch_curl_cheb(const GridDev& g, int N, const double* U, R* W6, const R* CA, const R* CB, const R* DA,
-                             const R* DB, const R* basey, double Vsuck, cudaStream_t st) {
+                             const R* DB, const R* basey, double Vsuck, cudaStream_t st,
+                             int bstride) {
   if ((N + 1) / 2 > 8 * CC_PT) return cudaErrorInvalidValue;
   static bool attr_set = false;
   if (!attr_set) {
@@ -325,14 +328,14 @@ cudaError_t launch_curl_cheb(const GridDev& g, int N, const double* U, R* W6, co
   }
   const int nlines = 2 * g.Md;
   k_curl_cheb<R><<<(nlines + CC_TL - 1) / CC_TL, 256, curl_cheb_smem_bytes<R>(N), st>>>(g, N, U, W6, CA, CB, DA, DB,
-                                                                                         basey, (R)Vsuck);
+                                                                                         basey, (R)Vsuck, bstride);
   return cudaGetLastError();
 }
 template cudaError_t launch_curl_cheb<float>(const GridDev&, int, const double*, float*, const float*, const float*,
-                                             const float*, const float*, const float*, double, cudaStream_t);
+                                             const float*, const float*, const float*, double, cudaStream_t, int);
 template cudaError_t launch_curl_cheb<double>(const GridDev&, int, const double*, double*, const double*,
                                               const double*, const double*, const double*, const double*, double,
-                                              cudaStream_t);
+                                              cudaStream_t, int);
 template size_t curl_cheb_smem_bytes<float>(int);
 template size_t curl_cheb_smem_bytes<double>(int);
 

@@ -149,10 +149,23 @@ __device__ __forceinline__ int n_func(int k, int Nb) {
   return 2 * Nb;
 }
 
-// One thread per mode: the TauSolver constructor for lambda = lambda_t + nu kappa^2.
-__global__ void k_tau_setup(GridDev g, int N, double lambda_t, double nu, HelmB hb, TauTable tt, double* scratch) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= g.Md) return;
+__device__ __forceinline__ void apply_slot(SolveParams& sp, const SlotParams& s) {
+  sp.nu = s.nu;
+  sp.constraint = s.constraint;
+  sp.dPdxRef = s.dPdxRef;
+  sp.dPdzRef = s.dPdzRef;
+  sp.umean = s.umean;
+  sp.wmean = s.wmean;
+  sp.baseShear[0] = s.baseShear[0];
+  sp.baseShear[1] = s.baseShear[1];
+}
+
+// One thread per mode: the TauSolver constructor for lambda = lambda_t + nu kappa^2,
+// for modes m0 .. m0+mcount-1.
+__global__ void k_tau_setup(GridDev g, int N, double lambda_t, double nu, HelmB hb, TauTable tt, double* scratch,
+                            int m0, int mcount) {
+  const int m = m0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= m0 + mcount || m >= g.Md) return;
   const size_t Md = g.Md;
   const size_t FN = (size_t)N * Md;
   auto T = [&](int f) { return Ln{tt.f + f * FN + m, Md}; };
@@ -228,9 +241,13 @@ __global__ void k_tau_setup(GridDev g, int N, double lambda_t, double nu, HelmB 
 }
 
 cudaError_t launch_tau_setup(const GridDev& g, int N, double lambda_t, double nu, const HelmB& hb, TauTable tt,
-                             double* scratch, cudaStream_t st) {
+                             double* scratch, cudaStream_t st, int m0, int mcount) {
   const int T = 64;
-  k_tau_setup<<<(g.Md + T - 1) / T, T, 0, st>>>(g, N, lambda_t, nu, hb, tt, scratch);
+  if (mcount <= 0) {
+    m0 = 0;
+    mcount = g.Md;
+  }
+  k_tau_setup<<<(mcount + T - 1) / T, T, 0, st>>>(g, N, lambda_t, nu, hb, tt, scratch, m0, mcount);
   return cudaGetLastError();
 }
 
@@ -368,6 +385,9 @@ __global__ void __launch_bounds__(128) k_tau_solve(GridDev g, int N, SolveParams
   const double kxL = 2 * M_PI * kx / g.Lx;
   const double kzL = 2 * M_PI * kz / g.Lz;
   const double scale = 4.0 / (g.b - g.a);
+  const int fld = mode_field(g, m);
+  if (P.slot) apply_slot(sp, P.slot[fld]);
+  const size_t fb = (size_t)P.base_stride * fld;
   const double nu = sp.nu;
   const double lambda = tt.s[TS_LAMBDA * Md + m];
   const double* __restrict__ hlo = hb.lo;
@@ -383,7 +403,7 @@ __global__ void __launch_bounds__(128) k_tau_solve(GridDev g, int N, SolveParams
         for (int j = 0; j < sp.order; ++j)
           acc += sp.a[j] * P.uin[j][c * comp + o] + sp.b[j] * (double)static_cast<const R*>(P.nin[j])[c * comp + o];
         if (m00 && part == 0 && c != 1) {
-          acc += nu * (c == 0 ? P.Ubaseyy[2 * i + q] : P.Wbaseyy[2 * i + q]);
+          acc += nu * (c == 0 ? P.Ubaseyy[fb + 2 * i + q] : P.Wbaseyy[fb + 2 * i + q]);
           if (2 * i + q == 0 && sp.constraint == 0) acc -= (c == 0 ? sp.dPdxRef : sp.dPdzRef);
         }
         if (act) SC[c][o] = acc;
@@ -440,7 +460,7 @@ __global__ void __launch_bounds__(128) k_tau_solve(GridDev g, int N, SolveParams
         }
         double L = d2 - kappa2 * uk[i] - gq;
         if (m00 && part == 0 && c != 1) {
-          L += nu * (c == 0 ? P.Ubaseyy[n] : P.Wbaseyy[n]);
+          L += nu * (c == 0 ? P.Ubaseyy[fb + n] : P.Wbaseyy[fb + n]);
           if (n == 0) L -= sp.constraint == 0 ? (c == 0 ? sp.dPdxRef : sp.dPdzRef)
                                               : wall + sp.baseShear[c == 0 ? 0 : 1];
         }
@@ -456,7 +476,7 @@ __global__ void __launch_bounds__(128) k_tau_solve(GridDev g, int N, SolveParams
           rhs = L + (sp.lam * u0 + sp.B_C * Qn);
         }
         if (m00 && part == 0 && c != 1) {
-          rhs += nu * (c == 0 ? P.Ubaseyy[n] : P.Wbaseyy[n]);
+          rhs += nu * (c == 0 ? P.Ubaseyy[fb + n] : P.Wbaseyy[fb + n]);
           if (n == 0 && sp.constraint == 0) rhs -= (c == 0 ? sp.dPdxRef : sp.dPdzRef);
         }
         if (act) out[i] = rhs;
@@ -693,6 +713,9 @@ __global__ void __launch_bounds__(32) k_tau_solve_s(GridDev g, int N, SolveParam
   const bool m00 = (kx == 0 && kz == 0);
   const double kxL = 2 * M_PI * kx / g.Lx;
   const double kzL = 2 * M_PI * kz / g.Lz;
+  const int fld = mode_field(g, m);
+  if (P.slot) apply_slot(sp, P.slot[fld]);
+  const size_t fb = (size_t)P.base_stride * fld;
   const double nu = sp.nu;
   const double lambda = tt.s[TS_LAMBDA * Md + m];
   const double* __restrict__ hlo = hb.lo;
@@ -710,7 +733,7 @@ __global__ void __launch_bounds__(32) k_tau_solve_s(GridDev g, int N, SolveParam
         for (int j = 0; j < sp.order; ++j)
           acc += sp.a[j] * P.uin[j][c * comp + o] + sp.b[j] * (double)static_cast<const R*>(P.nin[j])[c * comp + o];
         if (m00 && part == 0 && c != 1) {
-          acc += nu * (c == 0 ? P.Ubaseyy[2 * i + q] : P.Wbaseyy[2 * i + q]);
+          acc += nu * (c == 0 ? P.Ubaseyy[fb + 2 * i + q] : P.Wbaseyy[fb + 2 * i + q]);
           if (2 * i + q == 0 && sp.constraint == 0) acc -= (c == 0 ? sp.dPdxRef : sp.dPdzRef);
         }
         out[i] = acc;
@@ -789,7 +812,7 @@ __global__ void __launch_bounds__(32) k_tau_solve_s(GridDev g, int N, SolveParam
         const double u0 = uc[i];
         double L = d2 - kappa2 * (nu * u0) - gq;
         if (m00 && part == 0 && c != 1) {
-          L += nu * (c == 0 ? P.Ubaseyy[n] : P.Wbaseyy[n]);
+          L += nu * (c == 0 ? P.Ubaseyy[fb + n] : P.Wbaseyy[fb + n]);
           if (n == 0) L -= sp.constraint == 0 ? (c == 0 ? sp.dPdxRef : sp.dPdzRef)
                                               : wall + sp.baseShear[c == 0 ? 0 : 1];
         }
@@ -804,7 +827,7 @@ __global__ void __launch_bounds__(32) k_tau_solve_s(GridDev g, int N, SolveParam
           rhs = L + (sp.lam * u0 + sp.B_C * Qn);
         }
         if (m00 && part == 0 && c != 1) {
-          rhs += nu * (c == 0 ? P.Ubaseyy[n] : P.Wbaseyy[n]);
+          rhs += nu * (c == 0 ? P.Ubaseyy[fb + n] : P.Wbaseyy[fb + n]);
           if (n == 0 && sp.constraint == 0) rhs -= (c == 0 ? sp.dPdxRef : sp.dPdzRef);
         }
         out[i] = rhs;
@@ -1018,6 +1041,9 @@ __global__ void __launch_bounds__(32) k_tau_solve_t(GridDev g, int N, SolveParam
   const bool m00 = (kx == 0 && kz == 0);
   const double kxL = 2 * M_PI * kx / g.Lx;
   const double kzL = 2 * M_PI * kz / g.Lz;
+  const int fld = mode_field(g, m);
+  if (P.slot) apply_slot(sp, P.slot[fld]);
+  const size_t fb = (size_t)P.base_stride * fld;
   const double nu = sp.nu;
   const double lambda = tt.s[TS_LAMBDA * Md + m];
   const double* __restrict__ hlo = hb.lo;
@@ -1054,7 +1080,7 @@ __global__ void __launch_bounds__(32) k_tau_solve_t(GridDev g, int N, SolveParam
             const int i = i0 + k, n = 2 * i + q;
             double a = acc[k];
             if (m00 && part == 0 && c != 1) {
-              a += nu * (c == 0 ? P.Ubaseyy[n] : P.Wbaseyy[n]);
+              a += nu * (c == 0 ? P.Ubaseyy[fb + n] : P.Wbaseyy[fb + n]);
               if (n == 0 && sp.constraint == 0) a -= (c == 0 ? sp.dPdxRef : sp.dPdzRef);
             }
             if (c == 1) outy[i] = a;
@@ -1151,7 +1177,7 @@ __global__ void __launch_bounds__(32) k_tau_solve_t(GridDev g, int N, SolveParam
           const double u0 = uv[k];
           double L = d2 - kappa2 * (nu * u0) - gq;
           if (m00 && part == 0 && c != 1) {
-            L += nu * (c == 0 ? P.Ubaseyy[n] : P.Wbaseyy[n]);
+            L += nu * (c == 0 ? P.Ubaseyy[fb + n] : P.Wbaseyy[fb + n]);
             if (n == 0) L -= sp.constraint == 0 ? (c == 0 ? sp.dPdxRef : sp.dPdzRef)
                                                 : wall + sp.baseShear[c == 0 ? 0 : 1];
           }
@@ -1165,7 +1191,7 @@ __global__ void __launch_bounds__(32) k_tau_solve_t(GridDev g, int N, SolveParam
             rhs = L + (sp.lam * u0 + sp.B_C * Qn);
           }
           if (m00 && part == 0 && c != 1) {
-            rhs += nu * (c == 0 ? P.Ubaseyy[n] : P.Wbaseyy[n]);
+            rhs += nu * (c == 0 ? P.Ubaseyy[fb + n] : P.Wbaseyy[fb + n]);
             if (n == 0 && sp.constraint == 0) rhs -= (c == 0 ? sp.dPdxRef : sp.dPdzRef);
           }
           if (c == 1) outs[i] = rhs;

@@ -243,6 +243,19 @@ class Ensemble(DNS):
         L.check(self._lib.cfgpu_ensemble_get_field(self._h, int(slot), L.dptr(_as_field(u, self.grid, 3)),
                                                    L.dptr(_as_field(q, self.grid, 1))))
 
+    def set_params(self, slot: int, flags: DNSFlags, base=None):
+        """Field `slot` gets the nu, base flow and constraint of `flags` (dt and schemes stay shared)."""
+        fc = flags.to_c()
+        Ub = Wb = None
+        if base is not None:
+            Ub = np.ascontiguousarray(base[0], dtype=np.float64)
+            Wb = np.ascontiguousarray(base[1], dtype=np.float64)
+        L.check(self._lib.cfgpu_ensemble_set_params(self._h, int(slot), C.byref(fc), L.dptr(Ub), L.dptr(Wb)))
+
+    def load_slot(self, slot: int, dns: DNS):
+        """Move the time-stepping state of a started single-field DNS into field `slot`."""
+        L.check(self._lib.cfgpu_ensemble_load_slot(self._h, int(slot), dns._h))
+
     def CFL(self) -> np.ndarray:
         v = np.zeros(self.nfields)
         L.check(self._lib.cfgpu_ensemble_cfl(self._h, L.dptr(v)))

@@ -178,6 +178,54 @@ cfgpu_status cfgpu_ensemble_l2norm(cfgpu_dns dns, int field, double* l2);
 cfgpu_status cfgpu_ensemble_dPdx(cfgpu_dns dns, double* dPdx);
 
 /*
+ * Per-field parameters: field `slot` gets its own nu, base flow (from flags->baseflow and the walls,
+ * or Ubase/Wbase Chebyshev coefficients when both are non-null) and constraint (type, dPdx/dPdz or
+ * Ubulk/Wbulk), as NSE::createCFBaseFlow / initCFConstraint (channelflow/nse.cpp:589-671) compute
+ * them for a DNS with those flags; that field's tau tables are rebuilt for its nu.  dt, the schemes,
+ * the nonlinearity, dealiasing, taucorrection and Vsuck stay those of the ensemble (CFGPU_EINVAL
+ * otherwise).  Needs Ny <= 111.
+ */
+cfgpu_status cfgpu_ensemble_set_params(cfgpu_dns dns, int slot, const cfgpu_flags* flags, const double* Ubase,
+                                       const double* Wbase);
+
+/*
+ * Continuous batching: copy the complete time-stepping state of the single-field DNS `src` (velocity,
+ * pressure, multistep history or CNAB nonlinear terms, dPdx) into field `slot`.  src must have the
+ * ensemble's grid, precision, scheme, dt and nonlinearity, and both must be past their start-up
+ * steps (DNS::advance's init stepping, channelflow/dns.cpp:156-160): a request starts alone, then
+ * joins the batch, and its later steps are the steps it would have taken alone.  Set the slot's
+ * parameters (cfgpu_ensemble_set_params) to src's flags first.  An ensemble that has not run its own
+ * start-up steps runs main-scheme steps from the first load on (its fields are expected to arrive
+ * through this call).
+ */
+cfgpu_status cfgpu_ensemble_load_slot(cfgpu_dns dns, int slot, cfgpu_dns src);
+
+/*
+ * Request server (no reference counterpart; it serves the DNS integrations and f^T(u) evaluations
+ * that programs/simulateflow.cpp, cfDSI::f (channelflow/cfdsi.cpp:705-775) and the nsolver drivers
+ * run one at a time).  A request is nsteps fixed-dt steps of one field from the FlowField buffer u
+ * (f^T(u) with T = nsteps * flags->dt; cfgpu_timestep_adjust_for_T gives nsteps and dt for a horizon
+ * T).  Requests with the same grid, dt, schemes, nonlinearity, dealiasing, taucorrection and Vsuck
+ * share field ensembles of `slots` fields (per-field nu, base flow and constraint); new requests are
+ * admitted into free slots while others run (continuous batching), new ensembles only while their
+ * estimated device bytes fit in max_bytes.  cfgpu_server_pump admits, advances every ensemble by at
+ * most max_steps steps (ensembles overlap on their own streams) and collects finished requests;
+ * *active = requests queued or running.  cfgpu_server_poll: *status 0 queued, 1 running, 2 done,
+ * 3 failed (returns CFGPU_ENONFINITE); u receives the result when done; times = {submit, start, done}
+ * in seconds of a monotonic clock.  stats = {device bytes, ensembles, slots, running, queued,
+ * ensemble steps, field steps}.  Not thread-safe: one thread drives a server.
+ */
+typedef struct cfgpu_server_s* cfgpu_server;
+cfgpu_status cfgpu_server_create(long long max_bytes, int slots, int precision, cfgpu_server* out);
+cfgpu_status cfgpu_server_submit(cfgpu_server srv, const cfgpu_grid* grid, const cfgpu_flags* flags, int nsteps,
+                                 const double* u, long long* id);
+cfgpu_status cfgpu_server_pump(cfgpu_server srv, int max_steps, int* active);
+cfgpu_status cfgpu_server_poll(cfgpu_server srv, long long id, int* status, double* u, double* times);
+cfgpu_status cfgpu_server_release(cfgpu_server srv, long long id);
+cfgpu_status cfgpu_server_stats(cfgpu_server srv, long long* stats);
+cfgpu_status cfgpu_server_destroy(cfgpu_server srv);
+
+/*
  * TimeStep::adjust_for_T (channelflow/dnsflags.cpp:912-965): fits dT and dt to the horizon T; returns
  * n (steps per dT), N (dT intervals) and dt = dT/n, and updates ts->dt, ts->dT.
  */

@@ -100,3 +100,87 @@ def test_ensemble_slots_roundtrip_and_restart():
     d2 = DNS(u, to_cgrid(g), to_cflags(fl))
     d2.advance(u, q, 12)
     assert rel_l2(out, u, g) <= 1e-13
+
+
+def _mixed_params(g):
+    """Couette and Poiseuille fields at different Reynolds numbers in one box."""
+    out = []
+    for k, re in enumerate([400.0, 900.0, 1500.0, 2000.0]):
+        if k % 2 == 0:
+            out.append(dict(nu=1 / re, baseflow=O.LaminarBase, ulowerwall=-1.0, uupperwall=1.0))
+        else:
+            out.append(dict(nu=1 / re, baseflow=O.LaminarBase, ulowerwall=0.0, uupperwall=0.0,
+                            constraint=O.BulkVelocity, Ubulk=2 / 3))
+    return out
+
+
+@pytest.mark.parametrize("scheme", [O.SBDF3, O.CNAB2])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-13), ("mixed", 1e-12)])
+def test_heterogeneous_ensemble_equals_single_runs(scheme, precision, tol):
+    from channelflow_gb300 import DNS, Ensemble
+    g = O.Grid(16, 17, 16, *COUETTE_BOX)
+    common = dict(dt=0.02, timestepping=scheme, initstepping=O.SMRK2)
+    params = _mixed_params(g)
+    ens = Ensemble(to_cgrid(g), to_cflags(O.DNSFlags(**common, **params[0])), len(params), precision=precision)
+    us = []
+    for k, p in enumerate(params):
+        ens.set_params(k, to_cflags(O.DNSFlags(**common, **p)))
+        us.append(np.ascontiguousarray(O.random_divfree_field(g, seed=200 + k, norm=0.15,
+                                                              zero_mean_u=p.get("constraint") == O.BulkVelocity)))
+    U = np.ascontiguousarray(np.stack(us))
+    Q = np.zeros((len(params), 1) + us[0].shape[1:], complex)
+    ens.advance(U, Q, 10)
+    dps = ens.dPdx()
+    for k, p in enumerate(params):
+        fl = O.DNSFlags(**common, **p)
+        u, q = us[k].copy(), np.zeros((1,) + us[k].shape[1:], complex)
+        d = DNS(u, to_cgrid(g), to_cflags(fl), precision=precision)
+        d.advance(u, q, 10)
+        assert rel_l2(U[k], u, g) <= tol, (k, rel_l2(U[k], u, g))
+        assert abs(dps[k] - d.dPdx()) <= 1e-9 * max(abs(d.dPdx()), 1e-12)
+        d.close()
+
+
+@pytest.mark.parametrize("scheme", [O.SBDF3, O.CNAB2, O.CNRK2])
+def test_load_slot_continues_a_started_request(scheme):
+    """A request started alone (through its start-up steps) and moved into a running batch takes the
+    same steps it would have taken alone."""
+    from channelflow_gb300 import DNS, Ensemble
+    g = O.Grid(16, 17, 16, *COUETTE_BOX)
+    common = dict(dt=0.02, timestepping=scheme, initstepping=O.SMRK2)
+    params = _mixed_params(g)[:3]
+    ens = Ensemble(to_cgrid(g), to_cflags(O.DNSFlags(**common, **params[0])), 3)
+    us = [np.ascontiguousarray(O.random_divfree_field(g, seed=300 + k, norm=0.1,
+                                                      zero_mean_u=p.get("constraint") == O.BulkVelocity))
+          for k, p in enumerate(params)]
+    for k, p in enumerate(params):
+        ens.set_params(k, to_cflags(O.DNSFlags(**common, **p)))
+    U = np.ascontiguousarray(np.stack(us))
+    Q = np.zeros((3, 1) + us[0].shape[1:], complex)
+    ens.set_fields(U, Q)
+    ens.advance_resident(5)
+    # a new request with its own parameters: 3 steps alone, then into slot 1
+    newp = dict(nu=1 / 1200, baseflow=O.LaminarBase, ulowerwall=0.0, uupperwall=0.0,
+                constraint=O.BulkVelocity, Ubulk=2 / 3)
+    fl = O.DNSFlags(**common, **newp)
+    un = np.ascontiguousarray(O.random_divfree_field(g, seed=377, norm=0.12, zero_mean_u=True))
+    qn = np.zeros((1,) + un.shape[1:], complex)
+    alone = DNS(un.copy(), to_cgrid(g), to_cflags(fl))
+    alone.set_fields(un, qn)
+    alone.advance_resident(3)
+    ens.set_params(1, to_cflags(fl))
+    ens.load_slot(1, alone)
+    ens.advance_resident(6)
+    out, qo = np.zeros_like(un), np.zeros_like(qn)
+    ens.get_field(1, out, qo)
+    ref = DNS(un.copy(), to_cgrid(g), to_cflags(fl))
+    u, q = un.copy(), qn.copy()
+    ref.advance(u, q, 9)
+    assert rel_l2(out, u, g) <= 1e-13
+    # the other fields are untouched by the swap
+    ens.get_field(2, out, qo)
+    fl2 = O.DNSFlags(**common, **params[2])
+    u, q = us[2].copy(), np.zeros_like(qn)
+    d2 = DNS(u, to_cgrid(g), to_cflags(fl2))
+    d2.advance(u, q, 11)
+    assert rel_l2(out, u, g) <= 1e-13
