@@ -79,6 +79,7 @@ _SIGS = {
     "cfgpu_server_release": [C.c_void_p, C.c_longlong],
     "cfgpu_server_stats": [C.c_void_p, C.POINTER(C.c_longlong)],
     "cfgpu_server_destroy": [C.c_void_p],
+    "cfgpu_dns_set_graphs": [C.c_void_p, C.c_int],
     "cfgpu_ff_write": [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                        C.c_double, C.c_int, _PD],
     "cfgpu_ff_read_header": [C.c_char_p, _PI, _PD, _PI, C.c_char_p],

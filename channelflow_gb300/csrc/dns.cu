@@ -519,6 +519,15 @@ struct cfgpu_dns_s {
   // host staging (pinned)
   double* stage = nullptr;
   size_t stage_elems = 0;
+  // CUDA graphs of one main-scheme step, keyed by the step's buffer rotation state
+  bool use_graphs = true;
+  struct StepGraph {
+    int key;
+    cudaGraphExec_t exec;
+    long long launches;
+  };
+  std::vector<StepGraph> graphs;
+  bool graph_warm = false;  // one eager main step ran since the graphs were last dropped
   // phase profiling: event pairs recorded around NL passes (0) and tau solves (1)
   bool profiling = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -744,31 +753,98 @@ int ms_push(cfgpu_dns d) {
   return CFGPU_OK;
 }
 
-int ms_advance(cfgpu_dns d, int nsteps) {
+// One multistep step on the ring (rhs from u_j, N_j; solve into the oldest slot; rotate).
+int ms_step(cfgpu_dns d) {
   Scheme& s = d->main;
   const int K = s.order, J = K - 1;
   const double dt = d->fl.dt;
+  CKS(nonlinear(d, d->Uh[d->perm[0]], d->Nh[d->perm[0]]));
+  SolveParams sp = base_params(d);
+  sp.kind = 0;
+  sp.order = K;
+  SolvePtrs p = base_ptrs(d);
+  for (int j = 0; j < K; ++j) {
+    sp.a[j] = -s.alpha[j] / dt;
+    sp.b[j] = -s.beta[j];
+    p.uin[j] = d->Uh[d->perm[j]];
+    p.nin[j] = d->Nh[d->perm[j]];
+  }
+  p.uout = d->Uh[d->perm[J]];
+  p.qout = d->Qh[d->perm[J]];
+  CKS(tau_solve(d, sp, p, s.tau[0]));
+  ms_shift(d);
+  s.t += dt;
+  return CFGPU_OK;
+}
+
+int main_step(cfgpu_dns d);
+
+// Host-side state changes of one main step (replayed beside a graph launch).
+void main_step_host(cfgpu_dns d) {
+  Scheme& s = d->main;
+  if (s.family == 0) {
+    ms_shift(d);
+  } else if (s.family == 1) {
+    for (int j = 0; j < s.nsub; ++j) std::swap(d->fj[0], d->fj1[0]);
+  }
+  s.t += d->fl.dt;
+}
+
+// Rotation state that selects a step graph: ring phase (multistep) or fj/fj1 order (CNAB).
+int main_step_key(cfgpu_dns d) {
+  if (d->main.family == 0) return d->perm[0];
+  if (d->main.family == 1) return d->fj[0] < d->fj1[0] ? 0 : 1;
+  return 0;
+}
+
+void drop_graphs(cfgpu_dns d) {
+  for (auto& g : d->graphs) cudaGraphExecDestroy(g.exec);
+  d->graphs.clear();
+  d->graph_warm = false;
+}
+
+// One main-scheme step, replayed from a captured CUDA graph when one exists for this rotation state.
+// The first step of each state runs eagerly (first-use kernel attributes are set outside any
+// capture), the second is captured.
+int main_step_graph(cfgpu_dns d) {
+  const bool alternating = d->fl.nonlinearity == CFGPU_Alternating || d->fl.nonlinearity == CFGPU_Alternating_;
+  if (!d->use_graphs || d->profiling || alternating) return main_step(d);
+  const int key = main_step_key(d);
+  for (auto& g : d->graphs)
+    if (g.key == key) {
+      CK(cudaGraphLaunch(g.exec, d->st));
+      d->launches += g.launches;
+      main_step_host(d);
+      return CFGPU_OK;
+    }
+  if (!d->graph_warm) {
+    d->graph_warm = true;
+    return main_step(d);
+  }
+  const long long l0 = d->launches;
+  CK(cudaStreamBeginCapture(d->st, cudaStreamCaptureModeThreadLocal));
+  const int st = main_step(d);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(d->st, &graph);
+  if (st != CFGPU_OK) {
+    if (graph) cudaGraphDestroy(graph);
+    return st;
+  }
+  if (e != cudaSuccess) return fail(CFGPU_ECUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e));
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t e2 = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e2 != cudaSuccess) return fail(CFGPU_ECUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e2));
+  d->graphs.push_back({key, exec, d->launches - l0});
+  CK(cudaGraphLaunch(exec, d->st));  // the captured step has not run yet
+  return CFGPU_OK;
+}
+
+int ms_advance(cfgpu_dns d, int nsteps) {
   if (nsteps <= 0) return CFGPU_OK;
   CK(cudaMemcpyAsync(d->Uh[d->perm[0]], d->Ucur, 3 * state_bytes(d), cudaMemcpyDeviceToDevice, d->st));
   CK(cudaMemcpyAsync(d->Qh[d->perm[0]], d->Qcur, state_bytes(d), cudaMemcpyDeviceToDevice, d->st));
-  for (int step = 0; step < nsteps; ++step) {
-    CKS(nonlinear(d, d->Uh[d->perm[0]], d->Nh[d->perm[0]]));
-    SolveParams sp = base_params(d);
-    sp.kind = 0;
-    sp.order = K;
-    SolvePtrs p = base_ptrs(d);
-    for (int j = 0; j < K; ++j) {
-      sp.a[j] = -s.alpha[j] / dt;
-      sp.b[j] = -s.beta[j];
-      p.uin[j] = d->Uh[d->perm[j]];
-      p.nin[j] = d->Nh[d->perm[j]];
-    }
-    p.uout = d->Uh[d->perm[J]];
-    p.qout = d->Qh[d->perm[J]];
-    CKS(tau_solve(d, sp, p, s.tau[0]));
-    ms_shift(d);
-    s.t += dt;
-  }
+  for (int step = 0; step < nsteps; ++step) CKS(main_step_graph(d));
   CK(cudaMemcpyAsync(d->Ucur, d->Uh[d->perm[0]], 3 * state_bytes(d), cudaMemcpyDeviceToDevice, d->st));
   CK(cudaMemcpyAsync(d->Qcur, d->Qh[d->perm[0]], state_bytes(d), cudaMemcpyDeviceToDevice, d->st));
   return CFGPU_OK;
@@ -784,9 +860,9 @@ int cnab_push(cfgpu_dns d, int which) {
   return CFGPU_OK;
 }
 
-int cnab_advance(cfgpu_dns d, int which, int nsteps) {
+int cnab_step(cfgpu_dns d, int which) {
   Scheme& s = which == 0 ? d->main : d->init;
-  for (int n = 0; n < nsteps; ++n) {
+  {
     for (int j = 0; j < s.nsub; ++j) {
       std::swap(d->fj[which], d->fj1[which]);
       CKS(nonlinear(d, d->Ucur, d->fj[which], which));
@@ -811,9 +887,9 @@ int cnab_advance(cfgpu_dns d, int which, int nsteps) {
 }
 
 // ---- CNRK2 (dnsalgo.cpp:419-470) -------------------------------------------
-int rk_advance(cfgpu_dns d, int which, int nsteps) {
+int rk_step(cfgpu_dns d, int which) {
   Scheme& s = which == 0 ? d->main : d->init;
-  for (int n = 0; n < nsteps; ++n) {
+  {
     for (int j = 0; j < s.nsub; ++j) {
       CKS(nonlinear(d, d->Ucur, d->rkN, which));
       SolveParams sp = base_params(d);
@@ -835,11 +911,23 @@ int rk_advance(cfgpu_dns d, int which, int nsteps) {
   return CFGPU_OK;
 }
 
+int main_step(cfgpu_dns d) {
+  if (d->main.family == 0) return ms_step(d);
+  if (d->main.family == 1) return cnab_step(d, 0);
+  return rk_step(d, 0);
+}
+
 int scheme_advance(cfgpu_dns d, int which, int nsteps) {
   Scheme& s = which == 0 ? d->main : d->init;
-  if (s.family == 0) return ms_advance(d, nsteps);
-  if (s.family == 1) return cnab_advance(d, which, nsteps);
-  return rk_advance(d, which, nsteps);
+  if (which == 0 && s.family == 0) return ms_advance(d, nsteps);
+  for (int n = 0; n < nsteps; ++n) {
+    if (which == 0) {
+      CKS(main_step_graph(d));
+    } else {
+      CKS(s.family == 1 ? cnab_step(d, 1) : rk_step(d, 1));
+    }
+  }
+  return CFGPU_OK;
 }
 
 int scheme_push(cfgpu_dns d) {
@@ -1164,8 +1252,8 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
   if (!d->main.full && f.initstepping != f.timestepping) {
     CKS(setup_scheme(d->init, f.initstepping, f.dt));
     d->init.t = f.t0;
-    if (d->init.ninit != 0 && d->init.family == 0)
-      return fail(CFGPU_EINVAL, "init scheme needs initialization itself");
+    if (d->init.family == 0)
+      return fail(CFGPU_ENOTSUP, "multistep start-up schemes are not supported (use SMRK2, CNRK2 or CNAB2)");
     d->has_init = true;
   }
   auto alloc_scheme = [&](Scheme& s, int which) -> int {
@@ -1230,6 +1318,7 @@ void dns_free(cfgpu_dns d) {
     cudaEventDestroy(u.second.first);
     cudaEventDestroy(u.second.second);
   }
+  drop_graphs(d);
   if (d->st) cudaStreamDestroy(d->st);
   delete d;
 }
@@ -1428,6 +1517,7 @@ int ensure_hetero(cfgpu_dns d) {
   CKS(dalloc(&tmp, 4 * nb * N * d->rsz(), d->bytes));
   d->baseyS = tmp;
   d->sfl.assign(nb, d->fl);
+  drop_graphs(d);  // the solve and nonlinear kernels switch to per-field parameter arrays
   BaseFlow B;
   CKS(compute_base(d->fl, d->fl.baseflow == CFGPU_ArbitraryBase ? d->Ubase.data() : nullptr,
                    d->fl.baseflow == CFGPU_ArbitraryBase ? d->Wbase.data() : nullptr, d->N, d->g.a, d->g.b, B));
@@ -1635,6 +1725,7 @@ cfgpu_status cfgpu_dns_advance(cfgpu_dns d, double* u, double* q, int nsteps) {
 cfgpu_status cfgpu_dns_reset_dt(cfgpu_dns d, double dt) {
   if (!d || dt <= 0) return fail(CFGPU_EINVAL, "bad argument");
   d->fl.dt = dt;
+  drop_graphs(d);  // tables and step coefficients change
   // MultistepDNS/CNABstyleDNS/RungeKuttaDNS::reset_dt (dnsalgo.cpp:191-200, 404-413, 589-606)
   for (Scheme* s : {&d->main, &d->init}) {
     if (s == &d->init && !d->has_init) continue;
@@ -1724,6 +1815,13 @@ cfgpu_status cfgpu_dns_advance_timed(cfgpu_dns d, int nsteps, double* ms) {
 cfgpu_status cfgpu_dns_set_profiling(cfgpu_dns d, int enable) {
   if (!d) return fail(CFGPU_EINVAL, "null dns");
   d->profiling = enable != 0;
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_dns_set_graphs(cfgpu_dns d, int enable) {
+  if (!d) return fail(CFGPU_EINVAL, "null dns");
+  d->use_graphs = enable != 0;
+  if (!d->use_graphs) drop_graphs(d);
   return CFGPU_OK;
 }
 

@@ -132,6 +132,10 @@ class DNS:
         L.check(self._lib.cfgpu_dns_advance_timed(self._h, int(nsteps), C.byref(ms)))
         return ms.value
 
+    def set_graphs(self, enable: bool):
+        """Replay steady-state steps from captured CUDA graphs (default) or launch every kernel."""
+        L.check(self._lib.cfgpu_dns_set_graphs(self._h, int(bool(enable))))
+
     def set_profiling(self, enable: bool):
         L.check(self._lib.cfgpu_dns_set_profiling(self._h, int(bool(enable))))
 

@@ -150,6 +150,12 @@ cfgpu_status cfgpu_dns_destroy(cfgpu_dns dns);
  * since the last reset (and resets them).
  */
 cfgpu_status cfgpu_dns_advance_timed(cfgpu_dns dns, int nsteps, double* ms);
+/*
+ * Steady-state main-scheme steps are captured once per buffer-rotation state as CUDA graphs and replayed
+ * (one launch per step); enable = 0 launches every kernel eagerly.  Default on; graphs are not used while
+ * profiling is on or with the Alternating nonlinearity.
+ */
+cfgpu_status cfgpu_dns_set_graphs(cfgpu_dns dns, int enable);
 cfgpu_status cfgpu_dns_set_profiling(cfgpu_dns dns, int enable);
 cfgpu_status cfgpu_dns_phase_times(cfgpu_dns dns, double* nl_ms, long long* nl_count, double* tau_ms,
                                    long long* tau_count);
