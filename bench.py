@@ -247,8 +247,10 @@ def run_gpu(args, rank, world):
 
 def serve_requests(n, seed, horizon=(5.0, 50.0)):
     """Mixed-grid f^T(u) requests: Nx, Nz in {32, 48, 64, 96}, Ny in {33, 49, 65}, Re U[300, 2000],
-    Couette or Poiseuille (box Lx = 2pi/1.14, Lz = 2pi/2.5), T U[horizon] at dt = 0.02 (T a multiple of
-    dt), SBDF3 with SMRK2 start-up, seeded divergence-free fields of L2 norm U[0.05, 0.3]."""
+    Couette or Poiseuille (box Lx = 2pi/1.14, Lz = 2pi/2.5), T U[horizon], SBDF3 with SMRK2 start-up,
+    seeded divergence-free fields of L2 norm U[0.05, 0.3]; each evaluated as cfDSI's f(u, T) with the
+    reference's default CFL-adapted TimeStep started at dt = 0.02 (dT = 1, CFL in [0.4, 0.6],
+    dt in [0.001, 0.2])."""
     from channelflow_gb300 import DNSFlags, Grid
     from channelflow_gb300.fields import random_divfree_field
     rng = np.random.default_rng(seed)
@@ -259,7 +261,7 @@ def serve_requests(n, seed, horizon=(5.0, 50.0)):
         ny = int(rng.choice([33, 49, 65]))
         re = float(rng.uniform(300, 2000))
         couette = bool(rng.random() < 0.5)
-        steps = int(round(float(rng.uniform(*horizon)) / 0.02))
+        T = float(rng.uniform(*horizon))
         if couette:
             fl = DNSFlags(nu=1 / re, dt=0.02, baseflow=LaminarBase, ulowerwall=-1.0, uupperwall=1.0)
         else:
@@ -267,20 +269,24 @@ def serve_requests(n, seed, horizon=(5.0, 50.0)):
                           constraint=BulkVelocity, Ubulk=2 / 3)
         u = random_divfree_field(nx, ny, nz, lx, lz, seed=seed * 1000 + k, norm=float(rng.uniform(0.05, 0.3)),
                                  zero_mean_u=not couette)
-        out.append((Grid(nx, ny, nz, lx, lz), fl, steps, np.ascontiguousarray(u)))
+        out.append((Grid(nx, ny, nz, lx, lz), fl, T, np.ascontiguousarray(u)))
     return out
 
 
+def serve_timestep():
+    from channelflow_gb300.dsi import TimeStep
+    return TimeStep(dt=0.02, dtmin=0.001, dtmax=0.2, dT=1.0, CFLmin=0.4, CFLmax=0.6, variable=True)
+
+
 def run_alone(req, precision="fp64"):
-    """One request alone through the public single-field API (DNS::DNS + advance, as cfDSI::f runs it)."""
-    from channelflow_gb300 import DNS
-    g, fl, steps, u0 = req
-    u = u0.copy()
-    q = np.zeros((1,) + u.shape[1:], dtype=np.complex128)
-    d = DNS(u, g, fl, precision=precision)
-    d.advance(u, q, steps)
-    d.close()
-    return u
+    """One request alone: f^T(u) through cfgpu_ft (a DNS built per call, as cfDSI::f does)."""
+    from channelflow_gb300._lib import CfgpuError
+    from channelflow_gb300.dsi import ft
+    g, fl, T, u0 = req
+    try:
+        return ft(np.ascontiguousarray(u0), g, fl, serve_timestep(), T, precision=precision)[0]
+    except CfgpuError:  # non-finite result
+        return np.full_like(u0, np.nan)
 
 
 def run_serve(args):
@@ -289,16 +295,14 @@ def run_serve(args):
     from channelflow_gb300._lib import CfgpuError
     from channelflow_gb300.server import DONE, Server
     reqs = serve_requests(args.serve_requests, seed=7)
-    total_steps = sum(r[2] for r in reqs)
     # one at a time, plain FP64 (the reference's pattern: build a DNS per f^T(u) call)
-    run_alone(serve_requests(1, seed=99, horizon=(0.2, 0.2))[0])  # warm-up: library, context
+    run_alone(serve_requests(1, seed=99, horizon=(1.0, 1.0))[0])  # warm-up: library, context
     t0 = time.perf_counter()
     alone = [run_alone(r) for r in reqs]
     t_alone = time.perf_counter() - t0
-    out = {"requests": len(reqs), "field_steps": total_steps,
+    out = {"requests": len(reqs),
            "one_at_a_time_fp64": {"s": t_alone, "requests_per_s": len(reqs) / t_alone,
-                                  "non_finite": int(sum(not np.all(np.isfinite(a)) for a in alone)),
-                                  "field_steps_per_s": total_steps / t_alone}, "rates": []}
+                                  "non_finite": int(sum(not np.all(np.isfinite(a)) for a in alone))}, "rates": []}
     for rate in args.serve_rates:
         rng = np.random.default_rng(11)
         arrivals = np.cumsum(rng.exponential(1.0 / rate, size=len(reqs))) if rate > 0 else np.zeros(len(reqs))
@@ -309,8 +313,8 @@ def run_serve(args):
         while True:
             now = time.perf_counter() - start
             while nxt < len(reqs) and arrivals[nxt] <= now:
-                g, fl, steps, u = reqs[nxt]
-                ids[nxt] = srv.submit(g, fl, steps, u)
+                g, fl, T, u = reqs[nxt]
+                ids[nxt] = srv.submit_ft(g, fl, serve_timestep(), T, u)
                 nxt += 1
             active = srv.pump(args.serve_pump_steps)
             if nxt == len(reqs) and active == 0:
@@ -334,7 +338,7 @@ def run_serve(args):
         srv.close()
         out["rates"].append({
             "offered_per_s": rate, "makespan_s": makespan, "requests_per_s": len(reqs) / makespan,
-            "field_steps_per_s": total_steps / makespan, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+            "field_steps_per_s": stats["field_steps"] / makespan, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
             "p99_ms": 1e3 * float(np.percentile(lat, 99)),
             "vs_one_at_a_time_fp64": (len(reqs) / makespan) / (len(reqs) / t_alone),
             "max_rel_l2_vs_alone_fp64": float(max(errs)) if errs else None,
@@ -343,8 +347,8 @@ def run_serve(args):
             "ensemble_steps": stats["ensemble_steps"]})
     out.update(precision=args.serve_precision, slots=args.serve_slots, pump_steps=args.serve_pump_steps,
                workload="f^T(u) requests: Nx,Nz in {32,48,64,96}, Ny in {33,49,65}, Re U[300,2000], Couette or "
-                        "Poiseuille, T U[5,50] at dt=0.02, SBDF3 + SMRK2 start-up, seeded fields L2 U[0.05,0.3], "
-                        "Poisson arrivals")
+                        "Poiseuille, T U[5,50], CFL-adapted TimeStep from dt=0.02 (dT=1, CFL 0.4-0.6), SBDF3 + "
+                        "SMRK2 start-up, seeded fields L2 U[0.05,0.3], Poisson arrivals")
     return out
 
 

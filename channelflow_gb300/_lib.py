@@ -74,6 +74,8 @@ _SIGS = {
     "cfgpu_ensemble_load_slot": [C.c_void_p, C.c_int, C.c_void_p],
     "cfgpu_server_create": [C.c_longlong, C.c_int, C.c_int, C.POINTER(C.c_void_p)],
     "cfgpu_server_submit": [C.c_void_p, C.POINTER(Grid), C.POINTER(Flags), C.c_int, _PD, C.POINTER(C.c_longlong)],
+    "cfgpu_server_submit_ft": [C.c_void_p, C.POINTER(Grid), C.POINTER(Flags), C.POINTER(TimeStepC), C.c_double,
+                               _PD, C.POINTER(C.c_longlong)],
     "cfgpu_server_pump": [C.c_void_p, C.c_int, _PI],
     "cfgpu_server_poll": [C.c_void_p, C.c_longlong, _PI, _PD, _PD],
     "cfgpu_server_release": [C.c_void_p, C.c_longlong],

@@ -456,7 +456,24 @@ SlotParams slot_params(const cfgpu_flags& f, const BaseFlow& B) {
   p.wmean = B.WbulkRef - B.WbulkBase;
   p.baseShear[0] = B.baseShear[0];
   p.baseShear[1] = B.baseShear[1];
+  // scheme coefficients at this field's dt, computed as a single-field DNS computes them
+  Scheme m{}, i{};
+  if (setup_scheme(m, f.timestepping, f.dt) == CFGPU_OK) {
+    if (m.family == 0)
+      for (int j = 0; j < m.order; ++j) p.a[j] = -m.alpha[j] / f.dt;
+    else
+      for (int j = 0; j < m.nsub && j < 3; ++j) p.lam[0][j] = m.lambda_t[j];
+  }
+  if (f.initstepping != f.timestepping && setup_scheme(i, f.initstepping, f.dt) == CFGPU_OK && i.family != 0)
+    for (int j = 0; j < i.nsub && j < 3; ++j) p.lam[1][j] = i.lambda_t[j];
   return p;
+}
+
+// lambda_t of substep j of scheme `method` at dt (the tau tables of a field with that dt).
+double lambda_at(int method, double dt, int j) {
+  Scheme s{};
+  if (setup_scheme(s, method, dt) != CFGPU_OK || j >= (int)s.lambda_t.size()) return 0.0;
+  return s.lambda_t[j];
 }
 
 struct cfgpu_dns_s {
@@ -583,8 +600,10 @@ int build_tables(cfgpu_dns d, Scheme& s) {
     CKS(dalloc(&t.f, FN * TF_NFIELDS, d->bytes));
     CKS(dalloc(&t.s, (size_t)d->gm.Md * TS_NSCALARS, d->bytes));
     if (d->hetero) {
+      const int j = (int)s.tau.size();
       for (int f = 0; f < d->nb; ++f) {
-        CK(launch_tau_setup(d->gm, d->N, lt, d->sfl[f].nu, hb, t, d->scratch, d->st, f * d->g.Md, d->g.Md));
+        CK(launch_tau_setup(d->gm, d->N, lambda_at(s.method, d->sfl[f].dt, j), d->sfl[f].nu, hb, t, d->scratch,
+                            d->st, f * d->g.Md, d->g.Md));
         d->launches++;
       }
     } else {
@@ -602,8 +621,8 @@ int build_slot_tables(cfgpu_dns d, int f) {
   for (Scheme* s : {&d->main, &d->init}) {
     if (s == &d->init && !d->has_init) continue;
     for (size_t j = 0; j < s->tau.size(); ++j) {
-      CK(launch_tau_setup(d->gm, d->N, s->lambda_t[j], d->sfl[f].nu, hb, s->tau[j], d->scratch, d->st,
-                          f * d->g.Md, d->g.Md));
+      CK(launch_tau_setup(d->gm, d->N, lambda_at(s->method, d->sfl[f].dt, (int)j), d->sfl[f].nu, hb, s->tau[j],
+                          d->scratch, d->st, f * d->g.Md, d->g.Md));
       d->launches++;
     }
   }
@@ -868,6 +887,8 @@ int cnab_step(cfgpu_dns d, int which) {
       CKS(nonlinear(d, d->Ucur, d->fj[which], which));
       SolveParams sp = base_params(d);
       sp.kind = 1;
+      sp.scheme = which;
+      sp.substep = j;
       sp.lam = s.lambda_t[j];
       sp.a_b = s.ca[j] / s.cb[j];
       sp.g_b = s.cg[j] / s.cb[j];
@@ -894,6 +915,8 @@ int rk_step(cfgpu_dns d, int which) {
       CKS(nonlinear(d, d->Ucur, d->rkN, which));
       SolveParams sp = base_params(d);
       sp.kind = 2;
+      sp.scheme = which;
+      sp.substep = j;
       sp.lam = s.lambda_t[j];
       sp.rkA = s.rA[j];
       sp.B_C = s.rB[j] / s.rC[j];
@@ -1343,8 +1366,10 @@ int cfl_impl(cfgpu_dns d, double* cfl) {
   CK(cudaMemcpyAsync(key.data(), d->dred, d->nb * sizeof(unsigned long long), cudaMemcpyDeviceToHost, d->st));
   CK(cudaStreamSynchronize(d->st));
   const bool dxz = d->fl.dealiasing == CFGPU_DealiasXZ || d->fl.dealiasing == CFGPU_DealiasXYZ;
-  for (int f = 0; f < d->nb; ++f)
-    cfl[f] = cfl_key_to_double(key[f]) * (dxz ? 2.0 * M_PI / 3.0 * d->fl.dt : M_PI * d->fl.dt);
+  for (int f = 0; f < d->nb; ++f) {
+    const double dt = d->hetero ? d->sfl[f].dt : d->fl.dt;
+    cfl[f] = cfl_key_to_double(key[f]) * (dxz ? 2.0 * M_PI / 3.0 * dt : M_PI * dt);
+  }
   return CFGPU_OK;
 }
 
@@ -1361,72 +1386,7 @@ int l2norm_impl(cfgpu_dns d, int field, double* l2) {
 }
 }  // namespace
 
-// ---------------------------------------------------------------------------
-// TimeStep (channelflow/dnsflags.cpp:736-972): dt within [dtmin, dtmax] with
-// dT = n dt, CFL kept within [CFLmin, CFLmax] by adjust(); same arithmetic.
-// ---------------------------------------------------------------------------
-namespace {
-inline int iround_h(double x) { return int(x > 0.0 ? x + 0.5 : x - 0.5); }
-
-struct TimeStepH {
-  int n = 0, N = 0;
-  double dt = 0, dtmin = 0, dtmax = 0, dT = 0, T = 0, CFLmin = 0, CFL = 0, CFLmax = 0;
-  bool variable = false;
-  double value() const { return dT / n; }  // TimeStep::operator Real
-
-  int init(const cfgpu_timestep& t) {
-    dt = t.dt; dtmin = t.dtmin; dtmax = t.dtmax; dT = t.dT; CFLmin = t.CFLmin; CFLmax = t.CFLmax;
-    variable = t.variable != 0;
-    CFL = (CFLmax + CFLmin) / 2;
-    if (dtmin < 0 || dt < dtmin || dtmax < dt) return fail(CFGPU_EINVAL, "TimeStep: 0 <= dtmin <= dt <= dtmax");
-    if (CFLmin < 0 || CFLmax < CFLmin) return fail(CFGPU_EINVAL, "TimeStep: 0 <= CFLmin <= CFLmax");
-    if (dT < dtmin) return fail(CFGPU_EINVAL, "TimeStep: dT < dtmin");
-    n = std::max(iround_h(dT / dt), 1);
-    dt = dT / n;
-    while (dt < dtmin && n >= 2 && dT != 0) dt = dT / --n;
-    while (dt > dtmax && n <= INT_MAX && dT != 0) dt = dT / ++n;
-    return CFGPU_OK;
-  }
-  bool adjust(double c) {
-    CFL = c;
-    if (variable && (c <= CFLmin || c >= CFLmax)) return adjust_to_middle(c);
-    return false;
-  }
-  bool adjust_to_middle(double c) {
-    if (dtmin == dtmax || dT == 0.0) return false;
-    int nn = std::max(iround_h(2 * n * c / (CFLmax + CFLmin)), 1);
-    double d = dT / nn;
-    while (d < dtmin && d < dT) d = dT / --nn;
-    while (d > dtmax && nn <= INT_MAX) d = dT / ++nn;
-    c *= d / dt;
-    const bool adj = nn != n;
-    if (adj) {
-      n = nn;
-      dt = d;
-      CFL = c;
-    }
-    return adj;
-  }
-  bool adjust_for_T(double TT) {
-    T = TT;
-    if (TT == 0) {
-      const bool adj = dt != 0;
-      dt = 0; n = 0; dT = 0; T = 0;
-      return adj;
-    }
-    const int NN = std::max(iround_h(TT / dT), 1);
-    const double dTT = TT / NN;
-    int nn = std::max(iround_h(dTT / dt), 1);
-    double d = dTT / nn;
-    while (d < dtmin && nn > 2 && dTT != 0) d = dTT / --nn;
-    while (d > dtmax && nn <= INT_MAX && dTT != 0) d = dTT / ++nn;
-    const double c = d * CFL / dt;
-    const bool adj = d != dt;
-    n = nn; N = NN; dt = d; dT = dTT; CFL = c;
-    return adj;
-  }
-};
-}  // namespace
+#include "timestep.h"
 
 // ---------------------------------------------------------------------------
 // C ABI
@@ -1442,6 +1402,18 @@ int nfields(cfgpu_dns d) { return d->nb; }
 int startup_steps(cfgpu_dns d) {
   if (d->main.full) return 0;
   return d->main.family == 0 ? d->main.countdown : 1;
+}
+
+// Copy velocity and pressure of field `slot` of d into the one-field DNS dst (its only field).
+int store_slot(cfgpu_dns d, int slot, cfgpu_dns dst) {
+  if (dst->nb != 1 || d->g.Md != dst->g.Md || d->N != dst->N) return fail(CFGPU_EINVAL, "store_slot: shapes differ");
+  const size_t w = 2 * (size_t)d->g.Md, pitch = w * d->nb, N = d->N;
+  CK(cudaStreamSynchronize(dst->st));
+  CK(cudaMemcpy2DAsync(dst->Ucur, w * 8, d->Ucur + slot * w, pitch * 8, w * 8, 3 * N, cudaMemcpyDeviceToDevice,
+                       d->st));
+  CK(cudaMemcpy2DAsync(dst->Qcur, w * 8, d->Qcur + slot * w, pitch * 8, w * 8, N, cudaMemcpyDeviceToDevice, d->st));
+  CK(cudaStreamSynchronize(d->st));
+  return CFGPU_OK;
 }
 
 // Back to the state of a fresh DNS (time t0, start-up steps pending) without rebuilding tables.
@@ -1600,13 +1572,13 @@ cfgpu_status cfgpu_ensemble_set_params(cfgpu_dns d, int slot, const cfgpu_flags*
   if (!d || !f || slot < 0 || slot >= d->nb) return fail(CFGPU_EINVAL, "bad argument");
   if ((Ubase == nullptr) != (Wbase == nullptr)) return fail(CFGPU_EINVAL, "Ubase and Wbase must both be given");
   const cfgpu_flags& e = d->fl;
-  if (f->dt != e.dt || f->timestepping != e.timestepping || f->initstepping != e.initstepping ||
+  if (f->timestepping != e.timestepping || f->initstepping != e.initstepping ||
       f->nonlinearity != e.nonlinearity || f->dealiasing != e.dealiasing || f->taucorrection != e.taucorrection ||
       f->Vsuck != e.Vsuck)
     return fail(CFGPU_EINVAL,
-                "per-field flags may change nu, base flow, walls and constraint only (dt, schemes, nonlinearity, "
+                "per-field flags may change nu, dt, base flow, walls and constraint only (schemes, nonlinearity, "
                 "dealiasing, taucorrection and Vsuck are shared)");
-  if (f->nu <= 0) return fail(CFGPU_EINVAL, "nu must be positive");
+  if (f->nu <= 0 || f->dt <= 0) return fail(CFGPU_EINVAL, "nu and dt must be positive");
   if ((d->N + 1) / 2 > 56) return fail(CFGPU_ENOTSUP, "per-field parameters need Ny <= 111");
   CKS(ensure_hetero(d));
   BaseFlow B;
@@ -1624,7 +1596,8 @@ cfgpu_status cfgpu_ensemble_load_slot(cfgpu_dns d, int slot, cfgpu_dns src) {
   if (a.Nx != b.Nx || a.Ny != b.Ny || a.Nz != b.Nz || a.Md != b.Md || a.Lx != b.Lx || a.Lz != b.Lz ||
       a.a != b.a || a.b != b.b || d->precision != src->precision || d->device != src->device)
     return fail(CFGPU_EINVAL, "source DNS has another grid, precision or device");
-  if (d->fl.timestepping != src->fl.timestepping || d->fl.dt != src->fl.dt ||
+  const double dt_slot = d->hetero ? d->sfl[slot].dt : d->fl.dt, dt_src = src->hetero ? src->sfl[0].dt : src->fl.dt;
+  if (d->fl.timestepping != src->fl.timestepping || dt_slot != dt_src ||
       d->fl.nonlinearity != src->fl.nonlinearity || d->alt[0] != src->alt[0])
     return fail(CFGPU_EINVAL, "source DNS has another scheme, dt or nonlinearity state");
   if (!src->main.full) return fail(CFGPU_EINVAL, "the source DNS must be past its start-up steps");
@@ -1849,7 +1822,7 @@ cfgpu_status cfgpu_dns_phase_times(cfgpu_dns d, double* nl_ms, long long* nl_cou
 
 cfgpu_status cfgpu_timestep_adjust_for_T(cfgpu_timestep* ts, double T, int* n, int* N, double* dt) {
   if (!ts || T < 0) return fail(CFGPU_EINVAL, "bad argument");
-  TimeStepH h;
+  cfgpu_rt::TimeStepH h;
   CKS(h.init(*ts));
   h.adjust_for_T(T);
   ts->dt = h.dt;
@@ -1862,7 +1835,7 @@ cfgpu_status cfgpu_timestep_adjust_for_T(cfgpu_timestep* ts, double T, int* n, i
 
 cfgpu_status cfgpu_timestep_adjust(cfgpu_timestep* ts, double cfl, int* n, int* adjusted) {
   if (!ts) return fail(CFGPU_EINVAL, "bad argument");
-  TimeStepH h;
+  cfgpu_rt::TimeStepH h;
   CKS(h.init(*ts));
   const int adj = h.adjust(cfl) ? 1 : 0;
   ts->dt = h.dt;
@@ -1884,7 +1857,7 @@ cfgpu_status cfgpu_ft(const cfgpu_grid* grid, const cfgpu_flags* flags, const cf
     return CFGPU_OK;
   }
   if (T == 0) return CFGPU_OK;
-  TimeStepH dt;
+  cfgpu_rt::TimeStepH dt;
   CKS(dt.init(*timestep));
   dt.adjust_for_T(T);
   cfgpu_flags fl = *flags;

@@ -106,12 +106,16 @@ struct SolveParams {
   double baseShear[2];  // nu (U'(b) - U'(a)) / Ly and the same for W (bulk-velocity linear term)
   int taucorrection;
   int force_real00;  // NSE::solve keeps only the real part of the (0,0) mode
+  int scheme;        // 0 main scheme, 1 start-up scheme (selects per-field coefficients)
+  int substep;       // CNAB/RK substep j
 };
 
 // Per-field parameters of a heterogeneous field batch (one entry per field);
 // they replace the SolveParams fields of the same names for that field's modes.
 struct SlotParams {
   double nu, dPdxRef, dPdzRef, umean, wmean, baseShear[2];
+  double a[4];       // multistep rhs coefficients -alpha_j / dt of this field's dt
+  double lam[2][3];  // CNAB/RK lambda_t per substep of the main (0) and start-up (1) scheme at this dt
   int constraint;
   int pad;
 };

@@ -1,11 +1,16 @@
 // Request server: continuous batching of DNS integrations and f^T(u)
 // evaluations on one GPU.
 //
-// A request is (grid, flags, number of steps, initial velocity).  Requests
-// whose grid and shared flags (dt, schemes, nonlinearity, dealiasing,
-// taucorrection, Vsuck, precision) agree form one batch key; every key has
-// field ensembles of `slots` fields whose kernels cover all fields at once,
-// with per-field nu, base flow and constraint.  The scheduler (pump):
+// A request is (grid, flags, time step, initial velocity): either a fixed
+// number of steps at flags.dt, or f^T(u) with a TimeStep exactly as cfDSI's
+// f(u, T) runs it (channelflow/cfdsi.cpp:705-775): dt fitted to T, with a
+// variable TimeStep a one-step CFL probe and then, every dT, the CFL number
+// taken at the start of the interval adjusts dt after it (a dt change
+// restarts the start-up steps, as DNS::reset_dt does).  Requests whose grid
+// and shared flags (schemes, nonlinearity, dealiasing, taucorrection,
+// Vsuck, precision) agree form one batch key; every key has field ensembles
+// of `slots` fields whose kernels cover all fields at once, with per-field
+// nu, dt, base flow and constraint.  The scheduler (pump):
 //   1. admits queued requests into free slots, FIFO, skipping requests whose
 //      key has no free slot and whose new ensemble would not fit in the HBM
 //      budget; a request first runs its start-up steps (DNS::advance's init
@@ -30,6 +35,7 @@
 
 #include "../../include/cfgpu.h"
 #include "kernels.h"
+#include "timestep.h"
 
 namespace cfgpu_rt {
 int advance_async(cfgpu_dns d, int nsteps);
@@ -37,6 +43,7 @@ cudaStream_t stream(cfgpu_dns d);
 long long bytes(cfgpu_dns d);
 int startup_steps(cfgpu_dns d);
 int restart(cfgpu_dns d);
+int store_slot(cfgpu_dns d, int slot, cfgpu_dns dst);
 long long estimate_bytes(const cfgpu_grid& grid, const cfgpu_flags& f, int nb, int precision);
 }  // namespace cfgpu_rt
 
@@ -57,7 +64,7 @@ int sfail(int code, const std::string& m) { return cfgpu_record_error(code, m); 
 
 struct Key {
   int Nx, Ny, Nz;
-  double Lx, Lz, a, b, dt, Vsuck;
+  double Lx, Lz, a, b, Vsuck;
   int ts, is, nl, da, tc;
   bool operator<(const Key& o) const {
     return std::memcmp(this, &o, sizeof(Key)) < 0;
@@ -69,7 +76,7 @@ Key make_key(const cfgpu_grid& g, const cfgpu_flags& f) {
   std::memset(&k, 0, sizeof(k));
   k.Nx = g.Nx; k.Ny = g.Ny; k.Nz = g.Nz;
   k.Lx = g.Lx; k.Lz = g.Lz; k.a = g.a; k.b = g.b;
-  k.dt = f.dt; k.Vsuck = f.Vsuck;
+  k.Vsuck = f.Vsuck;
   k.ts = f.timestepping; k.is = f.initstepping; k.nl = f.nonlinearity; k.da = f.dealiasing; k.tc = f.taucorrection;
   return k;
 }
@@ -79,8 +86,14 @@ enum { ST_QUEUED = 0, ST_RUNNING = 1, ST_DONE = 2, ST_FAILED = 3 };
 struct Request {
   long long id = 0;
   cfgpu_grid grid{};
-  cfgpu_flags flags{};
+  cfgpu_flags flags{};  // flags.dt follows the request's TimeStep
   Key key{};
+  cfgpu_rt::TimeStepH ts;  // N intervals of n steps (fixed-step requests: N = 1, n = nsteps)
+  int interval = 0;        // current interval, 1..N
+  int left = 0;            // steps left in the current interval
+  double cfl_start = 0;    // CFL number at the start of the current interval
+  double cfl = 0;          // last CFL number taken
+  bool fixed = true;        // fixed-step request: flags.dt as given
   int nsteps = 0, done = 0;
   std::vector<double> u, q;  // FlowField buffers (velocity, pressure)
   int status = ST_QUEUED;
@@ -143,22 +156,69 @@ int finish(cfgpu_server_s* s, Request& r, cfgpu_dns h, int slot) {
   return CFGPU_OK;
 }
 
-// Start request r: its start-up steps in the staging DNS, then into a free slot of e.
+double slot_cfl(cfgpu_dns h, int slot, int nb) {
+  std::vector<double> c(nb);
+  if (cfgpu_ensemble_cfl(h, c.data()) != CFGPU_OK) return NAN;
+  return c[slot];
+}
+
+// Give the staging DNS the request's flags at its current dt and restart its start-up steps.
+int stage_restart(cfgpu_dns st, Request& r) {
+  if (!r.fixed) r.flags.dt = r.ts.value();
+  SCK(cfgpu_ensemble_set_params(st, 0, &r.flags, nullptr, nullptr));
+  return cfgpu_rt::restart(st);
+}
+
+int advance_sync(cfgpu_dns h, int n) {
+  SCK(cfgpu_rt::advance_async(h, n));
+  if (cudaStreamSynchronize(cfgpu_rt::stream(h)) != cudaSuccess) return sfail(CFGPU_ECUDA, "step failed");
+  return CFGPU_OK;
+}
+
+// Run the request in the staging DNS (its fields already there) from the start of interval r.interval
+// until it is past its start-up steps with steps left in the interval (returns with *done = false) or
+// finished (*done = true).  Interval ends inside the start-up phase are handled here as in cfDSI::f.
+int stage_run(cfgpu_server_s* s, Request& r, cfgpu_dns st, bool* finished) {
+  *finished = false;
+  for (;;) {
+    r.cfl_start = r.cfl = slot_cfl(st, 0, 1);
+    r.left = r.ts.n;
+    const int n0 = std::min(cfgpu_rt::startup_steps(st), r.left);
+    if (n0 > 0) {
+      SCK(advance_sync(st, n0));
+      r.left -= n0;
+      r.done += n0;
+    }
+    if (r.left > 0) return CFGPU_OK;
+    if (r.interval >= r.ts.N) {
+      *finished = true;
+      return CFGPU_OK;
+    }
+    if (r.ts.variable && r.ts.adjust(r.cfl_start)) SCK(stage_restart(st, r));
+    r.interval++;
+  }
+}
+
+// Start request r: dt fitted to T, the CFL probe (variable TimeStep), the start-up steps in the staging
+// DNS, then into the free slot `slot` of e.
 int start_request(cfgpu_server_s* s, Request& r, Ens* e, int slot) {
   cfgpu_dns st = nullptr;
   SCK(make_staging(s, r, &st));
-  SCK(cfgpu_ensemble_set_params(st, 0, &r.flags, nullptr, nullptr));
-  SCK(cfgpu_rt::restart(st));
+  SCK(stage_restart(st, r));
   SCK(cfgpu_ensemble_set_field(st, 0, r.u.data(), r.q.data()));
   r.t_start = now_s();
   r.status = ST_RUNNING;
-  const int n0 = std::min(cfgpu_rt::startup_steps(st), r.nsteps);
-  if (n0 > 0) {
-    SCK(cfgpu_rt::advance_async(st, n0));
-    if (cudaStreamSynchronize(cfgpu_rt::stream(st)) != cudaSuccess) return sfail(CFGPU_ECUDA, "staging step failed");
-    r.done = n0;
+  if (r.ts.variable) {
+    // cfDSI::f: one step to measure the CFL number, adjust, reset_dt, restart from u (q kept)
+    SCK(advance_sync(st, 1));
+    r.ts.adjust(slot_cfl(st, 0, 1));
+    SCK(stage_restart(st, r));
+    SCK(cfgpu_ensemble_set_field(st, 0, r.u.data(), nullptr));
   }
-  if (r.done >= r.nsteps) return finish(s, r, st, 0);
+  r.interval = 1;
+  bool finished = false;
+  SCK(stage_run(s, r, st, &finished));
+  if (finished) return finish(s, r, st, 0);
   SCK(cfgpu_ensemble_set_params(e->h, slot, &r.flags, nullptr, nullptr));
   SCK(cfgpu_ensemble_load_slot(e->h, slot, st));
   e->slot_req[slot] = r.id;
@@ -166,6 +226,38 @@ int start_request(cfgpu_server_s* s, Request& r, Ens* e, int slot) {
   for (size_t i = 0; i < s->ens.size(); ++i)
     if (s->ens[i].get() == e) r.ens = (int)i;
   r.slot = slot;
+  return CFGPU_OK;
+}
+
+// Interval end of the request in slot i of e (its steps of the interval are done).  Returns with the
+// slot freed (finished) or holding the request at the start of its next interval.
+int interval_end(cfgpu_server_s* s, Ens* e, int i, const std::vector<double>& cfl_now) {
+  Request& r = *s->reqs[e->slot_req[i]];
+  if (r.interval >= r.ts.N) {
+    SCK(finish(s, r, e->h, i));
+    e->slot_req[i] = -1;
+    return CFGPU_OK;
+  }
+  if (r.ts.variable && r.ts.adjust(r.cfl_start)) {
+    // dt changed: restart the start-up steps at the new dt through the staging DNS, then back into the slot
+    cfgpu_dns st = nullptr;
+    SCK(make_staging(s, r, &st));
+    SCK(stage_restart(st, r));
+    SCK(cfgpu_rt::store_slot(e->h, i, st));
+    r.interval++;
+    bool finished = false;
+    SCK(stage_run(s, r, st, &finished));
+    if (finished) {
+      SCK(finish(s, r, st, 0));
+      e->slot_req[i] = -1;
+      return CFGPU_OK;
+    }
+    SCK(cfgpu_ensemble_set_params(e->h, i, &r.flags, nullptr, nullptr));
+    return cfgpu_ensemble_load_slot(e->h, i, st);
+  }
+  r.interval++;
+  r.left = r.ts.n;
+  r.cfl_start = r.cfl = cfl_now[i];
   return CFGPU_OK;
 }
 
@@ -274,12 +366,19 @@ cfgpu_status cfgpu_server_submit(cfgpu_server s, const cfgpu_grid* grid, const c
                                  const double* u, long long* id) {
   if (!s || !grid || !flags || !u || !id || nsteps < 0) return sfail(CFGPU_EINVAL, "bad argument");
   if (flags->baseflow == CFGPU_ArbitraryBase) return sfail(CFGPU_ENOTSUP, "ArbitraryBase requests are not served");
+  if (flags->nonlinearity == CFGPU_Alternating || flags->nonlinearity == CFGPU_Alternating_)
+    return sfail(CFGPU_ENOTSUP, "Alternating nonlinearity requests are not served");
+  if (flags->dt <= 0) return sfail(CFGPU_EINVAL, "dt must be positive");
   auto r = std::make_unique<Request>();
   r->id = s->next_id++;
   r->grid = *grid;
   r->flags = *flags;
   r->key = make_key(*grid, *flags);
   r->nsteps = nsteps;
+  r->ts.n = nsteps;
+  r->ts.N = 1;
+  r->ts.dT = flags->dt * nsteps;
+  r->ts.dt = r->ts.dtmin = r->ts.dtmax = flags->dt;
   const size_t n1 = 2 * (size_t)grid->Ny * grid->Nx * (grid->Nz / 2 + 1);
   r->u.assign(u, u + 3 * n1);
   r->q.assign(n1, 0.0);
@@ -295,6 +394,21 @@ cfgpu_status cfgpu_server_submit(cfgpu_server s, const cfgpu_grid* grid, const c
   return CFGPU_OK;
 }
 
+cfgpu_status cfgpu_server_submit_ft(cfgpu_server s, const cfgpu_grid* grid, const cfgpu_flags* flags,
+                                    const cfgpu_timestep* timestep, double T, const double* u, long long* id) {
+  if (!s || !grid || !flags || !timestep || !u || !id) return sfail(CFGPU_EINVAL, "bad argument");
+  if (T <= 0) return sfail(CFGPU_EINVAL, "T must be positive (f^T(u) with T <= 0 needs no DNS)");
+  cfgpu_rt::TimeStepH ts;
+  SCK(ts.init(*timestep));
+  ts.adjust_for_T(T);
+  SCK(cfgpu_server_submit(s, grid, flags, ts.N * ts.n, u, id));
+  Request& r = *s->reqs[*id];
+  r.ts = ts;
+  r.fixed = false;
+  r.flags.dt = ts.value();
+  return CFGPU_OK;
+}
+
 cfgpu_status cfgpu_server_pump(cfgpu_server s, int max_steps, int* active) {
   if (!s || max_steps < 1) return sfail(CFGPU_EINVAL, "bad argument");
   SCK(admit(s));
@@ -303,10 +417,7 @@ cfgpu_status cfgpu_server_pump(cfgpu_server s, int max_steps, int* active) {
     if (!e) continue;
     int k = max_steps;
     for (long long id : e->slot_req)
-      if (id >= 0) {
-        const Request& r = *s->reqs[id];
-        k = std::min(k, r.nsteps - r.done);
-      }
+      if (id >= 0) k = std::min(k, s->reqs[id]->left);
     e->k = e->running() ? k : 0;
     if (e->k > 0) SCK(cfgpu_rt::advance_async(e->h, e->k));
   }
@@ -315,18 +426,22 @@ cfgpu_status cfgpu_server_pump(cfgpu_server s, int max_steps, int* active) {
     if (cudaStreamSynchronize(cfgpu_rt::stream(e->h)) != cudaSuccess)
       return sfail(CFGPU_ECUDA, "ensemble step failed");
     s->steps_done += e->k;
-    for (int i = 0; i < (int)e->slot_req.size(); ++i) {
-      const long long id = e->slot_req[i];
-      if (id < 0) continue;
-      Request& r = *s->reqs[id];
-      r.done += e->k;
-      s->field_steps += e->k;
-      if (r.done >= r.nsteps) {
-        SCK(finish(s, r, e->h, i));
-        e->slot_req[i] = -1;
+    bool boundary = false;
+    for (long long id : e->slot_req)
+      if (id >= 0) {
+        Request& r = *s->reqs[id];
+        r.done += e->k;
+        r.left -= e->k;
+        s->field_steps += e->k;
+        boundary |= r.left == 0;
       }
-    }
     e->k = 0;
+    if (!boundary) continue;
+    // CFL numbers at the interval boundary (the next interval's start), one pass over all fields
+    std::vector<double> cfl_now(e->slot_req.size(), 0.0);
+    if (cfgpu_ensemble_cfl(e->h, cfl_now.data()) != CFGPU_OK) return sfail(CFGPU_ECUDA, cfgpu_last_error());
+    for (int i = 0; i < (int)e->slot_req.size(); ++i)
+      if (e->slot_req[i] >= 0 && s->reqs[e->slot_req[i]]->left == 0) SCK(interval_end(s, e.get(), i, cfl_now));
   }
   if (active) {
     int n = (int)s->queue.size();

@@ -158,6 +158,11 @@ __device__ __forceinline__ void apply_slot(SolveParams& sp, const SlotParams& s)
   sp.wmean = s.wmean;
   sp.baseShear[0] = s.baseShear[0];
   sp.baseShear[1] = s.baseShear[1];
+  if (sp.kind == 0) {
+    for (int j = 0; j < 4; ++j) sp.a[j] = s.a[j];
+  } else {
+    sp.lam = s.lam[sp.scheme][sp.substep];
+  }
 }
 
 // One thread per mode: the TauSolver constructor for lambda = lambda_t + nu kappa^2,

@@ -37,6 +37,17 @@ class Server:
         self._shapes[rid.value] = u.shape
         return rid.value
 
+    def submit_ft(self, grid: Grid, flags: DNSFlags, timestep, T: float, u: np.ndarray) -> int:
+        """Queue f^T(u) with a TimeStep (channelflow_gb300.dsi.TimeStep), as cfDSI's f(u, T) evaluates it."""
+        u = np.ascontiguousarray(u)
+        _as_field(u, grid, 3)
+        rid = C.c_longlong()
+        gc, fc, tc = grid.to_c(), flags.to_c(), timestep.to_c()
+        L.check(self._lib.cfgpu_server_submit_ft(self._h, C.byref(gc), C.byref(fc), C.byref(tc), float(T),
+                                                 L.dptr(u), C.byref(rid)))
+        self._shapes[rid.value] = u.shape
+        return rid.value
+
     def pump(self, max_steps: int = 50) -> int:
         """One scheduling round; returns the number of queued or running requests."""
         active = C.c_int()

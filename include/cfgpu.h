@@ -184,12 +184,15 @@ cfgpu_status cfgpu_ensemble_l2norm(cfgpu_dns dns, int field, double* l2);
 cfgpu_status cfgpu_ensemble_dPdx(cfgpu_dns dns, double* dPdx);
 
 /*
- * Per-field parameters: field `slot` gets its own nu, base flow (from flags->baseflow and the walls,
- * or Ubase/Wbase Chebyshev coefficients when both are non-null) and constraint (type, dPdx/dPdz or
- * Ubulk/Wbulk), as NSE::createCFBaseFlow / initCFConstraint (channelflow/nse.cpp:589-671) compute
- * them for a DNS with those flags; that field's tau tables are rebuilt for its nu.  dt, the schemes,
- * the nonlinearity, dealiasing, taucorrection and Vsuck stay those of the ensemble (CFGPU_EINVAL
- * otherwise).  Needs Ny <= 111.
+ * Per-field parameters: field `slot` gets its own nu, dt, base flow (from flags->baseflow and the
+ * walls, or Ubase/Wbase Chebyshev coefficients when both are non-null) and constraint (type,
+ * dPdx/dPdz or Ubulk/Wbulk), as NSE::createCFBaseFlow / initCFConstraint (channelflow/nse.cpp:589-671)
+ * compute them for a DNS with those flags; that field's tau tables and scheme coefficients are
+ * recomputed for its nu and dt exactly as a single-field DNS computes them.  The schemes, the
+ * nonlinearity, dealiasing, taucorrection and Vsuck stay those of the ensemble (CFGPU_EINVAL
+ * otherwise); the ensemble's time (cfgpu_dns_time) advances by the ensemble's dt.  Changing a field's
+ * dt does not restart its start-up steps (restart it through a one-field DNS and
+ * cfgpu_ensemble_load_slot).  Needs Ny <= 111.
  */
 cfgpu_status cfgpu_ensemble_set_params(cfgpu_dns dns, int slot, const cfgpu_flags* flags, const double* Ubase,
                                        const double* Wbase);
@@ -210,9 +213,9 @@ cfgpu_status cfgpu_ensemble_load_slot(cfgpu_dns dns, int slot, cfgpu_dns src);
  * Request server (no reference counterpart; it serves the DNS integrations and f^T(u) evaluations
  * that programs/simulateflow.cpp, cfDSI::f (channelflow/cfdsi.cpp:705-775) and the nsolver drivers
  * run one at a time).  A request is nsteps fixed-dt steps of one field from the FlowField buffer u
- * (f^T(u) with T = nsteps * flags->dt; cfgpu_timestep_adjust_for_T gives nsteps and dt for a horizon
- * T).  Requests with the same grid, dt, schemes, nonlinearity, dealiasing, taucorrection and Vsuck
- * share field ensembles of `slots` fields (per-field nu, base flow and constraint); new requests are
+ * (cfgpu_server_submit), or f^T(u) with a TimeStep (cfgpu_server_submit_ft).  Requests with the same
+ * grid, schemes, nonlinearity, dealiasing, taucorrection and Vsuck share field ensembles of `slots`
+ * fields (per-field nu, dt, base flow and constraint); new requests are
  * admitted into free slots while others run (continuous batching), new ensembles only while their
  * estimated device bytes fit in max_bytes.  cfgpu_server_pump admits, advances every ensemble by at
  * most max_steps steps (ensembles overlap on their own streams) and collects finished requests;
@@ -225,6 +228,10 @@ typedef struct cfgpu_server_s* cfgpu_server;
 cfgpu_status cfgpu_server_create(long long max_bytes, int slots, int precision, cfgpu_server* out);
 cfgpu_status cfgpu_server_submit(cfgpu_server srv, const cfgpu_grid* grid, const cfgpu_flags* flags, int nsteps,
                                  const double* u, long long* id);
+/* f^T(u) request: the result equals cfgpu_ft(grid, flags, timestep, T, u, ...) run alone (CFL probe and
+ * dT-interval dt adjustments included when timestep->variable). T > 0. */
+cfgpu_status cfgpu_server_submit_ft(cfgpu_server srv, const cfgpu_grid* grid, const cfgpu_flags* flags,
+                                    const cfgpu_timestep* timestep, double T, const double* u, long long* id);
 cfgpu_status cfgpu_server_pump(cfgpu_server srv, int max_steps, int* active);
 cfgpu_status cfgpu_server_poll(cfgpu_server srv, long long id, int* status, double* u, double* times);
 cfgpu_status cfgpu_server_release(cfgpu_server srv, long long id);

@@ -184,3 +184,31 @@ def test_load_slot_continues_a_started_request(scheme):
     d2 = DNS(u, to_cgrid(g), to_cflags(fl2))
     d2.advance(u, q, 11)
     assert rel_l2(out, u, g) <= 1e-13
+
+
+@pytest.mark.parametrize("scheme", [O.SBDF3, O.CNAB2, O.CNRK2])
+def test_per_field_dt_equals_single_runs(scheme):
+    """Fields with their own dt (and nu) in one ensemble: each equals its single-field DNS bit for bit
+    up to round-off (scheme coefficients and tables are computed as the single DNS computes them)."""
+    from channelflow_gb300 import DNS, Ensemble
+    g = O.Grid(16, 17, 16, *COUETTE_BOX)
+    params = _mixed_params(g)
+    dts = [0.02, 0.013, 0.0075, 0.016]
+    ens = Ensemble(to_cgrid(g), to_cflags(O.DNSFlags(dt=0.02, timestepping=scheme, **params[0])), 4)
+    us = []
+    for k, p in enumerate(params):
+        ens.set_params(k, to_cflags(O.DNSFlags(dt=dts[k], timestepping=scheme, **p)))
+        us.append(np.ascontiguousarray(O.random_divfree_field(g, seed=500 + k, norm=0.15,
+                                                              zero_mean_u=p.get("constraint") == O.BulkVelocity)))
+    U = np.ascontiguousarray(np.stack(us))
+    Q = np.zeros((4, 1) + us[0].shape[1:], complex)
+    ens.advance(U, Q, 9)
+    cfl = ens.CFL()
+    for k, p in enumerate(params):
+        fl = O.DNSFlags(dt=dts[k], timestepping=scheme, **p)
+        u, q = us[k].copy(), np.zeros((1,) + us[k].shape[1:], complex)
+        d = DNS(u, to_cgrid(g), to_cflags(fl))
+        d.advance(u, q, 9)
+        assert rel_l2(U[k], u, g) <= 1e-13, (k, rel_l2(U[k], u, g))
+        assert abs(cfl[k] - d.CFL()) <= 1e-12 * d.CFL()
+        d.close()

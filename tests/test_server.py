@@ -88,3 +88,28 @@ def test_server_argument_errors():
         srv.poll(rid + 100)
     srv.release(rid)
     srv.close()
+
+
+@pytest.mark.gpu
+def test_served_ft_equals_ft_alone():
+    """f^T(u) requests with variable TimeSteps (CFL probe, dt changes every dT) served in shared
+    ensembles equal cfDSI-style f^T(u) evaluated alone (cfgpu_ft)."""
+    from channelflow_gb300.dsi import TimeStep, ft
+    from channelflow_gb300.server import DONE, Server
+    rng = np.random.default_rng(17)
+    reqs = _requests(rng, 10)
+    srv = Server(slots=3)
+    cases = []
+    for k, (g, fl, n, u) in enumerate(reqs):
+        ts = TimeStep(dt=0.02, dtmin=0.001, dtmax=0.05, dT=0.1, CFLmin=0.15 + 0.05 * (k % 3), CFLmax=0.3,
+                      variable=k % 4 != 3)
+        T = 0.2 * (1 + k % 5)
+        cases.append((g, fl, ts, T, u, srv.submit_ft(to_cgrid(g), to_cflags(fl), ts, T, u)))
+    srv.run(3)
+    for g, fl, ts, T, u, rid in cases:
+        status, res, _ = srv.poll(rid)
+        assert status == DONE
+        ref, _ = ft(u, to_cgrid(g), to_cflags(fl), TimeStep(**{k: getattr(ts, k) for k in ts.__dataclass_fields__}),
+                    T)
+        assert rel_l2(res, ref, g) <= 1e-13, (rid, rel_l2(res, ref, g))
+    srv.close()
