@@ -352,6 +352,56 @@ def run_serve(args):
     return out
 
 
+def run_ensemble(args):
+    """64 plane Couette trajectories (Re 400, 48x49x48, box Lx = 2pi/1.14, Lz = 2pi/2.5, SBDF3 + SMRK2
+    start-up, dt = 0.02), each from its own seeded perturbation with L2 norm U[0.05, 0.3]: one ensemble
+    (every kernel launch covers all 64 fields, graph-replayed steps) against the same fields run one
+    after another as single-field FP64 DNS.  Timed on a sample of steps (the full T = 200 is 10,000)."""
+    from channelflow_gb300 import DNS, DNSFlags, Ensemble, Grid
+    from channelflow_gb300.fields import l2norm, random_divfree_field
+    nf, K = args.ensemble_fields, args.ensemble_steps
+    lx, lz = 2 * math.pi / 1.14, 2 * math.pi / 2.5
+    g = Grid(48, 49, 48, lx, lz)
+    fl = DNSFlags(nu=1 / 400, dt=0.02, baseflow=LaminarBase, ulowerwall=-1.0, uupperwall=1.0)
+    rng = np.random.default_rng(3)
+    us = [random_divfree_field(48, 49, 48, lx, lz, seed=4000 + k, norm=float(rng.uniform(0.05, 0.3)))
+          for k in range(nf)]
+    U = np.ascontiguousarray(np.stack(us))
+    Q = np.zeros((nf, 1) + us[0].shape[1:], dtype=np.complex128)
+    out = {"workload": "64 plane Couette 48x49x48 Re=400 SBDF3, dt=0.02, perturbation L2 U[0.05,0.3]",
+           "fields": nf, "sample_steps": K}
+    for prec in ("mixed", "fp64"):
+        e = Ensemble(g, fl, nf, precision=prec)
+        e.set_fields(U.copy(), Q.copy())
+        e.advance_resident(3)
+        ms = e.advance_timed(K)
+        out[prec] = {"ms_per_step": ms / K, "field_steps_per_s": nf * K / (ms / 1e3),
+                     "grid_point_steps_per_s": nf * K / (ms / 1e3) * 48 * 49 * 48}
+        if prec == "fp64":
+            Ue, Qe = np.zeros_like(U), np.zeros_like(Q)
+            e.get_fields(Ue, Qe)
+        e.close()
+    # serial single-field FP64 runs (the reference's pattern), timed on a subset of the fields
+    ns = min(nf, args.ensemble_serial_fields)
+    t_dev = 0.0
+    for k in range(ns):
+        d = DNS(us[k].copy(), g, fl, precision="fp64")
+        d.set_fields(us[k].copy(), Q[0].copy())
+        d.advance_resident(3)
+        t_dev += d.advance_timed(K)
+        if k == 0:
+            u0, q0 = us[k].copy(), Q[0].copy()
+            d.get_fields(u0, q0)
+            out["rel_l2_field0_ensemble_vs_single_fp64"] = l2norm(Ue[0] - u0, 48, 48) / l2norm(u0, 48, 48)
+        d.close()
+    per_field = t_dev / ns / K
+    out["serial_fp64"] = {"ms_per_field_step": per_field, "field_steps_per_s": 1e3 / per_field,
+                          "fields_timed": ns}
+    out["speedup_mixed_vs_serial_fp64"] = out["mixed"]["field_steps_per_s"] / out["serial_fp64"]["field_steps_per_s"]
+    out["speedup_fp64_vs_serial_fp64"] = out["fp64"]["field_steps_per_s"] / out["serial_fp64"]["field_steps_per_s"]
+    return out
+
+
 def cpu_sample(nsteps):
     """The oracle (reference algorithm restated in NumPy) on the same workload: nsteps CNAB2 steps."""
     from oracle import cf_oracle as O
@@ -384,6 +434,9 @@ def main():
     ap.add_argument("--serve-slots", type=int, default=4)
     ap.add_argument("--serve-pump-steps", type=int, default=25)
     ap.add_argument("--serve-precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--ensemble-fields", type=int, default=64, help="ensemble block fields (0: skip)")
+    ap.add_argument("--ensemble-steps", type=int, default=200)
+    ap.add_argument("--ensemble-serial-fields", type=int, default=8)
     args = ap.parse_args()
     if args.grid:
         global NX, NY, NZ
@@ -411,6 +464,7 @@ def main():
 
     res, acc, hbm, peak_kind = run_gpu(args, rank, world)
     serve = run_serve(args) if (args.serve_requests > 0 and rank == 0) else None
+    ens = run_ensemble(args) if (args.ensemble_fields > 0 and rank == 0) else None
     if rank != 0:
         return
     m = res["mixed"]
@@ -462,6 +516,7 @@ def main():
         "clocks": m["clocks"],
         "cpu_baseline": cpu,
         "serve": serve,
+        "ensemble": ens,
     }
     print(json.dumps(line))
 

@@ -1356,7 +1356,8 @@ int cfl_impl(cfgpu_dns d, double* cfl) {
   if ((d->N + 1) / 2 > 56) return fail(CFGPU_ENOTSUP, "CFL needs Ny <= 111");
   R* W = (R*)d->W6;
   CK(launch_grad_cheb<R>(g, d->N, false, d->Ucur, W, (const R*)d->cinvA, (const R*)d->cinvB, (const R*)d->cderA,
-                         (const R*)d->cderB, (const R*)d->basey, 0.0, d->st));
+                         (const R*)d->cderB, (const R*)(d->hetero ? d->baseyS : d->basey), 0.0, d->st,
+                         d->hetero ? 4 * d->N : 0));
   CK(launch_xinv<R>(d->gp, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)W, (cpx<R>*)d->X6, 3, d->st));
   CK(cudaMemsetAsync(d->dred, 0, d->nb * sizeof(unsigned long long), d->st));
   CK(launch_zcfl<R>(d->gp, d->pz, (const cpx<R>*)d->twz, d->RP, (const cpx<R>*)d->X6, d->dyc, g.Lx / g.Nx,

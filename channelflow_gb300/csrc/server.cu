@@ -21,9 +21,11 @@
 //      streams before any is waited for, so their kernels overlap;
 //   3. reads out finished fields, frees their slots and, under memory
 //      pressure, drops ensembles without running fields.
-// Slots freed by a finished request keep computing on its last field until
-// the next request is loaded; fields never interact, so that work is wasted,
-// never wrong.  Each result equals the result of the request run alone.
+// A new ensemble gets as many fields as requests of its key are waiting (at
+// most `slots`).  Slots freed by a finished request keep computing on its last
+// field until the next request is loaded; fields never interact, so that work
+// is wasted, never wrong.  Each result equals the result of the request run
+// alone.
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -293,7 +295,13 @@ int admit(cfgpu_server_s* s) {
     int slot = -1;
     Ens* e = find_slot(s, r.key, &slot);
     if (!e) {
-      const long long est = cfgpu_rt::estimate_bytes(r.grid, r.flags, s->slots, s->precision) +
+      // Size the new ensemble to the requests of this key waiting now (at most `slots`): an unused slot
+      // would still be computed every step.
+      int want = 1;
+      for (long long q : s->queue)
+        if (std::memcmp(&s->reqs[q]->key, &r.key, sizeof(Key)) == 0) want++;
+      want = std::min(want, s->slots);
+      const long long est = cfgpu_rt::estimate_bytes(r.grid, r.flags, want, s->precision) +
                             (s->staging.count(r.key) ? 0 : cfgpu_rt::estimate_bytes(r.grid, r.flags, 1, s->precision));
       if (s->used + est > s->max_bytes && !dropped) {
         drop_idle(s);
@@ -305,7 +313,7 @@ int admit(cfgpu_server_s* s) {
       }
       auto ne = std::make_unique<Ens>();
       ne->key = r.key;
-      int st = cfgpu_ensemble_create(&r.grid, &r.flags, s->slots, s->precision, &ne->h);
+      int st = cfgpu_ensemble_create(&r.grid, &r.flags, want, s->precision, &ne->h);
       if (st != CFGPU_OK) {
         r.status = ST_FAILED;
         r.err = cfgpu_last_error();
@@ -313,7 +321,7 @@ int admit(cfgpu_server_s* s) {
       }
       ne->bytes = cfgpu_rt::bytes(ne->h);
       s->used += ne->bytes;
-      ne->slot_req.assign(s->slots, -1);
+      ne->slot_req.assign(want, -1);
       slot = 0;
       e = ne.get();
       bool placed = false;

@@ -214,8 +214,9 @@ cfgpu_status cfgpu_ensemble_load_slot(cfgpu_dns dns, int slot, cfgpu_dns src);
  * that programs/simulateflow.cpp, cfDSI::f (channelflow/cfdsi.cpp:705-775) and the nsolver drivers
  * run one at a time).  A request is nsteps fixed-dt steps of one field from the FlowField buffer u
  * (cfgpu_server_submit), or f^T(u) with a TimeStep (cfgpu_server_submit_ft).  Requests with the same
- * grid, schemes, nonlinearity, dealiasing, taucorrection and Vsuck share field ensembles of `slots`
- * fields (per-field nu, dt, base flow and constraint); new requests are
+ * grid, schemes, nonlinearity, dealiasing, taucorrection and Vsuck share field ensembles of up to
+ * `slots` fields (per-field nu, dt, base flow and constraint; a new ensemble is sized to the requests
+ * of its key waiting at that moment); new requests are
  * admitted into free slots while others run (continuous batching), new ensembles only while their
  * estimated device bytes fit in max_bytes.  cfgpu_server_pump admits, advances every ensemble by at
  * most max_steps steps (ensembles overlap on their own streams) and collects finished requests;
