@@ -27,11 +27,16 @@ class Flags(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("nu", "dPdx", "dPdz", "Ubulk", "Wbulk", "ulowerwall", "uupperwall",
                                           "wlowerwall", "wupperwall", "Vsuck", "t0", "dt")] + \
                [(n, C.c_int) for n in ("baseflow", "constraint", "timestepping", "initstepping", "nonlinearity",
-                                       "dealiasing", "taucorrection")]
+                                       "dealiasing", "taucorrection")] + [("rotation", C.c_double)]
 
 
 class TimeStepC(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("dt", "dtmin", "dtmax", "dT", "CFLmin", "CFLmax")] + [("variable", C.c_int)]
+
+
+class SymmetryC(C.Structure):
+    _fields_ = [("s", C.c_int), ("sx", C.c_int), ("sy", C.c_int), ("sz", C.c_int), ("ax", C.c_double),
+                ("az", C.c_double)]
 
 
 class CfgpuError(RuntimeError):
@@ -82,6 +87,9 @@ _SIGS = {
     "cfgpu_server_stats": [C.c_void_p, C.POINTER(C.c_longlong)],
     "cfgpu_server_destroy": [C.c_void_p],
     "cfgpu_dns_set_graphs": [C.c_void_p, C.c_int],
+    "cfgpu_dns_set_symmetries": [C.c_void_p, C.c_void_p, C.c_int, C.c_int],
+    "cfgpu_dns_symmetry": [C.c_void_p, C.POINTER(SymmetryC), C.c_int],
+    "cfgpu_field_symmetry": [C.POINTER(Grid), C.c_int, C.c_int, C.POINTER(SymmetryC), C.c_int, _PD],
     "cfgpu_ff_write": [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                        C.c_double, C.c_int, _PD],
     "cfgpu_ff_read_header": [C.c_char_p, _PI, _PD, _PI, C.c_char_p],

@@ -193,3 +193,59 @@ int measure_fp64(int device_sms, double* tflops, double* cycles_per_fma) {
   cudaFree(c);
   return cudaGetLastError() == cudaSuccess ? 0 : 1;
 }
+
+// ---------------------------------------------------------------------------
+// FieldSymmetry on spectral fields: FlowField::operator*=(FieldSymmetry) and
+// FlowField::project(FieldSymmetry) (channelflow/flowfield.cpp:1095-1272).
+// sigma (u,v,w)(x,y,z) = s (sx u, sy v, sz w)(sx x + ax Lx, sy y, sz z + az Lz).
+// In coefficients: the image at (kx, kz) is
+//   c(kx, kz, n) * X(u(sx sz kx, kz, n)),   X = conjugate when sz = -1,
+//   c = s * s_i * (-1)^n [sy = -1, n odd] * exp(2 pi i (ax sx kx + az sz kz)),
+// s_i = (sx, sy, sz) for the velocity components and 1 for scalars; project
+// replaces u by (u + sigma u)/2.  Fields are [c][n][field][m] (nb fields).
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void k_symmetry(GridDev g, int nb, int N, int ncomp, SymmetryDev sy, int project,
+                           const cpx<R>* __restrict__ in, cpx<R>* __restrict__ out) {
+  const size_t Mf = g.Md;
+  const size_t total = (size_t)ncomp * N * nb * Mf;
+  const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  const int m = (int)(t % Mf);
+  size_t r = t / Mf;
+  r /= nb;  // field index does not enter the map
+  const int n = (int)(r % N);
+  const int c = (int)(r / N);
+  const int kx = mode_kx(g, m), kz = mode_kz(g, m);
+  const int skx = sy.sx * sy.sz * kx;
+  const int ix = skx >= 0 ? skx : skx + g.NKx;
+  const size_t src = t - m + (size_t)ix * g.NKz + kz;  // same (c, n, field), source mode
+  const int si = ncomp == 3 ? (c == 0 ? sy.sx : (c == 1 ? sy.sy : sy.sz)) : 1;
+  const double sign = (double)(sy.s * si * ((sy.sy == -1 && (n & 1)) ? -1 : 1));
+  double sn, cs;
+  sincospi(2.0 * (sy.ax * sy.sx * kx + sy.az * sy.sz * kz), &sn, &cs);
+  cpx<R> v = in[src];
+  const double vx = (double)v.x, vy = sy.sz == -1 ? -(double)v.y : (double)v.y;
+  double wx = sign * (cs * vx - sn * vy), wy = sign * (cs * vy + sn * vx);
+  if (project) {
+    const cpx<R> a = in[t];
+    wx = 0.5 * ((double)a.x + wx);
+    wy = 0.5 * ((double)a.y + wy);
+  }
+  out[t] = cmk<R>((R)wx, (R)wy);
+}
+
+template <typename R>
+cudaError_t launch_symmetry(const GridDev& g, int nb, int N, int ncomp, const SymmetryDev& sy, int project,
+                            const void* in, void* out, cudaStream_t st) {
+  const size_t total = (size_t)ncomp * N * nb * g.Md;
+  const int T = 256;
+  k_symmetry<R><<<(unsigned)((total + T - 1) / T), T, 0, st>>>(g, nb, N, ncomp, sy, project,
+                                                              (const cpx<R>*)in, (cpx<R>*)out);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_symmetry<float>(const GridDev&, int, int, int, const SymmetryDev&, int, const void*, void*,
+                                            cudaStream_t);
+template cudaError_t launch_symmetry<double>(const GridDev&, int, int, int, const SymmetryDev&, int, const void*,
+                                             void*, cudaStream_t);

@@ -513,6 +513,7 @@ struct cfgpu_dns_s {
   void *cinvA = nullptr, *cinvB = nullptr, *cfwdA = nullptr, *cfwdB = nullptr;
   void *cderA = nullptr, *cderB = nullptr, *basey = nullptr;  // fused curl: (2/L) T'_n(y_j); U, U', W, W' at y_j
   void *cdfA = nullptr, *cdfB = nullptr;                       // (2/L) diff o chebyfft, parity split
+  void* zbasey = nullptr;  // zero base profiles [nb][4N] (LinearAboutProfile: u, v, w without base flow)
   double* dyc = nullptr;           // CFL grid spacing in y per Gauss-Lobatto point
   unsigned long long* dred = nullptr;  // reduction scratch (CFL key, L2 sum)
   int alt[2] = {0, 0};  // Alternating state of the main (0) and init (1) NSE: 0 = next is divergence
@@ -536,6 +537,9 @@ struct cfgpu_dns_s {
   // host staging (pinned)
   double* stage = nullptr;
   size_t stage_elems = 0;
+  // DNSFlags::symmetries / symmetryprojectioninterval (velocity; the pressure's symmetry is the identity)
+  std::vector<SymmetryDev> syms;
+  int sym_interval = 100;
   // CUDA graphs of one main-scheme step, keyed by the step's buffer rotation state
   bool use_graphs = true;
   struct StepGraph {
@@ -641,6 +645,19 @@ int nonlinear_impl(cfgpu_dns d, const double* U, void* Nout, int form) {
   R* W = (R*)d->W6;
   const size_t row = d->rowc(), comp = d->compc();
   int nin = 6, nout = 3;
+  const void* by = d->hetero ? d->baseyS : d->basey;
+  const int bstride = d->hetero ? 4 * N : 0;
+  if (form == CFGPU_LinearAboutProfile) {
+    // linearizedNL: u, v, w at the points (no base flow), (U d/dx + W d/dz) u + v (U', 0, W'), forward y
+    if ((N + 1) / 2 > 56) return fail(CFGPU_ENOTSUP, "Ny > 111 with LinearAboutProfile");
+    CK(launch_grad_cheb<R>(g, N, false, U, W, (const R*)d->cinvA, (const R*)d->cinvB, (const R*)d->cderA,
+                           (const R*)d->cderB, (const R*)d->zbasey, 0.0, d->st, bstride));
+    CK(launch_linprof<R>(g, N, W, (const R*)by, bstride, (R*)d->F3, d->st));
+    CK((launch_cheb<R, R, R>(N, false, (int)row, 3, (const R*)d->F3, row, comp, (R*)Nout, row, comp,
+                             (const R*)d->cfwdA, (const R*)d->cfwdB, d->st)));
+    d->launches += 3;
+    return CFGPU_OK;
+  }
   if (form == NL_ROTATIONAL) {
     if ((N + 1) / 2 <= 56) {
       CK(launch_curl_cheb<R>(g, N, U, W, (const R*)d->cinvA, (const R*)d->cinvB, (const R*)d->cderA,
@@ -689,6 +706,14 @@ int nonlinear_impl(cfgpu_dns d, const double* U, void* Nout, int form) {
   return CFGPU_OK;
 }
 
+template <typename R>
+int rotation_term(cfgpu_dns d, const double* U, void* Nout) {
+  const double* Ub = d->hetero ? d->dbaseS : d->dUbase;
+  CK(launch_rotation<R>(d->gm, d->N, U, Ub, d->hetero ? d->N : 0, d->fl.rotation, d->fl.Vsuck, (R*)Nout, d->st));
+  d->launches++;
+  return CFGPU_OK;
+}
+
 int nonlinear(cfgpu_dns d, const double* U, void* Nout, int which = 0) {
   PhaseScope ps(d, 0);
   int form = d->fl.nonlinearity;
@@ -697,8 +722,12 @@ int nonlinear(cfgpu_dns d, const double* U, void* Nout, int which = 0) {
     form = d->alt[which] == 0 ? NL_DIVERGENCE : NL_CONVECTION;
     d->alt[which] ^= 1;
   }
-  if (d->precision == CFGPU_FP64) return nonlinear_impl<double>(d, U, Nout, form);
-  return nonlinear_impl<float>(d, U, Nout, form);
+  const bool fp64 = d->precision == CFGPU_FP64;
+  CKS(fp64 ? nonlinear_impl<double>(d, U, Nout, form) : nonlinear_impl<float>(d, U, Nout, form));
+  // rotation about z (nse.cpp:62-78; not with LinearAboutProfile)
+  if (d->fl.rotation != 0.0 && form != CFGPU_LinearAboutProfile)
+    CKS(fp64 ? rotation_term<double>(d, U, Nout) : rotation_term<float>(d, U, Nout));
+  return CFGPU_OK;
 }
 
 SolveParams base_params(cfgpu_dns d) {
@@ -960,7 +989,39 @@ int scheme_push(cfgpu_dns d) {
 }
 
 // DNS::advance (dns.cpp:135-163)
+// sigma (or its projection) on ncomp components of the resident array a (element type size esz).
+int symmetry_on(cfgpu_dns d, void* a, size_t esz, int ncomp, const SymmetryDev& sy, int project) {
+  const size_t bytes = (size_t)ncomp * d->compc() * esz;
+  if (esz == 8) {
+    CK(launch_symmetry<double>(d->g, d->nb, d->N, ncomp, sy, project, a, d->scratch, d->st));
+  } else {
+    CK(launch_symmetry<float>(d->g, d->nb, d->N, ncomp, sy, project, a, d->scratch, d->st));
+  }
+  d->launches++;
+  CK(cudaMemcpyAsync(a, d->scratch, bytes, cudaMemcpyDeviceToDevice, d->st));
+  return CFGPU_OK;
+}
+
+// DNS::advance's projection (dns.cpp:151-155): the velocity and the main algorithm's stored fields
+// (MultistepDNS::project, dnsalgo.cpp:255-262: u_j and N_j; CNABstyleDNS::project, :628-632: f_j).
+int project_symmetries(cfgpu_dns d) {
+  const size_t rs = d->rsz();
+  for (const SymmetryDev& sy : d->syms) {
+    CKS(symmetry_on(d, d->Ucur, 8, 3, sy, 1));
+    if (d->main.family == 0) {
+      for (int j = 0; j < d->main.order; ++j) {
+        CKS(symmetry_on(d, d->Uh[j], 8, 3, sy, 1));
+        CKS(symmetry_on(d, d->Nh[j], rs, 3, sy, 1));
+      }
+    } else if (d->main.family == 1) {
+      CKS(symmetry_on(d, d->fj[0], rs, 3, sy, 1));
+    }
+  }
+  return CFGPU_OK;
+}
+
 int dns_advance_device(cfgpu_dns d, int nsteps) {
+  if (!d->syms.empty() && ((int)d->main.t) % d->sym_interval == 0) CKS(project_symmetries(d));
   int n = 0;
   while (!d->main.full && n < nsteps) {
     if (!d->has_init) return fail(CFGPU_EINVAL, "main algorithm uninitialized and no init algorithm");
@@ -1095,9 +1156,7 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
   if ((Ny + 1) / 2 > 72) return fail(CFGPU_ENOTSUP, "Ny > 143 not supported by the Chebyshev transform kernel");
   if (!(grid->b > grid->a) || grid->Lx <= 0 || grid->Lz <= 0) return fail(CFGPU_EINVAL, "bad box");
   if (f.dt <= 0 || f.nu <= 0) return fail(CFGPU_EINVAL, "dt and nu must be positive");
-  if (f.nonlinearity == CFGPU_LinearAboutProfile)
-    return fail(CFGPU_ENOTSUP, "LinearAboutProfile is not implemented on the device path");
-  if (f.nonlinearity < CFGPU_Rotational || f.nonlinearity > CFGPU_Alternating_)
+  if (f.nonlinearity < CFGPU_Rotational || f.nonlinearity > CFGPU_LinearAboutProfile)
     return fail(CFGPU_EINVAL, "unknown nonlinearity");
   if (f.dealiasing == CFGPU_DealiasY || f.dealiasing == CFGPU_DealiasXYZ)
     return fail(CFGPU_ENOTSUP, "DealiasY is not implemented on the device path");
@@ -1258,6 +1317,11 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
   CKS(dalloc(&tmp, nout * cd * rs, B));
   d->F3 = tmp;
   CKS(dalloc(&d->scratch, 8 * cd, B));
+  if (f.nonlinearity == CFGPU_LinearAboutProfile) {
+    CKS(dalloc(&tmp, 4 * (size_t)Ny * nb * rs, B));
+    d->zbasey = tmp;
+    CK(cudaMemset(d->zbasey, 0, 4 * (size_t)Ny * nb * rs));
+  }
   d->RP = fp64 ? 8 : 16;
   auto zbytes = [&](int form, int rp) {
     return fp64 ? zphys_smem_bytes<double>(g, form, rp) : zphys_smem_bytes<float>(g, form, rp);
@@ -1327,7 +1391,7 @@ void dns_free(cfgpu_dns d) {
   F(d->hb_lo); F(d->hb_di); F(d->hb_up);
   F(d->twx); F(d->twz); F(d->cinvA); F(d->cinvB); F(d->cfwdA); F(d->cfwdB);
   F(d->cderA); F(d->cderB); F(d->basey); F(d->cdfA); F(d->cdfB); F(d->dyc); F(d->dred); F(d->dmodes);
-  F(d->dslot); F(d->dbaseS); F(d->baseyS);
+  F(d->dslot); F(d->dbaseS); F(d->baseyS); F(d->zbasey);
   F(d->Ucur); F(d->Qcur);
   for (int j = 0; j < 4; ++j) { F(d->Uh[j]); F(d->Qh[j]); F(d->Nh[j]); }
   for (int w = 0; w < 2; ++w) { F(d->fj[w]); F(d->fj1[w]); F(d->rkQ[w]); }
@@ -1790,6 +1854,66 @@ cfgpu_status cfgpu_dns_set_profiling(cfgpu_dns d, int enable) {
   if (!d) return fail(CFGPU_EINVAL, "null dns");
   d->profiling = enable != 0;
   return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_dns_set_symmetries(cfgpu_dns d, const cfgpu_symmetry* syms, int n, int interval) {
+  if (!d || n < 0 || (n > 0 && !syms) || interval < 1) return fail(CFGPU_EINVAL, "bad argument");
+  d->syms.clear();
+  for (int i = 0; i < n; ++i) {
+    const cfgpu_symmetry& y = syms[i];
+    if (std::abs(y.s) != 1 || std::abs(y.sx) != 1 || std::abs(y.sy) != 1 || std::abs(y.sz) != 1)
+      return fail(CFGPU_EINVAL, "symmetry signs must be +1 or -1");
+    d->syms.push_back({y.s, y.sx, y.sy, y.sz, y.ax, y.az});
+  }
+  d->sym_interval = interval;
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_dns_symmetry(cfgpu_dns d, const cfgpu_symmetry* y, int project) {
+  if (!d || !y) return fail(CFGPU_EINVAL, "bad argument");
+  if (std::abs(y->s) != 1 || std::abs(y->sx) != 1 || std::abs(y->sy) != 1 || std::abs(y->sz) != 1)
+    return fail(CFGPU_EINVAL, "symmetry signs must be +1 or -1");
+  CKS(symmetry_on(d, d->Ucur, 8, 3, SymmetryDev{y->s, y->sx, y->sy, y->sz, y->ax, y->az}, project ? 1 : 0));
+  CK(cudaStreamSynchronize(d->st));
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_field_symmetry(const cfgpu_grid* grid, int dealias, int Nd, const cfgpu_symmetry* y, int project,
+                                  double* u) {
+  if (!grid || !y || !u || (Nd != 1 && Nd != 3) || grid->Nx < 4 || grid->Nz < 4 || grid->Ny < 2)
+    return fail(CFGPU_EINVAL, "bad argument");
+  if (std::abs(y->s) != 1 || std::abs(y->sx) != 1 || std::abs(y->sy) != 1 || std::abs(y->sz) != 1)
+    return fail(CFGPU_EINVAL, "symmetry signs must be +1 or -1");
+  cfgpu_dns_s tmp;  // a field's mode set and staging only; no DNS is built
+  GridDev& g = tmp.g;
+  g.Nx = grid->Nx; g.Ny = grid->Ny; g.Nz = grid->Nz;
+  g.Kx = dealias ? grid->Nx / 3 - 1 : grid->Nx / 2 - 1;
+  g.Kz = dealias ? grid->Nz / 3 - 1 : grid->Nz / 2 - 1;
+  g.NKx = 2 * g.Kx + 1;
+  g.NKz = g.Kz + 1;
+  g.Md = g.NKx * g.NKz;
+  g.kxmax = grid->Nx / 2;
+  g.kzmax = grid->Nz / 2;
+  tmp.N = grid->Ny;
+  const size_t n = (size_t)Nd * tmp.compc();
+  std::vector<double> h(n);
+  gather_modes(&tmp, u, Nd, h.data());
+  double *a = nullptr, *b = nullptr;
+  cudaError_t e = cudaMalloc(&a, 2 * n * sizeof(double));
+  if (e != cudaSuccess) return fail(CFGPU_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  b = a + n;
+  int st = CFGPU_OK;
+  do {
+    if ((e = cudaMemcpy(a, h.data(), n * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess) break;
+    if ((e = launch_symmetry<double>(g, 1, grid->Ny, Nd, SymmetryDev{y->s, y->sx, y->sy, y->sz, y->ax, y->az},
+                                     project ? 1 : 0, a, b, 0)) != cudaSuccess)
+      break;
+    if ((e = cudaMemcpy(h.data(), b, n * sizeof(double), cudaMemcpyDeviceToHost)) != cudaSuccess) break;
+  } while (false);
+  cudaFree(a);
+  if (e != cudaSuccess) st = fail(CFGPU_ECUDA, std::string("symmetry: ") + cudaGetErrorString(e));
+  if (st == CFGPU_OK) scatter_modes(&tmp, h.data(), Nd, u);
+  return st;
 }
 
 cfgpu_status cfgpu_dns_set_graphs(cfgpu_dns d, int enable) {

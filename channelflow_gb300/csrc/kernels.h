@@ -47,6 +47,14 @@ cudaError_t launch_cheb_fwd_div(const GridDev& g, int N, const R* pF, const R* p
                                 R wK, R wD, R* out, const R* FA, const R* FB, const R* DFA, const R* DFB,
                                 cudaStream_t st);
 
+// LinearAboutProfile term from u, v, w at the Gauss-Lobatto points (k_grad_cheb without base flow).
+template <typename R>
+cudaError_t launch_linprof(const GridDev& g, int N, const R* Y, const R* basey, int bstride, R* F, cudaStream_t st);
+// Rotation term added to the Chebyshev coefficients of N from the FP64 state U.
+template <typename R>
+cudaError_t launch_rotation(const GridDev& g, int N, const double* U, const double* Ub, int ustride, double rot,
+                            double Vsuck, R* F, cudaStream_t st);
+
 template <typename R>
 size_t xfft_smem_bytes(const GridDev& g);
 template <typename R>
@@ -140,6 +148,16 @@ struct SolvePtrs {
 template <typename R>
 cudaError_t launch_tau_solve(const GridDev& g, int N, const SolveParams& sp, const SolvePtrs& p, const HelmB& hb,
                              TauTable tt, cudaStream_t st);
+
+// FieldSymmetry (s, sx, sy, sz, ax, az) (channelflow/symmetry.h) on [c][n][field][m] spectral fields of the
+// per-field grid g (compact mode mapping); project = 1 gives (u + sigma u)/2.  out must not alias in.
+struct SymmetryDev {
+  int s, sx, sy, sz;
+  double ax, az;
+};
+template <typename R>
+cudaError_t launch_symmetry(const GridDev& g, int nb, int N, int ncomp, const SymmetryDev& sy, int project,
+                            const void* in, void* out, cudaStream_t st);
 
 // Diagnostics (diag.cu)
 template <typename R>

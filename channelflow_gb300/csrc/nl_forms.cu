@@ -478,7 +478,80 @@ cudaError_t launch_cheb_fwd_div(const GridDev& g, int N, const R* pF, const R* p
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// LinearAboutProfile: linearizedNL (channelflow/diffops.cpp:3288-3361),
+//   f = (U d/dx + W d/dz) u + v (U', 0, W'),
+// per mode at the Gauss-Lobatto points: Y holds u, v, w there ([c][j][2*Md], the
+// output of k_grad_cheb without base flow), basey the base profiles U, U', W, W'
+// at the points ([4][N] per field, field stride bstride).  Nyquist derivatives
+// are zero (no solved mode is a Nyquist mode).
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void k_linprof(GridDev g, int N, const R* __restrict__ Y, const R* __restrict__ basey, int bstride,
+                          R* __restrict__ F) {
+  const size_t row = 2 * (size_t)g.Md, comp = row * N;
+  const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (t >= (size_t)g.Md * N) return;
+  const int m = (int)(t % g.Md), j = (int)(t / g.Md);
+  const int kx = mode_kx(g, m), kz = mode_kz(g, m);
+  const R dx = (R)(2.0 * M_PI * kx / g.Lx), dz = (R)(2.0 * M_PI * kz / g.Lz);
+  const R* by = basey + (size_t)bstride * mode_field(g, m);
+  const R U = by[j], Uy = by[N + j], W = by[2 * N + j], Wy = by[3 * N + j];
+  const R d = U * dx + W * dz;  // (U d/dx + W d/dz) = i d
+  const size_t o = (size_t)j * row + 2 * (size_t)m;
+  const R ur = Y[o], ui = Y[o + 1], vr = Y[comp + o], vi = Y[comp + o + 1];
+  const R wr = Y[2 * comp + o], wi = Y[2 * comp + o + 1];
+  F[o] = -d * ui + Uy * vr;
+  F[o + 1] = d * ur + Uy * vi;
+  F[comp + o] = -d * vi;
+  F[comp + o + 1] = d * vr;
+  F[2 * comp + o] = -d * wi + Wy * vr;
+  F[2 * comp + o + 1] = d * wr + Wy * vi;
+}
+
+template <typename R>
+cudaError_t launch_linprof(const GridDev& g, int N, const R* Y, const R* basey, int bstride, R* F, cudaStream_t st) {
+  const size_t total = (size_t)g.Md * N;
+  k_linprof<R><<<(unsigned)((total + 255) / 256), 256, 0, st>>>(g, N, Y, basey, bstride, F);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Rotation about z (navierstokesNL, channelflow/nse.cpp:62-78): f -= rot e_z x (u + U):
+//   f_x -= rot (v - Vsuck on the (0,0) mode),  f_y += rot (u + U on the (0,0) mode),
+// linear in u, so added to the Chebyshev coefficients of N (the reference adds it at the
+// grid points and transforms back).  U: base coefficients [field][N] (stride ustride).
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void k_rotation(GridDev g, int N, const double* __restrict__ U, const double* __restrict__ Ub,
+                           int ustride, double rot, double Vsuck, R* __restrict__ F) {
+  const size_t row = 2 * (size_t)g.Md, comp = row * N;
+  const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (t >= row * N) return;
+  const int l = (int)(t % row), n = (int)(t / row);
+  const int m = l >> 1, part = l & 1;
+  const bool m00 = mode_kx(g, m) == 0 && mode_kz(g, m) == 0 && part == 0;
+  double u = U[t], v = U[comp + t];
+  if (m00) {
+    u += Ub[(size_t)ustride * mode_field(g, m) + n];
+    if (n == 0) v -= Vsuck;
+  }
+  F[t] = (R)((double)F[t] - rot * v);
+  F[comp + t] = (R)((double)F[comp + t] + rot * u);
+}
+
+template <typename R>
+cudaError_t launch_rotation(const GridDev& g, int N, const double* U, const double* Ub, int ustride, double rot,
+                            double Vsuck, R* F, cudaStream_t st) {
+  const size_t total = 2 * (size_t)g.Md * N;
+  k_rotation<R><<<(unsigned)((total + 255) / 256), 256, 0, st>>>(g, N, U, Ub, ustride, rot, Vsuck, F);
+  return cudaGetLastError();
+}
+
 #define INST_FORMS(R)                                                                                              \
+  template cudaError_t launch_linprof<R>(const GridDev&, int, const R*, const R*, int, R*, cudaStream_t);          \
+  template cudaError_t launch_rotation<R>(const GridDev&, int, const double*, const double*, int, double, double,   \
+                                          R*, cudaStream_t);                                                       \
   template size_t grad_cheb_smem_bytes<R>(int);                                                                    \
   template cudaError_t launch_grad_cheb<R>(const GridDev&, int, bool, const double*, R*, const R*, const R*,      \
                                            const R*, const R*, const R*, double, cudaStream_t, int);               \

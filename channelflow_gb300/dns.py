@@ -48,6 +48,7 @@ class DNSFlags:
     nonlinearity: int = Rotational
     dealiasing: int = DealiasXZ
     taucorrection: bool = True
+    rotation: float = 0.0
 
     def to_c(self) -> L.Flags:
         f = L.Flags()

@@ -68,6 +68,7 @@ typedef struct cfgpu_flags {
   double ulowerwall, uupperwall, wlowerwall, wupperwall;
   double Vsuck, t0, dt;
   int baseflow, constraint, timestepping, initstepping, nonlinearity, dealiasing, taucorrection;
+  double rotation; /* DNSFlags::rotation: dimensionless rotation about z (nse.cpp:62-78) */
 } cfgpu_flags;
 
 typedef struct cfgpu_dns_s* cfgpu_dns;
@@ -150,6 +151,27 @@ cfgpu_status cfgpu_dns_destroy(cfgpu_dns dns);
  * since the last reset (and resets them).
  */
 cfgpu_status cfgpu_dns_advance_timed(cfgpu_dns dns, int nsteps, double* ms);
+/*
+ * FieldSymmetry (channelflow/symmetry.h): sigma (u,v,w)(x,y,z) = s (sx u, sy v, sz w)(sx x + ax Lx, sy y,
+ * sz z + az Lz), signs +-1, ax and az shifts in units of Lx and Lz.
+ */
+typedef struct cfgpu_symmetry {
+  int s, sx, sy, sz;
+  double ax, az;
+} cfgpu_symmetry;
+
+/* DNSFlags::symmetries and symmetryprojectioninterval: DNS::advance projects the velocity and the scheme's
+ * stored fields onto the symmetric subspace when (int)time % interval == 0 (channelflow/dns.cpp:151-155,
+ * dnsalgo.cpp:255-262, 628-632).  n = 0 removes them. */
+cfgpu_status cfgpu_dns_set_symmetries(cfgpu_dns dns, const cfgpu_symmetry* syms, int n, int interval);
+/* u <- sigma u (project = 0, FlowField::operator*=) or (u + sigma u)/2 (project = 1, FlowField::project)
+ * for the resident velocity of every field (channelflow/flowfield.cpp:1095-1272). */
+cfgpu_status cfgpu_dns_symmetry(cfgpu_dns dns, const cfgpu_symmetry* sym, int project);
+/* The same on a host FlowField buffer (Nd = 1 or 3, spectral layout), over the modes |kx| <= Nx/3-1,
+ * kz <= Nz/3-1 (dealias != 0, a padded field) or all but the Nyquist modes; other modes are untouched. */
+cfgpu_status cfgpu_field_symmetry(const cfgpu_grid* grid, int dealias, int Nd, const cfgpu_symmetry* sym,
+                                  int project, double* u);
+
 /*
  * Steady-state main-scheme steps are captured once per buffer-rotation state as CUDA graphs and replayed
  * (one launch per step); enable = 0 launches every kernel eagerly.  Default on; graphs are not used while

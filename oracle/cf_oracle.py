@@ -539,6 +539,7 @@ class DNSFlags:
     nonlinearity: int = Rotational
     dealiasing: int = DealiasXZ
     taucorrection: bool = True
+    rotation: float = 0.0
 
     def dealias_xz(self) -> bool:
         return self.dealiasing in (DealiasXZ, DealiasXYZ)
@@ -770,6 +771,11 @@ class NSE:
         level; the returned u_after is that round-tripped field.
         """
         g, fl = self.g, self.flags
+        if fl.nonlinearity == LinearAboutProfile:
+            f = self._linearized(u)
+            if fl.dealias_xz():
+                f = zero_padded_modes(f, g)
+            return f, np.array(u, copy=True)
         u = np.array(u, copy=True)
         u[0, :, 0, 0] += self.Ubase
         u[2, :, 0, 0] += self.Wbase
@@ -791,12 +797,38 @@ class NSE:
             f, u = self._nl_grad_forms(u, nl)
         else:
             raise NotImplementedError("nonlinearity %d" % nl)
+        if fl.rotation != 0.0:
+            # -(Omega x u) with Omega = rotation e_z, on u + U (nse.cpp:62-78), linear in u
+            f = f.copy()
+            f[0] -= fl.rotation * u[1]
+            f[1] += fl.rotation * u[0]
         u[0, :, 0, 0] -= self.Ubase
         u[2, :, 0, 0] -= self.Wbase
         u[1, 0, 0, 0] += fl.Vsuck
         if fl.dealias_xz():
             f = zero_padded_modes(f, g)
         return f, u
+
+    def _linearized(self, u):
+        """linearizedNL (diffops.cpp:3288-3361): f = (U d/dx + W d/dz) u + v (U', 0, W'), per mode in
+        y-physical space (Nyquist derivatives zeroed)."""
+        g = self.g
+        L = g.b - g.a
+        U = ichebyfft(self.Ubase)
+        W = ichebyfft(self.Wbase)
+        Uy = ichebyfft(cdiff(self.Ubase, L))
+        Wy = ichebyfft(cdiff(self.Wbase, L))
+        uy = ichebyfft(u, axis=1)  # [i, ny, mx, mz] spectral in x,z, physical in y
+        kx = np.array([g.kx(m) for m in range(g.Nx)])
+        kz = np.arange(g.Mz)
+        ddx = 1j * 2 * PI * kx / g.Lx * (np.abs(kx) != g.Nx // 2)
+        ddz = 1j * 2 * PI * kz / g.Lz * (kz != g.Nz // 2)
+        D = U[:, None, None] * ddx[None, :, None] + W[:, None, None] * ddz[None, None, :]
+        f = np.zeros_like(uy)
+        f[0] = D * uy[0] + uy[1] * Uy[:, None, None]
+        f[1] = D * uy[1]
+        f[2] = D * uy[2] + uy[1] * Wy[:, None, None]
+        return chebyfft(f, axis=1)
 
     def _nl_grad_forms(self, u, nl):
         """u.grad u (dotgrad), div(uu) (divergence) and their average (skew-symmetric).
@@ -1117,7 +1149,26 @@ class DNS:
             self.init_nse = NSE(g, iflags, base, u)
             self.init = _new_algorithm(u, q, self.init_nse, iflags)
 
+    symmetries = ()
+    symmetry_interval = 100
+
+    def _project(self, u):
+        """DNS::advance's projection (dns.cpp:151-155, dnsalgo.cpp:255-262, 628-632)."""
+        dxz = self.flags.dealias_xz()
+        for sym in self.symmetries:
+            u = apply_symmetry(u, self.g, sym, True, dxz)
+            m = self.main
+            if isinstance(m, MultistepDNS):
+                for j in range(m.order):
+                    m.fields[j][0] = apply_symmetry(m.fields[j][0], self.g, sym, True, dxz)
+                    m.nonlf[j] = apply_symmetry(m.nonlf[j], self.g, sym, True, dxz)
+            elif isinstance(m, CNABstyleDNS):
+                m.fj = apply_symmetry(m.fj, self.g, sym, True, dxz)
+        return u
+
     def advance(self, u, q, nsteps):
+        if self.symmetries and int(self.main.t) % int(self.symmetry_interval) == 0:
+            u = self._project(u)
         n = 0
         while not self.main.full() and n < nsteps:
             u = self.main.push(u, q)
@@ -1486,3 +1537,33 @@ def ff_read(path):
         v = data[: Nd * Ny * Nx * (Nz // 2 + 1) * 2].reshape(Nd, Ny, Nx, Nz // 2 + 1, 2)
         u[:] = v[..., 0] + 1j * v[..., 1]
     return u, g, padded
+
+
+# ---------------------------------------------------------------------------
+# FieldSymmetry (symmetry.h) on spectral fields: FlowField::operator*= and
+# FlowField::project (flowfield.cpp:1095-1272).
+# ---------------------------------------------------------------------------
+
+def apply_symmetry(u, g: Grid, sym, project=False, dealias=True):
+    """sym = (s, sx, sy, sz, ax, az).  Acts on |kx| <= Kx, kz <= Kz (the 2/3 set when dealias, else all but
+    Nyquist), as the reference does for the stored half of the spectrum; other modes are left as they are."""
+    s, sx, sy, sz, ax, az = sym
+    Nd = u.shape[0]
+    Kx = g.Nx // 3 - 1 if dealias else g.Nx // 2 - 1
+    Kz = g.Nz // 3 - 1 if dealias else g.Nz // 2 - 1
+    out = u.copy()
+    n = np.arange(g.Ny)
+    syl = np.where((sy == -1) & (n % 2 == 1), -1.0, 1.0)
+    for i in range(Nd):
+        si = (sx, sy, sz)[i] if Nd == 3 else 1
+        for kx in range(-Kx, Kx + 1):
+            for kz in range(0, Kz + 1):
+                src = u[i, :, (sx * sz * kx) % g.Nx, kz]
+                if sz == -1:
+                    src = np.conj(src)
+                c = s * si * syl * np.exp(1j * (2 * PI * ax * sx * kx + 2 * PI * az * sz * kz))
+                img = c * src
+                if project:
+                    img = 0.5 * (u[i, :, kx % g.Nx, kz] + img)
+                out[i, :, kx % g.Nx, kz] = img
+    return out

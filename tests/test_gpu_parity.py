@@ -89,6 +89,21 @@ CASES = [
     ("suction_cnrk2_skew_nodealias", (8, 17, 8, *COUETTE_BOX),
      dict(nu=1 / 400, dt=0.02, timestepping=O.CNRK2, baseflow=O.SuctionBase, Vsuck=1 / 400,
           nonlinearity=O.SkewSymmetric, dealiasing=O.NoDealiasing), 6),
+    ("poiseuille_sbdf3_linearized_bulk", (12, 17, 12, *POISEUILLE_BOX),
+     dict(nu=1 / 2000, dt=0.01, timestepping=O.SBDF3, initstepping=O.SMRK2, baseflow=O.LaminarBase,
+          constraint=O.BulkVelocity, Ubulk=2.0 / 3.0, nonlinearity=O.LinearAboutProfile), 10),
+    ("couette_cnab2_linearized", (12, 17, 12, *COUETTE_BOX),
+     dict(nu=1 / 400, dt=0.02, timestepping=O.CNAB2, initstepping=O.SMRK2, baseflow=O.LaminarBase,
+          ulowerwall=-1.0, uupperwall=1.0, nonlinearity=O.LinearAboutProfile), 10),
+    ("couette_sbdf3_rotation", (12, 17, 12, *COUETTE_BOX),
+     dict(nu=1 / 400, dt=0.02, timestepping=O.SBDF3, initstepping=O.SMRK2, baseflow=O.LaminarBase,
+          ulowerwall=-1.0, uupperwall=1.0, rotation=0.3), 10),
+    ("poiseuille_cnrk2_rotation_skew_bulk", (12, 17, 12, *POISEUILLE_BOX),
+     dict(nu=1 / 2000, dt=0.01, timestepping=O.CNRK2, baseflow=O.LaminarBase, constraint=O.BulkVelocity,
+          Ubulk=2.0 / 3.0, rotation=-0.2, nonlinearity=O.SkewSymmetric), 8),
+    ("suction_sbdf2_rotation", (12, 17, 12, *COUETTE_BOX),
+     dict(nu=1 / 400, dt=0.02, timestepping=O.SBDF2, initstepping=O.SMRK2, baseflow=O.SuctionBase, Vsuck=1 / 400,
+          rotation=0.5), 8),
     ("poiseuille_48_cnab2", (48, 49, 48, *POISEUILLE_BOX),
      dict(nu=1 / 4000, dt=0.01, timestepping=O.CNAB2, initstepping=O.SMRK2, baseflow=O.LaminarBase,
           constraint=O.BulkVelocity, Ubulk=2.0 / 3.0), 5),

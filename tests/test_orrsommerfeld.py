@@ -45,11 +45,14 @@ ORACLE_ERR_SBDF3 = 1.0844443029260426e-07   # the oracle's sum for the SBDF3 / p
 NOUT, DT, T1 = 50, 0.02, 13.0
 
 
-def os_case(baseflow=True, timestepping=O.SBDF3, constraint=O.BulkVelocity):
+MAXERR_LINU = 1e-9   # dnsOrrsommTest.cpp:144-145: LinearAboutProfile follows the linear solution
+
+
+def os_case(baseflow=True, timestepping=O.SBDF3, constraint=O.BulkVelocity, nonlinearity=O.Rotational):
     d = np.load(GOLD)
     g = O.Grid(4, 65, 4, 2 * math.pi, math.pi, -1.0, 1.0)
     nu = 1.0 / 7500.0
-    fl = O.DNSFlags(nu=nu, dt=DT, baseflow=O.ZeroBase, dealiasing=O.NoDealiasing, nonlinearity=O.Rotational,
+    fl = O.DNSFlags(nu=nu, dt=DT, baseflow=O.ZeroBase, dealiasing=O.NoDealiasing, nonlinearity=nonlinearity,
                     constraint=constraint, timestepping=timestepping, initstepping=O.CNRK2,
                     ulowerwall=0.0, uupperwall=0.0, dPdx=-2.0 * nu, Ubulk=2.0 / 3.0)
     y = O.chebypoints(g.Ny, g.a, g.b)
@@ -124,18 +127,31 @@ def test_reference_up2q_offsets_mean_mode():
     assert 1e-7 < d[0, :, 1, 0].max() < 1e-3
 
 
+def test_oracle_orrsommerfeld_linearized():
+    """LinearAboutProfile about the parabola (the reference's --linU case): the DNS is the linear problem."""
+    g, fl, base, lin = os_case(nonlinearity=O.LinearAboutProfile)
+    err, _, _ = run_os(g, fl, base, lin, oracle_dns(g, fl, base))
+    assert err < MAXERR_LINU, err
+
+
 GPU_CASES = [(O.SBDF3, True, True), (O.SBDF3, False, True), (O.SBDF2, True, False), (O.SBDF4, True, False),
-             (O.CNAB2, True, False), (O.SMRK2, True, False), (O.CNRK2, True, False), (O.CNFE1, True, False)]
+             (O.CNAB2, True, False), (O.SMRK2, True, False), (O.CNRK2, True, False), (O.CNFE1, True, False),
+             ("linU", True, True)]
 
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("scheme,baseflow,vs_oracle", GPU_CASES,
                          ids=["sbdf3_parabola_base", "sbdf3_zero_base", "sbdf2", "sbdf4", "cnab2", "smrk2", "cnrk2",
-                              "cnfe1"])
+                              "cnfe1", "sbdf3_linearized"])
 def test_gpu_orrsommerfeld_growth(scheme, baseflow, vs_oracle):
     from channelflow_gb300 import DNS, build
     build.build()
-    g, fl, base, lin = os_case(baseflow=baseflow, timestepping=scheme)
+    if scheme == "linU":
+        g, fl, base, lin = os_case(baseflow=baseflow, nonlinearity=O.LinearAboutProfile)
+        maxerr = MAXERR_LINU
+    else:
+        g, fl, base, lin = os_case(baseflow=baseflow, timestepping=scheme)
+        maxerr = MAXERR[scheme]
     handles = []
 
     def make_gpu(u0, q0):
@@ -150,7 +166,7 @@ def test_gpu_orrsommerfeld_growth(scheme, baseflow, vs_oracle):
         return adv
 
     err, un, qn = run_os(g, fl, base, lin, make_gpu)
-    assert err < MAXERR[scheme], err
+    assert err < maxerr, err
     if not vs_oracle:
         return
     err_r, ur, qr = run_os(g, fl, base, lin, oracle_dns(g, fl, base))
