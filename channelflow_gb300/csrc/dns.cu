@@ -773,7 +773,7 @@ int tau_solve(cfgpu_dns d, const SolveParams& sp, const SolvePtrs& p, const TauT
   } else {
     CK(launch_tau_solve<float>(d->gm, d->N, sp, p, hb, tt, d->st));
   }
-  d->launches++;
+  d->launches += tau_solve_launches(d->N);
   return CFGPU_OK;
 }
 

@@ -145,6 +145,8 @@ struct SolvePtrs {
   int base_stride;         // 0: one base flow for all fields; N: Ubase/Wbase/Ubaseyy/Wbaseyy are [field][N]
 };
 
+// Kernel launches one launch_tau_solve makes for Ny = N (the right-hand-side kernel and the solve).
+int tau_solve_launches(int N);
 template <typename R>
 cudaError_t launch_tau_solve(const GridDev& g, int N, const SolveParams& sp, const SolvePtrs& p, const HelmB& hb,
                              TauTable tt, cudaStream_t st);

@@ -16,9 +16,11 @@
 //      budget; a request first runs its start-up steps (DNS::advance's init
 //      stepping, channelflow/dns.cpp:156-160) in a one-field staging DNS of
 //      its key and then moves into its slot with cfgpu_ensemble_load_slot;
-//   2. advances every ensemble with running fields by the largest step count
-//      that ends no request early, all ensembles enqueued on their own
-//      streams before any is waited for, so their kernels overlap;
+//   2. keeps every ensemble busy on its own stream: when its chunk in flight
+//      has completed (an event query, no wait), it processes interval ends and
+//      finished requests and enqueues the next chunk, the largest step count
+//      that ends no request's interval early (at most max_steps), so small
+//      and large ensembles run concurrently without lock-step rounds;
 //   3. reads out finished fields, frees their slots and, under memory
 //      pressure, drops ensembles without running fields.
 // A new ensemble gets as many fields as requests of its key are waiting (at
@@ -109,7 +111,8 @@ struct Ens {
   cfgpu_dns h = nullptr;
   std::vector<long long> slot_req;  // request id per slot, -1 free
   long long bytes = 0;
-  int k = 0;  // steps enqueued this round
+  int k = 0;                        // steps of the chunk in flight (0: idle)
+  cudaEvent_t done = nullptr;       // recorded after the chunk in flight
   int running() const {
     int n = 0;
     for (long long r : slot_req) n += r >= 0;
@@ -157,6 +160,8 @@ int finish(cfgpu_server_s* s, Request& r, cfgpu_dns h, int slot) {
   r.t_done = now_s();
   return CFGPU_OK;
 }
+
+int complete_chunk(cfgpu_server_s* s, Ens* e, bool wait, bool* completed);
 
 double slot_cfl(cfgpu_dns h, int slot, int nb) {
   std::vector<double> c(nb);
@@ -221,6 +226,12 @@ int start_request(cfgpu_server_s* s, Request& r, Ens* e, int slot) {
   bool finished = false;
   SCK(stage_run(s, r, st, &finished));
   if (finished) return finish(s, r, st, 0);
+  bool completed = false;
+  SCK(complete_chunk(s, e, true, &completed));  // the new field's steps start after the chunk in flight
+  if (e->slot_req[slot] >= 0) {
+    // the completed chunk's bookkeeping did not free this slot; find another one (cannot happen: slot was free)
+    return sfail(CFGPU_EINVAL, "slot taken");
+  }
   SCK(cfgpu_ensemble_set_params(e->h, slot, &r.flags, nullptr, nullptr));
   SCK(cfgpu_ensemble_load_slot(e->h, slot, st));
   e->slot_req[slot] = r.id;
@@ -263,6 +274,43 @@ int interval_end(cfgpu_server_s* s, Ens* e, int i, const std::vector<double>& cf
   return CFGPU_OK;
 }
 
+int interval_end(cfgpu_server_s* s, Ens* e, int i, const std::vector<double>& cfl_now);
+
+// The chunk in flight on e has completed (or is waited for when wait): count its steps, handle interval
+// ends (CFL numbers of the whole ensemble in one pass) and finished requests.
+int complete_chunk(cfgpu_server_s* s, Ens* e, bool wait, bool* completed) {
+  *completed = false;
+  if (e->k == 0) {
+    *completed = true;
+    return CFGPU_OK;
+  }
+  if (wait) {
+    if (cudaEventSynchronize(e->done) != cudaSuccess) return sfail(CFGPU_ECUDA, "ensemble step failed");
+  } else {
+    const cudaError_t q = cudaEventQuery(e->done);
+    if (q == cudaErrorNotReady) return CFGPU_OK;
+    if (q != cudaSuccess) return sfail(CFGPU_ECUDA, std::string("ensemble step failed: ") + cudaGetErrorString(q));
+  }
+  *completed = true;
+  s->steps_done += e->k;
+  bool boundary = false;
+  for (long long id : e->slot_req)
+    if (id >= 0) {
+      Request& r = *s->reqs[id];
+      r.done += e->k;
+      r.left -= e->k;
+      s->field_steps += e->k;
+      boundary |= r.left == 0;
+    }
+  e->k = 0;
+  if (!boundary) return CFGPU_OK;
+  std::vector<double> cfl_now(e->slot_req.size(), 0.0);
+  if (cfgpu_ensemble_cfl(e->h, cfl_now.data()) != CFGPU_OK) return sfail(CFGPU_ECUDA, cfgpu_last_error());
+  for (int i = 0; i < (int)e->slot_req.size(); ++i)
+    if (e->slot_req[i] >= 0 && s->reqs[e->slot_req[i]]->left == 0) SCK(interval_end(s, e, i, cfl_now));
+  return CFGPU_OK;
+}
+
 Ens* find_slot(cfgpu_server_s* s, const Key& k, int* slot) {
   for (auto& e : s->ens) {
     if (!e || std::memcmp(&e->key, &k, sizeof(Key)) != 0) continue;
@@ -279,8 +327,10 @@ Ens* find_slot(cfgpu_server_s* s, const Key& k, int* slot) {
 void drop_idle(cfgpu_server_s* s) {
   for (auto& e : s->ens)
     if (e && e->running() == 0) {
+      if (e->k) cudaEventSynchronize(e->done);
       s->used -= e->bytes;
       cfgpu_dns_destroy(e->h);
+      if (e->done) cudaEventDestroy(e->done);
       e.reset();
     }
 }
@@ -321,6 +371,13 @@ int admit(cfgpu_server_s* s) {
       }
       ne->bytes = cfgpu_rt::bytes(ne->h);
       s->used += ne->bytes;
+      if (cudaEventCreateWithFlags(&ne->done, cudaEventDisableTiming) != cudaSuccess) {
+        cfgpu_dns_destroy(ne->h);
+        s->used -= ne->bytes;
+        r.status = ST_FAILED;
+        r.err = "cudaEventCreate failed";
+        continue;
+      }
       ne->slot_req.assign(want, -1);
       slot = 0;
       e = ne.get();
@@ -420,36 +477,17 @@ cfgpu_status cfgpu_server_submit_ft(cfgpu_server s, const cfgpu_grid* grid, cons
 cfgpu_status cfgpu_server_pump(cfgpu_server s, int max_steps, int* active) {
   if (!s || max_steps < 1) return sfail(CFGPU_EINVAL, "bad argument");
   SCK(admit(s));
-  // advance: the largest step count that ends no running request early, capped by max_steps
   for (auto& e : s->ens) {
     if (!e) continue;
+    bool completed = false;
+    SCK(complete_chunk(s, e.get(), false, &completed));
+    if (!completed || !e->running()) continue;
     int k = max_steps;
     for (long long id : e->slot_req)
       if (id >= 0) k = std::min(k, s->reqs[id]->left);
-    e->k = e->running() ? k : 0;
-    if (e->k > 0) SCK(cfgpu_rt::advance_async(e->h, e->k));
-  }
-  for (auto& e : s->ens) {
-    if (!e || e->k == 0) continue;
-    if (cudaStreamSynchronize(cfgpu_rt::stream(e->h)) != cudaSuccess)
-      return sfail(CFGPU_ECUDA, "ensemble step failed");
-    s->steps_done += e->k;
-    bool boundary = false;
-    for (long long id : e->slot_req)
-      if (id >= 0) {
-        Request& r = *s->reqs[id];
-        r.done += e->k;
-        r.left -= e->k;
-        s->field_steps += e->k;
-        boundary |= r.left == 0;
-      }
-    e->k = 0;
-    if (!boundary) continue;
-    // CFL numbers at the interval boundary (the next interval's start), one pass over all fields
-    std::vector<double> cfl_now(e->slot_req.size(), 0.0);
-    if (cfgpu_ensemble_cfl(e->h, cfl_now.data()) != CFGPU_OK) return sfail(CFGPU_ECUDA, cfgpu_last_error());
-    for (int i = 0; i < (int)e->slot_req.size(); ++i)
-      if (e->slot_req[i] >= 0 && s->reqs[e->slot_req[i]]->left == 0) SCK(interval_end(s, e.get(), i, cfl_now));
+    SCK(cfgpu_rt::advance_async(e->h, k));
+    if (cudaEventRecord(e->done, cfgpu_rt::stream(e->h)) != cudaSuccess) return sfail(CFGPU_ECUDA, "event record");
+    e->k = k;
   }
   if (active) {
     int n = (int)s->queue.size();
@@ -507,7 +545,11 @@ cfgpu_status cfgpu_server_stats(cfgpu_server s, long long* stats) {
 cfgpu_status cfgpu_server_destroy(cfgpu_server s) {
   if (!s) return CFGPU_OK;
   for (auto& e : s->ens)
-    if (e) cfgpu_dns_destroy(e->h);
+    if (e) {
+      if (e->k) cudaEventSynchronize(e->done);
+      cfgpu_dns_destroy(e->h);
+      if (e->done) cudaEventDestroy(e->done);
+    }
   for (auto& kv : s->staging) cfgpu_dns_destroy(kv.second);
   delete s;
   return CFGPU_OK;

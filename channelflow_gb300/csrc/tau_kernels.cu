@@ -984,6 +984,204 @@ __device__ void helm_t(int M, int q, const double* __restrict__ hlo, const doubl
   }
 }
 
+// ---------------------------------------------------------------------------
+// Right-hand side of the step solve (NSE::linear and the scheme's combination,
+// nse.cpp:393-477, dnsalgo.cpp:202-253, 641-697, 419-470) for the table-staged
+// solve: one group of four lanes (re/im part, Chebyshev parity) per (mode,
+// component), three times the lanes of the solve, writing Rx, Ry, Rz to the
+// scratch lines 0, 2 and 1 (the solve reads them back).
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(32) k_tau_rhs(GridDev g, int N, SolveParams sp, SolvePtrs P) {
+  extern __shared__ double sm[];
+  const int lane = threadIdx.x;
+  const int t = blockIdx.x * 32 + lane;
+  const int Md = g.Md;
+  const int grp = t >> 2;
+  const bool act = grp < 3 * Md;
+  const int m = act ? grp / 3 : Md - 1;
+  const int cc = act ? grp % 3 : 0;
+  const int part = (t >> 1) & 1, q = t & 1;
+  const unsigned gmask = 0xFu << (lane & 28);
+  const int row = 2 * Md;
+  const size_t comp = (size_t)row * N;
+  const int off = 2 * m + part, poff = 2 * m + (1 - part);
+  const int M0 = (N - 1) / 2 + 1;
+  const int M = q ? (N - 1) / 2 : M0;
+  const int Nb = N - 1;
+  const double scale = 4.0 / (g.b - g.a);
+  double* ct = sm;
+  double* lines = sm + ((N + 1) & ~1);
+  for (int n = lane; n < N; n += 32) ct[n] = scale * (n + 1);
+  __syncwarp();
+  auto S = [&](int slot) { return SLn{lines + (size_t)slot * M0 * 32 + lane}; };
+  auto So = [&](int slot) { return SLn{lines + (size_t)slot * M0 * 32 + (lane ^ 1)}; };
+  auto G = [&](const double* base) { return PLn{const_cast<double*>(base) + off + q * row, 2 * row}; };
+  auto Go = [&](const double* base) { return PLn{const_cast<double*>(base) + off + (1 - q) * row, 2 * row}; };
+  auto Gp = [&](const double* base) { return PLn{const_cast<double*>(base) + poff + q * row, 2 * row}; };
+  double* Rxg = P.scratch;
+  double* Rzg = P.scratch + comp;
+  double* Ryg = P.scratch + 2 * comp;
+  const int kx = mode_kx(g, m), kz = mode_kz(g, m);
+  const bool m00 = (kx == 0 && kz == 0);
+  const int fld = mode_field(g, m);
+  if (P.slot) apply_slot(sp, P.slot[fld]);
+  const size_t fb = (size_t)P.base_stride * fld;
+  const double nu = sp.nu;
+
+  // ---- A: right-hand side -------------------------------------------------
+  if (sp.kind == 0) {
+    PLn outx = G(Rxg), outz = G(Rzg);
+    PLn outy = G(Ryg);
+    for (int c = cc; c <= cc; ++c) {
+      for (int i0 = 0; i0 < M; i0 += TCH) {
+        double acc[TCH];
+#pragma unroll
+        for (int k = 0; k < TCH; ++k) acc[k] = 0.0;
+        for (int j = 0; j < sp.order; ++j) {
+          const double* uj = P.uin[j] + c * comp;
+          const R* nj = static_cast<const R*>(P.nin[j]) + c * comp;
+          double uv[TCH], nv[TCH];
+#pragma unroll
+          for (int k = 0; k < TCH; ++k)
+            if (i0 + k < M) {
+              const size_t o = (size_t)(2 * (i0 + k) + q) * row + off;
+              uv[k] = __ldg(uj + o);
+              nv[k] = (double)__ldg(nj + o);
+            }
+#pragma unroll
+          for (int k = 0; k < TCH; ++k)
+            if (i0 + k < M) acc[k] += sp.a[j] * uv[k] + sp.b[j] * nv[k];
+        }
+#pragma unroll
+        for (int k = 0; k < TCH; ++k)
+          if (i0 + k < M) {
+            const int i = i0 + k, n = 2 * i + q;
+            double a = acc[k];
+            if (m00 && part == 0 && c != 1) {
+              a += nu * (c == 0 ? P.Ubaseyy[fb + n] : P.Wbaseyy[fb + n]);
+              if (n == 0 && sp.constraint == 0) a -= (c == 0 ? sp.dPdxRef : sp.dPdzRef);
+            }
+            if (act) (c == 0 ? outx : (c == 1 ? outy : outz))[i] = a;
+          }
+      }
+    }
+  } else {
+    const double kappa2 = 4 * M_PI * M_PI * ((kx / g.Lx) * (kx / g.Lx) + (kz / g.Lz) * (kz / g.Lz));
+    const double Dx = 2 * M_PI * kx / g.Lx * (kx == g.kxmax ? 0.0 : 1.0);
+    const double Dz = 2 * M_PI * kz / g.Lz * (kz == g.kzmax ? 0.0 : 1.0);
+    for (int c = cc; c <= cc; ++c) {
+      PLn uc = G(P.uin[0] + c * comp);
+      PLn uo = Go(P.uin[0] + c * comp);
+      SLn d1 = S(0);
+      __syncwarp(gmask);
+      double s = 0.0;
+      {
+        double dn2 = 0.0;
+        int i = M - 1;
+        if (q == 0) {
+          const double v = dn2 + ct[2 * i] * 0.0;
+          d1[i] = v;
+          s += v;
+          dn2 = v;
+          i--;
+        }
+        for (; i >= 0; i -= TCH) {
+          double xv[TCH];
+#pragma unroll
+          for (int k = 0; k < TCH; ++k)
+            if (i - k >= 0) xv[k] = uo[i - k + q];
+#pragma unroll
+          for (int k = 0; k < TCH; ++k)
+            if (i - k >= 0) {
+              const int n = 2 * (i - k) + q;
+              double v = dn2 + ct[n] * (nu * xv[k]);
+              dn2 = v;
+              if (n == 0) v *= 0.5;
+              d1[i - k] = v;
+              s += v;
+            }
+        }
+      }
+      const double so = __shfl_xor_sync(gmask, s, 1);
+      double wall = 0.0;
+      if (m00 && part == 0 && sp.constraint == 1 && c != 1) {
+        const double s0 = q == 0 ? s : so, s1 = q == 0 ? so : s;
+        wall = ((s0 + s1) - (s0 - s1)) / (g.b - g.a);
+      }
+      __syncwarp(gmask);
+      SLn d1o = So(0);
+      PLn qo = Go(P.qin);
+      PLn qp = Gp(P.qin);
+      PLn outg = G(c == 0 ? Rxg : Rzg);
+      PLn outs = G(Ryg);
+      const R* Nj = static_cast<const R*>(P.nin[0]) + c * comp + off + q * row;
+      const R* Nj1 = sp.kind == 1 ? static_cast<const R*>(P.nin[1]) + c * comp + off + q * row : nullptr;
+      R* Q = sp.kind == 2 ? static_cast<R*>(P.Q) + c * comp + off + q * row : nullptr;
+      const double kD = c == 0 ? Dx : Dz;
+      double d2n2 = 0.0, dqn2 = 0.0;
+      for (int i0 = M - 1; i0 >= 0; i0 -= TCH) {
+        // prefetch the streamed inputs of TCH consecutive (descending) elements
+        double uv[TCH], qv[TCH], nv[TCH], n1v[TCH];
+#pragma unroll
+        for (int k = 0; k < TCH; ++k) {
+          const int i = i0 - k;
+          if (i >= 0) {
+            const int n = 2 * i + q;
+            uv[k] = uc[i];
+            qv[k] = c == 1 ? ((n + 1 <= Nb) ? qo[i + q] : 0.0) : qp[i];
+            nv[k] = (double)Nj[(size_t)i * 2 * row];
+            n1v[k] = sp.kind == 1 ? (double)Nj1[(size_t)i * 2 * row] : (double)Q[(size_t)i * 2 * row];
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < TCH; ++k) {
+          const int i = i0 - k;
+          if (i < 0) break;
+          const int n = 2 * i + q;
+          const double x1 = (n + 1 <= Nb) ? d1o[i + q] : 0.0;
+          double d2 = d2n2 + ct[n] * x1;
+          d2n2 = d2;
+          if (n == 0) d2 *= 0.5;
+          double gq;
+          if (c == 1) {
+            double dq = dqn2 + ct[n] * qv[k];
+            dqn2 = dq;
+            if (n == 0) dq *= 0.5;
+            gq = dq;
+          } else {
+            gq = part == 0 ? -(kD * qv[k]) : kD * qv[k];
+          }
+          const double u0 = uv[k];
+          double L = d2 - kappa2 * (nu * u0) - gq;
+          if (m00 && part == 0 && c != 1) {
+            L += nu * (c == 0 ? P.Ubaseyy[fb + n] : P.Wbaseyy[fb + n]);
+            if (n == 0) L -= sp.constraint == 0 ? (c == 0 ? sp.dPdxRef : sp.dPdzRef)
+                                                : wall + sp.baseShear[c == 0 ? 0 : 1];
+          }
+          const double nj = nv[k];
+          double rhs;
+          if (sp.kind == 1) {
+            rhs = (u0 * sp.lam + sp.a_b * L) + ((-sp.g_b) * nj + (-sp.z_b) * n1v[k]);
+          } else {
+            const double Qn = n1v[k] * sp.rkA - nj;
+            if (act) Q[(size_t)i * 2 * row] = (R)Qn;
+            rhs = L + (sp.lam * u0 + sp.B_C * Qn);
+          }
+          if (m00 && part == 0 && c != 1) {
+            rhs += nu * (c == 0 ? P.Ubaseyy[fb + n] : P.Wbaseyy[fb + n]);
+            if (n == 0 && sp.constraint == 0) rhs -= (c == 0 ? sp.dPdxRef : sp.dPdzRef);
+          }
+          if (act) (c == 1 ? outs : outg)[i] = rhs;
+        }
+      }
+    }
+  }
+  __syncwarp(gmask);
+  __threadfence_block();
+
+}
+
 template <typename R>
 __global__ void __launch_bounds__(32) k_tau_solve_t(GridDev g, int N, SolveParams sp, SolvePtrs P, HelmB hb,
                                                     TauTable tt) {
@@ -1055,154 +1253,18 @@ __global__ void __launch_bounds__(32) k_tau_solve_t(GridDev g, int N, SolveParam
   const double* __restrict__ hdi = hb.di;
   const double* __restrict__ hup = hb.up;
 
-  // ---- A: right-hand side -------------------------------------------------
-  if (sp.kind == 0) {
-    PLn outx = G(Rxg), outz = G(Rzg);
+  // ---- A: right-hand side (k_tau_rhs): Rx, Rz in scratch lines 0, 1; Ry (line 2) into slot 0 ------
+  {
+    PLn Ryg = G(P.scratch + 2 * comp);
     SLn outy = S(0);
-    for (int c = 0; c < 3; ++c) {
-      for (int i0 = 0; i0 < M; i0 += TCH) {
-        double acc[TCH];
+    for (int i = 0; i < M; i += TCH) {
+      double v[TCH];
 #pragma unroll
-        for (int k = 0; k < TCH; ++k) acc[k] = 0.0;
-        for (int j = 0; j < sp.order; ++j) {
-          const double* uj = P.uin[j] + c * comp;
-          const R* nj = static_cast<const R*>(P.nin[j]) + c * comp;
-          double uv[TCH], nv[TCH];
+      for (int k = 0; k < TCH; ++k)
+        if (i + k < M) v[k] = Ryg[i + k];
 #pragma unroll
-          for (int k = 0; k < TCH; ++k)
-            if (i0 + k < M) {
-              const size_t o = (size_t)(2 * (i0 + k) + q) * row + off;
-              uv[k] = __ldg(uj + o);
-              nv[k] = (double)__ldg(nj + o);
-            }
-#pragma unroll
-          for (int k = 0; k < TCH; ++k)
-            if (i0 + k < M) acc[k] += sp.a[j] * uv[k] + sp.b[j] * nv[k];
-        }
-#pragma unroll
-        for (int k = 0; k < TCH; ++k)
-          if (i0 + k < M) {
-            const int i = i0 + k, n = 2 * i + q;
-            double a = acc[k];
-            if (m00 && part == 0 && c != 1) {
-              a += nu * (c == 0 ? P.Ubaseyy[fb + n] : P.Wbaseyy[fb + n]);
-              if (n == 0 && sp.constraint == 0) a -= (c == 0 ? sp.dPdxRef : sp.dPdzRef);
-            }
-            if (c == 1) outy[i] = a;
-            else if (act) (c == 0 ? outx : outz)[i] = a;
-          }
-      }
-    }
-  } else {
-    const double kappa2 = 4 * M_PI * M_PI * ((kx / g.Lx) * (kx / g.Lx) + (kz / g.Lz) * (kz / g.Lz));
-    const double Dx = 2 * M_PI * kx / g.Lx * (kx == g.kxmax ? 0.0 : 1.0);
-    const double Dz = 2 * M_PI * kz / g.Lz * (kz == g.kzmax ? 0.0 : 1.0);
-    for (int c = 0; c < 3; ++c) {
-      PLn uc = G(P.uin[0] + c * comp);
-      PLn uo = Go(P.uin[0] + c * comp);
-      SLn d1 = S(2);
-      __syncwarp(gmask);
-      double s = 0.0;
-      {
-        double dn2 = 0.0;
-        int i = M - 1;
-        if (q == 0) {
-          const double v = dn2 + ct[2 * i] * 0.0;
-          d1[i] = v;
-          s += v;
-          dn2 = v;
-          i--;
-        }
-        for (; i >= 0; i -= TCH) {
-          double xv[TCH];
-#pragma unroll
-          for (int k = 0; k < TCH; ++k)
-            if (i - k >= 0) xv[k] = uo[i - k + q];
-#pragma unroll
-          for (int k = 0; k < TCH; ++k)
-            if (i - k >= 0) {
-              const int n = 2 * (i - k) + q;
-              double v = dn2 + ct[n] * (nu * xv[k]);
-              dn2 = v;
-              if (n == 0) v *= 0.5;
-              d1[i - k] = v;
-              s += v;
-            }
-        }
-      }
-      const double so = __shfl_xor_sync(gmask, s, 1);
-      double wall = 0.0;
-      if (m00 && part == 0 && sp.constraint == 1 && c != 1) {
-        const double s0 = q == 0 ? s : so, s1 = q == 0 ? so : s;
-        wall = ((s0 + s1) - (s0 - s1)) / (g.b - g.a);
-      }
-      __syncwarp(gmask);
-      SLn d1o = So(2);
-      PLn qo = Go(P.qin);
-      PLn qp = Gp(P.qin);
-      PLn outg = G(c == 0 ? Rxg : Rzg);
-      SLn outs = S(0);
-      const R* Nj = static_cast<const R*>(P.nin[0]) + c * comp + off + q * row;
-      const R* Nj1 = sp.kind == 1 ? static_cast<const R*>(P.nin[1]) + c * comp + off + q * row : nullptr;
-      R* Q = sp.kind == 2 ? static_cast<R*>(P.Q) + c * comp + off + q * row : nullptr;
-      const double kD = c == 0 ? Dx : Dz;
-      double d2n2 = 0.0, dqn2 = 0.0;
-      for (int i0 = M - 1; i0 >= 0; i0 -= TCH) {
-        // prefetch the streamed inputs of TCH consecutive (descending) elements
-        double uv[TCH], qv[TCH], nv[TCH], n1v[TCH];
-#pragma unroll
-        for (int k = 0; k < TCH; ++k) {
-          const int i = i0 - k;
-          if (i >= 0) {
-            const int n = 2 * i + q;
-            uv[k] = uc[i];
-            qv[k] = c == 1 ? ((n + 1 <= Nb) ? qo[i + q] : 0.0) : qp[i];
-            nv[k] = (double)Nj[(size_t)i * 2 * row];
-            n1v[k] = sp.kind == 1 ? (double)Nj1[(size_t)i * 2 * row] : (double)Q[(size_t)i * 2 * row];
-          }
-        }
-#pragma unroll
-        for (int k = 0; k < TCH; ++k) {
-          const int i = i0 - k;
-          if (i < 0) break;
-          const int n = 2 * i + q;
-          const double x1 = (n + 1 <= Nb) ? d1o[i + q] : 0.0;
-          double d2 = d2n2 + ct[n] * x1;
-          d2n2 = d2;
-          if (n == 0) d2 *= 0.5;
-          double gq;
-          if (c == 1) {
-            double dq = dqn2 + ct[n] * qv[k];
-            dqn2 = dq;
-            if (n == 0) dq *= 0.5;
-            gq = dq;
-          } else {
-            gq = part == 0 ? -(kD * qv[k]) : kD * qv[k];
-          }
-          const double u0 = uv[k];
-          double L = d2 - kappa2 * (nu * u0) - gq;
-          if (m00 && part == 0 && c != 1) {
-            L += nu * (c == 0 ? P.Ubaseyy[fb + n] : P.Wbaseyy[fb + n]);
-            if (n == 0) L -= sp.constraint == 0 ? (c == 0 ? sp.dPdxRef : sp.dPdzRef)
-                                                : wall + sp.baseShear[c == 0 ? 0 : 1];
-          }
-          const double nj = nv[k];
-          double rhs;
-          if (sp.kind == 1) {
-            rhs = (u0 * sp.lam + sp.a_b * L) + ((-sp.g_b) * nj + (-sp.z_b) * n1v[k]);
-          } else {
-            const double Qn = n1v[k] * sp.rkA - nj;
-            if (act) Q[(size_t)i * 2 * row] = (R)Qn;
-            rhs = L + (sp.lam * u0 + sp.B_C * Qn);
-          }
-          if (m00 && part == 0 && c != 1) {
-            rhs += nu * (c == 0 ? P.Ubaseyy[fb + n] : P.Wbaseyy[fb + n]);
-            if (n == 0 && sp.constraint == 0) rhs -= (c == 0 ? sp.dPdxRef : sp.dPdzRef);
-          }
-          if (c == 1) outs[i] = rhs;
-          else if (act) outg[i] = rhs;
-        }
-      }
+      for (int k = 0; k < TCH; ++k)
+        if (i + k < M) outy[i + k] = v[k];
     }
   }
   __syncwarp(gmask);
@@ -1349,17 +1411,26 @@ __global__ void __launch_bounds__(32) k_tau_solve_t(GridDev g, int N, SolveParam
   }
 }
 
+static size_t tau_t_smem(int N) {
+  const int M0 = (N - 1) / 2 + 1;
+  return sizeof(double) * (((N + 1) & ~1) + (size_t)4 * M0 * 32 + (size_t)4 * N * 8);
+}
+
+int tau_solve_launches(int N) { return tau_t_smem(N) <= 227 * 1024 ? 2 : 1; }
+
 template <typename R>
 cudaError_t launch_tau_solve(const GridDev& g, int N, const SolveParams& sp, const SolvePtrs& p, const HelmB& hb,
                              TauTable tt, cudaStream_t st) {
   const int M0 = (N - 1) / 2 + 1;
-  const size_t smem_t = sizeof(double) * (((N + 1) & ~1) + (size_t)4 * M0 * 32 + (size_t)4 * N * 8);
+  const size_t smem_t = tau_t_smem(N);
   if (smem_t <= 227 * 1024) {
     static bool attr = false;
     if (!attr) {
       cudaFuncSetAttribute(k_tau_solve_t<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
       attr = true;
     }
+    const size_t smem_r = sizeof(double) * (((N + 1) & ~1) + (size_t)M0 * 32);
+    k_tau_rhs<R><<<(12 * g.Md + 31) / 32, 32, smem_r, st>>>(g, N, sp, p);
     k_tau_solve_t<R><<<(4 * g.Md + 31) / 32, 32, smem_t, st>>>(g, N, sp, p, hb, tt);
     return cudaGetLastError();
   }
