@@ -11,6 +11,11 @@
 // RungeKuttaDNS) and the DNS facade channelflow/dns.cpp:22-163.
 #include <climits>
 #include <cmath>
+#include <atomic>
+#include <functional>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <complex>
 #include <cstdio>
 #include <cstring>
@@ -530,7 +535,8 @@ struct cfgpu_dns_s {
   // NL work
   void *C6 = nullptr, *W6 = nullptr, *X6 = nullptr, *Z3 = nullptr, *F3 = nullptr;
   double* scratch = nullptr;
-  int RP = 8;
+  int RP = 8;     // x rows per block of the z pass (autotuned)
+  int xcols = 0;  // kz columns per block of the x passes (autotuned; 0 = all that fit)
   // schemes
   Scheme main, init;
   bool has_init = false;
@@ -542,6 +548,7 @@ struct cfgpu_dns_s {
   int sym_interval = 100;
   // CUDA graphs of one main-scheme step, keyed by the step's buffer rotation state
   bool use_graphs = true;
+  bool autotune = true;  // block shapes of the FFT passes timed at creation (cached per grid)
   struct StepGraph {
     int key;
     cudaGraphExec_t exec;
@@ -599,36 +606,46 @@ int build_tables(cfgpu_dns d, Scheme& s) {
     cudaFree(t.s);
   }
   s.tau.clear();
-  for (double lt : s.lambda_t) {
+  const int nt = (int)s.lambda_t.size();
+  if (nt > 4) return fail(CFGPU_EINVAL, "more than 4 substeps");
+  TauSetupBatch tb{};
+  for (int j = 0; j < nt; ++j) {
     TauTable t{};
     CKS(dalloc(&t.f, FN * TF_NFIELDS, d->bytes));
     CKS(dalloc(&t.s, (size_t)d->gm.Md * TS_NSCALARS, d->bytes));
-    if (d->hetero) {
-      const int j = (int)s.tau.size();
-      for (int f = 0; f < d->nb; ++f) {
-        CK(launch_tau_setup(d->gm, d->N, lambda_at(s.method, d->sfl[f].dt, j), d->sfl[f].nu, hb, t, d->scratch,
-                            d->st, f * d->g.Md, d->g.Md));
-        d->launches++;
-      }
-    } else {
-      CK(launch_tau_setup(d->gm, d->N, lt, d->fl.nu, hb, t, d->scratch, d->st));
+    s.tau.push_back(t);
+    tb.tab[j] = t;
+    tb.lambda_t[j] = s.lambda_t[j];
+  }
+  // all substep tables in one launch (per field when the fields have their own nu and dt)
+  if (d->hetero) {
+    for (int f = 0; f < d->nb; ++f) {
+      for (int j = 0; j < nt; ++j) tb.lambda_t[j] = lambda_at(s.method, d->sfl[f].dt, j);
+      CK(launch_tau_setup_batch(d->gm, d->N, tb, nt, d->sfl[f].nu, hb, d->scratch, d->st, f * d->g.Md, d->g.Md));
       d->launches++;
     }
-    s.tau.push_back(t);
+  } else {
+    CK(launch_tau_setup_batch(d->gm, d->N, tb, nt, d->fl.nu, hb, d->scratch, d->st));
+    d->launches++;
   }
   return CFGPU_OK;
 }
 
 // Rebuild one field's part of every tau table (its nu changed).
+// A DNS running main-scheme steps only (its start-up done, fields arriving through
+// cfgpu_ensemble_load_slot) needs no start-up tables: those are rebuilt by the next restart.
 int build_slot_tables(cfgpu_dns d, int f) {
   HelmB hb{d->hb_lo, d->hb_di, d->hb_up};
   for (Scheme* s : {&d->main, &d->init}) {
-    if (s == &d->init && !d->has_init) continue;
-    for (size_t j = 0; j < s->tau.size(); ++j) {
-      CK(launch_tau_setup(d->gm, d->N, lambda_at(s->method, d->sfl[f].dt, (int)j), d->sfl[f].nu, hb, s->tau[j],
-                          d->scratch, d->st, f * d->g.Md, d->g.Md));
-      d->launches++;
+    if (s == &d->init && (!d->has_init || d->main.full)) continue;
+    TauSetupBatch tb{};
+    const int nt = (int)s->tau.size();
+    for (int j = 0; j < nt; ++j) {
+      tb.lambda_t[j] = lambda_at(s->method, d->sfl[f].dt, j);
+      tb.tab[j] = s->tau[j];
     }
+    CK(launch_tau_setup_batch(d->gm, d->N, tb, nt, d->sfl[f].nu, hb, d->scratch, d->st, f * d->g.Md, d->g.Md));
+    d->launches++;
   }
   return CFGPU_OK;
 }
@@ -680,9 +697,9 @@ int nonlinear_impl(cfgpu_dns d, const double* U, void* Nout, int form) {
     nin = gradient ? 12 : 3;
     nout = form == NL_CONVECTION ? 3 : (form == NL_DIVERGENCE ? 6 : 9);
   }
-  CK(launch_xinv<R>(gp, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)W, (cpx<R>*)d->X6, nin, d->st));
+  CK(launch_xinv<R>(gp, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)W, (cpx<R>*)d->X6, nin, d->st, d->xcols));
   CK(launch_zphys<R>(gp, form, d->pz, (const cpx<R>*)d->twz, d->RP, (const cpx<R>*)d->X6, (cpx<R>*)d->Z3, d->st));
-  CK(launch_xfwd<R>(gp, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)d->Z3, (cpx<R>*)d->F3, nout, d->st));
+  CK(launch_xfwd<R>(gp, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)d->Z3, (cpx<R>*)d->F3, nout, d->st, d->xcols));
   d->launches += 3;
   const R* F = (const R*)d->F3;
   if (form == NL_ROTATIONAL || form == NL_CONVECTION) {
@@ -1146,6 +1163,95 @@ int upload_tw(const std::vector<std::complex<long double>>& tw, void** dst, long
   return CFGPU_OK;
 }
 
+// Autotuner of the FFT passes' block shapes: kz columns per block of the x passes and x rows per block of
+// the z pass, timed with CUDA events on this DNS's own work arrays (their contents do not change the
+// work), the fastest kept; choices are cached per (grid, planes, precision, form).
+struct TuneKey {
+  int Nx, planes, Nz, NKz, prec, form;
+  bool operator<(const TuneKey& o) const {
+    return std::tie(Nx, planes, Nz, NKz, prec, form) < std::tie(o.Nx, o.planes, o.Nz, o.NKz, o.prec, o.form);
+  }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, std::pair<int, int>> g_tune;
+std::atomic<int> g_autotune{1};
+
+template <typename R>
+float time_ms(cfgpu_dns d, const std::function<cudaError_t()>& f) {
+  cudaEvent_t a = take_event(d), b = take_event(d);
+  float best = 1e30f;
+  for (int rep = 0; rep < 4; ++rep) {
+    cudaEventRecord(a, d->st);
+    if (f() != cudaSuccess) {
+      cudaGetLastError();
+      best = 1e30f;
+      break;
+    }
+    cudaEventRecord(b, d->st);
+    cudaEventSynchronize(b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    if (rep > 0) best = std::min(best, ms);  // first run warms up
+  }
+  d->ev_pool.push_back(a);
+  d->ev_pool.push_back(b);
+  return best;
+}
+
+template <typename R>
+int autotune(cfgpu_dns d, int form, int nin, int nout) {
+  const GridDev& gp = d->gp;
+  const TuneKey key{gp.Nx, gp.Ny, gp.Nz, gp.NKz, (int)sizeof(R), form};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) {
+      d->xcols = it->second.first;
+      d->RP = it->second.second;
+      return CFGPU_OK;
+    }
+  }
+  // small grids are launch-bound: keep the defaults
+  if ((long long)gp.Ny * gp.Nx * gp.NKz < 200000) return CFGPU_OK;
+  const cpx<R>* tw = (const cpx<R>*)d->twx;
+  float best = 1e30f;
+  int bestc = d->xcols;
+  for (int div : {1, 2, 3, 4, 6}) {
+    const int c = (gp.NKz + div - 1) / div;
+    if (c < 2 || xfft_smem_bytes<R>(gp, c) > 200 * 1024) continue;
+    const float t = time_ms<R>(d, [&]() {
+      cudaError_t e = launch_xinv<R>(gp, d->px, tw, (const cpx<R>*)d->W6, (cpx<R>*)d->X6, nin, d->st, c);
+      if (e != cudaSuccess) return e;
+      return launch_xfwd<R>(gp, d->px, tw, (const cpx<R>*)d->Z3, (cpx<R>*)d->F3, nout, d->st, c);
+    });
+    if (t < best) {
+      best = t;
+      bestc = c;
+    }
+  }
+  d->xcols = bestc;
+  if (form >= 0) {
+    best = 1e30f;
+    int bestr = d->RP;
+    for (int rp = d->RP; rp >= 2; rp /= 2) {
+      if (zphys_smem_bytes<R>(gp, form, rp) > 200 * 1024) continue;
+      const float t = time_ms<R>(d, [&]() {
+        return launch_zphys<R>(gp, form, d->pz, (const cpx<R>*)d->twz, rp, (const cpx<R>*)d->X6, (cpx<R>*)d->Z3,
+                               d->st);
+      });
+      if (t < best) {
+        best = t;
+        bestr = rp;
+      }
+    }
+    d->RP = bestr;
+  }
+  CK(cudaStreamSynchronize(d->st));
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune[key] = {d->xcols, d->RP};
+  return CFGPU_OK;
+}
+
 int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flags, const double* Ub, const double* Wb,
                     const double* u0, int nb = 1) {
   d->fl = *flags;
@@ -1331,6 +1437,13 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
   if ((fp64 ? xfft_smem_bytes<double>(g) : xfft_smem_bytes<float>(g)) > 227 * 1024 || zbytes(zform, d->RP) > 227 * 1024)
     return fail(CFGPU_ENOTSUP, "grid too large for the shared-memory FFT passes");
   if (cheb_smem_bytes(Ny, rs) > 200 * 1024) return fail(CFGPU_ENOTSUP, "Ny too large for the Chebyshev kernel");
+  d->autotune = g_autotune.load() != 0;
+  if (d->autotune) {
+    const int tform = f.nonlinearity == CFGPU_LinearAboutProfile
+                          ? -1
+                          : (rot ? NL_ROTATIONAL : (f.nonlinearity == CFGPU_SkewSymmetric ? NL_SKEW : NL_CONVECTION));
+    CKS(fp64 ? autotune<double>(d, tform, nin, nout) : autotune<float>(d, tform, nin, nout));
+  }
 
   // schemes (DNS::DNS, dns.cpp:22-39)
   CKS(setup_scheme(d->main, f.timestepping, f.dt));
@@ -1422,7 +1535,7 @@ int cfl_impl(cfgpu_dns d, double* cfl) {
   CK(launch_grad_cheb<R>(g, d->N, false, d->Ucur, W, (const R*)d->cinvA, (const R*)d->cinvB, (const R*)d->cderA,
                          (const R*)d->cderB, (const R*)(d->hetero ? d->baseyS : d->basey), 0.0, d->st,
                          d->hetero ? 4 * d->N : 0));
-  CK(launch_xinv<R>(d->gp, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)W, (cpx<R>*)d->X6, 3, d->st));
+  CK(launch_xinv<R>(d->gp, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)W, (cpx<R>*)d->X6, 3, d->st, d->xcols));
   CK(cudaMemsetAsync(d->dred, 0, d->nb * sizeof(unsigned long long), d->st));
   CK(launch_zcfl<R>(d->gp, d->pz, (const cpx<R>*)d->twz, d->RP, (const cpx<R>*)d->X6, d->dyc, g.Lx / g.Nx,
                     g.Lz / g.Nz, d->nb, d->dred, d->st));
@@ -1914,6 +2027,15 @@ cfgpu_status cfgpu_field_symmetry(const cfgpu_grid* grid, int dealias, int Nd, c
   if (e != cudaSuccess) st = fail(CFGPU_ECUDA, std::string("symmetry: ") + cudaGetErrorString(e));
   if (st == CFGPU_OK) scatter_modes(&tmp, h.data(), Nd, u);
   return st;
+}
+
+cfgpu_status cfgpu_set_autotune(int enable) {
+  g_autotune.store(enable ? 1 : 0);
+  if (!enable) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune.clear();
+  }
+  return CFGPU_OK;
 }
 
 cfgpu_status cfgpu_dns_set_graphs(cfgpu_dns d, int enable) {

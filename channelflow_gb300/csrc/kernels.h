@@ -56,19 +56,20 @@ cudaError_t launch_rotation(const GridDev& g, int N, const double* U, const doub
                             double Vsuck, R* F, cudaStream_t st);
 
 template <typename R>
-size_t xfft_smem_bytes(const GridDev& g);
+size_t xfft_smem_bytes(const GridDev& g, int czc = 0);  // czc <= 0: all solved kz columns that fit
 template <typename R>
 size_t zcross_smem_bytes(const GridDev& g, int RP);
 
+// x passes: czc kz columns per block (0: as many as fit in shared memory)
 template <typename R>
 cudaError_t launch_xinv(const GridDev& g, const FftPlan& px, const cpx<R>* twx, const cpx<R>* W, cpx<R>* X, int ncomp,
-                        cudaStream_t st);
+                        cudaStream_t st, int czc = 0);
 template <typename R>
 cudaError_t launch_zcross(const GridDev& g, const FftPlan& pz, const cpx<R>* twz, int RP, const cpx<R>* X, cpx<R>* Z,
                           cudaStream_t st);
 template <typename R>
 cudaError_t launch_xfwd(const GridDev& g, const FftPlan& px, const cpx<R>* twx, const cpx<R>* Z, cpx<R>* F, int ncomp,
-                        cudaStream_t st);
+                        cudaStream_t st, int czc = 0);
 
 // ---------------------------------------------------------------------------
 // Tau / Helmholtz per-mode tables (FP64), layout [field][n][m] with m the
@@ -98,6 +99,13 @@ struct HelmB {
 // Tables of modes m0 .. m0+mcount-1 of g (mcount <= 0: all modes) for lambda_t and nu.
 cudaError_t launch_tau_setup(const GridDev& g, int N, double lambda_t, double nu, const HelmB& hb, TauTable tt,
                              double* scratch, cudaStream_t st, int m0 = 0, int mcount = 0);
+// Up to 4 tables (the substeps of a scheme) in one launch; scratch holds 4 lines of N*Md doubles per table.
+struct TauSetupBatch {
+  double lambda_t[4];
+  TauTable tab[4];
+};
+cudaError_t launch_tau_setup_batch(const GridDev& g, int N, const TauSetupBatch& tb, int ntab, double nu,
+                                   const HelmB& hb, double* scratch, cudaStream_t st, int m0 = 0, int mcount = 0);
 
 // Per-mode solve parameters for one substep.
 struct SolveParams {

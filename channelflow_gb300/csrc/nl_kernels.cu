@@ -541,8 +541,8 @@ int xfft_cols(const GridDev& g) {
   return c;
 }
 template <typename R>
-size_t xfft_smem_bytes(const GridDev& g) {
-  return 2 * sizeof(cpx<R>) * (size_t)xfft_cols<R>(g) * (g.Nx + 1);
+size_t xfft_smem_bytes(const GridDev& g, int czc) {
+  return 2 * sizeof(cpx<R>) * (size_t)(czc > 0 ? czc : xfft_cols<R>(g)) * (g.Nx + 1);
 }
 template <typename R>
 size_t zcross_smem_bytes(const GridDev& g, int RP) {
@@ -551,14 +551,15 @@ size_t zcross_smem_bytes(const GridDev& g, int RP) {
 
 template <typename R>
 cudaError_t launch_xinv(const GridDev& g, const FftPlan& px, const cpx<R>* twx, const cpx<R>* W, cpx<R>* X, int ncomp,
-                        cudaStream_t st) {
+                        cudaStream_t st, int czc) {
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(k_xinv<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     attr_set = true;
   }
-  const int czc = xfft_cols<R>(g);
-  k_xinv<R><<<dim3(g.Ny, ncomp, (g.NKz + czc - 1) / czc), 256, xfft_smem_bytes<R>(g), st>>>(g, px, twx, W, X, czc);
+  if (czc <= 0 || czc > g.NKz) czc = xfft_cols<R>(g);
+  k_xinv<R><<<dim3(g.Ny, ncomp, (g.NKz + czc - 1) / czc), 256, xfft_smem_bytes<R>(g, czc), st>>>(g, px, twx, W, X,
+                                                                                               czc);
   return cudaGetLastError();
 }
 
@@ -576,16 +577,16 @@ cudaError_t launch_zcross(const GridDev& g, const FftPlan& pz, const cpx<R>* twz
 
 template <typename R>
 cudaError_t launch_xfwd(const GridDev& g, const FftPlan& px, const cpx<R>* twx, const cpx<R>* Z, cpx<R>* F, int ncomp,
-                        cudaStream_t st) {
+                        cudaStream_t st, int czc) {
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(k_xfwd<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     attr_set = true;
   }
   const R scale = (R)(1.0 / ((double)g.Nx * (double)g.Nz));
-  const int czc = xfft_cols<R>(g);
-  k_xfwd<R><<<dim3(g.Ny, ncomp, (g.NKz + czc - 1) / czc), 256, xfft_smem_bytes<R>(g), st>>>(g, px, twx, Z, F, scale,
-                                                                                          czc);
+  if (czc <= 0 || czc > g.NKz) czc = xfft_cols<R>(g);
+  k_xfwd<R><<<dim3(g.Ny, ncomp, (g.NKz + czc - 1) / czc), 256, xfft_smem_bytes<R>(g, czc), st>>>(g, px, twx, Z, F,
+                                                                                               scale, czc);
   return cudaGetLastError();
 }
 
@@ -593,12 +594,12 @@ cudaError_t launch_xfwd(const GridDev& g, const FftPlan& px, const cpx<R>* twx, 
   template cudaError_t launch_curl_base<R>(const GridDev&, const double*, R*, const double*, const double*, double, \
                                            cudaStream_t);                                                           \
   template cudaError_t launch_xinv<R>(const GridDev&, const FftPlan&, const cpx<R>*, const cpx<R>*, cpx<R>*, int,   \
-                                      cudaStream_t);                                                                \
+                                      cudaStream_t, int);                                                           \
   template cudaError_t launch_zcross<R>(const GridDev&, const FftPlan&, const cpx<R>*, int, const cpx<R>*, cpx<R>*, \
                                         cudaStream_t);                                                              \
   template cudaError_t launch_xfwd<R>(const GridDev&, const FftPlan&, const cpx<R>*, const cpx<R>*, cpx<R>*, int,   \
-                                      cudaStream_t);                                                                \
-  template size_t xfft_smem_bytes<R>(const GridDev&);                                                               \
+                                      cudaStream_t, int);                                                           \
+  template size_t xfft_smem_bytes<R>(const GridDev&, int);                                                             \
   template size_t zcross_smem_bytes<R>(const GridDev&, int);
 
 INST_R(float)

@@ -172,8 +172,8 @@ double slot_cfl(cfgpu_dns h, int slot, int nb) {
 // Give the staging DNS the request's flags at its current dt and restart its start-up steps.
 int stage_restart(cfgpu_dns st, Request& r) {
   if (!r.fixed) r.flags.dt = r.ts.value();
-  SCK(cfgpu_ensemble_set_params(st, 0, &r.flags, nullptr, nullptr));
-  return cfgpu_rt::restart(st);
+  SCK(cfgpu_rt::restart(st));  // first: the start-up tables are then rebuilt with the request's parameters
+  return cfgpu_ensemble_set_params(st, 0, &r.flags, nullptr, nullptr);
 }
 
 int advance_sync(cfgpu_dns h, int n) {

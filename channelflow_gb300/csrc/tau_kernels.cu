@@ -955,9 +955,15 @@ struct TLn {
   const double* p;
   __device__ __forceinline__ double operator[](int i) const { return p[i * 16]; }
 };
+// staged factor line of the u/w kernel: [4 fields][N][4 modes]
+struct TLn4 {
+  const double* p;
+  __device__ __forceinline__ double operator[](int i) const { return p[i * 8]; }
+};
 
+template <typename TL>
 __device__ void helm_t(int M, int q, const double* __restrict__ hlo, const double* __restrict__ hdi,
-                       const double* __restrict__ hup, TLn band, TLn up, TLn lo, TLn inv, SLn f, SLn u, double bc) {
+                       const double* __restrict__ hup, TL band, TL up, TL lo, TL inv, SLn f, SLn u, double bc) {
   const int nM = 2 * (M - 1) + q;
   double fi = f[M - 1], fm = f[M - 2];
   double unext = __ldg(hlo + nM) * fm + __ldg(hdi + nM) * fi;
@@ -1095,7 +1101,7 @@ __global__ void __launch_bounds__(32) k_tau_rhs(GridDev g, int N, SolveParams sp
           for (int k = 0; k < TCH; ++k)
             if (i - k >= 0) {
               const int n = 2 * (i - k) + q;
-              double v = dn2 + ct[n] * (nu * xv[k]);
+              double v = dn2 + ct[n] * xv[k];  // diff(u)/... without the factor nu (applied in L)
               dn2 = v;
               if (n == 0) v *= 0.5;
               d1[i - k] = v;
@@ -1106,7 +1112,7 @@ __global__ void __launch_bounds__(32) k_tau_rhs(GridDev g, int N, SolveParams sp
       const double so = __shfl_xor_sync(gmask, s, 1);
       double wall = 0.0;
       if (m00 && part == 0 && sp.constraint == 1 && c != 1) {
-        const double s0 = q == 0 ? s : so, s1 = q == 0 ? so : s;
+        const double s0 = nu * (q == 0 ? s : so), s1 = nu * (q == 0 ? so : s);
         wall = ((s0 + s1) - (s0 - s1)) / (g.b - g.a);
       }
       __syncwarp(gmask);
@@ -1122,7 +1128,8 @@ __global__ void __launch_bounds__(32) k_tau_rhs(GridDev g, int N, SolveParams sp
       double d2n2 = 0.0, dqn2 = 0.0;
       for (int i0 = M - 1; i0 >= 0; i0 -= TCH) {
         // prefetch the streamed inputs of TCH consecutive (descending) elements
-        double uv[TCH], qv[TCH], nv[TCH], n1v[TCH];
+        double uv[TCH], qv[TCH];
+        R nv[TCH], n1v[TCH];
 #pragma unroll
         for (int k = 0; k < TCH; ++k) {
           const int i = i0 - k;
@@ -1130,8 +1137,8 @@ __global__ void __launch_bounds__(32) k_tau_rhs(GridDev g, int N, SolveParams sp
             const int n = 2 * i + q;
             uv[k] = uc[i];
             qv[k] = c == 1 ? ((n + 1 <= Nb) ? qo[i + q] : 0.0) : qp[i];
-            nv[k] = (double)Nj[(size_t)i * 2 * row];
-            n1v[k] = sp.kind == 1 ? (double)Nj1[(size_t)i * 2 * row] : (double)Q[(size_t)i * 2 * row];
+            nv[k] = Nj[(size_t)i * 2 * row];
+            n1v[k] = sp.kind == 1 ? Nj1[(size_t)i * 2 * row] : Q[(size_t)i * 2 * row];
           }
         }
 #pragma unroll
@@ -1153,20 +1160,21 @@ __global__ void __launch_bounds__(32) k_tau_rhs(GridDev g, int N, SolveParams sp
             gq = part == 0 ? -(kD * qv[k]) : kD * qv[k];
           }
           const double u0 = uv[k];
-          double L = d2 - kappa2 * (nu * u0) - gq;
+          double L = nu * (d2 - kappa2 * u0) - gq;  // nu (u'' - kappa^2 u) - grad q
           if (m00 && part == 0 && c != 1) {
             L += nu * (c == 0 ? P.Ubaseyy[fb + n] : P.Wbaseyy[fb + n]);
             if (n == 0) L -= sp.constraint == 0 ? (c == 0 ? sp.dPdxRef : sp.dPdzRef)
                                                 : wall + sp.baseShear[c == 0 ? 0 : 1];
           }
-          const double nj = nv[k];
+          // the nonlinear terms are combined at their own precision R (FP32 on the mixed path)
           double rhs;
           if (sp.kind == 1) {
-            rhs = (u0 * sp.lam + sp.a_b * L) + ((-sp.g_b) * nj + (-sp.z_b) * n1v[k]);
+            const R nc = (R)(-sp.g_b) * nv[k] + (R)(-sp.z_b) * n1v[k];
+            rhs = (u0 * sp.lam + sp.a_b * L) + (double)nc;
           } else {
-            const double Qn = n1v[k] * sp.rkA - nj;
-            if (act) Q[(size_t)i * 2 * row] = (R)Qn;
-            rhs = L + (sp.lam * u0 + sp.B_C * Qn);
+            const R Qn = n1v[k] * (R)sp.rkA - nv[k];
+            if (act) Q[(size_t)i * 2 * row] = Qn;
+            rhs = L + (sp.lam * u0 + sp.B_C * (double)Qn);
           }
           if (m00 && part == 0 && c != 1) {
             rhs += nu * (c == 0 ? P.Ubaseyy[fb + n] : P.Wbaseyy[fb + n]);
@@ -1368,40 +1376,8 @@ __global__ void __launch_bounds__(32) k_tau_solve_t(GridDev g, int N, SolveParam
     }
   }
   __syncwarp(gmask);
-  // ---- D: streamwise and spanwise velocity -------------------------------
-  SLn Ppt = Sp(1);
+  // ---- D: streamwise and spanwise velocity in k_tau_uw (reads q from qout) ----
   const bool zero_im = m00 && part == 1 && sp.force_real00;
-  for (int c = 0; c < 2; ++c) {
-    const double kL = c == 0 ? kxL : kzL;
-    PLn Rc = G(c == 0 ? Rxg : Rzg);
-    SLn r = S(2), o = S(3);
-    for (int i = 0; i < M; i += TCH) {
-      double rv[TCH];
-#pragma unroll
-      for (int k = 0; k < TCH; ++k)
-        if (i + k < M) rv[k] = Rc[i + k];
-#pragma unroll
-      for (int k = 0; k < TCH; ++k)
-        if (i + k < M) r[i + k] = part == 0 ? -(kL * Ppt[i + k]) - rv[k] : kL * Ppt[i + k] - rv[k];
-    }
-    helm_t(M, q, hlo, hdi, hup, TS(0), TS(1), TS(2), TS(3), r, o, 0.0);
-    if (m00 && sp.constraint == 1 && part == 0) {
-      if (q == 0) {
-        double amean = o[0];
-        for (int i = 1; i < M; ++i) amean -= o[i] / (double)((2 * i) * (2 * i) - 1);
-        const double ucmean = tt.s[TS_UCMEAN * Md + m];
-        const double target = c == 0 ? sp.umean : sp.wmean;
-        const double mu = nu * (target - amean) / ucmean;
-        r[0] = r[0] + mu;
-        helm_t(M, q, hlo, hdi, hup, TS(0), TS(1), TS(2), TS(3), r, o, 0.0);
-        if (act && P.dPdx_out) P.dPdx_out[2 * mode_field(g, m) + c] = mu;
-      }
-    }
-    if (act) {
-      PLn gout = G(P.uout + (c == 0 ? 0 : 2) * comp);
-      for (int i = 0; i < M; ++i) gout[i] = zero_im ? 0.0 : o[i];
-    }
-  }
   if (act) {
     PLn gq = G(P.qout), gv = G(P.uout + comp);
     for (int i = 0; i < M; ++i) {
@@ -1411,12 +1387,109 @@ __global__ void __launch_bounds__(32) k_tau_solve_t(GridDev g, int N, SolveParam
   }
 }
 
+// ---------------------------------------------------------------------------
+// Streamwise and spanwise velocity of the step solve (the u and w Helmholtz
+// solves of TauSolver::solve, tausolver.cpp:347-402, and the mean-constrained
+// solve of the (0,0) mode, helmholtz.cpp:158-213): one group of four lanes per
+// (mode, u or w), four modes per warp, from the pressure the solve kernel wrote
+// to qout and Rx, Rz in the scratch lines.  The solves run in place in one
+// shared-memory line per lane; the velocity factors of the warp's modes are
+// staged in shared memory.
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(32) k_tau_uw(GridDev g, int N, SolveParams sp, SolvePtrs P, HelmB hb,
+                                               TauTable tt) {
+  extern __shared__ double sm[];
+  const int lane = threadIdx.x;
+  const int t = blockIdx.x * 32 + lane;
+  const int Md = g.Md;
+  const int grp = t >> 2;
+  const bool act = grp < 2 * Md;
+  const int m = act ? grp >> 1 : Md - 1;
+  const int cu = act ? (grp & 1) : 0;  // 0: u, 1: w
+  const int mi = lane >> 3;            // mode within the warp
+  const int mbase = blockIdx.x * 4;
+  const int part = (t >> 1) & 1, q = t & 1;
+  const int row = 2 * Md;
+  const size_t comp = (size_t)row * N;
+  const int off = 2 * m + part, poff = 2 * m + (1 - part);
+  const size_t FN = (size_t)N * Md;
+  const int M0 = (N - 1) / 2 + 1;
+  const int M = q ? (N - 1) / 2 : M0;
+  double* tab = sm + (size_t)M0 * 32;  // [4][N][4]
+  {
+    const int total = 4 * N * 4;
+    for (int b0 = lane; b0 < total; b0 += 32 * 16) {
+      double v[16];
+#pragma unroll
+      for (int k2 = 0; k2 < 16; ++k2) {
+        const int idx = b0 + 32 * k2;
+        v[k2] = 0.0;
+        if (idx < total) {
+          const int k = idx / (N * 4), rem = idx - k * N * 4;
+          const int n = rem >> 2, mm = mbase + (rem & 3);
+          if (mm < Md) v[k2] = __ldg(&tt.f[(size_t)(TF_VBAND + k) * FN + (size_t)n * Md + mm]);
+        }
+      }
+#pragma unroll
+      for (int k2 = 0; k2 < 16; ++k2)
+        if (b0 + 32 * k2 < total) tab[b0 + 32 * k2] = v[k2];
+    }
+  }
+  __syncwarp();
+  auto TS = [&](int k) { return TLn4{tab + ((size_t)k * N + q) * 4 + mi}; };
+  auto G = [&](const double* base) { return PLn{const_cast<double*>(base) + off + q * row, 2 * row}; };
+  auto Gp = [&](const double* base) { return PLn{const_cast<double*>(base) + poff + q * row, 2 * row}; };
+  const int kx = mode_kx(g, m), kz = mode_kz(g, m);
+  const bool m00 = (kx == 0 && kz == 0);
+  const int fld = mode_field(g, m);
+  if (P.slot) apply_slot(sp, P.slot[fld]);
+  const double nu = sp.nu;
+  const double kL = cu == 0 ? 2 * M_PI * kx / g.Lx : 2 * M_PI * kz / g.Lz;
+  const bool zero_im = m00 && part == 1 && sp.force_real00;
+  SLn r{sm + lane};
+  PLn Rc = G(P.scratch + (cu == 0 ? 0 : comp));
+  PLn Pp = Gp(P.qout);
+  auto fill = [&]() {
+    for (int i = 0; i < M; i += TCH) {
+      double rv[TCH], pv[TCH];
+#pragma unroll
+      for (int k = 0; k < TCH; ++k)
+        if (i + k < M) {
+          rv[k] = Rc[i + k];
+          pv[k] = Pp[i + k];
+        }
+#pragma unroll
+      for (int k = 0; k < TCH; ++k)
+        if (i + k < M) r[i + k] = part == 0 ? -(kL * pv[k]) - rv[k] : kL * pv[k] - rv[k];
+    }
+  };
+  fill();
+  helm_t(M, q, hb.lo, hb.di, hb.up, TS(0), TS(1), TS(2), TS(3), r, r, 0.0);
+  if (m00 && sp.constraint == 1 && part == 0 && q == 0) {
+    // mean-constrained solve of the real part (the mean involves even n only)
+    double amean = r[0];
+    for (int i = 1; i < M; ++i) amean -= r[i] / (double)((2 * i) * (2 * i) - 1);
+    const double ucmean = tt.s[TS_UCMEAN * Md + m];
+    const double target = cu == 0 ? sp.umean : sp.wmean;
+    const double mu = nu * (target - amean) / ucmean;
+    fill();
+    r[0] = r[0] + mu;
+    helm_t(M, q, hb.lo, hb.di, hb.up, TS(0), TS(1), TS(2), TS(3), r, r, 0.0);
+    if (act && P.dPdx_out) P.dPdx_out[2 * mode_field(g, m) + cu] = mu;
+  }
+  if (act) {
+    PLn gout = G(P.uout + (cu == 0 ? 0 : 2) * comp);
+    for (int i = 0; i < M; ++i) gout[i] = zero_im ? 0.0 : r[i];
+  }
+}
+
 static size_t tau_t_smem(int N) {
   const int M0 = (N - 1) / 2 + 1;
   return sizeof(double) * (((N + 1) & ~1) + (size_t)4 * M0 * 32 + (size_t)4 * N * 8);
 }
 
-int tau_solve_launches(int N) { return tau_t_smem(N) <= 227 * 1024 ? 2 : 1; }
+int tau_solve_launches(int N) { return tau_t_smem(N) <= 227 * 1024 ? 3 : 1; }
 
 template <typename R>
 cudaError_t launch_tau_solve(const GridDev& g, int N, const SolveParams& sp, const SolvePtrs& p, const HelmB& hb,
@@ -1432,6 +1505,8 @@ cudaError_t launch_tau_solve(const GridDev& g, int N, const SolveParams& sp, con
     const size_t smem_r = sizeof(double) * (((N + 1) & ~1) + (size_t)M0 * 32);
     k_tau_rhs<R><<<(12 * g.Md + 31) / 32, 32, smem_r, st>>>(g, N, sp, p);
     k_tau_solve_t<R><<<(4 * g.Md + 31) / 32, 32, smem_t, st>>>(g, N, sp, p, hb, tt);
+    const size_t smem_u = sizeof(double) * ((size_t)M0 * 32 + (size_t)4 * N * 4);
+    k_tau_uw<R><<<(8 * g.Md + 31) / 32, 32, smem_u, st>>>(g, N, sp, p, hb, tt);
     return cudaGetLastError();
   }
   const int T = 64;

@@ -178,6 +178,12 @@ cfgpu_status cfgpu_field_symmetry(const cfgpu_grid* grid, int dealias, int Nd, c
  * profiling is on or with the Alternating nonlinearity.
  */
 cfgpu_status cfgpu_dns_set_graphs(cfgpu_dns dns, int enable);
+
+/* Block shapes of the FFT passes (kz columns per block of the x passes, x rows per block of the z pass) are
+ * chosen at DNS creation by timing candidates on the DNS's own arrays, cached per grid shape, for grids with
+ * Ny * Nx * (Kz+1) >= 200000 planes' worth of work; results do not depend on the choice.  enable = 0 makes
+ * later DNS objects use the defaults and clears the cache. */
+cfgpu_status cfgpu_set_autotune(int enable);
 cfgpu_status cfgpu_dns_set_profiling(cfgpu_dns dns, int enable);
 cfgpu_status cfgpu_dns_phase_times(cfgpu_dns dns, double* nl_ms, long long* nl_count, double* tau_ms,
                                    long long* tau_count);

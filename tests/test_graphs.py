@@ -57,3 +57,20 @@ def test_graphs_dropped_by_reset_dt():
     ue, qe, _ = _run(g, fl, False, 20, "fp64", reset_at=9)
     ug, qg, _ = _run(g, fl, True, 20, "fp64", reset_at=9)
     assert np.array_equal(ue, ug) and np.array_equal(qe, qg)
+
+
+def test_autotuned_block_shapes_do_not_change_results():
+    """The FFT passes' block shapes (autotuned above ~200k plane-columns) leave every column's arithmetic
+    unchanged: tuned and default runs are identical."""
+    from channelflow_gb300 import _lib as L
+    g = O.Grid(128, 65, 128, *COUETTE_BOX)
+    fl = O.DNSFlags(nu=1 / 400, dt=0.01, baseflow=O.LaminarBase, ulowerwall=-1.0, uupperwall=1.0)
+    lib = L.load()
+    try:
+        lib.cfgpu_set_autotune(0)
+        ud, qd, _ = _run(g, fl, True, 4, "mixed")
+        lib.cfgpu_set_autotune(1)
+        ut, qt, _ = _run(g, fl, True, 4, "mixed")
+    finally:
+        lib.cfgpu_set_autotune(1)
+    assert np.array_equal(ud, ut) and np.array_equal(qd, qt)
