@@ -167,12 +167,16 @@ __device__ __forceinline__ void apply_slot(SolveParams& sp, const SlotParams& s)
 
 // One thread per mode: the TauSolver constructor for lambda = lambda_t + nu kappa^2,
 // for modes m0 .. m0+mcount-1.
-__global__ void k_tau_setup(GridDev g, int N, double lambda_t, double nu, HelmB hb, TauTable tt, double* scratch,
-                            int m0, int mcount) {
+// blockIdx.y selects one of tb's tables (its lambda_t; 4 scratch lines of its own).
+__global__ void k_tau_setup(GridDev g, int N, TauSetupBatch tb, double nu, HelmB hb, double* scratch, int m0,
+                            int mcount) {
   const int m = m0 + blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= m0 + mcount || m >= g.Md) return;
   const size_t Md = g.Md;
   const size_t FN = (size_t)N * Md;
+  const double lambda_t = tb.lambda_t[blockIdx.y];
+  const TauTable tt = tb.tab[blockIdx.y];
+  scratch += (size_t)blockIdx.y * 4 * FN;
   auto T = [&](int f) { return Ln{tt.f + f * FN + m, Md}; };
   auto S = [&](int k) { return Ln{scratch + k * FN + m, Md}; };
   const int kx = mode_kx(g, m), kz = mode_kz(g, m);
@@ -245,15 +249,24 @@ __global__ void k_tau_setup(GridDev g, int N, double lambda_t, double nu, HelmB 
   s[TS_LAMBDA * Md] = lambda;
 }
 
-cudaError_t launch_tau_setup(const GridDev& g, int N, double lambda_t, double nu, const HelmB& hb, TauTable tt,
-                             double* scratch, cudaStream_t st, int m0, int mcount) {
+cudaError_t launch_tau_setup_batch(const GridDev& g, int N, const TauSetupBatch& tb, int ntab, double nu,
+                                   const HelmB& hb, double* scratch, cudaStream_t st, int m0, int mcount) {
   const int T = 64;
   if (mcount <= 0) {
     m0 = 0;
     mcount = g.Md;
   }
-  k_tau_setup<<<(mcount + T - 1) / T, T, 0, st>>>(g, N, lambda_t, nu, hb, tt, scratch, m0, mcount);
+  if (ntab < 1 || ntab > 4) return cudaErrorInvalidValue;
+  k_tau_setup<<<dim3((mcount + T - 1) / T, ntab), T, 0, st>>>(g, N, tb, nu, hb, scratch, m0, mcount);
   return cudaGetLastError();
+}
+
+cudaError_t launch_tau_setup(const GridDev& g, int N, double lambda_t, double nu, const HelmB& hb, TauTable tt,
+                             double* scratch, cudaStream_t st, int m0, int mcount) {
+  TauSetupBatch tb{};
+  tb.lambda_t[0] = lambda_t;
+  tb.tab[0] = tt;
+  return launch_tau_setup_batch(g, N, tb, 1, nu, hb, scratch, st, m0, mcount);
 }
 
 // ---------------------------------------------------------------------------
