@@ -131,6 +131,9 @@ struct cfgpu_server_s {
   std::vector<std::unique_ptr<Ens>> ens;  // null entries are dropped ensembles
   std::map<Key, cfgpu_dns> staging;       // one-field heterogeneous DNS per key
   long long steps_done = 0, field_steps = 0;
+  // host-side accounting: seconds in admission (staging), in interval ends (CFL pass, dt changes), chunks
+  double t_admit = 0, t_interval = 0;
+  long long chunks = 0, dt_changes = 0;
 };
 
 namespace {
@@ -253,6 +256,7 @@ int interval_end(cfgpu_server_s* s, Ens* e, int i, const std::vector<double>& cf
   }
   if (r.ts.variable && r.ts.adjust(r.cfl_start)) {
     // dt changed: restart the start-up steps at the new dt through the staging DNS, then back into the slot
+    s->dt_changes++;
     cfgpu_dns st = nullptr;
     SCK(make_staging(s, r, &st));
     SCK(stage_restart(st, r));
@@ -304,6 +308,12 @@ int complete_chunk(cfgpu_server_s* s, Ens* e, bool wait, bool* completed) {
     }
   e->k = 0;
   if (!boundary) return CFGPU_OK;
+  const double t0 = now_s();
+  struct Acc {
+    cfgpu_server_s* s;
+    double t0;
+    ~Acc() { s->t_interval += now_s() - t0; }
+  } acc{s, t0};
   std::vector<double> cfl_now(e->slot_req.size(), 0.0);
   if (cfgpu_ensemble_cfl(e->h, cfl_now.data()) != CFGPU_OK) return sfail(CFGPU_ECUDA, cfgpu_last_error());
   for (int i = 0; i < (int)e->slot_req.size(); ++i)
@@ -335,7 +345,16 @@ void drop_idle(cfgpu_server_s* s) {
     }
 }
 
+int admit_impl(cfgpu_server_s* s);
+
 int admit(cfgpu_server_s* s) {
+  const double t0 = now_s();
+  const int st = admit_impl(s);
+  s->t_admit += now_s() - t0;
+  return st;
+}
+
+int admit_impl(cfgpu_server_s* s) {
   std::deque<long long> keep;
   bool dropped = false;
   while (!s->queue.empty()) {
@@ -488,6 +507,7 @@ cfgpu_status cfgpu_server_pump(cfgpu_server s, int max_steps, int* active) {
     SCK(cfgpu_rt::advance_async(e->h, k));
     if (cudaEventRecord(e->done, cfgpu_rt::stream(e->h)) != cudaSuccess) return sfail(CFGPU_ECUDA, "event record");
     e->k = k;
+    s->chunks++;
   }
   if (active) {
     int n = (int)s->queue.size();
@@ -539,6 +559,10 @@ cfgpu_status cfgpu_server_stats(cfgpu_server s, long long* stats) {
   stats[4] = (long long)s->queue.size();
   stats[5] = s->steps_done;
   stats[6] = s->field_steps;
+  stats[7] = s->chunks;
+  stats[8] = s->dt_changes;
+  stats[9] = (long long)(s->t_admit * 1e6);
+  stats[10] = (long long)(s->t_interval * 1e6);
   return CFGPU_OK;
 }
 

@@ -251,7 +251,8 @@ cfgpu_status cfgpu_ensemble_load_slot(cfgpu_dns dns, int slot, cfgpu_dns src);
  * *active = requests queued or running.  cfgpu_server_poll: *status 0 queued, 1 running, 2 done,
  * 3 failed (returns CFGPU_ENONFINITE); u receives the result when done; times = {submit, start, done}
  * in seconds of a monotonic clock.  stats = {device bytes, ensembles, slots, running, queued,
- * ensemble steps, field steps}.  Not thread-safe: one thread drives a server.
+ * ensemble steps, field steps, chunks enqueued, dt changes, microseconds in admission, microseconds in
+ * interval ends} (11 values).  Not thread-safe: one thread drives a server.
  */
 typedef struct cfgpu_server_s* cfgpu_server;
 cfgpu_status cfgpu_server_create(long long max_bytes, int slots, int precision, cfgpu_server* out);
