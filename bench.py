@@ -46,9 +46,10 @@ NU, DT, UBULK = 1.0 / 4000.0, 0.01, 2.0 / 3.0
 WORKLOAD = ("plane Poiseuille 128x97x128 (Lx=4pi, Lz=2pi), CNAB2 + SMRK2 start-up, dt=0.01, bulk velocity "
             "Ubulk=2/3, Re_c=4000, rotational NL, 2/3 dealiasing, seeded perturbation L2=0.3")
 CNAB2, SMRK2, LaminarBase, BulkVelocity = 1, 3, 3, 1
-# DRAM bytes (read + write) per launch of the mixed-path kernels from one `ncu --set full` capture of
-# this workload (profiles/ncu_full_poiseuille_128x97x128_mixed.md); None where not captured.
-NCU_TRAFFIC = {"tau_solve": 76.130048e6 + 4.475648e6,
+# DRAM bytes (read + write) per step of the mixed-path phases from `ncu --set full` captures of this workload
+# (profiles/ncu_tau_solve_poiseuille_128x97x128_mixed.md: the three tau kernels;
+# profiles/ncu_full_poiseuille_128x97x128_mixed.md: the NL-pass kernels).
+NCU_TRAFFIC = {"tau_solve": (37.93971 + 0.697088 + 54.40486 + 0.448768 + 27.12601 + 19.968) * 1e6,
                "nonlinear_pass": (16.32896 + 16.315648 + 25.136128 + 12.600576 + 8.16384 + 0.003328) * 1e6}
 
 
