@@ -15,6 +15,7 @@
 #include <functional>
 #include <map>
 #include <mutex>
+#include <thread>
 #include <tuple>
 #include <complex>
 #include <cstdio>
@@ -1053,23 +1054,41 @@ int dns_advance_device(cfgpu_dns d, int nsteps) {
 // consecutive FlowFields (Nd components each, fields f0 .. f0+nf-1 of the
 // batch); the device side is [i][my][field][m] with nb fields (fstride = nb),
 // or one field's compact [i][my][m] (fstride = 1, f0 = 0).
+// Row-parallel loop over (field, component, y) rows: one contiguous run of Kz+1 complex values per solved kx
+// in both layouts.  Large transfers are split over host threads.
+template <typename F>
+void for_rows(size_t nrows, size_t row_bytes, const F& body) {
+  const size_t total = nrows * row_bytes;
+  unsigned nt = total > (8u << 20) ? std::min(8u, std::max(1u, std::thread::hardware_concurrency())) : 1u;
+  if (nt <= 1 || nrows < 2 * nt) {
+    for (size_t r = 0; r < nrows; ++r) body(r);
+    return;
+  }
+  std::vector<std::thread> th;
+  for (unsigned t = 0; t < nt; ++t)
+    th.emplace_back([&, t]() {
+      for (size_t r = t; r < nrows; r += nt) body(r);
+    });
+  for (auto& x : th) x.join();
+}
+
 void gather_modes(cfgpu_dns d, const double* h, int Nd, double* out, int f0 = 0, int nf = -1, int fstride = -1) {
   const GridDev& g = d->g;
   const int Mz = g.Nz / 2 + 1;
   if (nf < 0) nf = d->nb;
   if (fstride < 0) fstride = d->nb;
   const size_t hfield = (size_t)2 * Nd * g.Ny * g.Nx * Mz;
-  for (int f = 0; f < nf; ++f)
-    for (int i = 0; i < Nd; ++i)
-      for (int my = 0; my < g.Ny; ++my)
-        for (int m = 0; m < g.Md; ++m) {
-          const int kx = mode_kx(g, m), kz = mode_kz(g, m);
-          const int mx = kx >= 0 ? kx : kx + g.Nx;
-          const size_t src = f * hfield + 2 * ((((size_t)i * g.Ny + my) * g.Nx + mx) * Mz + kz);
-          const size_t dst = 2 * ((((size_t)i * g.Ny + my) * fstride + (f0 + f)) * g.Md + m);
-          out[dst] = h[src];
-          out[dst + 1] = h[src + 1];
-        }
+  const size_t nrows = (size_t)nf * Nd * g.Ny;
+  for_rows(nrows, (size_t)16 * g.Md, [&](size_t r) {
+    const int my = (int)(r % g.Ny), i = (int)((r / g.Ny) % Nd), f = (int)(r / ((size_t)g.Ny * Nd));
+    const double* src = h + f * hfield + 2 * (((size_t)i * g.Ny + my) * g.Nx) * Mz;
+    double* dst = out + 2 * ((((size_t)i * g.Ny + my) * fstride + (f0 + f)) * g.Md);
+    for (int ix = 0; ix < g.NKx; ++ix) {
+      const int kx = ix <= g.Kx ? ix : ix - g.NKx;
+      const int mx = kx >= 0 ? kx : kx + g.Nx;
+      memcpy(dst + 2 * (size_t)ix * g.NKz, src + 2 * (size_t)mx * Mz, 16 * (size_t)g.NKz);
+    }
+  });
 }
 void scatter_modes(cfgpu_dns d, const double* in, int Nd, double* h, int f0 = 0, int nf = -1, int fstride = -1) {
   const GridDev& g = d->g;
@@ -1077,17 +1096,17 @@ void scatter_modes(cfgpu_dns d, const double* in, int Nd, double* h, int f0 = 0,
   if (nf < 0) nf = d->nb;
   if (fstride < 0) fstride = d->nb;
   const size_t hfield = (size_t)2 * Nd * g.Ny * g.Nx * Mz;
-  for (int f = 0; f < nf; ++f)
-    for (int i = 0; i < Nd; ++i)
-      for (int my = 0; my < g.Ny; ++my)
-        for (int m = 0; m < g.Md; ++m) {
-          const int kx = mode_kx(g, m), kz = mode_kz(g, m);
-          const int mx = kx >= 0 ? kx : kx + g.Nx;
-          const size_t dst = f * hfield + 2 * ((((size_t)i * g.Ny + my) * g.Nx + mx) * Mz + kz);
-          const size_t src = 2 * ((((size_t)i * g.Ny + my) * fstride + (f0 + f)) * g.Md + m);
-          h[dst] = in[src];
-          h[dst + 1] = in[src + 1];
-        }
+  const size_t nrows = (size_t)nf * Nd * g.Ny;
+  for_rows(nrows, (size_t)16 * g.Md, [&](size_t r) {
+    const int my = (int)(r % g.Ny), i = (int)((r / g.Ny) % Nd), f = (int)(r / ((size_t)g.Ny * Nd));
+    double* dst = h + f * hfield + 2 * (((size_t)i * g.Ny + my) * g.Nx) * Mz;
+    const double* src = in + 2 * ((((size_t)i * g.Ny + my) * fstride + (f0 + f)) * g.Md);
+    for (int ix = 0; ix < g.NKx; ++ix) {
+      const int kx = ix <= g.Kx ? ix : ix - g.NKx;
+      const int mx = kx >= 0 ? kx : kx + g.Nx;
+      memcpy(dst + 2 * (size_t)mx * Mz, src + 2 * (size_t)ix * g.NKz, 16 * (size_t)g.NKz);
+    }
+  });
 }
 
 int set_fields(cfgpu_dns d, const double* u, const double* q) {
