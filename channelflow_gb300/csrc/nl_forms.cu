@@ -39,14 +39,17 @@ __global__ void __launch_bounds__(256) k_grad_cheb(GridDev g, int N, const doubl
   const int nlines = 2 * g.Md;
   const int l0 = blockIdx.x * GC_TL;
   const size_t row = (size_t)nlines, comp = row * N;
+#pragma unroll 8
   for (int i = tid; i < P * KA; i += blockDim.x) {
     sCA[i] = CA[i];
     if (MODE == 1) sDA[i] = DA[i];
   }
+#pragma unroll 8
   for (int i = tid; i < P * KB; i += blockDim.x) {
     sCB[i] = CB[i];
     if (MODE == 1) sDB[i] = DB[i];
   }
+#pragma unroll 4
   for (int i = tid; i < 3 * N * GC_TL; i += blockDim.x) {
     const int l = i % GC_TL, n = (i / GC_TL) % N, c = i / (GC_TL * N);
     const int gl = l0 + l;
@@ -223,6 +226,7 @@ __global__ void __launch_bounds__(256) k_zphys(GridDev g, FftPlan pz, const cpx<
   const size_t plane = (size_t)g.Nx * NKz;
   for (int i = tid; i < ninv * ss; i += nthr) A[i] = cmk<R>(0, 0);
   __syncthreads();
+#pragma unroll 4
   for (int i = tid; i < ninv * NKz; i += nthr) {
     const int iz = i % NKz, s = i / NKz;
     const int k0 = 2 * s, k1 = 2 * s + 1;
@@ -259,6 +263,7 @@ __global__ void __launch_bounds__(256) k_zphys(GridDev g, FftPlan pz, const cpx<
   }
   __syncthreads();
   fft_batch<R>(B, A, nfwd, ss, pz, twz, -1);
+#pragma unroll 4
   for (int i = tid; i < nfwd * NKz; i += nthr) {
     const int iz = i % NKz, s = i / NKz;
     const cpx<R>* sq = B + (size_t)s * ss;
@@ -301,15 +306,18 @@ __global__ void __launch_bounds__(256) k_cheb_fwd_div(GridDev g, int N, const R*
   const int nlines = 2 * g.Md;
   const int l0 = blockIdx.x * CF_TL;
   const size_t row = (size_t)nlines;
+#pragma unroll 8
   for (int i = tid; i < P * KA; i += blockDim.x) {
     sFA[i] = FA[i];
     sDB[i] = DFB[i];
   }
+#pragma unroll 8
   for (int i = tid; i < P * KB; i += blockDim.x) {
     sFB[i] = FB[i];
     sDA[i] = DFA[i];
   }
   const R* ins[4] = {pF, pKx, pKz, pD};
+#pragma unroll 4
   for (int i = tid; i < 4 * KA * CF_TL; i += blockDim.x) {
     const int l = i % CF_TL, j = (i / CF_TL) % KA, c = i / (CF_TL * KA);
     const int gl = l0 + l;

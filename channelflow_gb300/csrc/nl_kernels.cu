@@ -106,9 +106,12 @@ __global__ void __launch_bounds__(256) k_cheb(int N, int inverse, int nlines, co
   in += c * cs_in;
   out += c * cs_out;
   const int J = (N - 1) / 2;
+#pragma unroll 8
   for (int i = tid; i < P * KA; i += blockDim.x) As[i] = Amat[i];
+#pragma unroll 8
   for (int i = tid; i < P * KB; i += blockDim.x) Bs[i] = Bmat[i];
   // stage inputs
+#pragma unroll 4
   for (int i = tid; i < N * CHEB_TL; i += blockDim.x) {
     const int n = i / CHEB_TL, l = i % CHEB_TL;
     const int gl = l0 + l;
@@ -211,14 +214,17 @@ __global__ void __launch_bounds__(256) k_curl_cheb(GridDev g, int N, const doubl
   const int nlines = 2 * g.Md;
   const int l0 = blockIdx.x * CC_TL;
   const size_t row = (size_t)nlines, comp = row * N;
+#pragma unroll 8
   for (int i = tid; i < P * KA; i += blockDim.x) {
     sCA[i] = CA[i];
     sDA[i] = DA[i];
   }
+#pragma unroll 8
   for (int i = tid; i < P * KB; i += blockDim.x) {
     sCB[i] = CB[i];
     sDB[i] = DB[i];
   }
+#pragma unroll 4
   for (int i = tid; i < 3 * N * CC_TL; i += blockDim.x) {
     const int l = i % CC_TL, n = (i / CC_TL) % N, c = i / (CC_TL * N);
     const int gl = l0 + l;
@@ -359,6 +365,7 @@ __global__ void __launch_bounds__(256) k_xinv(GridDev g, FftPlan px, const cpx<R
   const cpx<R>* src = W + ((size_t)c * g.Ny + ny) * g.Md;
   for (int i = tid; i < nc * ss; i += nthr) a[i] = cmk<R>(0, 0);
   __syncthreads();
+#pragma unroll 4
   for (int i = tid; i < g.NKx * nc; i += nthr) {
     const int ix = i / nc, jz = i - ix * nc;
     const int kx = ix <= g.Kx ? ix : ix - g.NKx;
@@ -395,6 +402,7 @@ __global__ void __launch_bounds__(256) k_zcross(GridDev g, FftPlan pz, const cpx
   for (int i = tid; i < ninv * ss; i += nthr) A[i] = cmk<R>(0, 0);
   __syncthreads();
   // pack: sequence (r, p) = comps (2p, 2p+1) of row x0+r
+#pragma unroll 4
   for (int i = tid; i < RP * 3 * NKz; i += nthr) {
     const int iz = i % NKz;
     const int rp = i / NKz;
@@ -439,6 +447,7 @@ __global__ void __launch_bounds__(256) k_zcross(GridDev g, FftPlan pz, const cpx
   __syncthreads();
   fft_batch<R>(B, A, 3 * npair, ss, pz, twz, -1);
   // unpack P_k = (Z_k + conj(Z_-k))/2, Q_k = (Z_k - conj(Z_-k))/(2i)
+#pragma unroll 4
   for (int i = tid; i < npair * 3 * NKz; i += nthr) {
     const int iz = i % NKz;
     const int t = i / NKz;
@@ -475,6 +484,7 @@ __global__ void __launch_bounds__(256) k_xfwd(GridDev g, FftPlan px, const cpx<R
   const int ny = blockIdx.x, c = blockIdx.y;
   const int tid = threadIdx.x, nthr = blockDim.x;
   const cpx<R>* src = Z + ((size_t)c * g.Ny + ny) * (size_t)g.Nx * g.NKz;
+#pragma unroll 4
   for (int i = tid; i < g.Nx * nc; i += nthr) {
     const int x = i / nc, jz = i - x * nc;
     a[jz * ss + x] = src[x * g.NKz + iz0 + jz];
@@ -482,6 +492,7 @@ __global__ void __launch_bounds__(256) k_xfwd(GridDev g, FftPlan px, const cpx<R
   __syncthreads();
   fft_batch<R>(a, b, nc, ss, px, twx, -1);
   cpx<R>* dst = F + ((size_t)c * g.Ny + ny) * g.Md;
+#pragma unroll 4
   for (int i = tid; i < g.NKx * nc; i += nthr) {
     const int ix = i / nc, jz = i - ix * nc;
     const int kx = ix <= g.Kx ? ix : ix - g.NKx;
