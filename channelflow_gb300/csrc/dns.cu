@@ -522,6 +522,7 @@ struct cfgpu_dns_s {
   void* zbasey = nullptr;  // zero base profiles [nb][4N] (LinearAboutProfile: u, v, w without base flow)
   double* dyc = nullptr;           // CFL grid spacing in y per Gauss-Lobatto point
   unsigned long long* dred = nullptr;  // reduction scratch (CFL key, L2 sum)
+  unsigned long long* cfl_host = nullptr;  // pinned copy of the CFL keys (asynchronous CFL passes)
   int alt[2] = {0, 0};  // Alternating state of the main (0) and init (1) NSE: 0 = next is divergence
   // state: current fields
   double *Ucur = nullptr, *Qcur = nullptr;
@@ -1510,6 +1511,7 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
   if (d->has_init) CKS(build_tables(d, d->init));
   d->stage_elems = 4 * cd;
   CK(cudaMallocHost((void**)&d->stage, d->stage_elems * sizeof(double)));
+  CK(cudaMallocHost((void**)&d->cfl_host, (size_t)nb * sizeof(unsigned long long)));
   CK(cudaStreamSynchronize(d->st));
   return CFGPU_OK;
 }
@@ -1532,6 +1534,7 @@ void dns_free(cfgpu_dns d) {
   for (Scheme* s : {&d->main, &d->init})
     for (auto& t : s->tau) { F(t.f); F(t.s); }
   if (d->stage) cudaFreeHost(d->stage);
+  if (d->cfl_host) cudaFreeHost(d->cfl_host);
   for (auto& e : d->ev_pool) cudaEventDestroy(e);
   for (auto& u : d->ev_used) {
     cudaEventDestroy(u.second.first);
@@ -1545,9 +1548,10 @@ void dns_free(cfgpu_dns d) {
 }  // namespace
 
 namespace {
-// DNSAlgorithm::CFL of every field of the batch into cfl[0 .. nb).
+// DNSAlgorithm::CFL of every field of the batch: the pass is enqueued on the DNS's stream and its CFL keys
+// copied to pinned host memory (cfl_enqueue); cfl_finish converts them once the stream has reached that point.
 template <typename R>
-int cfl_impl(cfgpu_dns d, double* cfl) {
+int cfl_enqueue(cfgpu_dns d) {
   const GridDev& g = d->gm;
   if ((d->N + 1) / 2 > 56) return fail(CFGPU_ENOTSUP, "CFL needs Ny <= 111");
   R* W = (R*)d->W6;
@@ -1559,14 +1563,23 @@ int cfl_impl(cfgpu_dns d, double* cfl) {
   CK(launch_zcfl<R>(d->gp, d->pz, (const cpx<R>*)d->twz, d->RP, (const cpx<R>*)d->X6, d->dyc, g.Lx / g.Nx,
                     g.Lz / g.Nz, d->nb, d->dred, d->st));
   d->launches += 3;
-  std::vector<unsigned long long> key(d->nb);
-  CK(cudaMemcpyAsync(key.data(), d->dred, d->nb * sizeof(unsigned long long), cudaMemcpyDeviceToHost, d->st));
-  CK(cudaStreamSynchronize(d->st));
+  CK(cudaMemcpyAsync(d->cfl_host, d->dred, d->nb * sizeof(unsigned long long), cudaMemcpyDeviceToHost, d->st));
+  return CFGPU_OK;
+}
+
+void cfl_finish(cfgpu_dns d, double* cfl) {
   const bool dxz = d->fl.dealiasing == CFGPU_DealiasXZ || d->fl.dealiasing == CFGPU_DealiasXYZ;
   for (int f = 0; f < d->nb; ++f) {
     const double dt = d->hetero ? d->sfl[f].dt : d->fl.dt;
-    cfl[f] = cfl_key_to_double(key[f]) * (dxz ? 2.0 * M_PI / 3.0 * dt : M_PI * dt);
+    cfl[f] = cfl_key_to_double(d->cfl_host[f]) * (dxz ? 2.0 * M_PI / 3.0 * dt : M_PI * dt);
   }
+}
+
+template <typename R>
+int cfl_impl(cfgpu_dns d, double* cfl) {
+  CKS(cfl_enqueue<R>(d));
+  CK(cudaStreamSynchronize(d->st));
+  cfl_finish(d, cfl);
   return CFGPU_OK;
 }
 
@@ -1590,6 +1603,20 @@ int l2norm_impl(cfgpu_dns d, int field, double* l2) {
 // ---------------------------------------------------------------------------
 // Runtime hooks used by the request server (server.cu); not part of the C ABI.
 namespace cfgpu_rt {
+// CFL pass enqueued on the DNS's stream (results readable with cfl_collect once the stream passed it).
+int cfl_async(cfgpu_dns d) { return d->precision == CFGPU_FP64 ? cfl_enqueue<double>(d) : cfl_enqueue<float>(d); }
+void cfl_collect(cfgpu_dns d, double* out) { cfl_finish(d, out); }
+
+// Recreate the DNS's stream with a scheduling priority (cudaDeviceGetStreamPriorityRange).
+int set_priority(cfgpu_dns d, int prio) {
+  CK(cudaStreamSynchronize(d->st));
+  cudaStream_t ns = nullptr;
+  CK(cudaStreamCreateWithPriority(&ns, cudaStreamNonBlocking, prio));
+  cudaStreamDestroy(d->st);
+  d->st = ns;
+  return CFGPU_OK;
+}
+
 int advance_async(cfgpu_dns d, int nsteps) { return dns_advance_device(d, nsteps); }
 cudaStream_t stream(cfgpu_dns d) { return d->st; }
 long long bytes(cfgpu_dns d) { return d->bytes; }

@@ -48,6 +48,9 @@ long long bytes(cfgpu_dns d);
 int startup_steps(cfgpu_dns d);
 int restart(cfgpu_dns d);
 int store_slot(cfgpu_dns d, int slot, cfgpu_dns dst);
+int cfl_async(cfgpu_dns d);
+void cfl_collect(cfgpu_dns d, double* out);
+int set_priority(cfgpu_dns d, int prio);
 long long estimate_bytes(const cfgpu_grid& grid, const cfgpu_flags& f, int nb, int precision);
 }  // namespace cfgpu_rt
 
@@ -112,6 +115,7 @@ struct Ens {
   std::vector<long long> slot_req;  // request id per slot, -1 free
   long long bytes = 0;
   int k = 0;                        // steps of the chunk in flight (0: idle)
+  bool cfl_pending = false;         // the chunk ends with a CFL pass (some field reaches an interval end)
   cudaEvent_t done = nullptr;       // recorded after the chunk in flight
   int running() const {
     int n = 0;
@@ -144,6 +148,9 @@ int make_staging(cfgpu_server_s* s, Request& r, cfgpu_dns* out) {
     cfgpu_dns h = nullptr;
     SCK(cfgpu_ensemble_create(&r.grid, &r.flags, 1, s->precision, &h));
     s->used += cfgpu_rt::bytes(h);
+    // staging work is waited for by the host: schedule it ahead of the ensembles' queued steps
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) == cudaSuccess) SCK(cfgpu_rt::set_priority(h, greatest));
     it = s->staging.emplace(r.key, h).first;
   }
   *out = it->second;
@@ -307,6 +314,8 @@ int complete_chunk(cfgpu_server_s* s, Ens* e, bool wait, bool* completed) {
       boundary |= r.left == 0;
     }
   e->k = 0;
+  const bool pending = e->cfl_pending;
+  e->cfl_pending = false;
   if (!boundary) return CFGPU_OK;
   const double t0 = now_s();
   struct Acc {
@@ -315,7 +324,11 @@ int complete_chunk(cfgpu_server_s* s, Ens* e, bool wait, bool* completed) {
     ~Acc() { s->t_interval += now_s() - t0; }
   } acc{s, t0};
   std::vector<double> cfl_now(e->slot_req.size(), 0.0);
-  if (cfgpu_ensemble_cfl(e->h, cfl_now.data()) != CFGPU_OK) return sfail(CFGPU_ECUDA, cfgpu_last_error());
+  if (pending) {
+    cfgpu_rt::cfl_collect(e->h, cfl_now.data());  // the CFL pass ran at the end of the chunk
+  } else if (cfgpu_ensemble_cfl(e->h, cfl_now.data()) != CFGPU_OK) {
+    return sfail(CFGPU_ECUDA, cfgpu_last_error());
+  }
   for (int i = 0; i < (int)e->slot_req.size(); ++i)
     if (e->slot_req[i] >= 0 && s->reqs[e->slot_req[i]]->left == 0) SCK(interval_end(s, e, i, cfl_now));
   return CFGPU_OK;
@@ -505,6 +518,13 @@ cfgpu_status cfgpu_server_pump(cfgpu_server s, int max_steps, int* active) {
     for (long long id : e->slot_req)
       if (id >= 0) k = std::min(k, s->reqs[id]->left);
     SCK(cfgpu_rt::advance_async(e->h, k));
+    bool boundary = false;
+    for (long long id : e->slot_req)
+      if (id >= 0 && s->reqs[id]->left == k) boundary = true;
+    if (boundary) {
+      SCK(cfgpu_rt::cfl_async(e->h));  // CFL numbers at the interval end, read when the chunk completes
+      e->cfl_pending = true;
+    }
     if (cudaEventRecord(e->done, cfgpu_rt::stream(e->h)) != cudaSuccess) return sfail(CFGPU_ECUDA, "event record");
     e->k = k;
     s->chunks++;
