@@ -346,7 +346,9 @@ def run_serve(args):
             "median_rel_l2_vs_alone_fp64": float(np.median(errs)) if errs else None, "failed": failed,
             "ensembles": stats["ensembles"], "ensemble_steps": stats["ensemble_steps"],
             "field_steps": stats["field_steps"], "chunks": stats["chunks"], "dt_changes": stats["dt_changes"],
-            "host_s_admission": stats["admit_us"] / 1e6, "host_s_interval_ends": stats["interval_us"] / 1e6})
+            "host_s_admission": stats["admit_us"] / 1e6, "host_s_interval_ends": stats["interval_us"] / 1e6,
+            "host_s_create": stats["create_us"] / 1e6, "host_s_params": stats["params_us"] / 1e6,
+            "host_s_stage": stats["stage_us"] / 1e6, "host_s_load": stats["load_us"] / 1e6})
     out.update(precision=args.serve_precision, slots=args.serve_slots, pump_steps=args.serve_pump_steps,
                workload="f^T(u) requests: Nx,Nz in {32,48,64,96}, Ny in {33,49,65}, Re U[300,2000], Couette or "
                         "Poiseuille, T U[5,50], CFL-adapted TimeStep from dt=0.02 (dT=1, CFL 0.4-0.6), SBDF3 + "

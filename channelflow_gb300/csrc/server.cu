@@ -138,7 +138,18 @@ struct cfgpu_server_s {
   // host-side accounting: seconds in admission (staging), in interval ends (CFL pass, dt changes), chunks
   double t_admit = 0, t_interval = 0;
   long long chunks = 0, dt_changes = 0;
+  // finer host-time breakdown (seconds): ensemble/staging creation, set_params, staging runs, slot loads
+  double t_create = 0, t_params = 0, t_stage = 0, t_load = 0;
 };
+
+namespace {
+struct Timer {
+  double& acc;
+  double t0;
+  explicit Timer(double& a) : acc(a), t0(now_s()) {}
+  ~Timer() { acc += now_s() - t0; }
+};
+}  // namespace
 
 namespace {
 
@@ -146,6 +157,7 @@ int make_staging(cfgpu_server_s* s, Request& r, cfgpu_dns* out) {
   auto it = s->staging.find(r.key);
   if (it == s->staging.end()) {
     cfgpu_dns h = nullptr;
+    Timer tm(s->t_create);
     SCK(cfgpu_ensemble_create(&r.grid, &r.flags, 1, s->precision, &h));
     s->used += cfgpu_rt::bytes(h);
     // staging work is waited for by the host: schedule it ahead of the ensembles' queued steps
@@ -180,7 +192,8 @@ double slot_cfl(cfgpu_dns h, int slot, int nb) {
 }
 
 // Give the staging DNS the request's flags at its current dt and restart its start-up steps.
-int stage_restart(cfgpu_dns st, Request& r) {
+int stage_restart(cfgpu_server_s* s, cfgpu_dns st, Request& r) {
+  Timer tm(s->t_params);
   if (!r.fixed) r.flags.dt = r.ts.value();
   SCK(cfgpu_rt::restart(st));  // first: the start-up tables are then rebuilt with the request's parameters
   return cfgpu_ensemble_set_params(st, 0, &r.flags, nullptr, nullptr);
@@ -196,6 +209,7 @@ int advance_sync(cfgpu_dns h, int n) {
 // until it is past its start-up steps with steps left in the interval (returns with *done = false) or
 // finished (*done = true).  Interval ends inside the start-up phase are handled here as in cfDSI::f.
 int stage_run(cfgpu_server_s* s, Request& r, cfgpu_dns st, bool* finished) {
+  Timer tm(s->t_stage);
   *finished = false;
   for (;;) {
     r.cfl_start = r.cfl = slot_cfl(st, 0, 1);
@@ -211,7 +225,7 @@ int stage_run(cfgpu_server_s* s, Request& r, cfgpu_dns st, bool* finished) {
       *finished = true;
       return CFGPU_OK;
     }
-    if (r.ts.variable && r.ts.adjust(r.cfl_start)) SCK(stage_restart(st, r));
+    if (r.ts.variable && r.ts.adjust(r.cfl_start)) SCK(stage_restart(s, st, r));
     r.interval++;
   }
 }
@@ -221,7 +235,7 @@ int stage_run(cfgpu_server_s* s, Request& r, cfgpu_dns st, bool* finished) {
 int start_request(cfgpu_server_s* s, Request& r, Ens* e, int slot) {
   cfgpu_dns st = nullptr;
   SCK(make_staging(s, r, &st));
-  SCK(stage_restart(st, r));
+  SCK(stage_restart(s, st, r));
   SCK(cfgpu_ensemble_set_field(st, 0, r.u.data(), r.q.data()));
   r.t_start = now_s();
   r.status = ST_RUNNING;
@@ -229,7 +243,7 @@ int start_request(cfgpu_server_s* s, Request& r, Ens* e, int slot) {
     // cfDSI::f: one step to measure the CFL number, adjust, reset_dt, restart from u (q kept)
     SCK(advance_sync(st, 1));
     r.ts.adjust(slot_cfl(st, 0, 1));
-    SCK(stage_restart(st, r));
+    SCK(stage_restart(s, st, r));
     SCK(cfgpu_ensemble_set_field(st, 0, r.u.data(), nullptr));
   }
   r.interval = 1;
@@ -242,8 +256,11 @@ int start_request(cfgpu_server_s* s, Request& r, Ens* e, int slot) {
     // the completed chunk's bookkeeping did not free this slot; find another one (cannot happen: slot was free)
     return sfail(CFGPU_EINVAL, "slot taken");
   }
-  SCK(cfgpu_ensemble_set_params(e->h, slot, &r.flags, nullptr, nullptr));
-  SCK(cfgpu_ensemble_load_slot(e->h, slot, st));
+  {
+    Timer tm(s->t_load);
+    SCK(cfgpu_ensemble_set_params(e->h, slot, &r.flags, nullptr, nullptr));
+    SCK(cfgpu_ensemble_load_slot(e->h, slot, st));
+  }
   e->slot_req[slot] = r.id;
   r.ens = -1;
   for (size_t i = 0; i < s->ens.size(); ++i)
@@ -266,7 +283,7 @@ int interval_end(cfgpu_server_s* s, Ens* e, int i, const std::vector<double>& cf
     s->dt_changes++;
     cfgpu_dns st = nullptr;
     SCK(make_staging(s, r, &st));
-    SCK(stage_restart(st, r));
+    SCK(stage_restart(s, st, r));
     SCK(cfgpu_rt::store_slot(e->h, i, st));
     r.interval++;
     bool finished = false;
@@ -276,6 +293,7 @@ int interval_end(cfgpu_server_s* s, Ens* e, int i, const std::vector<double>& cf
       e->slot_req[i] = -1;
       return CFGPU_OK;
     }
+    Timer tm(s->t_load);
     SCK(cfgpu_ensemble_set_params(e->h, i, &r.flags, nullptr, nullptr));
     return cfgpu_ensemble_load_slot(e->h, i, st);
   }
@@ -395,7 +413,11 @@ int admit_impl(cfgpu_server_s* s) {
       }
       auto ne = std::make_unique<Ens>();
       ne->key = r.key;
-      int st = cfgpu_ensemble_create(&r.grid, &r.flags, want, s->precision, &ne->h);
+      int st;
+      {
+        Timer tm(s->t_create);
+        st = cfgpu_ensemble_create(&r.grid, &r.flags, want, s->precision, &ne->h);
+      }
       if (st != CFGPU_OK) {
         r.status = ST_FAILED;
         r.err = cfgpu_last_error();
@@ -583,6 +605,10 @@ cfgpu_status cfgpu_server_stats(cfgpu_server s, long long* stats) {
   stats[8] = s->dt_changes;
   stats[9] = (long long)(s->t_admit * 1e6);
   stats[10] = (long long)(s->t_interval * 1e6);
+  stats[11] = (long long)(s->t_create * 1e6);
+  stats[12] = (long long)(s->t_params * 1e6);
+  stats[13] = (long long)(s->t_stage * 1e6);
+  stats[14] = (long long)(s->t_load * 1e6);
   return CFGPU_OK;
 }
 

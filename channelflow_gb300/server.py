@@ -68,10 +68,10 @@ class Server:
         self._shapes.pop(rid, None)
 
     def stats(self) -> dict:
-        v = (C.c_longlong * 11)()
+        v = (C.c_longlong * 15)()
         L.check(self._lib.cfgpu_server_stats(self._h, v))
         keys = ("device_bytes", "ensembles", "slots", "running", "queued", "ensemble_steps", "field_steps", "chunks",
-                "dt_changes", "admit_us", "interval_us")
+                "dt_changes", "admit_us", "interval_us", "create_us", "params_us", "stage_us", "load_us")
         return dict(zip(keys, list(v)))
 
     def run(self, max_steps: int = 50):

@@ -252,7 +252,8 @@ cfgpu_status cfgpu_ensemble_load_slot(cfgpu_dns dns, int slot, cfgpu_dns src);
  * 3 failed (returns CFGPU_ENONFINITE); u receives the result when done; times = {submit, start, done}
  * in seconds of a monotonic clock.  stats = {device bytes, ensembles, slots, running, queued,
  * ensemble steps, field steps, chunks enqueued, dt changes, microseconds in admission, microseconds in
- * interval ends} (11 values).  Not thread-safe: one thread drives a server.
+ * interval ends, microseconds creating ensembles, setting staging parameters, running staging steps,
+ * loading slots} (15 values).  Not thread-safe: one thread drives a server.
  */
 typedef struct cfgpu_server_s* cfgpu_server;
 cfgpu_status cfgpu_server_create(long long max_bytes, int slots, int precision, cfgpu_server* out);
