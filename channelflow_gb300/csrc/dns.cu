@@ -299,12 +299,44 @@ void make_helm_b(int N, std::vector<double>& lo, std::vector<double>& di, std::v
 }
 
 template <typename T>
+int dalloc(T** p, size_t n, long long& bytes);
+
+// Device memory comes from the device's stream-ordered pool, which keeps freed memory reserved, so that DNS
+// objects created and destroyed at serving rates allocate in microseconds.  Allocations and frees are issued
+// on one internal stream per device; an allocation is complete when dalloc returns.
+cudaStream_t pool_stream() {
+  static std::mutex mu;
+  static std::map<int, cudaStream_t> streams;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = streams.find(dev);
+  if (it != streams.end()) return it->second;
+  cudaStream_t st = nullptr;
+  cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    unsigned long long keep = ~0ull;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  streams[dev] = st;
+  return st;
+}
+
+template <typename T>
 int dalloc(T** p, size_t n, long long& bytes) {
   if (n == 0) n = 1;
-  cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
-  if (e != cudaSuccess) return fail(CFGPU_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  cudaStream_t ps = pool_stream();
+  cudaError_t e = cudaMallocAsync((void**)p, n * sizeof(T), ps);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ps);
+  if (e != cudaSuccess) return fail(CFGPU_ENOMEM, std::string("cudaMallocAsync: ") + cudaGetErrorString(e));
   bytes += (long long)(n * sizeof(T));
   return CFGPU_OK;
+}
+
+// Back to the pool; the caller has synchronized every stream that used p.
+void dfree(void* p) {
+  if (p) cudaFreeAsync(p, pool_stream());
 }
 
 }  // namespace
@@ -603,9 +635,10 @@ struct PhaseScope {
 int build_tables(cfgpu_dns d, Scheme& s) {
   const size_t FN = (size_t)d->N * d->gm.Md;
   HelmB hb{d->hb_lo, d->hb_di, d->hb_up};
+  if (!s.tau.empty()) CK(cudaStreamSynchronize(d->st));  // no queued step still reads the old tables
   for (auto& t : s.tau) {
-    cudaFree(t.f);
-    cudaFree(t.s);
+    dfree(t.f);
+    dfree(t.s);
   }
   s.tau.clear();
   const int nt = (int)s.lambda_t.size();
@@ -1110,7 +1143,13 @@ void scatter_modes(cfgpu_dns d, const double* in, int Nd, double* h, int f0 = 0,
   });
 }
 
+int ensure_stage(cfgpu_dns d) {
+  if (!d->stage) CK(cudaMallocHost((void**)&d->stage, d->stage_elems * sizeof(double)));
+  return CFGPU_OK;
+}
+
 int set_fields(cfgpu_dns d, const double* u, const double* q) {
+  CKS(ensure_stage(d));
   const size_t cd = d->compc();
   if (u) {
     gather_modes(d, u, 3, d->stage);
@@ -1124,6 +1163,7 @@ int set_fields(cfgpu_dns d, const double* u, const double* q) {
 }
 
 int get_fields(cfgpu_dns d, double* u, double* q) {
+  CKS(ensure_stage(d));
   const size_t cd = d->compc();
   CK(cudaMemcpyAsync(d->stage, d->Ucur, 3 * cd * sizeof(double), cudaMemcpyDeviceToHost, d->st));
   CK(cudaMemcpyAsync(d->stage + 3 * cd, d->Qcur, cd * sizeof(double), cudaMemcpyDeviceToHost, d->st));
@@ -1135,6 +1175,7 @@ int get_fields(cfgpu_dns d, double* u, double* q) {
 
 // One field (slot) of a batch: the rows [c][ny] of that field are strided by nb*Md modes on the device.
 int set_slot(cfgpu_dns d, int slot, const double* u, const double* q) {
+  CKS(ensure_stage(d));
   const size_t w = 2 * (size_t)d->g.Md, pitch = w * d->nb, cd1 = w * d->N;
   if (u) {
     gather_modes(d, u, 3, d->stage, 0, 1, 1);
@@ -1151,6 +1192,7 @@ int set_slot(cfgpu_dns d, int slot, const double* u, const double* q) {
 }
 
 int get_slot(cfgpu_dns d, int slot, double* u, double* q) {
+  CKS(ensure_stage(d));
   const size_t w = 2 * (size_t)d->g.Md, pitch = w * d->nb, cd1 = w * d->N;
   CK(cudaMemcpy2DAsync(d->stage, w * sizeof(double), d->Ucur + slot * w, pitch * sizeof(double),
                        w * sizeof(double), 3 * (size_t)d->N, cudaMemcpyDeviceToHost, d->st));
@@ -1509,8 +1551,7 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
   if (d->has_init) CKS(alloc_scheme(d->init, 1));
   CKS(build_tables(d, d->main));
   if (d->has_init) CKS(build_tables(d, d->init));
-  d->stage_elems = 4 * cd;
-  CK(cudaMallocHost((void**)&d->stage, d->stage_elems * sizeof(double)));
+  d->stage_elems = 4 * cd;  // pinned host staging, allocated on first host transfer (ensure_stage)
   CK(cudaMallocHost((void**)&d->cfl_host, (size_t)nb * sizeof(unsigned long long)));
   CK(cudaStreamSynchronize(d->st));
   return CFGPU_OK;
@@ -1518,9 +1559,8 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
 
 void dns_free(cfgpu_dns d) {
   if (!d) return;
-  auto F = [](void* p) {
-    if (p) cudaFree(p);
-  };
+  if (d->st) cudaStreamSynchronize(d->st);
+  auto F = [](void* p) { dfree(p); };
   F(d->dUbase); F(d->dWbase); F(d->dUbaseyy); F(d->dWbaseyy); F(d->ddPdx);
   F(d->hb_lo); F(d->hb_di); F(d->hb_up);
   F(d->twx); F(d->twz); F(d->cinvA); F(d->cinvB); F(d->cfwdA); F(d->cfwdB);
@@ -1606,6 +1646,13 @@ namespace cfgpu_rt {
 // CFL pass enqueued on the DNS's stream (results readable with cfl_collect once the stream passed it).
 int cfl_async(cfgpu_dns d) { return d->precision == CFGPU_FP64 ? cfl_enqueue<double>(d) : cfl_enqueue<float>(d); }
 void cfl_collect(cfgpu_dns d, double* out) { cfl_finish(d, out); }
+
+// Issue the DNS's work on another stream (the caller has synchronized the current one); returns the old stream.
+cudaStream_t swap_stream(cfgpu_dns d, cudaStream_t s) {
+  cudaStream_t old = d->st;
+  d->st = s;
+  return old;
+}
 
 // Recreate the DNS's stream with a scheduling priority (cudaDeviceGetStreamPriorityRange).
 int set_priority(cfgpu_dns d, int prio) {
@@ -2288,9 +2335,10 @@ cfgpu_status cfgpu_tau_solve_batched(int N, int nmodes, const int* kx, const int
     return CFGPU_OK;
   };
   status = body();
+  if (st) cudaStreamSynchronize(st);
   for (void* p : {(void*)dkx, (void*)dkz, (void*)R3, (void*)U3, (void*)Q1, (void*)scr, (void*)zero, (void*)hlo,
                   (void*)hdi, (void*)hup, (void*)t.f, (void*)t.s})
-    if (p) cudaFree(p);
+    dfree(p);
   if (st) cudaStreamDestroy(st);
   return status;
 }

@@ -51,6 +51,7 @@ int store_slot(cfgpu_dns d, int slot, cfgpu_dns dst);
 int cfl_async(cfgpu_dns d);
 void cfl_collect(cfgpu_dns d, double* out);
 int set_priority(cfgpu_dns d, int prio);
+cudaStream_t swap_stream(cfgpu_dns d, cudaStream_t s);
 long long estimate_bytes(const cfgpu_grid& grid, const cfgpu_flags& f, int nb, int precision);
 }  // namespace cfgpu_rt
 
@@ -127,6 +128,7 @@ struct Ens {
 }  // namespace
 
 struct cfgpu_server_s {
+  cudaStream_t ctrl = nullptr;  // high-priority stream for control work on idle ensembles
   long long max_bytes = 0, used = 0;
   int slots = 8, precision = CFGPU_FP64;
   long long next_id = 1;
@@ -169,8 +171,21 @@ int make_staging(cfgpu_server_s* s, Request& r, cfgpu_dns* out) {
   return CFGPU_OK;
 }
 
+// Control work on an idle ensemble (slot copies, parameter uploads, table builds, reads) goes through the
+// server's high-priority stream, ahead of the other ensembles' queued steps.
+template <typename F>
+int on_ctrl(cfgpu_server_s* s, cfgpu_dns h, const F& f) {
+  if (!s->ctrl) return f();
+  if (cudaStreamSynchronize(cfgpu_rt::stream(h)) != cudaSuccess) return sfail(CFGPU_ECUDA, "stream sync");
+  cudaStream_t old = cfgpu_rt::swap_stream(h, s->ctrl);
+  const int st = f();
+  cudaStreamSynchronize(s->ctrl);
+  cfgpu_rt::swap_stream(h, old);
+  return st;
+}
+
 int finish(cfgpu_server_s* s, Request& r, cfgpu_dns h, int slot) {
-  SCK(cfgpu_ensemble_get_field(h, slot, r.u.data(), r.q.data()));
+  SCK(on_ctrl(s, h, [&]() { return cfgpu_ensemble_get_field(h, slot, r.u.data(), r.q.data()); }));
   for (double v : r.u)
     if (!std::isfinite(v)) {
       r.status = ST_FAILED;
@@ -258,8 +273,10 @@ int start_request(cfgpu_server_s* s, Request& r, Ens* e, int slot) {
   }
   {
     Timer tm(s->t_load);
-    SCK(cfgpu_ensemble_set_params(e->h, slot, &r.flags, nullptr, nullptr));
-    SCK(cfgpu_ensemble_load_slot(e->h, slot, st));
+    SCK(on_ctrl(s, e->h, [&]() {
+      SCK(cfgpu_ensemble_set_params(e->h, slot, &r.flags, nullptr, nullptr));
+      return cfgpu_ensemble_load_slot(e->h, slot, st);
+    }));
   }
   e->slot_req[slot] = r.id;
   r.ens = -1;
@@ -284,7 +301,7 @@ int interval_end(cfgpu_server_s* s, Ens* e, int i, const std::vector<double>& cf
     cfgpu_dns st = nullptr;
     SCK(make_staging(s, r, &st));
     SCK(stage_restart(s, st, r));
-    SCK(cfgpu_rt::store_slot(e->h, i, st));
+    SCK(on_ctrl(s, e->h, [&]() { return cfgpu_rt::store_slot(e->h, i, st); }));
     r.interval++;
     bool finished = false;
     SCK(stage_run(s, r, st, &finished));
@@ -294,8 +311,10 @@ int interval_end(cfgpu_server_s* s, Ens* e, int i, const std::vector<double>& cf
       return CFGPU_OK;
     }
     Timer tm(s->t_load);
-    SCK(cfgpu_ensemble_set_params(e->h, i, &r.flags, nullptr, nullptr));
-    return cfgpu_ensemble_load_slot(e->h, i, st);
+    return on_ctrl(s, e->h, [&]() {
+      SCK(cfgpu_ensemble_set_params(e->h, i, &r.flags, nullptr, nullptr));
+      return cfgpu_ensemble_load_slot(e->h, i, st);
+    });
   }
   r.interval++;
   r.left = r.ts.n;
@@ -474,6 +493,9 @@ cfgpu_status cfgpu_server_create(long long max_bytes, int slots, int precision, 
   if (!out || max_bytes <= 0 || slots < 1 || (precision != CFGPU_FP64 && precision != CFGPU_MIXED))
     return sfail(CFGPU_EINVAL, "bad argument");
   auto* s = new cfgpu_server_s();
+  int least = 0, greatest = 0;
+  if (cudaDeviceGetStreamPriorityRange(&least, &greatest) == cudaSuccess)
+    cudaStreamCreateWithPriority(&s->ctrl, cudaStreamNonBlocking, greatest);
   s->max_bytes = max_bytes;
   s->slots = slots;
   s->precision = precision;
@@ -621,6 +643,7 @@ cfgpu_status cfgpu_server_destroy(cfgpu_server s) {
       if (e->done) cudaEventDestroy(e->done);
     }
   for (auto& kv : s->staging) cfgpu_dns_destroy(kv.second);
+  if (s->ctrl) cudaStreamDestroy(s->ctrl);
   delete s;
   return CFGPU_OK;
 }
