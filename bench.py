@@ -301,9 +301,16 @@ def run_serve(args):
     t0 = time.perf_counter()
     alone = [run_alone(r) for r in reqs]
     t_alone = time.perf_counter() - t0
+    # the same requests alone in the server's precision: a served result must equal its request run alone
+    t0 = time.perf_counter()
+    alone_p = [run_alone(r, args.serve_precision) for r in reqs]
+    t_alone_p = time.perf_counter() - t0
     out = {"requests": len(reqs),
            "one_at_a_time_fp64": {"s": t_alone, "requests_per_s": len(reqs) / t_alone,
-                                  "non_finite": int(sum(not np.all(np.isfinite(a)) for a in alone))}, "rates": []}
+                                  "non_finite": int(sum(not np.all(np.isfinite(a)) for a in alone))},
+           "one_at_a_time_" + args.serve_precision: {
+               "s": t_alone_p, "requests_per_s": len(reqs) / t_alone_p,
+               "non_finite": int(sum(not np.all(np.isfinite(a)) for a in alone_p))}, "rates": []}
     for rate in args.serve_rates:
         rng = np.random.default_rng(11)
         arrivals = np.cumsum(rng.exponential(1.0 / rate, size=len(reqs))) if rate > 0 else np.zeros(len(reqs))
@@ -323,7 +330,7 @@ def run_serve(args):
             if active == 0 and nxt < len(reqs):
                 time.sleep(max(0.0, arrivals[nxt] - (time.perf_counter() - start)))
         makespan = time.perf_counter() - start
-        lat, errs, failed = [], [], 0
+        lat, errs, same, failed = [], [], [], 0
         for k, rid in enumerate(ids):
             try:
                 st, res, t = srv.poll(rid)
@@ -335,6 +342,8 @@ def run_serve(args):
             g = reqs[k][0]
             if np.all(np.isfinite(alone[k])):
                 errs.append(l2norm(res - alone[k], g.Nx, g.Nz) / l2norm(alone[k], g.Nx, g.Nz))
+            if np.all(np.isfinite(alone_p[k])):
+                same.append(float(np.max(np.abs(res - alone_p[k]))))
         stats = srv.stats()
         srv.close()
         out["rates"].append({
@@ -343,7 +352,9 @@ def run_serve(args):
             "p99_ms": 1e3 * float(np.percentile(lat, 99)),
             "vs_one_at_a_time_fp64": (len(reqs) / makespan) / (len(reqs) / t_alone),
             "max_rel_l2_vs_alone_fp64": float(max(errs)) if errs else None,
-            "median_rel_l2_vs_alone_fp64": float(np.median(errs)) if errs else None, "failed": failed,
+            "median_rel_l2_vs_alone_fp64": float(np.median(errs)) if errs else None,
+            "rel_l2_vs_alone_fp64_sorted": [float("%.2g" % e) for e in sorted(errs)],
+            "max_abs_diff_vs_alone_same_precision": float(max(same)) if same else None, "failed": failed,
             "ensembles": stats["ensembles"], "ensemble_steps": stats["ensemble_steps"],
             "field_steps": stats["field_steps"], "chunks": stats["chunks"], "dt_changes": stats["dt_changes"],
             "host_s_admission": stats["admit_us"] / 1e6, "host_s_interval_ends": stats["interval_us"] / 1e6,

@@ -66,3 +66,54 @@ __host__ __device__ __forceinline__ int mode_kz(const GridDev& g, int m) {
 }
 
 #define CFG_MAX_NY 1025
+
+// ---------------------------------------------------------------------------
+// Dithered FP32 constants (mixed precision).  Every constant the FP32 passes
+// use (Chebyshev matrices, FFT twiddles, base-flow values, wavenumbers,
+// scales) is a fixed operator: its rounding error is the same at every step,
+// so it accumulates linearly in time while arithmetic rounding of the
+// changing data accumulates like a random walk.  Each constant therefore
+// exists in DITHER_V roundings: version k is the float nearest to
+// x + s_k ulp(x) with the offsets s_k = (bitrev(k) + 1/2)/V - 1/2 (a
+// low-discrepancy order), so the mean over a cycle of V nonlinear evaluations
+// equals x to about ulp/(2V).  Each field carries its own version index (state
+// that moves with the field), advanced after every nonlinear evaluation.
+// Version blocks are `S` bytes apart (constant tables) and `Sb` bytes apart
+// (base-flow values).
+// ---------------------------------------------------------------------------
+#define DITHER_V 16
+
+struct Dither {
+  const int* ver;  // per-field version index; null: version 0 of undithered tables
+  long long S;     // bytes between versions of the constant tables
+  long long Sb;    // bytes between versions of the base-flow values
+  int nb;          // fields interleaved in the plane index of the x/z passes (plane p -> field p % nb)
+};
+
+__host__ __device__ __forceinline__ double dither_offset(int k) {
+  const int r = ((k & 1) << 3) | ((k & 2) << 1) | ((k & 4) >> 1) | ((k & 8) >> 3);
+  return (r + 0.5) / DITHER_V - 0.5;
+}
+
+__device__ __forceinline__ int dither_ver(const Dither& dt, int f) { return dt.ver ? __ldg(dt.ver + f) : 0; }
+
+template <typename T>
+__host__ __device__ __forceinline__ const T* dither_ptr(const T* p, int v, long long stride_bytes) {
+  return reinterpret_cast<const T*>(reinterpret_cast<const char*>(p) + (long long)v * stride_bytes);
+}
+
+// Version k of the constant x in R (FP64: x itself).
+template <typename R>
+__device__ __forceinline__ R dither_const(double x, int k);
+template <>
+__device__ __forceinline__ double dither_const<double>(double x, int) {
+  return x;
+}
+template <>
+__device__ __forceinline__ float dither_const<float>(double x, int k) {
+  const float r = __double2float_rn(x);
+  const float a = fabsf(r);
+  if (a == 0.0f) return r;
+  const float sp = nextafterf(a, 3.0e38f) - a;
+  return __double2float_rn(x + dither_offset(k) * (double)sp);
+}

@@ -114,12 +114,13 @@ __global__ void k_l2norm2(GridDev g, int N, int ncomp, const double* __restrict_
 template <typename R>
 cudaError_t launch_zcfl(const GridDev& g, const FftPlan& pz, const cpx<R>* twz, int RP, const cpx<R>* X,
                         const double* dyc, double dx, double dz, int nslot, unsigned long long* out, cudaStream_t st) {
-  static bool attr_set = false;
-  if (!attr_set) {
+  // kernel attributes set once per process (thread-safe static initialisation)
+  static const bool attr_set = [] {
     cudaFuncSetAttribute(k_zcfl<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaGetLastError();
-    attr_set = true;
-  }
+    return true;
+  }();
+  (void)attr_set;
   const size_t smem = 2 * sizeof(cpx<R>) * (size_t)(3 * RP / 2) * (g.Nz + 1);
   k_zcfl<R><<<dim3((g.Nx + RP - 1) / RP, g.Ny), 256, smem, st>>>(g, pz, twz, RP, X, dyc, dx, dz, nslot, out);
   return cudaGetLastError();

@@ -339,6 +339,41 @@ void dfree(void* p) {
   if (p) cudaFreeAsync(p, pool_stream());
 }
 
+// Page-locked host buffers come from a process-wide cache by power-of-two size class: page-locked
+// allocation is slow and can serialize the streams of other DNS objects running concurrently, so blocks
+// are allocated once and reused.
+std::mutex g_pin_mu;
+std::map<size_t, std::vector<void*>> g_pin_free;  // size class -> free blocks
+std::map<void*, size_t> g_pin_class;
+
+template <typename T>
+int pinned_alloc(T** p, size_t bytes) {
+  size_t c = 256;
+  while (c < bytes) c <<= 1;
+  {
+    std::lock_guard<std::mutex> lk(g_pin_mu);
+    auto& v = g_pin_free[c];
+    if (!v.empty()) {
+      *p = (T*)v.back();
+      v.pop_back();
+      return CFGPU_OK;
+    }
+  }
+  void* q = nullptr;
+  const cudaError_t e = cudaMallocHost(&q, c);
+  if (e != cudaSuccess) return fail(CFGPU_ENOMEM, std::string("cudaMallocHost: ") + cudaGetErrorString(e));
+  std::lock_guard<std::mutex> lk(g_pin_mu);
+  g_pin_class[q] = c;
+  *p = (T*)q;
+  return CFGPU_OK;
+}
+
+void pinned_free(void* p) {
+  if (!p) return;
+  std::lock_guard<std::mutex> lk(g_pin_mu);
+  g_pin_free[g_pin_class[p]].push_back(p);
+}
+
 }  // namespace
 
 int cfgpu_record_error(int code, const std::string& msg) { return fail(code, msg); }
@@ -552,9 +587,15 @@ struct cfgpu_dns_s {
   void *cderA = nullptr, *cderB = nullptr, *basey = nullptr;  // fused curl: (2/L) T'_n(y_j); U, U', W, W' at y_j
   void *cdfA = nullptr, *cdfB = nullptr;                       // (2/L) diff o chebyfft, parity split
   void* zbasey = nullptr;  // zero base profiles [nb][4N] (LinearAboutProfile: u, v, w without base flow)
+  // Mixed precision: the FP32 constant tables above live in one block of DITHER_V dithered versions (cS bytes
+  // apart; the pointers above address version 0), basey/baseyS likewise; dver holds each field's version.
+  void* cblock = nullptr;
+  long long cS = 0;
+  int* dver = nullptr;  // [nb]
   double* dyc = nullptr;           // CFL grid spacing in y per Gauss-Lobatto point
   unsigned long long* dred = nullptr;  // reduction scratch (CFL key, L2 sum)
   unsigned long long* cfl_host = nullptr;  // pinned copy of the CFL keys (asynchronous CFL passes)
+  double* stage1 = nullptr;                 // pinned staging of one field (slot transfers)
   int alt[2] = {0, 0};  // Alternating state of the main (0) and init (1) NSE: 0 = next is divergence
   // state: current fields
   double *Ucur = nullptr, *Qcur = nullptr;
@@ -685,6 +726,16 @@ int build_slot_tables(cfgpu_dns d, int f) {
   return CFGPU_OK;
 }
 
+// Constant versions of the nonlinear pass (mixed precision; FP64 uses its exact tables).
+Dither dither_of(cfgpu_dns d) {
+  Dither dt{};
+  dt.ver = d->precision == CFGPU_FP64 ? nullptr : d->dver;
+  dt.S = d->cS;
+  dt.Sb = (long long)4 * d->N * (d->hetero ? d->nb : 1) * (long long)d->rsz();
+  dt.nb = d->nb;
+  return dt;
+}
+
 // Nonlinear term N(u) of the fields in U (solved-mode layout) into Nout (R-typed):
 // navierstokesNL (nse.cpp:12-91) for the form selected by the flags; `which`
 // selects the NSE (0 main, 1 init) whose Alternating state is advanced.
@@ -699,14 +750,17 @@ int nonlinear_impl(cfgpu_dns d, const double* U, void* Nout, int form) {
   int nin = 6, nout = 3;
   const void* by = d->hetero ? d->baseyS : d->basey;
   const int bstride = d->hetero ? 4 * N : 0;
+  const Dither dt = dither_of(d);
+  Dither dt0 = dt;  // zero base profiles: one version
+  dt0.Sb = 0;
   if (form == CFGPU_LinearAboutProfile) {
     // linearizedNL: u, v, w at the points (no base flow), (U d/dx + W d/dz) u + v (U', 0, W'), forward y
     if ((N + 1) / 2 > 56) return fail(CFGPU_ENOTSUP, "Ny > 111 with LinearAboutProfile");
     CK(launch_grad_cheb<R>(g, N, false, U, W, (const R*)d->cinvA, (const R*)d->cinvB, (const R*)d->cderA,
-                           (const R*)d->cderB, (const R*)d->zbasey, 0.0, d->st, bstride));
-    CK(launch_linprof<R>(g, N, W, (const R*)by, bstride, (R*)d->F3, d->st));
+                           (const R*)d->cderB, (const R*)d->zbasey, 0.0, d->st, bstride, dt0));
+    CK(launch_linprof<R>(g, N, W, (const R*)by, bstride, (R*)d->F3, d->st, dt));
     CK((launch_cheb<R, R, R>(N, false, (int)row, 3, (const R*)d->F3, row, comp, (R*)Nout, row, comp,
-                             (const R*)d->cfwdA, (const R*)d->cfwdB, d->st)));
+                             (const R*)d->cfwdA, (const R*)d->cfwdB, d->st, dt)));
     d->launches += 3;
     return CFGPU_OK;
   }
@@ -714,12 +768,12 @@ int nonlinear_impl(cfgpu_dns d, const double* U, void* Nout, int form) {
     if ((N + 1) / 2 <= 56) {
       CK(launch_curl_cheb<R>(g, N, U, W, (const R*)d->cinvA, (const R*)d->cinvB, (const R*)d->cderA,
                              (const R*)d->cderB, (const R*)(d->hetero ? d->baseyS : d->basey), d->fl.Vsuck, d->st,
-                             d->hetero ? 4 * N : 0));
+                             d->hetero ? 4 * N : 0, dt));
       d->launches += 1;
     } else {
       CK(launch_curl_base<R>(g, U, C6, d->dUbase, d->dWbase, d->fl.Vsuck, d->st));
       CK((launch_cheb<R, R, R>(N, true, (int)row, 6, C6, row, comp, W, row, comp, (const R*)d->cinvA,
-                               (const R*)d->cinvB, d->st)));
+                               (const R*)d->cinvB, d->st, dt)));
       d->launches += 2;
     }
   } else {
@@ -727,19 +781,21 @@ int nonlinear_impl(cfgpu_dns d, const double* U, void* Nout, int form) {
     const bool gradient = form != NL_DIVERGENCE;
     CK(launch_grad_cheb<R>(g, N, gradient, U, W, (const R*)d->cinvA, (const R*)d->cinvB, (const R*)d->cderA,
                            (const R*)d->cderB, (const R*)(d->hetero ? d->baseyS : d->basey), d->fl.Vsuck, d->st,
-                           d->hetero ? 4 * N : 0));
+                           d->hetero ? 4 * N : 0, dt));
     d->launches += 1;
     nin = gradient ? 12 : 3;
     nout = form == NL_CONVECTION ? 3 : (form == NL_DIVERGENCE ? 6 : 9);
   }
-  CK(launch_xinv<R>(gp, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)W, (cpx<R>*)d->X6, nin, d->st, d->xcols));
-  CK(launch_zphys<R>(gp, form, d->pz, (const cpx<R>*)d->twz, d->RP, (const cpx<R>*)d->X6, (cpx<R>*)d->Z3, d->st));
-  CK(launch_xfwd<R>(gp, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)d->Z3, (cpx<R>*)d->F3, nout, d->st, d->xcols));
+  CK(launch_xinv<R>(gp, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)W, (cpx<R>*)d->X6, nin, d->st, d->xcols, dt));
+  CK(launch_zphys<R>(gp, form, d->pz, (const cpx<R>*)d->twz, d->RP, (const cpx<R>*)d->X6, (cpx<R>*)d->Z3, d->st,
+                     dt));
+  CK(launch_xfwd<R>(gp, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)d->Z3, (cpx<R>*)d->F3, nout, d->st, d->xcols,
+                    dt));
   d->launches += 3;
   const R* F = (const R*)d->F3;
   if (form == NL_ROTATIONAL || form == NL_CONVECTION) {
     CK((launch_cheb<R, R, R>(N, false, (int)row, 3, F, row, comp, (R*)Nout, row, comp, (const R*)d->cfwdA,
-                             (const R*)d->cfwdB, d->st)));
+                             (const R*)d->cfwdB, d->st, dt)));
     d->launches += 1;
   } else {
     // products p_ij (ij = uu, uv, uw, vv, vw, ww) follow the convection term for the skew form
@@ -751,7 +807,7 @@ int nonlinear_impl(cfgpu_dns d, const double* U, void* Nout, int form) {
       const R wF = form == NL_SKEW ? half : (R)0, w = form == NL_SKEW ? half : (R)1;
       CK(launch_cheb_fwd_div<R>(g, N, pF, p + pij[i][0] * comp, p + pij[i][2] * comp, p + pij[i][1] * comp, wF, w,
                                 w, (R*)Nout + i * comp, (const R*)d->cfwdA, (const R*)d->cfwdB,
-                                (const R*)d->cdfA, (const R*)d->cdfB, d->st));
+                                (const R*)d->cdfA, (const R*)d->cdfB, d->st, dt));
     }
     d->launches += 3;
   }
@@ -779,6 +835,10 @@ int nonlinear(cfgpu_dns d, const double* U, void* Nout, int which = 0) {
   // rotation about z (nse.cpp:62-78; not with LinearAboutProfile)
   if (d->fl.rotation != 0.0 && form != CFGPU_LinearAboutProfile)
     CKS(fp64 ? rotation_term<double>(d, U, Nout) : rotation_term<float>(d, U, Nout));
+  if (!fp64) {
+    CK(launch_dither_bump(d->dver, d->nb, d->st));  // next evaluation: next version of the FP32 constants
+    d->launches++;
+  }
   return CFGPU_OK;
 }
 
@@ -1144,7 +1204,7 @@ void scatter_modes(cfgpu_dns d, const double* in, int Nd, double* h, int f0 = 0,
 }
 
 int ensure_stage(cfgpu_dns d) {
-  if (!d->stage) CK(cudaMallocHost((void**)&d->stage, d->stage_elems * sizeof(double)));
+  if (!d->stage) CKS(pinned_alloc(&d->stage, d->stage_elems * sizeof(double)));
   return CFGPU_OK;
 }
 
@@ -1174,17 +1234,23 @@ int get_fields(cfgpu_dns d, double* u, double* q) {
 }
 
 // One field (slot) of a batch: the rows [c][ny] of that field are strided by nb*Md modes on the device.
+int ensure_stage1(cfgpu_dns d) {
+  if (!d->stage1) CKS(pinned_alloc(&d->stage1, 4 * 2 * (size_t)d->g.Md * d->N * sizeof(double)));
+  return CFGPU_OK;
+}
+
 int set_slot(cfgpu_dns d, int slot, const double* u, const double* q) {
-  CKS(ensure_stage(d));
+  CKS(ensure_stage1(d));
+  double* stage = d->stage1;
   const size_t w = 2 * (size_t)d->g.Md, pitch = w * d->nb, cd1 = w * d->N;
   if (u) {
-    gather_modes(d, u, 3, d->stage, 0, 1, 1);
-    CK(cudaMemcpy2DAsync(d->Ucur + slot * w, pitch * sizeof(double), d->stage, w * sizeof(double),
+    gather_modes(d, u, 3, stage, 0, 1, 1);
+    CK(cudaMemcpy2DAsync(d->Ucur + slot * w, pitch * sizeof(double), stage, w * sizeof(double),
                          w * sizeof(double), 3 * (size_t)d->N, cudaMemcpyHostToDevice, d->st));
   }
   if (q) {
-    gather_modes(d, q, 1, d->stage + 3 * cd1, 0, 1, 1);
-    CK(cudaMemcpy2DAsync(d->Qcur + slot * w, pitch * sizeof(double), d->stage + 3 * cd1, w * sizeof(double),
+    gather_modes(d, q, 1, stage + 3 * cd1, 0, 1, 1);
+    CK(cudaMemcpy2DAsync(d->Qcur + slot * w, pitch * sizeof(double), stage + 3 * cd1, w * sizeof(double),
                          w * sizeof(double), (size_t)d->N, cudaMemcpyHostToDevice, d->st));
   }
   CK(cudaStreamSynchronize(d->st));
@@ -1192,35 +1258,60 @@ int set_slot(cfgpu_dns d, int slot, const double* u, const double* q) {
 }
 
 int get_slot(cfgpu_dns d, int slot, double* u, double* q) {
-  CKS(ensure_stage(d));
+  CKS(ensure_stage1(d));
+  double* stage = d->stage1;
   const size_t w = 2 * (size_t)d->g.Md, pitch = w * d->nb, cd1 = w * d->N;
-  CK(cudaMemcpy2DAsync(d->stage, w * sizeof(double), d->Ucur + slot * w, pitch * sizeof(double),
+  CK(cudaMemcpy2DAsync(stage, w * sizeof(double), d->Ucur + slot * w, pitch * sizeof(double),
                        w * sizeof(double), 3 * (size_t)d->N, cudaMemcpyDeviceToHost, d->st));
-  CK(cudaMemcpy2DAsync(d->stage + 3 * cd1, w * sizeof(double), d->Qcur + slot * w, pitch * sizeof(double),
+  CK(cudaMemcpy2DAsync(stage + 3 * cd1, w * sizeof(double), d->Qcur + slot * w, pitch * sizeof(double),
                        w * sizeof(double), (size_t)d->N, cudaMemcpyDeviceToHost, d->st));
   CK(cudaStreamSynchronize(d->st));
-  if (u) scatter_modes(d, d->stage, 3, u, 0, 1, 1);
-  if (q) scatter_modes(d, d->stage + 3 * cd1, 1, q, 0, 1, 1);
+  if (u) scatter_modes(d, stage, 3, u, 0, 1, 1);
+  if (q) scatter_modes(d, stage + 3 * cd1, 1, q, 0, 1, 1);
   return CFGPU_OK;
 }
 
-template <typename R>
-int upload_as(const std::vector<double>& v, void** dst, long long& bytes) {
-  std::vector<R> t(v.begin(), v.end());
-  R* p;
-  CKS(dalloc(&p, t.size(), bytes));
-  CK(cudaMemcpy(p, t.data(), t.size() * sizeof(R), cudaMemcpyHostToDevice));
+// Host rounding of x to float with dither offset k (the device's dither_const<float>).
+float dither_round_host(double x, int k) {
+  const float r = (float)x;
+  const float a = std::fabs(r);
+  if (a == 0.0f) return r;
+  const float sp = std::nextafter(a, 3.0e38f) - a;
+  return (float)(x + dither_offset(k) * (double)sp);
+}
+
+// DITHER_V versions of the tables (tables[i] at float offset off[i] of each S-float version) in one block.
+int upload_dithered(const std::vector<std::vector<double>>& tables, const std::vector<size_t>& off, size_t S,
+                    void** dst, long long& bytes, cudaStream_t st) {
+  std::vector<float> h((size_t)DITHER_V * S, 0.0f);
+  for (int v = 0; v < DITHER_V; ++v)
+    for (size_t i = 0; i < tables.size(); ++i)
+      for (size_t e = 0; e < tables[i].size(); ++e) h[(size_t)v * S + off[i] + e] = dither_round_host(tables[i][e], v);
+  float* p;
+  CKS(dalloc(&p, h.size(), bytes));
+  CK(cudaMemcpyAsync(p, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+  CK(cudaStreamSynchronize(st));  // h is a local
   *dst = p;
   return CFGPU_OK;
 }
 
 template <typename R>
-int upload_tw(const std::vector<std::complex<long double>>& tw, void** dst, long long& bytes) {
+int upload_as(const std::vector<double>& v, void** dst, long long& bytes, cudaStream_t st) {
+  std::vector<R> t(v.begin(), v.end());
+  R* p;
+  CKS(dalloc(&p, t.size(), bytes));
+  CK(cudaMemcpyAsync(p, t.data(), t.size() * sizeof(R), cudaMemcpyHostToDevice, st));
+  *dst = p;
+  return CFGPU_OK;
+}
+
+template <typename R>
+int upload_tw(const std::vector<std::complex<long double>>& tw, void** dst, long long& bytes, cudaStream_t st) {
   std::vector<cpx<R>> t(tw.size() ? tw.size() : 1);
   for (size_t i = 0; i < tw.size(); ++i) t[i] = cmk<R>((R)tw[i].real(), (R)tw[i].imag());
   cpx<R>* p;
   CKS(dalloc(&p, t.size(), bytes));
-  CK(cudaMemcpy(p, t.data(), t.size() * sizeof(cpx<R>), cudaMemcpyHostToDevice));
+  CK(cudaMemcpyAsync(p, t.data(), t.size() * sizeof(cpx<R>), cudaMemcpyHostToDevice, st));
   *dst = p;
   return CFGPU_OK;
 }
@@ -1389,7 +1480,7 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
         ml[(size_t)nb * g.Md + (size_t)f * g.Md + m] = mode_kz(g, m);
       }
     CKS(dalloc(&d->dmodes, ml.size(), B));
-    CK(cudaMemcpy(d->dmodes, ml.data(), ml.size() * sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync(d->dmodes, ml.data(), ml.size() * sizeof(int), cudaMemcpyHostToDevice, d->st));
     d->gm.Md = nb * g.Md;
     d->gm.Mf = g.Md;
     d->gm.kxs = d->dmodes;
@@ -1402,19 +1493,19 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
     for (int j = 0; j < Ny; ++j) y[j] = (b + a) / 2 + (b - a) / 2 * std::cos(j * M_PI / (Ny - 1));
     for (int j = 0; j < Ny; ++j) dy[j] = (j == 0 || j == Ny - 1) ? y[0] - y[1] : (y[j - 1] - y[j + 1]) / 2.0;
     CKS(dalloc(&d->dyc, Ny, B));
-    CK(cudaMemcpy(d->dyc, dy.data(), Ny * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync(d->dyc, dy.data(), Ny * sizeof(double), cudaMemcpyHostToDevice, d->st));
   }
-  CK(cudaMemcpy(d->dUbase, d->Ubase.data(), Ny * sizeof(double), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(d->dWbase, d->Wbase.data(), Ny * sizeof(double), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(d->dUbaseyy, d->Ubaseyy.data(), Ny * sizeof(double), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(d->dWbaseyy, d->Wbaseyy.data(), Ny * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpyAsync(d->dUbase, d->Ubase.data(), Ny * sizeof(double), cudaMemcpyHostToDevice, d->st));
+  CK(cudaMemcpyAsync(d->dWbase, d->Wbase.data(), Ny * sizeof(double), cudaMemcpyHostToDevice, d->st));
+  CK(cudaMemcpyAsync(d->dUbaseyy, d->Ubaseyy.data(), Ny * sizeof(double), cudaMemcpyHostToDevice, d->st));
+  CK(cudaMemcpyAsync(d->dWbaseyy, d->Wbaseyy.data(), Ny * sizeof(double), cudaMemcpyHostToDevice, d->st));
   {
     std::vector<double> init(2 * (size_t)nb);
     for (int f = 0; f < nb; ++f) {
       init[2 * f] = d->dPdxAct;
       init[2 * f + 1] = d->dPdzAct;
     }
-    CK(cudaMemcpy(d->ddPdx, init.data(), init.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync(d->ddPdx, init.data(), init.size() * sizeof(double), cudaMemcpyHostToDevice, d->st));
   }
   // Helmholtz B rows
   {
@@ -1423,9 +1514,9 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
     CKS(dalloc(&d->hb_lo, Ny, B));
     CKS(dalloc(&d->hb_di, Ny, B));
     CKS(dalloc(&d->hb_up, Ny, B));
-    CK(cudaMemcpy(d->hb_lo, lo.data(), Ny * sizeof(double), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(d->hb_di, di.data(), Ny * sizeof(double), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(d->hb_up, up.data(), Ny * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync(d->hb_lo, lo.data(), Ny * sizeof(double), cudaMemcpyHostToDevice, d->st));
+    CK(cudaMemcpyAsync(d->hb_di, di.data(), Ny * sizeof(double), cudaMemcpyHostToDevice, d->st));
+    CK(cudaMemcpyAsync(d->hb_up, up.data(), Ny * sizeof(double), cudaMemcpyHostToDevice, d->st));
   }
   // FFT plans, twiddles, Chebyshev matrices
   std::vector<std::complex<long double>> twx, twz;
@@ -1439,37 +1530,51 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
   const std::vector<double>& basey = bf.basey;
   const bool fp64 = d->precision == CFGPU_FP64;
   if (fp64) {
-    CKS(upload_tw<double>(twx, &d->twx, B));
-    CKS(upload_tw<double>(twz, &d->twz, B));
-    CKS(upload_as<double>(cm.invA, &d->cinvA, B));
-    CKS(upload_as<double>(cm.invB, &d->cinvB, B));
-    CKS(upload_as<double>(cm.fwdA, &d->cfwdA, B));
-    CKS(upload_as<double>(cm.fwdB, &d->cfwdB, B));
-    CKS(upload_as<double>(cm.derA, &d->cderA, B));
-    CKS(upload_as<double>(cm.derB, &d->cderB, B));
-    CKS(upload_as<double>(basey, &d->basey, B));
-    CKS(upload_as<double>(cm.dfA, &d->cdfA, B));
-    CKS(upload_as<double>(cm.dfB, &d->cdfB, B));
+    CKS(upload_tw<double>(twx, &d->twx, B, d->st));
+    CKS(upload_tw<double>(twz, &d->twz, B, d->st));
+    CKS(upload_as<double>(cm.invA, &d->cinvA, B, d->st));
+    CKS(upload_as<double>(cm.invB, &d->cinvB, B, d->st));
+    CKS(upload_as<double>(cm.fwdA, &d->cfwdA, B, d->st));
+    CKS(upload_as<double>(cm.fwdB, &d->cfwdB, B, d->st));
+    CKS(upload_as<double>(cm.derA, &d->cderA, B, d->st));
+    CKS(upload_as<double>(cm.derB, &d->cderB, B, d->st));
+    CKS(upload_as<double>(basey, &d->basey, B, d->st));
+    CKS(upload_as<double>(cm.dfA, &d->cdfA, B, d->st));
+    CKS(upload_as<double>(cm.dfB, &d->cdfB, B, d->st));
   } else {
-    CKS(upload_tw<float>(twx, &d->twx, B));
-    CKS(upload_tw<float>(twz, &d->twz, B));
-    CKS(upload_as<float>(cm.invA, &d->cinvA, B));
-    CKS(upload_as<float>(cm.invB, &d->cinvB, B));
-    CKS(upload_as<float>(cm.fwdA, &d->cfwdA, B));
-    CKS(upload_as<float>(cm.fwdB, &d->cfwdB, B));
-    CKS(upload_as<float>(cm.derA, &d->cderA, B));
-    CKS(upload_as<float>(cm.derB, &d->cderB, B));
-    CKS(upload_as<float>(basey, &d->basey, B));
-    CKS(upload_as<float>(cm.dfA, &d->cdfA, B));
-    CKS(upload_as<float>(cm.dfB, &d->cdfB, B));
+    // DITHER_V dithered versions of every FP32 constant table in one block (16-byte aligned tables)
+    std::vector<std::vector<double>> tabs = {cm.invA, cm.invB, cm.fwdA, cm.fwdB, cm.derA, cm.derB, cm.dfA, cm.dfB};
+    for (const auto* tw : {&twx, &twz}) {
+      std::vector<double> t(2 * (tw->size() ? tw->size() : 1), 0.0);
+      for (size_t i = 0; i < tw->size(); ++i) {
+        t[2 * i] = (double)(*tw)[i].real();
+        t[2 * i + 1] = (double)(*tw)[i].imag();
+      }
+      tabs.push_back(t);
+    }
+    std::vector<size_t> off(tabs.size());
+    size_t S = 0;
+    for (size_t i = 0; i < tabs.size(); ++i) {
+      off[i] = S;
+      S += (tabs[i].size() + 3) & ~(size_t)3;
+    }
+    CKS(upload_dithered(tabs, off, S, &d->cblock, B, d->st));
+    float* c0 = (float*)d->cblock;
+    void** dst[10] = {&d->cinvA, &d->cinvB, &d->cfwdA, &d->cfwdB, &d->cderA, &d->cderB, &d->cdfA, &d->cdfB,
+                      &d->twx, &d->twz};
+    for (size_t i = 0; i < tabs.size(); ++i) *dst[i] = c0 + off[i];
+    d->cS = (long long)(S * sizeof(float));
+    CKS(upload_dithered({basey}, {0}, basey.size(), &d->basey, B, d->st));
   }
+  CKS(dalloc(&d->dver, nb, B));
+  CK(cudaMemsetAsync(d->dver, 0, nb * sizeof(int), d->st));
   // state and work arrays
   const size_t cd = d->compc();
   const size_t rs = d->rsz();
   CKS(dalloc(&d->Ucur, 3 * cd, B));
   CKS(dalloc(&d->Qcur, cd, B));
-  CK(cudaMemset(d->Ucur, 0, 3 * cd * sizeof(double)));
-  CK(cudaMemset(d->Qcur, 0, cd * sizeof(double)));
+  CK(cudaMemsetAsync(d->Ucur, 0, 3 * cd * sizeof(double), d->st));
+  CK(cudaMemsetAsync(d->Qcur, 0, cd * sizeof(double), d->st));
   unsigned char* tmp;
   CKS(dalloc(&tmp, 6 * cd * rs, B));
   d->C6 = tmp;
@@ -1488,7 +1593,7 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
   if (f.nonlinearity == CFGPU_LinearAboutProfile) {
     CKS(dalloc(&tmp, 4 * (size_t)Ny * nb * rs, B));
     d->zbasey = tmp;
-    CK(cudaMemset(d->zbasey, 0, 4 * (size_t)Ny * nb * rs));
+    CK(cudaMemsetAsync(d->zbasey, 0, 4 * (size_t)Ny * nb * rs, d->st));
   }
   d->RP = fp64 ? 8 : 16;
   auto zbytes = [&](int form, int rp) {
@@ -1525,21 +1630,21 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
         CKS(dalloc(&d->Qh[j], cd, B));
         CKS(dalloc(&tmp, 3 * cd * rs, B));
         d->Nh[j] = tmp;
-        CK(cudaMemset(d->Uh[j], 0, 3 * cd * sizeof(double)));
-        CK(cudaMemset(d->Qh[j], 0, cd * sizeof(double)));
-        CK(cudaMemset(d->Nh[j], 0, 3 * cd * rs));
+        CK(cudaMemsetAsync(d->Uh[j], 0, 3 * cd * sizeof(double), d->st));
+        CK(cudaMemsetAsync(d->Qh[j], 0, cd * sizeof(double), d->st));
+        CK(cudaMemsetAsync(d->Nh[j], 0, 3 * cd * rs, d->st));
       }
     } else if (s.family == 1) {
       CKS(dalloc(&tmp, 3 * cd * rs, B));
       d->fj[which] = tmp;
       CKS(dalloc(&tmp, 3 * cd * rs, B));
       d->fj1[which] = tmp;
-      CK(cudaMemset(d->fj[which], 0, 3 * cd * rs));
-      CK(cudaMemset(d->fj1[which], 0, 3 * cd * rs));
+      CK(cudaMemsetAsync(d->fj[which], 0, 3 * cd * rs, d->st));
+      CK(cudaMemsetAsync(d->fj1[which], 0, 3 * cd * rs, d->st));
     } else {
       CKS(dalloc(&tmp, 3 * cd * rs, B));
       d->rkQ[which] = tmp;
-      CK(cudaMemset(d->rkQ[which], 0, 3 * cd * rs));
+      CK(cudaMemsetAsync(d->rkQ[which], 0, 3 * cd * rs, d->st));
       if (!d->rkN) {
         CKS(dalloc(&tmp, 3 * cd * rs, B));
         d->rkN = tmp;
@@ -1552,7 +1657,7 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
   CKS(build_tables(d, d->main));
   if (d->has_init) CKS(build_tables(d, d->init));
   d->stage_elems = 4 * cd;  // pinned host staging, allocated on first host transfer (ensure_stage)
-  CK(cudaMallocHost((void**)&d->cfl_host, (size_t)nb * sizeof(unsigned long long)));
+  CKS(pinned_alloc(&d->cfl_host, (size_t)nb * sizeof(unsigned long long)));
   CK(cudaStreamSynchronize(d->st));
   return CFGPU_OK;
 }
@@ -1561,11 +1666,15 @@ void dns_free(cfgpu_dns d) {
   if (!d) return;
   if (d->st) cudaStreamSynchronize(d->st);
   auto F = [](void* p) { dfree(p); };
+  if (d->cblock) {
+    // the FP32 constant tables live inside one block (all versions): freed once, below
+    d->twx = d->twz = d->cinvA = d->cinvB = d->cfwdA = d->cfwdB = d->cderA = d->cderB = d->cdfA = d->cdfB = nullptr;
+  }
   F(d->dUbase); F(d->dWbase); F(d->dUbaseyy); F(d->dWbaseyy); F(d->ddPdx);
   F(d->hb_lo); F(d->hb_di); F(d->hb_up);
   F(d->twx); F(d->twz); F(d->cinvA); F(d->cinvB); F(d->cfwdA); F(d->cfwdB);
   F(d->cderA); F(d->cderB); F(d->basey); F(d->cdfA); F(d->cdfB); F(d->dyc); F(d->dred); F(d->dmodes);
-  F(d->dslot); F(d->dbaseS); F(d->baseyS); F(d->zbasey);
+  F(d->dslot); F(d->dbaseS); F(d->baseyS); F(d->zbasey); F(d->cblock); F(d->dver);
   F(d->Ucur); F(d->Qcur);
   for (int j = 0; j < 4; ++j) { F(d->Uh[j]); F(d->Qh[j]); F(d->Nh[j]); }
   for (int w = 0; w < 2; ++w) { F(d->fj[w]); F(d->fj1[w]); F(d->rkQ[w]); }
@@ -1573,8 +1682,9 @@ void dns_free(cfgpu_dns d) {
   F(d->C6); F(d->W6); F(d->X6); F(d->Z3); F(d->F3); F(d->scratch);
   for (Scheme* s : {&d->main, &d->init})
     for (auto& t : s->tau) { F(t.f); F(t.s); }
-  if (d->stage) cudaFreeHost(d->stage);
-  if (d->cfl_host) cudaFreeHost(d->cfl_host);
+  pinned_free(d->stage);
+  pinned_free(d->cfl_host);
+  pinned_free(d->stage1);
   for (auto& e : d->ev_pool) cudaEventDestroy(e);
   for (auto& u : d->ev_used) {
     cudaEventDestroy(u.second.first);
@@ -1647,13 +1757,6 @@ namespace cfgpu_rt {
 int cfl_async(cfgpu_dns d) { return d->precision == CFGPU_FP64 ? cfl_enqueue<double>(d) : cfl_enqueue<float>(d); }
 void cfl_collect(cfgpu_dns d, double* out) { cfl_finish(d, out); }
 
-// Issue the DNS's work on another stream (the caller has synchronized the current one); returns the old stream.
-cudaStream_t swap_stream(cfgpu_dns d, cudaStream_t s) {
-  cudaStream_t old = d->st;
-  d->st = s;
-  return old;
-}
-
 // Recreate the DNS's stream with a scheduling priority (cudaDeviceGetStreamPriorityRange).
 int set_priority(cfgpu_dns d, int prio) {
   CK(cudaStreamSynchronize(d->st));
@@ -1683,7 +1786,14 @@ int store_slot(cfgpu_dns d, int slot, cfgpu_dns dst) {
   CK(cudaMemcpy2DAsync(dst->Ucur, w * 8, d->Ucur + slot * w, pitch * 8, w * 8, 3 * N, cudaMemcpyDeviceToDevice,
                        d->st));
   CK(cudaMemcpy2DAsync(dst->Qcur, w * 8, d->Qcur + slot * w, pitch * 8, w * 8, N, cudaMemcpyDeviceToDevice, d->st));
+  CK(cudaMemcpyAsync(dst->dver, d->dver + slot, sizeof(int), cudaMemcpyDeviceToDevice, d->st));  // constant version
   CK(cudaStreamSynchronize(d->st));
+  return CFGPU_OK;
+}
+
+// Field `slot` starts over as a fresh DNS does: version 0 of the dithered FP32 constants.
+int reset_version(cfgpu_dns d, int slot) {
+  CK(cudaMemsetAsync(d->dver + slot, 0, sizeof(int), d->st));
   return CFGPU_OK;
 }
 
@@ -1743,8 +1853,14 @@ int upload_slot(cfgpu_dns d, int f, const BaseFlow& B) {
   for (int k = 0; k < 4; ++k)
     CK(cudaMemcpyAsync(d->dbaseS + k * nN + f * N, arrs[k]->data(), N * sizeof(double), cudaMemcpyHostToDevice,
                        d->st));
-  std::vector<R> by(B.basey.begin(), B.basey.end());
-  CK(cudaMemcpyAsync((R*)d->baseyS + f * 4 * N, by.data(), by.size() * sizeof(R), cudaMemcpyHostToDevice, d->st));
+  const int nver = sizeof(R) == sizeof(double) ? 1 : DITHER_V;
+  std::vector<R> by((size_t)nver * 4 * N);
+  for (int v = 0; v < nver; ++v)
+    for (size_t e = 0; e < 4 * N; ++e)
+      by[v * 4 * N + e] = sizeof(R) == sizeof(double) ? (R)B.basey[e] : (R)dither_round_host(B.basey[e], v);
+  for (int v = 0; v < nver; ++v)
+    CK(cudaMemcpyAsync((R*)d->baseyS + (size_t)v * nN * 4 + f * 4 * N, by.data() + (size_t)v * 4 * N,
+                       4 * N * sizeof(R), cudaMemcpyHostToDevice, d->st));
   const double init[2] = {B.dPdxAct, B.dPdzAct};
   CK(cudaMemcpyAsync(d->ddPdx + 2 * f, init, sizeof(init), cudaMemcpyHostToDevice, d->st));
   CK(cudaStreamSynchronize(d->st));  // host sources are locals
@@ -1757,7 +1873,8 @@ int ensure_hetero(cfgpu_dns d) {
   CKS(dalloc(&d->dslot, nb, d->bytes));
   CKS(dalloc(&d->dbaseS, 4 * nb * N, d->bytes));
   unsigned char* tmp;
-  CKS(dalloc(&tmp, 4 * nb * N * d->rsz(), d->bytes));
+  const size_t nver = d->precision == CFGPU_FP64 ? 1 : DITHER_V;  // dithered versions (mixed precision)
+  CKS(dalloc(&tmp, nver * 4 * nb * N * d->rsz(), d->bytes));
   d->baseyS = tmp;
   d->sfl.assign(nb, d->fl);
   drop_graphs(d);  // the solve and nonlinear kernels switch to per-field parameter arrays
@@ -1901,6 +2018,7 @@ cfgpu_status cfgpu_ensemble_load_slot(cfgpu_dns d, int slot, cfgpu_dns src) {
     CKS(copy(d->rkQ[0], src->rkQ[0], rs, 3 * N));
   }
   CK(cudaMemcpyAsync(d->ddPdx + 2 * slot, src->ddPdx, 2 * sizeof(double), cudaMemcpyDeviceToDevice, d->st));
+  CK(cudaMemcpyAsync(d->dver + slot, src->dver, sizeof(int), cudaMemcpyDeviceToDevice, d->st));  // constant version
   CK(cudaStreamSynchronize(d->st));
   return CFGPU_OK;
 }
@@ -2024,6 +2142,49 @@ cfgpu_status cfgpu_dns_kernel_launches(cfgpu_dns d, long long* n) {
   return CFGPU_OK;
 }
 
+
+// navierstokesNL (channelflow/nse.cpp:12-91) followed by NSE::nonlinear's zeroPaddedModes
+// (nse.cpp:383-391): f = N(u) for the FlowField buffers u (nb velocity fields, spectral), computed by the
+// DNS's own kernels in its precision; the DNS's state is untouched (an Alternating form flips as in
+// navierstokesNL).
+cfgpu_status cfgpu_dns_nonlinear(cfgpu_dns d, const double* u, double* f) {
+  if (!d || !u || !f) return fail(CFGPU_EINVAL, "bad argument");
+  CKS(ensure_stage(d));
+  const size_t cd = d->compc(), rs = d->rsz();
+  long long B = 0;
+  double* Ud = nullptr;
+  unsigned char* Nd = nullptr;
+  CKS(dalloc(&Ud, 3 * cd, B));
+  int st = dalloc(&Nd, 3 * cd * rs, B);
+  std::vector<double> out(3 * cd);
+  std::vector<int> ver(d->nb);  // the evaluation advances the constant versions: put them back afterwards
+  if (st == CFGPU_OK) {
+    gather_modes(d, u, 3, d->stage);
+    cudaError_t e = cudaMemcpyAsync(ver.data(), d->dver, d->nb * sizeof(int), cudaMemcpyDeviceToHost, d->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(d->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(Ud, d->stage, 3 * cd * sizeof(double), cudaMemcpyHostToDevice, d->st);
+    if (e == cudaSuccess && (st = nonlinear(d, Ud, Nd, 0)) == CFGPU_OK) {
+      e = cudaMemcpyAsync(d->dver, ver.data(), d->nb * sizeof(int), cudaMemcpyHostToDevice, d->st);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(d->stage, Nd, 3 * cd * rs, cudaMemcpyDeviceToHost, d->st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(d->st);
+    }
+    if (e != cudaSuccess) st = fail(CFGPU_ECUDA, std::string("nonlinear: ") + cudaGetErrorString(e));
+  }
+  cudaStreamSynchronize(d->st);
+  dfree(Ud);
+  dfree(Nd);
+  if (st != CFGPU_OK) return st;
+  if (rs == sizeof(double)) {
+    memcpy(out.data(), d->stage, 3 * cd * sizeof(double));
+  } else {
+    const float* p = reinterpret_cast<const float*>(d->stage);
+    for (size_t i = 0; i < 3 * cd; ++i) out[i] = p[i];
+  }
+  const GridDev& g = d->g;
+  memset(f, 0, sizeof(double) * 3 * (size_t)d->nb * 2 * g.Ny * g.Nx * (g.Nz / 2 + 1));
+  scatter_modes(d, out.data(), 3, f);
+  return CFGPU_OK;
+}
 
 cfgpu_status cfgpu_dns_cfl(cfgpu_dns d, double* cfl) {
   if (!d || !cfl) return fail(CFGPU_EINVAL, "bad argument");
@@ -2273,8 +2434,8 @@ cfgpu_status cfgpu_tau_solve_batched(int N, int nmodes, const int* kx, const int
     CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     CKS(dalloc(&dkx, nmodes, bytes));
     CKS(dalloc(&dkz, nmodes, bytes));
-    CK(cudaMemcpy(dkx, kx, nmodes * sizeof(int), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(dkz, kz, nmodes * sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync(dkx, kx, nmodes * sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dkz, kz, nmodes * sizeof(int), cudaMemcpyHostToDevice, st));
     g.kxs = dkx;
     g.kzs = dkz;
     CKS(dalloc(&R3, 3 * comp, bytes));
@@ -2282,15 +2443,15 @@ cfgpu_status cfgpu_tau_solve_batched(int N, int nmodes, const int* kx, const int
     CKS(dalloc(&Q1, comp, bytes));
     CKS(dalloc(&scr, 8 * comp, bytes));
     CKS(dalloc(&zero, N, bytes));
-    CK(cudaMemset(zero, 0, N * sizeof(double)));
+    CK(cudaMemsetAsync(zero, 0, N * sizeof(double), st));
     std::vector<double> lo, di, up;
     make_helm_b(N, lo, di, up);
     CKS(dalloc(&hlo, N, bytes));
     CKS(dalloc(&hdi, N, bytes));
     CKS(dalloc(&hup, N, bytes));
-    CK(cudaMemcpy(hlo, lo.data(), N * sizeof(double), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(hdi, di.data(), N * sizeof(double), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(hup, up.data(), N * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync(hlo, lo.data(), N * sizeof(double), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(hdi, di.data(), N * sizeof(double), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(hup, up.data(), N * sizeof(double), cudaMemcpyHostToDevice, st));
     HelmB hb{hlo, hdi, hup};
     CKS(dalloc(&t.f, (size_t)N * nmodes * TF_NFIELDS, bytes));
     CKS(dalloc(&t.s, (size_t)nmodes * TS_NSCALARS, bytes));

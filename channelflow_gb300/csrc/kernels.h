@@ -13,6 +13,9 @@ template <typename R>
 cudaError_t launch_curl_base(const GridDev& g, const double* U, R* C6, const double* Ub, const double* Wb, double Vsuck,
                              cudaStream_t st);
 
+// Undithered constants (version 0 only; one field).
+constexpr Dither kNoDither{nullptr, 0, 0, 1};
+
 size_t cheb_smem_bytes(int N, size_t rsize);
 
 template <typename R>
@@ -20,11 +23,13 @@ size_t curl_cheb_smem_bytes(int N);
 template <typename R>
 cudaError_t launch_curl_cheb(const GridDev& g, int N, const double* U, R* W6, const R* CA, const R* CB, const R* DA,
                              const R* DB, const R* basey, double Vsuck, cudaStream_t st,
-                             int bstride = 0);
+                             int bstride = 0, const Dither& dt = kNoDither);
 
+// Lines split evenly over dt.nb fields (no block straddles two) when dithered.
 template <typename TI, typename R, typename TO>
 cudaError_t launch_cheb(int N, bool inverse, int nlines, int ncomp, const TI* in, size_t ld_in, size_t cs_in, TO* out,
-                        size_t ld_out, size_t cs_out, const R* A, const R* B, cudaStream_t st);
+                        size_t ld_out, size_t cs_out, const R* A, const R* B, cudaStream_t st,
+                        const Dither& dt = kNoDither);
 
 // Nonlinear forms (values of the reference's NonlinearMethod enum, dnsflags.h:28-35)
 enum { NL_ROTATIONAL = 0, NL_CONVECTION = 1, NL_DIVERGENCE = 2, NL_SKEW = 3 };
@@ -34,22 +39,23 @@ size_t grad_cheb_smem_bytes(int N);
 template <typename R>
 cudaError_t launch_grad_cheb(const GridDev& g, int N, bool gradient, const double* U, R* W, const R* CA, const R* CB,
                              const R* DA, const R* DB, const R* basey, double Vsuck, cudaStream_t st,
-                             int bstride = 0);
+                             int bstride = 0, const Dither& dt = kNoDither);
 template <typename R>
 size_t zphys_smem_bytes(const GridDev& g, int form, int RP);
 template <typename R>
 cudaError_t launch_zphys(const GridDev& g, int form, const FftPlan& pz, const cpx<R>* twz, int RP, const cpx<R>* X,
-                         cpx<R>* Z, cudaStream_t st);
+                         cpx<R>* Z, cudaStream_t st, const Dither& dt = kNoDither);
 template <typename R>
 size_t cheb_fwd_div_smem_bytes(int N);
 template <typename R>
 cudaError_t launch_cheb_fwd_div(const GridDev& g, int N, const R* pF, const R* pKx, const R* pKz, const R* pD, R wF,
                                 R wK, R wD, R* out, const R* FA, const R* FB, const R* DFA, const R* DFB,
-                                cudaStream_t st);
+                                cudaStream_t st, const Dither& dt = kNoDither);
 
 // LinearAboutProfile term from u, v, w at the Gauss-Lobatto points (k_grad_cheb without base flow).
 template <typename R>
-cudaError_t launch_linprof(const GridDev& g, int N, const R* Y, const R* basey, int bstride, R* F, cudaStream_t st);
+cudaError_t launch_linprof(const GridDev& g, int N, const R* Y, const R* basey, int bstride, R* F, cudaStream_t st,
+                           const Dither& dt = kNoDither);
 // Rotation term added to the Chebyshev coefficients of N from the FP64 state U.
 template <typename R>
 cudaError_t launch_rotation(const GridDev& g, int N, const double* U, const double* Ub, int ustride, double rot,
@@ -63,13 +69,16 @@ size_t zcross_smem_bytes(const GridDev& g, int RP);
 // x passes: czc kz columns per block (0: as many as fit in shared memory)
 template <typename R>
 cudaError_t launch_xinv(const GridDev& g, const FftPlan& px, const cpx<R>* twx, const cpx<R>* W, cpx<R>* X, int ncomp,
-                        cudaStream_t st, int czc = 0);
+                        cudaStream_t st, int czc = 0, const Dither& dt = kNoDither);
 template <typename R>
 cudaError_t launch_zcross(const GridDev& g, const FftPlan& pz, const cpx<R>* twz, int RP, const cpx<R>* X, cpx<R>* Z,
-                          cudaStream_t st);
+                          cudaStream_t st, const Dither& dt = kNoDither);
 template <typename R>
 cudaError_t launch_xfwd(const GridDev& g, const FftPlan& px, const cpx<R>* twx, const cpx<R>* Z, cpx<R>* F, int ncomp,
-                        cudaStream_t st, int czc = 0);
+                        cudaStream_t st, int czc = 0, const Dither& dt = kNoDither);
+
+// Advance every field's constant version (after a nonlinear evaluation).
+cudaError_t launch_dither_bump(int* ver, int nb, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // Tau / Helmholtz per-mode tables (FP64), layout [field][n][m] with m the

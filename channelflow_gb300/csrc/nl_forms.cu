@@ -26,8 +26,8 @@ template <typename R, int MODE>
 __global__ void __launch_bounds__(256) k_grad_cheb(GridDev g, int N, const double* __restrict__ U, R* __restrict__ W,
                                                    const R* __restrict__ CA, const R* __restrict__ CB,
                                                    const R* __restrict__ DA, const R* __restrict__ DB,
-                                                   const R* __restrict__ basey, R Vsuck,
-                                                   int bstride) {
+                                                   const R* __restrict__ basey, double Vsuck,
+                                                   int bstride, Dither dt, int lpf) {
   extern __shared__ unsigned char smem_raw[];
   const int P = (N + 1) / 2, KA = (N + 1) / 2, KB = (N - 1) / 2, J = (N - 1) / 2;
   R* xs = reinterpret_cast<R*>(smem_raw);  // [3][N][TL]: even coefs rows 0..KA-1, odd KA..N-1
@@ -36,9 +36,16 @@ __global__ void __launch_bounds__(256) k_grad_cheb(GridDev g, int N, const doubl
   R* sDA = sCB + P * KB;
   R* sDB = sDA + P * KA;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int nlines = 2 * g.Md;
-  const int l0 = blockIdx.x * GC_TL;
-  const size_t row = (size_t)nlines, comp = row * N;
+  const size_t row = 2 * (size_t)g.Md, comp = row * N;
+  // blocks never straddle two fields (lpf lines each): a block uses its field's version of the constants
+  const int bpf = (lpf + GC_TL - 1) / GC_TL, fld = blockIdx.x / bpf;
+  const int nlines = (fld + 1) * lpf;  // one past this field's last line
+  const int l0 = fld * lpf + (blockIdx.x - fld * bpf) * GC_TL;
+  const int ver = dither_ver(dt, fld);
+  CA = dither_ptr(CA, ver, dt.S);
+  CB = dither_ptr(CB, ver, dt.S);
+  DA = dither_ptr(DA, ver, dt.S);
+  DB = dither_ptr(DB, ver, dt.S);
 #pragma unroll 8
   for (int i = tid; i < P * KA; i += blockDim.x) {
     sCA[i] = CA[i];
@@ -106,10 +113,11 @@ __global__ void __launch_bounds__(256) k_grad_cheb(GridDev g, int N, const doubl
   const int m = min(gl, nlines - 1) >> 1;
   const int part = gl & 1;
   const int kx = mode_kx(g, m), kz = mode_kz(g, m);
-  const R dx = (R)(2.0 * M_PI * kx / g.Lx * (kx == g.kxmax ? 0.0 : 1.0));
-  const R dz = (R)(2.0 * M_PI * kz / g.Lz * (kz == g.kzmax ? 0.0 : 1.0));
+  const R dx = dither_const<R>(2.0 * M_PI * kx / g.Lx * (kx == g.kxmax ? 0.0 : 1.0), ver);
+  const R dz = dither_const<R>(2.0 * M_PI * kz / g.Lz * (kz == g.kzmax ? 0.0 : 1.0), ver);
+  const R vs = dither_const<R>(Vsuck, ver);
   const bool base = (kx == 0 && kz == 0 && part == 0);
-  const R* __restrict__ by = basey + (size_t)bstride * mode_field(g, m);  // this field's base flow
+  const R* __restrict__ by = dither_ptr(basey, ver, dt.Sb) + (size_t)bstride * mode_field(g, m);  // this field's base flow
 #pragma unroll
   for (int i = 0; i < GC_PT; ++i) {
     const int p = warp + 8 * i;
@@ -129,7 +137,7 @@ __global__ void __launch_bounds__(256) k_grad_cheb(GridDev g, int N, const doubl
       if (base) {
         u[0] += by[j];
         u[2] += by[2 * N + j];
-        u[1] -= Vsuck;
+        u[1] -= vs;
         if (MODE == 1) {
           dy[0] += by[N + j];
           dy[2] += by[3 * N + j];
@@ -212,9 +220,10 @@ __device__ __forceinline__ void phys_products(const R* c, R* f) {
 
 template <typename R, int FORM>
 __global__ void __launch_bounds__(256) k_zphys(GridDev g, FftPlan pz, const cpx<R>* __restrict__ twz, int RP,
-                                               const cpx<R>* __restrict__ X, cpx<R>* __restrict__ Z) {
+                                               const cpx<R>* __restrict__ X, cpx<R>* __restrict__ Z, Dither dt) {
   constexpr int NC = FormIO<FORM>::NC, NO = FormIO<FORM>::NO;
   extern __shared__ unsigned char smem_raw[];
+  twz = dither_ptr(twz, dither_ver(dt, blockIdx.y % dt.nb), dt.S);  // plane blockIdx.y -> its field's twiddles
   const int Nz = g.Nz, ss = Nz + 1, NKz = g.NKz;
   const int nseq = ((NC > NO ? NC : NO) * RP) / 2;
   const int ninv = NC * RP / 2, nfwd = NO * RP / 2;
@@ -294,7 +303,8 @@ __global__ void __launch_bounds__(256) k_cheb_fwd_div(GridDev g, int N, const R*
                                                       const R* __restrict__ pKx, const R* __restrict__ pKz,
                                                       const R* __restrict__ pD, R wF, R wK, R wD, R* __restrict__ out,
                                                       const R* __restrict__ FA, const R* __restrict__ FB,
-                                                      const R* __restrict__ DFA, const R* __restrict__ DFB) {
+                                                      const R* __restrict__ DFA, const R* __restrict__ DFB, Dither dt,
+                                                      int lpf) {
   extern __shared__ unsigned char smem_raw[];
   const int P = (N + 1) / 2, J = (N - 1) / 2, KA = J + 1, KB = J;
   R* xs = reinterpret_cast<R*>(smem_raw);  // [4 inputs][KA s-rows + KB d-rows][TL]
@@ -303,9 +313,16 @@ __global__ void __launch_bounds__(256) k_cheb_fwd_div(GridDev g, int N, const R*
   R* sDA = sFB + P * KB;  // P x KB (acts on d)
   R* sDB = sDA + P * KB;  // P x KA (acts on s)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int nlines = 2 * g.Md;
-  const int l0 = blockIdx.x * CF_TL;
-  const size_t row = (size_t)nlines;
+  const size_t row = 2 * (size_t)g.Md;
+  // blocks never straddle two fields (lpf lines each): a block uses its field's version of the constants
+  const int bpf = (lpf + CF_TL - 1) / CF_TL, fld = blockIdx.x / bpf;
+  const int nlines = (fld + 1) * lpf;  // one past this field's last line
+  const int l0 = fld * lpf + (blockIdx.x - fld * bpf) * CF_TL;
+  const int ver = dither_ver(dt, fld);
+  FA = dither_ptr(FA, ver, dt.S);
+  FB = dither_ptr(FB, ver, dt.S);
+  DFA = dither_ptr(DFA, ver, dt.S);
+  DFB = dither_ptr(DFB, ver, dt.S);
 #pragma unroll 8
   for (int i = tid; i < P * KA; i += blockDim.x) {
     sFA[i] = FA[i];
@@ -378,8 +395,8 @@ __global__ void __launch_bounds__(256) k_cheb_fwd_div(GridDev g, int N, const R*
   const int m = min(gl, nlines - 1) >> 1;
   const int part = gl & 1;
   const int kx = mode_kx(g, m), kz = mode_kz(g, m);
-  const R dx = (R)(2.0 * M_PI * kx / g.Lx * (kx == g.kxmax ? 0.0 : 1.0));
-  const R dz = (R)(2.0 * M_PI * kz / g.Lz * (kz == g.kzmax ? 0.0 : 1.0));
+  const R dx = dither_const<R>(2.0 * M_PI * kx / g.Lx * (kx == g.kxmax ? 0.0 : 1.0), ver);
+  const R dz = dither_const<R>(2.0 * M_PI * kz / g.Lz * (kz == g.kzmax ? 0.0 : 1.0), ver);
 #pragma unroll
   for (int i = 0; i < CF_PT; ++i) {
     const int p = warp + 8 * i;
@@ -413,20 +430,23 @@ size_t grad_cheb_smem_bytes(int N) {
 template <typename R>
 cudaError_t launch_grad_cheb(const GridDev& g, int N, bool gradient, const double* U, R* W, const R* CA, const R* CB,
                              const R* DA, const R* DB, const R* basey, double Vsuck, cudaStream_t st,
-                             int bstride) {
+                             int bstride, const Dither& dt) {
   if ((N + 1) / 2 > 8 * GC_PT) return cudaErrorInvalidValue;
-  static bool attr_set = false;
-  if (!attr_set) {
+  // kernel attributes set once per process (thread-safe static initialisation)
+  static const bool attr_set = [] {
     cudaFuncSetAttribute(k_grad_cheb<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     cudaFuncSetAttribute(k_grad_cheb<R, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    attr_set = true;
-  }
-  const int nlines = 2 * g.Md;
-  const dim3 grid((nlines + GC_TL - 1) / GC_TL);
+    return true;
+  }();
+  (void)attr_set;
+  const int nf = dt.nb > 0 ? dt.nb : 1, lpf = 2 * g.Md / nf;
+  const dim3 grid(nf * ((lpf + GC_TL - 1) / GC_TL));
   if (gradient)
-    k_grad_cheb<R, 1><<<grid, 256, grad_cheb_smem_bytes<R>(N), st>>>(g, N, U, W, CA, CB, DA, DB, basey, (R)Vsuck, bstride);
+    k_grad_cheb<R, 1><<<grid, 256, grad_cheb_smem_bytes<R>(N), st>>>(g, N, U, W, CA, CB, DA, DB, basey, Vsuck, bstride,
+                                                                     dt, lpf);
   else
-    k_grad_cheb<R, 2><<<grid, 256, grad_cheb_smem_bytes<R>(N), st>>>(g, N, U, W, CA, CB, DA, DB, basey, (R)Vsuck, bstride);
+    k_grad_cheb<R, 2><<<grid, 256, grad_cheb_smem_bytes<R>(N), st>>>(g, N, U, W, CA, CB, DA, DB, basey, Vsuck, bstride,
+                                                                     dt, lpf);
   return cudaGetLastError();
 }
 
@@ -442,25 +462,26 @@ size_t zphys_smem_bytes(const GridDev& g, int form, int RP) {
 
 template <typename R, int FORM>
 static cudaError_t launch_zphys_t(const GridDev& g, const FftPlan& pz, const cpx<R>* twz, int RP, const cpx<R>* X,
-                                  cpx<R>* Z, cudaStream_t st) {
-  static bool attr_set = false;
-  if (!attr_set) {
+                                  cpx<R>* Z, cudaStream_t st, const Dither& dt) {
+  // kernel attributes set once per process (thread-safe static initialisation)
+  static const bool attr_set = [] {
     cudaFuncSetAttribute(k_zphys<R, FORM>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    attr_set = true;
-  }
+    return true;
+  }();
+  (void)attr_set;
   k_zphys<R, FORM><<<dim3((g.Nx + RP - 1) / RP, g.Ny), 256, zphys_smem_bytes<R>(g, FORM, RP), st>>>(g, pz, twz, RP,
-                                                                                                    X, Z);
+                                                                                                    X, Z, dt);
   return cudaGetLastError();
 }
 
 template <typename R>
 cudaError_t launch_zphys(const GridDev& g, int form, const FftPlan& pz, const cpx<R>* twz, int RP, const cpx<R>* X,
-                         cpx<R>* Z, cudaStream_t st) {
+                         cpx<R>* Z, cudaStream_t st, const Dither& dt) {
   switch (form) {
-    case NL_ROTATIONAL: return launch_zphys_t<R, NL_ROTATIONAL>(g, pz, twz, RP, X, Z, st);
-    case NL_CONVECTION: return launch_zphys_t<R, NL_CONVECTION>(g, pz, twz, RP, X, Z, st);
-    case NL_DIVERGENCE: return launch_zphys_t<R, NL_DIVERGENCE>(g, pz, twz, RP, X, Z, st);
-    default: return launch_zphys_t<R, NL_SKEW>(g, pz, twz, RP, X, Z, st);
+    case NL_ROTATIONAL: return launch_zphys_t<R, NL_ROTATIONAL>(g, pz, twz, RP, X, Z, st, dt);
+    case NL_CONVECTION: return launch_zphys_t<R, NL_CONVECTION>(g, pz, twz, RP, X, Z, st, dt);
+    case NL_DIVERGENCE: return launch_zphys_t<R, NL_DIVERGENCE>(g, pz, twz, RP, X, Z, st, dt);
+    default: return launch_zphys_t<R, NL_SKEW>(g, pz, twz, RP, X, Z, st, dt);
   }
 }
 
@@ -473,16 +494,17 @@ size_t cheb_fwd_div_smem_bytes(int N) {
 template <typename R>
 cudaError_t launch_cheb_fwd_div(const GridDev& g, int N, const R* pF, const R* pKx, const R* pKz, const R* pD, R wF,
                                 R wK, R wD, R* out, const R* FA, const R* FB, const R* DFA, const R* DFB,
-                                cudaStream_t st) {
+                                cudaStream_t st, const Dither& dt) {
   if ((N + 1) / 2 > 8 * CF_PT) return cudaErrorInvalidValue;
-  static bool attr_set = false;
-  if (!attr_set) {
+  // kernel attributes set once per process (thread-safe static initialisation)
+  static const bool attr_set = [] {
     cudaFuncSetAttribute(k_cheb_fwd_div<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    attr_set = true;
-  }
-  const int nlines = 2 * g.Md;
-  k_cheb_fwd_div<R><<<(nlines + CF_TL - 1) / CF_TL, 256, cheb_fwd_div_smem_bytes<R>(N), st>>>(
-      g, N, pF, pKx, pKz, pD, wF, wK, wD, out, FA, FB, DFA, DFB);
+    return true;
+  }();
+  (void)attr_set;
+  const int nf = dt.nb > 0 ? dt.nb : 1, lpf = 2 * g.Md / nf;
+  k_cheb_fwd_div<R><<<nf * ((lpf + CF_TL - 1) / CF_TL), 256, cheb_fwd_div_smem_bytes<R>(N), st>>>(
+      g, N, pF, pKx, pKz, pD, wF, wK, wD, out, FA, FB, DFA, DFB, dt, lpf);
   return cudaGetLastError();
 }
 
@@ -496,14 +518,15 @@ cudaError_t launch_cheb_fwd_div(const GridDev& g, int N, const R* pF, const R* p
 // ---------------------------------------------------------------------------
 template <typename R>
 __global__ void k_linprof(GridDev g, int N, const R* __restrict__ Y, const R* __restrict__ basey, int bstride,
-                          R* __restrict__ F) {
+                          R* __restrict__ F, Dither dt) {
   const size_t row = 2 * (size_t)g.Md, comp = row * N;
   const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (t >= (size_t)g.Md * N) return;
   const int m = (int)(t % g.Md), j = (int)(t / g.Md);
   const int kx = mode_kx(g, m), kz = mode_kz(g, m);
-  const R dx = (R)(2.0 * M_PI * kx / g.Lx), dz = (R)(2.0 * M_PI * kz / g.Lz);
-  const R* by = basey + (size_t)bstride * mode_field(g, m);
+  const int ver = dither_ver(dt, mode_field(g, m));
+  const R dx = dither_const<R>(2.0 * M_PI * kx / g.Lx, ver), dz = dither_const<R>(2.0 * M_PI * kz / g.Lz, ver);
+  const R* by = dither_ptr(basey, ver, dt.Sb) + (size_t)bstride * mode_field(g, m);
   const R U = by[j], Uy = by[N + j], W = by[2 * N + j], Wy = by[3 * N + j];
   const R d = U * dx + W * dz;  // (U d/dx + W d/dz) = i d
   const size_t o = (size_t)j * row + 2 * (size_t)m;
@@ -518,9 +541,10 @@ __global__ void k_linprof(GridDev g, int N, const R* __restrict__ Y, const R* __
 }
 
 template <typename R>
-cudaError_t launch_linprof(const GridDev& g, int N, const R* Y, const R* basey, int bstride, R* F, cudaStream_t st) {
+cudaError_t launch_linprof(const GridDev& g, int N, const R* Y, const R* basey, int bstride, R* F, cudaStream_t st,
+                           const Dither& dt) {
   const size_t total = (size_t)g.Md * N;
-  k_linprof<R><<<(unsigned)((total + 255) / 256), 256, 0, st>>>(g, N, Y, basey, bstride, F);
+  k_linprof<R><<<(unsigned)((total + 255) / 256), 256, 0, st>>>(g, N, Y, basey, bstride, F, dt);
   return cudaGetLastError();
 }
 
@@ -557,18 +581,30 @@ cudaError_t launch_rotation(const GridDev& g, int N, const double* U, const doub
 }
 
 #define INST_FORMS(R)                                                                                              \
-  template cudaError_t launch_linprof<R>(const GridDev&, int, const R*, const R*, int, R*, cudaStream_t);          \
+  template cudaError_t launch_linprof<R>(const GridDev&, int, const R*, const R*, int, R*, cudaStream_t,           \
+                                         const Dither&);                                                          \
   template cudaError_t launch_rotation<R>(const GridDev&, int, const double*, const double*, int, double, double,   \
                                           R*, cudaStream_t);                                                       \
   template size_t grad_cheb_smem_bytes<R>(int);                                                                    \
   template cudaError_t launch_grad_cheb<R>(const GridDev&, int, bool, const double*, R*, const R*, const R*,      \
-                                           const R*, const R*, const R*, double, cudaStream_t, int);               \
+                                           const R*, const R*, const R*, double, cudaStream_t, int, const Dither&); \
   template size_t zphys_smem_bytes<R>(const GridDev&, int, int);                                                   \
   template cudaError_t launch_zphys<R>(const GridDev&, int, const FftPlan&, const cpx<R>*, int, const cpx<R>*,      \
-                                       cpx<R>*, cudaStream_t);                                                     \
+                                       cpx<R>*, cudaStream_t, const Dither&);                                      \
   template size_t cheb_fwd_div_smem_bytes<R>(int);                                                                 \
   template cudaError_t launch_cheb_fwd_div<R>(const GridDev&, int, const R*, const R*, const R*, const R*, R, R, R, \
-                                              R*, const R*, const R*, const R*, const R*, cudaStream_t);
+                                              R*, const R*, const R*, const R*, const R*, cudaStream_t, const Dither&);
 
 INST_FORMS(float)
 INST_FORMS(double)
+
+// Advance every field's constant version after a nonlinear evaluation (one thread per field).
+__global__ void k_dither_bump(int* ver, int nb) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f < nb) ver[f] = (ver[f] + 1) % DITHER_V;
+}
+
+cudaError_t launch_dither_bump(int* ver, int nb, cudaStream_t st) {
+  k_dither_bump<<<(nb + 127) / 128, 128, 0, st>>>(ver, nb);
+  return cudaGetLastError();
+}

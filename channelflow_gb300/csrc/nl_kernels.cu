@@ -94,14 +94,20 @@ template <typename TI, typename R, typename TO>
 __global__ void __launch_bounds__(256) k_cheb(int N, int inverse, int nlines, const TI* __restrict__ in, size_t ld_in,
                                               size_t cs_in, TO* __restrict__ out, size_t ld_out, size_t cs_out,
                                               const R* __restrict__ Amat, const R* __restrict__ Bmat, int P, int KA,
-                                              int KB) {
+                                              int KB, Dither dt, int lpf) {
   extern __shared__ unsigned char smem_raw[];
   R* xa = reinterpret_cast<R*>(smem_raw);
   R* xb = xa + (size_t)KA * CHEB_TL;
   R* As = xb + (size_t)KB * CHEB_TL;
   R* Bs = As + (size_t)P * KA;
   const int tid = threadIdx.x;
-  const int l0 = blockIdx.x * CHEB_TL;
+  // blocks never straddle two fields (lpf lines each): a block uses its field's version of the matrices
+  const int bpf = (lpf + CHEB_TL - 1) / CHEB_TL, fld = blockIdx.x / bpf;
+  const int l0 = fld * lpf + (blockIdx.x - fld * bpf) * CHEB_TL;
+  nlines = min(nlines, (fld + 1) * lpf);
+  const int ver = dither_ver(dt, fld);
+  Amat = dither_ptr(Amat, ver, dt.S);
+  Bmat = dither_ptr(Bmat, ver, dt.S);
   const int c = blockIdx.y;
   in += c * cs_in;
   out += c * cs_out;
@@ -201,8 +207,8 @@ template <typename R>
 __global__ void __launch_bounds__(256) k_curl_cheb(GridDev g, int N, const double* __restrict__ U, R* __restrict__ W6,
                                                    const R* __restrict__ CA, const R* __restrict__ CB,
                                                    const R* __restrict__ DA, const R* __restrict__ DB,
-                                                   const R* __restrict__ basey, R Vsuck,
-                                                   int bstride) {
+                                                   const R* __restrict__ basey, double Vsuck,
+                                                   int bstride, Dither dt, int lpf) {
   extern __shared__ unsigned char smem_raw[];
   const int P = (N + 1) / 2, KA = (N + 1) / 2, KB = (N - 1) / 2, J = (N - 1) / 2;
   R* xs = reinterpret_cast<R*>(smem_raw);           // [3][N][CC_TL]: even coefs rows 0..KA-1, odd KA..N-1
@@ -211,9 +217,16 @@ __global__ void __launch_bounds__(256) k_curl_cheb(GridDev g, int N, const doubl
   R* sDA = sCB + P * KB;
   R* sDB = sDA + P * KA;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int nlines = 2 * g.Md;
-  const int l0 = blockIdx.x * CC_TL;
-  const size_t row = (size_t)nlines, comp = row * N;
+  const size_t row = 2 * (size_t)g.Md, comp = row * N;
+  // blocks never straddle two fields (lpf lines each): a block uses its field's version of the constants
+  const int bpf = (lpf + CC_TL - 1) / CC_TL, fld = blockIdx.x / bpf;
+  const int nlines = (fld + 1) * lpf;  // one past this field's last line
+  const int l0 = fld * lpf + (blockIdx.x - fld * bpf) * CC_TL;
+  const int ver = dither_ver(dt, fld);
+  CA = dither_ptr(CA, ver, dt.S);
+  CB = dither_ptr(CB, ver, dt.S);
+  DA = dither_ptr(DA, ver, dt.S);
+  DB = dither_ptr(DB, ver, dt.S);
 #pragma unroll 8
   for (int i = tid; i < P * KA; i += blockDim.x) {
     sCA[i] = CA[i];
@@ -268,10 +281,11 @@ __global__ void __launch_bounds__(256) k_curl_cheb(GridDev g, int N, const doubl
   const int m = min(gl, nlines - 1) >> 1;
   const int part = gl & 1;
   const int kx = mode_kx(g, m), kz = mode_kz(g, m);
-  const R dx = (R)(2.0 * M_PI * kx / g.Lx * (kx == g.kxmax ? 0.0 : 1.0));
-  const R dz = (R)(2.0 * M_PI * kz / g.Lz * (kz == g.kzmax ? 0.0 : 1.0));
+  const R dx = dither_const<R>(2.0 * M_PI * kx / g.Lx * (kx == g.kxmax ? 0.0 : 1.0), ver);
+  const R dz = dither_const<R>(2.0 * M_PI * kz / g.Lz * (kz == g.kzmax ? 0.0 : 1.0), ver);
+  const R vs = dither_const<R>(Vsuck, ver);
   const bool base = (kx == 0 && kz == 0 && part == 0);
-  const R* __restrict__ by = basey + (size_t)bstride * mode_field(g, m);  // this field's base flow
+  const R* __restrict__ by = dither_ptr(basey, ver, dt.Sb) + (size_t)bstride * mode_field(g, m);  // this field's base flow
 #pragma unroll
   for (int i = 0; i < CC_PT; ++i) {
     const int p = warp + 8 * i;
@@ -288,7 +302,7 @@ __global__ void __launch_bounds__(256) k_curl_cheb(GridDev g, int N, const doubl
         du += by[N + j];
         w += by[2 * N + j];
         dw += by[3 * N + j];
-        v -= Vsuck;
+        v -= vs;
       }
       const R ou = __shfl_xor_sync(0xffffffffu, u, 1);
       const R ov = __shfl_xor_sync(0xffffffffu, v, 1);
@@ -325,23 +339,25 @@ size_t curl_cheb_smem_bytes(int N) {
 template <typename R>
 cudaError_t launch_curl_cheb(const GridDev& g, int N, const double* U, R* W6, const R* CA, const R* CB, const R* DA,
                              const R* DB, const R* basey, double Vsuck, cudaStream_t st,
-                             int bstride) {
+                             int bstride, const Dither& dt) {
   if ((N + 1) / 2 > 8 * CC_PT) return cudaErrorInvalidValue;
-  static bool attr_set = false;
-  if (!attr_set) {
+  // kernel attributes set once per process (thread-safe static initialisation)
+  static const bool attr_set = [] {
     cudaFuncSetAttribute(k_curl_cheb<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    attr_set = true;
-  }
-  const int nlines = 2 * g.Md;
-  k_curl_cheb<R><<<(nlines + CC_TL - 1) / CC_TL, 256, curl_cheb_smem_bytes<R>(N), st>>>(g, N, U, W6, CA, CB, DA, DB,
-                                                                                         basey, (R)Vsuck, bstride);
+    return true;
+  }();
+  (void)attr_set;
+  const int nf = dt.nb > 0 ? dt.nb : 1, lpf = 2 * g.Md / nf;
+  k_curl_cheb<R><<<nf * ((lpf + CC_TL - 1) / CC_TL), 256, curl_cheb_smem_bytes<R>(N), st>>>(
+      g, N, U, W6, CA, CB, DA, DB, basey, Vsuck, bstride, dt, lpf);
   return cudaGetLastError();
 }
 template cudaError_t launch_curl_cheb<float>(const GridDev&, int, const double*, float*, const float*, const float*,
-                                             const float*, const float*, const float*, double, cudaStream_t, int);
+                                             const float*, const float*, const float*, double, cudaStream_t, int,
+                                             const Dither&);
 template cudaError_t launch_curl_cheb<double>(const GridDev&, int, const double*, double*, const double*,
                                               const double*, const double*, const double*, const double*, double,
-                                              cudaStream_t, int);
+                                              cudaStream_t, int, const Dither&);
 template size_t curl_cheb_smem_bytes<float>(int);
 template size_t curl_cheb_smem_bytes<double>(int);
 
@@ -353,8 +369,10 @@ template size_t curl_cheb_smem_bytes<double>(int);
 // ---------------------------------------------------------------------------
 template <typename R>
 __global__ void __launch_bounds__(256) k_xinv(GridDev g, FftPlan px, const cpx<R>* __restrict__ twx,
-                                              const cpx<R>* __restrict__ W, cpx<R>* __restrict__ X, int czc) {
+                                              const cpx<R>* __restrict__ W, cpx<R>* __restrict__ X, int czc,
+                                              Dither dt) {
   extern __shared__ unsigned char smem_raw[];
+  twx = dither_ptr(twx, dither_ver(dt, blockIdx.x % dt.nb), dt.S);  // plane blockIdx.x -> its field's twiddles
   const int ss = g.Nx + 1;
   const int iz0 = blockIdx.z * czc;
   const int nc = min(czc, g.NKz - iz0);
@@ -389,8 +407,9 @@ __global__ void __launch_bounds__(256) k_xinv(GridDev g, FftPlan px, const cpx<R
 // ---------------------------------------------------------------------------
 template <typename R>
 __global__ void __launch_bounds__(256) k_zcross(GridDev g, FftPlan pz, const cpx<R>* __restrict__ twz, int RP,
-                                                const cpx<R>* __restrict__ X, cpx<R>* __restrict__ Z) {
+                                                const cpx<R>* __restrict__ X, cpx<R>* __restrict__ Z, Dither dt) {
   extern __shared__ unsigned char smem_raw[];
+  twz = dither_ptr(twz, dither_ver(dt, blockIdx.y % dt.nb), dt.S);  // plane blockIdx.y -> its field's twiddles
   const int Nz = g.Nz, ss = Nz + 1, NKz = g.NKz;
   const int ninv = 3 * RP;  // inverse sequences
   cpx<R>* A = reinterpret_cast<cpx<R>*>(smem_raw);
@@ -474,8 +493,12 @@ __global__ void __launch_bounds__(256) k_zcross(GridDev g, FftPlan pz, const cpx
 // ---------------------------------------------------------------------------
 template <typename R>
 __global__ void __launch_bounds__(256) k_xfwd(GridDev g, FftPlan px, const cpx<R>* __restrict__ twx,
-                                              const cpx<R>* __restrict__ Z, cpx<R>* __restrict__ F, R scale, int czc) {
+                                              const cpx<R>* __restrict__ Z, cpx<R>* __restrict__ F, double scale_d,
+                                              int czc, Dither dt) {
   extern __shared__ unsigned char smem_raw[];
+  const int ver = dither_ver(dt, blockIdx.x % dt.nb);  // plane blockIdx.x -> its field's constants
+  twx = dither_ptr(twx, ver, dt.S);
+  const R scale = dither_const<R>(scale_d, ver);
   const int ss = g.Nx + 1;
   const int iz0 = blockIdx.z * czc;
   const int nc = min(czc, g.NKz - iz0);
@@ -519,7 +542,7 @@ size_t cheb_smem_bytes(int N, size_t rsize) {
 
 template <typename TI, typename R, typename TO>
 cudaError_t launch_cheb(int N, bool inverse, int nlines, int ncomp, const TI* in, size_t ld_in, size_t cs_in, TO* out,
-                        size_t ld_out, size_t cs_out, const R* A, const R* B, cudaStream_t st) {
+                        size_t ld_out, size_t cs_out, const R* A, const R* B, cudaStream_t st, const Dither& dt) {
   if ((N + 1) / 2 > CHEB_WARPS * CHEB_PT) return cudaErrorInvalidValue;
   const int P = (N + 1) / 2;
   int KA, KB;
@@ -531,14 +554,16 @@ cudaError_t launch_cheb(int N, bool inverse, int nlines, int ncomp, const TI* in
     KB = (N - 1) / 2;
   }
   const size_t sm = cheb_smem_bytes(N, sizeof(R));
-  static bool attr_set = false;
-  if (!attr_set) {
+  // kernel attributes set once per process (thread-safe static initialisation)
+  static const bool attr_set = [] {
     cudaFuncSetAttribute(k_cheb<TI, R, TO>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr_set = true;
-  }
-  dim3 grid((nlines + CHEB_TL - 1) / CHEB_TL, ncomp);
+    return true;
+  }();
+  (void)attr_set;
+  const int nf = dt.nb > 0 ? dt.nb : 1, lpf = (nlines + nf - 1) / nf;
+  dim3 grid(nf * ((lpf + CHEB_TL - 1) / CHEB_TL), ncomp);
   k_cheb<TI, R, TO><<<grid, 32 * CHEB_WARPS, sm, st>>>(N, inverse ? 1 : 0, nlines, in, ld_in, cs_in, out, ld_out,
-                                                       cs_out, A, B, P, KA, KB);
+                                                       cs_out, A, B, P, KA, KB, dt, lpf);
   return cudaGetLastError();
 }
 
@@ -562,42 +587,45 @@ size_t zcross_smem_bytes(const GridDev& g, int RP) {
 
 template <typename R>
 cudaError_t launch_xinv(const GridDev& g, const FftPlan& px, const cpx<R>* twx, const cpx<R>* W, cpx<R>* X, int ncomp,
-                        cudaStream_t st, int czc) {
-  static bool attr_set = false;
-  if (!attr_set) {
+                        cudaStream_t st, int czc, const Dither& dt) {
+  // kernel attributes set once per process (thread-safe static initialisation)
+  static const bool attr_set = [] {
     cudaFuncSetAttribute(k_xinv<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    attr_set = true;
-  }
+    return true;
+  }();
+  (void)attr_set;
   if (czc <= 0 || czc > g.NKz) czc = xfft_cols<R>(g);
   k_xinv<R><<<dim3(g.Ny, ncomp, (g.NKz + czc - 1) / czc), 256, xfft_smem_bytes<R>(g, czc), st>>>(g, px, twx, W, X,
-                                                                                               czc);
+                                                                                               czc, dt);
   return cudaGetLastError();
 }
 
 template <typename R>
 cudaError_t launch_zcross(const GridDev& g, const FftPlan& pz, const cpx<R>* twz, int RP, const cpx<R>* X, cpx<R>* Z,
-                          cudaStream_t st) {
-  static bool attr_set = false;
-  if (!attr_set) {
+                          cudaStream_t st, const Dither& dt) {
+  // kernel attributes set once per process (thread-safe static initialisation)
+  static const bool attr_set = [] {
     cudaFuncSetAttribute(k_zcross<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    attr_set = true;
-  }
-  k_zcross<R><<<dim3((g.Nx + RP - 1) / RP, g.Ny), 256, zcross_smem_bytes<R>(g, RP), st>>>(g, pz, twz, RP, X, Z);
+    return true;
+  }();
+  (void)attr_set;
+  k_zcross<R><<<dim3((g.Nx + RP - 1) / RP, g.Ny), 256, zcross_smem_bytes<R>(g, RP), st>>>(g, pz, twz, RP, X, Z, dt);
   return cudaGetLastError();
 }
 
 template <typename R>
 cudaError_t launch_xfwd(const GridDev& g, const FftPlan& px, const cpx<R>* twx, const cpx<R>* Z, cpx<R>* F, int ncomp,
-                        cudaStream_t st, int czc) {
-  static bool attr_set = false;
-  if (!attr_set) {
+                        cudaStream_t st, int czc, const Dither& dt) {
+  // kernel attributes set once per process (thread-safe static initialisation)
+  static const bool attr_set = [] {
     cudaFuncSetAttribute(k_xfwd<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    attr_set = true;
-  }
-  const R scale = (R)(1.0 / ((double)g.Nx * (double)g.Nz));
+    return true;
+  }();
+  (void)attr_set;
+  const double scale = 1.0 / ((double)g.Nx * (double)g.Nz);
   if (czc <= 0 || czc > g.NKz) czc = xfft_cols<R>(g);
   k_xfwd<R><<<dim3(g.Ny, ncomp, (g.NKz + czc - 1) / czc), 256, xfft_smem_bytes<R>(g, czc), st>>>(g, px, twx, Z, F,
-                                                                                               scale, czc);
+                                                                                               scale, czc, dt);
   return cudaGetLastError();
 }
 
@@ -605,11 +633,11 @@ cudaError_t launch_xfwd(const GridDev& g, const FftPlan& px, const cpx<R>* twx, 
   template cudaError_t launch_curl_base<R>(const GridDev&, const double*, R*, const double*, const double*, double, \
                                            cudaStream_t);                                                           \
   template cudaError_t launch_xinv<R>(const GridDev&, const FftPlan&, const cpx<R>*, const cpx<R>*, cpx<R>*, int,   \
-                                      cudaStream_t, int);                                                           \
+                                      cudaStream_t, int, const Dither&);                                            \
   template cudaError_t launch_zcross<R>(const GridDev&, const FftPlan&, const cpx<R>*, int, const cpx<R>*, cpx<R>*, \
-                                        cudaStream_t);                                                              \
+                                        cudaStream_t, const Dither&);                                               \
   template cudaError_t launch_xfwd<R>(const GridDev&, const FftPlan&, const cpx<R>*, const cpx<R>*, cpx<R>*, int,   \
-                                      cudaStream_t, int);                                                           \
+                                      cudaStream_t, int, const Dither&);                                            \
   template size_t xfft_smem_bytes<R>(const GridDev&, int);                                                             \
   template size_t zcross_smem_bytes<R>(const GridDev&, int);
 
@@ -617,8 +645,9 @@ INST_R(float)
 INST_R(double)
 
 template cudaError_t launch_cheb<double, double, double>(int, bool, int, int, const double*, size_t, size_t, double*,
-                                                         size_t, size_t, const double*, const double*, cudaStream_t);
+                                                         size_t, size_t, const double*, const double*, cudaStream_t,
+                                                         const Dither&);
 template cudaError_t launch_cheb<float, float, float>(int, bool, int, int, const float*, size_t, size_t, float*, size_t,
-                                                      size_t, const float*, const float*, cudaStream_t);
+                                                      size_t, const float*, const float*, cudaStream_t, const Dither&);
 template cudaError_t launch_cheb<float, float, double>(int, bool, int, int, const float*, size_t, size_t, double*,
-                                                       size_t, size_t, const float*, const float*, cudaStream_t);
+                                                       size_t, size_t, const float*, const float*, cudaStream_t, const Dither&);

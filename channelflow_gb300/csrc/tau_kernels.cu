@@ -1510,11 +1510,12 @@ cudaError_t launch_tau_solve(const GridDev& g, int N, const SolveParams& sp, con
   const int M0 = (N - 1) / 2 + 1;
   const size_t smem_t = tau_t_smem(N);
   if (smem_t <= 227 * 1024) {
-    static bool attr = false;
-    if (!attr) {
+    // kernel attributes set once per process (thread-safe static initialisation)
+    static const bool attr = [] {
       cudaFuncSetAttribute(k_tau_solve_t<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-      attr = true;
-    }
+      return true;
+    }();
+    (void)attr;
     const size_t smem_r = sizeof(double) * (((N + 1) & ~1) + (size_t)M0 * 32);
     k_tau_rhs<R><<<(12 * g.Md + 31) / 32, 32, smem_r, st>>>(g, N, sp, p);
     k_tau_solve_t<R><<<(4 * g.Md + 31) / 32, 32, smem_t, st>>>(g, N, sp, p, hb, tt);

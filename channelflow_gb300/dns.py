@@ -167,6 +167,14 @@ class DNS:
         L.check(self._lib.cfgpu_dns_cfl(self._h, C.byref(v)))
         return v.value
 
+    def nonlinear(self, u) -> np.ndarray:
+        """navierstokesNL(u) + zeroPaddedModes (nse.cpp:12-91, 383-391) with this DNS's flags and precision;
+        the DNS's own fields are untouched."""
+        u = np.ascontiguousarray(_as_field(u, self.grid, 3))
+        f = np.zeros_like(u)
+        L.check(self._lib.cfgpu_dns_nonlinear(self._h, L.dptr(u), L.dptr(f)))
+        return f
+
     def l2norm(self, field: int = 0) -> float:
         """L2Norm (normalize=true) of the current u (field 0) or q (field 1)."""
         v = C.c_double()

@@ -123,6 +123,11 @@ cfgpu_status cfgpu_dns_dPdx(cfgpu_dns dns, double* dPdx);
  * DealiasXZ (pi dt otherwise).  Needs Ny <= 111.
  */
 cfgpu_status cfgpu_dns_cfl(cfgpu_dns dns, double* cfl);
+/* navierstokesNL (channelflow/nse.h:20, nse.cpp:12-91) plus NSE::nonlinear's zeroPaddedModes
+ * (nse.cpp:383-391): f = N(u) with the DNS's base flow, nonlinearity, Vsuck and rotation flags, in its
+ * precision.  u and f: FlowField buffers of the DNS's nfields velocity fields; the DNS's own fields are not
+ * touched (an Alternating form flips, as the reference's flag does). */
+cfgpu_status cfgpu_dns_nonlinear(cfgpu_dns dns, const double* u, double* f);
 
 /* L2Norm(field, normalize=true) (channelflow/diffops.cpp:415-487) of the current u (field 0) or q (field 1). */
 cfgpu_status cfgpu_dns_l2norm(cfgpu_dns dns, int field, double* l2);
@@ -246,14 +251,17 @@ cfgpu_status cfgpu_ensemble_load_slot(cfgpu_dns dns, int slot, cfgpu_dns src);
  * `slots` fields (per-field nu, dt, base flow and constraint; a new ensemble is sized to the requests
  * of its key waiting at that moment); new requests are
  * admitted into free slots while others run (continuous batching), new ensembles only while their
- * estimated device bytes fit in max_bytes.  cfgpu_server_pump admits, advances every ensemble by at
- * most max_steps steps (ensembles overlap on their own streams) and collects finished requests;
+ * estimated device bytes fit in max_bytes.  Each ensemble is driven by its own host thread, which
+ * loads new requests into its slots (start-up steps in a one-field staging DNS), advances its fields in
+ * chunks of at most max_steps steps on its own stream and handles interval ends and finished requests;
+ * cfgpu_server_pump is the admission round (it waits up to 2 ms for progress) and sets max_steps;
  * *active = requests queued or running.  cfgpu_server_poll: *status 0 queued, 1 running, 2 done,
  * 3 failed (returns CFGPU_ENONFINITE); u receives the result when done; times = {submit, start, done}
  * in seconds of a monotonic clock.  stats = {device bytes, ensembles, slots, running, queued,
  * ensemble steps, field steps, chunks enqueued, dt changes, microseconds in admission, microseconds in
  * interval ends, microseconds creating ensembles, setting staging parameters, running staging steps,
- * loading slots} (15 values).  Not thread-safe: one thread drives a server.
+ * loading slots} (15 values; "ensembles" counts those created; host times are summed over the server's
+ * threads).  The calls take the server's lock; one thread at a time may call destroy.
  */
 typedef struct cfgpu_server_s* cfgpu_server;
 cfgpu_status cfgpu_server_create(long long max_bytes, int slots, int precision, cfgpu_server* out);

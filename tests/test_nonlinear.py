@@ -1,0 +1,52 @@
+"""The nonlinear term alone: cfgpu_dns_nonlinear against the oracle's navierstokesNL + zeroPaddedModes.
+
+navierstokesNL (channelflow/nse.cpp:12-91): base flow and Vsuck added to the
+(0,0) mode, rotational / convection / skew-symmetric / divergence forms
+(diffops.cpp:2229-2880), linearizedNL (diffops.cpp:3288-3361), the rotation
+term (nse.cpp:62-78); NSE::nonlinear zeroes the padded modes (nse.cpp:383-391).
+Tolerances: FP64 path 1e-12 relative L2 of f; mixed path (FP32 transforms and
+products) 1e-5.
+"""
+
+import numpy as np
+import pytest
+
+from oracle import cf_oracle as O
+from tests.helpers import COUETTE_BOX, POISEUILLE_BOX, rel_l2, to_cflags, to_cgrid
+
+CASES = [
+    ("couette_rotational", (16, 17, 16), COUETTE_BOX,
+     dict(baseflow=O.LaminarBase, ulowerwall=-1.0, uupperwall=1.0, nonlinearity=O.Rotational)),
+    ("couette_convection", (18, 17, 12), COUETTE_BOX,
+     dict(baseflow=O.LaminarBase, ulowerwall=-1.0, uupperwall=1.0, nonlinearity=O.Convection)),
+    ("poiseuille_skew", (24, 33, 24), POISEUILLE_BOX,
+     dict(baseflow=O.LaminarBase, constraint=O.BulkVelocity, Ubulk=2 / 3, nonlinearity=O.SkewSymmetric)),
+    ("poiseuille_divergence_vsuck", (16, 25, 16), POISEUILLE_BOX,
+     dict(baseflow=O.SuctionBase, Vsuck=0.01, nonlinearity=O.Divergence)),
+    ("couette_linearized", (16, 17, 16), COUETTE_BOX,
+     dict(baseflow=O.LaminarBase, ulowerwall=-1.0, uupperwall=1.0, nonlinearity=O.LinearAboutProfile)),
+    ("couette_rotation", (16, 17, 16), COUETTE_BOX,
+     dict(baseflow=O.LaminarBase, ulowerwall=-1.0, uupperwall=1.0, nonlinearity=O.Rotational, rotation=0.3)),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed", 1e-5)])
+@pytest.mark.parametrize("name,dims,box,fkw", CASES, ids=[c[0] for c in CASES])
+def test_nonlinear_matches_oracle(name, dims, box, fkw, precision, tol):
+    from channelflow_gb300 import DNS, build
+    build.build()
+    g = O.Grid(dims[0], dims[1], dims[2], *box)
+    fl = O.DNSFlags(nu=1 / 400, dt=0.02, **fkw)
+    u = np.ascontiguousarray(O.random_divfree_field(g, seed=77, norm=0.2))
+    q = np.zeros((1,) + u.shape[1:], complex)
+    ref, _ = O.NSE(g, fl, None, u).nonlinear(u)
+    d = DNS(u.copy(), to_cgrid(g), to_cflags(fl), precision=precision)
+    f = d.nonlinear(u)
+    assert rel_l2(f, ref, g) <= tol, rel_l2(f, ref, g)
+    # the DNS's own state is untouched
+    u2, q2 = np.zeros_like(u), np.zeros_like(q)
+    d.get_fields(u2, q2)
+    m = np.abs(u2) > 0
+    assert np.array_equal(u2[m], u[m])
+    d.close()
