@@ -117,3 +117,4 @@ __device__ __forceinline__ float dither_const<float>(double x, int k) {
   const float sp = nextafterf(a, 3.0e38f) - a;
   return __double2float_rn(x + dither_offset(k) * (double)sp);
 }
+

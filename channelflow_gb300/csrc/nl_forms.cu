@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(256) k_grad_cheb(GridDev g, int N, const doubl
   for (int t = 0; t < NT; ++t)
 #pragma unroll
     for (int i = 0; i < GC_PT; ++i) ae[t][i] = bo[t][i] = 0;
-  for (int k = 0; k < KA; ++k) {
+  for (int k = KA - 1; k >= 0; --k) {  // high n first: the small terms are summed before the large
     R x[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) x[c] = xs[(c * N + k) * GC_TL + lane];
@@ -90,7 +90,7 @@ __global__ void __launch_bounds__(256) k_grad_cheb(GridDev g, int N, const doubl
       }
     }
   }
-  for (int k = 0; k < KB; ++k) {
+  for (int k = KB - 1; k >= 0; --k) {
     R x[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) x[c] = xs[(c * N + KA + k) * GC_TL + lane];

@@ -141,7 +141,7 @@ __global__ void __launch_bounds__(256) k_cheb(int N, int inverse, int nlines, co
   R accA[CHEB_PT][2], accB[CHEB_PT][2];
 #pragma unroll
   for (int i = 0; i < CHEB_PT; ++i) accA[i][0] = accA[i][1] = accB[i][0] = accB[i][1] = (R)0;
-  for (int k = 0; k < KA; ++k) {
+  for (int k = KA - 1; k >= 0; --k) {  // high n first: the small terms are summed before the large
     const R x0 = xa[k * CHEB_TL + lane], x1 = xa[k * CHEB_TL + lane + 32];
 #pragma unroll
     for (int i = 0; i < CHEB_PT; ++i) {
@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(256) k_cheb(int N, int inverse, int nlines, co
       }
     }
   }
-  for (int k = 0; k < KB; ++k) {
+  for (int k = KB - 1; k >= 0; --k) {
     const R x0 = xb[k * CHEB_TL + lane], x1 = xb[k * CHEB_TL + lane + 32];
 #pragma unroll
     for (int i = 0; i < CHEB_PT; ++i) {
@@ -253,7 +253,7 @@ __global__ void __launch_bounds__(256) k_curl_cheb(GridDev g, int N, const doubl
   const R* xu = xs + lane;
   const R* xv = xs + N * CC_TL + lane;
   const R* xw = xs + 2 * N * CC_TL + lane;
-  for (int k = 0; k < KA; ++k) {
+  for (int k = KA - 1; k >= 0; --k) {  // high n first: the small terms are summed before the large
     const R u = xu[k * CC_TL], v = xv[k * CC_TL], w = xw[k * CC_TL];
 #pragma unroll
     for (int i = 0; i < CC_PT; ++i) {
@@ -265,7 +265,7 @@ __global__ void __launch_bounds__(256) k_curl_cheb(GridDev g, int N, const doubl
       }
     }
   }
-  for (int k = 0; k < KB; ++k) {
+  for (int k = KB - 1; k >= 0; --k) {
     const R u = xu[(KA + k) * CC_TL], v = xv[(KA + k) * CC_TL], w = xw[(KA + k) * CC_TL];
 #pragma unroll
     for (int i = 0; i < CC_PT; ++i) {
