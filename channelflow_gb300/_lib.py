@@ -66,6 +66,8 @@ _SIGS = {
     "cfgpu_dns_destroy": [C.c_void_p],
     "cfgpu_dns_cfl": [C.c_void_p, _PD],
     "cfgpu_dns_nonlinear": [C.c_void_p, _PD, _PD],
+    "cfgpu_set_host_access": [C.c_int],
+    "cfgpu_dns_host_access": [C.c_void_p, C.POINTER(C.c_int)],
     "cfgpu_measure_fp64": [_PD, _PD],
     "cfgpu_timestep_adjust_for_T": [C.c_void_p, C.c_double, _PI, _PI, _PD],
     "cfgpu_timestep_adjust": [C.c_void_p, C.c_double, _PI, _PI],

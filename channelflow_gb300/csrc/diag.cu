@@ -250,3 +250,83 @@ template cudaError_t launch_symmetry<float>(const GridDev&, int, int, int, const
                                             cudaStream_t);
 template cudaError_t launch_symmetry<double>(const GridDev&, int, int, int, const SymmetryDev&, int, const void*,
                                              void*, cudaStream_t);
+
+// ---------------------------------------------------------------------------
+// Direct host access (devices whose kernels reach pageable host memory through the host page tables,
+// as GB300 does over NVLink-C2C): FlowField buffers in host memory ([field][c][ny][mx][mz] complex,
+// channelflow/flowfield.h layout) are read into / written from the solved-mode layout
+// ([c][ny][field][m] complex) by one kernel, without host-side gathers or staging copies.  Consecutive
+// threads take consecutive kz of one (c, ny, kx) row: contiguous on both sides.  VEC: 16-byte accesses.
+// ---------------------------------------------------------------------------
+template <bool TO_DEVICE, bool VEC>
+__global__ void __launch_bounds__(256) k_host_modes(GridDev g, int Nd, int nf, int f0, int fstride,
+                                                    const double* __restrict__ src, double* __restrict__ dst) {
+  const int Mz = g.Nz / 2 + 1;
+  const size_t hfield = (size_t)2 * Nd * g.Ny * g.Nx * Mz;
+  const size_t total = (size_t)nf * Nd * g.Ny * g.Md;
+  const size_t step = (size_t)gridDim.x * blockDim.x;
+  for (size_t t0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t0 < total; t0 += 4 * step) {
+    size_t so[4], dof[4];
+    bool ok[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const size_t t = t0 + k * step;
+      ok[k] = t < total;
+      const size_t tt = ok[k] ? t : 0;
+      const int iz = (int)(tt % g.NKz);
+      size_t r = tt / g.NKz;
+      const int ix = (int)(r % g.NKx);
+      r /= g.NKx;
+      const int ny = (int)(r % g.Ny);
+      r /= g.Ny;
+      const int c = (int)(r % Nd);
+      const int f = (int)(r / Nd);
+      const int kx = ix <= g.Kx ? ix : ix - g.NKx;
+      const int mx = kx >= 0 ? kx : kx + g.Nx;
+      const size_t h = f * hfield + 2 * ((((size_t)c * g.Ny + ny) * g.Nx + mx) * Mz + iz);
+      const size_t dv = 2 * ((((size_t)c * g.Ny + ny) * fstride + (f0 + f)) * g.Md + (size_t)ix * g.NKz + iz);
+      so[k] = TO_DEVICE ? h : dv;
+      dof[k] = TO_DEVICE ? dv : h;
+    }
+    if (VEC) {
+      double2 v[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (ok[k]) v[k] = *reinterpret_cast<const double2*>(src + so[k]);
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (ok[k]) *reinterpret_cast<double2*>(dst + dof[k]) = v[k];
+    } else {
+      double a[4], b[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (ok[k]) {
+          a[k] = src[so[k]];
+          b[k] = src[so[k] + 1];
+        }
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (ok[k]) {
+          dst[dof[k]] = a[k];
+          dst[dof[k] + 1] = b[k];
+        }
+    }
+  }
+}
+
+cudaError_t launch_host_modes(const GridDev& g, bool to_device, int Nd, int nf, int f0, int fstride, const double* src,
+                              double* dst, cudaStream_t st) {
+  const size_t total = (size_t)nf * Nd * g.Ny * g.Md;
+  if (total == 0) return cudaSuccess;
+  const size_t need = (total + 4 * 256 - 1) / (4 * 256);
+  const unsigned blocks = (unsigned)(need < 152 * 16 ? need : 152 * 16);
+  const bool vec = (((uintptr_t)src | (uintptr_t)dst) & 15) == 0;
+  if (to_device) {
+    if (vec) k_host_modes<true, true><<<blocks, 256, 0, st>>>(g, Nd, nf, f0, fstride, src, dst);
+    else k_host_modes<true, false><<<blocks, 256, 0, st>>>(g, Nd, nf, f0, fstride, src, dst);
+  } else {
+    if (vec) k_host_modes<false, true><<<blocks, 256, 0, st>>>(g, Nd, nf, f0, fstride, src, dst);
+    else k_host_modes<false, false><<<blocks, 256, 0, st>>>(g, Nd, nf, f0, fstride, src, dst);
+  }
+  return cudaGetLastError();
+}

@@ -596,6 +596,7 @@ struct cfgpu_dns_s {
   unsigned long long* dred = nullptr;  // reduction scratch (CFL key, L2 sum)
   unsigned long long* cfl_host = nullptr;  // pinned copy of the CFL keys (asynchronous CFL passes)
   double* stage1 = nullptr;                 // pinned staging of one field (slot transfers)
+  bool direct = false;  // kernels read/write the caller's FlowField buffers in host memory directly
   int alt[2] = {0, 0};  // Alternating state of the main (0) and init (1) NSE: 0 = next is divergence
   // state: current fields
   double *Ucur = nullptr, *Qcur = nullptr;
@@ -1209,6 +1210,11 @@ int ensure_stage(cfgpu_dns d) {
 }
 
 int set_fields(cfgpu_dns d, const double* u, const double* q) {
+  if (d->direct) {
+    if (u) CK(launch_host_modes(d->g, true, 3, d->nb, 0, d->nb, u, d->Ucur, d->st));
+    if (q) CK(launch_host_modes(d->g, true, 1, d->nb, 0, d->nb, q, d->Qcur, d->st));
+    return CFGPU_OK;  // the caller synchronizes before the buffers may change
+  }
   CKS(ensure_stage(d));
   const size_t cd = d->compc();
   if (u) {
@@ -1223,6 +1229,12 @@ int set_fields(cfgpu_dns d, const double* u, const double* q) {
 }
 
 int get_fields(cfgpu_dns d, double* u, double* q) {
+  if (d->direct) {
+    if (u) CK(launch_host_modes(d->g, false, 3, d->nb, 0, d->nb, d->Ucur, u, d->st));
+    if (q) CK(launch_host_modes(d->g, false, 1, d->nb, 0, d->nb, d->Qcur, q, d->st));
+    CK(cudaStreamSynchronize(d->st));
+    return CFGPU_OK;
+  }
   CKS(ensure_stage(d));
   const size_t cd = d->compc();
   CK(cudaMemcpyAsync(d->stage, d->Ucur, 3 * cd * sizeof(double), cudaMemcpyDeviceToHost, d->st));
@@ -1240,6 +1252,12 @@ int ensure_stage1(cfgpu_dns d) {
 }
 
 int set_slot(cfgpu_dns d, int slot, const double* u, const double* q) {
+  if (d->direct) {
+    if (u) CK(launch_host_modes(d->g, true, 3, 1, slot, d->nb, u, d->Ucur, d->st));
+    if (q) CK(launch_host_modes(d->g, true, 1, 1, slot, d->nb, q, d->Qcur, d->st));
+    CK(cudaStreamSynchronize(d->st));
+    return CFGPU_OK;
+  }
   CKS(ensure_stage1(d));
   double* stage = d->stage1;
   const size_t w = 2 * (size_t)d->g.Md, pitch = w * d->nb, cd1 = w * d->N;
@@ -1258,6 +1276,12 @@ int set_slot(cfgpu_dns d, int slot, const double* u, const double* q) {
 }
 
 int get_slot(cfgpu_dns d, int slot, double* u, double* q) {
+  if (d->direct) {
+    if (u) CK(launch_host_modes(d->g, false, 3, 1, slot, d->nb, d->Ucur, u, d->st));
+    if (q) CK(launch_host_modes(d->g, false, 1, 1, slot, d->nb, d->Qcur, q, d->st));
+    CK(cudaStreamSynchronize(d->st));
+    return CFGPU_OK;
+  }
   CKS(ensure_stage1(d));
   double* stage = d->stage1;
   const size_t w = 2 * (size_t)d->g.Md, pitch = w * d->nb, cd1 = w * d->N;
@@ -1328,6 +1352,7 @@ struct TuneKey {
 std::mutex g_tune_mu;
 std::map<TuneKey, std::pair<int, int>> g_tune;
 std::atomic<int> g_autotune{1};
+std::atomic<int> g_host_access{1};  // direct host-buffer access when the device supports it
 
 template <typename R>
 float time_ms(cfgpu_dns d, const std::function<cudaError_t()>& f) {
@@ -1444,6 +1469,14 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
   d->alt[0] = d->alt[1] = (f.nonlinearity == CFGPU_Alternating_) ? 1 : 0;
   CK(cudaGetDevice(&d->device));
   CK(cudaStreamCreateWithFlags(&d->st, cudaStreamNonBlocking));
+  {
+    // kernels may touch pageable host memory through the host page tables (no migration, no faults
+    // to service): FlowField buffers are then read and written in place
+    int ats = 0;
+    if (cudaDeviceGetAttribute(&ats, cudaDevAttrPageableMemoryAccessUsesHostPageTables, d->device) != cudaSuccess)
+      ats = 0;
+    d->direct = ats == 1 && g_host_access.load() != 0;
+  }
 
   // base flow and constraint (NSE::createCFBaseFlow, nse.cpp:589-632; NSE::initCFConstraint, nse.cpp:634-671)
   const double a = g.a, b = g.b;
@@ -2289,6 +2322,17 @@ cfgpu_status cfgpu_set_autotune(int enable) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_tune.clear();
   }
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_set_host_access(int enable) {
+  g_host_access.store(enable ? 1 : 0);
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_dns_host_access(cfgpu_dns d, int* direct) {
+  if (!d || !direct) return fail(CFGPU_EINVAL, "bad argument");
+  *direct = d->direct ? 1 : 0;
   return CFGPU_OK;
 }
 

@@ -80,6 +80,12 @@ cudaError_t launch_xfwd(const GridDev& g, const FftPlan& px, const cpx<R>* twx, 
 // Advance every field's constant version (after a nonlinear evaluation).
 cudaError_t launch_dither_bump(int* ver, int nb, cudaStream_t st);
 
+// FlowField buffer(s) in host memory (nf fields of Nd components) <-> solved modes of fields f0.. of a
+// batch of fstride fields on the device, read/written by the GPU directly (pageable memory through the
+// host page tables).  g: the one-field grid.
+cudaError_t launch_host_modes(const GridDev& g, bool to_device, int Nd, int nf, int f0, int fstride, const double* src,
+                              double* dst, cudaStream_t st);
+
 // ---------------------------------------------------------------------------
 // Tau / Helmholtz per-mode tables (FP64), layout [field][n][m] with m the
 // compact mode index (stride Md), plus per-mode scalars [s][m].

@@ -133,6 +133,12 @@ class DNS:
         L.check(self._lib.cfgpu_dns_advance_timed(self._h, int(nsteps), C.byref(ms)))
         return ms.value
 
+    def host_access(self) -> bool:
+        """True when this DNS reads and writes host FlowField buffers with its own kernels (no staging)."""
+        v = C.c_int()
+        L.check(self._lib.cfgpu_dns_host_access(self._h, C.byref(v)))
+        return bool(v.value)
+
     def set_graphs(self, enable: bool):
         """Replay steady-state steps from captured CUDA graphs (default) or launch every kernel."""
         L.check(self._lib.cfgpu_dns_set_graphs(self._h, int(bool(enable))))
@@ -299,3 +305,9 @@ def tau_solve_batched(N, kx, kz, Lx, Lz, a, b, lambda_t, nu, Rx, Ry, Rz, taucorr
                                         float(b), float(lambda_t), float(nu), int(bool(taucorrection)),
                                         *[L.dptr(r) for r in Rs], *[L.dptr(o) for o in outs]))
     return tuple(outs)
+
+
+def set_host_access(enable: bool):
+    """Direct host-buffer access for DNS objects created from now on (default: on where the device
+    supports it); off: host-side gathers and pinned staging copies."""
+    L.check(L.load().cfgpu_set_host_access(int(bool(enable))))

@@ -189,6 +189,12 @@ cfgpu_status cfgpu_dns_set_graphs(cfgpu_dns dns, int enable);
  * Ny * Nx * (Kz+1) >= 200000 planes' worth of work; results do not depend on the choice.  enable = 0 makes
  * later DNS objects use the defaults and clears the cache. */
 cfgpu_status cfgpu_set_autotune(int enable);
+/* Host FlowField buffers: on devices whose kernels reach pageable host memory through the host page
+ * tables (GB300 over NVLink-C2C), DNS objects created while enable != 0 (the default) read and write the
+ * caller's buffers with one kernel each way; otherwise through host-side gathers and pinned staging
+ * copies.  cfgpu_dns_host_access reports which path a DNS uses (1 direct, 0 staged). */
+cfgpu_status cfgpu_set_host_access(int enable);
+cfgpu_status cfgpu_dns_host_access(cfgpu_dns dns, int* direct);
 cfgpu_status cfgpu_dns_set_profiling(cfgpu_dns dns, int enable);
 cfgpu_status cfgpu_dns_phase_times(cfgpu_dns dns, double* nl_ms, long long* nl_count, double* tau_ms,
                                    long long* tau_count);
