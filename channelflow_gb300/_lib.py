@@ -67,6 +67,14 @@ _SIGS = {
     "cfgpu_dns_cfl": [C.c_void_p, _PD],
     "cfgpu_dns_nonlinear": [C.c_void_p, _PD, _PD],
     "cfgpu_set_host_access": [C.c_int],
+    "cfgpu_field2vector_size": [C.c_void_p, C.POINTER(C.c_longlong)],
+    "cfgpu_field2vector": [C.c_void_p, _PD, _PD],
+    "cfgpu_vector2field": [C.c_void_p, _PD, _PD],
+    "cfgpu_ensemble_field2vector": [C.c_void_p, C.c_int, _PD],
+    "cfgpu_ensemble_vector2field": [C.c_void_p, C.c_int, _PD],
+    "cfgpu_helmholtz_solve_batched": [C.c_int, C.c_int, C.c_double, C.c_double, _PD, C.c_double, _PD, _PD, _PD, _PD],
+    "cfgpu_helmholtz_solve_mean_batched": [C.c_int, C.c_int, C.c_double, C.c_double, _PD, C.c_double, _PD, _PD,
+                                           _PD, _PD, _PD, _PD],
     "cfgpu_dns_host_access": [C.c_void_p, C.POINTER(C.c_int)],
     "cfgpu_measure_fp64": [_PD, _PD],
     "cfgpu_timestep_adjust_for_T": [C.c_void_p, C.c_double, _PI, _PI, _PD],

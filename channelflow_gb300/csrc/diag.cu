@@ -330,3 +330,178 @@ cudaError_t launch_host_modes(const GridDev& g, bool to_device, int Nd, int nf, 
   }
   return cudaGetLastError();
 }
+
+// ---------------------------------------------------------------------------
+// field2vector / vector2field (channelflow/flowfield.cpp:4448-4760) on a field in the solved-mode layout
+// (field f of a batch of fstride fields).  The vector holds the independent real coefficients of a
+// divergence-free no-slip velocity: the (0,0) block (u, w real, n = 2..Ny-1), then one block of 4Ny-12
+// per mode in the reference's order ((kx,0) kx = 1..Kx; (0,kz) kz = 1..Kz; (kx,kz) kx = -Kx..Kx, kx != 0,
+// kz = 1..Kz): first component cA at n = 2..Ny-1, then cB at n = 3..Ny-2, re/im interleaved, with
+// (cA, cB) = (w, u) for the (kx,0) modes and (u, w) otherwise.  ord[j] = solved-mode index of block j;
+// blk[m] = block of mode m (-1: the (0,0) mode; -(j+2): the conjugate of block j, kz = 0 and kx < 0).
+// ---------------------------------------------------------------------------
+struct CLine {  // complex Chebyshev line of one mode: element n at p + n*s (re), +1 (im)
+  double* p;
+  size_t s;
+  __device__ __forceinline__ double& re(int n) const { return p[(size_t)n * s]; }
+  __device__ __forceinline__ double& im(int n) const { return p[(size_t)n * s + 1]; }
+};
+
+__global__ void k_field2vector(GridDev g, int f, int fstride, const int* __restrict__ ord, int nblk,
+                               const double* __restrict__ U, double* __restrict__ v) {
+  const int Ny = g.Ny, B = 4 * Ny - 12, off0 = 2 * (Ny - 2);
+  const size_t total = (size_t)off0 + (size_t)nblk * B;
+  const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  const size_t row = 2 * (size_t)g.Md * fstride, comp = row * Ny, fo = 2 * (size_t)g.Md * f;
+  if (t < (size_t)off0) {  // (0,0): u then w, real parts, n = 2..Ny-1
+    const int c = t < (size_t)(Ny - 2) ? 0 : 2, n = 2 + (int)(t % (Ny - 2));
+    v[t] = U[c * comp + n * row + fo];
+    return;
+  }
+  const size_t r = t - off0;
+  const int j = (int)(r / B), e = (int)(r % B);
+  const int m = ord[j];
+  const bool kz0 = mode_kz(g, m) == 0;
+  int c, n;
+  if (e < 2 * (Ny - 2)) {
+    c = kz0 ? 2 : 0;
+    n = 2 + e / 2;
+  } else {
+    c = kz0 ? 0 : 2;
+    n = 3 + (e - 2 * (Ny - 2)) / 2;
+  }
+  v[t] = U[c * comp + n * row + fo + 2 * (size_t)m + (e & 1)];
+}
+
+__device__ void cl_eval(const CLine& L, int N, double* a_re, double* a_im, double* b_re, double* b_im) {
+  double sar = 0, sai = 0, sbr = 0, sbi = 0;
+  for (int n = N - 1; n >= 0; --n) {
+    const double r = L.re(n), i = L.im(n);
+    sbr += r;
+    sbi += i;
+    if (n % 2 == 0) {
+      sar += r;
+      sai += i;
+    } else {
+      sar -= r;
+      sai -= i;
+    }
+  }
+  *a_re = sar, *a_im = sai, *b_re = sbr, *b_im = sbi;
+}
+__device__ void cl_mean(const CLine& L, int N, double* re, double* im) {
+  double sr = L.re(0), si = L.im(0);
+  for (int n = 2; n < N; n += 2) {
+    sr -= L.re(n) / (double)(n * n - 1);
+    si -= L.im(n) / (double)(n * n - 1);
+  }
+  *re = sr, *im = si;
+}
+__device__ void cl_fix_diri(const CLine& L, int N) {
+  double ar, ai, br, bi;
+  cl_eval(L, N, &ar, &ai, &br, &bi);
+  L.re(0) -= 0.5 * (br + ar), L.im(0) -= 0.5 * (bi + ai);
+  L.re(1) -= 0.5 * (br - ar), L.im(1) -= 0.5 * (bi - ai);
+}
+// f(a) = f(b) = 0 and mean(f) + extra = 0 through f[0..2] (fixDiriMean with extra = 0)
+__device__ void cl_fix_diri_mean(const CLine& L, int N, double xr, double xi) {
+  double ar, ai, br, bi, mr, mi;
+  cl_eval(L, N, &ar, &ai, &br, &bi);
+  cl_mean(L, N, &mr, &mi);
+  mr += xr, mi += xi;
+  L.re(0) -= 0.125 * (ar + br) + 0.75 * mr, L.im(0) -= 0.125 * (ai + bi) + 0.75 * mi;
+  L.re(1) -= 0.5 * (br - ar), L.im(1) -= 0.5 * (bi - ai);
+  L.re(2) -= 0.375 * (ar + br) - 0.75 * mr, L.im(2) -= 0.375 * (ai + bi) - 0.75 * mi;
+}
+// u = integrate(du) (zero mean), then u[0] -= (u(a) + u(b))/2, then u *= (0, k)
+__device__ void cl_integrate_v(const CLine& du, const CLine& u, int N, double h2, double k) {
+  u.re(1) = h2 * (du.re(0) - du.re(2) / 2), u.im(1) = h2 * (du.im(0) - du.im(2) / 2);
+  for (int n = 2; n < N - 1; ++n) {
+    u.re(n) = h2 * (du.re(n - 1) - du.re(n + 1)) / (2 * n);
+    u.im(n) = h2 * (du.im(n - 1) - du.im(n + 1)) / (2 * n);
+  }
+  u.re(N - 1) = h2 * du.re(N - 2) / (2 * (N - 1)), u.im(N - 1) = h2 * du.im(N - 2) / (2 * (N - 1));
+  u.re(0) = 0.0, u.im(0) = 0.0;
+  double mr, mi;
+  cl_mean(u, N, &mr, &mi);
+  u.re(0) = -mr, u.im(0) = -mi;
+  double ar, ai, br, bi;
+  cl_eval(u, N, &ar, &ai, &br, &bi);
+  u.re(0) -= 0.5 * (ar + br), u.im(0) -= 0.5 * (ai + bi);
+  if (k != 1.0)
+    for (int n = 0; n < N; ++n) {
+      const double r = u.re(n), i = u.im(n);
+      u.re(n) = -k * i, u.im(n) = k * r;
+    }
+}
+
+__global__ void k_vector2field(GridDev g, int f, int fstride, const int* __restrict__ blk,
+                               const double* __restrict__ v, double* __restrict__ U, double* __restrict__ W) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= g.Md) return;
+  const int Ny = g.Ny, B = 4 * Ny - 12, off0 = 2 * (Ny - 2);
+  const size_t row = 2 * (size_t)g.Md * fstride, comp = row * Ny, fo = 2 * (size_t)g.Md * f + 2 * (size_t)m;
+  const CLine Lu{U + fo, row}, Lv{U + comp + fo, row}, Lw{U + 2 * comp + fo, row};
+  const CLine Ls{W + 2 * (size_t)m, 2 * (size_t)g.Md};  // scratch line of this mode
+  const double h2 = (g.b - g.a) / 2;
+  const int b = blk[m];
+  for (int n = 0; n < Ny; ++n) {
+    Lu.re(n) = Lu.im(n) = Lv.re(n) = Lv.im(n) = Lw.re(n) = Lw.im(n) = 0.0;
+  }
+  if (b == -1) {  // (0,0): u and w real, v = 0
+    for (int n = 2; n < Ny; ++n) {
+      Lu.re(n) = v[n - 2];
+      Lw.re(n) = v[(Ny - 2) + n - 2];
+    }
+    cl_fix_diri(Lu, Ny);
+    cl_fix_diri(Lw, Ny);
+    return;
+  }
+  const int j = b >= 0 ? b : -(b + 2);
+  const double* a = v + off0 + (size_t)j * B;
+  const int kx = b >= 0 ? mode_kx(g, m) : -mode_kx(g, m), kz = mode_kz(g, m);
+  const double ax = 2 * M_PI * kx / g.Lx, gz = 2 * M_PI * kz / g.Lz;
+  const CLine& LA = kz == 0 ? Lw : Lu;  // first block part: n = 2..Ny-1
+  const CLine& LB = kz == 0 ? Lu : Lw;  // second part: n = 3..Ny-2
+  for (int n = 2; n < Ny; ++n) {
+    LA.re(n) = a[2 * (n - 2)];
+    LA.im(n) = a[2 * (n - 2) + 1];
+  }
+  cl_fix_diri(LA, Ny);
+  for (int n = 3; n < Ny - 1; ++n) {
+    LB.re(n) = a[2 * (Ny - 2) + 2 * (n - 3)];
+    LB.im(n) = a[2 * (Ny - 2) + 2 * (n - 3) + 1];
+  }
+  if (kz == 0 || kx == 0) {
+    cl_fix_diri_mean(LB, Ny, 0.0, 0.0);
+    cl_integrate_v(LB, Lv, Ny, h2, kz == 0 ? -ax : -gz);  // v = int(-d/dx u) or int(-d/dz w)
+  } else {
+    const double r = (double)(kx * g.Lz) / (kz * g.Lx);
+    Lw.re(Ny - 1) = -Lu.re(Ny - 1) * r, Lw.im(Ny - 1) = -Lu.im(Ny - 1) * r;
+    double mr, mi;
+    cl_mean(Lu, Ny, &mr, &mi);
+    cl_fix_diri_mean(Lw, Ny, r * mr, r * mi);
+    // v = int(-i ax u - i gz w) dy
+    for (int n = 0; n < Ny; ++n) {
+      Ls.re(n) = ax * Lu.im(n) + gz * Lw.im(n);
+      Ls.im(n) = -(ax * Lu.re(n) + gz * Lw.re(n));
+    }
+    cl_integrate_v(Ls, Lv, Ny, h2, 1.0);
+  }
+  if (b < -1)  // kz = 0, kx < 0: the conjugate of (|kx|, 0)
+    for (int n = 0; n < Ny; ++n) Lu.im(n) = -Lu.im(n), Lv.im(n) = -Lv.im(n), Lw.im(n) = -Lw.im(n);
+}
+
+cudaError_t launch_field2vector(const GridDev& g, int f, int fstride, const int* ord, int nblk, const double* U,
+                                double* v, cudaStream_t st) {
+  const size_t total = 2 * (size_t)(g.Ny - 2) + (size_t)nblk * (4 * g.Ny - 12);
+  k_field2vector<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(g, f, fstride, ord, nblk, U, v);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_vector2field(const GridDev& g, int f, int fstride, const int* blk, const double* v, double* U,
+                                double* W, cudaStream_t st) {
+  k_vector2field<<<(g.Md + 63) / 64, 64, 0, st>>>(g, f, fstride, blk, v, U, W);
+  return cudaGetLastError();
+}

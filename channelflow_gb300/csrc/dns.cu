@@ -2278,6 +2278,184 @@ cfgpu_status cfgpu_dns_symmetry(cfgpu_dns d, const cfgpu_symmetry* y, int projec
   return CFGPU_OK;
 }
 
+}  // extern "C"
+
+namespace {
+// Block order of the field <-> vector map (flowfield.cpp:4480-4557) over the solved set of g (dealiased):
+// ord[j] = solved-mode index of block j; blk[m] = block of mode m (-1: the (0,0) mode; -(j+2): kz = 0,
+// kx < 0, the conjugate of block j).
+void f2v_tables(const GridDev& g, std::vector<int>& ord, std::vector<int>& blk) {
+  auto midx = [&](int kx, int kz) { return (kx >= 0 ? kx : kx + g.NKx) * g.NKz + kz; };
+  ord.clear();
+  blk.assign(g.Md, -1);
+  for (int kx = 1; kx <= g.Kx; ++kx) {
+    blk[midx(kx, 0)] = (int)ord.size();
+    blk[midx(-kx, 0)] = -((int)ord.size() + 2);
+    ord.push_back(midx(kx, 0));
+  }
+  for (int kz = 1; kz <= g.Kz; ++kz) {
+    blk[midx(0, kz)] = (int)ord.size();
+    ord.push_back(midx(0, kz));
+  }
+  for (int kx = -g.Kx; kx <= g.Kx; ++kx) {
+    if (kx == 0) continue;
+    for (int kz = 1; kz <= g.Kz; ++kz) {
+      blk[midx(kx, kz)] = (int)ord.size();
+      ord.push_back(midx(kx, kz));
+    }
+  }
+}
+
+long long f2v_size(int Ny, int Kx, int Kz) {
+  return 2LL * (Ny - 2) + (long long)(Kx + Kz + 2 * Kx * Kz) * (4LL * Ny - 12);
+}
+
+// field f of a batch of fstride fields (device, solved-mode layout) -> vector in host memory
+int f2v_device(const GridDev& g, int f, int fstride, const double* U, double* v, cudaStream_t st) {
+  std::vector<int> ord, blk;
+  f2v_tables(g, ord, blk);
+  const size_t n = (size_t)f2v_size(g.Ny, g.Kx, g.Kz);
+  long long B = 0;
+  int* dord = nullptr;
+  double* dv = nullptr;
+  int status = CFGPU_OK;
+  auto body = [&]() -> int {
+    CKS(dalloc(&dord, ord.size(), B));
+    CKS(dalloc(&dv, n, B));
+    CK(cudaMemcpyAsync(dord, ord.data(), ord.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(launch_field2vector(g, f, fstride, dord, (int)ord.size(), U, dv, st));
+    CK(cudaMemcpyAsync(v, dv, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return CFGPU_OK;
+  };
+  status = body();
+  cudaStreamSynchronize(st);
+  dfree(dord);
+  dfree(dv);
+  return status;
+}
+
+// vector in host memory -> field f of a batch (device); every coefficient of that field's solved modes is set
+int v2f_device(const GridDev& g, int f, int fstride, const double* v, double* U, cudaStream_t st) {
+  std::vector<int> ord, blk;
+  f2v_tables(g, ord, blk);
+  const size_t n = (size_t)f2v_size(g.Ny, g.Kx, g.Kz);
+  long long B = 0;
+  int* dblk = nullptr;
+  double *dv = nullptr, *W = nullptr;
+  int status = CFGPU_OK;
+  auto body = [&]() -> int {
+    CKS(dalloc(&dblk, blk.size(), B));
+    CKS(dalloc(&dv, n, B));
+    CKS(dalloc(&W, 2 * (size_t)g.Md * g.Ny, B));
+    CK(cudaMemcpyAsync(dblk, blk.data(), blk.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dv, v, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    CK(launch_vector2field(g, f, fstride, dblk, dv, U, W, st));
+    CK(cudaStreamSynchronize(st));
+    return CFGPU_OK;
+  };
+  status = body();
+  cudaStreamSynchronize(st);
+  dfree(dblk);
+  dfree(dv);
+  dfree(W);
+  return status;
+}
+
+int f2v_grid(const cfgpu_grid* grid, cfgpu_dns_s& tmp) {
+  if (!grid || grid->Nx < 6 || grid->Nz < 6 || grid->Ny < 5 || grid->Nx % 2 || grid->Nz % 2)
+    return fail(CFGPU_EINVAL, "bad grid (Nx, Nz even >= 6, Ny >= 5)");
+  GridDev& g = tmp.g;
+  g.Nx = grid->Nx; g.Ny = grid->Ny; g.Nz = grid->Nz;
+  g.Kx = grid->Nx / 3 - 1;
+  g.Kz = grid->Nz / 3 - 1;
+  g.NKx = 2 * g.Kx + 1;
+  g.NKz = g.Kz + 1;
+  g.Md = g.NKx * g.NKz;
+  g.kxmax = grid->Nx / 2;
+  g.kzmax = grid->Nz / 2;
+  g.Lx = grid->Lx; g.Lz = grid->Lz; g.a = grid->a; g.b = grid->b;
+  tmp.N = grid->Ny;
+  tmp.nb = 1;
+  return CFGPU_OK;
+}
+}  // namespace
+
+extern "C" {
+
+cfgpu_status cfgpu_field2vector_size(const cfgpu_grid* grid, long long* n) {
+  cfgpu_dns_s tmp;
+  if (!n) return fail(CFGPU_EINVAL, "bad argument");
+  CKS(f2v_grid(grid, tmp));
+  *n = f2v_size(tmp.g.Ny, tmp.g.Kx, tmp.g.Kz);
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_field2vector(const cfgpu_grid* grid, const double* u, double* v) {
+  cfgpu_dns_s tmp;  // mode set only; no DNS is built
+  if (!u || !v) return fail(CFGPU_EINVAL, "bad argument");
+  CKS(f2v_grid(grid, tmp));
+  const size_t n = 3 * tmp.compc();
+  std::vector<double> h(n);
+  gather_modes(&tmp, u, 3, h.data());
+  cudaStream_t st = nullptr;
+  CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  long long B = 0;
+  double* U = nullptr;
+  int status = dalloc(&U, n, B);
+  if (status == CFGPU_OK) {
+    const cudaError_t e = cudaMemcpyAsync(U, h.data(), n * sizeof(double), cudaMemcpyHostToDevice, st);
+    status = e == cudaSuccess ? f2v_device(tmp.g, 0, 1, U, v, st) : fail(CFGPU_ECUDA, cudaGetErrorString(e));
+  }
+  cudaStreamSynchronize(st);
+  dfree(U);
+  cudaStreamDestroy(st);
+  return status;
+}
+
+cfgpu_status cfgpu_vector2field(const cfgpu_grid* grid, const double* v, double* u) {
+  cfgpu_dns_s tmp;
+  if (!u || !v) return fail(CFGPU_EINVAL, "bad argument");
+  CKS(f2v_grid(grid, tmp));
+  const size_t n = 3 * tmp.compc();
+  std::vector<double> h(n);
+  cudaStream_t st = nullptr;
+  CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  long long B = 0;
+  double* U = nullptr;
+  int status = dalloc(&U, n, B);
+  if (status == CFGPU_OK) status = v2f_device(tmp.g, 0, 1, v, U, st);
+  if (status == CFGPU_OK) {
+    cudaError_t e = cudaMemcpyAsync(h.data(), U, n * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) status = fail(CFGPU_ECUDA, cudaGetErrorString(e));
+  }
+  cudaStreamSynchronize(st);
+  dfree(U);
+  cudaStreamDestroy(st);
+  if (status != CFGPU_OK) return status;
+  const GridDev& g = tmp.g;
+  memset(u, 0, sizeof(double) * 3 * 2 * (size_t)g.Ny * g.Nx * (g.Nz / 2 + 1));
+  scatter_modes(&tmp, h.data(), 3, u);
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_ensemble_field2vector(cfgpu_dns d, int slot, double* v) {
+  if (!d || !v || slot < 0 || slot >= d->nb) return fail(CFGPU_EINVAL, "bad argument");
+  if (d->g.Kx != d->g.Nx / 3 - 1 || d->g.Kz != d->g.Nz / 3 - 1 || d->N < 5)
+    return fail(CFGPU_ENOTSUP, "field2vector needs the 2/3-dealiased mode set");
+  CK(cudaStreamSynchronize(d->st));
+  return f2v_device(d->g, slot, d->nb, d->Ucur, v, d->st);
+}
+
+cfgpu_status cfgpu_ensemble_vector2field(cfgpu_dns d, int slot, const double* v) {
+  if (!d || !v || slot < 0 || slot >= d->nb) return fail(CFGPU_EINVAL, "bad argument");
+  if (d->g.Kx != d->g.Nx / 3 - 1 || d->g.Kz != d->g.Nz / 3 - 1 || d->N < 5)
+    return fail(CFGPU_ENOTSUP, "vector2field needs the 2/3-dealiased mode set");
+  CK(cudaStreamSynchronize(d->st));
+  return v2f_device(d->g, slot, d->nb, v, d->Ucur, d->st);
+}
+
 cfgpu_status cfgpu_field_symmetry(const cfgpu_grid* grid, int dealias, int Nd, const cfgpu_symmetry* y, int project,
                                   double* u) {
   if (!grid || !y || !u || (Nd != 1 && Nd != 3) || grid->Nx < 4 || grid->Nz < 4 || grid->Ny < 2)
@@ -2446,6 +2624,83 @@ cfgpu_status cfgpu_dns_destroy(cfgpu_dns d) {
   cudaStreamSynchronize(d->st);
   dns_free(d);
   return CFGPU_OK;
+}
+
+}  // extern "C"
+
+namespace {
+// HelmholtzSolver(N, a, b, lambda_s, nu).solve for nsys systems at once (helmholtz.cpp:18-95); with umean the
+// mean-constrained solve (helmholtz.cpp:158-213).  Host arrays [nsys][N] (ChebyCoeff data per system).
+int helmholtz_batched(int N, int nsys, double a, double b, const double* lambda, double nu, const double* f,
+                      const double* ua, const double* ub, const double* umean, double* u, double* mu) {
+  if (N < 3 || N % 2 == 0) return fail(CFGPU_EINVAL, "N must be odd and >= 3 (HelmholtzSolver asserts odd N)");
+  if (nsys < 1 || !lambda || !f || !u || !(b > a) || nu == 0.0) return fail(CFGPU_EINVAL, "bad argument");
+  const size_t FN = (size_t)N * nsys;
+  std::vector<double> ft(FN), hbv;
+  for (int sy = 0; sy < nsys; ++sy)
+    for (int n = 0; n < N; ++n) ft[(size_t)n * nsys + sy] = f[(size_t)sy * N + n];
+  std::vector<double> lo, di, up;
+  make_helm_b(N, lo, di, up);
+  long long B = 0;
+  double *dl = nullptr, *df = nullptr, *dua = nullptr, *dub = nullptr, *dum = nullptr, *du = nullptr, *dmu = nullptr;
+  double *dW = nullptr, *dhb = nullptr;
+  cudaStream_t st = nullptr;
+  int status = CFGPU_OK;
+  auto body = [&]() -> int {
+    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    CKS(dalloc(&dl, nsys, B));
+    CKS(dalloc(&df, FN, B));
+    CKS(dalloc(&du, FN, B));
+    CKS(dalloc(&dW, 7 * FN, B));
+    CKS(dalloc(&dhb, 3 * (size_t)N, B));
+    CK(cudaMemcpyAsync(dl, lambda, nsys * sizeof(double), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(df, ft.data(), FN * sizeof(double), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dhb, lo.data(), N * sizeof(double), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dhb + N, di.data(), N * sizeof(double), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dhb + 2 * N, up.data(), N * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (ua) {
+      CKS(dalloc(&dua, nsys, B));
+      CK(cudaMemcpyAsync(dua, ua, nsys * sizeof(double), cudaMemcpyHostToDevice, st));
+    }
+    if (ub) {
+      CKS(dalloc(&dub, nsys, B));
+      CK(cudaMemcpyAsync(dub, ub, nsys * sizeof(double), cudaMemcpyHostToDevice, st));
+    }
+    if (umean) {
+      CKS(dalloc(&dum, nsys, B));
+      CKS(dalloc(&dmu, nsys, B));
+      CK(cudaMemcpyAsync(dum, umean, nsys * sizeof(double), cudaMemcpyHostToDevice, st));
+    }
+    HelmB hb{dhb, dhb + N, dhb + 2 * N};
+    CK(launch_helmholtz(N, nsys, a, b, dl, nu, hb, df, dua, dub, dum, du, dmu, dW, st));
+    CK(cudaMemcpyAsync(ft.data(), du, FN * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (umean && mu) CK(cudaMemcpyAsync(mu, dmu, nsys * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return CFGPU_OK;
+  };
+  status = body();
+  if (st) cudaStreamSynchronize(st);
+  for (double* p : {dl, df, dua, dub, dum, du, dmu, dW, dhb}) dfree(p);
+  if (st) cudaStreamDestroy(st);
+  if (status != CFGPU_OK) return status;
+  for (int sy = 0; sy < nsys; ++sy)
+    for (int n = 0; n < N; ++n) u[(size_t)sy * N + n] = ft[(size_t)n * nsys + sy];
+  return CFGPU_OK;
+}
+}  // namespace
+
+extern "C" {
+
+cfgpu_status cfgpu_helmholtz_solve_batched(int N, int nsys, double a, double b, const double* lambda, double nu,
+                                           const double* f, const double* ua, const double* ub, double* u) {
+  return helmholtz_batched(N, nsys, a, b, lambda, nu, f, ua, ub, nullptr, u, nullptr);
+}
+
+cfgpu_status cfgpu_helmholtz_solve_mean_batched(int N, int nsys, double a, double b, const double* lambda, double nu,
+                                                const double* f, const double* umean, const double* ua,
+                                                const double* ub, double* u, double* mu) {
+  if (!umean) return fail(CFGPU_EINVAL, "bad argument");
+  return helmholtz_batched(N, nsys, a, b, lambda, nu, f, ua, ub, umean, u, mu);
 }
 
 cfgpu_status cfgpu_tau_solve_batched(int N, int nmodes, const int* kx, const int* kz, double Lx, double Lz, double a,

@@ -77,6 +77,14 @@ template <typename R>
 cudaError_t launch_xfwd(const GridDev& g, const FftPlan& px, const cpx<R>* twx, const cpx<R>* Z, cpx<R>* F, int ncomp,
                         cudaStream_t st, int czc = 0, const Dither& dt = kNoDither);
 
+// field2vector / vector2field on field f of a batch of fstride fields in the solved-mode layout (one-field
+// grid g, dealiased): ord = solved-mode index of each vector block, blk = block of each mode; W: 2 Md Ny
+// doubles of scratch.
+cudaError_t launch_field2vector(const GridDev& g, int f, int fstride, const int* ord, int nblk, const double* U,
+                                double* v, cudaStream_t st);
+cudaError_t launch_vector2field(const GridDev& g, int f, int fstride, const int* blk, const double* v, double* U,
+                                double* W, cudaStream_t st);
+
 // Advance every field's constant version (after a nonlinear evaluation).
 cudaError_t launch_dither_bump(int* ver, int nb, cudaStream_t st);
 
@@ -110,6 +118,12 @@ struct HelmB {
   const double* di;
   const double* up;
 };
+
+// Batched HelmholtzSolver: nsys systems, lines [n][nsys]; umean null: plain solve, else mean-constrained
+// (mu out).  W: 7 N nsys doubles of work space.
+cudaError_t launch_helmholtz(int N, int nsys, double a, double b, const double* lambda, double nu, const HelmB& hb,
+                             const double* f, const double* ua, const double* ub, const double* umean, double* u,
+                             double* mu, double* W, cudaStream_t st);
 
 // Tables of modes m0 .. m0+mcount-1 of g (mcount <= 0: all modes) for lambda_t and nu.
 cudaError_t launch_tau_setup(const GridDev& g, int N, double lambda_t, double nu, const HelmB& hb, TauTable tt,

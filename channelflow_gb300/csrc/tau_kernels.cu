@@ -261,6 +261,51 @@ cudaError_t launch_tau_setup_batch(const GridDev& g, int N, const TauSetupBatch&
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Batched HelmholtzSolver (helmholtz.cpp:18-95, 158-213): one thread per system
+// nu u'' - lambda_s u = f_s (+ mu_s), u(a) = ua_s, u(b) = ub_s, with the
+// mean-constrained variant when umean is given.  Lines are [n][nsys] (W holds
+// 7 work lines: 4 UL factors, 2 scratch, f copy).
+// ---------------------------------------------------------------------------
+__global__ void k_helmholtz(int N, int nsys, double a, double b, const double* __restrict__ lambda, double nu,
+                           HelmB hb, const double* __restrict__ f, const double* __restrict__ ua,
+                           const double* __restrict__ ub, const double* __restrict__ umean, double* __restrict__ u,
+                           double* __restrict__ mu, double* __restrict__ W) {
+  const int sidx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (sidx >= nsys) return;
+  const size_t s = nsys, FN = (size_t)N * nsys;
+  auto L = [&](double* base) { return Ln{base + sidx, s}; };
+  HelmFac F{L(W), L(W + FN), L(W + 2 * FN), L(W + 3 * FN)};
+  helm_build(N, a, b, lambda[sidx], nu, F);
+  Ln fl = Ln{const_cast<double*>(f) + sidx, s}, ul = L(u), t0 = L(W + 4 * FN), t1 = L(W + 5 * FN);
+  const double A = ua ? ua[sidx] : 0.0, B = ub ? ub[sidx] : 0.0;
+  if (!umean) {
+    helm_solve(F, hb, N, fl, ul, A, B);
+    return;
+  }
+  // mean-constrained: mu = nu (umean - mean(u_f)) / mean(u_1), u_1 solving nu u'' - lambda u = nu
+  helm_solve(F, hb, N, fl, t0, A, B);
+  const double uamean = cheb_mean(N, t0);
+  for (int n = 0; n < N; ++n) t1[n] = 0.0;
+  t1[0] = nu;
+  helm_solve(F, hb, N, t1, t0, 0.0, 0.0);
+  const double ucmean = cheb_mean(N, t0);
+  const double m = nu * (umean[sidx] - uamean) / ucmean;
+  Ln fc = L(W + 6 * FN);
+  for (int n = 0; n < N; ++n) fc[n] = fl[n];
+  fc[0] = fc[0] + m;
+  helm_solve(F, hb, N, fc, ul, A, B);
+  if (mu) mu[sidx] = m;
+}
+
+cudaError_t launch_helmholtz(int N, int nsys, double a, double b, const double* lambda, double nu, const HelmB& hb,
+                             const double* f, const double* ua, const double* ub, const double* umean, double* u,
+                             double* mu, double* W, cudaStream_t st) {
+  if (nsys <= 0) return cudaSuccess;
+  k_helmholtz<<<(nsys + 127) / 128, 128, 0, st>>>(N, nsys, a, b, lambda, nu, hb, f, ua, ub, umean, u, mu, W);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_tau_setup(const GridDev& g, int N, double lambda_t, double nu, const HelmB& hb, TauTable tt,
                              double* scratch, cudaStream_t st, int m0, int mcount) {
   TauSetupBatch tb{};

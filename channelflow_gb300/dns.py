@@ -133,6 +133,18 @@ class DNS:
         L.check(self._lib.cfgpu_dns_advance_timed(self._h, int(nsteps), C.byref(ms)))
         return ms.value
 
+    def field2vector(self, slot: int = 0) -> np.ndarray:
+        """field2vector of the resident velocity (of field `slot` of an ensemble), computed on the GPU."""
+        from .dsi import field2vector_size
+        v = np.zeros(field2vector_size(self.grid))
+        L.check(self._lib.cfgpu_ensemble_field2vector(self._h, int(slot), L.dptr(v)))
+        return v
+
+    def vector2field(self, v: np.ndarray, slot: int = 0):
+        """Set the resident velocity (of field `slot`) to vector2field(v), on the GPU; the pressure is kept."""
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        L.check(self._lib.cfgpu_ensemble_vector2field(self._h, int(slot), L.dptr(v)))
+
     def host_access(self) -> bool:
         """True when this DNS reads and writes host FlowField buffers with its own kernels (no staging)."""
         v = C.c_int()
@@ -311,3 +323,24 @@ def set_host_access(enable: bool):
     """Direct host-buffer access for DNS objects created from now on (default: on where the device
     supports it); off: host-side gathers and pinned staging copies."""
     L.check(L.load().cfgpu_set_host_access(int(bool(enable))))
+
+
+def helmholtz_solve_batched(a: float, b: float, lam, nu: float, f, ua=None, ub=None, umean=None):
+    """HelmholtzSolver(N, a, b, lambda_s, nu).solve for many systems (helmholtz.cpp:18-95): f is
+    [nsys][N] Chebyshev coefficients; returns u [nsys][N], or (u, mu) with umean given (the
+    mean-constrained solve, helmholtz.cpp:158-213)."""
+    f = np.ascontiguousarray(np.atleast_2d(np.asarray(f, dtype=np.float64)))
+    nsys, N = f.shape
+    lam = np.ascontiguousarray(np.broadcast_to(np.asarray(lam, dtype=np.float64), (nsys,)))
+    vec = lambda v: None if v is None else np.ascontiguousarray(np.broadcast_to(np.asarray(v, np.float64), (nsys,)))
+    ua, ub, umean = vec(ua), vec(ub), vec(umean)
+    u = np.zeros_like(f)
+    lib = L.load()
+    if umean is None:
+        L.check(lib.cfgpu_helmholtz_solve_batched(N, nsys, a, b, L.dptr(lam), nu, L.dptr(f), L.dptr(ua), L.dptr(ub),
+                                                  L.dptr(u)))
+        return u
+    mu = np.zeros(nsys)
+    L.check(lib.cfgpu_helmholtz_solve_mean_batched(N, nsys, a, b, L.dptr(lam), nu, L.dptr(f), L.dptr(umean),
+                                                   L.dptr(ua), L.dptr(ub), L.dptr(u), L.dptr(mu)))
+    return u, mu

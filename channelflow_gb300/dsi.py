@@ -59,3 +59,33 @@ def ft(u: np.ndarray, grid: Grid, flags: DNSFlags, timestep: TimeStep, T: float,
     L.check(L.load().cfgpu_ft(C.byref(gc), C.byref(fc), C.byref(tc), float(T), L.dptr(u), L.dptr(fu),
                               C.byref(cfl), prec))
     return fu, cfl.value
+
+
+def field2vector_size(grid: Grid) -> int:
+    """field2vector_size (flowfield.cpp:4448-4478): independent reals of a div-free no-slip field."""
+    n = C.c_longlong()
+    gc = grid.to_c()
+    L.check(L.load().cfgpu_field2vector_size(C.byref(gc), C.byref(n)))
+    return n.value
+
+
+def field2vector(u: np.ndarray, grid: Grid) -> np.ndarray:
+    """field2vector (flowfield.cpp:4480-4557), on the GPU."""
+    u = np.ascontiguousarray(u)
+    _as_field(u, grid, 3)
+    v = np.zeros(field2vector_size(grid))
+    gc = grid.to_c()
+    L.check(L.load().cfgpu_field2vector(C.byref(gc), L.dptr(u.view(np.float64)), L.dptr(v)))
+    return v
+
+
+def vector2field(v: np.ndarray, grid: Grid) -> np.ndarray:
+    """vector2field (flowfield.cpp:4559-4760), on the GPU: the div-free no-slip field with independent
+    coefficients v."""
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    if v.shape != (field2vector_size(grid),):
+        raise ValueError("vector has the wrong size")
+    u = np.zeros((3, grid.Ny, grid.Nx, grid.Nz // 2 + 1), dtype=np.complex128)
+    gc = grid.to_c()
+    L.check(L.load().cfgpu_vector2field(C.byref(gc), L.dptr(v), L.dptr(u.view(np.float64))))
+    return u

@@ -129,6 +129,19 @@ cfgpu_status cfgpu_dns_cfl(cfgpu_dns dns, double* cfl);
  * touched (an Alternating form flips, as the reference's flag does). */
 cfgpu_status cfgpu_dns_nonlinear(cfgpu_dns dns, const double* u, double* f);
 
+/*
+ * field2vector / vector2field (channelflow/flowfield.h:617-620, flowfield.cpp:4448-4760): the vector of the
+ * independent real coefficients of a divergence-free, no-slip velocity field (2/3-dealiased modes), the
+ * unknowns of cfDSI's Newton-Krylov searches (cfdsi.cpp:52-61).  vector2field rebuilds the other
+ * coefficients from the wall conditions and continuity and zeroes every other mode.  The _ensemble forms
+ * act on a field resident on the GPU (slot of an ensemble or the field of a DNS; the pressure is kept).
+ */
+cfgpu_status cfgpu_field2vector_size(const cfgpu_grid* grid, long long* n);
+cfgpu_status cfgpu_field2vector(const cfgpu_grid* grid, const double* u, double* v);
+cfgpu_status cfgpu_vector2field(const cfgpu_grid* grid, const double* v, double* u);
+cfgpu_status cfgpu_ensemble_field2vector(cfgpu_dns dns, int slot, double* v);
+cfgpu_status cfgpu_ensemble_vector2field(cfgpu_dns dns, int slot, const double* v);
+
 /* L2Norm(field, normalize=true) (channelflow/diffops.cpp:415-487) of the current u (field 0) or q (field 1). */
 cfgpu_status cfgpu_dns_l2norm(cfgpu_dns dns, int field, double* l2);
 
@@ -321,6 +334,19 @@ cfgpu_status cfgpu_ff_write(const char* path, int Nx, int Ny, int Nz, int Nd, do
                             double b, int padded, const double* data);
 cfgpu_status cfgpu_ff_read_header(const char* path, int* dims, double* geom, int* padded, char* state);
 cfgpu_status cfgpu_ff_read(const char* path, double* data, size_t ndoubles);
+
+/*
+ * HelmholtzSolver(N, a, b, lambda_s, nu).solve(u_s, f_s, ua_s, ub_s) (channelflow/helmholtz.h:29-38,
+ * helmholtz.cpp:18-95) for nsys systems at once: nu u'' - lambda_s u = f_s, u(a) = ua_s, u(b) = ub_s (ua/ub
+ * may be null: zero).  f and u are [nsys][N] Chebyshev coefficients (ChebyCoeff data per system); N odd.
+ * The _mean variant is solve(u, mu, f, umean, ua, ub) (helmholtz.cpp:158-213): mu_s is chosen so that
+ * mean(u_s) = umean_s with nu u'' - lambda u = f + mu.
+ */
+cfgpu_status cfgpu_helmholtz_solve_batched(int N, int nsys, double a, double b, const double* lambda, double nu,
+                                           const double* f, const double* ua, const double* ub, double* u);
+cfgpu_status cfgpu_helmholtz_solve_mean_batched(int N, int nsys, double a, double b, const double* lambda, double nu,
+                                                const double* f, const double* umean, const double* ua,
+                                                const double* ub, double* u, double* mu);
 
 /*
  * Batched TauSolver (channelflow/tausolver.cpp:81-176 constructor and

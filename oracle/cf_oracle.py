@@ -1378,6 +1378,149 @@ def solved_modes(g: Grid, dealias_xz: bool = True):
     return out
 
 
+# ---------------------------------------------------------------------------
+# Vector of the independent real coefficients of a divergence-free, no-slip
+# velocity field (field2vector / vector2field, flowfield.cpp:4448-4760; the
+# table of Gibson, Halcrow & Cvitanovic cited there).  The vector is what
+# cfDSI's Newton-Krylov search works on (cfdsi.cpp:52-61, 140).
+# ---------------------------------------------------------------------------
+
+def fix_diri(f: np.ndarray) -> np.ndarray:
+    """fixDiri (utilfuncs.cpp:712-719, complex form :757-760): f(a) = f(b) = 0 via f[0], f[1]."""
+    fa, fb = eval_a(f), eval_b(f)
+    f = np.array(f, copy=True)
+    f[0] = f[0] - 0.5 * (fb + fa)
+    f[1] = f[1] - 0.5 * (fb - fa)
+    return f
+
+
+def fix_diri_mean(f: np.ndarray) -> np.ndarray:
+    """fixDiriMean (utilfuncs.cpp:721-728): f(a) = f(b) = 0 and mean 0 via f[0], f[1], f[2]."""
+    fa, fb, fm = eval_a(f), eval_b(f), cmean(f)
+    f = np.array(f, copy=True)
+    f[0] = f[0] - (0.125 * (fa + fb) + 0.75 * fm)
+    f[1] = f[1] - 0.5 * (fb - fa)
+    f[2] = f[2] - (0.375 * (fa + fb) - 0.75 * fm)
+    return f
+
+
+def cintegrate(du: np.ndarray, a: float, b: float) -> np.ndarray:
+    """integrate (chebyshev.cpp:637-664, complex form :1243-1246), N >= 3: zero-mean antiderivative."""
+    N = du.shape[0]
+    h2 = (b - a) / 2
+    u = np.zeros_like(du)
+    u[1] = h2 * (du[0] - du[2] / 2)
+    for n in range(2, N - 1):
+        u[n] = h2 * (du[n - 1] - du[n + 1]) / (2 * n)
+    u[N - 1] = h2 * du[N - 2] / (2 * (N - 1))
+    u[0] = u[0] - cmean(u)
+    return u
+
+
+def field2vector_size(g: Grid) -> int:
+    """field2vector_size (flowfield.cpp:4448-4478)."""
+    Kx, Kz, Ny = g.Nx // 3 - 1, g.Nz // 3 - 1, g.Ny
+    return 2 * (Ny - 2) + (Kx + Kz + 2 * Kx * Kz) * (2 * (Ny - 2) + 2 * (Ny - 4))
+
+
+def _ri(c: np.ndarray) -> np.ndarray:
+    return np.column_stack([c.real, c.imag]).ravel()
+
+
+def field2vector(u: np.ndarray, g: Grid) -> np.ndarray:
+    """field2vector (flowfield.cpp:4480-4557): the independent real coefficients, in the reference's order."""
+    Kx, Kz, Ny = g.Nx // 3 - 1, g.Nz // 3 - 1, g.Ny
+    out = [u[0, 2:Ny, 0, 0].real, u[2, 2:Ny, 0, 0].real]
+    for kx in range(1, Kx + 1):
+        mx = g.mx(kx)
+        out += [_ri(u[2, 2:Ny, mx, 0]), _ri(u[0, 3:Ny - 1, mx, 0])]
+    for kz in range(1, Kz + 1):
+        out += [_ri(u[0, 2:Ny, 0, kz]), _ri(u[2, 3:Ny - 1, 0, kz])]
+    for kx in range(-Kx, Kx + 1):
+        if kx == 0:
+            continue
+        mx = g.mx(kx)
+        for kz in range(1, Kz + 1):
+            out += [_ri(u[0, 2:Ny, mx, kz]), _ri(u[2, 3:Ny - 1, mx, kz])]
+    return np.concatenate(out)
+
+
+def vector2field(a: np.ndarray, g: Grid) -> np.ndarray:
+    """vector2field (flowfield.cpp:4559-4760): the field whose independent coefficients are a, the others from
+    the no-slip BCs and continuity; (kz=0, kx<0) modes are the conjugates of kx>0."""
+    Kx, Kz, Ny = g.Nx // 3 - 1, g.Nz // 3 - 1, g.Ny
+    Lx, Lz, ya, yb = g.Lx, g.Lz, g.a, g.b
+    u = np.zeros((3, Ny, g.Nx, g.Mz), dtype=complex)
+    pos = [0]
+
+    def real(k):
+        v = a[pos[0]:pos[0] + k]
+        pos[0] += k
+        return v
+
+    def cplx(k):
+        v = a[pos[0]:pos[0] + 2 * k:2] + 1j * a[pos[0] + 1:pos[0] + 2 * k:2]
+        pos[0] += 2 * k
+        return v
+
+    f0 = np.zeros(Ny)
+    f0[2:] = real(Ny - 2)
+    u[0, :, 0, 0] = fix_diri(f0)
+    f2 = np.zeros(Ny)
+    f2[2:] = real(Ny - 2)
+    u[2, :, 0, 0] = fix_diri(f2)
+    for kx in range(1, Kx + 1):
+        mx = g.mx(kx)
+        f2 = np.zeros(Ny, complex)
+        f2[2:] = cplx(Ny - 2)
+        f2 = fix_diri(f2)
+        f0 = np.zeros(Ny, complex)
+        f0[3:Ny - 1] = cplx(Ny - 4)
+        f0 = fix_diri_mean(f0)
+        f1 = cintegrate(f0, ya, yb)
+        f1[0] = f1[0] - 0.5 * (eval_a(f1) + eval_b(f1))
+        f1 = f1 * complex(0.0, -(2 * PI * kx) / Lx)
+        u[0, :, mx, 0], u[1, :, mx, 0], u[2, :, mx, 0] = f0, f1, f2
+        mxm = g.mx(-kx)
+        u[:, :, mxm, 0] = np.conj(u[:, :, mx, 0])
+    for kz in range(1, Kz + 1):
+        f0 = np.zeros(Ny, complex)
+        f0[2:] = cplx(Ny - 2)
+        f0 = fix_diri(f0)
+        f2 = np.zeros(Ny, complex)
+        f2[3:Ny - 1] = cplx(Ny - 4)
+        f2 = fix_diri_mean(f2)
+        f1 = cintegrate(f2, ya, yb)
+        f1[0] = f1[0] - 0.5 * (eval_a(f1) + eval_b(f1))
+        f1 = f1 * complex(0.0, -(2 * PI * kz) / Lz)
+        u[0, :, 0, kz], u[1, :, 0, kz], u[2, :, 0, kz] = f0, f1, f2
+    for kx in range(-Kx, Kx + 1):
+        if kx == 0:
+            continue
+        mx = g.mx(kx)
+        for kz in range(1, Kz + 1):
+            f0 = np.zeros(Ny, complex)
+            f0[2:] = cplx(Ny - 2)
+            f0 = fix_diri(f0)
+            u[0, :, mx, kz] = f0
+            r = (kx * Lz) / (kz * Lx)
+            f2 = np.zeros(Ny, complex)
+            f2[3:Ny - 1] = cplx(Ny - 4)
+            f2[Ny - 1] = -f0[Ny - 1] * r
+            f2a, f2b = eval_a(f2), eval_b(f2)
+            f2m = cmean(f2) + r * cmean(f0)
+            f2[0] = f2[0] - (0.125 * (f2a + f2b) + 0.75 * f2m)
+            f2[1] = f2[1] - 0.5 * (f2b - f2a)
+            f2[2] = f2[2] - (0.375 * (f2a + f2b) - 0.75 * f2m)
+            u[2, :, mx, kz] = f2
+            g0 = f0 * complex(0, -2 * PI * kx / Lx) + f2 * complex(0, -2 * PI * kz / Lz)
+            f1 = cintegrate(g0, ya, yb)
+            f1[0] = f1[0] - 0.5 * (eval_a(f1) + eval_b(f1))
+            u[1, :, mx, kz] = f1
+    assert pos[0] == a.shape[0]
+    return u
+
+
 def random_divfree_field(g: Grid, seed: int, norm: float, decay_k: float = 0.5, decay_n: float = 0.7,
                          zero_mean_u: bool = False) -> np.ndarray:
     """Seeded divergence-free, no-slip perturbation with the workloads' spectral decay.
