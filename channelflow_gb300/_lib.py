@@ -68,6 +68,7 @@ _SIGS = {
     "cfgpu_dns_nonlinear": [C.c_void_p, _PD, _PD],
     "cfgpu_set_host_access": [C.c_int],
     "cfgpu_field2vector_size": [C.c_void_p, C.POINTER(C.c_longlong)],
+    "cfgpu_orthogonalize": [C.c_int, C.c_int, _PD, _PD, _PD],
     "cfgpu_field2vector": [C.c_void_p, _PD, _PD],
     "cfgpu_vector2field": [C.c_void_p, _PD, _PD],
     "cfgpu_ensemble_field2vector": [C.c_void_p, C.c_int, _PD],

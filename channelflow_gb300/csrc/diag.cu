@@ -505,3 +505,83 @@ cudaError_t launch_vector2field(const GridDev& g, int f, int fstride, const int*
   k_vector2field<<<(g.Md + 63) / 64, 64, 0, st>>>(g, f, fstride, blk, v, U, W);
   return cudaGetLastError();
 }
+
+// ---------------------------------------------------------------------------
+// GMRES orthogonalisation in FP64 (the Arnoldi step of nsolver/gmres.cpp:47-83): w is made orthogonal to
+// the k rows of V (k x n) by classical Gram-Schmidt applied twice, h_j = sum of both passes' projections,
+// h_k = |w| afterwards, w /= h_k.  Reductions are deterministic: per-block partial sums in a fixed order,
+// then one block sums the partials in index order.
+// ---------------------------------------------------------------------------
+#define ORTHO_T 256
+__device__ double block_sum(double v, double* sh) {
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int s = ORTHO_T / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+    __syncthreads();
+  }
+  const double r = sh[0];
+  __syncthreads();
+  return r;
+}
+
+// partial[j * nb + b] = sum over block b's slice of V[j][i] w[i] (j < k), or of w[i]^2 (j == k, V unused)
+__global__ void __launch_bounds__(ORTHO_T) k_ortho_dots(int n, int k, const double* __restrict__ V,
+                                                        const double* __restrict__ w, int norm_only,
+                                                        double* __restrict__ partial) {
+  __shared__ double sh[ORTHO_T];
+  const int nb = gridDim.x, b = blockIdx.x;
+  const int j = blockIdx.y;  // row (or the norm when norm_only)
+  const size_t per = ((size_t)n + nb - 1) / nb, i0 = (size_t)b * per, i1 = min((size_t)n, i0 + per);
+  double s = 0.0;
+  for (size_t i = i0 + threadIdx.x; i < i1; i += ORTHO_T) s += norm_only ? w[i] * w[i] : V[(size_t)j * n + i] * w[i];
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) partial[(size_t)j * nb + b] = s;
+}
+
+__global__ void __launch_bounds__(ORTHO_T) k_ortho_reduce(int nb, int rows, const double* __restrict__ partial,
+                                                          double* __restrict__ out, int accumulate) {
+  __shared__ double sh[ORTHO_T];
+  const int j = blockIdx.x;
+  if (j >= rows) return;
+  double s = 0.0;
+  for (int b = threadIdx.x; b < nb; b += ORTHO_T) s += partial[(size_t)j * nb + b];
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) out[j] = accumulate ? out[j] + s : s;
+}
+
+// w[i] -= sum_j c[j] V[j][i]
+__global__ void k_ortho_update(int n, int k, const double* __restrict__ V, const double* __restrict__ c,
+                               double* __restrict__ w) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= (size_t)n) return;
+  double s = w[i];
+  for (int j = 0; j < k; ++j) s -= c[j] * V[(size_t)j * n + i];
+  w[i] = s;
+}
+
+__global__ void k_ortho_scale(int n, const double* __restrict__ nrm2, double* __restrict__ w, double* __restrict__ h,
+                              int k) {
+  const double nrm = sqrt(nrm2[0]);
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i == 0) h[k] = nrm;
+  if (i < (size_t)n && nrm > 0.0) w[i] /= nrm;
+}
+
+// work: (k + 1) * 64 + k + 1 doubles
+cudaError_t launch_orthogonalize(int n, int k, const double* V, double* w, double* h, double* work,
+                                 cudaStream_t st) {
+  const int nb = 64;
+  double* partial = work;
+  double* c = work + (size_t)(k + 1) * nb;
+  for (int pass = 0; pass < 2 && k > 0; ++pass) {
+    k_ortho_dots<<<dim3(nb, k), ORTHO_T, 0, st>>>(n, k, V, w, 0, partial);
+    k_ortho_reduce<<<k, ORTHO_T, 0, st>>>(nb, k, partial, c, 0);
+    k_ortho_reduce<<<k, ORTHO_T, 0, st>>>(nb, k, partial, h, pass);  // h = pass 1 + pass 2 projections
+    k_ortho_update<<<(unsigned)(((size_t)n + 255) / 256), 256, 0, st>>>(n, k, V, c, w);
+  }
+  k_ortho_dots<<<dim3(nb, 1), ORTHO_T, 0, st>>>(n, 0, V, w, 1, partial);
+  k_ortho_reduce<<<1, ORTHO_T, 0, st>>>(nb, 1, partial, c, 0);
+  k_ortho_scale<<<(unsigned)(((size_t)n + 255) / 256), 256, 0, st>>>(n, c, w, h, k);
+  return cudaGetLastError();
+}

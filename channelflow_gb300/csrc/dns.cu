@@ -2383,6 +2383,32 @@ int f2v_grid(const cfgpu_grid* grid, cfgpu_dns_s& tmp) {
 
 extern "C" {
 
+cfgpu_status cfgpu_orthogonalize(int n, int k, const double* V, double* w, double* h) {
+  if (n < 1 || k < 0 || !w || !h || (k > 0 && !V)) return fail(CFGPU_EINVAL, "bad argument");
+  cudaStream_t st = nullptr;
+  CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  long long B = 0;
+  double *dV = nullptr, *dw = nullptr, *dh = nullptr, *work = nullptr;
+  auto body = [&]() -> int {
+    if (k > 0) CKS(dalloc(&dV, (size_t)k * n, B));
+    CKS(dalloc(&dw, n, B));
+    CKS(dalloc(&dh, (size_t)k + 1, B));
+    CKS(dalloc(&work, (size_t)(k + 1) * 64 + k + 1, B));
+    if (k > 0) CK(cudaMemcpyAsync(dV, V, (size_t)k * n * sizeof(double), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dw, w, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, st));
+    CK(launch_orthogonalize(n, k, dV, dw, dh, work, st));
+    CK(cudaMemcpyAsync(w, dw, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(h, dh, ((size_t)k + 1) * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return CFGPU_OK;
+  };
+  const int status = body();
+  cudaStreamSynchronize(st);
+  for (double* p : {dV, dw, dh, work}) dfree(p);
+  cudaStreamDestroy(st);
+  return status;
+}
+
 cfgpu_status cfgpu_field2vector_size(const cfgpu_grid* grid, long long* n) {
   cfgpu_dns_s tmp;
   if (!n) return fail(CFGPU_EINVAL, "bad argument");

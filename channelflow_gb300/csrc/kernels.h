@@ -85,6 +85,10 @@ cudaError_t launch_field2vector(const GridDev& g, int f, int fstride, const int*
 cudaError_t launch_vector2field(const GridDev& g, int f, int fstride, const int* blk, const double* v, double* U,
                                 double* W, cudaStream_t st);
 
+// Arnoldi step in FP64: w orthogonalised against the k rows of V (k x n, device), h[0..k-1] the projections,
+// h[k] = |w|, w normalised.  work: (k + 1) * 64 + k + 1 doubles.
+cudaError_t launch_orthogonalize(int n, int k, const double* V, double* w, double* h, double* work, cudaStream_t st);
+
 // Advance every field's constant version (after a nonlinear evaluation).
 cudaError_t launch_dither_bump(int* ver, int nb, cudaStream_t st);
 

@@ -136,6 +136,11 @@ cfgpu_status cfgpu_dns_nonlinear(cfgpu_dns dns, const double* u, double* f);
  * coefficients from the wall conditions and continuity and zeroes every other mode.  The _ensemble forms
  * act on a field resident on the GPU (slot of an ensemble or the field of a DNS; the pressure is kept).
  */
+/* The Arnoldi step of GMRES in FP64 on the GPU (nsolver/gmres.cpp:47-83 orthogonalises the new Krylov
+ * vector against the basis): w (n) is orthogonalised against the k rows of V (k x n, row-major) by classical
+ * Gram-Schmidt applied twice; h[j] = w.V_j summed over both passes (j < k), h[k] = |w| after, and w is
+ * normalised (unless h[k] == 0).  Host arrays. */
+cfgpu_status cfgpu_orthogonalize(int n, int k, const double* V, double* w, double* h);
 cfgpu_status cfgpu_field2vector_size(const cfgpu_grid* grid, long long* n);
 cfgpu_status cfgpu_field2vector(const cfgpu_grid* grid, const double* u, double* v);
 cfgpu_status cfgpu_vector2field(const cfgpu_grid* grid, const double* v, double* u);
