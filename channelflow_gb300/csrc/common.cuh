@@ -118,3 +118,29 @@ __device__ __forceinline__ float dither_const<float>(double x, int k) {
   return __double2float_rn(x + dither_offset(k) * (double)sp);
 }
 
+// 16-byte vector of R (LDS.128): four floats or two doubles.
+template <typename R>
+struct Vec16;
+template <>
+struct Vec16<float> {
+  typedef float4 T;
+};
+template <>
+struct Vec16<double> {
+  typedef double2 T;
+};
+
+// Matrix loads of the dense Chebyshev kernels whose FP64 form is bound by FP64 arithmetic: 16-byte vectors
+// for FP32 (fewer shared-memory instructions), scalars for FP64 (fewer registers).
+template <typename R>
+struct VecLds;
+template <>
+struct VecLds<float> {
+  typedef float4 T;
+  static constexpr int W = 4;
+};
+template <>
+struct VecLds<double> {
+  typedef double T;
+  static constexpr int W = 1;
+};

@@ -28,13 +28,17 @@ __global__ void __launch_bounds__(256) k_grad_cheb(GridDev g, int N, const doubl
                                                    const R* __restrict__ DA, const R* __restrict__ DB,
                                                    const R* __restrict__ basey, double Vsuck,
                                                    int bstride, Dither dt, int lpf) {
-  extern __shared__ unsigned char smem_raw[];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  typedef typename Vec16<R>::T V;
+  constexpr int VW = 16 / sizeof(R);
   const int P = (N + 1) / 2, KA = (N + 1) / 2, KB = (N - 1) / 2, J = (N - 1) / 2;
-  R* xs = reinterpret_cast<R*>(smem_raw);  // [3][N][TL]: even coefs rows 0..KA-1, odd KA..N-1
-  R* sCA = xs + 3 * N * GC_TL;
-  R* sCB = sCA + P * KA;
-  R* sDA = sCB + P * KB;
-  R* sDB = sDA + P * KA;
+  // coefficient rows padded to whole 16-byte vectors (zero-filled): the matrices are read VW columns per load
+  const int KAp = (KA + VW - 1) / VW * VW, KBp = (KB + VW - 1) / VW * VW, NP = KAp + KBp;
+  R* xs = reinterpret_cast<R*>(smem_raw);  // [3][NP][TL]: even coefs rows 0..KAp-1, odd KAp..NP-1
+  R* sCA = xs + 3 * NP * GC_TL;
+  R* sCB = sCA + P * KAp;
+  R* sDA = sCB + P * KBp;
+  R* sDB = sDA + P * KAp;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const size_t row = 2 * (size_t)g.Md, comp = row * N;
   // blocks never straddle two fields (lpf lines each): a block uses its field's version of the constants
@@ -47,22 +51,29 @@ __global__ void __launch_bounds__(256) k_grad_cheb(GridDev g, int N, const doubl
   DA = dither_ptr(DA, ver, dt.S);
   DB = dither_ptr(DB, ver, dt.S);
 #pragma unroll 8
-  for (int i = tid; i < P * KA; i += blockDim.x) {
-    sCA[i] = CA[i];
-    if (MODE == 1) sDA[i] = DA[i];
+  for (int i = tid; i < P * KAp; i += blockDim.x) {
+    const int pp = i / KAp, k = i - pp * KAp;
+    sCA[i] = k < KA ? CA[pp * KA + k] : (R)0;
+    if (MODE == 1) sDA[i] = k < KA ? DA[pp * KA + k] : (R)0;
   }
 #pragma unroll 8
-  for (int i = tid; i < P * KB; i += blockDim.x) {
-    sCB[i] = CB[i];
-    if (MODE == 1) sDB[i] = DB[i];
+  for (int i = tid; i < P * KBp; i += blockDim.x) {
+    const int pp = i / KBp, k = i - pp * KBp;
+    sCB[i] = k < KB ? CB[pp * KB + k] : (R)0;
+    if (MODE == 1) sDB[i] = k < KB ? DB[pp * KB + k] : (R)0;
+  }
+  for (int i = tid; i < 3 * (NP - N) * GC_TL; i += blockDim.x) {  // padding rows
+    const int l = i % GC_TL, t = i / GC_TL, c = t / (NP - N), e = t % (NP - N);
+    const int r = e < KAp - KA ? KA + e : KAp + KB + (e - (KAp - KA));
+    xs[(c * NP + r) * GC_TL + l] = (R)0;
   }
 #pragma unroll 4
   for (int i = tid; i < 3 * N * GC_TL; i += blockDim.x) {
     const int l = i % GC_TL, n = (i / GC_TL) % N, c = i / (GC_TL * N);
     const int gl = l0 + l;
     const R v = gl < nlines ? (R)U[c * comp + (size_t)n * row + gl] : (R)0;
-    const int r = (n & 1) ? KA + (n >> 1) : (n >> 1);
-    xs[(c * N + r) * GC_TL + l] = v;
+    const int r = (n & 1) ? KAp + (n >> 1) : (n >> 1);
+    xs[(c * NP + r) * GC_TL + l] = v;
   }
   __syncthreads();
   constexpr int NT = MODE == 1 ? 6 : 3;  // transforms: C u_c (3) and, for the gradient, CD u_c (3)
@@ -71,40 +82,57 @@ __global__ void __launch_bounds__(256) k_grad_cheb(GridDev g, int N, const doubl
   for (int t = 0; t < NT; ++t)
 #pragma unroll
     for (int i = 0; i < GC_PT; ++i) ae[t][i] = bo[t][i] = 0;
-  for (int k = KA - 1; k >= 0; --k) {  // high n first: the small terms are summed before the large
-    R x[3];
+  // high n first (the small terms are summed before the large), VW columns per matrix load
+  for (int kb = KAp / VW - 1; kb >= 0; --kb) {
+    R x[3][VW];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) x[c] = xs[(c * N + k) * GC_TL + lane];
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int e = 0; e < VW; ++e) x[c][e] = xs[(c * NP + kb * VW + e) * GC_TL + lane];
 #pragma unroll
     for (int i = 0; i < GC_PT; ++i) {
       const int p = warp + 8 * i;
       if (p < P) {
-        const R cc = sCA[p * KA + k];
+        const V c4 = *reinterpret_cast<const V*>(sCA + p * KAp + kb * VW);
+        const R* cc = reinterpret_cast<const R*>(&c4);
 #pragma unroll
-        for (int c = 0; c < 3; ++c) ae[c][i] += cc * x[c];
+        for (int e = VW - 1; e >= 0; --e)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) ae[c][i] += cc[e] * x[c][e];
         if (MODE == 1) {
-          const R d = sDA[p * KA + k];
+          const V d4 = *reinterpret_cast<const V*>(sDA + p * KAp + kb * VW);
+          const R* d = reinterpret_cast<const R*>(&d4);
 #pragma unroll
-          for (int c = 0; c < 3; ++c) ae[3 + c][i] += d * x[c];
+          for (int e = VW - 1; e >= 0; --e)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) ae[3 + c][i] += d[e] * x[c][e];
         }
       }
     }
   }
-  for (int k = KB - 1; k >= 0; --k) {
-    R x[3];
+  for (int kb = KBp / VW - 1; kb >= 0; --kb) {
+    R x[3][VW];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) x[c] = xs[(c * N + KA + k) * GC_TL + lane];
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int e = 0; e < VW; ++e) x[c][e] = xs[(c * NP + KAp + kb * VW + e) * GC_TL + lane];
 #pragma unroll
     for (int i = 0; i < GC_PT; ++i) {
       const int p = warp + 8 * i;
       if (p < P) {
-        const R cc = sCB[p * KB + k];
+        const V c4 = *reinterpret_cast<const V*>(sCB + p * KBp + kb * VW);
+        const R* cc = reinterpret_cast<const R*>(&c4);
 #pragma unroll
-        for (int c = 0; c < 3; ++c) bo[c][i] += cc * x[c];
+        for (int e = VW - 1; e >= 0; --e)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) bo[c][i] += cc[e] * x[c][e];
         if (MODE == 1) {
-          const R d = sDB[p * KB + k];
+          const V d4 = *reinterpret_cast<const V*>(sDB + p * KBp + kb * VW);
+          const R* d = reinterpret_cast<const R*>(&d4);
 #pragma unroll
-          for (int c = 0; c < 3; ++c) bo[3 + c][i] += d * x[c];
+          for (int e = VW - 1; e >= 0; --e)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) bo[3 + c][i] += d[e] * x[c][e];
         }
       }
     }
@@ -423,8 +451,9 @@ __global__ void __launch_bounds__(256) k_cheb_fwd_div(GridDev g, int N, const R*
 // ---------------------------------------------------------------------------
 template <typename R>
 size_t grad_cheb_smem_bytes(int N) {
-  const int P = (N + 1) / 2, KA = (N + 1) / 2, KB = (N - 1) / 2;
-  return sizeof(R) * ((size_t)3 * N * GC_TL + 2 * (size_t)P * (KA + KB));
+  const int VW = 16 / sizeof(R);
+  const int P = (N + 1) / 2, KAp = ((N + 1) / 2 + VW - 1) / VW * VW, KBp = ((N - 1) / 2 + VW - 1) / VW * VW;
+  return sizeof(R) * ((size_t)3 * (KAp + KBp) * GC_TL + 2 * (size_t)P * (KAp + KBp));
 }
 
 template <typename R>

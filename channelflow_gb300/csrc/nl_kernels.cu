@@ -95,11 +95,15 @@ __global__ void __launch_bounds__(256) k_cheb(int N, int inverse, int nlines, co
                                               size_t cs_in, TO* __restrict__ out, size_t ld_out, size_t cs_out,
                                               const R* __restrict__ Amat, const R* __restrict__ Bmat, int P, int KA,
                                               int KB, Dither dt, int lpf) {
-  extern __shared__ unsigned char smem_raw[];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  typedef typename VecLds<R>::T V;
+  constexpr int VW = VecLds<R>::W;
+  // rows padded to whole 16-byte vectors (zero-filled): the matrices are read VW columns per load
+  const int KAp = (KA + VW - 1) / VW * VW, KBp = (KB + VW - 1) / VW * VW;
   R* xa = reinterpret_cast<R*>(smem_raw);
-  R* xb = xa + (size_t)KA * CHEB_TL;
-  R* As = xb + (size_t)KB * CHEB_TL;
-  R* Bs = As + (size_t)P * KA;
+  R* xb = xa + (size_t)KAp * CHEB_TL;
+  R* As = xb + (size_t)KBp * CHEB_TL;
+  R* Bs = As + (size_t)P * KAp;
   const int tid = threadIdx.x;
   // blocks never straddle two fields (lpf lines each): a block uses its field's version of the matrices
   const int bpf = (lpf + CHEB_TL - 1) / CHEB_TL, fld = blockIdx.x / bpf;
@@ -113,9 +117,17 @@ __global__ void __launch_bounds__(256) k_cheb(int N, int inverse, int nlines, co
   out += c * cs_out;
   const int J = (N - 1) / 2;
 #pragma unroll 8
-  for (int i = tid; i < P * KA; i += blockDim.x) As[i] = Amat[i];
+  for (int i = tid; i < P * KAp; i += blockDim.x) {
+    const int p = i / KAp, k = i - p * KAp;
+    As[i] = k < KA ? Amat[p * KA + k] : (R)0;
+  }
 #pragma unroll 8
-  for (int i = tid; i < P * KB; i += blockDim.x) Bs[i] = Bmat[i];
+  for (int i = tid; i < P * KBp; i += blockDim.x) {
+    const int p = i / KBp, k = i - p * KBp;
+    Bs[i] = k < KB ? Bmat[p * KB + k] : (R)0;
+  }
+  for (int i = tid; i < (KAp - KA) * CHEB_TL; i += blockDim.x) xa[KA * CHEB_TL + i] = (R)0;
+  for (int i = tid; i < (KBp - KB) * CHEB_TL; i += blockDim.x) xb[KB * CHEB_TL + i] = (R)0;
   // stage inputs
 #pragma unroll 4
   for (int i = tid; i < N * CHEB_TL; i += blockDim.x) {
@@ -141,27 +153,46 @@ __global__ void __launch_bounds__(256) k_cheb(int N, int inverse, int nlines, co
   R accA[CHEB_PT][2], accB[CHEB_PT][2];
 #pragma unroll
   for (int i = 0; i < CHEB_PT; ++i) accA[i][0] = accA[i][1] = accB[i][0] = accB[i][1] = (R)0;
-  for (int k = KA - 1; k >= 0; --k) {  // high n first: the small terms are summed before the large
-    const R x0 = xa[k * CHEB_TL + lane], x1 = xa[k * CHEB_TL + lane + 32];
+  // high n first (the small terms are summed before the large), VW columns per matrix load
+  for (int kb = KAp / VW - 1; kb >= 0; --kb) {
+    R x0[VW], x1[VW];
+#pragma unroll
+    for (int e = 0; e < VW; ++e) {
+      x0[e] = xa[(kb * VW + e) * CHEB_TL + lane];
+      x1[e] = xa[(kb * VW + e) * CHEB_TL + lane + 32];
+    }
 #pragma unroll
     for (int i = 0; i < CHEB_PT; ++i) {
       const int p = warp + CHEB_WARPS * i;
       if (p < P) {
-        const R a = As[p * KA + k];
-        accA[i][0] += a * x0;
-        accA[i][1] += a * x1;
+        const V a4 = *reinterpret_cast<const V*>(As + p * KAp + kb * VW);
+        const R* a = reinterpret_cast<const R*>(&a4);
+#pragma unroll
+        for (int e = VW - 1; e >= 0; --e) {
+          accA[i][0] += a[e] * x0[e];
+          accA[i][1] += a[e] * x1[e];
+        }
       }
     }
   }
-  for (int k = KB - 1; k >= 0; --k) {
-    const R x0 = xb[k * CHEB_TL + lane], x1 = xb[k * CHEB_TL + lane + 32];
+  for (int kb = KBp / VW - 1; kb >= 0; --kb) {
+    R x0[VW], x1[VW];
+#pragma unroll
+    for (int e = 0; e < VW; ++e) {
+      x0[e] = xb[(kb * VW + e) * CHEB_TL + lane];
+      x1[e] = xb[(kb * VW + e) * CHEB_TL + lane + 32];
+    }
 #pragma unroll
     for (int i = 0; i < CHEB_PT; ++i) {
       const int p = warp + CHEB_WARPS * i;
       if (p < P) {
-        const R bq = Bs[p * KB + k];
-        accB[i][0] += bq * x0;
-        accB[i][1] += bq * x1;
+        const V b4 = *reinterpret_cast<const V*>(Bs + p * KBp + kb * VW);
+        const R* b = reinterpret_cast<const R*>(&b4);
+#pragma unroll
+        for (int e = VW - 1; e >= 0; --e) {
+          accB[i][0] += b[e] * x0[e];
+          accB[i][1] += b[e] * x1[e];
+        }
       }
     }
   }
@@ -198,10 +229,12 @@ __global__ void __launch_bounds__(256) k_cheb(int N, int inverse, int nlines, co
 // adds the base flow (U, U', W, W' at y_j; -Vsuck on v) to the (0,0) mode and
 // forms omega = curl(u) pointwise in y, pairing the re/im lines of a mode
 // through a lane shuffle.  Output: W6[c][j][line], c = u, v, w, ox, oy, oz.
-// Block: 256 threads (8 warps) x 32 lines; warp w handles j = w, w+8, ...
+// Block: 256 threads (8 warps) x 32 lines x one half of the output rows
+// (blockIdx.y): warp w handles p = 8 (2i + half) + w, i < CC_PT, and the block
+// stages only those matrix rows.
 // ---------------------------------------------------------------------------
 #define CC_TL 32
-#define CC_PT 7
+#define CC_PT 4  // output rows per warp and block half: P <= 8 warps * 4 * 2 halves = 64
 
 template <typename R>
 __global__ void __launch_bounds__(256) k_curl_cheb(GridDev g, int N, const double* __restrict__ U, R* __restrict__ W6,
@@ -209,13 +242,19 @@ __global__ void __launch_bounds__(256) k_curl_cheb(GridDev g, int N, const doubl
                                                    const R* __restrict__ DA, const R* __restrict__ DB,
                                                    const R* __restrict__ basey, double Vsuck,
                                                    int bstride, Dither dt, int lpf) {
-  extern __shared__ unsigned char smem_raw[];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  typedef typename Vec16<R>::T V;
+  constexpr int VW = 16 / sizeof(R);
   const int P = (N + 1) / 2, KA = (N + 1) / 2, KB = (N - 1) / 2, J = (N - 1) / 2;
-  R* xs = reinterpret_cast<R*>(smem_raw);           // [3][N][CC_TL]: even coefs rows 0..KA-1, odd KA..N-1
-  R* sCA = xs + 3 * N * CC_TL;
-  R* sCB = sCA + P * KA;
-  R* sDA = sCB + P * KB;
-  R* sDB = sDA + P * KA;
+  // coefficient rows padded to whole 16-byte vectors (zero-filled): the matrices are read VW columns per load
+  const int KAp = (KA + VW - 1) / VW * VW, KBp = (KB + VW - 1) / VW * VW, NP = KAp + KBp;
+  constexpr int PL = 8 * CC_PT;  // matrix rows of this block half: local row r <-> p = 8 (2 (r / 8) + half) + r % 8
+  const int half = blockIdx.y;
+  R* xs = reinterpret_cast<R*>(smem_raw);  // [3][NP][CC_TL]: even coefs rows 0..KAp-1, odd KAp..NP-1
+  R* sCA = xs + 3 * NP * CC_TL;
+  R* sCB = sCA + PL * KAp;
+  R* sDA = sCB + PL * KBp;
+  R* sDB = sDA + PL * KAp;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const size_t row = 2 * (size_t)g.Md, comp = row * N;
   // blocks never straddle two fields (lpf lines each): a block uses its field's version of the constants
@@ -228,22 +267,31 @@ __global__ void __launch_bounds__(256) k_curl_cheb(GridDev g, int N, const doubl
   DA = dither_ptr(DA, ver, dt.S);
   DB = dither_ptr(DB, ver, dt.S);
 #pragma unroll 8
-  for (int i = tid; i < P * KA; i += blockDim.x) {
-    sCA[i] = CA[i];
-    sDA[i] = DA[i];
+  for (int i = tid; i < PL * KAp; i += blockDim.x) {
+    const int r = i / KAp, k = i - r * KAp, pp = 8 * (2 * (r >> 3) + half) + (r & 7);
+    const bool in = k < KA && pp < P;
+    sCA[i] = in ? CA[pp * KA + k] : (R)0;
+    sDA[i] = in ? DA[pp * KA + k] : (R)0;
   }
 #pragma unroll 8
-  for (int i = tid; i < P * KB; i += blockDim.x) {
-    sCB[i] = CB[i];
-    sDB[i] = DB[i];
+  for (int i = tid; i < PL * KBp; i += blockDim.x) {
+    const int r = i / KBp, k = i - r * KBp, pp = 8 * (2 * (r >> 3) + half) + (r & 7);
+    const bool in = k < KB && pp < P;
+    sCB[i] = in ? CB[pp * KB + k] : (R)0;
+    sDB[i] = in ? DB[pp * KB + k] : (R)0;
+  }
+  for (int i = tid; i < 3 * (NP - N) * CC_TL; i += blockDim.x) {  // padding rows
+    const int l = i % CC_TL, t = i / CC_TL, c = t / (NP - N), e = t % (NP - N);
+    const int r = e < KAp - KA ? KA + e : KAp + KB + (e - (KAp - KA));
+    xs[(c * NP + r) * CC_TL + l] = (R)0;
   }
 #pragma unroll 4
   for (int i = tid; i < 3 * N * CC_TL; i += blockDim.x) {
     const int l = i % CC_TL, n = (i / CC_TL) % N, c = i / (CC_TL * N);
     const int gl = l0 + l;
     const R v = gl < nlines ? (R)U[c * comp + (size_t)n * row + gl] : (R)0;
-    const int r = (n & 1) ? KA + (n >> 1) : (n >> 1);
-    xs[(c * N + r) * CC_TL + l] = v;
+    const int r = (n & 1) ? KAp + (n >> 1) : (n >> 1);
+    xs[(c * NP + r) * CC_TL + l] = v;
   }
   __syncthreads();
   R aCu[CC_PT], aCv[CC_PT], aCw[CC_PT], aDu[CC_PT], aDw[CC_PT];   // even-coefficient sums
@@ -251,29 +299,56 @@ __global__ void __launch_bounds__(256) k_curl_cheb(GridDev g, int N, const doubl
 #pragma unroll
   for (int i = 0; i < CC_PT; ++i) aCu[i] = aCv[i] = aCw[i] = aDu[i] = aDw[i] = bCu[i] = bCv[i] = bCw[i] = bDu[i] = bDw[i] = 0;
   const R* xu = xs + lane;
-  const R* xv = xs + N * CC_TL + lane;
-  const R* xw = xs + 2 * N * CC_TL + lane;
-  for (int k = KA - 1; k >= 0; --k) {  // high n first: the small terms are summed before the large
-    const R u = xu[k * CC_TL], v = xv[k * CC_TL], w = xw[k * CC_TL];
+  const R* xv = xs + NP * CC_TL + lane;
+  const R* xw = xs + 2 * NP * CC_TL + lane;
+  // high n first (the small terms are summed before the large), VW coefficients per matrix load
+  for (int kb = KAp / VW - 1; kb >= 0; --kb) {
+    R u[VW], v[VW], w[VW];
+#pragma unroll
+    for (int e = 0; e < VW; ++e) {
+      const int k = kb * VW + e;
+      u[e] = xu[k * CC_TL];
+      v[e] = xv[k * CC_TL];
+      w[e] = xw[k * CC_TL];
+    }
 #pragma unroll
     for (int i = 0; i < CC_PT; ++i) {
-      const int p = warp + 8 * i;
+      const int p = 8 * (2 * i + half) + warp, r = warp + 8 * i;
       if (p < P) {
-        const R c = sCA[p * KA + k], d = sDA[p * KA + k];
-        aCu[i] += c * u; aCv[i] += c * v; aCw[i] += c * w;
-        aDu[i] += d * u; aDw[i] += d * w;
+        const V c4 = *reinterpret_cast<const V*>(sCA + r * KAp + kb * VW);
+        const V d4 = *reinterpret_cast<const V*>(sDA + r * KAp + kb * VW);
+        const R* c = reinterpret_cast<const R*>(&c4);
+        const R* d = reinterpret_cast<const R*>(&d4);
+#pragma unroll
+        for (int e = VW - 1; e >= 0; --e) {
+          aCu[i] += c[e] * u[e]; aCv[i] += c[e] * v[e]; aCw[i] += c[e] * w[e];
+          aDu[i] += d[e] * u[e]; aDw[i] += d[e] * w[e];
+        }
       }
     }
   }
-  for (int k = KB - 1; k >= 0; --k) {
-    const R u = xu[(KA + k) * CC_TL], v = xv[(KA + k) * CC_TL], w = xw[(KA + k) * CC_TL];
+  for (int kb = KBp / VW - 1; kb >= 0; --kb) {
+    R u[VW], v[VW], w[VW];
+#pragma unroll
+    for (int e = 0; e < VW; ++e) {
+      const int k = KAp + kb * VW + e;
+      u[e] = xu[k * CC_TL];
+      v[e] = xv[k * CC_TL];
+      w[e] = xw[k * CC_TL];
+    }
 #pragma unroll
     for (int i = 0; i < CC_PT; ++i) {
-      const int p = warp + 8 * i;
+      const int p = 8 * (2 * i + half) + warp, r = warp + 8 * i;
       if (p < P) {
-        const R c = sCB[p * KB + k], d = sDB[p * KB + k];
-        bCu[i] += c * u; bCv[i] += c * v; bCw[i] += c * w;
-        bDu[i] += d * u; bDw[i] += d * w;
+        const V c4 = *reinterpret_cast<const V*>(sCB + r * KBp + kb * VW);
+        const V d4 = *reinterpret_cast<const V*>(sDB + r * KBp + kb * VW);
+        const R* c = reinterpret_cast<const R*>(&c4);
+        const R* d = reinterpret_cast<const R*>(&d4);
+#pragma unroll
+        for (int e = VW - 1; e >= 0; --e) {
+          bCu[i] += c[e] * u[e]; bCv[i] += c[e] * v[e]; bCw[i] += c[e] * w[e];
+          bDu[i] += d[e] * u[e]; bDw[i] += d[e] * w[e];
+        }
       }
     }
   }
@@ -288,7 +363,7 @@ __global__ void __launch_bounds__(256) k_curl_cheb(GridDev g, int N, const doubl
   const R* __restrict__ by = dither_ptr(basey, ver, dt.Sb) + (size_t)bstride * mode_field(g, m);  // this field's base flow
 #pragma unroll
   for (int i = 0; i < CC_PT; ++i) {
-    const int p = warp + 8 * i;
+    const int p = 8 * (2 * i + half) + warp;
     if (p >= P) continue;  // uniform per warp
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
@@ -332,15 +407,16 @@ __global__ void __launch_bounds__(256) k_curl_cheb(GridDev g, int N, const doubl
 
 template <typename R>
 size_t curl_cheb_smem_bytes(int N) {
-  const int P = (N + 1) / 2, KA = (N + 1) / 2, KB = (N - 1) / 2;
-  return sizeof(R) * ((size_t)3 * N * CC_TL + 2 * (size_t)P * (KA + KB));
+  const int VW = 16 / sizeof(R);
+  const int KAp = ((N + 1) / 2 + VW - 1) / VW * VW, KBp = ((N - 1) / 2 + VW - 1) / VW * VW;
+  return sizeof(R) * ((size_t)3 * (KAp + KBp) * CC_TL + 2 * (size_t)(8 * CC_PT) * (KAp + KBp));
 }
 
 template <typename R>
 cudaError_t launch_curl_cheb(const GridDev& g, int N, const double* U, R* W6, const R* CA, const R* CB, const R* DA,
                              const R* DB, const R* basey, double Vsuck, cudaStream_t st,
                              int bstride, const Dither& dt) {
-  if ((N + 1) / 2 > 8 * CC_PT) return cudaErrorInvalidValue;
+  if ((N + 1) / 2 > 16 * CC_PT) return cudaErrorInvalidValue;
   // kernel attributes set once per process (thread-safe static initialisation)
   static const bool attr_set = [] {
     cudaFuncSetAttribute(k_curl_cheb<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
@@ -348,7 +424,7 @@ cudaError_t launch_curl_cheb(const GridDev& g, int N, const double* U, R* W6, co
   }();
   (void)attr_set;
   const int nf = dt.nb > 0 ? dt.nb : 1, lpf = 2 * g.Md / nf;
-  k_curl_cheb<R><<<nf * ((lpf + CC_TL - 1) / CC_TL), 256, curl_cheb_smem_bytes<R>(N), st>>>(
+  k_curl_cheb<R><<<dim3(nf * ((lpf + CC_TL - 1) / CC_TL), 2), 256, curl_cheb_smem_bytes<R>(N), st>>>(
       g, N, U, W6, CA, CB, DA, DB, basey, Vsuck, bstride, dt, lpf);
   return cudaGetLastError();
 }
@@ -536,8 +612,9 @@ cudaError_t launch_curl_base(const GridDev& g, const double* U, R* C6, const dou
 }
 
 size_t cheb_smem_bytes(int N, size_t rsize) {
-  const int KA = (N + 1) / 2, KB = (N - 1) / 2, P = (N + 1) / 2;
-  return rsize * ((size_t)(KA + KB) * CHEB_TL + (size_t)P * (KA + KB));
+  const int VW = rsize == 4 ? VecLds<float>::W : VecLds<double>::W;
+  const int KAp = ((N + 1) / 2 + VW - 1) / VW * VW, KBp = ((N - 1) / 2 + VW - 1) / VW * VW, P = (N + 1) / 2;
+  return rsize * ((size_t)(KAp + KBp) * CHEB_TL + (size_t)P * (KAp + KBp));
 }
 
 template <typename TI, typename R, typename TO>
