@@ -144,3 +144,17 @@ struct VecLds<double> {
   typedef double T;
   static constexpr int W = 1;
 };
+
+// q = i / d, r = i % d for 0 <= i < 2^22 and d >= 1, with inv = 1.0f / d: a float reciprocal and one
+// correction step (the float product is within one of the quotient in that range).
+__device__ __forceinline__ void divmod_small(int i, int d, float inv, int& q, int& r) {
+  q = __float2int_rz(__int2float_rn(i) * inv);
+  r = i - q * d;
+  if (r >= d) {
+    ++q;
+    r -= d;
+  } else if (r < 0) {
+    --q;
+    r += d;
+  }
+}

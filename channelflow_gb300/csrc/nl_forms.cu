@@ -261,11 +261,21 @@ __global__ void __launch_bounds__(256) k_zphys(GridDev g, FftPlan pz, const cpx<
   const int x0 = blockIdx.x * RP;
   const int tid = threadIdx.x, nthr = blockDim.x;
   const size_t plane = (size_t)g.Nx * NKz;
-  for (int i = tid; i < ninv * ss; i += nthr) A[i] = cmk<R>(0, 0);
-  __syncthreads();
+  // the pack below writes bins 0..NKz-1 and Nz-NKz+1..Nz-1 of every inverse sequence: zero the gap
+  const float invk = 1.0f / NKz;
+  {
+    const int G = Nz - 2 * NKz + 1;
+    const float invg = 1.0f / G;
+    for (int i = tid; i < ninv * G; i += nthr) {
+      int sq, z;
+      divmod_small(i, G, invg, sq, z);
+      A[(size_t)sq * ss + NKz + z] = cmk<R>(0, 0);
+    }
+  }
 #pragma unroll 4
   for (int i = tid; i < ninv * NKz; i += nthr) {
-    const int iz = i % NKz, s = i / NKz;
+    int s, iz;
+    divmod_small(i, NKz, invk, s, iz);
     const int k0 = 2 * s, k1 = 2 * s + 1;
     const int r0 = k0 / NC, c0 = k0 % NC, r1 = k1 / NC, c1 = k1 % NC;
     cpx<R> ca = cmk<R>(0, 0), cb = cmk<R>(0, 0);
@@ -302,7 +312,8 @@ __global__ void __launch_bounds__(256) k_zphys(GridDev g, FftPlan pz, const cpx<
   fft_batch<R>(B, A, nfwd, ss, pz, twz, -1);
 #pragma unroll 4
   for (int i = tid; i < nfwd * NKz; i += nthr) {
-    const int iz = i % NKz, s = i / NKz;
+    int s, iz;
+    divmod_small(i, NKz, invk, s, iz);
     const cpx<R>* sq = B + (size_t)s * ss;
     const cpx<R> zk = sq[iz];
     const cpx<R> zm = sq[iz == 0 ? 0 : Nz - iz];

@@ -452,6 +452,7 @@ __global__ void __launch_bounds__(256) k_xinv(GridDev g, FftPlan px, const cpx<R
   const int ss = g.Nx + 1;
   const int iz0 = blockIdx.z * czc;
   const int nc = min(czc, g.NKz - iz0);
+  const float invc = 1.0f / nc;
   cpx<R>* a = reinterpret_cast<cpx<R>*>(smem_raw);
   cpx<R>* b = a + (size_t)czc * ss;
   const int ny = blockIdx.x, c = blockIdx.y;
@@ -461,7 +462,8 @@ __global__ void __launch_bounds__(256) k_xinv(GridDev g, FftPlan px, const cpx<R
   __syncthreads();
 #pragma unroll 4
   for (int i = tid; i < g.NKx * nc; i += nthr) {
-    const int ix = i / nc, jz = i - ix * nc;
+    int ix, jz;
+    divmod_small(i, nc, invc, ix, jz);
     const int kx = ix <= g.Kx ? ix : ix - g.NKx;
     const int pos = kx >= 0 ? kx : g.Nx + kx;
     a[jz * ss + pos] = src[ix * g.NKz + iz0 + jz];
@@ -470,7 +472,8 @@ __global__ void __launch_bounds__(256) k_xinv(GridDev g, FftPlan px, const cpx<R
   fft_batch<R>(a, b, nc, ss, px, twx, +1);
   cpx<R>* dst = X + ((size_t)c * g.Ny + ny) * (size_t)g.Nx * g.NKz;
   for (int i = tid; i < g.Nx * nc; i += nthr) {
-    const int x = i / nc, jz = i - x * nc;
+    int x, jz;
+    divmod_small(i, nc, invc, x, jz);
     dst[x * g.NKz + iz0 + jz] = a[jz * ss + x];
   }
 }
@@ -578,6 +581,7 @@ __global__ void __launch_bounds__(256) k_xfwd(GridDev g, FftPlan px, const cpx<R
   const int ss = g.Nx + 1;
   const int iz0 = blockIdx.z * czc;
   const int nc = min(czc, g.NKz - iz0);
+  const float invc = 1.0f / nc;
   cpx<R>* a = reinterpret_cast<cpx<R>*>(smem_raw);
   cpx<R>* b = a + (size_t)czc * ss;
   const int ny = blockIdx.x, c = blockIdx.y;
@@ -585,7 +589,8 @@ __global__ void __launch_bounds__(256) k_xfwd(GridDev g, FftPlan px, const cpx<R
   const cpx<R>* src = Z + ((size_t)c * g.Ny + ny) * (size_t)g.Nx * g.NKz;
 #pragma unroll 4
   for (int i = tid; i < g.Nx * nc; i += nthr) {
-    const int x = i / nc, jz = i - x * nc;
+    int x, jz;
+    divmod_small(i, nc, invc, x, jz);
     a[jz * ss + x] = src[x * g.NKz + iz0 + jz];
   }
   __syncthreads();
@@ -593,7 +598,8 @@ __global__ void __launch_bounds__(256) k_xfwd(GridDev g, FftPlan px, const cpx<R
   cpx<R>* dst = F + ((size_t)c * g.Ny + ny) * g.Md;
 #pragma unroll 4
   for (int i = tid; i < g.NKx * nc; i += nthr) {
-    const int ix = i / nc, jz = i - ix * nc;
+    int ix, jz;
+    divmod_small(i, nc, invc, ix, jz);
     const int kx = ix <= g.Kx ? ix : ix - g.NKx;
     const int pos = kx >= 0 ? kx : g.Nx + kx;
     dst[ix * g.NKz + iz0 + jz] = cscale(a[jz * ss + pos], scale);
