@@ -88,6 +88,11 @@ struct Dither {
   long long S;     // bytes between versions of the constant tables
   long long Sb;    // bytes between versions of the base-flow values
   int nb;          // fields interleaved in the plane index of the x/z passes (plane p -> field p % nb)
+  // FP32 passes: version 0 of the tables of d/dx by solved kx index, d/dz by kz, and {1/(Nx Nz), Vsuck}
+  // (host-built, so kernels do no FP64 arithmetic to dither them); unused by FP64 passes
+  const float* kdx;
+  const float* kdz;
+  const float* kmisc;
 };
 
 __host__ __device__ __forceinline__ double dither_offset(int k) {
@@ -156,5 +161,37 @@ __device__ __forceinline__ void divmod_small(int i, int d, float inv, int& q, in
   } else if (r < 0) {
     --q;
     r += d;
+  }
+}
+
+// d/dx and d/dz factors of mode (kx, kz) and the scalar constants for version ver: FP32 passes read the
+// dithered tables, FP64 passes compute them (Nyquist derivatives are zero).
+// Without tables (launches outside the nonlinear pass: CFL, autotuning) FP32 passes round on the fly.
+template <typename R>
+__device__ __forceinline__ R k_dx(const Dither& dt, int ver, const GridDev& g, int kx) {
+  if constexpr (sizeof(R) == 4) {
+    if (dt.kdx) return dither_ptr(dt.kdx, ver, dt.S)[kx >= 0 ? kx : kx + g.NKx];
+    return dither_const<R>(2.0 * M_PI * kx / g.Lx * (kx == g.kxmax ? 0.0 : 1.0), ver);
+  } else {
+    return 2.0 * M_PI * kx / g.Lx * (kx == g.kxmax ? 0.0 : 1.0);
+  }
+}
+template <typename R>
+__device__ __forceinline__ R k_dz(const Dither& dt, int ver, const GridDev& g, int kz) {
+  if constexpr (sizeof(R) == 4) {
+    if (dt.kdz) return dither_ptr(dt.kdz, ver, dt.S)[kz];
+    return dither_const<R>(2.0 * M_PI * kz / g.Lz * (kz == g.kzmax ? 0.0 : 1.0), ver);
+  } else {
+    return 2.0 * M_PI * kz / g.Lz * (kz == g.kzmax ? 0.0 : 1.0);
+  }
+}
+// idx 0: 1/(Nx Nz), 1: Vsuck (value: the exact constant)
+template <typename R>
+__device__ __forceinline__ R k_misc(const Dither& dt, int ver, int idx, double value) {
+  if constexpr (sizeof(R) == 4) {
+    if (dt.kmisc) return dither_ptr(dt.kmisc, ver, dt.S)[idx];
+    return dither_const<R>(value, ver);
+  } else {
+    return value;
   }
 }

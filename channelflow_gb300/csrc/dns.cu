@@ -591,6 +591,7 @@ struct cfgpu_dns_s {
   // apart; the pointers above address version 0), basey/baseyS likewise; dver holds each field's version.
   void* cblock = nullptr;
   long long cS = 0;
+  const float *kdx = nullptr, *kdz = nullptr, *kmisc = nullptr;  // dithered d/dx, d/dz, {1/(Nx Nz), Vsuck}
   int* dver = nullptr;  // [nb]
   double* dyc = nullptr;           // CFL grid spacing in y per Gauss-Lobatto point
   unsigned long long* dred = nullptr;  // reduction scratch (CFL key, L2 sum)
@@ -734,6 +735,9 @@ Dither dither_of(cfgpu_dns d) {
   dt.S = d->cS;
   dt.Sb = (long long)4 * d->N * (d->hetero ? d->nb : 1) * (long long)d->rsz();
   dt.nb = d->nb;
+  dt.kdx = d->precision == CFGPU_FP64 ? nullptr : d->kdx;
+  dt.kdz = d->precision == CFGPU_FP64 ? nullptr : d->kdz;
+  dt.kmisc = d->precision == CFGPU_FP64 ? nullptr : d->kmisc;
   return dt;
 }
 
@@ -1585,6 +1589,20 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
       }
       tabs.push_back(t);
     }
+    {
+      // d/dx by solved kx index, d/dz by kz, {1/(Nx Nz), Vsuck}
+      std::vector<double> tx(g.NKx), tz(g.NKz), tm(4, 0.0);
+      for (int ix = 0; ix < g.NKx; ++ix) {
+        const int kx = ix <= g.Kx ? ix : ix - g.NKx;
+        tx[ix] = 2.0 * M_PI * kx / g.Lx * (kx == g.kxmax ? 0.0 : 1.0);
+      }
+      for (int iz = 0; iz < g.NKz; ++iz) tz[iz] = 2.0 * M_PI * iz / g.Lz * (iz == g.kzmax ? 0.0 : 1.0);
+      tm[0] = 1.0 / ((double)Nx * (double)Nz);
+      tm[1] = f.Vsuck;
+      tabs.push_back(tx);
+      tabs.push_back(tz);
+      tabs.push_back(tm);
+    }
     std::vector<size_t> off(tabs.size());
     size_t S = 0;
     for (size_t i = 0; i < tabs.size(); ++i) {
@@ -1595,7 +1613,10 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
     float* c0 = (float*)d->cblock;
     void** dst[10] = {&d->cinvA, &d->cinvB, &d->cfwdA, &d->cfwdB, &d->cderA, &d->cderB, &d->cdfA, &d->cdfB,
                       &d->twx, &d->twz};
-    for (size_t i = 0; i < tabs.size(); ++i) *dst[i] = c0 + off[i];
+    for (size_t i = 0; i < 10; ++i) *dst[i] = c0 + off[i];
+    d->kdx = c0 + off[10];
+    d->kdz = c0 + off[11];
+    d->kmisc = c0 + off[12];
     d->cS = (long long)(S * sizeof(float));
     CKS(upload_dithered({basey}, {0}, basey.size(), &d->basey, B, d->st));
   }

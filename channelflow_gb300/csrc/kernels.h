@@ -14,7 +14,7 @@ cudaError_t launch_curl_base(const GridDev& g, const double* U, R* C6, const dou
                              cudaStream_t st);
 
 // Undithered constants (version 0 only; one field).
-constexpr Dither kNoDither{nullptr, 0, 0, 1};
+constexpr Dither kNoDither{nullptr, 0, 0, 1, nullptr, nullptr, nullptr};
 
 size_t cheb_smem_bytes(int N, size_t rsize);
 

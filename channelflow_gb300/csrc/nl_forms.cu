@@ -141,9 +141,9 @@ __global__ void __launch_bounds__(256) k_grad_cheb(GridDev g, int N, const doubl
   const int m = min(gl, nlines - 1) >> 1;
   const int part = gl & 1;
   const int kx = mode_kx(g, m), kz = mode_kz(g, m);
-  const R dx = dither_const<R>(2.0 * M_PI * kx / g.Lx * (kx == g.kxmax ? 0.0 : 1.0), ver);
-  const R dz = dither_const<R>(2.0 * M_PI * kz / g.Lz * (kz == g.kzmax ? 0.0 : 1.0), ver);
-  const R vs = dither_const<R>(Vsuck, ver);
+  const R dx = k_dx<R>(dt, ver, g, kx);
+  const R dz = k_dz<R>(dt, ver, g, kz);
+  const R vs = k_misc<R>(dt, ver, 1, Vsuck);
   const bool base = (kx == 0 && kz == 0 && part == 0);
   const R* __restrict__ by = dither_ptr(basey, ver, dt.Sb) + (size_t)bstride * mode_field(g, m);  // this field's base flow
 #pragma unroll
@@ -434,8 +434,8 @@ __global__ void __launch_bounds__(256) k_cheb_fwd_div(GridDev g, int N, const R*
   const int m = min(gl, nlines - 1) >> 1;
   const int part = gl & 1;
   const int kx = mode_kx(g, m), kz = mode_kz(g, m);
-  const R dx = dither_const<R>(2.0 * M_PI * kx / g.Lx * (kx == g.kxmax ? 0.0 : 1.0), ver);
-  const R dz = dither_const<R>(2.0 * M_PI * kz / g.Lz * (kz == g.kzmax ? 0.0 : 1.0), ver);
+  const R dx = k_dx<R>(dt, ver, g, kx);
+  const R dz = k_dz<R>(dt, ver, g, kz);
 #pragma unroll
   for (int i = 0; i < CF_PT; ++i) {
     const int p = warp + 8 * i;
@@ -565,7 +565,7 @@ __global__ void k_linprof(GridDev g, int N, const R* __restrict__ Y, const R* __
   const int m = (int)(t % g.Md), j = (int)(t / g.Md);
   const int kx = mode_kx(g, m), kz = mode_kz(g, m);
   const int ver = dither_ver(dt, mode_field(g, m));
-  const R dx = dither_const<R>(2.0 * M_PI * kx / g.Lx, ver), dz = dither_const<R>(2.0 * M_PI * kz / g.Lz, ver);
+  const R dx = k_dx<R>(dt, ver, g, kx), dz = k_dz<R>(dt, ver, g, kz);
   const R* by = dither_ptr(basey, ver, dt.Sb) + (size_t)bstride * mode_field(g, m);
   const R U = by[j], Uy = by[N + j], W = by[2 * N + j], Wy = by[3 * N + j];
   const R d = U * dx + W * dz;  // (U d/dx + W d/dz) = i d

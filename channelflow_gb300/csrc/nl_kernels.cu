@@ -356,9 +356,9 @@ __global__ void __launch_bounds__(256) k_curl_cheb(GridDev g, int N, const doubl
   const int m = min(gl, nlines - 1) >> 1;
   const int part = gl & 1;
   const int kx = mode_kx(g, m), kz = mode_kz(g, m);
-  const R dx = dither_const<R>(2.0 * M_PI * kx / g.Lx * (kx == g.kxmax ? 0.0 : 1.0), ver);
-  const R dz = dither_const<R>(2.0 * M_PI * kz / g.Lz * (kz == g.kzmax ? 0.0 : 1.0), ver);
-  const R vs = dither_const<R>(Vsuck, ver);
+  const R dx = k_dx<R>(dt, ver, g, kx);
+  const R dz = k_dz<R>(dt, ver, g, kz);
+  const R vs = k_misc<R>(dt, ver, 1, Vsuck);
   const bool base = (kx == 0 && kz == 0 && part == 0);
   const R* __restrict__ by = dither_ptr(basey, ver, dt.Sb) + (size_t)bstride * mode_field(g, m);  // this field's base flow
 #pragma unroll
@@ -577,7 +577,7 @@ __global__ void __launch_bounds__(256) k_xfwd(GridDev g, FftPlan px, const cpx<R
   extern __shared__ unsigned char smem_raw[];
   const int ver = dither_ver(dt, blockIdx.x % dt.nb);  // plane blockIdx.x -> its field's constants
   twx = dither_ptr(twx, ver, dt.S);
-  const R scale = dither_const<R>(scale_d, ver);
+  const R scale = k_misc<R>(dt, ver, 0, scale_d);
   const int ss = g.Nx + 1;
   const int iz0 = blockIdx.z * czc;
   const int nc = min(czc, g.NKz - iz0);
