@@ -47,10 +47,9 @@ WORKLOAD = ("plane Poiseuille 128x97x128 (Lx=4pi, Lz=2pi), CNAB2 + SMRK2 start-u
             "Ubulk=2/3, Re_c=4000, rotational NL, 2/3 dealiasing, seeded perturbation L2=0.3")
 CNAB2, SMRK2, LaminarBase, BulkVelocity = 1, 3, 3, 1
 # DRAM bytes (read + write) per step of the mixed-path phases from `ncu --set full` captures of this workload
-# (profiles/ncu_tau_solve_poiseuille_128x97x128_mixed.md: the three tau kernels;
-# profiles/ncu_full_poiseuille_128x97x128_mixed.md: the NL-pass kernels).
-NCU_TRAFFIC = {"tau_solve": (37.93971 + 0.697088 + 54.40486 + 0.448768 + 27.12601 + 19.968) * 1e6,
-               "nonlinear_pass": (16.32896 + 16.315648 + 25.136128 + 12.600576 + 8.16384 + 0.003328) * 1e6}
+# (profiles/ncu_step_poiseuille_128x97x128_mixed.md: the eight kernels of one step, tau and NL pass).
+NCU_TRAFFIC = {"tau_solve": (37.94 + 0.50 + 54.41 + 0.50 + 27.13 + 0.0) * 1e6,
+               "nonlinear_pass": (16.32 + 0.0 + 16.70 + 0.39 + 25.13 + 0.0 + 12.60 + 0.0 + 8.17 + 0.0) * 1e6}
 
 
 def peaks():
