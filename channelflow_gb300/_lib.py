@@ -67,6 +67,12 @@ _SIGS = {
     "cfgpu_dns_cfl": [C.c_void_p, _PD],
     "cfgpu_dns_nonlinear": [C.c_void_p, _PD, _PD],
     "cfgpu_set_host_access": [C.c_int],
+    "cfgpu_field_create": [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)],
+    "cfgpu_field_upload": [C.c_void_p, _PD],
+    "cfgpu_field_download": [C.c_void_p, _PD],
+    "cfgpu_field_destroy": [C.c_void_p],
+    "cfgpu_dns_set_fields_device": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p],
+    "cfgpu_dns_get_fields_device": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p],
     "cfgpu_field2vector_size": [C.c_void_p, C.POINTER(C.c_longlong)],
     "cfgpu_orthogonalize": [C.c_int, C.c_int, _PD, _PD, _PD],
     "cfgpu_field2vector": [C.c_void_p, _PD, _PD],

@@ -2112,6 +2112,126 @@ cfgpu_status cfgpu_ensemble_dPdx(cfgpu_dns d, double* dPdx) {
   return CFGPU_OK;
 }
 
+}  // extern "C"
+
+// A field on the GPU in the solved-mode layout of its grid (2/3-dealiased modes): Nd components, complex
+// [c][ny][m]; the C ABI's FlowField handle.
+struct cfgpu_field_s {
+  cfgpu_dns_s g;  // mode set, staging and stream only (no DNS is built)
+  int Nd = 3;
+  double* data = nullptr;
+  long long bytes = 0;
+};
+
+namespace {
+int f2v_grid(const cfgpu_grid* grid, cfgpu_dns_s& tmp);
+
+int field_transfer(cfgpu_field f, const double* host_in, double* host_out) {
+  cfgpu_dns_s& t = f->g;
+  const size_t n = (size_t)f->Nd * t.compc();
+  if (t.direct) {
+    if (host_in) CK(launch_host_modes(t.g, true, f->Nd, 1, 0, 1, host_in, f->data, t.st));
+    if (host_out) CK(launch_host_modes(t.g, false, f->Nd, 1, 0, 1, f->data, host_out, t.st));
+    CK(cudaStreamSynchronize(t.st));
+    return CFGPU_OK;
+  }
+  std::vector<double> h(n);
+  if (host_in) {
+    gather_modes(&t, host_in, f->Nd, h.data());
+    CK(cudaMemcpyAsync(f->data, h.data(), n * sizeof(double), cudaMemcpyHostToDevice, t.st));
+    CK(cudaStreamSynchronize(t.st));
+  }
+  if (host_out) {
+    CK(cudaMemcpyAsync(h.data(), f->data, n * sizeof(double), cudaMemcpyDeviceToHost, t.st));
+    CK(cudaStreamSynchronize(t.st));
+    scatter_modes(&t, h.data(), f->Nd, host_out);
+  }
+  return CFGPU_OK;
+}
+
+// The field's grid and mode set must be the DNS's (one field of it).
+bool field_matches(cfgpu_dns d, cfgpu_field f, int Nd) {
+  const GridDev &a = d->g, &b = f->g.g;
+  return f->Nd == Nd && a.Nx == b.Nx && a.Ny == b.Ny && a.Nz == b.Nz && a.Md == b.Md && a.Lx == b.Lx &&
+         a.Lz == b.Lz && a.a == b.a && a.b == b.b;
+}
+}  // namespace
+
+extern "C" {
+
+cfgpu_status cfgpu_field_create(const cfgpu_grid* grid, int Nd, cfgpu_field* out) {
+  if (!out || (Nd != 1 && Nd != 3)) return fail(CFGPU_EINVAL, "bad argument");
+  *out = nullptr;
+  auto* f = new cfgpu_field_s();
+  int st = f2v_grid(grid, f->g);
+  if (st == CFGPU_OK) {
+    f->Nd = Nd;
+    int ats = 0, dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&ats, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess) ats = 0;
+    f->g.direct = ats == 1 && g_host_access.load() != 0;
+    if (cudaStreamCreateWithFlags(&f->g.st, cudaStreamNonBlocking) != cudaSuccess)
+      st = fail(CFGPU_ECUDA, "cudaStreamCreate failed");
+  }
+  const size_t n = (size_t)Nd * f->g.compc();
+  if (st == CFGPU_OK) st = dalloc(&f->data, n, f->bytes);
+  if (st == CFGPU_OK && cudaMemsetAsync(f->data, 0, n * sizeof(double), f->g.st) != cudaSuccess)
+    st = fail(CFGPU_ECUDA, "cudaMemset failed");
+  if (st == CFGPU_OK && cudaStreamSynchronize(f->g.st) != cudaSuccess) st = fail(CFGPU_ECUDA, "stream sync");
+  if (st != CFGPU_OK) {
+    cfgpu_field_destroy(f);
+    return st;
+  }
+  *out = f;
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_field_upload(cfgpu_field f, const double* u) {
+  if (!f || !u) return fail(CFGPU_EINVAL, "bad argument");
+  return field_transfer(f, u, nullptr);
+}
+
+cfgpu_status cfgpu_field_download(cfgpu_field f, double* u) {
+  if (!f || !u) return fail(CFGPU_EINVAL, "bad argument");
+  const GridDev& g = f->g.g;
+  memset(u, 0, sizeof(double) * f->Nd * 2 * (size_t)g.Ny * g.Nx * (g.Nz / 2 + 1));
+  return field_transfer(f, nullptr, u);
+}
+
+cfgpu_status cfgpu_field_destroy(cfgpu_field f) {
+  if (!f) return CFGPU_OK;
+  if (f->g.st) cudaStreamSynchronize(f->g.st);
+  dfree(f->data);
+  if (f->g.st) cudaStreamDestroy(f->g.st);
+  f->g.st = nullptr;
+  delete f;
+  return CFGPU_OK;
+}
+
+// The DNS's current velocity / pressure (field 0 of an ensemble: slot) from / into GPU fields (device to
+// device; either may be null).
+cfgpu_status cfgpu_dns_set_fields_device(cfgpu_dns d, int slot, cfgpu_field u, cfgpu_field q) {
+  if (!d || slot < 0 || slot >= d->nb || (u && !field_matches(d, u, 3)) || (q && !field_matches(d, q, 1)))
+    return fail(CFGPU_EINVAL, "bad argument (fields must have the DNS's grid and 2/3-dealiased modes)");
+  const size_t w = 2 * (size_t)d->g.Md, pitch = w * d->nb, N = d->N;
+  if (u) CK(cudaStreamSynchronize(u->g.st));
+  if (q) CK(cudaStreamSynchronize(q->g.st));
+  if (u) CK(cudaMemcpy2DAsync(d->Ucur + slot * w, pitch * 8, u->data, w * 8, w * 8, 3 * N, cudaMemcpyDeviceToDevice, d->st));
+  if (q) CK(cudaMemcpy2DAsync(d->Qcur + slot * w, pitch * 8, q->data, w * 8, w * 8, N, cudaMemcpyDeviceToDevice, d->st));
+  CK(cudaStreamSynchronize(d->st));
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_dns_get_fields_device(cfgpu_dns d, int slot, cfgpu_field u, cfgpu_field q) {
+  if (!d || slot < 0 || slot >= d->nb || (u && !field_matches(d, u, 3)) || (q && !field_matches(d, q, 1)))
+    return fail(CFGPU_EINVAL, "bad argument (fields must have the DNS's grid and 2/3-dealiased modes)");
+  const size_t w = 2 * (size_t)d->g.Md, pitch = w * d->nb, N = d->N;
+  if (u) CK(cudaMemcpy2DAsync(u->data, w * 8, d->Ucur + slot * w, pitch * 8, w * 8, 3 * N, cudaMemcpyDeviceToDevice, d->st));
+  if (q) CK(cudaMemcpy2DAsync(q->data, w * 8, d->Qcur + slot * w, pitch * 8, w * 8, N, cudaMemcpyDeviceToDevice, d->st));
+  CK(cudaStreamSynchronize(d->st));
+  return CFGPU_OK;
+}
+
 cfgpu_status cfgpu_dns_set_fields(cfgpu_dns d, const double* u, const double* q) {
   if (!d) return fail(CFGPU_EINVAL, "null dns");
   CKS(set_fields(d, u, q));

@@ -344,3 +344,45 @@ def helmholtz_solve_batched(a: float, b: float, lam, nu: float, f, ua=None, ub=N
     L.check(lib.cfgpu_helmholtz_solve_mean_batched(N, nsys, a, b, L.dptr(lam), nu, L.dptr(f), L.dptr(umean),
                                                    L.dptr(ua), L.dptr(ub), L.dptr(u), L.dptr(mu)))
     return u, mu
+
+
+class DeviceField:
+    """FlowField on the GPU (2/3-dealiased modes of Nd components): upload / download host FlowField buffers,
+    hand to and take from a DNS without a host round trip."""
+
+    def __init__(self, grid: Grid, Nd: int = 3):
+        self.grid, self.Nd = grid, Nd
+        self._lib = L.load()
+        h = C.c_void_p()
+        gc = grid.to_c()
+        L.check(self._lib.cfgpu_field_create(C.byref(gc), int(Nd), C.byref(h)))
+        self._h = h
+
+    def upload(self, u):
+        L.check(self._lib.cfgpu_field_upload(self._h, L.dptr(_as_field(np.ascontiguousarray(u), self.grid, self.Nd))))
+
+    def download(self) -> np.ndarray:
+        out = np.zeros((self.Nd, self.grid.Ny, self.grid.Nx, self.grid.Nz // 2 + 1), dtype=np.complex128)
+        L.check(self._lib.cfgpu_field_download(self._h, L.dptr(out)))
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.cfgpu_field_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def set_fields_device(dns, u: DeviceField | None, q: DeviceField | None = None, slot: int = 0):
+    """The DNS's (slot's) velocity / pressure from GPU fields, device to device."""
+    L.check(dns._lib.cfgpu_dns_set_fields_device(dns._h, int(slot), u._h if u else None, q._h if q else None))
+
+
+def get_fields_device(dns, u: DeviceField | None, q: DeviceField | None = None, slot: int = 0):
+    """The DNS's (slot's) velocity / pressure into GPU fields, device to device."""
+    L.check(dns._lib.cfgpu_dns_get_fields_device(dns._h, int(slot), u._h if u else None, q._h if q else None))

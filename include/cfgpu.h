@@ -73,6 +73,21 @@ typedef struct cfgpu_flags {
 
 typedef struct cfgpu_dns_s* cfgpu_dns;
 
+/*
+ * FlowField on the GPU (channelflow/flowfield.h:52-345: construction, the spectral data, upload/download in
+ * the serial layout complex [i][my][mx][mz]): the 2/3-dealiased modes of Nd = 1 or 3 components, in the
+ * layout the DNS kernels use.  download zeroes the other modes.  cfgpu_dns_set/get_fields_device move a
+ * DNS's velocity (Nd = 3) and pressure (Nd = 1) from/to such fields on the device (field `slot` of an
+ * ensemble; either may be null).
+ */
+typedef struct cfgpu_field_s* cfgpu_field;
+cfgpu_status cfgpu_field_create(const cfgpu_grid* grid, int Nd, cfgpu_field* out);
+cfgpu_status cfgpu_field_upload(cfgpu_field f, const double* u);
+cfgpu_status cfgpu_field_download(cfgpu_field f, double* u);
+cfgpu_status cfgpu_field_destroy(cfgpu_field f);
+cfgpu_status cfgpu_dns_set_fields_device(cfgpu_dns dns, int slot, cfgpu_field u, cfgpu_field q);
+cfgpu_status cfgpu_dns_get_fields_device(cfgpu_dns dns, int slot, cfgpu_field u, cfgpu_field q);
+
 /* TimeStep parameters (channelflow/dnsflags.h:166-198): dt within [dtmin, dtmax], dT = n dt the CFL-check
  * interval, CFL kept within [CFLmin, CFLmax] when variable != 0. */
 typedef struct cfgpu_timestep {
