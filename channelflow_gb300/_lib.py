@@ -67,6 +67,10 @@ _SIGS = {
     "cfgpu_dns_cfl": [C.c_void_p, _PD],
     "cfgpu_dns_nonlinear": [C.c_void_p, _PD, _PD],
     "cfgpu_set_host_access": [C.c_int],
+    "cfgpu_dns_reset_time": [C.c_void_p, C.c_double],
+    "cfgpu_dns_reset_gradp": [C.c_void_p, C.c_double, C.c_double],
+    "cfgpu_dns_reset_bulkv": [C.c_void_p, C.c_double, C.c_double],
+    "cfgpu_dns_constraint": [C.c_void_p, _PD],
     "cfgpu_field_create": [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)],
     "cfgpu_field_upload": [C.c_void_p, _PD],
     "cfgpu_field_download": [C.c_void_p, _PD],

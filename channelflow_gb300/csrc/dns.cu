@@ -575,6 +575,7 @@ struct cfgpu_dns_s {
   std::vector<double> Ubase, Wbase, Ubaseyy, Wbaseyy;
   double UbulkBase = 0, WbulkBase = 0, dPdxRef = 0, dPdzRef = 0, UbulkRef = 0, WbulkRef = 0;
   double dPdxAct = 0, dPdzAct = 0;
+  double UbulkAct = 0, WbulkAct = 0;  // NSE::UbulkAct_ (nse.cpp:645): set from the initial field at construction
   double baseShear[2] = {0, 0};
   double *dUbase = nullptr, *dWbase = nullptr, *dUbaseyy = nullptr, *dWbaseyy = nullptr;
   double* ddPdx = nullptr;  // [2]
@@ -1500,7 +1501,17 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
   d->dPdxRef = bf.dPdxRef;
   d->dPdzAct = bf.dPdzAct;
   d->dPdzRef = bf.dPdzRef;
-  (void)u0;
+  if (u0) {
+    // getUbulk / getWbulk (diffops.cpp:3839-3867): mean over y of the (0,0) mode of u and w
+    const size_t plane = 2 * (size_t)Nx * (Nz / 2 + 1), comp = plane * Ny;
+    double su = u0[0], sw = u0[2 * comp];
+    for (int n = 2; n < Ny; n += 2) {
+      su -= u0[n * plane] / (double)(n * n - 1);
+      sw -= u0[2 * comp + n * plane] / (double)(n * n - 1);
+    }
+    d->UbulkAct = bf.UbulkBase + su;
+    d->WbulkAct = bf.WbulkBase + sw;
+  }
   long long& B = d->bytes;
   CKS(dalloc(&d->dUbase, Ny, B));
   CKS(dalloc(&d->dWbase, Ny, B));
@@ -2273,6 +2284,39 @@ cfgpu_status cfgpu_dns_reset_dt(cfgpu_dns d, double dt) {
     CKS(build_tables(d, *s));
   }
   CK(cudaStreamSynchronize(d->st));
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_dns_reset_time(cfgpu_dns d, double t) {
+  if (!d) return fail(CFGPU_EINVAL, "bad argument");
+  d->main.t = t;
+  if (d->has_init) d->init.t = t;
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_dns_reset_gradp(cfgpu_dns d, double dPdx, double dPdz) {
+  if (!d) return fail(CFGPU_EINVAL, "bad argument");
+  if (d->hetero) return fail(CFGPU_ENOTSUP, "per-field parameters: set the constraint with cfgpu_ensemble_set_params");
+  d->fl.constraint = CFGPU_PressureGradient;
+  d->fl.dPdx = dPdx, d->fl.dPdz = dPdz, d->fl.Ubulk = 0.0, d->fl.Wbulk = 0.0;
+  d->dPdxRef = dPdx, d->dPdzRef = dPdz, d->UbulkRef = 0.0, d->WbulkRef = 0.0;
+  drop_graphs(d);  // the step parameters change
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_dns_reset_bulkv(cfgpu_dns d, double Ubulk, double Wbulk) {
+  if (!d) return fail(CFGPU_EINVAL, "bad argument");
+  if (d->hetero) return fail(CFGPU_ENOTSUP, "per-field parameters: set the constraint with cfgpu_ensemble_set_params");
+  d->fl.constraint = CFGPU_BulkVelocity;
+  d->fl.Ubulk = Ubulk, d->fl.Wbulk = Wbulk, d->fl.dPdx = 0.0, d->fl.dPdz = 0.0;
+  d->UbulkRef = Ubulk, d->WbulkRef = Wbulk, d->dPdxRef = 0.0, d->dPdzRef = 0.0;
+  drop_graphs(d);
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_dns_constraint(cfgpu_dns d, double* v) {
+  if (!d || !v) return fail(CFGPU_EINVAL, "bad argument");
+  v[0] = d->UbulkAct, v[1] = d->WbulkAct, v[2] = d->UbulkRef, v[3] = d->WbulkRef, v[4] = d->dPdxRef, v[5] = d->dPdzRef;
   return CFGPU_OK;
 }
 

@@ -145,6 +145,24 @@ class DNS:
         v = np.ascontiguousarray(v, dtype=np.float64)
         L.check(self._lib.cfgpu_ensemble_vector2field(self._h, int(slot), L.dptr(v)))
 
+    def reset_time(self, t: float):
+        """DNS::reset_time (dns.cpp:199-205)."""
+        L.check(self._lib.cfgpu_dns_reset_time(self._h, float(t)))
+
+    def reset_gradp(self, dPdx: float, dPdz: float = 0.0):
+        """DNS::reset_gradp (dns.cpp:221-226): pressure-gradient constraint from the next step on."""
+        L.check(self._lib.cfgpu_dns_reset_gradp(self._h, float(dPdx), float(dPdz)))
+
+    def reset_bulkv(self, Ubulk: float, Wbulk: float = 0.0):
+        """DNS::reset_bulkv (dns.cpp:227-232): bulk-velocity constraint from the next step on."""
+        L.check(self._lib.cfgpu_dns_reset_bulkv(self._h, float(Ubulk), float(Wbulk)))
+
+    def constraint(self) -> dict:
+        """DNS::Ubulk, Wbulk, UbulkRef, WbulkRef, dPdxRef, dPdzRef (dns.cpp:298-330)."""
+        v = np.zeros(6)
+        L.check(self._lib.cfgpu_dns_constraint(self._h, L.dptr(v)))
+        return dict(zip(("Ubulk", "Wbulk", "UbulkRef", "WbulkRef", "dPdxRef", "dPdzRef"), v.tolist()))
+
     def host_access(self) -> bool:
         """True when this DNS reads and writes host FlowField buffers with its own kernels (no staging)."""
         v = C.c_int()

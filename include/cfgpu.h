@@ -129,6 +129,15 @@ cfgpu_status cfgpu_dns_reset_dt(cfgpu_dns dns, double dt);
 
 /* DNS::time(), DNS::dPdx(), DNS::Ubulk() style queries (channelflow/dns.h:55-75). */
 cfgpu_status cfgpu_dns_time(cfgpu_dns dns, double* t);
+/* DNS::reset_time (channelflow/dns.cpp:199-205); reset_gradp / reset_bulkv (dns.cpp:221-232, NSE
+ * nse.cpp:724-745): switch to the pressure-gradient or bulk-velocity constraint from the next step on,
+ * keeping the base flow (not for ensembles with per-field parameters).  cfgpu_dns_constraint: v[6] =
+ * {Ubulk, Wbulk (NSE::UbulkAct_, set from the initial field at construction, nse.cpp:645), UbulkRef,
+ * WbulkRef, dPdxRef, dPdzRef} (dns.cpp:306-330). */
+cfgpu_status cfgpu_dns_reset_time(cfgpu_dns dns, double t);
+cfgpu_status cfgpu_dns_reset_gradp(cfgpu_dns dns, double dPdx, double dPdz);
+cfgpu_status cfgpu_dns_reset_bulkv(cfgpu_dns dns, double Ubulk, double Wbulk);
+cfgpu_status cfgpu_dns_constraint(cfgpu_dns dns, double* v);
 cfgpu_status cfgpu_dns_dPdx(cfgpu_dns dns, double* dPdx);
 
 /*

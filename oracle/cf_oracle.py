@@ -1182,6 +1182,30 @@ class DNS:
         if self.init is not None:
             self.init.reset_dt(dt)
 
+    def reset_time(self, t):
+        """DNS::reset_time (dns.cpp:199-205): both schemes' clocks."""
+        self.main.t = t
+        if self.init is not None:
+            self.init.t = t
+
+    def _nses(self):
+        return [n for n in (getattr(self, "init_nse", None) if self.init is not None else None, self.main_nse) if n]
+
+    def reset_gradp(self, dPdx, dPdz):
+        """DNS::reset_gradp (dns.cpp:221-226) -> NSE::reset_gradp (nse.cpp:724-734): the pressure-gradient
+        constraint from now on; the base flow is kept."""
+        for n in self._nses():
+            f = n.flags
+            f.constraint, f.dPdx, f.dPdz, f.Ubulk, f.Wbulk = PressureGradient, dPdx, dPdz, 0.0, 0.0
+            n.dPdxRef, n.dPdzRef, n.UbulkRef, n.WbulkRef = dPdx, dPdz, 0.0, 0.0
+
+    def reset_bulkv(self, Ubulk, Wbulk):
+        """DNS::reset_bulkv (dns.cpp:227-232) -> NSE::reset_bulkv (nse.cpp:735-745)."""
+        for n in self._nses():
+            f = n.flags
+            f.constraint, f.Ubulk, f.Wbulk, f.dPdx, f.dPdz = BulkVelocity, Ubulk, Wbulk, 0.0, 0.0
+            n.UbulkRef, n.WbulkRef, n.dPdxRef, n.dPdzRef = Ubulk, Wbulk, 0.0, 0.0
+
     def CFL(self, u):
         """DNSAlgorithm::CFL (dnsalgo.cpp:62-66)."""
         c = cfl_factor(u, self.g, self.main_nse.Ubase, self.main_nse.Wbase)
