@@ -14,6 +14,8 @@
 // Every per-mode quantity lives in global memory as a "line" of N values
 // with a fixed stride between consecutive Chebyshev indices, so a warp of
 // threads (consecutive modes) touches consecutive addresses at each step.
+#include <type_traits>
+
 #include "kernels.h"
 
 struct Ln {
@@ -1134,58 +1136,77 @@ __global__ void __launch_bounds__(32) k_tau_rhs(GridDev g, int N, SolveParams sp
     const double kappa2 = 4 * M_PI * M_PI * ((kx / g.Lx) * (kx / g.Lx) + (kz / g.Lz) * (kz / g.Lz));
     const double Dx = 2 * M_PI * kx / g.Lx * (kx == g.kxmax ? 0.0 : 1.0);
     const double Dz = 2 * M_PI * kz / g.Lz * (kz == g.kzmax ? 0.0 : 1.0);
-    for (int c = cc; c <= cc; ++c) {
-      PLn uc = G(P.uin[0] + c * comp);
-      PLn uo = Go(P.uin[0] + c * comp);
-      SLn d1 = S(0);
-      __syncwarp(gmask);
-      double s = 0.0;
-      {
-        double dn2 = 0.0;
-        int i = M - 1;
-        if (q == 0) {
-          const double v = dn2 + ct[2 * i] * 0.0;
-          d1[i] = v;
-          s += v;
-          dn2 = v;
-          i--;
-        }
-        for (; i >= 0; i -= TCH) {
-          double xv[TCH];
-#pragma unroll
-          for (int k = 0; k < TCH; ++k)
-            if (i - k >= 0) xv[k] = uo[i - k + q];
-#pragma unroll
-          for (int k = 0; k < TCH; ++k)
-            if (i - k >= 0) {
-              const int n = 2 * (i - k) + q;
-              double v = dn2 + ct[n] * xv[k];  // diff(u)/... without the factor nu (applied in L)
-              dn2 = v;
-              if (n == 0) v *= 0.5;
-              d1[i - k] = v;
-              s += v;
-            }
-        }
+    const int c = cc;
+    PLn uc = G(P.uin[0] + c * comp);
+    PLn uo = Go(P.uin[0] + c * comp);
+    SLn d1 = S(0);
+    __syncwarp(gmask);
+    // first derivative of this lane's parity from the other parity's coefficients (descending recurrence,
+    // without the factor nu); the n = 0 coefficient is halved after the sweep
+    {
+      double dn2 = 0.0;
+      int i = M - 1;
+      if (q == 0) {
+        d1[i] = 0.0;
+        i--;
       }
-      const double so = __shfl_xor_sync(gmask, s, 1);
-      double wall = 0.0;
-      if (m00 && part == 0 && sp.constraint == 1 && c != 1) {
-        const double s0 = nu * (q == 0 ? s : so), s1 = nu * (q == 0 ? so : s);
-        wall = ((s0 + s1) - (s0 - s1)) / (g.b - g.a);
+      for (; i >= 0; i -= TCH) {
+        double xv[TCH];
+#pragma unroll
+        for (int k = 0; k < TCH; ++k)
+          if (i - k >= 0) xv[k] = uo[i - k + q];
+#pragma unroll
+        for (int k = 0; k < TCH; ++k)
+          if (i - k >= 0) {
+            const double v = dn2 + ct[2 * (i - k) + q] * xv[k];
+            dn2 = v;
+            d1[i - k] = v;
+          }
       }
-      __syncwarp(gmask);
-      SLn d1o = So(0);
-      PLn qo = Go(P.qin);
-      PLn qp = Gp(P.qin);
-      PLn outg = G(c == 0 ? Rxg : Rzg);
-      PLn outs = G(Ryg);
-      const R* Nj = static_cast<const R*>(P.nin[0]) + c * comp + off + q * row;
-      const R* Nj1 = sp.kind == 1 ? static_cast<const R*>(P.nin[1]) + c * comp + off + q * row : nullptr;
-      R* Q = sp.kind == 2 ? static_cast<R*>(P.Q) + c * comp + off + q * row : nullptr;
-      const double kD = c == 0 ? Dx : Dz;
+      if (q == 0) d1[0] = 0.5 * d1[0];
+    }
+    // wall shear of the (0,0) mode's u and w (bulk-velocity constraint): the sum of u' over the
+    // coefficients of each parity, combined across the lane pair
+    const bool shear = m00 && part == 0 && sp.constraint == 1 && c != 1;
+    double s = 0.0;
+    if (shear)
+      for (int i = M - 1; i >= 0; --i) s += d1[i];
+    const double so = __shfl_xor_sync(gmask, s, 1);
+    double wall = 0.0;
+    if (shear) {
+      const double s0 = nu * (q == 0 ? s : so), s1 = nu * (q == 0 ? so : s);
+      wall = ((s0 + s1) - (s0 - s1)) / (g.b - g.a);
+    }
+    __syncwarp(gmask);
+    SLn d1o = So(0);
+    PLn qo = Go(P.qin);
+    PLn qp = Gp(P.qin);
+    PLn out = G(c == 0 ? Rxg : (c == 1 ? Ryg : Rzg));
+    const R* Nj = static_cast<const R*>(P.nin[0]) + c * comp + off + q * row;
+    const R* Nj1 = sp.kind == 1 ? static_cast<const R*>(P.nin[1]) + c * comp + off + q * row : nullptr;
+    R* Q = sp.kind == 2 ? static_cast<R*>(P.Q) + c * comp + off + q * row : nullptr;
+    // L = nu (u'' - kappa^2 u) - grad q; CNAB: rhs = lam u + a_b L - g_b N_j - z_b N_{j-1}; CNRK2:
+    // rhs = L + lam u + B_C Q.  Both as rhs = cu u + cd u'' + cg g + Nc with g = q (u, w: times the sign of
+    // i k of the part) or q' (v), the constants folded per mode; the n = 0 row takes the halved derivative.
+    const double kD = c == 0 ? Dx : Dz;
+    const double aL = sp.kind == 1 ? sp.a_b : 1.0;
+    const double cu = sp.lam - aL * (nu * kappa2);
+    const double cd = aL * nu;
+    const double cg = c == 1 ? -aL : (part == 0 ? aL * kD : -(aL * kD));
+    const double cd0 = 0.5 * cd, cg0 = c == 1 ? 0.5 * cg : cg;
+    const R gN = (R)(-sp.g_b), zN = (R)(-sp.z_b), rA = (R)sp.rkA;
+    const double BC = sp.B_C;
+    // the (0,0) mode's extra terms of u and w: nu U'' of the base flow in L and in the scheme's constant,
+    // and the pressure-gradient / bulk-velocity term of the n = 0 row
+    const bool extra = m00 && part == 0 && c != 1;
+    const double dP = c == 0 ? sp.dPdxRef : sp.dPdzRef;
+    const double e0L = sp.constraint == 0 ? dP : wall + sp.baseShear[c == 0 ? 0 : 1];
+    const double e0 = aL * e0L + (sp.constraint == 0 ? dP : 0.0);
+    const double* Byy = c == 0 ? P.Ubaseyy + fb : P.Wbaseyy + fb;
+    auto sweep = [&](auto KIND) {
+      constexpr int kind = decltype(KIND)::value;
       double d2n2 = 0.0, dqn2 = 0.0;
       for (int i0 = M - 1; i0 >= 0; i0 -= TCH) {
-        // prefetch the streamed inputs of TCH consecutive (descending) elements
         double uv[TCH], qv[TCH];
         R nv[TCH], n1v[TCH];
 #pragma unroll
@@ -1196,7 +1217,7 @@ __global__ void __launch_bounds__(32) k_tau_rhs(GridDev g, int N, SolveParams sp
             uv[k] = uc[i];
             qv[k] = c == 1 ? ((n + 1 <= Nb) ? qo[i + q] : 0.0) : qp[i];
             nv[k] = Nj[(size_t)i * 2 * row];
-            n1v[k] = sp.kind == 1 ? Nj1[(size_t)i * 2 * row] : Q[(size_t)i * 2 * row];
+            n1v[k] = kind == 1 ? Nj1[(size_t)i * 2 * row] : Q[(size_t)i * 2 * row];
           }
         }
 #pragma unroll
@@ -1205,43 +1226,33 @@ __global__ void __launch_bounds__(32) k_tau_rhs(GridDev g, int N, SolveParams sp
           if (i < 0) break;
           const int n = 2 * i + q;
           const double x1 = (n + 1 <= Nb) ? d1o[i + q] : 0.0;
-          double d2 = d2n2 + ct[n] * x1;
+          const double d2 = d2n2 + ct[n] * x1;
           d2n2 = d2;
-          if (n == 0) d2 *= 0.5;
-          double gq;
+          double gv = qv[k];
           if (c == 1) {
-            double dq = dqn2 + ct[n] * qv[k];
-            dqn2 = dq;
-            if (n == 0) dq *= 0.5;
-            gq = dq;
-          } else {
-            gq = part == 0 ? -(kD * qv[k]) : kD * qv[k];
-          }
-          const double u0 = uv[k];
-          double L = nu * (d2 - kappa2 * u0) - gq;  // nu (u'' - kappa^2 u) - grad q
-          if (m00 && part == 0 && c != 1) {
-            L += nu * (c == 0 ? P.Ubaseyy[fb + n] : P.Wbaseyy[fb + n]);
-            if (n == 0) L -= sp.constraint == 0 ? (c == 0 ? sp.dPdxRef : sp.dPdzRef)
-                                                : wall + sp.baseShear[c == 0 ? 0 : 1];
+            gv = dqn2 + ct[n] * qv[k];
+            dqn2 = gv;
           }
           // the nonlinear terms are combined at their own precision R (FP32 on the mixed path)
-          double rhs;
-          if (sp.kind == 1) {
-            const R nc = (R)(-sp.g_b) * nv[k] + (R)(-sp.z_b) * n1v[k];
-            rhs = (u0 * sp.lam + sp.a_b * L) + (double)nc;
+          double Nc;
+          if (kind == 1) {
+            Nc = (double)(gN * nv[k] + zN * n1v[k]);
           } else {
-            const R Qn = n1v[k] * (R)sp.rkA - nv[k];
+            const R Qn = n1v[k] * rA - nv[k];
             if (act) Q[(size_t)i * 2 * row] = Qn;
-            rhs = L + (sp.lam * u0 + sp.B_C * (double)Qn);
+            Nc = BC * (double)Qn;
           }
-          if (m00 && part == 0 && c != 1) {
-            rhs += nu * (c == 0 ? P.Ubaseyy[fb + n] : P.Wbaseyy[fb + n]);
-            if (n == 0 && sp.constraint == 0) rhs -= (c == 0 ? sp.dPdxRef : sp.dPdzRef);
-          }
-          if (act) (c == 1 ? outs : outg)[i] = rhs;
+          const bool n0 = n == 0;
+          double rhs = fma(cu, uv[k], fma(n0 ? cd0 : cd, d2, fma(n0 ? cg0 : cg, gv, Nc)));
+          if (extra) rhs += (aL + 1.0) * (nu * Byy[n]) - (n0 ? e0 : 0.0);
+          if (act) out[i] = rhs;
         }
       }
-    }
+    };
+    if (sp.kind == 1)
+      sweep(std::integral_constant<int, 1>{});
+    else
+      sweep(std::integral_constant<int, 2>{});
   }
   __syncwarp(gmask);
   __threadfence_block();
@@ -1508,6 +1519,7 @@ __global__ void __launch_bounds__(32) k_tau_uw(GridDev g, int N, SolveParams sp,
   SLn r{sm + lane};
   PLn Rc = G(P.scratch + (cu == 0 ? 0 : comp));
   PLn Pp = Gp(P.qout);
+  const double sk = part == 0 ? -kL : kL;  // the part's sign of i k
   auto fill = [&]() {
     for (int i = 0; i < M; i += TCH) {
       double rv[TCH], pv[TCH];
@@ -1519,7 +1531,7 @@ __global__ void __launch_bounds__(32) k_tau_uw(GridDev g, int N, SolveParams sp,
         }
 #pragma unroll
       for (int k = 0; k < TCH; ++k)
-        if (i + k < M) r[i + k] = part == 0 ? -(kL * pv[k]) - rv[k] : kL * pv[k] - rv[k];
+        if (i + k < M) r[i + k] = fma(sk, pv[k], -rv[k]);
     }
   };
   fill();
