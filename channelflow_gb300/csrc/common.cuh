@@ -73,11 +73,19 @@ __host__ __device__ __forceinline__ int mode_kz(const GridDev& g, int m) {
 // scales) is a fixed operator: its rounding error is the same at every step,
 // so it accumulates linearly in time while arithmetic rounding of the
 // changing data accumulates like a random walk.  Each constant therefore
-// exists in DITHER_V roundings: version k is the float nearest to
-// x + s_k ulp(x) with the offsets s_k = (bitrev(k) + 1/2)/V - 1/2 (a
-// low-discrepancy order), so the mean over a cycle of V nonlinear evaluations
-// equals x to about ulp/(2V).  Each field carries its own version index (state
-// that moves with the field), advanced after every nonlinear evaluation.
+// exists in DITHER_V roundings, a stratified stochastic rounding between the
+// two floats lo < x < hi that bracket it: with f = (x - lo)/(hi - lo),
+// version k is hi when f > 1 - t_k and lo otherwise, for the thresholds
+// t_k = (r_k + 1/2)/V where r_k = bitrev(k) with its top bit flipped (a
+// low-discrepancy order whose version 0 is round-to-nearest up to 1/(2V)).
+// Over a cycle of V nonlinear evaluations the mean of the versions equals x
+// to about ulp/(2V), and constants that are floats (1, the FFT scale 2^-m,
+// unit twiddles, integer derivative weights) are exact in every version: an
+// offset rounding of x + s ulp(x) instead would move powers of two down in
+// the versions with s < -1/4 (the float spacing below 2^e is half the
+// spacing above), a bias that does not average out.  Each field carries its
+// own version index (state that moves with the field), advanced after every
+// nonlinear evaluation.
 // Version blocks are `S` bytes apart (constant tables) and `Sb` bytes apart
 // (base-flow values).
 // ---------------------------------------------------------------------------
@@ -95,9 +103,25 @@ struct Dither {
   const float* kmisc;
 };
 
-__host__ __device__ __forceinline__ double dither_offset(int k) {
-  const int r = ((k & 1) << 3) | ((k & 2) << 1) | ((k & 4) >> 1) | ((k & 8) >> 3);
-  return (r + 0.5) / DITHER_V - 0.5;
+// Threshold t_k of version k: (r + 1/2)/V with r the 4-bit reversal of k, top bit flipped.
+__host__ __device__ __forceinline__ double dither_threshold(int k) {
+  const int r = (((k & 1) << 3) | ((k & 2) << 1) | ((k & 4) >> 1) | ((k & 8) >> 3)) ^ 8;
+  return (r + 0.5) / DITHER_V;
+}
+
+// Version k of x in FP32: the bracketing float chosen by the stratified threshold.
+__host__ __device__ __forceinline__ float dither_round(double x, int k) {
+  float lo = (float)x;  // nearest
+  if ((double)lo == x) return lo;
+  float hi;
+  if ((double)lo > x) {
+    hi = lo;
+    lo = nextafterf(hi, -3.0e38f);
+  } else {
+    hi = nextafterf(lo, 3.0e38f);
+  }
+  const double f = (x - (double)lo) / ((double)hi - (double)lo);
+  return f > 1.0 - dither_threshold(k) ? hi : lo;
 }
 
 __device__ __forceinline__ int dither_ver(const Dither& dt, int f) { return dt.ver ? __ldg(dt.ver + f) : 0; }
@@ -116,11 +140,7 @@ __device__ __forceinline__ double dither_const<double>(double x, int) {
 }
 template <>
 __device__ __forceinline__ float dither_const<float>(double x, int k) {
-  const float r = __double2float_rn(x);
-  const float a = fabsf(r);
-  if (a == 0.0f) return r;
-  const float sp = nextafterf(a, 3.0e38f) - a;
-  return __double2float_rn(x + dither_offset(k) * (double)sp);
+  return dither_round(x, k);
 }
 
 // 16-byte vector of R (LDS.128): four floats or two doubles.

@@ -1301,13 +1301,7 @@ int get_slot(cfgpu_dns d, int slot, double* u, double* q) {
 }
 
 // Host rounding of x to float with dither offset k (the device's dither_const<float>).
-float dither_round_host(double x, int k) {
-  const float r = (float)x;
-  const float a = std::fabs(r);
-  if (a == 0.0f) return r;
-  const float sp = std::nextafter(a, 3.0e38f) - a;
-  return (float)(x + dither_offset(k) * (double)sp);
-}
+float dither_round_host(double x, int k) { return dither_round(x, k); }
 
 // DITHER_V versions of the tables (tables[i] at float offset off[i] of each S-float version) in one block.
 int upload_dithered(const std::vector<std::vector<double>>& tables, const std::vector<size_t>& off, size_t S,

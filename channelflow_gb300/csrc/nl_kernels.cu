@@ -85,13 +85,26 @@ __global__ void k_curl_base(GridDev g, const double* __restrict__ U, R* __restri
 //   forward (values -> coefficients, chebyfft, chebyshev.cpp:262-284):
 //       a_{2k} = sum_j Fe[k][j] (u_j + u_{N-1-j}),  a_{2k+1} = sum_j Fo[k][j] (u_j - u_{N-1-j})
 // A (P x KA) and B (P x KB) hold the two half matrices (host-built in double).
+// CS (FP32 forward transforms): the sum runs over groups of four terms (one
+// matrix vector load), each group summed with FMAs and added to the running
+// sum with an error-free two-sum whose errors are accumulated separately
+// (compensated summation): the forward sums add terms of similar size, so the
+// plain running sum's rounding would grow with the number of terms.
 // ---------------------------------------------------------------------------
 #define CHEB_TL 64
 #define CHEB_WARPS 8
 #define CHEB_PT 9
 
-template <typename TI, typename R, typename TO>
-__global__ void __launch_bounds__(256) k_cheb(int N, int inverse, int nlines, const TI* __restrict__ in, size_t ld_in,
+template <typename R>
+__device__ __forceinline__ void two_sum_acc(R& s, R t, R& c) {
+  const R s1 = s + t;
+  const R bp = s1 - s;
+  c += (s - (s1 - bp)) + (t - bp);
+  s = s1;
+}
+
+template <typename TI, typename R, typename TO, bool CS>
+__global__ void __launch_bounds__(256, CS ? 3 : 1) k_cheb(int N, int inverse, int nlines, const TI* __restrict__ in, size_t ld_in,
                                               size_t cs_in, TO* __restrict__ out, size_t ld_out, size_t cs_out,
                                               const R* __restrict__ Amat, const R* __restrict__ Bmat, int P, int KA,
                                               int KB, Dither dt, int lpf) {
@@ -151,8 +164,10 @@ __global__ void __launch_bounds__(256) k_cheb(int N, int inverse, int nlines, co
   __syncthreads();
   const int lane = tid & 31, warp = tid >> 5;
   R accA[CHEB_PT][2], accB[CHEB_PT][2];
+  R cmpA[CHEB_PT][2], cmpB[CHEB_PT][2];  // compensation terms (CS)
 #pragma unroll
-  for (int i = 0; i < CHEB_PT; ++i) accA[i][0] = accA[i][1] = accB[i][0] = accB[i][1] = (R)0;
+  for (int i = 0; i < CHEB_PT; ++i)
+    accA[i][0] = accA[i][1] = accB[i][0] = accB[i][1] = cmpA[i][0] = cmpA[i][1] = cmpB[i][0] = cmpB[i][1] = (R)0;
   // high n first (the small terms are summed before the large), VW columns per matrix load
   for (int kb = KAp / VW - 1; kb >= 0; --kb) {
     R x0[VW], x1[VW];
@@ -167,10 +182,21 @@ __global__ void __launch_bounds__(256) k_cheb(int N, int inverse, int nlines, co
       if (p < P) {
         const V a4 = *reinterpret_cast<const V*>(As + p * KAp + kb * VW);
         const R* a = reinterpret_cast<const R*>(&a4);
+        if (CS) {
+          R t0 = a[VW - 1] * x0[VW - 1], t1 = a[VW - 1] * x1[VW - 1];
 #pragma unroll
-        for (int e = VW - 1; e >= 0; --e) {
-          accA[i][0] += a[e] * x0[e];
-          accA[i][1] += a[e] * x1[e];
+          for (int e = VW - 2; e >= 0; --e) {
+            t0 += a[e] * x0[e];
+            t1 += a[e] * x1[e];
+          }
+          two_sum_acc(accA[i][0], t0, cmpA[i][0]);
+          two_sum_acc(accA[i][1], t1, cmpA[i][1]);
+        } else {
+#pragma unroll
+          for (int e = VW - 1; e >= 0; --e) {
+            accA[i][0] += a[e] * x0[e];
+            accA[i][1] += a[e] * x1[e];
+          }
         }
       }
     }
@@ -188,10 +214,21 @@ __global__ void __launch_bounds__(256) k_cheb(int N, int inverse, int nlines, co
       if (p < P) {
         const V b4 = *reinterpret_cast<const V*>(Bs + p * KBp + kb * VW);
         const R* b = reinterpret_cast<const R*>(&b4);
+        if (CS) {
+          R t0 = b[VW - 1] * x0[VW - 1], t1 = b[VW - 1] * x1[VW - 1];
 #pragma unroll
-        for (int e = VW - 1; e >= 0; --e) {
-          accB[i][0] += b[e] * x0[e];
-          accB[i][1] += b[e] * x1[e];
+          for (int e = VW - 2; e >= 0; --e) {
+            t0 += b[e] * x0[e];
+            t1 += b[e] * x1[e];
+          }
+          two_sum_acc(accB[i][0], t0, cmpB[i][0]);
+          two_sum_acc(accB[i][1], t1, cmpB[i][1]);
+        } else {
+#pragma unroll
+          for (int e = VW - 1; e >= 0; --e) {
+            accB[i][0] += b[e] * x0[e];
+            accB[i][1] += b[e] * x1[e];
+          }
         }
       }
     }
@@ -210,8 +247,8 @@ __global__ void __launch_bounds__(256) k_cheb(int N, int inverse, int nlines, co
         if (p < J) out[(N - 1 - p) * ld_out + gl] = (TO)(accA[i][h] - accB[i][h]);
       } else {
         // p = k: even coefficient 2k, odd coefficient 2k+1
-        out[(2 * p) * ld_out + gl] = (TO)accA[i][h];
-        if (2 * p + 1 < N) out[(2 * p + 1) * ld_out + gl] = (TO)accB[i][h];
+        out[(2 * p) * ld_out + gl] = (TO)(CS ? accA[i][h] + cmpA[i][h] : accA[i][h]);
+        if (2 * p + 1 < N) out[(2 * p + 1) * ld_out + gl] = (TO)(CS ? accB[i][h] + cmpB[i][h] : accB[i][h]);
       }
     }
   }
@@ -639,14 +676,24 @@ cudaError_t launch_cheb(int N, bool inverse, int nlines, int ncomp, const TI* in
   const size_t sm = cheb_smem_bytes(N, sizeof(R));
   // kernel attributes set once per process (thread-safe static initialisation)
   static const bool attr_set = [] {
-    cudaFuncSetAttribute(k_cheb<TI, R, TO>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_cheb<TI, R, TO, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if constexpr (sizeof(R) == 4)
+      cudaFuncSetAttribute(k_cheb<TI, R, TO, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     return true;
   }();
   (void)attr_set;
   const int nf = dt.nb > 0 ? dt.nb : 1, lpf = (nlines + nf - 1) / nf;
   dim3 grid(nf * ((lpf + CHEB_TL - 1) / CHEB_TL), ncomp);
-  k_cheb<TI, R, TO><<<grid, 32 * CHEB_WARPS, sm, st>>>(N, inverse ? 1 : 0, nlines, in, ld_in, cs_in, out, ld_out,
-                                                       cs_out, A, B, P, KA, KB, dt, lpf);
+  // compensated sums for the FP32 forward transforms
+  if constexpr (sizeof(R) == 4) {
+    if (!inverse) {
+      k_cheb<TI, R, TO, true><<<grid, 32 * CHEB_WARPS, sm, st>>>(N, 0, nlines, in, ld_in, cs_in, out, ld_out, cs_out,
+                                                                 A, B, P, KA, KB, dt, lpf);
+      return cudaGetLastError();
+    }
+  }
+  k_cheb<TI, R, TO, false><<<grid, 32 * CHEB_WARPS, sm, st>>>(N, inverse ? 1 : 0, nlines, in, ld_in, cs_in, out,
+                                                              ld_out, cs_out, A, B, P, KA, KB, dt, lpf);
   return cudaGetLastError();
 }
 
