@@ -88,6 +88,7 @@ _SIGS = {
                                            _PD, _PD, _PD, _PD],
     "cfgpu_dns_host_access": [C.c_void_p, C.POINTER(C.c_int)],
     "cfgpu_measure_fp64": [_PD, _PD],
+    "cfgpu_dither_versions": [C.c_double, C.POINTER(C.c_float)],
     "cfgpu_timestep_adjust_for_T": [C.c_void_p, C.c_double, _PI, _PI, _PD],
     "cfgpu_timestep_adjust": [C.c_void_p, C.c_double, _PI, _PI],
     "cfgpu_ensemble_create": [C.POINTER(Grid), C.POINTER(Flags), C.c_int, C.c_int, C.POINTER(C.c_void_p)],

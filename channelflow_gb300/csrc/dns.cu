@@ -1951,6 +1951,12 @@ extern "C" {
 
 const char* cfgpu_version(void) { return "cfgpu 0.1 (sm_103a)"; }
 
+cfgpu_status cfgpu_dither_versions(double x, float* versions16) {
+  if (!versions16) return fail(CFGPU_EINVAL, "null argument");
+  for (int k = 0; k < DITHER_V; ++k) versions16[k] = dither_round_host(x, k);
+  return CFGPU_OK;
+}
+
 cfgpu_status cfgpu_measure_fp64(double* tflops, double* cycles_per_fma) {
   if (!tflops || !cycles_per_fma) return fail(CFGPU_EINVAL, "null argument");
   int dev = 0, sms = 0;
