@@ -727,19 +727,19 @@ __device__ double diff_s(int M, int q, const double* ct, SLn xo, SLn* dst) {
   double dn2 = 0.0, sum = 0.0;
   int i = M - 1;
   if (q == 0) {  // top even index n = N-1: x[N] = 0
-    const double v = dn2 + ct[2 * i] * 0.0;
-    if (dst) (*dst)[i] = v;
-    sum += v;
-    dn2 = v;
+    if (dst) (*dst)[i] = 0.0;
     i--;
   }
   for (; i >= 0; --i) {
-    const int n = 2 * i + q;
-    double v = dn2 + ct[n] * xo[i + q];
+    const double v = dn2 + ct[2 * i + q] * xo[i + q];
     dn2 = v;
-    if (n == 0) v *= 0.5;
     if (dst) (*dst)[i] = v;
     sum += v;
+  }
+  // the n = 0 coefficient is halved (q = 0: the last one summed, dn2)
+  if (q == 0) {
+    if (dst) (*dst)[0] = 0.5 * dn2;
+    sum -= 0.5 * dn2;
   }
   return sum;
 }
@@ -1031,6 +1031,7 @@ __device__ void helm_t(int M, int q, const double* __restrict__ hlo, const doubl
   double acc = bc - band[M - 1] * unext;
   double fi1 = fi;
   fi = fm;
+#pragma unroll 4
   for (int i = M - 2; i >= 1; --i) {
     const int n = 2 * i + q;
     const double fm1 = f[i - 1];
@@ -1044,6 +1045,7 @@ __device__ void helm_t(int M, int q, const double* __restrict__ hlo, const doubl
   }
   double prev = acc / band[0];
   u[0] = prev;
+#pragma unroll 4
   for (int i = 1; i < M; ++i) {
     prev = (u[i] - lo[i] * prev) * inv[i];
     u[i] = prev;
@@ -1294,24 +1296,25 @@ __global__ void __launch_bounds__(32) k_tau_solve_t(GridDev g, int N, SolveParam
   auto TB = [&](int f) { return PLn{tt.f + f * FN + m + q * Md, 2 * Md}; };
   auto TS = [&](int k) { return TLn{tab + ((size_t)k * N + q) * 8 + mi}; };
   // stage factor fields f0..f3 of this warp's 8 modes into tab
-  auto stage = [&](int f0) {
+  // (lane l copies mode mbase + l % 8 of rows n = l / 8 + 4 j: entry [k][n][l % 8] = tab[k N 8 + l + 32 j])
+  auto stage = [&](int f0, int nf) {
     __syncwarp();
-    const int total = 4 * N * 8;
-    for (int b0 = lane; b0 < total; b0 += 32 * 16) {
-      double v[16];
+    const bool mok = mbase + (lane & 7) < Md;
+#pragma unroll 1
+    for (int k = 0; k < nf; ++k) {
+      const double* src = tt.f + (size_t)(f0 + k) * FN + mbase + (lane & 7) + (size_t)(lane >> 3) * Md;
+      double* dst = tab + (size_t)k * N * 8 + lane;
+      for (int n0 = lane >> 3; n0 < N; n0 += 4 * 16) {
+        double v[16];
 #pragma unroll
-      for (int k2 = 0; k2 < 16; ++k2) {
-        const int idx = b0 + 32 * k2;
-        v[k2] = 0.0;
-        if (idx < total) {
-          const int k = idx / (N * 8), rem = idx - k * N * 8;
-          const int n = rem >> 3, mm = mbase + (rem & 7);
-          if (mm < Md) v[k2] = __ldg(&tt.f[(size_t)(f0 + k) * FN + (size_t)n * Md + mm]);
-        }
+        for (int k2 = 0; k2 < 16; ++k2)
+          v[k2] = (mok && n0 + 4 * k2 < N) ? __ldg(src + (size_t)(4 * k2) * Md) : 0.0;
+#pragma unroll
+        for (int k2 = 0; k2 < 16; ++k2)
+          if (n0 + 4 * k2 < N) dst[32 * k2] = v[k2];
+        src += (size_t)64 * Md;
+        dst += 32 * 16;
       }
-#pragma unroll
-      for (int k2 = 0; k2 < 16; ++k2)
-        if (b0 + 32 * k2 < total) tab[b0 + 32 * k2] = v[k2];
     }
     __syncwarp();
   };
@@ -1323,7 +1326,6 @@ __global__ void __launch_bounds__(32) k_tau_solve_t(GridDev g, int N, SolveParam
   const double kzL = 2 * M_PI * kz / g.Lz;
   const int fld = mode_field(g, m);
   if (P.slot) apply_slot(sp, P.slot[fld]);
-  const size_t fb = (size_t)P.base_stride * fld;
   const double nu = sp.nu;
   const double lambda = tt.s[TS_LAMBDA * Md + m];
   const double* __restrict__ hlo = hb.lo;
@@ -1332,15 +1334,16 @@ __global__ void __launch_bounds__(32) k_tau_solve_t(GridDev g, int N, SolveParam
 
   // ---- A: right-hand side (k_tau_rhs): Rx, Rz in scratch lines 0, 1; Ry (line 2) into slot 0 ------
   {
+    // batches of 2 TCH loads in flight (one warp per SM sub-partition: nothing else hides their latency)
     PLn Ryg = G(P.scratch + 2 * comp);
     SLn outy = S(0);
-    for (int i = 0; i < M; i += TCH) {
-      double v[TCH];
+    for (int i = 0; i < M; i += 2 * TCH) {
+      double v[2 * TCH];
 #pragma unroll
-      for (int k = 0; k < TCH; ++k)
+      for (int k = 0; k < 2 * TCH; ++k)
         if (i + k < M) v[k] = Ryg[i + k];
 #pragma unroll
-      for (int k = 0; k < TCH; ++k)
+      for (int k = 0; k < 2 * TCH; ++k)
         if (i + k < M) outy[i + k] = v[k];
     }
   }
@@ -1348,21 +1351,21 @@ __global__ void __launch_bounds__(32) k_tau_solve_t(GridDev g, int N, SolveParam
   __threadfence_block();
 
   // ---- B: pressure ---------------------------------------------------------
-  stage(TF_PBAND);
+  stage(TF_PBAND, 4);
   {
     SLn rr = S(2);
     diff_s(M, q, ct, So(0), &rr);
     PLn Rxp = Gp(Rxg), Rzp = Gp(Rzg);
-    for (int i = 0; i < M; i += TCH) {
-      double xa[TCH], za[TCH];
+    for (int i = 0; i < M; i += 2 * TCH) {
+      double xa[2 * TCH], za[2 * TCH];
 #pragma unroll
-      for (int k = 0; k < TCH; ++k)
+      for (int k = 0; k < 2 * TCH; ++k)
         if (i + k < M) {
           xa[k] = Rxp[i + k];
           za[k] = Rzp[i + k];
         }
 #pragma unroll
-      for (int k = 0; k < TCH; ++k)
+      for (int k = 0; k < 2 * TCH; ++k)
         if (i + k < M) {
           const double x = kxL * xa[k] + kzL * za[k];
           rr[i + k] = part == 0 ? rr[i + k] - x : rr[i + k] + x;
@@ -1370,7 +1373,7 @@ __global__ void __launch_bounds__(32) k_tau_solve_t(GridDev g, int N, SolveParam
     }
     helm_t(M, q, hlo, hdi, hup, TS(0), TS(1), TS(2), TS(3), rr, S(1), 0.0);
   }
-  stage(TF_VBAND);
+  stage(TF_VBAND, 4);
   // ---- C: wall-normal velocity, influence and tau corrections -------------
   SLn Pl = S(1), Vl = S(0);
   const double RyTop = S(0)[M - 1];
@@ -1487,22 +1490,23 @@ __global__ void __launch_bounds__(32) k_tau_uw(GridDev g, int N, SolveParams sp,
   const int M = q ? (N - 1) / 2 : M0;
   double* tab = sm + (size_t)M0 * 32;  // [4][N][4]
   {
-    const int total = 4 * N * 4;
-    for (int b0 = lane; b0 < total; b0 += 32 * 16) {
-      double v[16];
+    // lane l copies mode mbase + l % 4 of rows n = l / 4 + 8 j: entry [k][n][l % 4] = tab[k N 4 + l + 32 j]
+    const bool mok = mbase + (lane & 3) < Md;
+#pragma unroll 1
+    for (int k = 0; k < 4; ++k) {
+      const double* src = tt.f + (size_t)(TF_VBAND + k) * FN + mbase + (lane & 3) + (size_t)(lane >> 2) * Md;
+      double* dst = tab + (size_t)k * N * 4 + lane;
+      for (int n0 = lane >> 2; n0 < N; n0 += 8 * 16) {
+        double v[16];
 #pragma unroll
-      for (int k2 = 0; k2 < 16; ++k2) {
-        const int idx = b0 + 32 * k2;
-        v[k2] = 0.0;
-        if (idx < total) {
-          const int k = idx / (N * 4), rem = idx - k * N * 4;
-          const int n = rem >> 2, mm = mbase + (rem & 3);
-          if (mm < Md) v[k2] = __ldg(&tt.f[(size_t)(TF_VBAND + k) * FN + (size_t)n * Md + mm]);
-        }
+        for (int k2 = 0; k2 < 16; ++k2)
+          v[k2] = (mok && n0 + 8 * k2 < N) ? __ldg(src + (size_t)(8 * k2) * Md) : 0.0;
+#pragma unroll
+        for (int k2 = 0; k2 < 16; ++k2)
+          if (n0 + 8 * k2 < N) dst[32 * k2] = v[k2];
+        src += (size_t)128 * Md;
+        dst += 32 * 16;
       }
-#pragma unroll
-      for (int k2 = 0; k2 < 16; ++k2)
-        if (b0 + 32 * k2 < total) tab[b0 + 32 * k2] = v[k2];
     }
   }
   __syncwarp();
@@ -1521,16 +1525,16 @@ __global__ void __launch_bounds__(32) k_tau_uw(GridDev g, int N, SolveParams sp,
   PLn Pp = Gp(P.qout);
   const double sk = part == 0 ? -kL : kL;  // the part's sign of i k
   auto fill = [&]() {
-    for (int i = 0; i < M; i += TCH) {
-      double rv[TCH], pv[TCH];
+    for (int i = 0; i < M; i += 2 * TCH) {
+      double rv[2 * TCH], pv[2 * TCH];
 #pragma unroll
-      for (int k = 0; k < TCH; ++k)
+      for (int k = 0; k < 2 * TCH; ++k)
         if (i + k < M) {
           rv[k] = Rc[i + k];
           pv[k] = Pp[i + k];
         }
 #pragma unroll
-      for (int k = 0; k < TCH; ++k)
+      for (int k = 0; k < 2 * TCH; ++k)
         if (i + k < M) r[i + k] = fma(sk, pv[k], -rv[k]);
     }
   };
