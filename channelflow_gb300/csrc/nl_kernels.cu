@@ -85,8 +85,8 @@ __global__ void k_curl_base(GridDev g, const double* __restrict__ U, R* __restri
 //   forward (values -> coefficients, chebyfft, chebyshev.cpp:262-284):
 //       a_{2k} = sum_j Fe[k][j] (u_j + u_{N-1-j}),  a_{2k+1} = sum_j Fo[k][j] (u_j - u_{N-1-j})
 // A (P x KA) and B (P x KB) hold the two half matrices (host-built in double).
-// CS (FP32 forward transforms): the sum runs over groups of four terms (one
-// matrix vector load), each group summed with FMAs and added to the running
+// CS (FP32 forward transforms): the sum runs over groups of eight terms (two
+// matrix vector loads), each group summed with FMAs and added to the running
 // sum with an error-free two-sum whose errors are accumulated separately
 // (compensated summation): the forward sums add terms of similar size, so the
 // plain running sum's rounding would grow with the number of terms.
@@ -168,66 +168,86 @@ __global__ void __launch_bounds__(256, CS ? 3 : 1) k_cheb(int N, int inverse, in
 #pragma unroll
   for (int i = 0; i < CHEB_PT; ++i)
     accA[i][0] = accA[i][1] = accB[i][0] = accB[i][1] = cmpA[i][0] = cmpA[i][1] = cmpB[i][0] = cmpB[i][1] = (R)0;
-  // high n first (the small terms are summed before the large), VW columns per matrix load
-  for (int kb = KAp / VW - 1; kb >= 0; --kb) {
-    R x0[VW], x1[VW];
+  // high n first (the small terms are summed before the large), VW columns per matrix load; the compensated
+  // form adds groups of CG matrix loads (2 VW terms) to the running sum
+  constexpr int CG = CS ? 2 : 1;
+  for (int kb = KAp / VW - 1; kb >= 0; kb -= CG) {
+    R x0[CG][VW], x1[CG][VW];
 #pragma unroll
-    for (int e = 0; e < VW; ++e) {
-      x0[e] = xa[(kb * VW + e) * CHEB_TL + lane];
-      x1[e] = xa[(kb * VW + e) * CHEB_TL + lane + 32];
-    }
+    for (int gq = 0; gq < CG; ++gq)
+#pragma unroll
+      for (int e = 0; e < VW; ++e) {
+        const int k = (kb - gq) * VW + e;
+        x0[gq][e] = k >= 0 ? xa[k * CHEB_TL + lane] : (R)0;
+        x1[gq][e] = k >= 0 ? xa[k * CHEB_TL + lane + 32] : (R)0;
+      }
 #pragma unroll
     for (int i = 0; i < CHEB_PT; ++i) {
       const int p = warp + CHEB_WARPS * i;
       if (p < P) {
-        const V a4 = *reinterpret_cast<const V*>(As + p * KAp + kb * VW);
-        const R* a = reinterpret_cast<const R*>(&a4);
         if (CS) {
-          R t0 = a[VW - 1] * x0[VW - 1], t1 = a[VW - 1] * x1[VW - 1];
+          R t0 = (R)0, t1 = (R)0;
 #pragma unroll
-          for (int e = VW - 2; e >= 0; --e) {
-            t0 += a[e] * x0[e];
-            t1 += a[e] * x1[e];
+          for (int gq = 0; gq < CG; ++gq) {
+            if (kb - gq < 0) break;  // uniform over the block
+            const V a4 = *reinterpret_cast<const V*>(As + p * KAp + (kb - gq) * VW);
+            const R* a = reinterpret_cast<const R*>(&a4);
+#pragma unroll
+            for (int e = VW - 1; e >= 0; --e) {
+              t0 += a[e] * x0[gq][e];
+              t1 += a[e] * x1[gq][e];
+            }
           }
           two_sum_acc(accA[i][0], t0, cmpA[i][0]);
           two_sum_acc(accA[i][1], t1, cmpA[i][1]);
         } else {
+          const V a4 = *reinterpret_cast<const V*>(As + p * KAp + kb * VW);
+          const R* a = reinterpret_cast<const R*>(&a4);
 #pragma unroll
           for (int e = VW - 1; e >= 0; --e) {
-            accA[i][0] += a[e] * x0[e];
-            accA[i][1] += a[e] * x1[e];
+            accA[i][0] += a[e] * x0[0][e];
+            accA[i][1] += a[e] * x1[0][e];
           }
         }
       }
     }
   }
-  for (int kb = KBp / VW - 1; kb >= 0; --kb) {
-    R x0[VW], x1[VW];
+  for (int kb = KBp / VW - 1; kb >= 0; kb -= CG) {
+    R x0[CG][VW], x1[CG][VW];
 #pragma unroll
-    for (int e = 0; e < VW; ++e) {
-      x0[e] = xb[(kb * VW + e) * CHEB_TL + lane];
-      x1[e] = xb[(kb * VW + e) * CHEB_TL + lane + 32];
-    }
+    for (int gq = 0; gq < CG; ++gq)
+#pragma unroll
+      for (int e = 0; e < VW; ++e) {
+        const int k = (kb - gq) * VW + e;
+        x0[gq][e] = k >= 0 ? xb[k * CHEB_TL + lane] : (R)0;
+        x1[gq][e] = k >= 0 ? xb[k * CHEB_TL + lane + 32] : (R)0;
+      }
 #pragma unroll
     for (int i = 0; i < CHEB_PT; ++i) {
       const int p = warp + CHEB_WARPS * i;
       if (p < P) {
-        const V b4 = *reinterpret_cast<const V*>(Bs + p * KBp + kb * VW);
-        const R* b = reinterpret_cast<const R*>(&b4);
         if (CS) {
-          R t0 = b[VW - 1] * x0[VW - 1], t1 = b[VW - 1] * x1[VW - 1];
+          R t0 = (R)0, t1 = (R)0;
 #pragma unroll
-          for (int e = VW - 2; e >= 0; --e) {
-            t0 += b[e] * x0[e];
-            t1 += b[e] * x1[e];
+          for (int gq = 0; gq < CG; ++gq) {
+            if (kb - gq < 0) break;  // uniform over the block
+            const V b4 = *reinterpret_cast<const V*>(Bs + p * KBp + (kb - gq) * VW);
+            const R* b = reinterpret_cast<const R*>(&b4);
+#pragma unroll
+            for (int e = VW - 1; e >= 0; --e) {
+              t0 += b[e] * x0[gq][e];
+              t1 += b[e] * x1[gq][e];
+            }
           }
           two_sum_acc(accB[i][0], t0, cmpB[i][0]);
           two_sum_acc(accB[i][1], t1, cmpB[i][1]);
         } else {
+          const V b4 = *reinterpret_cast<const V*>(Bs + p * KBp + kb * VW);
+          const R* b = reinterpret_cast<const R*>(&b4);
 #pragma unroll
           for (int e = VW - 1; e >= 0; --e) {
-            accB[i][0] += b[e] * x0[e];
-            accB[i][1] += b[e] * x1[e];
+            accB[i][0] += b[e] * x0[0][e];
+            accB[i][1] += b[e] * x1[0][e];
           }
         }
       }

@@ -1135,6 +1135,7 @@ __global__ void __launch_bounds__(32) k_tau_rhs(GridDev g, int N, SolveParams sp
       }
     }
   } else {
+    constexpr int RB = TCH;  // loads in flight per batch of the streamed lines
     const double kappa2 = 4 * M_PI * M_PI * ((kx / g.Lx) * (kx / g.Lx) + (kz / g.Lz) * (kz / g.Lz));
     const double Dx = 2 * M_PI * kx / g.Lx * (kx == g.kxmax ? 0.0 : 1.0);
     const double Dz = 2 * M_PI * kz / g.Lz * (kz == g.kzmax ? 0.0 : 1.0);
@@ -1152,13 +1153,13 @@ __global__ void __launch_bounds__(32) k_tau_rhs(GridDev g, int N, SolveParams sp
         d1[i] = 0.0;
         i--;
       }
-      for (; i >= 0; i -= TCH) {
-        double xv[TCH];
+      for (; i >= 0; i -= RB) {
+        double xv[RB];
 #pragma unroll
-        for (int k = 0; k < TCH; ++k)
+        for (int k = 0; k < RB; ++k)
           if (i - k >= 0) xv[k] = uo[i - k + q];
 #pragma unroll
-        for (int k = 0; k < TCH; ++k)
+        for (int k = 0; k < RB; ++k)
           if (i - k >= 0) {
             const double v = dn2 + ct[2 * (i - k) + q] * xv[k];
             dn2 = v;
@@ -1208,11 +1209,11 @@ __global__ void __launch_bounds__(32) k_tau_rhs(GridDev g, int N, SolveParams sp
     auto sweep = [&](auto KIND) {
       constexpr int kind = decltype(KIND)::value;
       double d2n2 = 0.0, dqn2 = 0.0;
-      for (int i0 = M - 1; i0 >= 0; i0 -= TCH) {
-        double uv[TCH], qv[TCH];
-        R nv[TCH], n1v[TCH];
+      for (int i0 = M - 1; i0 >= 0; i0 -= RB) {
+        double uv[RB], qv[RB];
+        R nv[RB], n1v[RB];
 #pragma unroll
-        for (int k = 0; k < TCH; ++k) {
+        for (int k = 0; k < RB; ++k) {
           const int i = i0 - k;
           if (i >= 0) {
             const int n = 2 * i + q;
@@ -1223,7 +1224,7 @@ __global__ void __launch_bounds__(32) k_tau_rhs(GridDev g, int N, SolveParams sp
           }
         }
 #pragma unroll
-        for (int k = 0; k < TCH; ++k) {
+        for (int k = 0; k < RB; ++k) {
           const int i = i0 - k;
           if (i < 0) break;
           const int n = 2 * i + q;
