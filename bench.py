@@ -143,6 +143,24 @@ def bytes_per_step(Md, prec):
     return bnl, btau
 
 
+def flops_per_step(Md):
+    """Algorithmic FP64-roofline FLOPs of one step (fixed by formula, independent of the implementation):
+    9 component transforms (6 inverse, 3 forward), each Ny planes x 2.5 NxNz log2(NxNz) for x-z plus
+    2 Md lines x 2.5 (2(Ny-1)) log2(2(Ny-1)) for y, and about 150 Ny flops per mode for the tau solve."""
+    xz = NY * 2.5 * NX * NZ * math.log2(NX * NZ)
+    y = 2 * Md * 2.5 * 2 * (NY - 1) * math.log2(2 * (NY - 1))
+    return 9 * (xz + y), 150.0 * NY * Md
+
+
+def fp64_peak():
+    """FP64 FMA throughput of this GPU in TFLOP/s (cfgpu_measure_fp64: 8 independent chains per thread)."""
+    import ctypes as C
+    from channelflow_gb300 import _lib as L
+    tf, cyc = C.c_double(), C.c_double()
+    L.check(L.load().cfgpu_measure_fp64(C.byref(tf), C.byref(cyc)))
+    return tf.value, cyc.value
+
+
 def run_gpu(args, rank, world):
     import ctypes  # noqa: F401
     from channelflow_gb300 import DNS, Grid
@@ -521,6 +539,9 @@ def main():
                "sample": "%d full CNAB2 steps of the 128x97x128 field (after 1 untimed SMRK2 start-up step), "
                          "NumPy restatement of the reference on one host core, %.1f s" % (args.cpu_steps, csecs)}
     bnl64, btau64 = bytes_per_step(Md, "fp64")
+    ftr, ftau = flops_per_step(Md)
+    pk64, cyc64 = fp64_peak()
+    tau64 = f["tau_ms"] / max(1, f["tau_n"])
     line = {
         "metric": METRIC, "value": sps, "unit": "steps/s", "n_gpus": world, "steps": m["K"],
         "warmup": args.warmup, "ms_per_step": m["ms"] / m["K"], "higher_is_better": True, "scaling": "weak",
@@ -542,6 +563,17 @@ def main():
         "fp64": {"value": sps64, "unit": "steps/s", "ms_per_step": f["ms"] / f["K"], "steps": f["K"],
                  "nl_avg_ms": f["nl_ms"] / max(1, f["nl_n"]), "tau_avg_ms": f["tau_ms"] / max(1, f["tau_n"]),
                  "nl_alg_bytes": bnl64, "tau_alg_bytes": btau64},
+        # FP64 roofline (the tau solve of both paths and the whole plain-FP64 step compute in FP64): algorithmic
+        # FLOPs by formula over the FP64 FMA throughput measured on this GPU in this run
+        "roofline_fp64": {"peak_tflops": pk64, "dependent_dfma_cycles": cyc64,
+                          "peak_source": "cfgpu_measure_fp64 (FMA microbenchmark, this run)",
+                          "tau_solve_mixed": {"flops": ftau, "achieved_tflops": ftau / (tau_avg / 1e3) / 1e12,
+                                              "frac": ftau / (tau_avg / 1e3) / 1e12 / pk64},
+                          "tau_solve_fp64": {"flops": ftau, "achieved_tflops": ftau / (tau64 / 1e3) / 1e12,
+                                             "frac": ftau / (tau64 / 1e3) / 1e12 / pk64},
+                          "fp64_step": {"flops": ftr + ftau,
+                                        "achieved_tflops": (ftr + ftau) / (f["ms"] / f["K"] / 1e3) / 1e12,
+                                        "frac": (ftr + ftau) / (f["ms"] / f["K"] / 1e3) / 1e12 / pk64}},
         "accuracy": acc,
         "e2e": {"value": world * e["K"] / e["s"], "unit": "steps/s", "h2d_bytes_per_step": e["h2d"],
                 "d2h_bytes_per_step": e["d2h"],
