@@ -73,7 +73,7 @@ __host__ __device__ __forceinline__ int mode_kz(const GridDev& g, int m) {
 // scales) is a fixed operator: its rounding error is the same at every step,
 // so it accumulates linearly in time while arithmetic rounding of the
 // changing data accumulates like a random walk.  Each constant therefore
-// exists in DITHER_V roundings, a stratified stochastic rounding between the
+// exists in DITHER_V (64) roundings, a stratified stochastic rounding between the
 // two floats lo < x < hi that bracket it: with f = (x - lo)/(hi - lo),
 // version k is hi when f > 1 - t_k and lo otherwise, for the thresholds
 // t_k = (r_k + 1/2)/V where r_k = bitrev(k) with its top bit flipped (a
@@ -89,7 +89,8 @@ __host__ __device__ __forceinline__ int mode_kz(const GridDev& g, int m) {
 // Version blocks are `S` bytes apart (constant tables) and `Sb` bytes apart
 // (base-flow values).
 // ---------------------------------------------------------------------------
-#define DITHER_V 16
+#define DITHER_BITS 6
+#define DITHER_V (1 << DITHER_BITS)
 
 struct Dither {
   const int* ver;  // per-field version index; null: version 0 of undithered tables
@@ -103,10 +104,11 @@ struct Dither {
   const float* kmisc;
 };
 
-// Threshold t_k of version k: (r + 1/2)/V with r the 4-bit reversal of k, top bit flipped.
+// Threshold t_k of version k: (r + 1/2)/V with r the DITHER_BITS-bit reversal of k, top bit flipped.
 __host__ __device__ __forceinline__ double dither_threshold(int k) {
-  const int r = (((k & 1) << 3) | ((k & 2) << 1) | ((k & 4) >> 1) | ((k & 8) >> 3)) ^ 8;
-  return (r + 0.5) / DITHER_V;
+  int r = 0;
+  for (int b = 0; b < DITHER_BITS; ++b) r |= ((k >> b) & 1) << (DITHER_BITS - 1 - b);
+  return ((r ^ (DITHER_V / 2)) + 0.5) / DITHER_V;
 }
 
 // Version k of x in FP32: the bracketing float chosen by the stratified threshold.

@@ -1951,9 +1951,10 @@ extern "C" {
 
 const char* cfgpu_version(void) { return "cfgpu 0.1 (sm_103a)"; }
 
-cfgpu_status cfgpu_dither_versions(double x, float* versions16) {
-  if (!versions16) return fail(CFGPU_EINVAL, "null argument");
-  for (int k = 0; k < DITHER_V; ++k) versions16[k] = dither_round_host(x, k);
+cfgpu_status cfgpu_dither_versions(double x, float* versions) {
+  static_assert(DITHER_V == CFGPU_DITHER_VERSIONS, "version count of the C ABI");
+  if (!versions) return fail(CFGPU_EINVAL, "null argument");
+  for (int k = 0; k < DITHER_V; ++k) versions[k] = dither_round_host(x, k);
   return CFGPU_OK;
 }
 

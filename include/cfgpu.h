@@ -425,12 +425,14 @@ cfgpu_status cfgpu_tau_solve_batched_noalloc(int N, int nmodes, const int* kx, c
 cfgpu_status cfgpu_measure_fp64(double* tflops, double* cycles_per_fma);
 
 /*
- * The 16 FP32 versions of the constant x that the mixed precision passes
- * cycle through, one per nonlinear evaluation (no reference counterpart; host
- * only, no device call): a stratified stochastic rounding between the two
- * floats that bracket x, whose mean is x to 1/32 of the float spacing.
+ * The CFGPU_DITHER_VERSIONS FP32 versions of the constant x that the mixed
+ * precision passes cycle through, one per nonlinear evaluation (no reference
+ * counterpart; host only, no device call): a stratified stochastic rounding
+ * between the two floats that bracket x, whose mean is x to 1/(2 V) of the
+ * float spacing.  versions holds CFGPU_DITHER_VERSIONS floats.
  */
-cfgpu_status cfgpu_dither_versions(double x, float* versions16);
+#define CFGPU_DITHER_VERSIONS 64
+cfgpu_status cfgpu_dither_versions(double x, float* versions);
 
 /* Library version string. */
 const char* cfgpu_version(void);

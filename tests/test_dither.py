@@ -1,17 +1,19 @@
 """The dithered FP32 constants of the mixed precision passes (cfgpu_dither_versions, host only).
 
-Each constant exists in 16 versions cycled one per nonlinear evaluation, so that the rounding of a fixed
+Each constant exists in V = 64 versions cycled one per nonlinear evaluation, so that the rounding of a fixed
 operator does not repeat every step.  Properties:
 * every version is one of the two floats that bracket x;
-* the mean of the 16 versions is x to 1/32 of the float spacing, with no bias over many constants;
+* the mean of the V versions is x to 1/(2V) of the float spacing, with no bias over many constants;
 * constants that are floats (powers of two among them) are exact in every version;
-* version 0 is round-to-nearest except within 1/32 of a spacing of the midpoint.
+* version 0 is round-to-nearest except within 1/(2V) of a spacing of the midpoint.
 """
 
 import ctypes as C
 
 import numpy as np
 import pytest
+
+V = 64
 
 
 @pytest.fixture(scope="module")
@@ -20,7 +22,7 @@ def versions():
     from channelflow_gb300 import build
     build.build()
     lib = L.load()
-    buf = (C.c_float * 16)()
+    buf = (C.c_float * V)()
 
     def get(x):
         L.check(lib.cfgpu_dither_versions(float(x), buf))
@@ -45,7 +47,7 @@ def test_versions_bracket_and_average(versions):
         assert np.all((v == lo) | (v == lo + sp)), x
         errs.append((v.mean() - x) / sp)
     errs = np.array(errs)
-    assert np.abs(errs).max() <= 1.0 / 32 + 1e-12
+    assert np.abs(errs).max() <= 1.0 / (2 * V) + 1e-12
     assert abs(errs.mean()) <= 0.002           # unbiased over many constants
 
 
