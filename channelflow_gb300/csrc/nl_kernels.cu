@@ -103,7 +103,7 @@ __device__ __forceinline__ void two_sum_acc(R& s, R t, R& c) {
   s = s1;
 }
 
-template <typename TI, typename R, typename TO, bool CS>
+template <typename TI, typename R, typename TO, bool CS, int PT>
 __global__ void __launch_bounds__(256, CS ? 3 : 1) k_cheb(int N, int inverse, int nlines, const TI* __restrict__ in, size_t ld_in,
                                               size_t cs_in, TO* __restrict__ out, size_t ld_out, size_t cs_out,
                                               const R* __restrict__ Amat, const R* __restrict__ Bmat, int P, int KA,
@@ -129,15 +129,20 @@ __global__ void __launch_bounds__(256, CS ? 3 : 1) k_cheb(int N, int inverse, in
   in += c * cs_in;
   out += c * cs_out;
   const int J = (N - 1) / 2;
+  {
+    const float invA = 1.0f / KAp, invB = 1.0f / KBp;
 #pragma unroll 8
-  for (int i = tid; i < P * KAp; i += blockDim.x) {
-    const int p = i / KAp, k = i - p * KAp;
-    As[i] = k < KA ? Amat[p * KA + k] : (R)0;
-  }
+    for (int i = tid; i < P * KAp; i += blockDim.x) {
+      int p, k;
+      divmod_small(i, KAp, invA, p, k);
+      As[i] = k < KA ? Amat[p * KA + k] : (R)0;
+    }
 #pragma unroll 8
-  for (int i = tid; i < P * KBp; i += blockDim.x) {
-    const int p = i / KBp, k = i - p * KBp;
-    Bs[i] = k < KB ? Bmat[p * KB + k] : (R)0;
+    for (int i = tid; i < P * KBp; i += blockDim.x) {
+      int p, k;
+      divmod_small(i, KBp, invB, p, k);
+      Bs[i] = k < KB ? Bmat[p * KB + k] : (R)0;
+    }
   }
   for (int i = tid; i < (KAp - KA) * CHEB_TL; i += blockDim.x) xa[KA * CHEB_TL + i] = (R)0;
   for (int i = tid; i < (KBp - KB) * CHEB_TL; i += blockDim.x) xb[KB * CHEB_TL + i] = (R)0;
@@ -163,11 +168,9 @@ __global__ void __launch_bounds__(256, CS ? 3 : 1) k_cheb(int N, int inverse, in
   }
   __syncthreads();
   const int lane = tid & 31, warp = tid >> 5;
-  R accA[CHEB_PT][2], accB[CHEB_PT][2];
-  R cmpA[CHEB_PT][2], cmpB[CHEB_PT][2];  // compensation terms (CS)
+  R accA[PT][2], cmpA[PT][2];  // even sums and their compensation terms (CS)
 #pragma unroll
-  for (int i = 0; i < CHEB_PT; ++i)
-    accA[i][0] = accA[i][1] = accB[i][0] = accB[i][1] = cmpA[i][0] = cmpA[i][1] = cmpB[i][0] = cmpB[i][1] = (R)0;
+  for (int i = 0; i < PT; ++i) accA[i][0] = accA[i][1] = cmpA[i][0] = cmpA[i][1] = (R)0;
   // high n first (the small terms are summed before the large), VW columns per matrix load; the compensated
   // form adds groups of CG matrix loads (2 VW terms) to the running sum
   constexpr int CG = CS ? 2 : 1;
@@ -182,7 +185,7 @@ __global__ void __launch_bounds__(256, CS ? 3 : 1) k_cheb(int N, int inverse, in
         x1[gq][e] = k >= 0 ? xa[k * CHEB_TL + lane + 32] : (R)0;
       }
 #pragma unroll
-    for (int i = 0; i < CHEB_PT; ++i) {
+    for (int i = 0; i < PT; ++i) {
       const int p = warp + CHEB_WARPS * i;
       if (p < P) {
         if (CS) {
@@ -212,6 +215,22 @@ __global__ void __launch_bounds__(256, CS ? 3 : 1) k_cheb(int N, int inverse, in
       }
     }
   }
+  if constexpr (CS) {
+    // forward: the even coefficients are complete; store them before the odd sums
+#pragma unroll
+    for (int i = 0; i < PT; ++i) {
+      const int p = warp + CHEB_WARPS * i;
+      if (p >= P) continue;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int gl = l0 + lane + 32 * h;
+        if (gl < nlines) out[(2 * p) * ld_out + gl] = (TO)(accA[i][h] + cmpA[i][h]);
+      }
+    }
+  }
+  R accB[PT][2], cmpB[PT][2];  // odd sums
+#pragma unroll
+  for (int i = 0; i < PT; ++i) accB[i][0] = accB[i][1] = cmpB[i][0] = cmpB[i][1] = (R)0;
   for (int kb = KBp / VW - 1; kb >= 0; kb -= CG) {
     R x0[CG][VW], x1[CG][VW];
 #pragma unroll
@@ -223,7 +242,7 @@ __global__ void __launch_bounds__(256, CS ? 3 : 1) k_cheb(int N, int inverse, in
         x1[gq][e] = k >= 0 ? xb[k * CHEB_TL + lane + 32] : (R)0;
       }
 #pragma unroll
-    for (int i = 0; i < CHEB_PT; ++i) {
+    for (int i = 0; i < PT; ++i) {
       const int p = warp + CHEB_WARPS * i;
       if (p < P) {
         if (CS) {
@@ -254,7 +273,7 @@ __global__ void __launch_bounds__(256, CS ? 3 : 1) k_cheb(int N, int inverse, in
     }
   }
 #pragma unroll
-  for (int i = 0; i < CHEB_PT; ++i) {
+  for (int i = 0; i < PT; ++i) {
     const int p = warp + CHEB_WARPS * i;
     if (p >= P) continue;
 #pragma unroll
@@ -266,8 +285,8 @@ __global__ void __launch_bounds__(256, CS ? 3 : 1) k_cheb(int N, int inverse, in
         out[p * ld_out + gl] = (TO)(accA[i][h] + accB[i][h]);
         if (p < J) out[(N - 1 - p) * ld_out + gl] = (TO)(accA[i][h] - accB[i][h]);
       } else {
-        // p = k: even coefficient 2k, odd coefficient 2k+1
-        out[(2 * p) * ld_out + gl] = (TO)(CS ? accA[i][h] + cmpA[i][h] : accA[i][h]);
+        // p = k: even coefficient 2k (stored above by the compensated form), odd coefficient 2k+1
+        if (!CS) out[(2 * p) * ld_out + gl] = (TO)accA[i][h];
         if (2 * p + 1 < N) out[(2 * p + 1) * ld_out + gl] = (TO)(CS ? accB[i][h] + cmpB[i][h] : accB[i][h]);
       }
     }
@@ -680,41 +699,55 @@ size_t cheb_smem_bytes(int N, size_t rsize) {
   return rsize * ((size_t)(KAp + KBp) * CHEB_TL + (size_t)P * (KAp + KBp));
 }
 
+// One launch of k_cheb with PT output rows per warp.
+template <typename TI, typename R, typename TO, bool CS, int PT>
+cudaError_t launch_cheb_pt(dim3 grid, size_t sm, cudaStream_t st, int N, int inverse, int nlines, const TI* in,
+                           size_t ld_in, size_t cs_in, TO* out, size_t ld_out, size_t cs_out, const R* A, const R* B,
+                           int P, int KA, int KB, const Dither& dt, int lpf) {
+  // kernel attributes set once per process and instantiation (thread-safe static initialisation)
+  static const bool attr_set = [] {
+    cudaFuncSetAttribute(k_cheb<TI, R, TO, CS, PT>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    return true;
+  }();
+  (void)attr_set;
+  k_cheb<TI, R, TO, CS, PT><<<grid, 32 * CHEB_WARPS, sm, st>>>(N, inverse, nlines, in, ld_in, cs_in, out, ld_out,
+                                                               cs_out, A, B, P, KA, KB, dt, lpf);
+  return cudaGetLastError();
+}
+
+template <typename TI, typename R, typename TO, bool CS>
+cudaError_t launch_cheb_cs(dim3 grid, size_t sm, cudaStream_t st, int N, int inverse, int nlines, const TI* in,
+                           size_t ld_in, size_t cs_in, TO* out, size_t ld_out, size_t cs_out, const R* A, const R* B,
+                           int P, int KA, int KB, const Dither& dt, int lpf) {
+  // the fewest rows per warp that cover P (registers: two sums per row and line)
+  const int pt = (P + CHEB_WARPS - 1) / CHEB_WARPS;
+  if (pt <= 4)
+    return launch_cheb_pt<TI, R, TO, CS, 4>(grid, sm, st, N, inverse, nlines, in, ld_in, cs_in, out, ld_out, cs_out,
+                                            A, B, P, KA, KB, dt, lpf);
+  if (pt <= 7)
+    return launch_cheb_pt<TI, R, TO, CS, 7>(grid, sm, st, N, inverse, nlines, in, ld_in, cs_in, out, ld_out, cs_out,
+                                            A, B, P, KA, KB, dt, lpf);
+  return launch_cheb_pt<TI, R, TO, CS, CHEB_PT>(grid, sm, st, N, inverse, nlines, in, ld_in, cs_in, out, ld_out,
+                                                cs_out, A, B, P, KA, KB, dt, lpf);
+}
+
 template <typename TI, typename R, typename TO>
 cudaError_t launch_cheb(int N, bool inverse, int nlines, int ncomp, const TI* in, size_t ld_in, size_t cs_in, TO* out,
                         size_t ld_out, size_t cs_out, const R* A, const R* B, cudaStream_t st, const Dither& dt) {
   if ((N + 1) / 2 > CHEB_WARPS * CHEB_PT) return cudaErrorInvalidValue;
   const int P = (N + 1) / 2;
-  int KA, KB;
-  if (inverse) {
-    KA = (N + 1) / 2;
-    KB = (N - 1) / 2;
-  } else {
-    KA = (N + 1) / 2;
-    KB = (N - 1) / 2;
-  }
+  const int KA = (N + 1) / 2, KB = (N - 1) / 2;
   const size_t sm = cheb_smem_bytes(N, sizeof(R));
-  // kernel attributes set once per process (thread-safe static initialisation)
-  static const bool attr_set = [] {
-    cudaFuncSetAttribute(k_cheb<TI, R, TO, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    if constexpr (sizeof(R) == 4)
-      cudaFuncSetAttribute(k_cheb<TI, R, TO, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    return true;
-  }();
-  (void)attr_set;
   const int nf = dt.nb > 0 ? dt.nb : 1, lpf = (nlines + nf - 1) / nf;
   dim3 grid(nf * ((lpf + CHEB_TL - 1) / CHEB_TL), ncomp);
   // compensated sums for the FP32 forward transforms
   if constexpr (sizeof(R) == 4) {
-    if (!inverse) {
-      k_cheb<TI, R, TO, true><<<grid, 32 * CHEB_WARPS, sm, st>>>(N, 0, nlines, in, ld_in, cs_in, out, ld_out, cs_out,
-                                                                 A, B, P, KA, KB, dt, lpf);
-      return cudaGetLastError();
-    }
+    if (!inverse)
+      return launch_cheb_cs<TI, R, TO, true>(grid, sm, st, N, 0, nlines, in, ld_in, cs_in, out, ld_out, cs_out, A, B,
+                                             P, KA, KB, dt, lpf);
   }
-  k_cheb<TI, R, TO, false><<<grid, 32 * CHEB_WARPS, sm, st>>>(N, inverse ? 1 : 0, nlines, in, ld_in, cs_in, out,
-                                                              ld_out, cs_out, A, B, P, KA, KB, dt, lpf);
-  return cudaGetLastError();
+  return launch_cheb_cs<TI, R, TO, false>(grid, sm, st, N, inverse ? 1 : 0, nlines, in, ld_in, cs_in, out, ld_out,
+                                          cs_out, A, B, P, KA, KB, dt, lpf);
 }
 
 // Columns per block of the x passes: all NKz when they fit in shared memory.
