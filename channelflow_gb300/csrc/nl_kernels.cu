@@ -342,16 +342,21 @@ __global__ void __launch_bounds__(256) k_curl_cheb(GridDev g, int N, const doubl
   CB = dither_ptr(CB, ver, dt.S);
   DA = dither_ptr(DA, ver, dt.S);
   DB = dither_ptr(DB, ver, dt.S);
+  const float invKA = 1.0f / KAp, invKB = 1.0f / KBp;
 #pragma unroll 8
   for (int i = tid; i < PL * KAp; i += blockDim.x) {
-    const int r = i / KAp, k = i - r * KAp, pp = 8 * (2 * (r >> 3) + half) + (r & 7);
+    int r, k;
+    divmod_small(i, KAp, invKA, r, k);
+    const int pp = 8 * (2 * (r >> 3) + half) + (r & 7);
     const bool in = k < KA && pp < P;
     sCA[i] = in ? CA[pp * KA + k] : (R)0;
     sDA[i] = in ? DA[pp * KA + k] : (R)0;
   }
 #pragma unroll 8
   for (int i = tid; i < PL * KBp; i += blockDim.x) {
-    const int r = i / KBp, k = i - r * KBp, pp = 8 * (2 * (r >> 3) + half) + (r & 7);
+    int r, k;
+    divmod_small(i, KBp, invKB, r, k);
+    const int pp = 8 * (2 * (r >> 3) + half) + (r & 7);
     const bool in = k < KB && pp < P;
     sCB[i] = in ? CB[pp * KB + k] : (R)0;
     sDB[i] = in ? DB[pp * KB + k] : (R)0;
@@ -361,13 +366,19 @@ __global__ void __launch_bounds__(256) k_curl_cheb(GridDev g, int N, const doubl
     const int r = e < KAp - KA ? KA + e : KAp + KB + (e - (KAp - KA));
     xs[(c * NP + r) * CC_TL + l] = (R)0;
   }
+  {
+    // lane l stages line l0 + l; warp w takes the coefficients n = w, w + 8, ... of each component
+    const int gl = l0 + lane;
+    const bool ok = gl < nlines;
+    for (int c = 0; c < 3; ++c) {
+      const double* uc = U + c * comp + gl;
 #pragma unroll 4
-  for (int i = tid; i < 3 * N * CC_TL; i += blockDim.x) {
-    const int l = i % CC_TL, n = (i / CC_TL) % N, c = i / (CC_TL * N);
-    const int gl = l0 + l;
-    const R v = gl < nlines ? (R)U[c * comp + (size_t)n * row + gl] : (R)0;
-    const int r = (n & 1) ? KAp + (n >> 1) : (n >> 1);
-    xs[(c * NP + r) * CC_TL + l] = v;
+      for (int n = warp; n < N; n += 8) {
+        const R v = ok ? (R)uc[(size_t)n * row] : (R)0;
+        const int r = (n & 1) ? KAp + (n >> 1) : (n >> 1);
+        xs[(c * NP + r) * CC_TL + lane] = v;
+      }
+    }
   }
   __syncthreads();
   R aCu[CC_PT], aCv[CC_PT], aCw[CC_PT], aDu[CC_PT], aDw[CC_PT];   // even-coefficient sums
