@@ -110,6 +110,13 @@ CASES = [
     ("poiseuille_48_cnab2", (48, 49, 48, *POISEUILLE_BOX),
      dict(nu=1 / 4000, dt=0.01, timestepping=O.CNAB2, initstepping=O.SMRK2, baseflow=O.LaminarBase,
           constraint=O.BulkVelocity, Ubulk=2.0 / 3.0), 5),
+    # tall grids: the Chebyshev kernels' row tilings for Ny = 97 (the bench workload's Ny) and Ny = 129
+    ("poiseuille_tall97_cnab2", (12, 97, 12, *POISEUILLE_BOX),
+     dict(nu=1 / 4000, dt=0.01, timestepping=O.CNAB2, initstepping=O.SMRK2, baseflow=O.LaminarBase,
+          constraint=O.BulkVelocity, Ubulk=2.0 / 3.0), 6),
+    ("couette_tall129_sbdf3", (12, 129, 12, *COUETTE_BOX),
+     dict(nu=1 / 400, dt=0.01, timestepping=O.SBDF3, initstepping=O.SMRK2, baseflow=O.LaminarBase,
+          ulowerwall=-1.0, uupperwall=1.0), 6),
 ]
 
 
@@ -155,6 +162,19 @@ def test_dns_mixed_matches_oracle():
     u0 = O.random_divfree_field(g, seed=5, norm=0.1)
     ou, _, _ = oracle_run(u0, g, fl, 50)
     gu, _, _ = gpu_run(u0, g, fl, 50, precision="mixed")
+    ou[:, :, ~solved_mask(g)] = 0
+    assert rel_l2(gu, ou, g) <= MIXED_TOL
+
+
+@pytest.mark.parametrize("ny", [97, 129])
+def test_dns_mixed_tall_grids(ny):
+    """Mixed path with the compensated forward Chebyshev sums at Ny = 97 and 129 (7 and 9 rows per warp)."""
+    g = O.Grid(12, ny, 12, *COUETTE_BOX)
+    fl = O.DNSFlags(nu=1 / 400, dt=0.01, timestepping=O.SBDF3, initstepping=O.SMRK2, baseflow=O.LaminarBase,
+                    ulowerwall=-1.0, uupperwall=1.0)
+    u0 = O.random_divfree_field(g, seed=ny, norm=0.1)
+    ou, _, _ = oracle_run(u0, g, fl, 20)
+    gu, _, _ = gpu_run(u0, g, fl, 20, precision="mixed")
     ou[:, :, ~solved_mask(g)] = 0
     assert rel_l2(gu, ou, g) <= MIXED_TOL
 
