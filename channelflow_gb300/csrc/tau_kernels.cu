@@ -1056,8 +1056,8 @@ __device__ void helm_t(int M, int q, const double* __restrict__ hlo, const doubl
 // Right-hand side of the step solve (NSE::linear and the scheme's combination,
 // nse.cpp:393-477, dnsalgo.cpp:202-253, 641-697, 419-470) for the table-staged
 // solve: one group of four lanes (re/im part, Chebyshev parity) per (mode,
-// component), three times the lanes of the solve, writing Rx, Ry, Rz to the
-// scratch lines 0, 2 and 1 (the solve reads them back).
+// component), one component per grid row (blockIdx.y), writing Rx, Ry, Rz to
+// the scratch lines 0, 2 and 1 (the solve reads them back).
 // ---------------------------------------------------------------------------
 template <typename R>
 __global__ void __launch_bounds__(32) k_tau_rhs(GridDev g, int N, SolveParams sp, SolvePtrs P) {
@@ -1065,10 +1065,11 @@ __global__ void __launch_bounds__(32) k_tau_rhs(GridDev g, int N, SolveParams sp
   const int lane = threadIdx.x;
   const int t = blockIdx.x * 32 + lane;
   const int Md = g.Md;
+  // one component per grid row: the eight lane groups of a warp read eight consecutive modes of one plane
   const int grp = t >> 2;
-  const bool act = grp < 3 * Md;
-  const int m = act ? grp / 3 : Md - 1;
-  const int cc = act ? grp % 3 : 0;
+  const bool act = grp < Md;
+  const int m = act ? grp : Md - 1;
+  const int cc = blockIdx.y;
   const int part = (t >> 1) & 1, q = t & 1;
   const unsigned gmask = 0xFu << (lane & 28);
   const int row = 2 * Md;
@@ -1579,7 +1580,7 @@ cudaError_t launch_tau_solve(const GridDev& g, int N, const SolveParams& sp, con
     }();
     (void)attr;
     const size_t smem_r = sizeof(double) * (((N + 1) & ~1) + (size_t)M0 * 32);
-    k_tau_rhs<R><<<(12 * g.Md + 31) / 32, 32, smem_r, st>>>(g, N, sp, p);
+    k_tau_rhs<R><<<dim3((4 * g.Md + 31) / 32, 3), 32, smem_r, st>>>(g, N, sp, p);
     k_tau_solve_t<R><<<(4 * g.Md + 31) / 32, 32, smem_t, st>>>(g, N, sp, p, hb, tt);
     const size_t smem_u = sizeof(double) * ((size_t)M0 * 32 + (size_t)4 * N * 4);
     k_tau_uw<R><<<(8 * g.Md + 31) / 32, 32, smem_u, st>>>(g, N, sp, p, hb, tt);
