@@ -95,6 +95,8 @@ __global__ void k_curl_base(GridDev g, const double* __restrict__ U, R* __restri
 #define CHEB_WARPS 8
 #define CHEB_PT 9
 
+// s + t = s1 + err exactly (Knuth's two-sum; needs IEEE rounding of each operation, so the library is built
+// without fast-math); err is added to the running compensation c.
 template <typename R>
 __device__ __forceinline__ void two_sum_acc(R& s, R t, R& c) {
   const R s1 = s + t;
