@@ -168,25 +168,9 @@ def run_gpu(args, rank, world):
     from channelflow_gb300.fields import l2norm
 
     b.build()
-    dist = None
-    if world > 1:
-        import torch
-        import torch.distributed as dist_
-        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", rank)))
-        dist_.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-        dist = dist_
-
-    def barrier():
-        if dist:
-            dist.barrier()
-
-    def max_over_ranks(x):
-        if not dist:
-            return x
-        import torch
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    from channelflow_gb300.replicas import Replicas
+    reps = Replicas(rank, world)  # independent DNS per rank; barriers and the slowest rank's time only
+    barrier, max_over_ranks = reps.barrier, reps.max_over_ranks
 
     grid = Grid(NX, NY, NZ, LX, LZ)
     u0 = initial_field(seed=1 + rank)
