@@ -18,6 +18,13 @@
 
 #include "kernels.h"
 
+// Asynchronous 8-byte global -> shared copy (cp.async, no register staging); nbytes = 0 writes zeros.
+__device__ __forceinline__ void cp_async8(double* dst_smem, const double* src, int nbytes) {
+  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst_smem));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src), "r"(nbytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 struct Ln {
   double* p;
   size_t s;
@@ -1299,25 +1306,23 @@ __global__ void __launch_bounds__(32) k_tau_solve_t(GridDev g, int N, SolveParam
   auto TS = [&](int k) { return TLn{tab + ((size_t)k * N + q) * 8 + mi}; };
   // stage factor fields f0..f3 of this warp's 8 modes into tab
   // (lane l copies mode mbase + l % 8 of rows n = l / 8 + 4 j: entry [k][n][l % 8] = tab[k N 8 + l + 32 j])
+  // All copies of a staging are issued asynchronously (cp.async, zero fill past the last mode) and waited
+  // for together: one memory latency per staging instead of one per batch of loads.
   auto stage = [&](int f0, int nf) {
     __syncwarp();
     const bool mok = mbase + (lane & 7) < Md;
-#pragma unroll 1
+    const int nb = mok ? 8 : 0;
     for (int k = 0; k < nf; ++k) {
-      const double* src = tt.f + (size_t)(f0 + k) * FN + mbase + (lane & 7) + (size_t)(lane >> 3) * Md;
+      const double* src = mok ? tt.f + (size_t)(f0 + k) * FN + mbase + (lane & 7) + (size_t)(lane >> 3) * Md : tt.f;
+      const size_t step = mok ? (size_t)4 * Md : 0;
       double* dst = tab + (size_t)k * N * 8 + lane;
-      for (int n0 = lane >> 3; n0 < N; n0 += 4 * 16) {
-        double v[16];
-#pragma unroll
-        for (int k2 = 0; k2 < 16; ++k2)
-          v[k2] = (mok && n0 + 4 * k2 < N) ? __ldg(src + (size_t)(4 * k2) * Md) : 0.0;
-#pragma unroll
-        for (int k2 = 0; k2 < 16; ++k2)
-          if (n0 + 4 * k2 < N) dst[32 * k2] = v[k2];
-        src += (size_t)64 * Md;
-        dst += 32 * 16;
+      for (int n = lane >> 3; n < N; n += 4) {
+        cp_async8(dst, src, nb);
+        src += step;
+        dst += 32;
       }
     }
+    cp_async_wait_all();
     __syncwarp();
   };
   double* Rxg = P.scratch;          // global scratch lines for Rx and Rz
