@@ -48,8 +48,8 @@ WORKLOAD = ("plane Poiseuille 128x97x128 (Lx=4pi, Lz=2pi), CNAB2 + SMRK2 start-u
 CNAB2, SMRK2, LaminarBase, BulkVelocity = 1, 3, 3, 1
 # DRAM bytes (read + write) per step of the mixed-path phases from `ncu --set full` captures of this workload
 # (profiles/ncu_step_poiseuille_128x97x128_mixed.md: the eight kernels of one step, tau and NL pass).
-NCU_TRAFFIC = {"tau_solve": (37.94 + 0.79 + 54.38 + 0.52 + 27.11 + 0.01) * 1e6,
-               "nonlinear_pass": (16.32 + 0.0 + 17.53 + 1.23 + 25.13 + 0.0 + 12.60 + 0.0 + 8.18 + 0.0) * 1e6}
+NCU_TRAFFIC = {"tau_solve": (37.94 + 0.68 + 54.39 + 0.55 + 27.11 + 0.02) * 1e6,
+               "nonlinear_pass": (16.32 + 0.0 + 16.73 + 0.42 + 25.13 + 0.0 + 12.60 + 0.0 + 8.18 + 0.0) * 1e6}
 
 
 def peaks():
