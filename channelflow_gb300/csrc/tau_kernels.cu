@@ -1302,7 +1302,6 @@ __global__ void __launch_bounds__(32) k_tau_solve_t(GridDev g, int N, SolveParam
   auto G = [&](const double* base) { return PLn{const_cast<double*>(base) + off + q * row, 2 * row}; };
   auto Go = [&](const double* base) { return PLn{const_cast<double*>(base) + off + (1 - q) * row, 2 * row}; };
   auto Gp = [&](const double* base) { return PLn{const_cast<double*>(base) + poff + q * row, 2 * row}; };
-  auto TB = [&](int f) { return PLn{tt.f + f * FN + m + q * Md, 2 * Md}; };
   auto TS = [&](int k) { return TLn{tab + ((size_t)k * N + q) * 8 + mi}; };
   // stage factor fields f0..f3 of this warp's 8 modes into tab
   // (lane l copies mode mbase + l % 8 of rows n = l / 8 + 4 j: entry [k][n][l % 8] = tab[k N 8 + l + 32 j])
@@ -1403,7 +1402,9 @@ __global__ void __launch_bounds__(32) k_tau_solve_t(GridDev g, int N, SolveParam
     const double i00 = sc[TS_I00 * Md], i01 = sc[TS_I01 * Md], i10 = sc[TS_I10 * Md], i11 = sc[TS_I11 * Md];
     const double dp = -i00 * plus - i01 * minus;
     const double dm = -i10 * plus - i11 * minus;
-    PLn Pp = TB(TF_PP), Vp = TB(TF_VP), Pm = TB(TF_PM), Vm = TB(TF_VM);
+    // influence solutions P+-, V+- staged like the factors (the V factors are no longer needed)
+    stage(TF_PP, 4);
+    const TLn Pp = TS(0), Vp = TS(1), Pm = TS(2), Vm = TS(3);
     if (!m00)
       for (int i = 0; i < M; i += TCH) {
         double a[TCH], b[TCH], c2[TCH], d[TCH];
@@ -1430,12 +1431,13 @@ __global__ void __launch_bounds__(32) k_tau_solve_t(GridDev g, int N, SolveParam
     }
     const double ox = __shfl_xor_sync(gmask, x0, 1);
     const double oy = __shfl_xor_sync(gmask, y0, 1);
+    if (sp.taucorrection) stage(TF_P0, 2);  // tau-correction solutions P0, V0
     if (!m00 && sp.taucorrection) {
       const double s1Nb = (q == 0 ? x0 : ox) + 0.0;
       const double s1Nb1 = q == 0 ? ox + y0 : x0 + oy;
       const double sNb = s1Nb / (1.0 - sc[TS_S0NB * Md]);
       const double sNb1 = s1Nb1 / (1.0 - sc[TS_S0NB1 * Md]);
-      PLn P0 = TB(TF_P0), V0 = TB(TF_V0);
+      const TLn P0 = TS(0), V0 = TS(1);
       const double fP = q == 0 ? sNb1 : sNb, fV = q == 0 ? sNb : sNb1;
       for (int i = 0; i < M; i += TCH) {
         double a[TCH], b[TCH];
@@ -1497,24 +1499,22 @@ __global__ void __launch_bounds__(32) k_tau_uw(GridDev g, int N, SolveParams sp,
   const int M = q ? (N - 1) / 2 : M0;
   double* tab = sm + (size_t)M0 * 32;  // [4][N][4]
   {
-    // lane l copies mode mbase + l % 4 of rows n = l / 4 + 8 j: entry [k][n][l % 4] = tab[k N 4 + l + 32 j]
+    // lane l copies mode mbase + l % 4 of rows n = l / 4 + 8 j: entry [k][n][l % 4] = tab[k N 4 + l + 32 j];
+    // all copies asynchronous (cp.async, zero fill past the last mode), waited for together
     const bool mok = mbase + (lane & 3) < Md;
-#pragma unroll 1
+    const int nb = mok ? 8 : 0;
     for (int k = 0; k < 4; ++k) {
-      const double* src = tt.f + (size_t)(TF_VBAND + k) * FN + mbase + (lane & 3) + (size_t)(lane >> 2) * Md;
+      const double* src =
+          mok ? tt.f + (size_t)(TF_VBAND + k) * FN + mbase + (lane & 3) + (size_t)(lane >> 2) * Md : tt.f;
+      const size_t step = mok ? (size_t)8 * Md : 0;
       double* dst = tab + (size_t)k * N * 4 + lane;
-      for (int n0 = lane >> 2; n0 < N; n0 += 8 * 16) {
-        double v[16];
-#pragma unroll
-        for (int k2 = 0; k2 < 16; ++k2)
-          v[k2] = (mok && n0 + 8 * k2 < N) ? __ldg(src + (size_t)(8 * k2) * Md) : 0.0;
-#pragma unroll
-        for (int k2 = 0; k2 < 16; ++k2)
-          if (n0 + 8 * k2 < N) dst[32 * k2] = v[k2];
-        src += (size_t)128 * Md;
-        dst += 32 * 16;
+      for (int n = lane >> 2; n < N; n += 8) {
+        cp_async8(dst, src, nb);
+        src += step;
+        dst += 32;
       }
     }
+    cp_async_wait_all();
   }
   __syncwarp();
   auto TS = [&](int k) { return TLn4{tab + ((size_t)k * N + q) * 4 + mi}; };
