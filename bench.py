@@ -47,7 +47,7 @@ WORKLOAD = ("plane Poiseuille 128x97x128 (Lx=4pi, Lz=2pi), CNAB2 + SMRK2 start-u
             "Ubulk=2/3, Re_c=4000, rotational NL, 2/3 dealiasing, seeded perturbation L2=0.3")
 CNAB2, SMRK2, LaminarBase, BulkVelocity = 1, 3, 3, 1
 # DRAM bytes (read + write) per step of the mixed-path phases from `ncu --set full` captures of this workload
-# (profiles/ncu_step_poiseuille_128x97x128_mixed.md: the eight kernels of one step, tau and NL pass).
+# (the eight kernels of one step: tau solve and nonlinear pass).
 NCU_TRAFFIC = {"tau_solve": (37.94 + 0.68 + 54.39 + 0.55 + 27.11 + 0.02) * 1e6,
                "nonlinear_pass": (16.32 + 0.0 + 16.73 + 0.42 + 25.13 + 0.0 + 12.60 + 0.0 + 8.18 + 0.0) * 1e6}
 
@@ -60,10 +60,31 @@ def peaks():
     return 6800.0, "fallback"
 
 
-class ClockSampler:
-    """nvidia-smi clocks/throttle sampling during the timed region."""
+def current_gpu_bus_id():
+    """PCI bus id of the CUDA device this process computes on (the runtime's current device).
 
-    def __init__(self, index=0):
+    nvidia-smi numbers GPUs physically and ignores CUDA_VISIBLE_DEVICES, so the clock sampler names the GPU
+    by bus id; None when the runtime cannot say (the sampler then records nothing)."""
+    import ctypes
+    for name in ("libcudart.so.13", "libcudart.so.12", "libcudart.so"):
+        try:
+            rt = ctypes.CDLL(name)
+            break
+        except OSError:
+            rt = None
+    if rt is None:
+        return None
+    dev = ctypes.c_int(0)
+    buf = ctypes.create_string_buffer(64)
+    if rt.cudaGetDevice(ctypes.byref(dev)) != 0 or rt.cudaDeviceGetPCIBusId(buf, 64, dev) != 0:
+        return None
+    return buf.value.decode() or None
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region, for the GPU with the given PCI bus id."""
+
+    def __init__(self, index=None):
         self.index = index
         self.proc = None
         self.path = None
@@ -74,6 +95,8 @@ class ClockSampler:
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        if self.index is None:
+            return self
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
                                           "--format=csv,noheader,nounits", "-lms", "100"],
@@ -187,7 +210,7 @@ def run_gpu(args, rank, world):
         dns.phase_times()
         l0 = dns.kernel_launches()
         barrier()
-        with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as cs:
+        with ClockSampler(current_gpu_bus_id()) as cs:
             ms = dns.advance_timed(K)
         ms = max_over_ranks(ms)
         launches = dns.kernel_launches() - l0

@@ -63,16 +63,11 @@ cudaError_t launch_rotation(const GridDev& g, int N, const double* U, const doub
 
 template <typename R>
 size_t xfft_smem_bytes(const GridDev& g, int czc = 0);  // czc <= 0: all solved kz columns that fit
-template <typename R>
-size_t zcross_smem_bytes(const GridDev& g, int RP);
 
 // x passes: czc kz columns per block (0: as many as fit in shared memory)
 template <typename R>
 cudaError_t launch_xinv(const GridDev& g, const FftPlan& px, const cpx<R>* twx, const cpx<R>* W, cpx<R>* X, int ncomp,
                         cudaStream_t st, int czc = 0, const Dither& dt = kNoDither);
-template <typename R>
-cudaError_t launch_zcross(const GridDev& g, const FftPlan& pz, const cpx<R>* twz, int RP, const cpx<R>* X, cpx<R>* Z,
-                          cudaStream_t st, const Dither& dt = kNoDither);
 template <typename R>
 cudaError_t launch_xfwd(const GridDev& g, const FftPlan& px, const cpx<R>* twx, const cpx<R>* Z, cpx<R>* F, int ncomp,
                         cudaStream_t st, int czc = 0, const Dither& dt = kNoDither);

@@ -568,94 +568,6 @@ __global__ void __launch_bounds__(256) k_xinv(GridDev g, FftPlan px, const cpx<R
 }
 
 // ---------------------------------------------------------------------------
-// z-direction pass for RP x-rows of one y-plane: c2r inverse FFT of the six
-// fields (u, v, w, ox, oy, oz; two real rows packed per complex FFT), the
-// physical-space cross product f = omega x u, and the r2c forward FFT of f
-// (again two real rows per complex FFT), keeping kz in [0, Kz].
-// ---------------------------------------------------------------------------
-template <typename R>
-__global__ void __launch_bounds__(256) k_zcross(GridDev g, FftPlan pz, const cpx<R>* __restrict__ twz, int RP,
-                                                const cpx<R>* __restrict__ X, cpx<R>* __restrict__ Z, Dither dt) {
-  extern __shared__ unsigned char smem_raw[];
-  twz = dither_ptr(twz, dither_ver(dt, blockIdx.y % dt.nb), dt.S);  // plane blockIdx.y -> its field's twiddles
-  const int Nz = g.Nz, ss = Nz + 1, NKz = g.NKz;
-  const int ninv = 3 * RP;  // inverse sequences
-  cpx<R>* A = reinterpret_cast<cpx<R>*>(smem_raw);
-  cpx<R>* B = A + (size_t)ninv * ss;
-  const int ny = blockIdx.y;
-  const int x0 = blockIdx.x * RP;
-  const int tid = threadIdx.x, nthr = blockDim.x;
-  const size_t plane = (size_t)g.Nx * NKz;
-  for (int i = tid; i < ninv * ss; i += nthr) A[i] = cmk<R>(0, 0);
-  __syncthreads();
-  // pack: sequence (r, p) = comps (2p, 2p+1) of row x0+r
-#pragma unroll 4
-  for (int i = tid; i < RP * 3 * NKz; i += nthr) {
-    const int iz = i % NKz;
-    const int rp = i / NKz;
-    const int p = rp % 3, r = rp / 3;
-    const int x = x0 + r;
-    if (x >= g.Nx) continue;
-    const size_t o = ((size_t)(2 * p) * g.Ny + ny) * plane + (size_t)x * NKz + iz;
-    cpx<R> ca = X[o];
-    cpx<R> cb = X[o + (size_t)g.Ny * plane];
-    cpx<R>* s = A + (size_t)(r * 3 + p) * ss;
-    if (iz == 0) {
-      s[0] = cmk<R>(ca.x, cb.x);
-    } else {
-      s[iz] = cmk<R>(ca.x - cb.y, ca.y + cb.x);           // A_k + i B_k
-      s[Nz - iz] = cmk<R>(ca.x + cb.y, -ca.y + cb.x);     // conj(A_k) + i conj(B_k)
-    }
-  }
-  __syncthreads();
-  fft_batch<R>(A, B, ninv, ss, pz, twz, +1);
-  // cross product into B: forward sequences per row pair (r0 = 2q, r1 = 2q+1):
-  //   s0 = f0(r0) + i f1(r0), s1 = f2(r0) + i f2(r1), s2 = f0(r1) + i f1(r1)
-  const int npair = RP / 2;
-  for (int i = tid; i < RP * Nz; i += nthr) {
-    const int z = i % Nz, r = i / Nz;
-    const cpx<R> s0 = A[(size_t)(r * 3 + 0) * ss + z];  // u, v
-    const cpx<R> s1 = A[(size_t)(r * 3 + 1) * ss + z];  // w, ox
-    const cpx<R> s2 = A[(size_t)(r * 3 + 2) * ss + z];  // oy, oz
-    const R u = s0.x, v = s0.y, w = s1.x, ox = s1.y, oy = s2.x, oz = s2.y;
-    const R f0 = oy * w - oz * v;
-    const R f1 = oz * u - ox * w;
-    const R f2 = ox * v - oy * u;
-    const int q = r >> 1;
-    cpx<R>* base = B + (size_t)(q * 3) * ss;
-    if ((r & 1) == 0) {
-      base[z] = cmk<R>(f0, f1);
-      base[ss + z].x = f2;
-    } else {
-      base[2 * ss + z] = cmk<R>(f0, f1);
-      base[ss + z].y = f2;
-    }
-  }
-  __syncthreads();
-  fft_batch<R>(B, A, 3 * npair, ss, pz, twz, -1);
-  // unpack P_k = (Z_k + conj(Z_-k))/2, Q_k = (Z_k - conj(Z_-k))/(2i)
-#pragma unroll 4
-  for (int i = tid; i < npair * 3 * NKz; i += nthr) {
-    const int iz = i % NKz;
-    const int t = i / NKz;
-    const int sidx = t % 3, q = t / 3;
-    const cpx<R>* s = B + (size_t)(q * 3 + sidx) * ss;
-    const cpx<R> zk = s[iz];
-    const cpx<R> zm = s[iz == 0 ? 0 : Nz - iz];
-    const cpx<R> Pk = cmk<R>((R)0.5 * (zk.x + zm.x), (R)0.5 * (zk.y - zm.y));
-    const cpx<R> Qk = cmk<R>((R)0.5 * (zk.y + zm.y), (R)0.5 * (zm.x - zk.x));
-    const int r0 = x0 + 2 * q, r1 = r0 + 1;
-    // sidx 0: (f0, f1) of r0; 1: (f2 r0, f2 r1); 2: (f0, f1) of r1
-    int cP, cQ, xP, xQ;
-    if (sidx == 0) { cP = 0; cQ = 1; xP = r0; xQ = r0; }
-    else if (sidx == 1) { cP = 2; cQ = 2; xP = r0; xQ = r1; }
-    else { cP = 0; cQ = 1; xP = r1; xQ = r1; }
-    if (xP < g.Nx) Z[((size_t)cP * g.Ny + ny) * plane + (size_t)xP * NKz + iz] = Pk;
-    if (xQ < g.Nx) Z[((size_t)cQ * g.Ny + ny) * plane + (size_t)xQ * NKz + iz] = Qk;
-  }
-}
-
-// ---------------------------------------------------------------------------
 // x-direction forward FFT of the kz columns of one plane/component, keeping
 // the solved kx and applying the 1/(Nx Nz) scale of makeSpectral_xz.
 // ---------------------------------------------------------------------------
@@ -776,10 +688,6 @@ template <typename R>
 size_t xfft_smem_bytes(const GridDev& g, int czc) {
   return 2 * sizeof(cpx<R>) * (size_t)(czc > 0 ? czc : xfft_cols<R>(g)) * (g.Nx + 1);
 }
-template <typename R>
-size_t zcross_smem_bytes(const GridDev& g, int RP) {
-  return 2 * sizeof(cpx<R>) * (size_t)(3 * RP) * (g.Nz + 1);
-}
 
 template <typename R>
 cudaError_t launch_xinv(const GridDev& g, const FftPlan& px, const cpx<R>* twx, const cpx<R>* W, cpx<R>* X, int ncomp,
@@ -793,19 +701,6 @@ cudaError_t launch_xinv(const GridDev& g, const FftPlan& px, const cpx<R>* twx, 
   if (czc <= 0 || czc > g.NKz) czc = xfft_cols<R>(g);
   k_xinv<R><<<dim3(g.Ny, ncomp, (g.NKz + czc - 1) / czc), 256, xfft_smem_bytes<R>(g, czc), st>>>(g, px, twx, W, X,
                                                                                                czc, dt);
-  return cudaGetLastError();
-}
-
-template <typename R>
-cudaError_t launch_zcross(const GridDev& g, const FftPlan& pz, const cpx<R>* twz, int RP, const cpx<R>* X, cpx<R>* Z,
-                          cudaStream_t st, const Dither& dt) {
-  // kernel attributes set once per process (thread-safe static initialisation)
-  static const bool attr_set = [] {
-    cudaFuncSetAttribute(k_zcross<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    return true;
-  }();
-  (void)attr_set;
-  k_zcross<R><<<dim3((g.Nx + RP - 1) / RP, g.Ny), 256, zcross_smem_bytes<R>(g, RP), st>>>(g, pz, twz, RP, X, Z, dt);
   return cudaGetLastError();
 }
 
@@ -830,12 +725,9 @@ cudaError_t launch_xfwd(const GridDev& g, const FftPlan& px, const cpx<R>* twx, 
                                            cudaStream_t);                                                           \
   template cudaError_t launch_xinv<R>(const GridDev&, const FftPlan&, const cpx<R>*, const cpx<R>*, cpx<R>*, int,   \
                                       cudaStream_t, int, const Dither&);                                            \
-  template cudaError_t launch_zcross<R>(const GridDev&, const FftPlan&, const cpx<R>*, int, const cpx<R>*, cpx<R>*, \
-                                        cudaStream_t, const Dither&);                                               \
   template cudaError_t launch_xfwd<R>(const GridDev&, const FftPlan&, const cpx<R>*, const cpx<R>*, cpx<R>*, int,   \
                                       cudaStream_t, int, const Dither&);                                            \
-  template size_t xfft_smem_bytes<R>(const GridDev&, int);                                                             \
-  template size_t zcross_smem_bytes<R>(const GridDev&, int);
+  template size_t xfft_smem_bytes<R>(const GridDev&, int);
 
 INST_R(float)
 INST_R(double)

@@ -8,14 +8,22 @@
 // break the budget, or a latency-sensitive loop that must not pay for
 // allocation and synchronising frees.  cfgpu_tau_solve_batched_noalloc()
 // gives them the same solve with all device working memory taken from the
-// file-scope array below, which is part of the loaded module: every GPU that
-// loads the library holds these CFGPU_NOALLOC_BYTES until the process exits.
+// file-scope array below, which is part of this file's device module.  The
+// module, and with it the array's CFGPU_NOALLOC_BYTES, is reserved on a
+// device when the module is loaded there: with the CUDA runtime's default
+// lazy module loading that is the first call of this entry point on the
+// device (the symbol lookup below); with CUDA_MODULE_LOADING=EAGER it is the
+// creation of the context.  From then on the device holds the array until
+// the process exits.  A caller whose GPU memory will be taken over by another
+// allocator therefore makes one (small) call before that allocator reserves
+// the memory.
 //
 // The kernels are the ones cfgpu_tau_solve_batched() launches (k_tau_setup,
 // k_tau_solve); only where their memory comes from differs.
 #include "../../include/cfgpu.h"
 #include "kernels.h"
 
+#include <atomic>
 #include <string>
 
 namespace {
@@ -25,7 +33,9 @@ constexpr size_t kNoallocDoubles = (size_t)CFGPU_NOALLOC_BYTES / sizeof(double);
 static __device__ __align__(256) double g_noalloc_scratch[kNoallocDoubles];
 
 constexpr int kMaxDevices = 64;
-double* g_scratch_ptr[kMaxDevices] = {nullptr};  // device address of g_noalloc_scratch, per device
+// Device address of g_noalloc_scratch, per device.  Several host threads may look it up at once; they all
+// store the same value, and the atomics make that well defined.
+std::atomic<double*> g_scratch_ptr[kMaxDevices] = {};
 
 // Device words a call with these sizes needs (must match the carving below).
 size_t noalloc_words(int N, int nmodes) {
@@ -106,15 +116,23 @@ extern "C" cfgpu_status cfgpu_tau_solve_batched_noalloc(int N, int nmodes, const
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return na_fail(CFGPU_ECUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
   if (dev < 0 || dev >= kMaxDevices) return na_fail(CFGPU_ENOTSUP, "device ordinal beyond the supported range");
-  if (!g_scratch_ptr[dev]) {
-    // First call on this device (current device): look up where the static array lives.
+  double* base = g_scratch_ptr[dev].load(std::memory_order_acquire);
+  if (!base) {
+    // First call on this device (current device): look up where the static array lives.  Under lazy module
+    // loading this loads the module and so reserves the array; that can fail when the device's memory is
+    // already taken.
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e == cudaErrorMemoryAllocation)
+      return na_fail(CFGPU_ENOMEM, "the static working array (" + std::to_string((size_t)CFGPU_NOALLOC_BYTES) +
+                                       " bytes) could not be reserved on this device: make the first call before "
+                                       "another allocator takes the GPU's memory, or load modules eagerly "
+                                       "(CUDA_MODULE_LOADING=EAGER)");
     if (e != cudaSuccess || !p)
       return na_fail(CFGPU_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-    g_scratch_ptr[dev] = static_cast<double*>(p);
+    base = static_cast<double*>(p);
+    g_scratch_ptr[dev].store(base, std::memory_order_release);
   }
-  double* base = g_scratch_ptr[dev];
   const size_t cl = 2 * (size_t)N * nmodes, FN = (size_t)N * nmodes;
   double* raw_in = base;             // 3 cl
   double* raw_out = raw_in + 3 * cl;  // 4 cl
@@ -133,10 +151,15 @@ extern "C" cfgpu_status cfgpu_tau_solve_batched_noalloc(int N, int nmodes, const
   int* dkz = dkx + nmodes;
   cudaStream_t st = 0;
   const size_t cb = cl * sizeof(double);
+  // On an error after the first enqueue, wait for the work already queued (its copies into the caller's
+  // buffers and its use of the shared array) before returning, so that nothing of this call runs on after it.
 #define NA_CK(x)                                                                                     \
   do {                                                                                               \
     cudaError_t e_ = (x);                                                                            \
-    if (e_ != cudaSuccess) return na_fail(CFGPU_ECUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
+    if (e_ != cudaSuccess) {                                                                         \
+      (void)cudaStreamSynchronize(st);                                                               \
+      return na_fail(CFGPU_ECUDA, std::string(#x) + ": " + cudaGetErrorString(e_));                  \
+    }                                                                                                \
   } while (0)
   NA_CK(cudaMemcpyAsync(dkx, kx, nmodes * sizeof(int), cudaMemcpyHostToDevice, st));
   NA_CK(cudaMemcpyAsync(dkz, kz, nmodes * sizeof(int), cudaMemcpyHostToDevice, st));

@@ -666,68 +666,14 @@ __global__ void __launch_bounds__(128) k_tau_solve(GridDev g, int N, SolveParams
 }
 
 // ---------------------------------------------------------------------------
-// Shared-memory variant of the step solve (the one launched).  Same thread
-// mapping as k_tau_solve (4 lanes per mode: part x parity, one warp = 8 modes
-// per block); every per-thread working line lives in shared memory as
-// [slot][i][lane], so the re-reads between passes and the neighbour-lane
-// reads cost shared-memory latency instead of L2 round trips.  The per-mode
-// tables and the history arrays stream from global memory.
-// Slots: 0 = Rx, 1 = Rz, 2 = Ry then v, 3 = P, 4 and 5 = scratch.
+// Per-lane working lines in shared memory, laid out [i][lane] (32 lanes per
+// warp), so the re-reads between passes and the neighbour-lane reads cost
+// shared-memory latency instead of L2 round trips.
 // ---------------------------------------------------------------------------
 struct SLn {
   double* p;
   __device__ __forceinline__ double& operator[](int i) const { return p[i * 32]; }
 };
-
-__device__ void helm_s(int M, int q, const double* __restrict__ hlo, const double* __restrict__ hdi,
-                       const double* __restrict__ hup, PLn band, PLn up, PLn lo, PLn inv, SLn f, SLn u, double bc) {
-  const int nM = 2 * (M - 1) + q;
-  double fi = f[M - 1], fm = f[M - 2];
-  double unext = __ldg(hlo + nM) * fm + __ldg(hdi + nM) * fi;
-  u[M - 1] = unext;
-  double acc = bc - band[M - 1] * unext;
-  double fi1 = fi;
-  fi = fm;
-  for (int i = M - 2; i >= 1; i -= TCH) {
-    double upv[TCH], bv[TCH];
-#pragma unroll
-    for (int k = 0; k < TCH; ++k)
-      if (i - k >= 1) {
-        upv[k] = up[i - k];
-        bv[k] = band[i - k];
-      }
-#pragma unroll
-    for (int k = 0; k < TCH; ++k)
-      if (i - k >= 1) {
-        const int n = 2 * (i - k) + q;
-        const double fm1 = f[i - k - 1];
-        const double bf = (__ldg(hlo + n) * fm1 + __ldg(hdi + n) * fi) + __ldg(hup + n) * fi1;
-        const double ui = bf - upv[k] * unext;
-        u[i - k] = ui;
-        unext = ui;
-        acc -= bv[k] * ui;
-        fi1 = fi;
-        fi = fm1;
-      }
-  }
-  double prev = acc / band[0];
-  u[0] = prev;
-  for (int i = 1; i < M; i += TCH) {
-    double lv[TCH], iv[TCH];
-#pragma unroll
-    for (int k = 0; k < TCH; ++k)
-      if (i + k < M) {
-        lv[k] = lo[i + k];
-        iv[k] = inv[i + k];
-      }
-#pragma unroll
-    for (int k = 0; k < TCH; ++k)
-      if (i + k < M) {
-        prev = (u[i + k] - lv[k] * prev) * iv[k];
-        u[i + k] = prev;
-      }
-  }
-}
 
 // Parity q of d = diff(x) with ct[n] = scale*(n+1); xo is the other parity of x; returns the parity's sum.
 __device__ double diff_s(int M, int q, const double* ct, SLn xo, SLn* dst) {
@@ -751,266 +697,8 @@ __device__ double diff_s(int M, int q, const double* ct, SLn xo, SLn* dst) {
   return sum;
 }
 
-template <typename R>
-__global__ void __launch_bounds__(32) k_tau_solve_s(GridDev g, int N, SolveParams sp, SolvePtrs P, HelmB hb,
-                                                    TauTable tt) {
-  extern __shared__ double sm[];
-  const int lane = threadIdx.x;
-  const int t = blockIdx.x * 32 + lane;
-  const int Md = g.Md;
-  const bool act = (t >> 2) < Md;
-  const int m = act ? (t >> 2) : Md - 1;
-  const int part = (t >> 1) & 1, q = t & 1;
-  const unsigned gmask = 0xFu << (lane & 28);
-  const int row = 2 * Md;
-  const size_t comp = (size_t)row * N;
-  const int off = 2 * m + part, poff = 2 * m + (1 - part);
-  const size_t FN = (size_t)N * Md;
-  const int M0 = (N - 1) / 2 + 1;
-  const int M = q ? (N - 1) / 2 : M0;
-  const int Nb = N - 1;
-  const double scale = 4.0 / (g.b - g.a);
-  double* ct = sm;  // scale*(n+1), n = 0..N-1
-  double* lines = sm + ((N + 1) & ~1);
-  for (int n = lane; n < N; n += 32) ct[n] = scale * (n + 1);
-  __syncwarp();
-  auto S = [&](int slot) { return SLn{lines + (size_t)slot * M0 * 32 + lane}; };
-  auto So = [&](int slot) { return SLn{lines + (size_t)slot * M0 * 32 + (lane ^ 1)}; };  // other parity
-  auto Sp = [&](int slot) { return SLn{lines + (size_t)slot * M0 * 32 + (lane ^ 2)}; };  // other part
-  auto G = [&](const double* base) { return PLn{const_cast<double*>(base) + off + q * row, 2 * row}; };
-  auto Go = [&](const double* base) { return PLn{const_cast<double*>(base) + off + (1 - q) * row, 2 * row}; };
-  auto Gp = [&](const double* base) { return PLn{const_cast<double*>(base) + poff + q * row, 2 * row}; };
-  auto TB = [&](int f) { return PLn{tt.f + f * FN + m + q * Md, 2 * Md}; };
-  const int kx = mode_kx(g, m), kz = mode_kz(g, m);
-  const bool m00 = (kx == 0 && kz == 0);
-  const double kxL = 2 * M_PI * kx / g.Lx;
-  const double kzL = 2 * M_PI * kz / g.Lz;
-  const int fld = mode_field(g, m);
-  if (P.slot) apply_slot(sp, P.slot[fld]);
-  const size_t fb = (size_t)P.base_stride * fld;
-  const double nu = sp.nu;
-  const double lambda = tt.s[TS_LAMBDA * Md + m];
-  const double* __restrict__ hlo = hb.lo;
-  const double* __restrict__ hdi = hb.di;
-  const double* __restrict__ hup = hb.up;
-  const int rslot[3] = {0, 2, 1};
-
-  // ---- A: right-hand side -------------------------------------------------
-  if (sp.kind == 0) {
-    for (int c = 0; c < 3; ++c) {
-      SLn out = S(rslot[c]);
-      for (int i = 0; i < M; ++i) {
-        const size_t o = (size_t)(2 * i + q) * row + off;
-        double acc = 0.0;
-        for (int j = 0; j < sp.order; ++j)
-          acc += sp.a[j] * P.uin[j][c * comp + o] + sp.b[j] * (double)static_cast<const R*>(P.nin[j])[c * comp + o];
-        if (m00 && part == 0 && c != 1) {
-          acc += nu * (c == 0 ? P.Ubaseyy[fb + 2 * i + q] : P.Wbaseyy[fb + 2 * i + q]);
-          if (2 * i + q == 0 && sp.constraint == 0) acc -= (c == 0 ? sp.dPdxRef : sp.dPdzRef);
-        }
-        out[i] = acc;
-      }
-    }
-  } else {
-    const double kappa2 = 4 * M_PI * M_PI * ((kx / g.Lx) * (kx / g.Lx) + (kz / g.Lz) * (kz / g.Lz));
-    const double Dx = 2 * M_PI * kx / g.Lx * (kx == g.kxmax ? 0.0 : 1.0);
-    const double Dz = 2 * M_PI * kz / g.Lz * (kz == g.kzmax ? 0.0 : 1.0);
-    for (int c = 0; c < 3; ++c) {
-      PLn uc = G(P.uin[0] + c * comp);
-      PLn uo = Go(P.uin[0] + c * comp);
-      SLn d1 = S(4);
-      __syncwarp(gmask);
-      // d1 = D(nu u) for my parity; partial sum for the bulk wall-shear term
-      double s = 0.0;
-      {
-        double dn2 = 0.0;
-        int i = M - 1;
-        if (q == 0) {
-          const double v = dn2 + ct[2 * i] * 0.0;
-          d1[i] = v;
-          s += v;
-          dn2 = v;
-          i--;
-        }
-        for (; i >= 0; i -= TCH) {
-          double xv[TCH];
-#pragma unroll
-          for (int k = 0; k < TCH; ++k)
-            if (i - k >= 0) xv[k] = uo[i - k + q];
-#pragma unroll
-          for (int k = 0; k < TCH; ++k)
-            if (i - k >= 0) {
-              const int n = 2 * (i - k) + q;
-              double v = dn2 + ct[n] * (nu * xv[k]);
-              dn2 = v;
-              if (n == 0) v *= 0.5;
-              d1[i - k] = v;
-              s += v;
-            }
-        }
-      }
-      const double so = __shfl_xor_sync(gmask, s, 1);
-      double wall = 0.0;
-      if (m00 && part == 0 && sp.constraint == 1 && c != 1) {
-        const double s0 = q == 0 ? s : so, s1 = q == 0 ? so : s;
-        wall = ((s0 + s1) - (s0 - s1)) / (g.b - g.a);
-      }
-      __syncwarp(gmask);
-      SLn d1o = So(4);
-      PLn qo = Go(P.qin);
-      PLn qp = Gp(P.qin);
-      SLn out = S(rslot[c]);
-      const R* Nj = static_cast<const R*>(P.nin[0]) + c * comp + off + q * row;
-      const R* Nj1 = sp.kind == 1 ? static_cast<const R*>(P.nin[1]) + c * comp + off + q * row : nullptr;
-      R* Q = sp.kind == 2 ? static_cast<R*>(P.Q) + c * comp + off + q * row : nullptr;
-      const double kD = c == 0 ? Dx : Dz;
-      double d2n2 = 0.0, dqn2 = 0.0;
-      for (int i = M - 1; i >= 0; --i) {
-        const int n = 2 * i + q;
-        const double x1 = (n + 1 <= Nb) ? d1o[i + q] : 0.0;
-        double d2 = d2n2 + ct[n] * x1;
-        d2n2 = d2;
-        if (n == 0) d2 *= 0.5;
-        double gq;
-        if (c == 1) {
-          const double y1 = (n + 1 <= Nb) ? qo[i + q] : 0.0;
-          double dq = dqn2 + ct[n] * y1;
-          dqn2 = dq;
-          if (n == 0) dq *= 0.5;
-          gq = dq;
-        } else {
-          gq = part == 0 ? -(kD * qp[i]) : kD * qp[i];
-        }
-        const double u0 = uc[i];
-        double L = d2 - kappa2 * (nu * u0) - gq;
-        if (m00 && part == 0 && c != 1) {
-          L += nu * (c == 0 ? P.Ubaseyy[fb + n] : P.Wbaseyy[fb + n]);
-          if (n == 0) L -= sp.constraint == 0 ? (c == 0 ? sp.dPdxRef : sp.dPdzRef)
-                                              : wall + sp.baseShear[c == 0 ? 0 : 1];
-        }
-        const double nj = (double)Nj[(size_t)i * 2 * row];
-        double rhs;
-        if (sp.kind == 1) {
-          const double nj1 = (double)Nj1[(size_t)i * 2 * row];
-          rhs = (u0 * sp.lam + sp.a_b * L) + ((-sp.g_b) * nj + (-sp.z_b) * nj1);
-        } else {
-          const double Qn = (double)Q[(size_t)i * 2 * row] * sp.rkA - nj;
-          if (act) Q[(size_t)i * 2 * row] = (R)Qn;
-          rhs = L + (sp.lam * u0 + sp.B_C * Qn);
-        }
-        if (m00 && part == 0 && c != 1) {
-          rhs += nu * (c == 0 ? P.Ubaseyy[fb + n] : P.Wbaseyy[fb + n]);
-          if (n == 0 && sp.constraint == 0) rhs -= (c == 0 ? sp.dPdxRef : sp.dPdzRef);
-        }
-        out[i] = rhs;
-      }
-    }
-  }
-  __syncwarp(gmask);
-
-  // ---- B: pressure ---------------------------------------------------------
-  PLn PH_band = TB(TF_PBAND), PH_up = TB(TF_PUP), PH_lo = TB(TF_PLO), PH_inv = TB(TF_PINV);
-  PLn VH_band = TB(TF_VBAND), VH_up = TB(TF_VUP), VH_lo = TB(TF_VLO), VH_inv = TB(TF_VINV);
-  {
-    SLn rr = S(4);
-    diff_s(M, q, ct, So(2), &rr);
-    SLn Rxp = Sp(0), Rzp = Sp(1);
-    for (int i = 0; i < M; ++i) {
-      const double x = kxL * Rxp[i] + kzL * Rzp[i];
-      rr[i] = part == 0 ? rr[i] - x : rr[i] + x;
-    }
-    helm_s(M, q, hlo, hdi, hup, PH_band, PH_up, PH_lo, PH_inv, rr, S(3), 0.0);
-  }
-  __syncwarp(gmask);
-  // ---- C: wall-normal velocity, influence and tau corrections -------------
-  SLn Pl = S(3), Vl = S(2);
-  const double RyTop = S(2)[M - 1];
-  if (m00) {
-    for (int i = 0; i < M; ++i) Vl[i] = 0.0;
-  } else {
-    SLn tmp = S(5);
-    diff_s(M, q, ct, So(3), &tmp);
-    SLn Ry = S(2);
-    for (int i = 0; i < M; ++i) tmp[i] -= Ry[i];
-    helm_s(M, q, hlo, hdi, hup, VH_band, VH_up, VH_lo, VH_inv, tmp, Vl, 0.0);
-  }
-  __syncwarp(gmask);
-  {
-    const double s = m00 ? 0.0 : diff_s(M, q, ct, So(2), nullptr);
-    const double so = __shfl_xor_sync(gmask, s, 1);
-    const double s0 = q == 0 ? s : so, s1 = q == 0 ? so : s;
-    const double plus = s0 + s1, minus = s0 - s1;
-    const double* sc = tt.s + m;
-    const double i00 = sc[TS_I00 * Md], i01 = sc[TS_I01 * Md], i10 = sc[TS_I10 * Md], i11 = sc[TS_I11 * Md];
-    const double dp = -i00 * plus - i01 * minus;
-    const double dm = -i10 * plus - i11 * minus;
-    PLn Pp = TB(TF_PP), Vp = TB(TF_VP), Pm = TB(TF_PM), Vm = TB(TF_VM);
-    if (!m00)
-      for (int i = 0; i < M; ++i) {
-        Pl[i] += dp * Pp[i] + dm * Pm[i];
-        Vl[i] += dp * Vp[i] + dm * Vm[i];
-      }
-    const int itop = M - 1;
-    double x0 = 0.0, y0 = 0.0;
-    if (!m00) {
-      x0 = lambda * Vl[itop] - nu * 0.0 - RyTop;
-      y0 = q == 0 ? ct[Nb - 1] * Pl[itop] : 0.0;
-    }
-    const double ox = __shfl_xor_sync(gmask, x0, 1);
-    const double oy = __shfl_xor_sync(gmask, y0, 1);
-    if (!m00 && sp.taucorrection) {
-      const double s1Nb = (q == 0 ? x0 : ox) + 0.0;
-      const double s1Nb1 = q == 0 ? ox + y0 : x0 + oy;
-      const double sNb = s1Nb / (1.0 - sc[TS_S0NB * Md]);
-      const double sNb1 = s1Nb1 / (1.0 - sc[TS_S0NB1 * Md]);
-      PLn P0 = TB(TF_P0), V0 = TB(TF_V0);
-      const double fP = q == 0 ? sNb1 : sNb, fV = q == 0 ? sNb : sNb1;
-      for (int i = 0; i < M; ++i) {
-        Pl[i] += fP * P0[i];
-        Vl[i] += fV * V0[i];
-      }
-    }
-  }
-  __syncwarp(gmask);
-  // ---- D: streamwise and spanwise velocity -------------------------------
-  SLn Ppt = Sp(3);
-  const bool zero_im = m00 && part == 1 && sp.force_real00;
-  for (int c = 0; c < 2; ++c) {
-    const double kL = c == 0 ? kxL : kzL;
-    SLn Rc = S(c == 0 ? 0 : 1);
-    SLn r = S(4), o = S(5);
-    for (int i = 0; i < M; ++i) r[i] = part == 0 ? -(kL * Ppt[i]) - Rc[i] : kL * Ppt[i] - Rc[i];
-    helm_s(M, q, hlo, hdi, hup, VH_band, VH_up, VH_lo, VH_inv, r, o, 0.0);
-    if (m00 && sp.constraint == 1 && part == 0) {
-      // mean-constrained solve of the real part (helmholtz.cpp:158-213); the mean involves even n only
-      double amean = 0.0;
-      if (q == 0) {
-        amean = o[0];
-        for (int i = 1; i < M; ++i) amean -= o[i] / (double)((2 * i) * (2 * i) - 1);
-        const double ucmean = tt.s[TS_UCMEAN * Md + m];
-        const double target = c == 0 ? sp.umean : sp.wmean;
-        const double mu = nu * (target - amean) / ucmean;
-        r[0] = r[0] + mu;
-        helm_s(M, q, hlo, hdi, hup, VH_band, VH_up, VH_lo, VH_inv, r, o, 0.0);
-        if (act && P.dPdx_out) P.dPdx_out[2 * mode_field(g, m) + c] = mu;
-      }
-    }
-    if (act) {
-      PLn gout = G(P.uout + (c == 0 ? 0 : 2) * comp);
-      for (int i = 0; i < M; ++i) gout[i] = zero_im ? 0.0 : o[i];
-    }
-  }
-  if (act) {
-    PLn gq = G(P.qout), gv = G(P.uout + comp);
-    for (int i = 0; i < M; ++i) {
-      gq[i] = zero_im ? 0.0 : Pl[i];
-      gv[i] = zero_im ? 0.0 : Vl[i];
-    }
-  }
-}
-
 // ---------------------------------------------------------------------------
-// Table-staged variant (the one launched).  As k_tau_solve_s, but before each
+// Table-staged variant (the one launched).  Before each
 // Helmholtz solve the warp copies the four UL-factor lines of its 8 modes into
 // shared memory with one burst of independent coalesced loads, so the
 // dependent sweeps read factors at shared-memory latency.  Rx and Rz, which

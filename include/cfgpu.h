@@ -395,11 +395,18 @@ cfgpu_status cfgpu_tau_solve_batched(int N, int nmodes, const int* kx, const int
  *
  * Same arguments, host buffers and results as cfgpu_tau_solve_batched, but
  * it calls no cudaMalloc/cudaFree: all device working memory comes from one
- * static array of CFGPU_NOALLOC_BYTES (16 MiB) that every GPU loading this
- * library holds until the process exits.  It is for callers that must not
- * allocate GPU memory: processes whose GPU memory is fully reserved by
- * another allocator (a framework's pool, a fixed budget on a shared GPU),
- * and latency-sensitive loops that cannot pay for allocation.
+ * static array of CFGPU_NOALLOC_BYTES (16 MiB) in the library's device code.
+ * It is for callers that must not allocate GPU memory: processes whose GPU
+ * memory is fully reserved by another allocator (a framework's pool, a fixed
+ * budget on a shared GPU), and latency-sensitive loops that cannot pay for
+ * allocation.
+ *
+ * When the array is reserved: with the CUDA runtime's default lazy module
+ * loading, at the first call of this function on a device; with
+ * CUDA_MODULE_LOADING=EAGER, when the context is created.  From then on that
+ * device holds it until the process exits.  Make the first call (any size)
+ * before another allocator takes the device's memory; if the array cannot be
+ * reserved the call returns CFGPU_ENOMEM and says so in cfgpu_last_error().
  *
  * Limit: 54*N*nmodes + 9*nmodes + 4*N doubles must fit in the array, e.g.
  * N = 49 allows nmodes <= 789, N = 97 allows nmodes <= 399; larger requests

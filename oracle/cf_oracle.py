@@ -28,6 +28,7 @@ round-off; everything else follows the reference's operation order.
 from __future__ import annotations
 
 import math
+import os
 from dataclasses import dataclass, field
 from typing import List, Optional, Sequence
 
@@ -35,6 +36,9 @@ import numpy as np
 import scipy.fft as sfft
 
 PI = math.pi
+# Threads for the FFT/DCT calls (scipy.fft workers). The transforms are the oracle's cost at large grids;
+# the thread count does not change any result.
+WORKERS = int(os.environ.get("CF_ORACLE_WORKERS", "0")) or (os.cpu_count() or 1)
 
 # Enumerations mirroring channelflow/dnsflags.h:24-38 (same names, same order).
 ZeroBase, LinearBase, ParabolicBase, LaminarBase, SuctionBase, ArbitraryBase = range(6)
@@ -62,7 +66,7 @@ def chebyfft(x: np.ndarray, axis: int = 0) -> np.ndarray:
     FFTW REDFT00 is the unnormalised DCT-I; scipy's type-1 DCT is the same sum.
     """
     N = x.shape[axis]
-    y = sfft.dct(x, type=1, axis=axis)
+    y = sfft.dct(x, type=1, axis=axis, workers=WORKERS)
     nrm = 1.0 / (N - 1)
     y = y * nrm
     sl0 = [slice(None)] * y.ndim
@@ -80,7 +84,7 @@ def ichebyfft(c: np.ndarray, axis: int = 0) -> np.ndarray:
     sl = [slice(None)] * x.ndim
     sl[axis] = slice(1, N - 1)
     x[tuple(sl)] *= 0.5
-    return sfft.dct(x, type=1, axis=axis)
+    return sfft.dct(x, type=1, axis=axis, workers=WORKERS)
 
 
 def cdiff(u: np.ndarray, L: float) -> np.ndarray:
@@ -576,12 +580,12 @@ class Grid:
 def make_physical(u: np.ndarray, g: Grid) -> np.ndarray:
     """Spectral [i,my,mx,mz] -> physical [i,ny,nx,nz] (makePhysical_y then makePhysical_xz)."""
     uy = ichebyfft(u, axis=1)
-    return np.fft.irfft2(uy, s=(g.Nx, g.Nz), axes=(2, 3)) * (g.Nx * g.Nz)
+    return sfft.irfft2(uy, s=(g.Nx, g.Nz), axes=(2, 3), workers=WORKERS) * (g.Nx * g.Nz)
 
 
 def make_spectral(p: np.ndarray, g: Grid) -> np.ndarray:
     """Physical -> spectral (makeSpectral_xz with 1/(Nx Nz) scaling, then makeSpectral_y)."""
-    s = np.fft.rfft2(p, axes=(2, 3)) * (1.0 / (g.Nx * g.Nz))
+    s = sfft.rfft2(p, axes=(2, 3), workers=WORKERS) * (1.0 / (g.Nx * g.Nz))
     return chebyfft(s, axis=1)
 
 
@@ -1609,7 +1613,7 @@ def random_divfree_field(g: Grid, seed: int, norm: float, decay_k: float = 0.5, 
 
 
 def divergence_norm(u: np.ndarray, g: Grid) -> float:
-    """L2 norm of div(u) for a spectral field."""
+    """L2 norm of div(u) for a spectral field (divNorm, diffops.cpp:89-115: the divergence's normalised L2 norm)."""
     kx = np.array([g.kx(m) for m in range(g.Nx)])
     kz = np.arange(g.Mz)
     Dx = (1j * 2 * PI * kx / g.Lx)[None, :, None]
@@ -1617,6 +1621,21 @@ def divergence_norm(u: np.ndarray, g: Grid) -> float:
     L = g.b - g.a
     d = Dx * u[0] + Dz * u[2] + cdiff(u[1].real, L) + 1j * cdiff(u[1].imag, L)
     return L2Norm(d[None], g)
+
+
+def bc_norm(u: np.ndarray, g: Grid) -> float:
+    """bcNorm (diffops.cpp:18-48, 85): sqrt of the sum over components and (kx, kz) modes of |u(a)|^2 + |u(b)|^2."""
+    ua = eval_a(u.reshape(u.shape[0], g.Ny, -1).transpose(1, 0, 2).reshape(g.Ny, -1))
+    ub = eval_b(u.reshape(u.shape[0], g.Ny, -1).transpose(1, 0, 2).reshape(g.Ny, -1))
+    return math.sqrt(float(np.sum(np.abs(ua) ** 2) + np.sum(np.abs(ub) ** 2)))
+
+
+def wall_slope_norm(u: np.ndarray, g: Grid) -> float:
+    """Like bc_norm for dv/dy: the no-slip and continuity conditions give v' = 0 at both walls."""
+    L = g.b - g.a
+    v = u[1].reshape(g.Ny, -1)
+    dv = cdiff(v.real, L) + 1j * cdiff(v.imag, L)
+    return math.sqrt(float(np.sum(np.abs(eval_a(dv)) ** 2) + np.sum(np.abs(eval_b(dv)) ** 2)))
 
 
 def load_io_field(phys_io: np.ndarray, Nx: int, Nz: int) -> np.ndarray:

@@ -1,9 +1,9 @@
 """Generate the committed golden fixtures from the channelflow reference's own test data.
 
-Run in a container that has the reference checkout (its path is the first
-argument, default ``/root/reference``):
+Run where a channelflow checkout exists; its path is the first argument or,
+failing that, the CHANNELFLOW_SRC environment variable:
 
-    python tests/golden/make_golden.py [/path/to/channelflow]
+    python tests/golden/make_golden.py /path/to/channelflow
 
 It writes, next to this script:
 
@@ -227,7 +227,10 @@ def read_asc_basis(path):
     return vals[..., 0] + 1j * vals[..., 1], head
 
 
-def main(ref="/root/reference"):
+def main(ref=None):
+    ref = ref or os.environ.get("CHANNELFLOW_SRC")
+    if not ref:
+        raise SystemExit("usage: make_golden.py /path/to/channelflow (or set CHANNELFLOW_SRC)")
     here = os.path.dirname(os.path.abspath(__file__))
     dd = os.path.join(ref, "tests", "data")
     out = {}

@@ -34,12 +34,14 @@ def gpu_run(u0, g, fl, nsteps, precision="fp64", base=None, chunks=None):
     return u, q, dns
 
 
-def test_tau_batched_matches_oracle():
+@pytest.mark.parametrize("N,cases", [(49, 10), (301, 2)])
+def test_tau_batched_matches_oracle(N, cases):
+    """N = 301 exceeds the shared-memory staging of the three-kernel solve and takes the one-kernel path."""
     from channelflow_gb300 import tau_solve_batched
     from tests.test_oracle_golden import tau_case
     rng = np.random.default_rng(11)
-    for _ in range(10):
-        c = tau_case(rng)
+    for _ in range(cases):
+        c = tau_case(rng, N=N)
         kxs = np.array([c["kx"], 0, 1, 3])
         kzs = np.array([c["kz"], 0, 0, 2])
         R = [np.stack([c[k]] * 4) for k in ("Rx", "Ry", "Rz")]

@@ -115,3 +115,44 @@ def test_dns_zero(ts, constraint):
     u = np.zeros((3, g.Ny, g.Nx, g.Mz), complex)
     u, q, _ = oracle_run(u, g, fl, 20)
     assert O.L2Norm(u, g) < 1e-8
+
+
+@pytest.mark.parametrize("ts,where,constraint", [
+    (O.CNFE1, "fluc", O.BulkVelocity), (O.CNAB2, "base", O.PressureGradient), (O.CNRK2, "fluc", O.PressureGradient),
+    (O.SMRK2, "base", O.BulkVelocity), (O.SBDF2, "fluc", O.BulkVelocity), (O.SBDF3, "fluc", O.PressureGradient),
+    (O.SBDF4, "base", O.BulkVelocity)])
+def test_dns_parabola(ts, where, constraint):
+    """tests/dnsParabolaTest.cpp:50-266: the parabola 1 - y^2, carried by the base flow ("base") or by u
+    ("fluc"), is a steady state under dPdx = -2 nu or Ubulk = 2/3; the distance from it, summed over
+    t = 0..9 (10 steps of dt = 0.1 between samples), stays below 1e-13. One case per scheme here; the GPU
+    test runs all 28."""
+    g = O.Grid(8, 33, 8, 2 * math.pi, 2 * math.pi)
+    nu = 1.0 / 400
+    fl = O.DNSFlags(nu=nu, dt=0.1, timestepping=ts, initstepping=O.SMRK2, constraint=constraint,
+                    baseflow=O.ZeroBase, dPdx=-2.0 * nu, Ubulk=2.0 / 3.0)
+    zero = np.zeros(g.Ny)
+    parabola = np.zeros(g.Ny)
+    parabola[0], parabola[2] = 0.5, -0.5
+    u = np.zeros((3, g.Ny, g.Nx, g.Mz), complex)
+    if where == "fluc":
+        u[0, :, 0, 0] = parabola
+    ut = u.copy()
+    q = np.zeros((1,) + u.shape[1:], complex)
+    dns = O.DNS(u.copy(), q.copy(), g, fl, base=[parabola if where == "base" else zero, zero])
+    err = 0.0
+    for _ in range(10):
+        err += O.L2Dist(u, ut, g)
+        u, q = dns.advance(u, q, 10)
+    assert err < 1e-13
+
+
+def test_constraint_norms_of_seeded_field():
+    """bc_norm / wall_slope_norm / divergence_norm vanish on the seeded initial fields and detect a violation."""
+    g = O.Grid(16, 17, 16, *COUETTE_BOX)
+    u = O.random_divfree_field(g, seed=3, norm=0.2)
+    n = O.L2Norm(u, g)
+    assert O.divergence_norm(u, g) < 1e-13 * n and O.bc_norm(u, g) < 1e-13 * n
+    assert O.wall_slope_norm(u, g) < 1e-13 * n
+    bad = u.copy()
+    bad[1, 1, 1, 1] += 1e-3
+    assert O.bc_norm(bad, g) > 1e-4 and O.wall_slope_norm(bad, g) > 1e-4

@@ -48,6 +48,37 @@ def test_noalloc_matches_allocating_entry_point_twice(lib):
             assert np.abs(a - b).max() <= TOL * max(1.0, np.abs(b).max())
 
 
+def _free_device_bytes():
+    cudart = None
+    for name in ("libcudart.so.13", "libcudart.so.12", "libcudart.so"):
+        try:
+            cudart = C.CDLL(name)
+            break
+        except OSError:
+            continue
+    assert cudart is not None, "CUDA runtime library not found"
+    free, total = C.c_size_t(), C.c_size_t()
+    assert cudart.cudaMemGetInfo(C.byref(free), C.byref(total)) == 0
+    return free.value
+
+
+def test_noalloc_call_leaves_device_memory_unchanged(lib):
+    """After the first call (which may reserve the static array), further calls take no device memory."""
+    rng = np.random.default_rng(5)
+    c = tau_case(rng)
+    N, nm = c["N"], 24
+    kx = rng.integers(-8, 9, nm).astype(np.int32)
+    kz = rng.integers(0, 9, nm).astype(np.int32)
+    R = [np.ascontiguousarray(np.stack([c[k]] * nm)) for k in ("Rx", "Ry", "Rz")]
+    first = _solve(lib, "cfgpu_tau_solve_batched_noalloc", N, kx, kz, c, R)
+    before = _free_device_bytes()
+    second = _solve(lib, "cfgpu_tau_solve_batched_noalloc", N, kx, kz, c, R)
+    after = _free_device_bytes()
+    assert after == before
+    for a, b in zip(first, second):
+        assert np.array_equal(a, b)
+
+
 def test_noalloc_rejects_oversize_request(lib):
     N, nm = 97, 400
     kx = np.zeros(nm, np.int32)
