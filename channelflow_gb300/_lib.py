@@ -123,6 +123,19 @@ _SIGS = {
     "cfgpu_dns_advance_timed": [C.c_void_p, C.c_int, _PD],
     "cfgpu_dns_set_profiling": [C.c_void_p, C.c_int],
     "cfgpu_dns_phase_times": [C.c_void_p, _PD, C.POINTER(C.c_longlong), _PD, C.POINTER(C.c_longlong)],
+    "cfgpu_flowfield_create": [C.POINTER(Grid), C.c_int, C.POINTER(C.c_void_p)],
+    "cfgpu_flowfield_destroy": [C.c_void_p],
+    "cfgpu_flowfield_size": [C.c_void_p, C.POINTER(C.c_longlong)],
+    "cfgpu_flowfield_data": [C.c_void_p, C.POINTER(C.c_void_p)],
+    "cfgpu_flowfield_upload": [C.c_void_p, _PD, C.c_int, C.c_int],
+    "cfgpu_flowfield_download": [C.c_void_p, _PD],
+    "cfgpu_flowfield_state": [C.c_void_p, _PI, _PI],
+    "cfgpu_flowfield_make_physical": [C.c_void_p],
+    "cfgpu_flowfield_make_spectral": [C.c_void_p],
+    "cfgpu_flowfield_make_physical_xz": [C.c_void_p],
+    "cfgpu_flowfield_make_spectral_xz": [C.c_void_p],
+    "cfgpu_flowfield_make_physical_y": [C.c_void_p],
+    "cfgpu_flowfield_make_spectral_y": [C.c_void_p],
     "cfgpu_tau_solve_batched": [C.c_int, C.c_int, _PI, _PI, C.c_double, C.c_double, C.c_double, C.c_double,
                                 C.c_double, C.c_double, C.c_int, _PD, _PD, _PD, _PD, _PD, _PD, _PD],
     "cfgpu_tau_solve_batched_noalloc": [C.c_int, C.c_int, _PI, _PI, C.c_double, C.c_double, C.c_double, C.c_double,

@@ -378,6 +378,8 @@ void pinned_free(void* p) {
 
 int cfgpu_record_error(int code, const std::string& msg) { return fail(code, msg); }
 
+bool cfgpu_fft_plan(int L, FftPlan& p, std::vector<std::complex<long double>>& tw) { return make_fft_plan(L, p, tw); }
+
 // ---------------------------------------------------------------------------
 // The DNS object
 // ---------------------------------------------------------------------------

@@ -88,6 +88,33 @@ cfgpu_status cfgpu_field_destroy(cfgpu_field f);
 cfgpu_status cfgpu_dns_set_fields_device(cfgpu_dns dns, int slot, cfgpu_field u, cfgpu_field q);
 cfgpu_status cfgpu_dns_get_fields_device(cfgpu_dns dns, int slot, cfgpu_field u, cfgpu_field q);
 
+/*
+ * A whole FlowField on the GPU (every mode, Nyquist included) with the reference's transforms:
+ * FlowField::makePhysical / makeSpectral and their _xz / _y halves (channelflow/flowfield.cpp:1850-1997),
+ * in place, FP64.  The buffer is the reference's serial FlowField buffer (flowfield.h:370-400):
+ * Nd*Ny*Nx*Nzpad doubles with Nzpad = 2*(Nz/2+1); xz-spectral data is complex [i][my][mx][mz], xz-physical
+ * data real [i][ny][nx][nz] with rows of Nzpad.  The (xzstate, ystate) pair follows the reference
+ * (fieldstate, cfbasics/mathdefs.h:77: Physical = 0, Spectral = 1); a transform to the current state does
+ * nothing, makeSpectral runs xz then y, makePhysical y then xz.  Forward xz scales by 1/(Nx Nz); y uses the
+ * chebyfft/ichebyfft scaling (chebyshev.cpp:262-303).  cfgpu_flowfield_data gives the device buffer.
+ * Nx and Nz even and 2,3,5-smooth.
+ */
+enum { CFGPU_PHYSICAL = 0, CFGPU_SPECTRAL = 1 };
+typedef struct cfgpu_flowfield_s* cfgpu_flowfield;
+cfgpu_status cfgpu_flowfield_create(const cfgpu_grid* grid, int Nd, cfgpu_flowfield* out);
+cfgpu_status cfgpu_flowfield_destroy(cfgpu_flowfield f);
+cfgpu_status cfgpu_flowfield_size(cfgpu_flowfield f, long long* ndoubles);
+cfgpu_status cfgpu_flowfield_data(cfgpu_flowfield f, double** device_ptr);
+cfgpu_status cfgpu_flowfield_upload(cfgpu_flowfield f, const double* host, int xzstate, int ystate);
+cfgpu_status cfgpu_flowfield_download(cfgpu_flowfield f, double* host);
+cfgpu_status cfgpu_flowfield_state(cfgpu_flowfield f, int* xzstate, int* ystate);
+cfgpu_status cfgpu_flowfield_make_physical(cfgpu_flowfield f);
+cfgpu_status cfgpu_flowfield_make_spectral(cfgpu_flowfield f);
+cfgpu_status cfgpu_flowfield_make_physical_xz(cfgpu_flowfield f);
+cfgpu_status cfgpu_flowfield_make_spectral_xz(cfgpu_flowfield f);
+cfgpu_status cfgpu_flowfield_make_physical_y(cfgpu_flowfield f);
+cfgpu_status cfgpu_flowfield_make_spectral_y(cfgpu_flowfield f);
+
 /* TimeStep parameters (channelflow/dnsflags.h:166-198): dt within [dtmin, dtmax], dT = n dt the CFL-check
  * interval, CFL kept within [CFLmin, CFLmax] when variable != 0. */
 typedef struct cfgpu_timestep {
