@@ -111,6 +111,7 @@ _SIGS = {
     "cfgpu_server_destroy": [C.c_void_p],
     "cfgpu_dns_set_graphs": [C.c_void_p, C.c_int],
     "cfgpu_set_autotune": [C.c_int],
+    "cfgpu_set_fused_xz": [C.c_int],
     "cfgpu_dns_set_symmetries": [C.c_void_p, C.c_void_p, C.c_int, C.c_int],
     "cfgpu_dns_symmetry": [C.c_void_p, C.POINTER(SymmetryC), C.c_int],
     "cfgpu_field_symmetry": [C.POINTER(Grid), C.c_int, C.c_int, C.POINTER(SymmetryC), C.c_int, _PD],

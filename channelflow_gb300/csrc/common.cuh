@@ -13,8 +13,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+// 8-byte (FP32) / 16-byte (FP64) aligned, so a complex moves with one vector load or store.
 template <typename R>
-struct cpx {
+struct alignas(2 * sizeof(R)) cpx {
   R x, y;
 };
 

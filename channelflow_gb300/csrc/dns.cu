@@ -201,6 +201,24 @@ bool make_fft_plan(int L, FftPlan& p, std::vector<std::complex<long double>>& tw
   return true;
 }
 
+// exp(-2 pi i e / L) for e < L, re/im interleaved; quarter-circle points exact (0, +-1).
+std::vector<double> circle_table(int L) {
+  std::vector<double> t(2 * (size_t)L);
+  const long double PI_L = 3.14159265358979323846264338327950288L;
+  auto snap = [](long double v) -> double {
+    if (fabsl(v) < 1e-18L) return 0.0;
+    if (fabsl(v - 1.0L) < 1e-18L) return 1.0;
+    if (fabsl(v + 1.0L) < 1e-18L) return -1.0;
+    return (double)v;
+  };
+  for (int e = 0; e < L; ++e) {
+    const long double ang = 2.0L * PI_L * (long double)e / (long double)L;
+    t[2 * (size_t)e] = snap(cosl(ang));
+    t[2 * (size_t)e + 1] = snap(-sinl(ang));
+  }
+  return t;
+}
+
 struct ChebMats {
   std::vector<double> invA, invB, fwdA, fwdB;  // P x KA, P x KB (row-major)
   std::vector<double> derA, derB;              // (2/L) T'_n at y_j for even / odd n
@@ -586,6 +604,10 @@ struct cfgpu_dns_s {
   // transforms
   FftPlan px{}, pz{};
   void *twx = nullptr, *twz = nullptr;  // R-typed complex
+  // fused x/z pass (rotational form): full-circle twiddle tables exp(-2 pi i e/L), cluster shape
+  void *twxf = nullptr, *twzf = nullptr;
+  bool xzf = false;
+  int xzC = 0, xzRC = 0;
   void *cinvA = nullptr, *cinvB = nullptr, *cfwdA = nullptr, *cfwdB = nullptr;
   void *cderA = nullptr, *cderB = nullptr, *basey = nullptr;  // fused curl: (2/L) T'_n(y_j); U, U', W, W' at y_j
   void *cdfA = nullptr, *cdfB = nullptr;                       // (2/L) diff o chebyfft, parity split
@@ -794,12 +816,19 @@ int nonlinear_impl(cfgpu_dns d, const double* U, void* Nout, int form) {
     nin = gradient ? 12 : 3;
     nout = form == NL_CONVECTION ? 3 : (form == NL_DIVERGENCE ? 6 : 9);
   }
-  CK(launch_xinv<R>(gp, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)W, (cpx<R>*)d->X6, nin, d->st, d->xcols, dt));
-  CK(launch_zphys<R>(gp, form, d->pz, (const cpx<R>*)d->twz, d->RP, (const cpx<R>*)d->X6, (cpx<R>*)d->Z3, d->st,
-                     dt));
-  CK(launch_xfwd<R>(gp, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)d->Z3, (cpx<R>*)d->F3, nout, d->st, d->xcols,
-                    dt));
-  d->launches += 3;
+  if (form == NL_ROTATIONAL && d->xzf) {
+    CK(launch_xz_rot<R>(gp, d->xzC, d->xzRC, (const cpx<R>*)W, (cpx<R>*)d->F3, (const cpx<R>*)d->twxf,
+                        (const cpx<R>*)d->twzf, d->st, dt));
+    d->launches += 1;
+  } else {
+    CK(launch_xinv<R>(gp, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)W, (cpx<R>*)d->X6, nin, d->st, d->xcols,
+                      dt));
+    CK(launch_zphys<R>(gp, form, d->pz, (const cpx<R>*)d->twz, d->RP, (const cpx<R>*)d->X6, (cpx<R>*)d->Z3, d->st,
+                       dt));
+    CK(launch_xfwd<R>(gp, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)d->Z3, (cpx<R>*)d->F3, nout, d->st,
+                      d->xcols, dt));
+    d->launches += 3;
+  }
   const R* F = (const R*)d->F3;
   if (form == NL_ROTATIONAL || form == NL_CONVECTION) {
     CK((launch_cheb<R, R, R>(N, false, (int)row, 3, F, row, comp, (R*)Nout, row, comp, (const R*)d->cfwdA,
@@ -1353,6 +1382,7 @@ struct TuneKey {
 std::mutex g_tune_mu;
 std::map<TuneKey, std::pair<int, int>> g_tune;
 std::atomic<int> g_autotune{1};
+std::atomic<int> g_fused_xz{1};
 std::atomic<int> g_host_access{1};  // direct host-buffer access when the device supports it
 
 template <typename R>
@@ -1573,9 +1603,12 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
   for (auto& v : cm.dfB) v *= 2.0 / (b - a);
   const std::vector<double>& basey = bf.basey;
   const bool fp64 = d->precision == CFGPU_FP64;
+  const std::vector<double> circx = circle_table(Nx), circz = circle_table(Nz);
   if (fp64) {
     CKS(upload_tw<double>(twx, &d->twx, B, d->st));
     CKS(upload_tw<double>(twz, &d->twz, B, d->st));
+    CKS(upload_as<double>(circx, &d->twxf, B, d->st));
+    CKS(upload_as<double>(circz, &d->twzf, B, d->st));
     CKS(upload_as<double>(cm.invA, &d->cinvA, B, d->st));
     CKS(upload_as<double>(cm.invB, &d->cinvB, B, d->st));
     CKS(upload_as<double>(cm.fwdA, &d->cfwdA, B, d->st));
@@ -1610,6 +1643,8 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
       tabs.push_back(tz);
       tabs.push_back(tm);
     }
+    tabs.push_back(circx);
+    tabs.push_back(circz);
     std::vector<size_t> off(tabs.size());
     size_t S = 0;
     for (size_t i = 0; i < tabs.size(); ++i) {
@@ -1624,6 +1659,8 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
     d->kdx = c0 + off[10];
     d->kdz = c0 + off[11];
     d->kmisc = c0 + off[12];
+    d->twxf = c0 + off[13];
+    d->twzf = c0 + off[14];
     d->cS = (long long)(S * sizeof(float));
     CKS(upload_dithered({basey}, {0}, basey.size(), &d->basey, B, d->st));
   }
@@ -1671,6 +1708,17 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
                           ? -1
                           : (rot ? NL_ROTATIONAL : (f.nonlinearity == CFGPU_SkewSymmetric ? NL_SKEW : NL_CONVECTION));
     CKS(fp64 ? autotune<double>(d, tform, nin, nout) : autotune<float>(d, tform, nin, nout));
+  }
+
+  // fused x/z pass for the rotational form (thread-block clusters over a y-plane)
+  d->xzf = false;
+  if (rot && g_fused_xz.load() != 0 && xz_fused_supported(d->gp)) {
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) nsm = 152;
+    const int sh = fp64 ? xz_fused_shape<double>(d->gp, nsm, d->xzC, d->xzRC)
+                        : xz_fused_shape<float>(d->gp, nsm, d->xzC, d->xzRC);
+    d->xzf = sh == 0;
   }
 
   // schemes (DNS::DNS, dns.cpp:22-39)
@@ -1730,7 +1778,9 @@ void dns_free(cfgpu_dns d) {
   if (d->cblock) {
     // the FP32 constant tables live inside one block (all versions): freed once, below
     d->twx = d->twz = d->cinvA = d->cinvB = d->cfwdA = d->cfwdB = d->cderA = d->cderB = d->cdfA = d->cdfB = nullptr;
+    d->twxf = d->twzf = nullptr;
   }
+  F(d->twxf); F(d->twzf);
   F(d->dUbase); F(d->dWbase); F(d->dUbaseyy); F(d->dWbaseyy); F(d->ddPdx);
   F(d->hb_lo); F(d->hb_di); F(d->hb_up);
   F(d->twx); F(d->twz); F(d->cinvA); F(d->cinvB); F(d->cfwdA); F(d->cfwdB);
@@ -2706,6 +2756,11 @@ cfgpu_status cfgpu_field_symmetry(const cfgpu_grid* grid, int dealias, int Nd, c
   if (e != cudaSuccess) st = fail(CFGPU_ECUDA, std::string("symmetry: ") + cudaGetErrorString(e));
   if (st == CFGPU_OK) scatter_modes(&tmp, h.data(), Nd, u);
   return st;
+}
+
+cfgpu_status cfgpu_set_fused_xz(int enable) {
+  g_fused_xz.store(enable ? 1 : 0);
+  return CFGPU_OK;
 }
 
 cfgpu_status cfgpu_set_autotune(int enable) {

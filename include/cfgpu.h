@@ -258,6 +258,11 @@ cfgpu_status cfgpu_dns_set_graphs(cfgpu_dns dns, int enable);
  * Ny * Nx * (Kz+1) >= 200000 planes' worth of work; results do not depend on the choice.  enable = 0 makes
  * later DNS objects use the defaults and clears the cache. */
 cfgpu_status cfgpu_set_autotune(int enable);
+/* No reference counterpart: DNS objects created while enable != 0 (the default) run the rotational form's
+ * x and z transforms and product as one fused kernel per step (a thread-block cluster per y-plane,
+ * distributed shared memory) when the grid allows (Nx, Nz in {32, 48, 64, 96, 128}); otherwise as three
+ * kernels. Both give the same results to rounding. */
+cfgpu_status cfgpu_set_fused_xz(int enable);
 /* Host FlowField buffers: on devices whose kernels reach pageable host memory through the host page
  * tables (GB300 over NVLink-C2C), DNS objects created while enable != 0 (the default) read and write the
  * caller's buffers with one kernel each way; otherwise through host-side gathers and pinned staging

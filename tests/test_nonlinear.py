@@ -50,3 +50,33 @@ def test_nonlinear_matches_oracle(name, dims, box, fkw, precision, tol):
     m = np.abs(u2) > 0
     assert np.array_equal(u2[m], u[m])
     d.close()
+
+
+FUSED_GRIDS = [(32, 33, 32), (48, 25, 64), (128, 33, 128), (96, 17, 48), (64, 21, 96)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol,tol_pair", [("fp64", 1e-12, 1e-13), ("mixed", 1e-5, 3e-6)])
+@pytest.mark.parametrize("dims", FUSED_GRIDS, ids=["%dx%dx%d" % d for d in FUSED_GRIDS])
+def test_fused_xz_pass_matches_oracle_and_three_kernel_path(dims, precision, tol, tol_pair):
+    """The rotational form's fused x/z kernel (one thread-block cluster per y-plane) against the oracle and
+    against the three-kernel path (x inverse, z pass, x forward) on the same field."""
+    from channelflow_gb300 import DNS, build
+    from channelflow_gb300 import _lib as L
+    build.build()
+    lib = L.load()
+    g = O.Grid(dims[0], dims[1], dims[2], *POISEUILLE_BOX)
+    fl = O.DNSFlags(nu=1 / 2000, dt=0.01, baseflow=O.LaminarBase, constraint=O.BulkVelocity, Ubulk=2 / 3)
+    u = np.ascontiguousarray(O.random_divfree_field(g, seed=sum(dims), norm=0.3, zero_mean_u=True))
+    ref, _ = O.NSE(g, fl, None, u).nonlinear(u)
+    out = {}
+    try:
+        for fused in (1, 0):
+            L.check(lib.cfgpu_set_fused_xz(fused))
+            d = DNS(u.copy(), to_cgrid(g), to_cflags(fl), precision=precision)
+            out[fused] = d.nonlinear(u)
+            d.close()
+    finally:
+        L.check(lib.cfgpu_set_fused_xz(1))
+    assert rel_l2(out[1], ref, g) <= tol
+    assert rel_l2(out[1], out[0], g) <= tol_pair
