@@ -817,8 +817,8 @@ int nonlinear_impl(cfgpu_dns d, const double* U, void* Nout, int form) {
     nout = form == NL_CONVECTION ? 3 : (form == NL_DIVERGENCE ? 6 : 9);
   }
   if (form == NL_ROTATIONAL && d->xzf) {
-    CK(launch_xz_rot<R>(gp, d->xzC, d->xzRC, (const cpx<R>*)W, (cpx<R>*)d->F3, (const cpx<R>*)d->twxf,
-                        (const cpx<R>*)d->twzf, d->st, dt));
+    CK(launch_xz_rot(gp, d->xzC, d->xzRC, (const cpx<R>*)W, (cpx<R>*)d->F3, (const cpx<R>*)d->twxf,
+                     (const cpx<R>*)d->twzf, d->st, dt));
     d->launches += 1;
   } else {
     CK(launch_xinv<R>(gp, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)W, (cpx<R>*)d->X6, nin, d->st, d->xcols,
@@ -1461,6 +1461,53 @@ int autotune(cfgpu_dns d, int form, int nin, int nout) {
   return CFGPU_OK;
 }
 
+// Launch shape of the fused x/z pass: the candidates the device can run, timed with CUDA events on this DNS's
+// own work arrays (contents do not change the work) when autotuning is on, else the model's first choice;
+// cached per (grid, planes, precision).
+std::map<TuneKey, std::pair<int, int>> g_tune_xz;
+
+template <typename R>
+int tune_xz(cfgpu_dns d) {
+  const GridDev& gp = d->gp;
+  const TuneKey key{gp.Nx, gp.Ny, gp.Nz, gp.NKz, (int)sizeof(R), NL_ROTATIONAL};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune_xz.find(key);
+    if (it != g_tune_xz.end()) {
+      d->xzC = it->second.first;
+      d->xzRC = it->second.second;
+      d->xzf = d->xzC > 0;
+      return CFGPU_OK;
+    }
+  }
+  const std::vector<XzShape> cand = xz_fused_candidates(gp, sizeof(R) == 8);
+  d->xzC = d->xzRC = 0;
+  if (!cand.empty()) {
+    d->xzC = cand[0].C;
+    d->xzRC = cand[0].RC;
+    if (d->autotune && cand.size() > 1) {
+      float best = 1e30f;
+      for (const XzShape& c : cand) {
+        const float t = time_ms<R>(d, [&]() {
+          return launch_xz_rot(gp, c.C, c.RC, (const cpx<R>*)d->W6, (cpx<R>*)d->F3, (const cpx<R>*)d->twxf,
+                               (const cpx<R>*)d->twzf, d->st, kNoDither);
+        });
+        if (t < best) {
+          best = t;
+          d->xzC = c.C;
+          d->xzRC = c.RC;
+        }
+      }
+      if (best >= 1e30f) d->xzC = d->xzRC = 0;  // no candidate launched: the three-kernel path
+    }
+  }
+  d->xzf = d->xzC > 0;
+  CK(cudaStreamSynchronize(d->st));
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune_xz[key] = {d->xzC, d->xzRC};
+  return CFGPU_OK;
+}
+
 int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flags, const double* Ub, const double* Wb,
                     const double* u0, int nb = 1) {
   d->fl = *flags;
@@ -1712,14 +1759,7 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
 
   // fused x/z pass for the rotational form (thread-block clusters over a y-plane)
   d->xzf = false;
-  if (rot && g_fused_xz.load() != 0 && xz_fused_supported(d->gp)) {
-    int dev = 0, nsm = 0;
-    cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) nsm = 152;
-    const int sh = fp64 ? xz_fused_shape<double>(d->gp, nsm, d->xzC, d->xzRC)
-                        : xz_fused_shape<float>(d->gp, nsm, d->xzC, d->xzRC);
-    d->xzf = sh == 0;
-  }
+  if (rot && g_fused_xz.load() != 0 && xz_fused_supported(d->gp)) CKS(fp64 ? tune_xz<double>(d) : tune_xz<float>(d));
 
   // schemes (DNS::DNS, dns.cpp:22-39)
   CKS(setup_scheme(d->main, f.timestepping, f.dt));
@@ -2768,6 +2808,7 @@ cfgpu_status cfgpu_set_autotune(int enable) {
   if (!enable) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_tune.clear();
+    g_tune_xz.clear();
   }
   return CFGPU_OK;
 }

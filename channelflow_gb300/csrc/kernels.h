@@ -3,6 +3,7 @@
 #pragma once
 
 #include <string>
+#include <vector>
 
 #include "fft.cuh"
 
@@ -72,17 +73,20 @@ template <typename R>
 cudaError_t launch_xfwd(const GridDev& g, const FftPlan& px, const cpx<R>* twx, const cpx<R>* Z, cpx<R>* F, int ncomp,
                         cudaStream_t st, int czc = 0, const Dither& dt = kNoDither);
 
-// Fused x/z pass of the rotational form (xz_fused.cu): one thread-block cluster of C CTAs per plane of gp,
-// RC x rows per z chunk; W = u, v, w, ox, oy, oz at the Gauss-Lobatto points ([c][plane][mode]), F = the
-// transformed product ([c][plane][mode]); twxf/twzf = full-circle tables exp(-2 pi i e/L) (version 0).
+// Fused x/z pass of the rotational form (xz_fused.cu, xz_fused.cuh): one thread-block cluster of C CTAs per
+// plane of gp, RC x rows per z chunk; W = u, v, w, ox, oy, oz at the Gauss-Lobatto points ([c][plane][mode]),
+// F = the transformed product ([c][plane][mode]); twxf/twzf = full-circle tables exp(-2 pi i e/L) (version 0).
+struct XzShape {
+  int C = 0, RC = 0;
+  double cost = 0.0;
+};
 bool xz_fused_supported(const GridDev& gp);
-template <typename R>
-size_t xz_fused_smem(const GridDev& gp, int C, int RC);
-template <typename R>
-int xz_fused_shape(const GridDev& gp, int nsm, int& C, int& RC);
-template <typename R>
-cudaError_t launch_xz_rot(const GridDev& gp, int C, int RC, const cpx<R>* W, cpx<R>* F, const cpx<R>* twxf,
-                          const cpx<R>* twzf, cudaStream_t st, const Dither& dt);
+size_t xz_fused_smem(const GridDev& gp, int C, int RC, bool fp64);
+std::vector<XzShape> xz_fused_candidates(const GridDev& gp, bool fp64);
+cudaError_t launch_xz_rot(const GridDev& gp, int C, int RC, const cpx<float>* W, cpx<float>* F,
+                          const cpx<float>* twxf, const cpx<float>* twzf, cudaStream_t st, const Dither& dt);
+cudaError_t launch_xz_rot(const GridDev& gp, int C, int RC, const cpx<double>* W, cpx<double>* F,
+                          const cpx<double>* twxf, const cpx<double>* twzf, cudaStream_t st, const Dither& dt);
 
 // field2vector / vector2field on field f of a batch of fstride fields in the solved-mode layout (one-field
 // grid g, dealiased): ord = solved-mode index of each vector block, blk = block of each mode; W: 2 Md Ny
