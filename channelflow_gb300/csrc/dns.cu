@@ -1498,7 +1498,19 @@ int tune_xz(cfgpu_dns d) {
           d->xzRC = c.RC;
         }
       }
-      if (best >= 1e30f) d->xzC = d->xzRC = 0;  // no candidate launched: the three-kernel path
+      // the three-kernel path (x inverse, z pass, x forward) with its own tuned shapes, if faster
+      const float t3 = time_ms<R>(d, [&]() {
+        cudaError_t e = launch_xinv<R>(gp, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)d->W6, (cpx<R>*)d->X6, 6,
+                                       d->st, d->xcols);
+        if (e == cudaSuccess)
+          e = launch_zphys<R>(gp, NL_ROTATIONAL, d->pz, (const cpx<R>*)d->twz, d->RP, (const cpx<R>*)d->X6,
+                              (cpx<R>*)d->Z3, d->st);
+        if (e == cudaSuccess)
+          e = launch_xfwd<R>(gp, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)d->Z3, (cpx<R>*)d->F3, 3, d->st,
+                             d->xcols);
+        return e;
+      });
+      if (best >= 1e30f || t3 < best) d->xzC = d->xzRC = 0;
     }
   }
   d->xzf = d->xzC > 0;

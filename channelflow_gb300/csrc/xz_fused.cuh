@@ -189,6 +189,16 @@ struct SeqZf {
   }
 };
 
+// Asynchronous global -> shared copy of one complex value (cp.async; 8 bytes FP32, 16 bytes FP64).
+template <typename R>
+__device__ __forceinline__ void cp_async_cpx(cpx<R>* dst_smem, const cpx<R>* src) {
+  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst_smem));
+  if constexpr (sizeof(cpx<R>) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+
 template <int N1>
 __device__ __forceinline__ int pos_perm(int k) {
   return (N1 + 1) * (k & 7) + (k >> 3);
@@ -253,28 +263,20 @@ __global__ void __launch_bounds__(XZ_THREADS, 2)
   const bool kok = kl < ks;
 
   // ---- phase 1: the owned kz columns of u, v, w, ox, oy, oz, inverse transform along x ------------------
-  {
+  // every solved value is copied asynchronously (all copies of the CTA in flight at once), the rest zeroed
+  if (kok) {
     const cpx<R>* Wp = W + (size_t)plane * Mf + kz0 + kl;
-    for (int u0 = warp * RW + sub; u0 < 6 * NX; u0 += 4 * NW * RW) {
-      cpx<R> v[4];
-      int dst[4];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int u = u0 + j * NW * RW;
-        v[j] = cmk<R>(0, 0);
-        dst[j] = -1;
-        if (u < 6 * NX && kok) {
-          const int c = u / NX, p = u - c * NX;
-          const int kx = p <= NX / 2 ? p : p - NX;
-          if (kx >= -Kx && kx <= Kx) v[j] = Wp[c * cstr + (size_t)(kx >= 0 ? kx : kx + NKx) * NKz];
-          dst[j] = (c * ks + kl) * PX + pos_nat<N1X>(p);
-        }
-      }
-#pragma unroll
-      for (int j = 0; j < 4; ++j)
-        if (dst[j] >= 0) X[dst[j]] = v[j];
+    for (int u = warp * RW + sub; u < 6 * NX; u += NW * RW) {
+      const int c = u / NX, p = u - c * NX;
+      const int kx = p <= NX / 2 ? p : p - NX;
+      cpx<R>* dst = X + (c * ks + kl) * PX + pos_nat<N1X>(p);
+      if (kx >= -Kx && kx <= Kx)
+        cp_async_cpx<R>(dst, Wp + c * cstr + (size_t)(kx >= 0 ? kx : kx + NKx) * NKz);
+      else
+        *dst = cmk<R>(0, 0);
     }
   }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
   __syncthreads();
   pass_s<R, N1X, +1>(X, 6 * ks, SeqLinear{PX}, twX, tid, XZ_THREADS);
   __syncthreads();
@@ -284,28 +286,47 @@ __global__ void __launch_bounds__(XZ_THREADS, 2)
   // ---- phase 2: z transforms and omega x u for the owned x rows, RC rows at a time ------------------------
   for (int xc = x0; xc < x1; xc += RC) {
     const int nr = min(RC, x1 - xc);
-    // gather: one warp per (row, pair) sequence, lanes over kz bins, columns read from their owners (DSMEM)
-    for (int rq = warp; rq < nr * 3; rq += NW) {
-      const int row = rq / 3, qd = rq - 3 * row;
-      const int px = pos_perm<N1X>(xc + row);
-      cpx<R>* zs = Zs + (size_t)rq * PZ;
+    // gather: one warp per (row, pair) sequence, two sequences at a time, lanes over kz bins, columns read
+    // from their owners (DSMEM); all loads of both sequences are issued before the stores
+    for (int rq0 = warp; rq0 < nr * 3; rq0 += 2 * NW) {
+      constexpr int KI = (NZ + 31) / 32;
+      cpx<R> val[2][KI];
 #pragma unroll
-      for (int k = lane; k < NZ; k += 32) {
-        cpx<R> v = cmk<R>(0, 0);
-        if (k < NKz || k > NZ - NKz) {
-          const int kk = k < NKz ? k : NZ - k;
-          const int ow = oks[kk];
-          const cpx<R>* Xr = cluster.map_shared_rank(X, own[kk]);
-          const int ia = (2 * qd * ow + col[kk]) * PX + px;
-          const cpx<R> A = Xr[ia], B = Xr[ia + ow * PX];
-          if (k == 0)
-            v = cmk<R>(A.x, B.x);
-          else if (k < NKz)
-            v = cmk<R>(A.x - B.y, A.y + B.x);  // A_k + i B_k
-          else
-            v = cmk<R>(A.x + B.y, -A.y + B.x);  // conj(A_k) + i conj(B_k)
+      for (int h = 0; h < 2; ++h) {
+        const int rq = rq0 + h * NW;
+        const int row = rq / 3, qd = rq - 3 * row;
+        const int px = pos_perm<N1X>(xc + row);
+#pragma unroll
+        for (int i = 0; i < KI; ++i) {
+          const int k = lane + 32 * i;
+          cpx<R> v = cmk<R>(0, 0);
+          if (rq < nr * 3 && k < NZ && (k < NKz || k > NZ - NKz)) {
+            const int kk = k < NKz ? k : NZ - k;
+            const int ow = oks[kk];
+            const cpx<R>* Xr = cluster.map_shared_rank(X, own[kk]);
+            const int ia = (2 * qd * ow + col[kk]) * PX + px;
+            const cpx<R> A = Xr[ia], B = Xr[ia + ow * PX];
+            if (k == 0)
+              v = cmk<R>(A.x, B.x);
+            else if (k < NKz)
+              v = cmk<R>(A.x - B.y, A.y + B.x);  // A_k + i B_k
+            else
+              v = cmk<R>(A.x + B.y, -A.y + B.x);  // conj(A_k) + i conj(B_k)
+          }
+          val[h][i] = v;
         }
-        zs[pos_nat<N1Z>(k)] = v;
+      }
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int rq = rq0 + h * NW;
+        if (rq < nr * 3) {
+          cpx<R>* zs = Zs + (size_t)rq * PZ;
+#pragma unroll
+          for (int i = 0; i < KI; ++i) {
+            const int k = lane + 32 * i;
+            if (k < NZ) zs[pos_nat<N1Z>(k)] = val[h][i];
+          }
+        }
       }
     }
     __syncthreads();
