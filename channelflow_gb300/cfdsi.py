@@ -12,12 +12,17 @@ and zrelative off).  Reference behaviour restated:
 The f^T(u) evaluations run on the GPU (cfgpu_ft, a DNS per call as cfDSI::f builds one, or the request
 server, which evaluates a whole set of them concurrently: eval_many / jacobian_many).  The Arnoldi step of
 GMRES is done in FP64 on the GPU (cfgpu_orthogonalize).  newton_gmres is a minimal host driver for these
-pieces (Newton with GMRES and backtracking), not the reference's hookstep algorithm.
+pieces (Newton with GMRES and backtracking); hookstep_search is nsolver's Newton-Krylov-hookstep algorithm
+(NewtonAlgorithm::solve with GMRES and NewtonAlgorithm::hookstep, nsolver/newtonalgorithm.cpp:334-789,
+895-1346), with the x phase shift of a travelling wave as an optional extra unknown (cfDSI with xrelative,
+cfdsi.cpp:555-615).
 """
 
 from __future__ import annotations
 
 import copy
+import math
+from dataclasses import dataclass
 
 import numpy as np
 
@@ -41,28 +46,52 @@ def orthogonalize(V: np.ndarray, w: np.ndarray):
 
 
 class CFDSI:
-    """G(x) = field2vector((sigma f^T(u) - u) [/ T]) with u = vector2field(x)."""
+    """G(x) = field2vector((sigma f^T(u) - u) [/ T]) with u = vector2field(x).
+
+    With xrelative, x carries the x phase shift ax of sigma as one more unknown after the field's reals
+    (cfDSI::extractVector, cfdsi.cpp:555-580) and G's last entry is zero (cfdsi.cpp:52-61)."""
 
     def __init__(self, grid: Grid, flags: DNSFlags, timestep: TimeStep, T: float, sigma: FieldSymmetry | None = None,
-                 Tnormalize: bool = True, precision: str = "fp64", server=None):
+                 Tnormalize: bool = True, precision: str = "fp64", server=None, xrelative: bool = False):
         self.grid, self.flags, self.timestep, self.T = grid, flags, timestep, float(T)
         self.sigma, self.Tnormalize, self.precision, self.server = sigma, Tnormalize, precision, server
+        self.xrelative = bool(xrelative)
         self.fcount = 0
 
-    def _G_from_fu(self, u: np.ndarray, fu: np.ndarray) -> np.ndarray:
-        if self.sigma is not None:
-            fu = apply(fu, self.grid, self.sigma)
+    def make_vector(self, u: np.ndarray, ax: float | None = None) -> np.ndarray:
+        """x from a field (and, with xrelative, the x shift; default: sigma's)."""
+        v = field2vector(np.ascontiguousarray(u), self.grid)
+        if not self.xrelative:
+            return v
+        if ax is None:
+            ax = self.sigma.ax if self.sigma is not None else 0.0
+        return np.concatenate([v, [float(ax)]])
+
+    def _split(self, x: np.ndarray):
+        """(u, sigma) of x (cfDSI::extractVector)."""
+        n = x.shape[0] - (1 if self.xrelative else 0)
+        u = vector2field(np.ascontiguousarray(x[:n]), self.grid)
+        sig = self.sigma
+        if self.xrelative:
+            b = sig if sig is not None else FieldSymmetry()
+            sig = FieldSymmetry(b.sx, b.sy, b.sz, float(x[n]), b.az, b.s)
+        return u, sig
+
+    def _G_from_fu(self, u: np.ndarray, fu: np.ndarray, sig) -> np.ndarray:
+        if sig is not None:
+            fu = apply(fu, self.grid, sig)
         Gu = fu - u
         if self.Tnormalize:
             Gu = Gu * (1.0 / self.T)
-        return field2vector(np.ascontiguousarray(Gu), self.grid)
+        g = field2vector(np.ascontiguousarray(Gu), self.grid)
+        return np.concatenate([g, [0.0]]) if self.xrelative else g
 
     def eval(self, x: np.ndarray) -> np.ndarray:
         """cfDSI::eval (cfdsi.cpp:52-61)."""
-        u = vector2field(x, self.grid)
+        u, sig = self._split(x)
         fu, _ = ft(u, self.grid, self.flags, copy.copy(self.timestep), self.T, precision=self.precision)
         self.fcount += 1
-        return self._G_from_fu(u, fu)
+        return self._G_from_fu(u, fu, sig)
 
     def eval_many(self, xs) -> list:
         """cfDSI::eval of every x in xs; with a server, all f^T evaluations are submitted at once and run
@@ -70,18 +99,30 @@ class CFDSI:
         if self.server is None:
             return [self.eval(x) for x in xs]
         from .server import DONE
-        us = [vector2field(x, self.grid) for x in xs]
-        ids = [self.server.submit_ft(self.grid, self.flags, copy.copy(self.timestep), self.T, u) for u in us]
+        parts = [self._split(x) for x in xs]
+        ids = [self.server.submit_ft(self.grid, self.flags, copy.copy(self.timestep), self.T, u) for u, _ in parts]
         self.server.run()
         out = []
-        for u, rid in zip(us, ids):
+        for (u, sig), rid in zip(parts, ids):
             st, fu, _ = self.server.poll(rid)
             if st != DONE:
                 raise RuntimeError("f^T(u) request %d did not finish" % rid)
             self.server.release(rid)
-            out.append(self._G_from_fu(u, fu))
+            out.append(self._G_from_fu(u, fu, sig))
         self.fcount += len(xs)
         return out
+
+    def xdiff(self, x: np.ndarray) -> np.ndarray:
+        """cfDSI::xdiff (cfdsi.cpp:606-615): field2vector of du/dx, normalised; zero in the shift entry."""
+        n = x.shape[0] - (1 if self.xrelative else 0)
+        u = vector2field(np.ascontiguousarray(x[:n]), self.grid)
+        Nx = self.grid.Nx
+        kx = np.array([m if m <= Nx // 2 else m - Nx for m in range(Nx)], dtype=float)
+        kx[Nx // 2] = 0.0  # the Nyquist mode has no derivative
+        du = u * (2j * math.pi * kx / self.grid.Lx)[None, None, :, None]
+        d = field2vector(np.ascontiguousarray(du), self.grid)
+        d = d / np.linalg.norm(d)
+        return np.concatenate([d, [0.0]]) if self.xrelative else d
 
     @staticmethod
     def _eps(dx, epsDx):
@@ -139,3 +180,289 @@ def newton_gmres(dsi: CFDSI, x0: np.ndarray, tol: float = 1e-12, maxit: int = 10
         x, Gx = xn, Gn
         hist.append(float(np.linalg.norm(Gx)))
     return x, Gx, hist
+
+
+# ---------------------------------------------------------------------------------------------------------------
+# Newton-Krylov-hookstep (nsolver)
+# ---------------------------------------------------------------------------------------------------------------
+
+@dataclass
+class NewtonSearchFlags:
+    """The options of nsolver's NewtonSearchFlags with their defaults (nsolver/newtonalgorithm.cpp:62-120)."""
+    epsSearch: float = 1e-13      # stop when L2Norm(G(x)) < epsSearch
+    epsKrylov: float = 1e-14      # minimum norm of a new Krylov vector (GMRES benign breakdown)
+    epsDx: float = 1e-7           # relative size of dx in the finite-difference Jacobian
+    epsSolver: float = 1e-3       # GMRES stops when |Ax - b|/|b| < epsSolver
+    epsSolverF: float = 0.05      # accept the last GMRES iterate below this residual
+    centdiff: bool = False        # centred differences for the Jacobian
+    Nnewton: int = 20
+    Nsolver: int = 500            # GMRES iterations per Newton step
+    Nhook: int = 20               # iterations of the search for the hookstep's mu
+    delta: float = 0.01           # initial trust-region radius
+    deltaMin: float = 1e-12
+    deltaMax: float = 0.1
+    deltaFuzz: float = 1e-6
+    lambdaMin: float = 0.2
+    lambdaMax: float = 1.5
+    lambdaRequiredReduction: float = 0.5
+    improvReq: float = 1e-3
+    improvOk: float = 0.10
+    improvGood: float = 0.75
+    improvAcc: float = 0.10
+
+
+def _adjust_delta(delta, rate, dmin, dmax):
+    """adjustDelta (cfbasics/cfbasics.h:964-988)."""
+    if delta == dmin and delta * rate < dmin:
+        return dmin
+    delta *= rate
+    if delta <= dmin:
+        delta = 0.5 * dmin
+    if delta > dmax:
+        delta = dmax
+    return delta
+
+
+def _adjust_lambda(lam, lmin, lmax):
+    """adjustLambda (cfbasics/cfbasics.h:990-999).  The reference's second test repeats lam < lmin, so lam is
+    never capped at lmax; kept as it is."""
+    if lam < lmin:
+        lam = lmin
+    return lam
+
+
+class GMRES:
+    """nsolver's GMRES (nsolver/gmres.cpp:19-100): Arnoldi on Q with the (n+1) x n Hessenberg H, least-squares
+    solution in the Krylov space; the Gram-Schmidt step is `ortho` (by default the FP64 GPU step)."""
+
+    def __init__(self, b: np.ndarray, nmax: int, min_condition: float, ortho=None, rng=None):
+        self.M, self.nmax, self.cond = b.shape[0], int(nmax), float(min_condition)
+        self.bnorm = float(np.linalg.norm(b))
+        self.Q = [b / self.bnorm]
+        self.H = np.zeros((self.nmax + 1, self.nmax))
+        self.n = 0
+        self.residual = 1.0
+        self.x = np.zeros(self.M)
+        self.ortho = ortho or orthogonalize
+        self.rng = rng or np.random.default_rng(0)
+
+    def test_vector(self) -> np.ndarray:
+        return self.Q[self.n]
+
+    def iterate(self, Aq: np.ndarray):
+        n = self.n
+        V = np.array(self.Q)
+        w, h = self.ortho(V, Aq)
+        retries = 0
+        while abs(h[-1]) < self.cond and retries < 10:   # benign breakdown: a random vector instead
+            retries += 1
+            w, h2 = self.ortho(V, self.rng.standard_normal(self.M))
+            h = np.concatenate([h[:-1], [h2[-1]]])
+        self.H[: n + 1, n] = h[:-1]
+        self.H[n + 1, n] = h[-1]
+        self.Q.append(w)
+        Hn = self.H[: n + 2, : n + 1]
+        bk = np.zeros(n + 2)
+        bk[0] = self.bnorm
+        y = np.linalg.lstsq(Hn, bk, rcond=None)[0]
+        self.residual = float(np.linalg.norm(Hn @ y - bk) / self.bnorm)
+        self.x = np.array(self.Q[: n + 1]).T @ y
+        self.n = n + 1
+
+
+def _numpy_ortho(V: np.ndarray, w: np.ndarray):
+    """Gram-Schmidt twice on the host (the same step as cfgpu_orthogonalize), for host-only use."""
+    w = np.array(w, dtype=np.float64, copy=True)
+    k = V.shape[0] if V.size else 0
+    h = np.zeros(k + 1)
+    for _ in range(2):
+        if k:
+            p = V @ w
+            w -= V.T @ p
+            h[:k] += p
+    h[k] = float(np.linalg.norm(w))
+    if h[k] > 0:
+        w /= h[k]
+    return w, h
+
+
+def hookstep_search(dsi, x0: np.ndarray, flags: NewtonSearchFlags | None = None, ortho=None, log=None):
+    """Newton-Krylov-hookstep search for G(x) = 0: NewtonAlgorithm::solve with the GMRES solver and hookstep
+    optimization (nsolver/newtonalgorithm.cpp:334-789, 895-1346).  dsi provides eval(x), jacobian(x, dx, Gx,
+    epsDx, centdiff) and, when dsi.xrelative, xdiff(x) (the phase condition: the Krylov rows of the shift
+    unknown are (dx, du0/dx), newtonalgorithm.cpp:540-550, 612-620).
+
+    Returns (x, G(x), info) with info = {"gx": [L2Norm(G) per Newton step], "fcount": f evaluations,
+    "converged": bool, "reason": why the search stopped, "gmres": [Krylov dimension per step],
+    "delta": [trust radius per step]}.
+    """
+    f = flags or NewtonSearchFlags()
+    say = log or (lambda *a: None)
+    xrel = bool(getattr(dsi, "xrelative", False))
+    ncut = 1 if xrel else 0  # the field part of x: norms and trust region exclude the shift unknown
+
+    def fnorm(v):
+        return float(np.linalg.norm(v[: v.shape[0] - ncut] if ncut else v))
+
+    x = np.array(x0, dtype=np.float64, copy=True)
+    E = dsi.xdiff(x0) if xrel else None
+    Gx = dsi.eval(x)
+    nunk = x.shape[0]
+    nsolver = min(nunk, f.Nsolver)
+    delta = f.delta
+    info = {"gx": [], "fcount": 1, "converged": False, "reason": "", "gmres": [], "delta": []}
+
+    def jac(xx, dx, G, cd):
+        info["fcount"] += 2 if cd else 1
+        return dsi.jacobian(xx, dx, G, f.epsDx, cd)
+
+    def ev(xx):
+        info["fcount"] += 1
+        return dsi.eval(xx)
+
+    for nnewton in range(f.Nnewton + 1):
+        rx = 0.5 * float(Gx @ Gx)
+        gx = float(np.linalg.norm(Gx))
+        info["gx"].append(gx)
+        info["delta"].append(delta)
+        say("Newton %d: L2Norm(G(x)) = %.6e, delta = %.3e" % (nnewton, gx, delta))
+        if gx < f.epsSearch:
+            info["converged"], info["reason"] = True, "L2Norm(G(x)) < epsSearch"
+            return x, Gx, info
+        if nnewton == f.Nnewton:
+            info["reason"] = "maximum number of Newton steps"
+            return x, Gx, info
+        # GMRES for DG(x) dx = -G(x)
+        b = -Gx
+        gm = GMRES(b, nsolver, f.epsKrylov, ortho=ortho)
+        dxN = None
+        for n in range(nsolver):
+            q = gm.test_vector()
+            Lq = jac(x, q, Gx, f.centdiff)
+            if xrel:
+                Lq = Lq.copy()
+                Lq[-1] = float(q @ E)
+            gm.iterate(Lq)
+            if gm.residual < f.epsSolver or (n == nsolver - 1 and gm.residual < f.epsSolverF):
+                dxN = gm.x
+                break
+        info["gmres"].append(gm.n)
+        if dxN is None:
+            info["reason"] = "GMRES failed to converge"
+            return x, Gx, info
+        # hookstep (newtonalgorithm.cpp:895-1346)
+        Nk = gm.n
+        Hn = gm.H[: Nk + 1, :Nk]
+        Q = np.array(gm.Q[: Nk + 1]).T  # M x (Nk+1)
+        U, D, Vt = np.linalg.svd(Hn, full_matrices=False)
+        bh = U.T @ (Q.T @ b)
+        have_backup = False
+        backup = None
+        delta_max_local = f.deltaMax
+        while True:
+            dxn = fnorm(dxN)
+            if dxn <= delta:
+                newton_inside = True
+                dxH = dxN
+            else:
+                newton_inside = False
+                mu = 0.0
+                found = False
+                for hs in range(f.Nhook):
+                    dxHmu = bh / (D + mu)
+                    nd = float(np.linalg.norm(dxHmu))
+                    phi = nd * nd - delta * delta
+                    if nd < delta or ((1 - f.deltaFuzz) * delta < nd < (1 + f.deltaFuzz) * delta):
+                        found = True
+                        break
+                    if hs < f.Nhook - 1:
+                        dphi = -2.0 * float(np.sum(bh * bh / (D + mu) ** 3))
+                        mu -= (nd / delta) * (phi / dphi)
+                if not found:
+                    info["reason"] = "no hookstep of radius delta"
+                    return x, Gx, info
+                dxH = Q[:, :Nk] @ (Vt.T @ dxHmu)
+            GxH = ev(x + dxH)
+            rH = 0.5 * float(GxH @ GxH)
+            d_rH = rH - rx
+            DG = jac(x, dxH, Gx, f.centdiff)
+            d_rL = float(Gx @ DG)
+            if rx + d_rL >= rx:
+                if f.centdiff:
+                    info["reason"] = "local linear model of the residual is increasing"
+                    return x, Gx, info
+                DG = jac(x, dxH, Gx, True)
+                d_rL = float(Gx @ DG)
+                if rx + d_rL >= rx:
+                    info["reason"] = "local linear model of the residual is increasing (centred differences)"
+                    return x, Gx, info
+            rQ = 0.5 * float(np.linalg.norm(DG + Gx) ** 2)
+            d_rQ = rQ - rx
+            dxHnorm = fnorm(dxH)
+            drdx = d_rL / dxHnorm
+            lam = -0.5 * drdx * dxHnorm / (rH - rx - drdx * dxHnorm)
+            req = f.improvReq * drdx * dxHnorm
+            ok = f.improvOk * d_rQ
+            good = f.improvGood * d_rQ
+            acc = abs(f.improvAcc * d_rQ)
+            if d_rH > req:
+                imp = "unacceptable"
+            elif d_rH > ok:
+                imp = "poor"
+            elif d_rH < ok and d_rH > good:
+                imp = "ok"
+            else:
+                imp = "good"
+                if d_rQ - acc <= d_rH <= d_rQ + acc:
+                    imp = "accurate"
+                elif d_rH < d_rL:
+                    imp = "negacurve"
+            recompute = False
+            if imp == "unacceptable":
+                if have_backup:
+                    dxH, GxH, rH, dxHnorm, delta = backup
+                else:
+                    delta_max_local = delta
+                    lam = _adjust_lambda(lam, f.lambdaMin, f.lambdaRequiredReduction)
+                    delta = _adjust_delta(delta, lam, f.deltaMin, f.deltaMax)
+                    if delta < f.deltaMin:
+                        delta = f.deltaMin
+                        info["reason"] = "trust region below deltaMin"
+                        return x, Gx, info
+                    if delta > dxHnorm:
+                        delta = 0.5 * dxHnorm
+                        if delta < f.deltaMin:
+                            info["reason"] = "trust region below deltaMin"
+                            return x, Gx, info
+                    recompute = True
+            elif imp in ("negacurve", "accurate") and not (have_backup and backup[2] < rH) and not newton_inside \
+                    and not delta >= f.deltaMax:
+                new_delta = _adjust_delta(delta, f.lambdaMax, f.deltaMin, f.deltaMax)
+                if new_delta < delta_max_local:
+                    have_backup = True
+                    backup = (dxH, GxH, rH, dxHnorm, delta)
+                    recompute = True
+                    delta = new_delta
+                else:
+                    delta = delta_max_local
+            else:
+                if have_backup and backup[2] < rH:
+                    dxH, GxH, rH, dxHnorm, delta = backup
+                elif have_backup:
+                    pass
+                elif imp == "poor":
+                    lam = _adjust_lambda(lam, f.lambdaMin, 1.0)
+                    delta = _adjust_delta(delta, lam, f.deltaMin, f.deltaMax)
+                    if delta < f.deltaMin:
+                        info["reason"] = "trust region below deltaMin"
+                        return x, Gx, info
+                elif imp == "ok" or newton_inside or delta >= f.deltaMax:
+                    pass
+                else:
+                    lam = _adjust_lambda(lam, 1.0, f.lambdaMax)
+                    delta = _adjust_delta(delta, lam, f.deltaMin, f.deltaMax)
+            if not recompute:
+                break
+        x = x + dxH
+        Gx = GxH
+    return x, Gx, info

@@ -243,6 +243,13 @@ def main(ref=None):
         for k in ("X", "Y", "Z"):
             out[tag + "_coord_" + k] = data[k]
     np.savez_compressed(os.path.join(here, "timeintegration.npz"), **out)
+    # the equilibrium (travelling wave) of tests/findsolnTest.cpp and its symmetry (x shift) sigmabest.asc
+    attrs, data = read_nc(os.path.join(dd, "eq.nc"))
+    eq = {"eq": np.stack([data["Velocity_X"], data["Velocity_Y"], data["Velocity_Z"]])}
+    for k in ("Nx", "Ny", "Nz", "Lx", "Lz", "a", "b"):
+        eq["eq_" + k] = np.asarray(attrs[k])
+    eq["sigmabest"] = np.loadtxt(os.path.join(dd, "sigmabest.asc"))
+    np.savez_compressed(os.path.join(here, "eq.npz"), **eq)
     ueig, uhead = read_asc_basis(os.path.join(dd, "os_ueig10_65.asc"))
     peig, phead = read_asc_basis(os.path.join(dd, "os_peig10_65.asc"))
     om = np.loadtxt(os.path.join(dd, "os_omega10_65.cmplx"))
