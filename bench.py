@@ -218,7 +218,7 @@ def run_gpu(args, rank, world):
         dns.set_profiling(False)
         results[prec] = dict(ms=ms, K=K, launches=launches, clocks=cs.summary(), nl_ms=nl_ms, nl_n=nl_n,
                              tau_ms=tau_ms, tau_n=tau_n, Md=dns.num_modes(), bytes=dns.device_bytes())
-        if prec == "mixed":
+        if True:
             # end-to-end through the public API: host buffers in, host buffers out, every step
             Ke = max(3, min(args.steps, 50))
             ue, qe = u0.copy(), q0.copy()
@@ -230,7 +230,8 @@ def run_gpu(args, rank, world):
                 dns_e.advance(ue, qe, 1)
             te = max_over_ranks(time.perf_counter() - t0)
             Md = dns_e.num_modes()
-            results["e2e"] = dict(s=te, K=Ke, h2d=4 * NY * Md * 16, d2h=4 * NY * Md * 16)
+            results["e2e" if prec == "mixed" else "e2e_fp64"] = dict(s=te, K=Ke, h2d=4 * NY * Md * 16,
+                                                                       d2h=4 * NY * Md * 16)
             dns_e.close()
         dns.close()
     acc = None
@@ -461,6 +462,103 @@ def run_ensemble(args):
     return out
 
 
+def run_config0(args):
+    """The 32x33x32 plane Couette configuration (Re 400, box 2pi/1.14 x 2pi/2.5, SBDF3 + SMRK2 start-up,
+    dt = 0.02, seeded perturbation of L2 norm 0.1): steps/s of both precisions over 500 steps (T = 10), fields
+    resident, CUDA events on the library's stream; and end to end through cfgpu_dns_advance with host buffers."""
+    from channelflow_gb300 import DNS, DNSFlags, Grid
+    from channelflow_gb300.fields import random_divfree_field
+    lx, lz = 2 * math.pi / 1.14, 2 * math.pi / 2.5
+    g = Grid(32, 33, 32, lx, lz)
+    fl = DNSFlags(nu=1 / 400, dt=0.02, baseflow=LaminarBase, ulowerwall=-1.0, uupperwall=1.0)
+    u0 = random_divfree_field(32, 33, 32, lx, lz, seed=1, norm=0.1)
+    q0 = np.zeros((1,) + u0.shape[1:], dtype=np.complex128)
+    out = {"workload": "plane Couette 32x33x32 Re=400 SBDF3, dt=0.02, 500 steps (T=10), perturbation L2 0.1"}
+    for prec in ("mixed", "fp64"):
+        u, q = u0.copy(), q0.copy()
+        d = DNS(u, g, fl, precision=prec)
+        d.set_fields(u, q)
+        d.advance_resident(5)
+        ms = d.advance_timed(500)
+        d.close()
+        ue, qe = u0.copy(), q0.copy()
+        de = DNS(ue, g, fl, precision=prec)
+        de.advance(ue, qe, 5)
+        t0 = time.perf_counter()
+        for _ in range(100):
+            de.advance(ue, qe, 1)
+        te = time.perf_counter() - t0
+        de.close()
+        out[prec] = {"steps_per_s": 500 / (ms / 1e3), "ms_per_step": ms / 500,
+                     "e2e_steps_per_s": 100 / te}
+    return out
+
+
+def run_newton(args):
+    """Newton-Krylov-hookstep searches (nsolver's algorithm on the host, every f^T(u) on the GPU).
+
+    search: the equilibrium-search configuration: plane Couette Re = 400, 32x35x32, box 2pi/1.14 x 2pi/2.5,
+    initial guess a seeded perturbation symmetrised with the shift-reflect symmetry (u + sigma u)/2,
+    sigma = (1, 1, -1, 1/2, 0), rescaled to L2 norm 0.2; G(u) = (f^T(u) - u)/T with T = 10, fixed dt = 0.02
+    (500 steps per f^T); GMRES dimension <= 100, hookstep; f^T in mixed precision for the search, then Newton
+    steps with FP64 f^T from where the search stopped.
+    travelling_wave: the reference's equilibrium data (tests/data/eq, a travelling wave, 24x33x24) times
+    1.001 with its x shift times 1.001, searched with the shift as an unknown, FP64 f^T: the FP64 residual
+    a converged search reaches."""
+    from channelflow_gb300 import DNSFlags, Grid
+    from channelflow_gb300.cfdsi import CFDSI, NewtonSearchFlags, hookstep_search
+    from channelflow_gb300.dsi import TimeStep
+    from channelflow_gb300.fields import l2norm, random_divfree_field
+    from channelflow_gb300.symmetry import FieldSymmetry, apply
+    lx, lz = 2 * math.pi / 1.14, 2 * math.pi / 2.5
+    fl = DNSFlags(nu=1 / 400, dt=0.02, baseflow=LaminarBase, ulowerwall=-1.0, uupperwall=1.0)
+    ts = TimeStep(dt=0.02, dtmin=0.02, dtmax=0.02, dT=10.0, CFLmin=0.0, CFLmax=1.0, variable=False)
+    out = {}
+    # --- equilibrium search (32x35x32) --------------------------------------------------------------------
+    g = Grid(32, 35, 32, lx, lz)
+    u = random_divfree_field(32, 35, 32, lx, lz, seed=3, norm=0.2)
+    u = apply(u, g, FieldSymmetry(1, 1, -1, 0.5, 0.0, 1), project=True)
+    u = np.ascontiguousarray(u * (0.2 / l2norm(u, 32, 32)))
+    res = {}
+    x = None
+    for prec, nn in (("mixed", args.newton_steps), ("fp64", args.newton_polish_steps)):
+        dsi = CFDSI(g, fl, ts, 10.0, precision=prec)
+        x0 = dsi.make_vector(u) if x is None else x
+        flags = NewtonSearchFlags(Nnewton=nn, Nsolver=100, epsSolver=1e-3 if prec == "mixed" else 1e-8)
+        t0 = time.perf_counter()
+        x, Gx, info = hookstep_search(dsi, x0, flags)
+        secs = time.perf_counter() - t0
+        res[prec] = {"newton_steps": len(info["gx"]) - 1, "gx": [float("%.4g" % v) for v in info["gx"]],
+                     "gmres_dims": info["gmres"], "f_evaluations": dsi.fcount, "seconds": secs,
+                     "s_per_newton_step": secs / max(1, len(info["gx"]) - 1),
+                     "ms_per_f_evaluation": 1e3 * secs / max(1, dsi.fcount), "stop": info["reason"],
+                     "converged": info["converged"]}
+    uf = CFDSI(g, fl, ts, 10.0)._split(x)[0]
+    res["L2Norm_u_final"] = l2norm(uf, 32, 32)
+    res["workload"] = ("plane Couette 32x35x32 Re=400, shift-reflect symmetric seeded guess L2 0.2, f^T T=10 "
+                       "dt=0.02 SBDF3, GMRES<=100, hookstep; mixed-precision search then FP64 Newton steps")
+    out["search"] = res
+    # --- travelling wave from the reference's data (FP64) ---------------------------------------------------
+    z = np.load(os.path.join(ROOT, "tests", "golden", "eq.npz"))
+    from channelflow_gb300.fields import io_to_spectral
+    ueq = io_to_spectral(z["eq"], int(z["eq_Nx"]), int(z["eq_Nz"]))
+    sb = z["sigmabest"]
+    g2 = Grid(int(z["eq_Nx"]), int(z["eq_Ny"]), int(z["eq_Nz"]), float(z["eq_Lx"]), float(z["eq_Lz"]))
+    sig = FieldSymmetry(int(sb[1]), int(sb[2]), int(sb[3]), float(sb[4]) * 1.001, float(sb[5]), int(sb[0]))
+    dsi = CFDSI(g2, fl, ts, 10.0, sigma=sig, xrelative=True)
+    t0 = time.perf_counter()
+    x, Gx, info = hookstep_search(dsi, dsi.make_vector(np.ascontiguousarray(ueq * 1.001)),
+                                  NewtonSearchFlags(epsSearch=1e-13, Nnewton=8, epsSolver=1e-9, Nsolver=120))
+    secs = time.perf_counter() - t0
+    out["travelling_wave"] = {"gx": [float("%.4g" % v) for v in info["gx"]], "converged": info["converged"],
+                              "final_residual_fp64": float(np.linalg.norm(Gx)), "ax": float(x[-1]),
+                              "f_evaluations": dsi.fcount, "seconds": secs,
+                              "ms_per_f_evaluation": 1e3 * secs / max(1, dsi.fcount),
+                              "workload": "reference tests/data/eq travelling wave 24x33x24 x1.001, x shift "
+                                          "unknown, T=10 dt=0.02, FP64"}
+    return out
+
+
 def cpu_sample(nsteps):
     """The oracle (reference algorithm restated in NumPy) on the same workload: nsteps CNAB2 steps."""
     from oracle import cf_oracle as O
@@ -475,7 +573,7 @@ def cpu_sample(nsteps):
     for _ in range(nsteps):
         u, q = dns.advance(u, q, 1)
     dt = time.perf_counter() - t0
-    return nsteps / dt, dt
+    return nsteps / dt, dt, O.WORKERS
 
 
 def main():
@@ -485,7 +583,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--accuracy-steps", type=int, default=1000, help="steps for the mixed-vs-FP64 error (T=10)")
-    ap.add_argument("--cpu-steps", type=int, default=3, help="oracle steps in the cpu_baseline sample")
+    ap.add_argument("--cpu-steps", type=int, default=12, help="oracle steps in the cpu_baseline sample")
     ap.add_argument("--grid", default=None, help="Nx,Ny,Nz override for small profiling cases (not a bench line)")
     ap.add_argument("--serve-requests", type=int, default=48, help="requests in the serving stream (0: skip)")
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[4.0, 16.0, 0.0],
@@ -496,6 +594,10 @@ def main():
     ap.add_argument("--ensemble-fields", type=int, default=64, help="ensemble block fields (0: skip)")
     ap.add_argument("--ensemble-steps", type=int, default=200)
     ap.add_argument("--ensemble-serial-fields", type=int, default=8)
+    ap.add_argument("--config0", type=int, default=1, help="32x33x32 Couette block (0: skip)")
+    ap.add_argument("--newton-steps", type=int, default=3, help="mixed-precision Newton steps of the search "
+                                                                 "block (0: skip the Newton block)")
+    ap.add_argument("--newton-polish-steps", type=int, default=2)
     args = ap.parse_args()
     if args.grid:
         global NX, NY, NZ
@@ -509,14 +611,15 @@ def main():
         warm = max(0, min(args.warmup, 3))
         from oracle import cf_oracle as O  # noqa: F401
         n = max(1, min(args.steps, 20))
-        sps, secs = cpu_sample(n)
+        sps, secs, cores = cpu_sample(n)
         line = {"metric": METRIC, "impl": "reference", "value": sps, "unit": "steps/s", "n_gpus": args.gpus,
                 "steps": n, "warmup": warm, "ms_per_step": 1000.0 / sps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": {"workload": WORKLOAD, "grid": [NX, NY, NZ]},
-                "cpu_baseline": {"value": sps, "unit": "steps/s", "cores": 1, "kind": "port",
+                "cpu_baseline": {"value": sps, "unit": "steps/s", "cores": cores, "kind": "port",
                                  "sample": "%d full CNAB2 steps of the 128x97x128 field after 1 SMRK2 start-up "
-                                           "step (NumPy restatement of the reference, one core)" % n},
+                                           "step (NumPy/SciPy restatement of the reference, FFTs and DCTs on "
+                                           "%d host threads)" % (n, cores)},
                 "e2e": {"value": sps, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -524,6 +627,8 @@ def main():
     res, acc, hbm, peak_kind = run_gpu(args, rank, world)
     serve = run_serve(args) if (args.serve_requests > 0 and rank == 0) else None
     ens = run_ensemble(args) if (args.ensemble_fields > 0 and rank == 0) else None
+    cfg0 = run_config0(args) if (args.config0 and rank == 0) else None
+    newton = run_newton(args) if (args.newton_steps > 0 and rank == 0) else None
     if rank != 0:
         return
     m = res["mixed"]
@@ -541,10 +646,11 @@ def main():
     e = res["e2e"]
     cpu = None
     if world == 1 and args.cpu_steps > 0:
-        cps, csecs = cpu_sample(args.cpu_steps)
-        cpu = {"value": cps, "unit": "steps/s", "cores": 1, "kind": "port",
+        cps, csecs, cores = cpu_sample(args.cpu_steps)
+        cpu = {"value": cps, "unit": "steps/s", "cores": cores, "kind": "port",
                "sample": "%d full CNAB2 steps of the 128x97x128 field (after 1 untimed SMRK2 start-up step), "
-                         "NumPy restatement of the reference on one host core, %.1f s" % (args.cpu_steps, csecs)}
+                         "NumPy/SciPy restatement of the reference, FFTs and DCTs on %d host threads of %d, "
+                         "%.1f s" % (args.cpu_steps, cores, os.cpu_count() or 1, csecs)}
     bnl64, btau64 = bytes_per_step(Md, "fp64")
     ftr, ftau = flops_per_step(Md)
     pk64, cyc64 = fp64_peak()
@@ -584,12 +690,15 @@ def main():
         "accuracy": acc,
         "e2e": {"value": world * e["K"] / e["s"], "unit": "steps/s", "h2d_bytes_per_step": e["h2d"],
                 "d2h_bytes_per_step": e["d2h"],
-                "path": "cfgpu_dns_advance(u, q, 1) per step with host FlowField buffers"},
+                "path": "cfgpu_dns_advance(u, q, 1) per step with host FlowField buffers",
+                "fp64": world * res["e2e_fp64"]["K"] / res["e2e_fp64"]["s"]},
         "gpu_launches": m["launches"],
         "clocks": m["clocks"],
         "cpu_baseline": cpu,
         "serve": serve,
         "ensemble": ens,
+        "config0": cfg0,
+        "newton": newton,
     }
     print(json.dumps(line))
 

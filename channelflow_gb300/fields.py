@@ -126,3 +126,20 @@ def random_divfree_field(Nx: int, Ny: int, Nz: int, Lx: float, Lz: float, seed: 
                 if kz == 0:
                     u[:, :, (-k) % Nx, 0] = np.conj(u[:, :, mx, 0])
     return u * (norm / l2norm(u, Nx, Nz))
+
+
+def io_to_spectral(phys_io: np.ndarray, Nx: int, Nz: int) -> np.ndarray:
+    """Spectral field (Nd, Ny, Nx, Nz//2+1) from physical data on a file's unpadded I/O grid.
+
+    The role of FlowField::readNetCDF followed by the padded-mode fill (channelflow/flowfield.cpp:3605-3826):
+    phys_io is [i][nz][ny][nx] on the 2(Nx/3) x Ny x 2(Nz/3) grid; its xz Fourier coefficients (scaled by
+    1/(nx nz)) fill the kx >= 0 and kx < 0 blocks of the Nx x Nz spectral grid, the remaining modes are zero,
+    and the values at the Gauss-Lobatto points become Chebyshev coefficients."""
+    Nd, Nz_io, Ny, Nx_io = phys_io.shape
+    p = np.transpose(phys_io, (0, 2, 3, 1))  # [i][ny][nx][nz]
+    c = np.fft.rfft2(p, axes=(2, 3)) * (1.0 / (Nx_io * Nz_io))
+    out = np.zeros((Nd, Ny, Nx, Nz // 2 + 1), dtype=np.complex128)
+    h = Nx_io // 2 + 1
+    out[:, :, :h, : Nz_io // 2 + 1] = c[:, :, :h, :]
+    out[:, :, h + (Nx - Nx_io): Nx, : Nz_io // 2 + 1] = c[:, :, h:, :]
+    return np.ascontiguousarray(chebyfft(out, axis=1))

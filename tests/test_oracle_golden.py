@@ -156,3 +156,16 @@ def test_constraint_norms_of_seeded_field():
     bad = u.copy()
     bad[1, 1, 1, 1] += 1e-3
     assert O.bc_norm(bad, g) > 1e-4 and O.wall_slope_norm(bad, g) > 1e-4
+
+
+def test_io_grid_loader_matches_oracle():
+    """The package's reader of I/O-grid physical data (the role of FlowField::readNetCDF and the padded-mode
+    fill, flowfield.cpp:3605-3826) equals the oracle's on the reference's own files."""
+    from channelflow_gb300.fields import io_to_spectral
+    z = np.load(os.path.join(GOLD, "timeintegration.npz"))
+    assert np.array_equal(io_to_spectral(z["uinit"], 48, 48), O.load_io_field(z["uinit"], 48, 48))
+    e = np.load(os.path.join(GOLD, "eq.npz"))
+    u = io_to_spectral(e["eq"], 24, 24)
+    assert np.array_equal(u, O.load_io_field(e["eq"], 24, 24))
+    g = O.Grid(24, 33, 24, float(e["eq_Lx"]), float(e["eq_Lz"]))
+    assert O.divergence_norm(u, g) < 1e-13 and O.bc_norm(u, g) < 1e-13
