@@ -658,12 +658,7 @@ struct cfgpu_dns_s {
   };
   std::vector<StepGraph> graphs;
   bool graph_warm = false;  // one eager main step ran since the graphs were last dropped
-  // second stream: the right-hand side of the tau solve runs there while the nonlinear pass runs on st
-  cudaStream_t st2 = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-  bool overlap = true;
-  // phase profiling: event pairs recorded around NL passes (0) and tau solves (1; 2 = the right-hand side of
-  // a split solve, counted in the tau time but not as a separate solve)
+  // phase profiling: event pairs recorded around NL passes (0) and tau solves (1)
   bool profiling = false;
   std::vector<cudaEvent_t> ev_pool;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_used;
@@ -931,66 +926,6 @@ int tau_solve(cfgpu_dns d, const SolveParams& sp, const SolvePtrs& p, const TauT
   return CFGPU_OK;
 }
 
-// The nonlinear term N_j of U into Nout, then the tau solve.  Where the solve has its right-hand side in a
-// kernel of its own, that kernel runs first on the second stream without the N_j terms (zero weight, and a
-// history buffer that nothing writes meanwhile in N_j's place) while the nonlinear pass runs on the main
-// stream; the N_j terms are added after both (k_rhs_addN), then the solve proper.  Same arithmetic as the
-// combined right-hand side except the order of the additions (FP64 round-off).  Used for multistep steps
-// of order > 1 and CNAB substeps; with profiling on the parts run in order on the main stream.
-int nl_then_solve(cfgpu_dns d, const double* U, void* Nout, int which, const SolveParams& sp, const SolvePtrs& p,
-                  const TauTable& tt) {
-  const bool split = d->overlap && tau_solve_launches(d->N) == 3 &&
-                     (sp.kind == 1 || (sp.kind == 0 && sp.order > 1));
-  if (!split) {
-    CKS(nonlinear(d, U, Nout, which));
-    return tau_solve(d, sp, p, tt);
-  }
-  SolveParams sl = sp;
-  SolvePtrs pl = p;
-  double coef;
-  if (sp.kind == 1) {
-    coef = -sp.g_b;
-    sl.g_b = 0.0;
-  } else {
-    coef = sp.b[0];
-    sl.b[0] = 0.0;
-  }
-  pl.nin[0] = p.nin[1];
-  const bool fp64 = d->precision == CFGPU_FP64;
-  const bool concurrent = !d->profiling;
-  if (concurrent && !d->st2) {
-    int prio = 0;
-    CK(cudaStreamGetPriority(d->st, &prio));
-    CK(cudaStreamCreateWithPriority(&d->st2, cudaStreamNonBlocking, prio));
-    CK(cudaEventCreateWithFlags(&d->ev_fork, cudaEventDisableTiming));
-    CK(cudaEventCreateWithFlags(&d->ev_join, cudaEventDisableTiming));
-  }
-  cudaStream_t sr = concurrent ? d->st2 : d->st;
-  if (concurrent) {
-    CK(cudaEventRecord(d->ev_fork, d->st));
-    CK(cudaStreamWaitEvent(d->st2, d->ev_fork, 0));
-  }
-  {
-    PhaseScope ps(d, 2);
-    CK(fp64 ? launch_tau_rhs<double>(d->gm, d->N, sl, pl, sr) : launch_tau_rhs<float>(d->gm, d->N, sl, pl, sr));
-    d->launches++;
-  }
-  if (concurrent) CK(cudaEventRecord(d->ev_join, d->st2));
-  CKS(nonlinear(d, U, Nout, which));
-  if (concurrent) CK(cudaStreamWaitEvent(d->st, d->ev_join, 0));
-  PhaseScope ps(d, 1);
-  HelmB hb{d->hb_lo, d->hb_di, d->hb_up};
-  if (fp64) {
-    CK(launch_rhs_addN<double>(d->gm, d->N, p.scratch, Nout, coef, sp.kind == 1, d->st));
-    CK(launch_tau_solve_rest<double>(d->gm, d->N, sp, p, hb, tt, d->st));
-  } else {
-    CK(launch_rhs_addN<float>(d->gm, d->N, p.scratch, Nout, coef, sp.kind == 1, d->st));
-    CK(launch_tau_solve_rest<float>(d->gm, d->N, sp, p, hb, tt, d->st));
-  }
-  d->launches += 3;
-  return CFGPU_OK;
-}
-
 size_t state_bytes(cfgpu_dns d) { return d->compc() * sizeof(double); }
 
 // ---- multistep (dnsalgo.cpp:202-315) ---------------------------------------
@@ -1020,6 +955,7 @@ int ms_step(cfgpu_dns d) {
   Scheme& s = d->main;
   const int K = s.order, J = K - 1;
   const double dt = d->fl.dt;
+  CKS(nonlinear(d, d->Uh[d->perm[0]], d->Nh[d->perm[0]]));
   SolveParams sp = base_params(d);
   sp.kind = 0;
   sp.order = K;
@@ -1032,7 +968,7 @@ int ms_step(cfgpu_dns d) {
   }
   p.uout = d->Uh[d->perm[J]];
   p.qout = d->Qh[d->perm[J]];
-  CKS(nl_then_solve(d, d->Uh[d->perm[0]], d->Nh[d->perm[0]], 0, sp, p, s.tau[0]));
+  CKS(tau_solve(d, sp, p, s.tau[0]));
   ms_shift(d);
   s.t += dt;
   return CFGPU_OK;
@@ -1126,6 +1062,7 @@ int cnab_step(cfgpu_dns d, int which) {
   {
     for (int j = 0; j < s.nsub; ++j) {
       std::swap(d->fj[which], d->fj1[which]);
+      CKS(nonlinear(d, d->Ucur, d->fj[which], which));
       SolveParams sp = base_params(d);
       sp.kind = 1;
       sp.scheme = which;
@@ -1141,7 +1078,7 @@ int cnab_step(cfgpu_dns d, int which) {
       p.qin = d->Qcur;
       p.uout = d->Ucur;
       p.qout = d->Qcur;
-      CKS(nl_then_solve(d, d->Ucur, d->fj[which], which, sp, p, s.tau[j]));
+      CKS(tau_solve(d, sp, p, s.tau[j]));
     }
     s.t += d->fl.dt;
   }
@@ -1917,12 +1854,6 @@ void dns_free(cfgpu_dns d) {
     cudaEventDestroy(u.second.second);
   }
   drop_graphs(d);
-  if (d->st2) {
-    cudaStreamSynchronize(d->st2);
-    cudaStreamDestroy(d->st2);
-  }
-  if (d->ev_fork) cudaEventDestroy(d->ev_fork);
-  if (d->ev_join) cudaEventDestroy(d->ev_join);
   if (d->st) cudaStreamDestroy(d->st);
   delete d;
 }
@@ -1996,14 +1927,6 @@ int set_priority(cfgpu_dns d, int prio) {
   CK(cudaStreamCreateWithPriority(&ns, cudaStreamNonBlocking, prio));
   cudaStreamDestroy(d->st);
   d->st = ns;
-  if (d->st2) {
-    // the right-hand-side stream follows at the same priority
-    CK(cudaStreamSynchronize(d->st2));
-    cudaStream_t n2 = nullptr;
-    CK(cudaStreamCreateWithPriority(&n2, cudaStreamNonBlocking, prio));
-    cudaStreamDestroy(d->st2);
-    d->st2 = n2;
-  }
   return CFGPU_OK;
 }
 
@@ -2929,8 +2852,8 @@ cfgpu_status cfgpu_dns_phase_times(cfgpu_dns d, double* nl_ms, long long* nl_cou
   for (auto& u : d->ev_used) {
     float ms = 0;
     CK(cudaEventElapsedTime(&ms, u.second.first, u.second.second));
-    t[u.first == 2 ? 1 : u.first] += ms;
-    if (u.first != 2) n[u.first] += 1;
+    t[u.first] += ms;
+    n[u.first] += 1;
     d->ev_pool.push_back(u.second.first);
     d->ev_pool.push_back(u.second.second);
   }

@@ -202,14 +202,6 @@ int tau_solve_launches(int N);
 template <typename R>
 cudaError_t launch_tau_solve(const GridDev& g, int N, const SolveParams& sp, const SolvePtrs& p, const HelmB& hb,
                              TauTable tt, cudaStream_t st);
-template <typename R>
-cudaError_t launch_tau_rhs(const GridDev& g, int N, const SolveParams& sp, const SolvePtrs& p, cudaStream_t st);
-template <typename R>
-cudaError_t launch_tau_solve_rest(const GridDev& g, int N, const SolveParams& sp, const SolvePtrs& p,
-                                  const HelmB& hb, TauTable tt, cudaStream_t st);
-template <typename R>
-cudaError_t launch_rhs_addN(const GridDev& g, int N, double* scratch, const void* Nj, double coef, bool prod_in_R,
-                            cudaStream_t st);
 
 // FieldSymmetry (s, sx, sy, sz, ax, az) (channelflow/symmetry.h) on [c][n][field][m] spectral fields of the
 // per-field grid g (compact mode mapping); project = 1 gives (u + sigma u)/2.  out must not alias in.

@@ -1284,63 +1284,6 @@ cudaError_t launch_tau_solve(const GridDev& g, int N, const SolveParams& sp, con
   return cudaGetLastError();
 }
 
-// The three-kernel solve in two parts: the right-hand side alone (k_tau_rhs), and the rest (k_tau_solve_t,
-// k_tau_uw) after rhs_addN has added the terms of the current nonlinear term, so that the right-hand side can
-// run on another stream while the nonlinear pass computes N_j.  Only where tau_solve_launches(N) == 3.
-template <typename R>
-cudaError_t launch_tau_rhs(const GridDev& g, int N, const SolveParams& sp, const SolvePtrs& p, cudaStream_t st) {
-  const int M0 = (N - 1) / 2 + 1;
-  const size_t smem_r = sizeof(double) * (((N + 1) & ~1) + (size_t)M0 * 32);
-  k_tau_rhs<R><<<dim3((4 * g.Md + 31) / 32, 3), 32, smem_r, st>>>(g, N, sp, p);
-  return cudaGetLastError();
-}
-
-template <typename R>
-cudaError_t launch_tau_solve_rest(const GridDev& g, int N, const SolveParams& sp, const SolvePtrs& p,
-                                  const HelmB& hb, TauTable tt, cudaStream_t st) {
-  const int M0 = (N - 1) / 2 + 1;
-  static const bool attr = [] {
-    cudaFuncSetAttribute(k_tau_solve_t<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    return true;
-  }();
-  (void)attr;
-  k_tau_solve_t<R><<<(4 * g.Md + 31) / 32, 32, tau_t_smem(N), st>>>(g, N, sp, p, hb, tt);
-  const size_t smem_u = sizeof(double) * ((size_t)M0 * 32 + (size_t)4 * N * 4);
-  k_tau_uw<R><<<(8 * g.Md + 31) / 32, 32, smem_u, st>>>(g, N, sp, p, hb, tt);
-  return cudaGetLastError();
-}
-
-// Rx, Ry, Rz of the solve's scratch (lines 0, 2, 1) += coef N_c, c = x, y, z (N R-typed [c][n][2 Md]); the
-// product in R (prod_in_R: as the CNAB right-hand side combines its nonlinear terms) or in FP64.
-template <typename R>
-__global__ void k_rhs_addN(size_t per, double* __restrict__ scratch, const R* __restrict__ Nj, double coef,
-                           int prod_in_R) {
-  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (i >= per) return;
-  const int c = blockIdx.y;
-  const int dst = c == 0 ? 0 : (c == 1 ? 2 : 1);
-  const R v = Nj[c * per + i];
-  scratch[dst * per + i] += prod_in_R ? (double)((R)coef * v) : coef * (double)v;
-}
-
-template <typename R>
-cudaError_t launch_rhs_addN(const GridDev& g, int N, double* scratch, const void* Nj, double coef, bool prod_in_R,
-                            cudaStream_t st) {
-  const size_t per = 2 * (size_t)g.Md * N;
-  k_rhs_addN<R><<<dim3((unsigned)((per + 255) / 256), 3), 256, 0, st>>>(per, scratch, static_cast<const R*>(Nj),
-                                                                     coef, prod_in_R ? 1 : 0);
-  return cudaGetLastError();
-}
-
-template cudaError_t launch_tau_rhs<float>(const GridDev&, int, const SolveParams&, const SolvePtrs&, cudaStream_t);
-template cudaError_t launch_tau_rhs<double>(const GridDev&, int, const SolveParams&, const SolvePtrs&, cudaStream_t);
-template cudaError_t launch_tau_solve_rest<float>(const GridDev&, int, const SolveParams&, const SolvePtrs&,
-                                                  const HelmB&, TauTable, cudaStream_t);
-template cudaError_t launch_tau_solve_rest<double>(const GridDev&, int, const SolveParams&, const SolvePtrs&,
-                                                   const HelmB&, TauTable, cudaStream_t);
-template cudaError_t launch_rhs_addN<float>(const GridDev&, int, double*, const void*, double, bool, cudaStream_t);
-template cudaError_t launch_rhs_addN<double>(const GridDev&, int, double*, const void*, double, bool, cudaStream_t);
-
 template cudaError_t launch_tau_solve<float>(const GridDev&, int, const SolveParams&, const SolvePtrs&, const HelmB&,
                                              TauTable, cudaStream_t);
 template cudaError_t launch_tau_solve<double>(const GridDev&, int, const SolveParams&, const SolvePtrs&, const HelmB&,
