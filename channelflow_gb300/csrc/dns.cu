@@ -1527,7 +1527,9 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
   const int Nx = grid->Nx, Ny = grid->Ny, Nz = grid->Nz;
   if (Nx < 4 || Nz < 4 || Nx % 2 || Nz % 2) return fail(CFGPU_EINVAL, "Nx and Nz must be even and >= 4");
   if (Ny < 5 || Ny % 2 == 0) return fail(CFGPU_EINVAL, "Ny must be odd and >= 5 (HelmholtzSolver asserts odd N)");
-  if ((Ny + 1) / 2 > 72) return fail(CFGPU_ENOTSUP, "Ny > 143 not supported by the Chebyshev transform kernel");
+  if (Ny > 257) return fail(CFGPU_ENOTSUP, "Ny > 257 not supported by the Chebyshev transform kernels");
+  if ((Ny + 1) / 2 > 56 && f.nonlinearity != CFGPU_Rotational)
+    return fail(CFGPU_ENOTSUP, "Ny > 111 needs the rotational nonlinear form");
   if (!(grid->b > grid->a) || grid->Lx <= 0 || grid->Lz <= 0) return fail(CFGPU_EINVAL, "bad box");
   if (f.dt <= 0 || f.nu <= 0) return fail(CFGPU_EINVAL, "dt and nu must be positive");
   if (f.nonlinearity < CFGPU_Rotational || f.nonlinearity > CFGPU_LinearAboutProfile)
@@ -1866,11 +1868,21 @@ namespace {
 template <typename R>
 int cfl_enqueue(cfgpu_dns d) {
   const GridDev& g = d->gm;
-  if ((d->N + 1) / 2 > 56) return fail(CFGPU_ENOTSUP, "CFL needs Ny <= 111");
   R* W = (R*)d->W6;
-  CK(launch_grad_cheb<R>(g, d->N, false, d->Ucur, W, (const R*)d->cinvA, (const R*)d->cinvB, (const R*)d->cderA,
-                         (const R*)d->cderB, (const R*)(d->hetero ? d->baseyS : d->basey), 0.0, d->st,
-                         d->hetero ? 4 * d->N : 0));
+  if ((d->N + 1) / 2 > 56) {
+    // tall grids: u + base flow as Chebyshev coefficients (the curl pass's first three components), then the
+    // inverse transform to the Gauss-Lobatto points
+    if (d->hetero) return fail(CFGPU_ENOTSUP, "CFL of per-field base flows needs Ny <= 111");
+    const size_t row = d->rowc(), comp = d->compc();
+    CK(launch_curl_base<R>(g, d->Ucur, (R*)d->C6, d->dUbase, d->dWbase, 0.0, d->st));
+    CK((launch_cheb<R, R, R>(d->N, true, (int)row, 3, (const R*)d->C6, row, comp, W, row, comp, (const R*)d->cinvA,
+                             (const R*)d->cinvB, d->st)));
+    d->launches += 1;
+  } else {
+    CK(launch_grad_cheb<R>(g, d->N, false, d->Ucur, W, (const R*)d->cinvA, (const R*)d->cinvB, (const R*)d->cderA,
+                           (const R*)d->cderB, (const R*)(d->hetero ? d->baseyS : d->basey), 0.0, d->st,
+                           d->hetero ? 4 * d->N : 0));
+  }
   CK(launch_xinv<R>(d->gp, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)W, (cpx<R>*)d->X6, 3, d->st, d->xcols));
   CK(cudaMemsetAsync(d->dred, 0, d->nb * sizeof(unsigned long long), d->st));
   CK(launch_zcfl<R>(d->gp, d->pz, (const cpx<R>*)d->twz, d->RP, (const cpx<R>*)d->X6, d->dyc, g.Lx / g.Nx,

@@ -117,8 +117,11 @@ __global__ void __launch_bounds__(256, CS ? 3 : 1) k_cheb(int N, int inverse, in
   const int KAp = (KA + VW - 1) / VW * VW, KBp = (KB + VW - 1) / VW * VW;
   R* xa = reinterpret_cast<R*>(smem_raw);
   R* xb = xa + (size_t)KAp * CHEB_TL;
+  // output rows p0 .. p0 + PB of this block (blockIdx.z: row blocks of tall grids; one block covers P otherwise)
+  constexpr int PB = CHEB_WARPS * PT;
+  const int p0 = blockIdx.z * PB, np = min(PB, P - p0);
   R* As = xb + (size_t)KBp * CHEB_TL;
-  R* Bs = As + (size_t)P * KAp;
+  R* Bs = As + (size_t)np * KAp;
   const int tid = threadIdx.x;
   // blocks never straddle two fields (lpf lines each): a block uses its field's version of the matrices
   const int bpf = (lpf + CHEB_TL - 1) / CHEB_TL, fld = blockIdx.x / bpf;
@@ -134,16 +137,16 @@ __global__ void __launch_bounds__(256, CS ? 3 : 1) k_cheb(int N, int inverse, in
   {
     const float invA = 1.0f / KAp, invB = 1.0f / KBp;
 #pragma unroll 8
-    for (int i = tid; i < P * KAp; i += blockDim.x) {
+    for (int i = tid; i < np * KAp; i += blockDim.x) {
       int p, k;
       divmod_small(i, KAp, invA, p, k);
-      As[i] = k < KA ? Amat[p * KA + k] : (R)0;
+      As[i] = k < KA ? Amat[(p0 + p) * KA + k] : (R)0;
     }
 #pragma unroll 8
-    for (int i = tid; i < P * KBp; i += blockDim.x) {
+    for (int i = tid; i < np * KBp; i += blockDim.x) {
       int p, k;
       divmod_small(i, KBp, invB, p, k);
-      Bs[i] = k < KB ? Bmat[p * KB + k] : (R)0;
+      Bs[i] = k < KB ? Bmat[(p0 + p) * KB + k] : (R)0;
     }
   }
   for (int i = tid; i < (KAp - KA) * CHEB_TL; i += blockDim.x) xa[KA * CHEB_TL + i] = (R)0;
@@ -188,8 +191,8 @@ __global__ void __launch_bounds__(256, CS ? 3 : 1) k_cheb(int N, int inverse, in
       }
 #pragma unroll
     for (int i = 0; i < PT; ++i) {
-      const int p = warp + CHEB_WARPS * i;
-      if (p < P) {
+      const int p = warp + CHEB_WARPS * i;  // row of the block
+      if (p < np) {
         if (CS) {
           R t0 = (R)0, t1 = (R)0;
 #pragma unroll
@@ -222,11 +225,11 @@ __global__ void __launch_bounds__(256, CS ? 3 : 1) k_cheb(int N, int inverse, in
 #pragma unroll
     for (int i = 0; i < PT; ++i) {
       const int p = warp + CHEB_WARPS * i;
-      if (p >= P) continue;
+      if (p >= np) continue;
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const int gl = l0 + lane + 32 * h;
-        if (gl < nlines) out[(2 * p) * ld_out + gl] = (TO)(accA[i][h] + cmpA[i][h]);
+        if (gl < nlines) out[(2 * (p0 + p)) * ld_out + gl] = (TO)(accA[i][h] + cmpA[i][h]);
       }
     }
   }
@@ -246,7 +249,7 @@ __global__ void __launch_bounds__(256, CS ? 3 : 1) k_cheb(int N, int inverse, in
 #pragma unroll
     for (int i = 0; i < PT; ++i) {
       const int p = warp + CHEB_WARPS * i;
-      if (p < P) {
+      if (p < np) {
         if (CS) {
           R t0 = (R)0, t1 = (R)0;
 #pragma unroll
@@ -276,8 +279,9 @@ __global__ void __launch_bounds__(256, CS ? 3 : 1) k_cheb(int N, int inverse, in
   }
 #pragma unroll
   for (int i = 0; i < PT; ++i) {
-    const int p = warp + CHEB_WARPS * i;
-    if (p >= P) continue;
+    const int pl = warp + CHEB_WARPS * i;
+    if (pl >= np) continue;
+    const int p = p0 + pl;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const int gl = l0 + lane + 32 * h;
@@ -618,10 +622,19 @@ cudaError_t launch_curl_base(const GridDev& g, const double* U, R* C6, const dou
   return cudaGetLastError();
 }
 
+// Output rows per block: all P while they fit one block's warps (CHEB_WARPS x CHEB_PT); taller grids run row
+// blocks of CHEB_WARPS x CHEB_PT rows (FP32) or CHEB_WARPS x 4 rows (FP64, whose matrix rows take twice the
+// shared memory).
+int cheb_rows_per_block(int N, size_t rsize) {
+  const int P = (N + 1) / 2;
+  if (P <= CHEB_WARPS * CHEB_PT) return P;
+  return rsize == 4 ? CHEB_WARPS * CHEB_PT : CHEB_WARPS * 4;
+}
+
 size_t cheb_smem_bytes(int N, size_t rsize) {
   const int VW = rsize == 4 ? VecLds<float>::W : VecLds<double>::W;
-  const int KAp = ((N + 1) / 2 + VW - 1) / VW * VW, KBp = ((N - 1) / 2 + VW - 1) / VW * VW, P = (N + 1) / 2;
-  return rsize * ((size_t)(KAp + KBp) * CHEB_TL + (size_t)P * (KAp + KBp));
+  const int KAp = ((N + 1) / 2 + VW - 1) / VW * VW, KBp = ((N - 1) / 2 + VW - 1) / VW * VW;
+  return rsize * ((size_t)(KAp + KBp) * CHEB_TL + (size_t)cheb_rows_per_block(N, rsize) * (KAp + KBp));
 }
 
 // One launch of k_cheb with PT output rows per warp.
@@ -659,12 +672,26 @@ cudaError_t launch_cheb_cs(dim3 grid, size_t sm, cudaStream_t st, int N, int inv
 template <typename TI, typename R, typename TO>
 cudaError_t launch_cheb(int N, bool inverse, int nlines, int ncomp, const TI* in, size_t ld_in, size_t cs_in, TO* out,
                         size_t ld_out, size_t cs_out, const R* A, const R* B, cudaStream_t st, const Dither& dt) {
-  if ((N + 1) / 2 > CHEB_WARPS * CHEB_PT) return cudaErrorInvalidValue;
   const int P = (N + 1) / 2;
   const int KA = (N + 1) / 2, KB = (N - 1) / 2;
   const size_t sm = cheb_smem_bytes(N, sizeof(R));
+  if (sm > 200 * 1024) return cudaErrorInvalidValue;
+  const int PB = cheb_rows_per_block(N, sizeof(R));
   const int nf = dt.nb > 0 ? dt.nb : 1, lpf = (nlines + nf - 1) / nf;
-  dim3 grid(nf * ((lpf + CHEB_TL - 1) / CHEB_TL), ncomp);
+  dim3 grid(nf * ((lpf + CHEB_TL - 1) / CHEB_TL), ncomp, (P + PB - 1) / PB);
+  if (grid.z > 1) {
+    // row blocks: the rows per warp that make one block's PB rows
+    if constexpr (sizeof(R) == 4) {
+      if (!inverse)
+        return launch_cheb_pt<TI, R, TO, true, CHEB_PT>(grid, sm, st, N, 0, nlines, in, ld_in, cs_in, out, ld_out,
+                                                        cs_out, A, B, P, KA, KB, dt, lpf);
+      return launch_cheb_pt<TI, R, TO, false, CHEB_PT>(grid, sm, st, N, 1, nlines, in, ld_in, cs_in, out, ld_out,
+                                                       cs_out, A, B, P, KA, KB, dt, lpf);
+    } else {
+      return launch_cheb_pt<TI, R, TO, false, 4>(grid, sm, st, N, inverse ? 1 : 0, nlines, in, ld_in, cs_in, out,
+                                                 ld_out, cs_out, A, B, P, KA, KB, dt, lpf);
+    }
+  }
   // compensated sums for the FP32 forward transforms
   if constexpr (sizeof(R) == 4) {
     if (!inverse)

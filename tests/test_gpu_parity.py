@@ -119,6 +119,13 @@ CASES = [
     ("couette_tall129_sbdf3", (12, 129, 12, *COUETTE_BOX),
      dict(nu=1 / 400, dt=0.01, timestepping=O.SBDF3, initstepping=O.SMRK2, baseflow=O.LaminarBase,
           ulowerwall=-1.0, uupperwall=1.0), 6),
+    # taller than one block of the dense Chebyshev kernels: row blocks, curl then transform, tall CFL
+    ("couette_tall161_sbdf3", (12, 161, 12, *COUETTE_BOX),
+     dict(nu=1 / 400, dt=0.01, timestepping=O.SBDF3, initstepping=O.SMRK2, baseflow=O.LaminarBase,
+          ulowerwall=-1.0, uupperwall=1.0), 6),
+    ("poiseuille_tall257_cnab2", (12, 257, 12, *POISEUILLE_BOX),
+     dict(nu=1 / 4000, dt=0.005, timestepping=O.CNAB2, initstepping=O.SMRK2, baseflow=O.LaminarBase,
+          constraint=O.BulkVelocity, Ubulk=2.0 / 3.0), 6),
 ]
 
 
@@ -168,7 +175,7 @@ def test_dns_mixed_matches_oracle():
     assert rel_l2(gu, ou, g) <= MIXED_TOL
 
 
-@pytest.mark.parametrize("ny", [97, 129])
+@pytest.mark.parametrize("ny", [97, 129, 161, 257])
 def test_dns_mixed_tall_grids(ny):
     """Mixed path with the compensated forward Chebyshev sums at Ny = 97 and 129 (7 and 9 rows per warp)."""
     g = O.Grid(12, ny, 12, *COUETTE_BOX)
@@ -208,9 +215,10 @@ def test_resident_path_equals_host_path():
     assert np.array_equal(u, a)
 
 
+@pytest.mark.parametrize("ny", [33, 161])
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed", 1e-5)])
-def test_cfl_and_l2norm_match_oracle(precision, tol):
-    g = O.Grid(24, 33, 24, *COUETTE_BOX)
+def test_cfl_and_l2norm_match_oracle(precision, tol, ny):
+    g = O.Grid(24, ny, 24, *COUETTE_BOX)
     fl = O.DNSFlags(nu=1 / 400, dt=0.02, baseflow=O.LaminarBase, ulowerwall=-1.0, uupperwall=1.0)
     u0 = O.random_divfree_field(g, seed=21, norm=0.2)
     gu, gq, dns = gpu_run(u0, g, fl, 3, precision=precision)
