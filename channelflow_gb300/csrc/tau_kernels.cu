@@ -1269,6 +1269,9 @@ cudaError_t launch_tau_solve(const GridDev& g, int N, const SolveParams& sp, con
     // kernel attributes set once per process (thread-safe static initialisation)
     static const bool attr = [] {
       cudaFuncSetAttribute(k_tau_solve_t<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+      // tall grids take more than the default 48 KB in the right-hand-side and u/w kernels too
+      cudaFuncSetAttribute(k_tau_rhs<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+      cudaFuncSetAttribute(k_tau_uw<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
       return true;
     }();
     (void)attr;
