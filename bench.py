@@ -217,7 +217,8 @@ def run_gpu(args, rank, world):
         nl_ms, nl_n, tau_ms, tau_n = dns.phase_times()
         dns.set_profiling(False)
         results[prec] = dict(ms=ms, K=K, launches=launches, clocks=cs.summary(), nl_ms=nl_ms, nl_n=nl_n,
-                             tau_ms=tau_ms, tau_n=tau_n, Md=dns.num_modes(), bytes=dns.device_bytes())
+                             tau_ms=tau_ms, tau_n=tau_n, Md=dns.num_modes(), bytes=dns.device_bytes(),
+                             cheb_fft=dns.cheb_fft())
         if True:
             # end-to-end through the public API: host buffers in, host buffers out, every step
             Ke = max(3, min(args.steps, 50))
@@ -670,7 +671,8 @@ def main():
         "config": {"workload": WORKLOAD, "precision": "mixed", "grid": [NX, NY, NZ], "solved_modes": Md,
                    "grid_point_steps_per_s": sps * NX * NY * NZ,
                    "l2": "no flush: per-step working set %.0f MB > 129 MB L2" % (m["bytes"] / 1e6),
-                   "parallelism": "replicas" if world > 1 else "single"},
+                   "parallelism": "replicas" if world > 1 else "single",
+                   "cheb_transforms": "fft" if m["cheb_fft"] else "matrix"},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm, "unit": "GB/s",
                      "frac": ach / hbm, "peak_source": peak_kind,
                      "traffic": NCU_TRAFFIC.get(dom) if (NX, NY, NZ) == (128, 97, 128) else None,
@@ -682,7 +684,8 @@ def main():
                                  "achieved_gbs": btau / (tau_avg / 1e3) / 1e9 if tau_avg else None}},
         "fp64": {"value": sps64, "unit": "steps/s", "ms_per_step": f["ms"] / f["K"], "steps": f["K"],
                  "nl_avg_ms": f["nl_ms"] / max(1, f["nl_n"]), "tau_avg_ms": f["tau_ms"] / max(1, f["tau_n"]),
-                 "nl_alg_bytes": bnl64, "tau_alg_bytes": btau64},
+                 "nl_alg_bytes": bnl64, "tau_alg_bytes": btau64,
+                 "cheb_transforms": "fft" if f["cheb_fft"] else "matrix"},
         # FP64 roofline (the tau solve of both paths and the whole plain-FP64 step compute in FP64): algorithmic
         # FLOPs by formula over the FP64 FMA throughput measured on this GPU in this run
         "roofline_fp64": {"peak_tflops": pk64, "dependent_dfma_cycles": cyc64,

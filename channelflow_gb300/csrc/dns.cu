@@ -608,6 +608,9 @@ struct cfgpu_dns_s {
   void *twxf = nullptr, *twzf = nullptr;
   bool xzf = false;
   int xzC = 0, xzRC = 0;
+  // Chebyshev transforms of the rotational form through the FFT (dct_table(Ny), R-typed): chosen at creation
+  void* cdct = nullptr;
+  bool ydct = false;
   void *cinvA = nullptr, *cinvB = nullptr, *cfwdA = nullptr, *cfwdB = nullptr;
   void *cderA = nullptr, *cderB = nullptr, *basey = nullptr;  // fused curl: (2/L) T'_n(y_j); U, U', W, W' at y_j
   void *cdfA = nullptr, *cdfB = nullptr;                       // (2/L) diff o chebyfft, parity split
@@ -794,14 +797,22 @@ int nonlinear_impl(cfgpu_dns d, const double* U, void* Nout, int form) {
     d->launches += 3;
     return CFGPU_OK;
   }
-  if (form == NL_ROTATIONAL) {
+  const double* bU = d->hetero ? d->dbaseS : d->dUbase;
+  const double* bW = d->hetero ? d->dbaseS + (size_t)d->nb * N : d->dWbase;
+  if (form == NL_ROTATIONAL && d->ydct) {
+    // spectral curl, then the inverse transform of u, v, w, ox, oy, oz through the FFT
+    CK(launch_curl_base<R>(g, U, C6, bU, bW, d->hetero ? N : 0, d->fl.Vsuck, d->st));
+    CK(launch_dct<R>(N, true, g.Md, 6, (const cpx<R>*)C6, row / 2, comp / 2, (cpx<R>*)W, row / 2, comp / 2,
+                     (const cpx<R>*)d->cdct, d->st, dt));
+    d->launches += 2;
+  } else if (form == NL_ROTATIONAL) {
     if ((N + 1) / 2 <= 56) {
       CK(launch_curl_cheb<R>(g, N, U, W, (const R*)d->cinvA, (const R*)d->cinvB, (const R*)d->cderA,
                              (const R*)d->cderB, (const R*)(d->hetero ? d->baseyS : d->basey), d->fl.Vsuck, d->st,
                              d->hetero ? 4 * N : 0, dt));
       d->launches += 1;
     } else {
-      CK(launch_curl_base<R>(g, U, C6, d->dUbase, d->dWbase, d->fl.Vsuck, d->st));
+      CK(launch_curl_base<R>(g, U, C6, bU, bW, d->hetero ? N : 0, d->fl.Vsuck, d->st));
       CK((launch_cheb<R, R, R>(N, true, (int)row, 6, C6, row, comp, W, row, comp, (const R*)d->cinvA,
                                (const R*)d->cinvB, d->st, dt)));
       d->launches += 2;
@@ -830,7 +841,11 @@ int nonlinear_impl(cfgpu_dns d, const double* U, void* Nout, int form) {
     d->launches += 3;
   }
   const R* F = (const R*)d->F3;
-  if (form == NL_ROTATIONAL || form == NL_CONVECTION) {
+  if (form == NL_ROTATIONAL && d->ydct) {
+    CK(launch_dct<R>(N, false, g.Md, 3, (const cpx<R>*)F, row / 2, comp / 2, (cpx<R>*)Nout, row / 2, comp / 2,
+                     (const cpx<R>*)d->cdct, d->st, dt));
+    d->launches += 1;
+  } else if (form == NL_ROTATIONAL || form == NL_CONVECTION) {
     CK((launch_cheb<R, R, R>(N, false, (int)row, 3, F, row, comp, (R*)Nout, row, comp, (const R*)d->cfwdA,
                              (const R*)d->cfwdB, d->st, dt)));
     d->launches += 1;
@@ -1520,6 +1535,68 @@ int tune_xz(cfgpu_dns d) {
   return CFGPU_OK;
 }
 
+// Chebyshev transforms of the rotational form: dense matrix products (fused curl + inverse, forward) or the
+// FFT form (spectral curl, inverse and forward through the FFT), timed with CUDA events on this DNS's own
+// arrays when the mode is automatic; cached per (grid, planes, precision).
+std::atomic<int> g_cheb_fft{1};
+std::map<TuneKey, int> g_tune_cheb;
+
+template <typename R>
+int tune_cheb(cfgpu_dns d) {
+  d->ydct = false;
+  const int mode = g_cheb_fft.load();
+  if (mode == 0 || !d->cdct || !dct_supported(d->N)) return CFGPU_OK;
+  if (mode == 2) {
+    d->ydct = true;
+    return CFGPU_OK;
+  }
+  const GridDev& g = d->gm;
+  const TuneKey key{d->gp.Nx, d->gp.Ny, d->gp.Nz, d->gp.NKz, (int)sizeof(R), 100};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune_cheb.find(key);
+    if (it != g_tune_cheb.end()) {
+      d->ydct = it->second != 0;
+      return CFGPU_OK;
+    }
+  }
+  const int N = d->N;
+  const size_t row = d->rowc(), comp = d->compc();
+  R* C6 = (R*)d->C6;
+  R* W = (R*)d->W6;
+  const float tdense = time_ms<R>(d, [&]() {
+    cudaError_t e;
+    if ((N + 1) / 2 <= 56) {
+      e = launch_curl_cheb<R>(g, N, d->Ucur, W, (const R*)d->cinvA, (const R*)d->cinvB, (const R*)d->cderA,
+                              (const R*)d->cderB, (const R*)d->basey, 0.0, d->st);
+    } else {
+      e = launch_curl_base<R>(g, d->Ucur, C6, d->dUbase, d->dWbase, 0, 0.0, d->st);
+      if (e == cudaSuccess)
+        e = launch_cheb<R, R, R>(N, true, (int)row, 6, C6, row, comp, W, row, comp, (const R*)d->cinvA,
+                                 (const R*)d->cinvB, d->st);
+    }
+    if (e == cudaSuccess)
+      e = launch_cheb<R, R, R>(N, false, (int)row, 3, (const R*)d->F3, row, comp, C6, row, comp, (const R*)d->cfwdA,
+                               (const R*)d->cfwdB, d->st);
+    return e;
+  });
+  const float tfft = time_ms<R>(d, [&]() {
+    cudaError_t e = launch_curl_base<R>(g, d->Ucur, C6, d->dUbase, d->dWbase, 0, 0.0, d->st);
+    if (e == cudaSuccess)
+      e = launch_dct<R>(N, true, g.Md, 6, (const cpx<R>*)C6, row / 2, comp / 2, (cpx<R>*)W, row / 2, comp / 2,
+                        (const cpx<R>*)d->cdct, d->st);
+    if (e == cudaSuccess)
+      e = launch_dct<R>(N, false, g.Md, 3, (const cpx<R>*)d->F3, row / 2, comp / 2, (cpx<R>*)C6, row / 2,
+                        comp / 2, (const cpx<R>*)d->cdct, d->st);
+    return e;
+  });
+  d->ydct = tfft < 1e30f && tfft < tdense;
+  CK(cudaStreamSynchronize(d->st));
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune_cheb[key] = d->ydct ? 1 : 0;
+  return CFGPU_OK;
+}
+
 int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flags, const double* Ub, const double* Wb,
                     const double* u0, int nb = 1) {
   d->fl = *flags;
@@ -1679,6 +1756,7 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
     CKS(upload_as<double>(basey, &d->basey, B, d->st));
     CKS(upload_as<double>(cm.dfA, &d->cdfA, B, d->st));
     CKS(upload_as<double>(cm.dfB, &d->cdfB, B, d->st));
+    if (dct_supported(Ny)) CKS(upload_as<double>(dct_table(Ny), &d->cdct, B, d->st));
   } else {
     // DITHER_V dithered versions of every FP32 constant table in one block (16-byte aligned tables)
     std::vector<std::vector<double>> tabs = {cm.invA, cm.invB, cm.fwdA, cm.fwdB, cm.derA, cm.derB, cm.dfA, cm.dfB};
@@ -1706,6 +1784,7 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
     }
     tabs.push_back(circx);
     tabs.push_back(circz);
+    tabs.push_back(dct_supported(Ny) ? dct_table(Ny) : std::vector<double>(2, 0.0));
     std::vector<size_t> off(tabs.size());
     size_t S = 0;
     for (size_t i = 0; i < tabs.size(); ++i) {
@@ -1722,6 +1801,7 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
     d->kmisc = c0 + off[12];
     d->twxf = c0 + off[13];
     d->twzf = c0 + off[14];
+    if (dct_supported(Ny)) d->cdct = c0 + off[15];
     d->cS = (long long)(S * sizeof(float));
     CKS(upload_dithered({basey}, {0}, basey.size(), &d->basey, B, d->st));
   }
@@ -1774,6 +1854,8 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
   // fused x/z pass for the rotational form (thread-block clusters over a y-plane)
   d->xzf = false;
   if (rot && g_fused_xz.load() != 0 && xz_fused_supported(d->gp)) CKS(fp64 ? tune_xz<double>(d) : tune_xz<float>(d));
+  // Chebyshev transforms of the rotational form: dense or through the FFT
+  if (rot) CKS(fp64 ? tune_cheb<double>(d) : tune_cheb<float>(d));
 
   // schemes (DNS::DNS, dns.cpp:22-39)
   CKS(setup_scheme(d->main, f.timestepping, f.dt));
@@ -1832,9 +1914,9 @@ void dns_free(cfgpu_dns d) {
   if (d->cblock) {
     // the FP32 constant tables live inside one block (all versions): freed once, below
     d->twx = d->twz = d->cinvA = d->cinvB = d->cfwdA = d->cfwdB = d->cderA = d->cderB = d->cdfA = d->cdfB = nullptr;
-    d->twxf = d->twzf = nullptr;
+    d->twxf = d->twzf = d->cdct = nullptr;
   }
-  F(d->twxf); F(d->twzf);
+  F(d->twxf); F(d->twzf); F(d->cdct);
   F(d->dUbase); F(d->dWbase); F(d->dUbaseyy); F(d->dWbaseyy); F(d->ddPdx);
   F(d->hb_lo); F(d->hb_di); F(d->hb_up);
   F(d->twx); F(d->twz); F(d->cinvA); F(d->cinvB); F(d->cfwdA); F(d->cfwdB);
@@ -1869,15 +1951,19 @@ template <typename R>
 int cfl_enqueue(cfgpu_dns d) {
   const GridDev& g = d->gm;
   R* W = (R*)d->W6;
-  if ((d->N + 1) / 2 > 56) {
-    // tall grids: u + base flow as Chebyshev coefficients (the curl pass's first three components), then the
-    // inverse transform to the Gauss-Lobatto points
-    if (d->hetero) return fail(CFGPU_ENOTSUP, "CFL of per-field base flows needs Ny <= 111");
-    const size_t row = d->rowc(), comp = d->compc();
-    CK(launch_curl_base<R>(g, d->Ucur, (R*)d->C6, d->dUbase, d->dWbase, 0.0, d->st));
-    CK((launch_cheb<R, R, R>(d->N, true, (int)row, 3, (const R*)d->C6, row, comp, W, row, comp, (const R*)d->cinvA,
-                             (const R*)d->cinvB, d->st)));
-    d->launches += 1;
+  if ((d->N + 1) / 2 > 56 || d->ydct) {
+    // tall grids, or transforms through the FFT: u + base flow as Chebyshev coefficients (the curl pass's
+    // first three components), then the inverse transform to the Gauss-Lobatto points
+    const size_t row = d->rowc(), comp = d->compc(), nN = (size_t)d->nb * d->N;
+    CK(launch_curl_base<R>(g, d->Ucur, (R*)d->C6, d->hetero ? d->dbaseS : d->dUbase,
+                           d->hetero ? d->dbaseS + nN : d->dWbase, d->hetero ? d->N : 0, 0.0, d->st));
+    if (d->ydct)
+      CK(launch_dct<R>(d->N, true, g.Md, 3, (const cpx<R>*)d->C6, row / 2, comp / 2, (cpx<R>*)W, row / 2, comp / 2,
+                       (const cpx<R>*)d->cdct, d->st));
+    else
+      CK((launch_cheb<R, R, R>(d->N, true, (int)row, 3, (const R*)d->C6, row, comp, W, row, comp,
+                               (const R*)d->cinvA, (const R*)d->cinvB, d->st)));
+    d->launches += 2;
   } else {
     CK(launch_grad_cheb<R>(g, d->N, false, d->Ucur, W, (const R*)d->cinvA, (const R*)d->cinvB, (const R*)d->cderA,
                            (const R*)d->cderB, (const R*)(d->hetero ? d->baseyS : d->basey), 0.0, d->st,
@@ -2827,12 +2913,27 @@ cfgpu_status cfgpu_set_fused_xz(int enable) {
   return CFGPU_OK;
 }
 
+cfgpu_status cfgpu_set_cheb_fft(int mode) {
+  if (mode < 0 || mode > 2) return fail(CFGPU_EINVAL, "mode must be 0 (matrix), 1 (automatic) or 2 (FFT)");
+  g_cheb_fft.store(mode);
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune_cheb.clear();
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_dns_cheb_fft(cfgpu_dns dns, int* fft) {
+  if (!dns || !fft) return fail(CFGPU_EINVAL, "null argument");
+  *fft = dns->ydct ? 1 : 0;
+  return CFGPU_OK;
+}
+
 cfgpu_status cfgpu_set_autotune(int enable) {
   g_autotune.store(enable ? 1 : 0);
   if (!enable) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_tune.clear();
     g_tune_xz.clear();
+    g_tune_cheb.clear();
   }
   return CFGPU_OK;
 }

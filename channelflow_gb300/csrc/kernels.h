@@ -10,12 +10,27 @@
 // Records the message returned by cfgpu_last_error() on this thread; returns code.
 int cfgpu_record_error(int code, const std::string& msg);
 
-template <typename R>
-cudaError_t launch_curl_base(const GridDev& g, const double* U, R* C6, const double* Ub, const double* Wb, double Vsuck,
-                             cudaStream_t st);
-
 // Undithered constants (version 0 only; one field).
 constexpr Dither kNoDither{nullptr, 0, 0, 1, nullptr, nullptr, nullptr};
+
+// Spectral curl (cheb_dct.cu): C6 = u, v, w, ox, oy, oz as Chebyshev coefficients, base flow (per field:
+// Ub/Wb + field * bstride) added to the (0,0) mode.
+template <typename R>
+cudaError_t launch_curl_base(const GridDev& g, const double* U, R* C6, const double* Ub, const double* Wb,
+                             int bstride, double Vsuck, cudaStream_t st);
+
+// Chebyshev transforms along y through one complex FFT of length N - 1 per mode (cheb_dct.cu), for
+// N - 1 = 8 N1, N1 in {4, 6, 8, 12, 16}.  Element (n, mode) of component c at in[c cs_in + n ld_in + mode]
+// (complex units); modes split evenly over dt.nb fields.  tab = dct_table(N) (one version per field version).
+bool dct_supported(int N);
+std::vector<double> dct_table(int N);
+template <typename R>
+size_t dct_smem_bytes(int N);
+template <typename R>
+cudaError_t launch_dct(int N, bool inverse, int nmodes, int ncomp, const cpx<R>* in, size_t ld_in, size_t cs_in,
+                       cpx<R>* out, size_t ld_out, size_t cs_out, const cpx<R>* tab, cudaStream_t st,
+                       const Dither& dt = kNoDither);
+
 
 size_t cheb_smem_bytes(int N, size_t rsize);
 

@@ -1,5 +1,5 @@
-// Nonlinear-term kernels of the DNS step: spectral curl, Chebyshev (y)
-// transforms and the x/z FFT passes with the physical-space cross product.
+// Nonlinear-term kernels of the DNS step: dense Chebyshev (y) transforms (the
+// spectral curl fused in) and the x/z FFT passes with the physical-space cross product.
 //
 // Reference functions restated (channelflow project paths):
 //   curl               channelflow/diffops.cpp:2229-2334
@@ -12,68 +12,6 @@
 //                      are ever stored, so truncation is implicit)
 #include "fft.cuh"
 #include "kernels.h"
-
-// ---------------------------------------------------------------------------
-// Spectral curl with the base flow added to the (0,0) mode.
-//   out[0..2] = u + base,  out[3..5] = curl(u + base)   (Chebyshev coeffs)
-// One thread per mode; the y-derivative is the reference's downward
-// recurrence d[n] = d[n+2] + (4/L)(n+1) u[n+1], d[0] *= 1/2.
-// ---------------------------------------------------------------------------
-template <typename R>
-__global__ void k_curl_base(GridDev g, const double* __restrict__ U, R* __restrict__ C6,
-                            const double* __restrict__ Ubase, const double* __restrict__ Wbase, double Vsuck) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= g.Md) return;
-  const int Ny = g.Ny;
-  const size_t row = 2 * (size_t)g.Md;
-  const size_t comp = row * Ny;
-  const int kx = mode_kx(g, m), kz = mode_kz(g, m);
-  const double dx = 2.0 * M_PI * kx / g.Lx * (kx == g.kxmax ? 0.0 : 1.0);
-  const double dz = 2.0 * M_PI * kz / g.Lz * (kz == g.kzmax ? 0.0 : 1.0);
-  const bool m00 = (kx == 0 && kz == 0);
-  const double scale = 4.0 / (g.b - g.a);
-  const int Nb = Ny - 1;
-  // Downward recurrence d[n] = d[n+2] + (n+1)*scale*x[n+1] with d[Nb+1] =
-  // d[Nb+2] = 0; (d1, d2) hold d[n+1], d[n+2]; xn holds x[n+1].
-  cpx<double> dw1 = cmk(0.0, 0.0), dw2 = cmk(0.0, 0.0), du1 = cmk(0.0, 0.0), du2 = cmk(0.0, 0.0);
-  cpx<double> un = cmk(0.0, 0.0), wn = cmk(0.0, 0.0);
-  for (int n = Nb; n >= 0; --n) {
-    const size_t o = n * row + 2 * (size_t)m;
-    cpx<double> u = cmk(U[o], U[o + 1]);
-    cpx<double> v = cmk(U[comp + o], U[comp + o + 1]);
-    cpx<double> w = cmk(U[2 * comp + o], U[2 * comp + o + 1]);
-    if (m00) {
-      u.x += Ubase[n];
-      w.x += Wbase[n];
-      if (n == 0) v.x -= Vsuck;
-    }
-    const double c = (n + 1) * scale;
-    const cpx<double> dwn = cmk(dw2.x + c * wn.x, dw2.y + c * wn.y);
-    const cpx<double> dun = cmk(du2.x + c * un.x, du2.y + c * un.y);
-    dw2 = dw1;
-    dw1 = dwn;
-    du2 = du1;
-    du1 = dun;
-    un = u;
-    wn = w;
-    cpx<double> Dw = dwn, Du = dun;
-    if (n == 0) {
-      Dw.x *= 0.5; Dw.y *= 0.5;
-      Du.x *= 0.5; Du.y *= 0.5;
-    }
-    // omega_x = Dw - i dz v ; omega_y = i dz u - i dx w ; omega_z = i dx v - Du
-    cpx<double> ox = cmk(Dw.x + dz * v.y, Dw.y - dz * v.x);
-    cpx<double> oy = cmk(-dz * u.y + dx * w.y, dz * u.x - dx * w.x);
-    cpx<double> oz = cmk(-dx * v.y - Du.x, dx * v.x - Du.y);
-    R* out = C6 + o;
-    out[0] = (R)u.x; out[1] = (R)u.y;
-    out[comp] = (R)v.x; out[comp + 1] = (R)v.y;
-    out[2 * comp] = (R)w.x; out[2 * comp + 1] = (R)w.y;
-    out[3 * comp] = (R)ox.x; out[3 * comp + 1] = (R)ox.y;
-    out[4 * comp] = (R)oy.x; out[4 * comp + 1] = (R)oy.y;
-    out[5 * comp] = (R)oz.x; out[5 * comp + 1] = (R)oz.y;
-  }
-}
 
 // ---------------------------------------------------------------------------
 // Chebyshev transform along y of many real lines, parity split.
@@ -614,14 +552,6 @@ __global__ void __launch_bounds__(256) k_xfwd(GridDev g, FftPlan px, const cpx<R
 // ---------------------------------------------------------------------------
 // Host launchers
 // ---------------------------------------------------------------------------
-template <typename R>
-cudaError_t launch_curl_base(const GridDev& g, const double* U, R* C6, const double* Ub, const double* Wb, double Vsuck,
-                             cudaStream_t st) {
-  const int T = 128;
-  k_curl_base<R><<<(g.Md + T - 1) / T, T, 0, st>>>(g, U, C6, Ub, Wb, Vsuck);
-  return cudaGetLastError();
-}
-
 // Output rows per block: all P while they fit one block's warps (CHEB_WARPS x CHEB_PT); taller grids run row
 // blocks of CHEB_WARPS x CHEB_PT rows (FP32) or CHEB_WARPS x 4 rows (FP64, whose matrix rows take twice the
 // shared memory).
@@ -748,8 +678,6 @@ cudaError_t launch_xfwd(const GridDev& g, const FftPlan& px, const cpx<R>* twx, 
 }
 
 #define INST_R(R)                                                                                                   \
-  template cudaError_t launch_curl_base<R>(const GridDev&, const double*, R*, const double*, const double*, double, \
-                                           cudaStream_t);                                                           \
   template cudaError_t launch_xinv<R>(const GridDev&, const FftPlan&, const cpx<R>*, const cpx<R>*, cpx<R>*, int,   \
                                       cudaStream_t, int, const Dither&);                                            \
   template cudaError_t launch_xfwd<R>(const GridDev&, const FftPlan&, const cpx<R>*, const cpx<R>*, cpx<R>*, int,   \

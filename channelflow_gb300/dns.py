@@ -127,6 +127,12 @@ class DNS:
         L.check(self._lib.cfgpu_dns_get_fields(self._h, L.dptr(_as_field(u, self.grid, 3)),
                                                L.dptr(_as_field(q, self.grid, 1))))
 
+    def cheb_fft(self) -> bool:
+        """True when the nonlinear term's Chebyshev transforms run through the FFT (else matrix products)."""
+        v = C.c_int()
+        L.check(self._lib.cfgpu_dns_cheb_fft(self._h, C.byref(v)))
+        return bool(v.value)
+
     def advance_timed(self, nsteps: int) -> float:
         """Resident advance bracketed by CUDA events on the library's stream; device milliseconds."""
         ms = C.c_double()

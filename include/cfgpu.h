@@ -263,6 +263,14 @@ cfgpu_status cfgpu_set_autotune(int enable);
  * distributed shared memory) when the grid allows (Nx, Nz in {32, 48, 64, 96, 128}); otherwise as three
  * kernels. Both give the same results to rounding. */
 cfgpu_status cfgpu_set_fused_xz(int enable);
+/* No reference counterpart: the Chebyshev transforms of the rotational form's nonlinear term (the inverse
+ * transform of u and curl u, the forward transform of the product) run either as dense parity-split matrix
+ * products or through one complex FFT of length Ny - 1 per mode (Ny - 1 in {32, 48, 64, 96, 128}).  For DNS
+ * objects created afterwards: mode 0 matrix products; 1 (the default) both timed at creation on the DNS's own
+ * arrays, the faster kept (cached per grid shape and precision); 2 the FFT wherever the grid allows.  Both
+ * give the same results to rounding.  cfgpu_dns_cheb_fft reports a DNS's choice (1 FFT, 0 matrix). */
+cfgpu_status cfgpu_set_cheb_fft(int mode);
+cfgpu_status cfgpu_dns_cheb_fft(cfgpu_dns dns, int* fft);
 /* Host FlowField buffers: on devices whose kernels reach pageable host memory through the host page
  * tables (GB300 over NVLink-C2C), DNS objects created while enable != 0 (the default) read and write the
  * caller's buffers with one kernel each way; otherwise through host-side gathers and pinned staging

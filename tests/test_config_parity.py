@@ -65,11 +65,19 @@ def oracle_result(name):
     return _ORACLE[name]
 
 
-def gpu_run(u0, g, fl, nsteps, precision):
+def gpu_run(u0, g, fl, nsteps, precision, cheb=1):
+    """cheb: Chebyshev transforms of the nonlinear term as matrix products (0), the faster of the two (1),
+    or through the FFT (2)."""
     from channelflow_gb300 import DNS
+    from channelflow_gb300 import _lib as L
+    lib = L.load()
     u = np.ascontiguousarray(u0.copy())
     q = np.zeros((1,) + u.shape[1:], complex)
-    dns = DNS(u, to_cgrid(g), to_cflags(fl), precision=precision)
+    L.check(lib.cfgpu_set_cheb_fft(cheb))
+    try:
+        dns = DNS(u, to_cgrid(g), to_cflags(fl), precision=precision)
+    finally:
+        L.check(lib.cfgpu_set_cheb_fft(1))
     dns.advance(u, q, nsteps)
     return u, dns
 
@@ -81,19 +89,24 @@ def check_constraints(u, g):
     assert O.wall_slope_norm(u, g) <= BC_TOL * n
 
 
+CHEB = pytest.mark.parametrize("cheb", [0, 2], ids=["matrix", "fft"])
+
+
+@CHEB
 @pytest.mark.parametrize("name", ["poiseuille", "couette"])
-def test_config_fp64_matches_oracle(name):
+def test_config_fp64_matches_oracle(name, cheb):
     g, fl, u0, n, ou = oracle_result(name)
-    gu, dns = gpu_run(u0, g, fl, n, "fp64")
+    gu, dns = gpu_run(u0, g, fl, n, "fp64", cheb)
     assert rel_l2(gu, ou, g) <= FP64_TOL
     assert abs(dns.time() - n * fl.dt) < 1e-12
     check_constraints(gu, g)
 
 
+@CHEB
 @pytest.mark.parametrize("name,tol", [("poiseuille", MIXED_TOL_POIS_100), ("couette", MIXED_TOL_COUETTE)])
-def test_config_mixed_matches_oracle(name, tol):
+def test_config_mixed_matches_oracle(name, tol, cheb):
     g, fl, u0, n, ou = oracle_result(name)
-    gu, _ = gpu_run(u0, g, fl, n, "mixed")
+    gu, _ = gpu_run(u0, g, fl, n, "mixed", cheb)
     assert rel_l2(gu, ou, g) <= tol
     check_constraints(gu, g)
 

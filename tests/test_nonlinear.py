@@ -80,3 +80,72 @@ def test_fused_xz_pass_matches_oracle_and_three_kernel_path(dims, precision, tol
         L.check(lib.cfgpu_set_fused_xz(1))
     assert rel_l2(out[1], ref, g) <= tol
     assert rel_l2(out[1], out[0], g) <= tol_pair
+
+
+CHEB_FFT_CASES = [
+    ("poiseuille_33", (16, 33, 16), POISEUILLE_BOX,
+     dict(baseflow=O.LaminarBase, constraint=O.BulkVelocity, Ubulk=2 / 3)),
+    ("couette_49", (24, 49, 18), COUETTE_BOX, dict(baseflow=O.LaminarBase, ulowerwall=-1.0, uupperwall=1.0)),
+    ("suction_65", (16, 65, 16), POISEUILLE_BOX, dict(baseflow=O.SuctionBase, Vsuck=0.01)),
+    ("poiseuille_97", (32, 97, 32), POISEUILLE_BOX,
+     dict(baseflow=O.LaminarBase, constraint=O.BulkVelocity, Ubulk=2 / 3)),
+    ("couette_rotation_129", (16, 129, 12), COUETTE_BOX,
+     dict(baseflow=O.LaminarBase, ulowerwall=-1.0, uupperwall=1.0, rotation=0.3)),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol,tol_pair", [("fp64", 1e-12, 1e-13), ("mixed", 1e-5, 3e-6)])
+@pytest.mark.parametrize("name,dims,box,fkw", CHEB_FFT_CASES, ids=[c[0] for c in CHEB_FFT_CASES])
+def test_cheb_fft_matches_oracle_and_matrix_path(name, dims, box, fkw, precision, tol, tol_pair):
+    """The rotational form with its Chebyshev transforms through the FFT (spectral curl, inverse and forward
+    DCT-I as one complex FFT of length Ny - 1 per mode) against the oracle and against the dense matrix
+    products on the same field."""
+    from channelflow_gb300 import DNS, build
+    from channelflow_gb300 import _lib as L
+    build.build()
+    lib = L.load()
+    g = O.Grid(dims[0], dims[1], dims[2], *box)
+    fl = O.DNSFlags(nu=1 / 1000, dt=0.01, nonlinearity=O.Rotational, **fkw)
+    u = np.ascontiguousarray(O.random_divfree_field(g, seed=dims[1], norm=0.3))
+    ref, _ = O.NSE(g, fl, None, u).nonlinear(u)
+    out = {}
+    try:
+        for mode in (2, 0):
+            L.check(lib.cfgpu_set_cheb_fft(mode))
+            d = DNS(u.copy(), to_cgrid(g), to_cflags(fl), precision=precision)
+            used = ctypes_int()
+            L.check(lib.cfgpu_dns_cheb_fft(d._h, used))
+            assert used.value == (1 if mode == 2 else 0)
+            out[mode] = d.nonlinear(u)
+            d.close()
+    finally:
+        L.check(lib.cfgpu_set_cheb_fft(1))
+    assert rel_l2(out[2], ref, g) <= tol, rel_l2(out[2], ref, g)
+    assert rel_l2(out[2], out[0], g) <= tol_pair, rel_l2(out[2], out[0], g)
+
+
+@pytest.mark.gpu
+def test_cheb_fft_not_used_where_the_length_does_not_factor():
+    """Ny - 1 = 34 has the factor 17: the FFT form is unavailable and the DNS keeps the matrix products."""
+    from channelflow_gb300 import DNS, build
+    from channelflow_gb300 import _lib as L
+    build.build()
+    lib = L.load()
+    g = O.Grid(16, 35, 16, *POISEUILLE_BOX)
+    fl = O.DNSFlags(nu=1 / 1000, dt=0.01, baseflow=O.LaminarBase)
+    u = np.ascontiguousarray(O.random_divfree_field(g, seed=5, norm=0.1))
+    L.check(lib.cfgpu_set_cheb_fft(2))
+    try:
+        d = DNS(u.copy(), to_cgrid(g), to_cflags(fl), precision="fp64")
+    finally:
+        L.check(lib.cfgpu_set_cheb_fft(1))
+    used = ctypes_int()
+    L.check(lib.cfgpu_dns_cheb_fft(d._h, used))
+    assert used.value == 0
+    d.close()
+
+
+def ctypes_int():
+    import ctypes
+    return ctypes.c_int(-1)
