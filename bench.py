@@ -254,6 +254,7 @@ def run_gpu(args, rank, world):
                 d.close()
                 outs[prec] = u
             acc[key] = l2norm(outs["mixed"] - outs["fp64"], NX, NZ) / l2norm(outs["fp64"], NX, NZ)
+        outs0_fp64 = outs["fp64"]
         acc["rel_l2_mixed_vs_fp64"] = acc["T10_dt0.005"]
         # The T = 10 figure is one trajectory of a chaotic flow: any change of rounding reshuffles it.  Two
         # more realizations from the initial field perturbed at 1e-15 (FP64 and mixed both rerun) state the
@@ -275,6 +276,24 @@ def run_gpu(args, rank, world):
                 outs[prec] = u
             reals.append(l2norm(outs["mixed"] - outs["fp64"], NX, NZ) / l2norm(outs["fp64"], NX, NZ))
         acc["T10_dt0.005_realizations"] = reals
+        # the mixed path with its Chebyshev transforms through the FFT (the matrix products are the mixed
+        # path's default where they are faster), same field and horizon
+        from channelflow_gb300 import _lib as L
+        lib = L.load()
+        u, q = u0.copy(), q0.copy()
+        fl = make_flags()
+        fl.dt = DT / 2
+        L.check(lib.cfgpu_set_cheb_fft(2))
+        try:
+            d = DNS(u, grid, fl, precision="mixed")
+        finally:
+            L.check(lib.cfgpu_set_cheb_fft(1))
+        d.set_fields(u, q)
+        d.advance_resident(2 * args.accuracy_steps)
+        d.get_fields(u, q)
+        d.close()
+        fp64_first = outs0_fp64
+        acc["T10_dt0.005_mixed_cheb_fft"] = l2norm(u - fp64_first, NX, NZ) / l2norm(fp64_first, NX, NZ)
         # Control: the same FP64 run from the initial field rounded to FP32 (one FP32 rounding of the input,
         # what the mixed path's first transform does) -- how far the flow itself carries a 2^-24 input change.
         u, q = u0.copy(), q0.copy()
@@ -290,6 +309,39 @@ def run_gpu(args, rank, world):
         acc["T10_dt0.005_fp64_from_fp32_rounded_input"] = l2norm(u - outs["fp64"], NX, NZ) / l2norm(outs["fp64"], NX,
                                                                                                       NZ)
     return results, acc, hbm, peak_kind
+
+
+def run_cheb_forms(args):
+    """The nonlinear term's Chebyshev transforms as dense matrix products and through the FFT, both
+    precisions, on the benchmark field: device ms per step and per nonlinear pass (CUDA events)."""
+    from channelflow_gb300 import DNS, Grid
+    from channelflow_gb300 import _lib as L
+    lib = L.load()
+    grid = Grid(NX, NY, NZ, LX, LZ)
+    u0 = initial_field(seed=1)
+    out = {}
+    for prec in ("mixed", "fp64"):
+        out[prec] = {}
+        for mode, name in ((0, "matrix"), (2, "fft")):
+            u, q = u0.copy(), np.zeros((1,) + u0.shape[1:], dtype=np.complex128)
+            L.check(lib.cfgpu_set_cheb_fft(mode))
+            try:
+                d = DNS(u, grid, make_flags(), precision=prec)
+            finally:
+                L.check(lib.cfgpu_set_cheb_fft(1))
+            if mode == 2 and not d.cheb_fft():
+                d.close()
+                continue
+            d.set_fields(u, q)
+            d.advance_resident(args.warmup)
+            K = max(3, args.steps // (4 if prec == "fp64" else 2))
+            d.set_profiling(True)
+            d.phase_times()
+            ms = d.advance_timed(K)
+            nl_ms, nl_n, _, _ = d.phase_times()
+            d.close()
+            out[prec][name] = {"step_ms": ms / K, "nl_avg_ms": nl_ms / max(1, nl_n), "steps": K}
+    return out
 
 
 def serve_requests(n, seed, horizon=(5.0, 50.0)):
@@ -606,6 +658,7 @@ def main():
     ap.add_argument("--newton-steps", type=int, default=3, help="mixed-precision Newton steps of the search "
                                                                  "block (0: skip the Newton block)")
     ap.add_argument("--newton-polish-steps", type=int, default=2)
+    ap.add_argument("--cheb-forms", type=int, default=1, help="matrix vs FFT Chebyshev transform block (0: skip)")
     args = ap.parse_args()
     if args.grid:
         global NX, NY, NZ
@@ -633,6 +686,7 @@ def main():
         return
 
     res, acc, hbm, peak_kind = run_gpu(args, rank, world)
+    forms = run_cheb_forms(args) if (args.cheb_forms and rank == 0) else None
     serve = run_serve(args) if (args.serve_requests > 0 and rank == 0) else None
     ens = run_ensemble(args) if (args.ensemble_fields > 0 and rank == 0) else None
     cfg0 = run_config0(args) if (args.config0 and rank == 0) else None
@@ -709,6 +763,7 @@ def main():
         "ensemble": ens,
         "config0": cfg0,
         "newton": newton,
+        "cheb_forms": forms,
     }
     print(json.dumps(line))
 

@@ -146,6 +146,13 @@ __device__ __forceinline__ float dither_const<float>(double x, int k) {
   return dither_round(x, k);
 }
 
+// Asynchronous 8-byte global -> shared copy (cp.async, no register staging); nbytes = 0 writes zeros.
+__device__ __forceinline__ void cp_async8(double* dst_smem, const double* src, int nbytes) {
+  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst_smem));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src), "r"(nbytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // 16-byte vector of R (LDS.128): four floats or two doubles.
 template <typename R>
 struct Vec16;

@@ -2913,6 +2913,11 @@ cfgpu_status cfgpu_set_fused_xz(int enable) {
   return CFGPU_OK;
 }
 
+cfgpu_status cfgpu_set_tau_segmented(int enable) {
+  set_tau_segmented(enable);
+  return CFGPU_OK;
+}
+
 cfgpu_status cfgpu_set_cheb_fft(int mode) {
   if (mode < 0 || mode > 2) return fail(CFGPU_EINVAL, "mode must be 0 (matrix), 1 (automatic) or 2 (FFT)");
   g_cheb_fft.store(mode);

@@ -132,9 +132,19 @@ enum TauField {
   TF_PBAND = 0, TF_PUP, TF_PLO, TF_PINV,  // pressure Helmholtz UL factors (lambda = kappa^2, nu = 1)
   TF_VBAND, TF_VUP, TF_VLO, TF_VINV,      // velocity Helmholtz UL factors (lambda, nu)
   TF_PP, TF_VP, TF_PM, TF_VM, TF_P0, TF_V0,
+  // segment products of the UL sweeps (tau_seg.cu; four segments of tau_seg_rows(N) rows per parity): H[n] =
+  // prod of -up over rows i .. the segment's top, G[n] = prod of -lo inv over the segment's first row .. i
+  TF_PH, TF_PG, TF_VH, TF_VG,
   TF_NFIELDS
 };
-enum TauScalar { TS_I00 = 0, TS_I01, TS_I10, TS_I11, TS_S0NB1, TS_S0NB, TS_UCMEAN, TS_LAMBDA, TS_NSCALARS };
+enum TauScalar {
+  TS_I00 = 0, TS_I01, TS_I10, TS_I11, TS_S0NB1, TS_S0NB, TS_UCMEAN, TS_LAMBDA,
+  TS_KXL, TS_KZL,      // 2 pi kx / Lx, 2 pi kz / Lz
+  TS_DX, TS_DZ,        // the same with the Nyquist modes' derivatives zero
+  TS_KAPPA2,           // 4 pi^2 ((kx / Lx)^2 + (kz / Lz)^2)
+  TS_RS0NB1, TS_RS0NB, // 1 / (1 - sigma0_Nb1), 1 / (1 - sigma0_Nb) (0 for the (0,0) mode)
+  TS_NSCALARS
+};
 
 struct TauTable {
   double* f;  // [TF_NFIELDS][N][Md]
@@ -195,6 +205,25 @@ struct SlotParams {
   int pad;
 };
 
+#ifdef __CUDACC__
+// A heterogeneous batch's per-field parameters over the launch-wide ones.
+__device__ __forceinline__ void apply_slot(SolveParams& sp, const SlotParams& s) {
+  sp.nu = s.nu;
+  sp.constraint = s.constraint;
+  sp.dPdxRef = s.dPdxRef;
+  sp.dPdzRef = s.dPdzRef;
+  sp.umean = s.umean;
+  sp.wmean = s.wmean;
+  sp.baseShear[0] = s.baseShear[0];
+  sp.baseShear[1] = s.baseShear[1];
+  if (sp.kind == 0) {
+    for (int j = 0; j < 4; ++j) sp.a[j] = s.a[j];
+  } else {
+    sp.lam = s.lam[sp.scheme][sp.substep];
+  }
+}
+#endif
+
 struct SolvePtrs {
   const double* uin[4];  // multistep history u_j (3 comps each, complex [3][N][Md])
   const void* nin[4];    // N_j (R-typed, [3][N][Md] complex)
@@ -214,6 +243,13 @@ struct SolvePtrs {
 
 // Kernel launches one launch_tau_solve makes for Ny = N (the right-hand-side kernel and the solve).
 int tau_solve_launches(int N);
+// Pressure / v and u / w passes of the step solve with segmented parity sweeps (tau_seg.cu), for
+// tau_seg_rows(N) <= 17 (rows per segment lane); the right-hand sides Rx, Rz, Ry in scratch lines 0, 1, 2.
+// set_tau_segmented(0) keeps the one-lane sweeps.
+__host__ __device__ inline int tau_seg_rows(int N) { return ((N + 1) / 2 + 3) / 4; }
+cudaError_t launch_tau_pvuw_seg(const GridDev& g, int N, const SolveParams& sp, const SolvePtrs& p,
+                                const HelmB& hb, TauTable tt, cudaStream_t st);
+void set_tau_segmented(int enable);
 template <typename R>
 cudaError_t launch_tau_solve(const GridDev& g, int N, const SolveParams& sp, const SolvePtrs& p, const HelmB& hb,
                              TauTable tt, cudaStream_t st);

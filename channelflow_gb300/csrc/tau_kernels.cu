@@ -14,16 +14,25 @@
 // Every per-mode quantity lives in global memory as a "line" of N values
 // with a fixed stride between consecutive Chebyshev indices, so a warp of
 // threads (consecutive modes) touches consecutive addresses at each step.
+#include <atomic>
 #include <type_traits>
 
 #include "kernels.h"
 
-// Asynchronous 8-byte global -> shared copy (cp.async, no register staging); nbytes = 0 writes zeros.
-__device__ __forceinline__ void cp_async8(double* dst_smem, const double* src, int nbytes) {
-  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst_smem));
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src), "r"(nbytes) : "memory");
+
+// Exact FP32 -> FP64 conversion by integer operations for zero and normal numbers (the conversion
+// instruction runs on the FP64 pipe, 64 cycles per warp instruction on GB300); subnormals, infinities and
+// NaNs take the conversion instruction.  FP64 values pass through.
+__device__ __forceinline__ double widen(double x) { return x; }
+__device__ __forceinline__ double widen(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned long long sgn = (unsigned long long)(u & 0x80000000u) << 32;
+  const unsigned e = (u >> 23) & 0xFFu;
+  if ((u & 0x7FFFFFFFu) == 0) return __longlong_as_double((long long)sgn);
+  if (e == 0 || e == 0xFFu) return (double)f;
+  const unsigned long long bits = sgn | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)bits);
 }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 struct Ln {
   double* p;
@@ -158,22 +167,6 @@ __device__ __forceinline__ int n_func(int k, int Nb) {
   return 2 * Nb;
 }
 
-__device__ __forceinline__ void apply_slot(SolveParams& sp, const SlotParams& s) {
-  sp.nu = s.nu;
-  sp.constraint = s.constraint;
-  sp.dPdxRef = s.dPdxRef;
-  sp.dPdzRef = s.dPdzRef;
-  sp.umean = s.umean;
-  sp.wmean = s.wmean;
-  sp.baseShear[0] = s.baseShear[0];
-  sp.baseShear[1] = s.baseShear[1];
-  if (sp.kind == 0) {
-    for (int j = 0; j < 4; ++j) sp.a[j] = s.a[j];
-  } else {
-    sp.lam = s.lam[sp.scheme][sp.substep];
-  }
-}
-
 // One thread per mode: the TauSolver constructor for lambda = lambda_t + nu kappa^2,
 // for modes m0 .. m0+mcount-1.
 // blockIdx.y selects one of tb's tables (its lambda_t; 4 scratch lines of its own).
@@ -242,6 +235,31 @@ __global__ void k_tau_setup(GridDev g, int N, TauSetupBatch tb, double nu, HelmB
   cheb_diff(N, scale, d, d3);
   const double s0Nb1 = lambda * V0[Nb - 1] + d2[Nb - 1] - nu * d3[Nb - 1];
   const double s0Nb = lambda * V0[Nb] + d2[Nb] - nu * d3[Nb];
+  // segment products of the UL sweeps of both factorisations (four segments of L rows per parity)
+  {
+    const int L = tau_seg_rows(N);
+    const HelmFac* fac[2] = {&PH, &VH};
+    Ln Hs[2] = {T(TF_PH), T(TF_VH)}, Gs[2] = {T(TF_PG), T(TF_VG)};
+    for (int f = 0; f < 2; ++f)
+      for (int q = 0; q < 2; ++q) {
+        const int M = q == 0 ? nE_of(N) : nO_of(N);
+        Hs[f][q] = 1.0;
+        Gs[f][q] = 1.0;
+        for (int i0 = 0; i0 < M; i0 += L) {
+          const int ia = i0 > 1 ? i0 : 1, ib = i0 + L < M ? i0 + L : M;
+          double h = 1.0;
+          for (int i = ib - 1; i >= ia; --i) {
+            h = -fac[f]->up[2 * i + q] * h;
+            Hs[f][2 * i + q] = h;
+          }
+          double gg = 1.0;
+          for (int i = ia; i < ib; ++i) {
+            gg = (-fac[f]->lo[2 * i + q] * gg) * fac[f]->inv[2 * i + q];
+            Gs[f][2 * i + q] = gg;
+          }
+        }
+      }
+  }
   // mean-constrained helper (helmholtz.cpp:193-205): mean of the solution of nu u'' - lambda u = nu
   for (int n = 0; n < N; ++n) z[n] = 0.0;
   z[0] = nu;
@@ -256,6 +274,13 @@ __global__ void k_tau_setup(GridDev g, int N, TauSetupBatch tb, double nu, HelmB
   s[TS_S0NB * Md] = s0Nb;
   s[TS_UCMEAN * Md] = ucmean;
   s[TS_LAMBDA * Md] = lambda;
+  s[TS_KXL * Md] = 2 * M_PI * kx / Lx;
+  s[TS_KZL * Md] = 2 * M_PI * kz / Lz;
+  s[TS_DX * Md] = 2 * M_PI * kx / Lx * (kx == g.kxmax ? 0.0 : 1.0);
+  s[TS_DZ * Md] = 2 * M_PI * kz / Lz * (kz == g.kzmax ? 0.0 : 1.0);
+  s[TS_KAPPA2 * Md] = kappa2;
+  s[TS_RS0NB1 * Md] = zero ? 0.0 : 1.0 / (1.0 - s0Nb1);
+  s[TS_RS0NB * Md] = zero ? 0.0 : 1.0 / (1.0 - s0Nb);
 }
 
 cudaError_t launch_tau_setup_batch(const GridDev& g, int N, const TauSetupBatch& tb, int ntab, double nu,
@@ -482,9 +507,10 @@ __global__ void __launch_bounds__(128) k_tau_solve(GridDev g, int N, SolveParams
       }
     }
   } else {
-    const double kappa2 = 4 * M_PI * M_PI * ((kx / g.Lx) * (kx / g.Lx) + (kz / g.Lz) * (kz / g.Lz));
-    const double Dx = 2 * M_PI * kx / g.Lx * (kx == g.kxmax ? 0.0 : 1.0);
-    const double Dz = 2 * M_PI * kz / g.Lz * (kz == g.kzmax ? 0.0 : 1.0);
+    // per-mode constants from the tables (no FP64 divisions here)
+    const double kappa2 = tt.s[TS_KAPPA2 * Md + m];
+    const double Dx = tt.s[TS_DX * Md + m];
+    const double Dz = tt.s[TS_DZ * Md + m];
     double* uin0 = const_cast<double*>(P.uin[0]);
     double* qin = const_cast<double*>(P.qin);
     for (int c = 0; c < 3; ++c) {
@@ -755,7 +781,7 @@ __device__ void helm_t(int M, int q, const double* __restrict__ hlo, const doubl
 // the scratch lines 0, 2 and 1 (the solve reads them back).
 // ---------------------------------------------------------------------------
 template <typename R>
-__global__ void __launch_bounds__(32) k_tau_rhs(GridDev g, int N, SolveParams sp, SolvePtrs P) {
+__global__ void __launch_bounds__(32) k_tau_rhs(GridDev g, int N, SolveParams sp, SolvePtrs P, TauTable tt) {
   extern __shared__ double sm[];
   const int lane = threadIdx.x;
   const int t = blockIdx.x * 32 + lane;
@@ -832,9 +858,10 @@ __global__ void __launch_bounds__(32) k_tau_rhs(GridDev g, int N, SolveParams sp
     }
   } else {
     constexpr int RB = TCH;  // loads in flight per batch of the streamed lines
-    const double kappa2 = 4 * M_PI * M_PI * ((kx / g.Lx) * (kx / g.Lx) + (kz / g.Lz) * (kz / g.Lz));
-    const double Dx = 2 * M_PI * kx / g.Lx * (kx == g.kxmax ? 0.0 : 1.0);
-    const double Dz = 2 * M_PI * kz / g.Lz * (kz == g.kzmax ? 0.0 : 1.0);
+    // per-mode constants from the tables (no FP64 divisions here)
+    const double kappa2 = tt.s[TS_KAPPA2 * Md + m];
+    const double Dx = tt.s[TS_DX * Md + m];
+    const double Dz = tt.s[TS_DZ * Md + m];
     const int c = cc;
     PLn uc = G(P.uin[0] + c * comp);
     PLn uo = Go(P.uin[0] + c * comp);
@@ -935,11 +962,11 @@ __global__ void __launch_bounds__(32) k_tau_rhs(GridDev g, int N, SolveParams sp
           // the nonlinear terms are combined at their own precision R (FP32 on the mixed path)
           double Nc;
           if (kind == 1) {
-            Nc = (double)(gN * nv[k] + zN * n1v[k]);
+            Nc = widen(gN * nv[k] + zN * n1v[k]);
           } else {
             const R Qn = n1v[k] * rA - nv[k];
             if (act) Q[(size_t)i * 2 * row] = Qn;
-            Nc = BC * (double)Qn;
+            Nc = BC * widen(Qn);
           }
           const bool n0 = n == 0;
           double rhs = fma(cu, uv[k], fma(n0 ? cd0 : cd, d2, fma(n0 ? cg0 : cg, gv, Nc)));
@@ -1260,11 +1287,29 @@ static size_t tau_t_smem(int N) {
 
 int tau_solve_launches(int N) { return tau_t_smem(N) <= 227 * 1024 ? 3 : 1; }
 
+static std::atomic<int> g_tau_seg{1};
+void set_tau_segmented(int enable) { g_tau_seg.store(enable ? 1 : 0); }
+
 template <typename R>
 cudaError_t launch_tau_solve(const GridDev& g, int N, const SolveParams& sp, const SolvePtrs& p, const HelmB& hb,
                              TauTable tt, cudaStream_t st) {
   const int M0 = (N - 1) / 2 + 1;
   const size_t smem_t = tau_t_smem(N);
+  if (g_tau_seg.load() != 0 && tau_seg_rows(N) <= 17) {
+    // right-hand side (one lane per parity sweep: its derivative recurrences cost twice the FP64 operations
+    // when segmented, and it is FP64-bound already), then the pressure / v and the u / w passes with
+    // segmented sweeps (tau_seg.cu)
+    static const bool attr = [] {
+      cudaFuncSetAttribute(k_tau_rhs<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+      return true;
+    }();
+    (void)attr;
+    const size_t smem_r = sizeof(double) * (((N + 1) & ~1) + (size_t)M0 * 32);
+    k_tau_rhs<R><<<dim3((4 * g.Md + 31) / 32, 3), 32, smem_r, st>>>(g, N, sp, p, tt);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return launch_tau_pvuw_seg(g, N, sp, p, hb, tt, st);
+  }
   if (smem_t <= 227 * 1024) {
     // kernel attributes set once per process (thread-safe static initialisation)
     static const bool attr = [] {
@@ -1276,7 +1321,7 @@ cudaError_t launch_tau_solve(const GridDev& g, int N, const SolveParams& sp, con
     }();
     (void)attr;
     const size_t smem_r = sizeof(double) * (((N + 1) & ~1) + (size_t)M0 * 32);
-    k_tau_rhs<R><<<dim3((4 * g.Md + 31) / 32, 3), 32, smem_r, st>>>(g, N, sp, p);
+    k_tau_rhs<R><<<dim3((4 * g.Md + 31) / 32, 3), 32, smem_r, st>>>(g, N, sp, p, tt);
     k_tau_solve_t<R><<<(4 * g.Md + 31) / 32, 32, smem_t, st>>>(g, N, sp, p, hb, tt);
     const size_t smem_u = sizeof(double) * ((size_t)M0 * 32 + (size_t)4 * N * 4);
     k_tau_uw<R><<<(8 * g.Md + 31) / 32, 32, smem_u, st>>>(g, N, sp, p, hb, tt);

@@ -270,6 +270,11 @@ cfgpu_status cfgpu_set_fused_xz(int enable);
  * arrays, the faster kept (cached per grid shape and precision); 2 the FFT wherever the grid allows.  Both
  * give the same results to rounding.  cfgpu_dns_cheb_fft reports a DNS's choice (1 FFT, 0 matrix). */
 cfgpu_status cfgpu_set_cheb_fft(int mode);
+/* No reference counterpart: the per-mode step solve (TauSolver::solve) runs its parity sweeps split over
+ * four lanes each (first-order recurrences joined across segments; the default, for Ny <= 135) or one lane
+ * per sweep (enable = 0).  Both give the same results to rounding.  Affects solves launched afterwards (a
+ * DNS captures its step graphs on its first steps). */
+cfgpu_status cfgpu_set_tau_segmented(int enable);
 cfgpu_status cfgpu_dns_cheb_fft(cfgpu_dns dns, int* fft);
 /* Host FlowField buffers: on devices whose kernels reach pageable host memory through the host page
  * tables (GB300 over NVLink-C2C), DNS objects created while enable != 0 (the default) read and write the
