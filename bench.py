@@ -449,6 +449,9 @@ def run_serve(args):
             "field_steps_per_s": stats["field_steps"] / makespan, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
             "p99_ms": 1e3 * float(np.percentile(lat, 99)),
             "vs_one_at_a_time_fp64": (len(reqs) / makespan) / (len(reqs) / t_alone),
+            "vs_one_at_a_time_same_precision": (len(reqs) / makespan) / (len(reqs) / t_alone_p),
+            # requests whose field blew up (non-finite) count in the makespan; the completed ones alone:
+            "blown_up": failed, "completed_per_s": (len(reqs) - failed) / makespan,
             "max_rel_l2_vs_alone_fp64": float(max(errs)) if errs else None,
             "median_rel_l2_vs_alone_fp64": float(np.median(errs)) if errs else None,
             "rel_l2_vs_alone_fp64_sorted": [float("%.2g" % e) for e in sorted(errs)],
