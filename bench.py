@@ -218,7 +218,7 @@ def run_gpu(args, rank, world):
         dns.set_profiling(False)
         results[prec] = dict(ms=ms, K=K, launches=launches, clocks=cs.summary(), nl_ms=nl_ms, nl_n=nl_n,
                              tau_ms=tau_ms, tau_n=tau_n, Md=dns.num_modes(), bytes=dns.device_bytes(),
-                             cheb_fft=dns.cheb_fft())
+                             cheb_fft=dns.cheb_fft(), cheb_tensor=dns.cheb_tensor())
         if True:
             # end-to-end through the public API: host buffers in, host buffers out, every step
             Ke = max(3, min(args.steps, 50))
@@ -294,6 +294,21 @@ def run_gpu(args, rank, world):
         d.close()
         fp64_first = outs0_fp64
         acc["T10_dt0.005_mixed_cheb_fft"] = l2norm(u - fp64_first, NX, NZ) / l2norm(fp64_first, NX, NZ)
+        # the mixed path with its forward Chebyshev transform as compensated FP32 matrix products (the tensor
+        # cores take it by default where they are faster)
+        u, q = u0.copy(), q0.copy()
+        L.check(lib.cfgpu_set_cheb_fft(0))
+        L.check(lib.cfgpu_set_cheb_tensor(0))
+        try:
+            d = DNS(u, grid, fl, precision="mixed")
+        finally:
+            L.check(lib.cfgpu_set_cheb_fft(1))
+            L.check(lib.cfgpu_set_cheb_tensor(CHEB_TENSOR_DEFAULT))
+        d.set_fields(u, q)
+        d.advance_resident(2 * args.accuracy_steps)
+        d.get_fields(u, q)
+        d.close()
+        acc["T10_dt0.005_mixed_matrix_forward"] = l2norm(u - fp64_first, NX, NZ) / l2norm(fp64_first, NX, NZ)
         # Control: the same FP64 run from the initial field rounded to FP32 (one FP32 rounding of the input,
         # what the mixed path's first transform does) -- how far the flow itself carries a 2^-24 input change.
         u, q = u0.copy(), q0.copy()
@@ -311,6 +326,9 @@ def run_gpu(args, rank, world):
     return results, acc, hbm, peak_kind
 
 
+CHEB_TENSOR_DEFAULT = 1  # the library's default mode of cfgpu_set_cheb_tensor
+
+
 def run_cheb_forms(args):
     """The nonlinear term's Chebyshev transforms as dense matrix products and through the FFT, both
     precisions, on the benchmark field: device ms per step and per nonlinear pass (CUDA events)."""
@@ -322,14 +340,17 @@ def run_cheb_forms(args):
     out = {}
     for prec in ("mixed", "fp64"):
         out[prec] = {}
-        for mode, name in ((0, "matrix"), (2, "fft")):
+        forms = ((0, 0, "matrix"), (2, 0, "fft")) + (((0, 2, "tensor_forward"),) if prec == "mixed" else ())
+        for mode, tc, name in forms:
             u, q = u0.copy(), np.zeros((1,) + u0.shape[1:], dtype=np.complex128)
             L.check(lib.cfgpu_set_cheb_fft(mode))
+            L.check(lib.cfgpu_set_cheb_tensor(tc))
             try:
                 d = DNS(u, grid, make_flags(), precision=prec)
             finally:
                 L.check(lib.cfgpu_set_cheb_fft(1))
-            if mode == 2 and not d.cheb_fft():
+                L.check(lib.cfgpu_set_cheb_tensor(CHEB_TENSOR_DEFAULT))
+            if (mode == 2 and not d.cheb_fft()) or (tc == 2 and not d.cheb_tensor()):
                 d.close()
                 continue
             d.set_fields(u, q)
@@ -729,7 +750,8 @@ def main():
                    "grid_point_steps_per_s": sps * NX * NY * NZ,
                    "l2": "no flush: per-step working set %.0f MB > 129 MB L2" % (m["bytes"] / 1e6),
                    "parallelism": "replicas" if world > 1 else "single",
-                   "cheb_transforms": "fft" if m["cheb_fft"] else "matrix"},
+                   "cheb_transforms": "fft" if m["cheb_fft"] else "matrix",
+                   "forward_cheb_on_tensor_cores": m["cheb_tensor"]},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm, "unit": "GB/s",
                      "frac": ach / hbm, "peak_source": peak_kind,
                      "traffic": NCU_TRAFFIC.get(dom) if (NX, NY, NZ) == (128, 97, 128) else None,

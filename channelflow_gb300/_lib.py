@@ -114,6 +114,8 @@ _SIGS = {
     "cfgpu_set_fused_xz": [C.c_int],
     "cfgpu_set_cheb_fft": [C.c_int],
     "cfgpu_set_tau_segmented": [C.c_int],
+    "cfgpu_set_cheb_tensor": [C.c_int],
+    "cfgpu_dns_cheb_tensor": [C.c_void_p, C.POINTER(C.c_int)],
     "cfgpu_dns_cheb_fft": [C.c_void_p, C.POINTER(C.c_int)],
     "cfgpu_dns_set_symmetries": [C.c_void_p, C.c_void_p, C.c_int, C.c_int],
     "cfgpu_dns_symmetry": [C.c_void_p, C.POINTER(SymmetryC), C.c_int],

@@ -611,6 +611,10 @@ struct cfgpu_dns_s {
   // Chebyshev transforms of the rotational form through the FFT (dct_table(Ny), R-typed): chosen at creation
   void* cdct = nullptr;
   bool ydct = false;
+  // forward Chebyshev transform of the mixed path on the tensor cores (cheb_tc_matrix(Ny), BF16 splits)
+  void* ctc = nullptr;
+  int* dtcerr = nullptr;
+  bool ytc = false;
   void *cinvA = nullptr, *cinvB = nullptr, *cfwdA = nullptr, *cfwdB = nullptr;
   void *cderA = nullptr, *cderB = nullptr, *basey = nullptr;  // fused curl: (2/L) T'_n(y_j); U, U', W, W' at y_j
   void *cdfA = nullptr, *cdfB = nullptr;                       // (2/L) diff o chebyfft, parity split
@@ -841,6 +845,13 @@ int nonlinear_impl(cfgpu_dns d, const double* U, void* Nout, int form) {
     d->launches += 3;
   }
   const R* F = (const R*)d->F3;
+  if constexpr (sizeof(R) == 4) {
+    if ((form == NL_ROTATIONAL || form == NL_CONVECTION) && d->ytc) {
+      CK(launch_cheb_tc(N, (int)row, 3, (const float*)F, row, comp, (float*)Nout, d->ctc, d->dtcerr, d->st));
+      d->launches += 1;
+      return CFGPU_OK;
+    }
+  }
   if (form == NL_ROTATIONAL && d->ydct) {
     CK(launch_dct<R>(N, false, g.Md, 3, (const cpx<R>*)F, row / 2, comp / 2, (cpx<R>*)Nout, row / 2, comp / 2,
                      (const cpx<R>*)d->cdct, d->st, dt));
@@ -1483,7 +1494,10 @@ std::map<TuneKey, std::pair<int, int>> g_tune_xz;
 
 template <typename R>
 int tune_xz(cfgpu_dns d) {
-  const GridDev& gp = d->gp;
+  // keyed and timed on one field's planes, so that a batch and a single field of the same grid take the same
+  // form (the forms agree to rounding, not bit for bit)
+  GridDev gp = d->gp;
+  gp.Ny = d->g.Ny;
   const TuneKey key{gp.Nx, gp.Ny, gp.Nz, gp.NKz, (int)sizeof(R), NL_ROTATIONAL};
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -1550,8 +1564,10 @@ int tune_cheb(cfgpu_dns d) {
     d->ydct = true;
     return CFGPU_OK;
   }
-  const GridDev& g = d->gm;
-  const TuneKey key{d->gp.Nx, d->gp.Ny, d->gp.Nz, d->gp.NKz, (int)sizeof(R), 100};
+  // keyed and timed on one field (its modes), so that a batch and a single field take the same form
+  GridDev g = d->gm;
+  g.Md = d->g.Md;
+  const TuneKey key{d->g.Nx, d->g.Ny, d->g.Nz, d->g.NKz, (int)sizeof(R), 100};
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune_cheb.find(key);
@@ -1562,6 +1578,7 @@ int tune_cheb(cfgpu_dns d) {
   }
   const int N = d->N;
   const size_t row = d->rowc(), comp = d->compc();
+  const int nl1 = 2 * d->g.Md;  // one field's real lines
   R* C6 = (R*)d->C6;
   R* W = (R*)d->W6;
   const float tdense = time_ms<R>(d, [&]() {
@@ -1572,11 +1589,11 @@ int tune_cheb(cfgpu_dns d) {
     } else {
       e = launch_curl_base<R>(g, d->Ucur, C6, d->dUbase, d->dWbase, 0, 0.0, d->st);
       if (e == cudaSuccess)
-        e = launch_cheb<R, R, R>(N, true, (int)row, 6, C6, row, comp, W, row, comp, (const R*)d->cinvA,
+        e = launch_cheb<R, R, R>(N, true, nl1, 6, C6, row, comp, W, row, comp, (const R*)d->cinvA,
                                  (const R*)d->cinvB, d->st);
     }
     if (e == cudaSuccess)
-      e = launch_cheb<R, R, R>(N, false, (int)row, 3, (const R*)d->F3, row, comp, C6, row, comp, (const R*)d->cfwdA,
+      e = launch_cheb<R, R, R>(N, false, nl1, 3, (const R*)d->F3, row, comp, C6, row, comp, (const R*)d->cfwdA,
                                (const R*)d->cfwdB, d->st);
     return e;
   });
@@ -1594,6 +1611,46 @@ int tune_cheb(cfgpu_dns d) {
   CK(cudaStreamSynchronize(d->st));
   std::lock_guard<std::mutex> lk(g_tune_mu);
   g_tune_cheb[key] = d->ydct ? 1 : 0;
+  return CFGPU_OK;
+}
+
+// Forward Chebyshev transform of the mixed path on the tensor cores or as compensated FP32 matrix products:
+// mode 0 never, 1 timed on the DNS's own arrays (cached per grid shape), 2 wherever supported.
+std::atomic<int> g_cheb_tc{1};
+std::map<TuneKey, int> g_tune_tc;
+
+int tune_cheb_tc(cfgpu_dns d) {
+  d->ytc = false;
+  const int mode = g_cheb_tc.load();
+  if (mode == 0 || !d->ctc || d->ydct) return CFGPU_OK;
+  if (mode == 2) {
+    d->ytc = true;
+    return CFGPU_OK;
+  }
+  const TuneKey key{d->g.Nx, d->g.Ny, d->g.Nz, d->g.NKz, 4, 101};  // one field's grid (see tune_cheb)
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune_tc.find(key);
+    if (it != g_tune_tc.end()) {
+      d->ytc = it->second != 0;
+      return CFGPU_OK;
+    }
+  }
+  const int N = d->N;
+  const size_t row = d->rowc(), comp = d->compc();
+  float* out = (float*)d->C6;
+  const int nl1 = 2 * d->g.Md;  // one field's real lines
+  const float tm = time_ms<float>(d, [&]() {
+    return launch_cheb<float, float, float>(N, false, nl1, 3, (const float*)d->F3, row, comp, out, row, comp,
+                                            (const float*)d->cfwdA, (const float*)d->cfwdB, d->st);
+  });
+  const float tt = time_ms<float>(d, [&]() {
+    return launch_cheb_tc(N, nl1, 3, (const float*)d->F3, row, comp, out, d->ctc, d->dtcerr, d->st);
+  });
+  d->ytc = tt < 1e30f && tt < tm;
+  CK(cudaStreamSynchronize(d->st));
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune_tc[key] = d->ytc ? 1 : 0;
   return CFGPU_OK;
 }
 
@@ -1802,6 +1859,21 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
     d->twxf = c0 + off[13];
     d->twzf = c0 + off[14];
     if (dct_supported(Ny)) d->cdct = c0 + off[15];
+    if (cheb_tc_supported(Ny)) {
+      // full forward matrix F[n][j] = w_j cos(pi n j / (N-1)) c_n / (N-1) (chebyfft), four BF16 splits
+      std::vector<double> Fm((size_t)Ny * Ny);
+      for (int n = 0; n < Ny; ++n)
+        for (int j = 0; j < Ny; ++j) {
+          const long double cn = (n == 0 || n == Ny - 1) ? 0.5L : 1.0L;
+          const long double w = (j == 0 || j == Ny - 1) ? 1.0L : 2.0L;
+          Fm[(size_t)n * Ny + j] = (double)(w * cospi_ratio((long long)n * j, Ny - 1) * cn / (Ny - 1));
+        }
+      const std::vector<uint16_t> tcm = cheb_tc_matrix(Fm, Ny);
+      CKS(dalloc(&d->ctc, tcm.size() * sizeof(uint16_t), B));
+      CK(cudaMemcpyAsync(d->ctc, tcm.data(), tcm.size() * sizeof(uint16_t), cudaMemcpyHostToDevice, d->st));
+      CKS(dalloc(&d->dtcerr, 1, B));
+      CK(cudaMemsetAsync(d->dtcerr, 0, sizeof(int), d->st));
+    }
     d->cS = (long long)(S * sizeof(float));
     CKS(upload_dithered({basey}, {0}, basey.size(), &d->basey, B, d->st));
   }
@@ -1856,6 +1928,7 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
   if (rot && g_fused_xz.load() != 0 && xz_fused_supported(d->gp)) CKS(fp64 ? tune_xz<double>(d) : tune_xz<float>(d));
   // Chebyshev transforms of the rotational form: dense or through the FFT
   if (rot) CKS(fp64 ? tune_cheb<double>(d) : tune_cheb<float>(d));
+  if (!fp64 && (rot || f.nonlinearity == CFGPU_Convection)) CKS(tune_cheb_tc(d));
 
   // schemes (DNS::DNS, dns.cpp:22-39)
   CKS(setup_scheme(d->main, f.timestepping, f.dt));
@@ -1916,7 +1989,7 @@ void dns_free(cfgpu_dns d) {
     d->twx = d->twz = d->cinvA = d->cinvB = d->cfwdA = d->cfwdB = d->cderA = d->cderB = d->cdfA = d->cdfB = nullptr;
     d->twxf = d->twzf = d->cdct = nullptr;
   }
-  F(d->twxf); F(d->twzf); F(d->cdct);
+  F(d->twxf); F(d->twzf); F(d->cdct); F(d->ctc); F(d->dtcerr);
   F(d->dUbase); F(d->dWbase); F(d->dUbaseyy); F(d->dWbaseyy); F(d->ddPdx);
   F(d->hb_lo); F(d->hb_di); F(d->hb_up);
   F(d->twx); F(d->twz); F(d->cinvA); F(d->cinvB); F(d->cfwdA); F(d->cfwdB);
@@ -2918,6 +2991,20 @@ cfgpu_status cfgpu_set_tau_segmented(int enable) {
   return CFGPU_OK;
 }
 
+cfgpu_status cfgpu_set_cheb_tensor(int mode) {
+  if (mode < 0 || mode > 2) return fail(CFGPU_EINVAL, "mode must be 0 (never), 1 (timed) or 2 (always)");
+  g_cheb_tc.store(mode);
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune_tc.clear();
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_dns_cheb_tensor(cfgpu_dns dns, int* on) {
+  if (!dns || !on) return fail(CFGPU_EINVAL, "null argument");
+  *on = dns->ytc ? 1 : 0;
+  return CFGPU_OK;
+}
+
 cfgpu_status cfgpu_set_cheb_fft(int mode) {
   if (mode < 0 || mode > 2) return fail(CFGPU_EINVAL, "mode must be 0 (matrix), 1 (automatic) or 2 (FFT)");
   g_cheb_fft.store(mode);
@@ -2939,6 +3026,7 @@ cfgpu_status cfgpu_set_autotune(int enable) {
     g_tune.clear();
     g_tune_xz.clear();
     g_tune_cheb.clear();
+    g_tune_tc.clear();
   }
   return CFGPU_OK;
 }

@@ -2,6 +2,7 @@
 // the host runtime (not part of the public C ABI).
 #pragma once
 
+#include <cstdint>
 #include <string>
 #include <vector>
 
@@ -46,6 +47,13 @@ template <typename TI, typename R, typename TO>
 cudaError_t launch_cheb(int N, bool inverse, int nlines, int ncomp, const TI* in, size_t ld_in, size_t cs_in, TO* out,
                         size_t ld_out, size_t cs_out, const R* A, const R* B, cudaStream_t st,
                         const Dither& dt = kNoDither);
+
+// Forward Chebyshev transform of FP32 lines on the tensor cores (cheb_tc.cu), N <= 128: Ag = cheb_tc_matrix
+// (four BF16 splits of the N x N forward matrix, uploaded); err: device flag set if an MMA wait timed out.
+bool cheb_tc_supported(int N);
+std::vector<uint16_t> cheb_tc_matrix(const std::vector<double>& F, int N);
+cudaError_t launch_cheb_tc(int N, int nlines, int ncomp, const float* in, size_t ld, size_t cs, float* out,
+                           const void* Ag, int* err, cudaStream_t st);
 
 // Nonlinear forms (values of the reference's NonlinearMethod enum, dnsflags.h:28-35)
 enum { NL_ROTATIONAL = 0, NL_CONVECTION = 1, NL_DIVERGENCE = 2, NL_SKEW = 3 };

@@ -133,6 +133,12 @@ class DNS:
         L.check(self._lib.cfgpu_dns_cheb_fft(self._h, C.byref(v)))
         return bool(v.value)
 
+    def cheb_tensor(self) -> bool:
+        """True when the mixed path's forward Chebyshev transform runs on the tensor cores."""
+        v = C.c_int()
+        L.check(self._lib.cfgpu_dns_cheb_tensor(self._h, C.byref(v)))
+        return bool(v.value)
+
     def advance_timed(self, nsteps: int) -> float:
         """Resident advance bracketed by CUDA events on the library's stream; device milliseconds."""
         ms = C.c_double()

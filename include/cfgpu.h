@@ -275,6 +275,13 @@ cfgpu_status cfgpu_set_cheb_fft(int mode);
  * per sweep (enable = 0).  Both give the same results to rounding.  Affects solves launched afterwards (a
  * DNS captures its step graphs on its first steps). */
 cfgpu_status cfgpu_set_tau_segmented(int enable);
+/* No reference counterpart: the mixed path's forward Chebyshev transform (rotational and convection forms,
+ * Ny <= 128) on the tensor cores (BF16 splits of the FP32 data and of the constant matrix, FP32 accumulation)
+ * instead of compensated FP32 matrix products.  For DNS objects created afterwards: mode 0 never, 1 (the
+ * default) timed against the matrix products at creation (cached per grid shape), 2 always.
+ * cfgpu_dns_cheb_tensor reports a DNS's choice. */
+cfgpu_status cfgpu_set_cheb_tensor(int mode);
+cfgpu_status cfgpu_dns_cheb_tensor(cfgpu_dns dns, int* on);
 cfgpu_status cfgpu_dns_cheb_fft(cfgpu_dns dns, int* fft);
 /* Host FlowField buffers: on devices whose kernels reach pageable host memory through the host page
  * tables (GB300 over NVLink-C2C), DNS objects created while enable != 0 (the default) read and write the

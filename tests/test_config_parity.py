@@ -66,18 +66,20 @@ def oracle_result(name):
 
 
 def gpu_run(u0, g, fl, nsteps, precision, cheb=1):
-    """cheb: Chebyshev transforms of the nonlinear term as matrix products (0), the faster of the two (1),
-    or through the FFT (2)."""
+    """cheb: Chebyshev transforms of the nonlinear term as matrix products on the CUDA cores (0), the library's
+    timed choice (1), or through the FFT (2)."""
     from channelflow_gb300 import DNS
     from channelflow_gb300 import _lib as L
     lib = L.load()
     u = np.ascontiguousarray(u0.copy())
     q = np.zeros((1,) + u.shape[1:], complex)
     L.check(lib.cfgpu_set_cheb_fft(cheb))
+    L.check(lib.cfgpu_set_cheb_tensor(1 if cheb == 1 else 0))
     try:
         dns = DNS(u, to_cgrid(g), to_cflags(fl), precision=precision)
     finally:
         L.check(lib.cfgpu_set_cheb_fft(1))
+        L.check(lib.cfgpu_set_cheb_tensor(1))
     dns.advance(u, q, nsteps)
     return u, dns
 
