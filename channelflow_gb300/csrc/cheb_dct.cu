@@ -252,12 +252,12 @@ __global__ void __launch_bounds__(256) k_curl_coef(GridDev g, int N, const doubl
     const cpx<double> oy = cmk(-dz * u.y + dx * w.y, dz * u.x - dx * w.x);
     const cpx<double> oz = cmk(-dx * v.y - Du.x, dx * v.x - Du.y);
     R* o = C6 + n * orow + 2 * (size_t)m;
-    o[0] = narrow<R>(u.x); o[1] = narrow<R>(u.y);
-    o[ocomp] = narrow<R>(v.x); o[ocomp + 1] = narrow<R>(v.y);
-    o[2 * ocomp] = narrow<R>(w.x); o[2 * ocomp + 1] = narrow<R>(w.y);
-    o[3 * ocomp] = narrow<R>(ox.x); o[3 * ocomp + 1] = narrow<R>(ox.y);
-    o[4 * ocomp] = narrow<R>(oy.x); o[4 * ocomp + 1] = narrow<R>(oy.y);
-    o[5 * ocomp] = narrow<R>(oz.x); o[5 * ocomp + 1] = narrow<R>(oz.y);
+    o[0] = (R)u.x; o[1] = (R)u.y;
+    o[ocomp] = (R)v.x; o[ocomp + 1] = (R)v.y;
+    o[2 * ocomp] = (R)w.x; o[2 * ocomp + 1] = (R)w.y;
+    o[3 * ocomp] = (R)ox.x; o[3 * ocomp + 1] = (R)ox.y;
+    o[4 * ocomp] = (R)oy.x; o[4 * ocomp + 1] = (R)oy.y;
+    o[5 * ocomp] = (R)oz.x; o[5 * ocomp + 1] = (R)oz.y;
   }
 }
 

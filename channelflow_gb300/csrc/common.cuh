@@ -146,29 +146,6 @@ __device__ __forceinline__ float dither_const<float>(double x, int k) {
   return dither_round(x, k);
 }
 
-// FP64 -> R with round-to-nearest-even.  For FP32 the conversion instruction runs on the FP64 pipe (64 cycles
-// per warp instruction on GB300); zero and results in the normal FP32 range are rounded here by integer
-// operations (bit-identical to the conversion), the rest (subnormal results, overflow, NaN) take the instruction.
-template <typename R>
-__device__ __forceinline__ R narrow(double x);
-template <>
-__device__ __forceinline__ double narrow<double>(double x) {
-  return x;
-}
-template <>
-__device__ __forceinline__ float narrow<float>(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
-  if ((b & 0x7FFFFFFFFFFFFFFFull) == 0) return __uint_as_float(sign);
-  const int ef = (int)((b >> 52) & 0x7FF) - 1023 + 127;
-  if (ef <= 0 || ef >= 255) return (float)x;
-  const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
-  unsigned mr = (unsigned)(m >> 29);
-  const unsigned rem = (unsigned)(m & 0x1FFFFFFFull);
-  mr += (rem > 0x10000000u || (rem == 0x10000000u && (mr & 1u))) ? 1u : 0u;
-  return __uint_as_float((sign | ((unsigned)ef << 23)) + mr);  // a mantissa carry raises the exponent
-}
-
 // Asynchronous 8-byte global -> shared copy (cp.async, no register staging); nbytes = 0 writes zeros.
 __device__ __forceinline__ void cp_async8(double* dst_smem, const double* src, int nbytes) {
   const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst_smem));

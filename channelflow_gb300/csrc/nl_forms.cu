@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(256) k_grad_cheb(GridDev g, int N, const doubl
   for (int i = tid; i < 3 * N * GC_TL; i += blockDim.x) {
     const int l = i % GC_TL, n = (i / GC_TL) % N, c = i / (GC_TL * N);
     const int gl = l0 + l;
-    const R v = gl < nlines ? narrow<R>(U[c * comp + (size_t)n * row + gl]) : (R)0;
+    const R v = gl < nlines ? (R)U[c * comp + (size_t)n * row + gl] : (R)0;
     const int r = (n & 1) ? KAp + (n >> 1) : (n >> 1);
     xs[(c * NP + r) * GC_TL + l] = v;
   }

@@ -318,7 +318,7 @@ __global__ void __launch_bounds__(256) k_curl_cheb(GridDev g, int N, const doubl
       const double* uc = U + c * comp + gl;
 #pragma unroll 4
       for (int n = warp; n < N; n += 8) {
-        const R v = ok ? narrow<R>(uc[(size_t)n * row]) : (R)0;
+        const R v = ok ? (R)uc[(size_t)n * row] : (R)0;
         const int r = (n & 1) ? KAp + (n >> 1) : (n >> 1);
         xs[(c * NP + r) * CC_TL + lane] = v;
       }
