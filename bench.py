@@ -184,6 +184,18 @@ def fp64_peak():
     return tf.value, cyc.value
 
 
+def pin_forms(args, prec):
+    """Chebyshev forms of the DNS objects created next: the library's timed choice unless pinned on the command
+    line (profiling runs pin the timed run's choices, since timing under a profiler can choose differently);
+    prec None restores the defaults."""
+    from channelflow_gb300 import _lib as L
+    lib = L.load()
+    fft = {"mixed": args.cheb_fft_mixed, "fp64": args.cheb_fft_fp64}.get(prec, -1)
+    L.check(lib.cfgpu_set_cheb_fft(1 if fft < 0 else fft))
+    L.check(lib.cfgpu_set_cheb_tensor(CHEB_TENSOR_DEFAULT if (prec is None or args.cheb_tensor < 0) else
+                                      args.cheb_tensor))
+
+
 def run_gpu(args, rank, world):
     import ctypes  # noqa: F401
     from channelflow_gb300 import DNS, Grid
@@ -202,6 +214,7 @@ def run_gpu(args, rank, world):
     hbm, peak_kind = peaks()
     for prec in ("mixed", "fp64"):
         u, q = u0.copy(), q0.copy()
+        pin_forms(args, prec)
         dns = DNS(u, grid, make_flags(), precision=prec)
         dns.set_fields(u, q)
         dns.advance_resident(args.warmup)
@@ -224,6 +237,7 @@ def run_gpu(args, rank, world):
             Ke = max(3, min(args.steps, 50))
             ue, qe = u0.copy(), q0.copy()
             dns_e = DNS(ue, grid, make_flags(), precision=prec)
+            pin_forms(args, None)
             dns_e.advance(ue, qe, args.warmup)
             barrier()
             t0 = time.perf_counter()
@@ -683,6 +697,10 @@ def main():
                                                                  "block (0: skip the Newton block)")
     ap.add_argument("--newton-polish-steps", type=int, default=2)
     ap.add_argument("--cheb-forms", type=int, default=1, help="matrix vs FFT Chebyshev transform block (0: skip)")
+    ap.add_argument("--cheb-fft-mixed", type=int, default=-1, help="pin cfgpu_set_cheb_fft for the mixed DNS "
+                                                                    "(-1: timed choice)")
+    ap.add_argument("--cheb-fft-fp64", type=int, default=-1, help="pin cfgpu_set_cheb_fft for the FP64 DNS")
+    ap.add_argument("--cheb-tensor", type=int, default=-1, help="pin cfgpu_set_cheb_tensor (-1: timed choice)")
     args = ap.parse_args()
     if args.grid:
         global NX, NY, NZ

@@ -62,13 +62,6 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t mbar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bytes of the shared region holding the constant matrix (all splits) and, after the MMAs, the output rows.
-__host__ __device__ constexpr size_t tc_region_a(int KS) {
-  return (size_t)2 * TC_ASPLIT * TC_M * 16 * KS > (size_t)4 * TC_M * (TC_NT + 1)
-             ? (size_t)2 * TC_ASPLIT * TC_M * 16 * KS
-             : (size_t)4 * TC_M * (TC_NT + 1);
-}
-
 // 4-byte asynchronous global -> shared copy; nbytes = 0 writes zero.
 __device__ __forceinline__ void cp_async4(void* dst_smem, const void* src, int nbytes) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(smem_u32(dst_smem)), "l"(src), "r"(nbytes)
@@ -83,22 +76,23 @@ __device__ __forceinline__ void two_sum_c(float& s, float t, float& c) {
   s = s1;
 }
 
+// Persistent: one CTA per SM loads the constant matrix once (bulk copy) and walks the tiles (64 lines of one
+// component) with stride gridDim.x; the next tile's FP32 lines are copied (cp.async) while the current one is
+// split, multiplied and written.  Shared memory: constant matrix, BF16 tile, two FP32 tiles (the current one
+// also stages the output rows, XOR-swizzled), barriers.
 __global__ void __launch_bounds__(TC_THREADS, 1)
-    k_cheb_tc(int N, int KS, int nlines, const float* __restrict__ in, size_t ld, size_t cs,
+    k_cheb_tc(int N, int KS, int nlines, int ncomp, const float* __restrict__ in, size_t ld, size_t cs,
               float* __restrict__ out, const __nv_bfloat16* __restrict__ Ag, int* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int KP = 16 * KS;                       // padded K
   const int asz = TC_M * KP, bsz = TC_NT * KP;  // elements per split
   __nv_bfloat16* As = reinterpret_cast<__nv_bfloat16*>(smem_raw);
-  // the constant matrix's region also stages the output rows: at least 128 x 65 floats
-  __nv_bfloat16* Bs = reinterpret_cast<__nv_bfloat16*>(smem_raw + tc_region_a(KS));
-  float* Xs = reinterpret_cast<float*>(Bs + TC_BSPLIT * bsz);  // [KP][64] FP32 tile
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(Xs + KP * TC_NT);  // [0]: constant matrix copied, [1]: MMAs done
+  __nv_bfloat16* Bs = As + TC_ASPLIT * asz;
+  float* Xs = reinterpret_cast<float*>(Bs + TC_BSPLIT * bsz);  // [2][KP][64] FP32 tiles
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(Xs + 2 * KP * TC_NT);  // [0]: constant matrix, [1]: MMAs done
   uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 2);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int l0 = blockIdx.x * TC_NT;
-  in += blockIdx.y * cs;
-  out += blockIdx.y * cs;
+  const int tpc = (nlines + TC_NT - 1) / TC_NT, ntiles = tpc * ncomp;
   const uint32_t abytes = (uint32_t)(TC_ASPLIT * asz * 2);
 
   if (tid == 0) {
@@ -125,134 +119,156 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           : "memory");
     }
   }
-  // this tile's FP32 lines, all copies in flight (zero past the last line and in the K padding)
-  for (int i = tid; i < KP * TC_NT; i += TC_THREADS) {
-    const int k = i / TC_NT, c = i - k * TC_NT;
-    const bool ok = k < N && l0 + c < nlines;
-    cp_async4(Xs + i, ok ? in + (size_t)k * ld + l0 + c : in, ok ? 4 : 0);
+  // FP32 lines of a tile into X, all copies in flight (zero past the last line and in the K padding)
+  auto issue = [&](int tile, float* X) {
+    const int comp = tile / tpc, l0 = (tile - comp * tpc) * TC_NT;
+    const float* src = in + comp * cs;
+    for (int i = tid; i < KP * TC_NT; i += TC_THREADS) {
+      const int k = i / TC_NT, c = i - k * TC_NT;
+      const bool okc = k < N && l0 + c < nlines;
+      cp_async4(X + i, okc ? src + (size_t)k * ld + l0 + c : src, okc ? 4 : 0);
+    }
+  };
+  const uint32_t tmem = *tslot;
+  if (blockIdx.x < ntiles) issue(blockIdx.x, Xs);
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+  bool ok = true;
+  int it = 0;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
+    float* X = Xs + (it & 1) * KP * TC_NT;
+    if (t + (int)gridDim.x < ntiles) issue(t + gridDim.x, Xs + ((it + 1) & 1) * KP * TC_NT);
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    asm volatile("cp.async.wait_group 1;\n" ::: "memory");  // this tile's copies have landed
+    __syncthreads();
+    // split every value into three BF16 parts in the operand layout: a thread takes one line and eight
+    // consecutive k (one 16-byte core-matrix row per split)
+    for (int i = tid; i < (KP / 8) * TC_NT; i += TC_THREADS) {
+      const int kg = i / TC_NT, c = i - kg * TC_NT;
+      uint32_t p1[4], p2[4], p3[4];
+#pragma unroll
+      for (int e = 0; e < 8; e += 2) {
+        __nv_bfloat16 b1[2], b2[2], b3[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const float x = X[(8 * kg + e + h) * TC_NT + c];
+          b1[h] = __float2bfloat16_rn(x);
+          const float r1 = x - __bfloat162float(b1[h]);
+          b2[h] = __float2bfloat16_rn(r1);
+          b3[h] = __float2bfloat16_rn(r1 - __bfloat162float(b2[h]));
+        }
+        p1[e >> 1] = (uint32_t)__bfloat16_as_ushort(b1[0]) | ((uint32_t)__bfloat16_as_ushort(b1[1]) << 16);
+        p2[e >> 1] = (uint32_t)__bfloat16_as_ushort(b2[0]) | ((uint32_t)__bfloat16_as_ushort(b2[1]) << 16);
+        p3[e >> 1] = (uint32_t)__bfloat16_as_ushort(b3[0]) | ((uint32_t)__bfloat16_as_ushort(b3[1]) << 16);
+      }
+      const int o = kmaj_off(c, 8 * kg, TC_NT);
+      *reinterpret_cast<uint4*>(Bs + o) = make_uint4(p1[0], p1[1], p1[2], p1[3]);
+      *reinterpret_cast<uint4*>(Bs + bsz + o) = make_uint4(p2[0], p2[1], p2[2], p2[3]);
+      *reinterpret_cast<uint4*>(Bs + 2 * bsz + o) = make_uint4(p3[0], p3[1], p3[2], p3[3]);
+    }
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (tid == 0) {
+      if (it == 0) {
+        bool got = false;
+        for (int w = 0; w < (1 << 20); ++w)
+          if (mbar_try_wait(smem_u32(mbar), 0)) {
+            got = true;
+            break;
+          }
+        if (!got) {
+          ok = false;
+          if (err) atomicExch(err, 1);
+        }
+      }
+      if (ok) {
+        // D f32, A and B BF16, both K-major, N = 64, M = 128
+        const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TC_NT >> 3) << 17) |
+                               ((uint32_t)(TC_M >> 4) << 24);
+        // one accumulator (64 TMEM columns) per K slice; the products Fi xj (i + j <= 5) smallest first, so the
+        // leading product is added last to the slice's sum
+        const int pa[TC_NPROD] = {1, 2, 3, 0, 1, 2, 0, 1, 0};
+        const int pb[TC_NPROD] = {2, 1, 0, 2, 1, 0, 1, 0, 0};
+        const uint32_t a0 = smem_u32(As), b0 = smem_u32(Bs);
+        for (int ks = 0; ks < KS; ++ks)
+          for (int p = 0; p < TC_NPROD; ++p) {
+            const uint64_t da = umma_desc(a0 + 2u * (uint32_t)(pa[p] * asz + ks * TC_M * 16), 128, 256);
+            const uint64_t db = umma_desc(b0 + 2u * (uint32_t)(pb[p] * bsz + ks * TC_NT * 16), 128, 256);
+            mma_bf16(tmem + (uint32_t)(ks * TC_NT), da, db, idesc, p != 0);
+          }
+      }
+      // arrive on the MMA barrier in every case (after the MMAs when they were issued)
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                       smem_u32(mbar + 1))
+                   : "memory");
+    }
+    bool done = false;
+    for (int w = 0; w < (1 << 20); ++w)
+      if (mbar_try_wait(smem_u32(mbar + 1), (uint32_t)(it & 1))) {
+        done = true;
+        break;
+      }
+    if (!done && err) atomicExch(err, 1);
+    ok = __syncthreads_and(ok && done) != 0;
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (its sub-partition's) and columns 16 (w / 4) .. + 15;
+    // the K-slice sums are combined with error-free two-sums and the rows staged over this tile's FP32 lines
+    // (row r, column c at r 64 + (c ^ (r mod 32)): conflict-free both ways)
+    float* Os = X;
+    const int n = 32 * (warp & 3) + lane;
+    {
+      const int cb = 16 * (warp >> 2);
+      float sum[16], cmp[16];
+#pragma unroll
+      for (int j = 0; j < 16; ++j) sum[j] = cmp[j] = 0.0f;
+#pragma unroll 1
+      for (int ks = 0; ks < KS; ++ks) {
+        uint32_t v[16];
+        const uint32_t ta = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(ks * TC_NT + cb);
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+            "%14, %15}, [%16];\n"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+            : "r"(ta));
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+        for (int j = 0; j < 16; ++j) two_sum_c(sum[j], __uint_as_float(v[j]), cmp[j]);
+      }
+      if (n < N) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) Os[n * TC_NT + ((cb + j) ^ (n & 31))] = sum[j] + cmp[j];
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (ok) {
+      const int comp = t / tpc, l0 = (t - comp * tpc) * TC_NT;
+      float* dst = out + comp * cs;
+      for (int i = tid; i < N * TC_NT; i += TC_THREADS) {
+        const int r = i / TC_NT, c = i - r * TC_NT;
+        if (l0 + c < nlines) dst[(size_t)r * ld + l0 + c] = Os[r * TC_NT + (c ^ (r & 31))];
+      }
+    }
+    __syncthreads();
   }
   asm volatile("cp.async.wait_all;\n" ::: "memory");
   __syncthreads();
-  // split every value into three BF16 parts in the operand layout: a thread takes one line and eight
-  // consecutive k (one 16-byte core-matrix row per split)
-  for (int i = tid; i < (KP / 8) * TC_NT; i += TC_THREADS) {
-    const int kg = i / TC_NT, c = i - kg * TC_NT;
-    uint32_t p1[4], p2[4], p3[4];
-#pragma unroll
-    for (int e = 0; e < 8; e += 2) {
-      float x[2];
-      __nv_bfloat16 b1[2], b2[2], b3[2];
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        x[h] = Xs[(8 * kg + e + h) * TC_NT + c];
-        b1[h] = __float2bfloat16_rn(x[h]);
-        const float r1 = x[h] - __bfloat162float(b1[h]);
-        b2[h] = __float2bfloat16_rn(r1);
-        b3[h] = __float2bfloat16_rn(r1 - __bfloat162float(b2[h]));
-      }
-      p1[e >> 1] = (uint32_t)__bfloat16_as_ushort(b1[0]) | ((uint32_t)__bfloat16_as_ushort(b1[1]) << 16);
-      p2[e >> 1] = (uint32_t)__bfloat16_as_ushort(b2[0]) | ((uint32_t)__bfloat16_as_ushort(b2[1]) << 16);
-      p3[e >> 1] = (uint32_t)__bfloat16_as_ushort(b3[0]) | ((uint32_t)__bfloat16_as_ushort(b3[1]) << 16);
-    }
-    const int o = kmaj_off(c, 8 * kg, TC_NT);
-    *reinterpret_cast<uint4*>(Bs + o) = make_uint4(p1[0], p1[1], p1[2], p1[3]);
-    *reinterpret_cast<uint4*>(Bs + bsz + o) = make_uint4(p2[0], p2[1], p2[2], p2[3]);
-    *reinterpret_cast<uint4*>(Bs + 2 * bsz + o) = make_uint4(p3[0], p3[1], p3[2], p3[3]);
-  }
-  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-  const uint32_t tmem = *tslot;
-  bool ok = true;
-  if (tid == 0) {
-    bool got = false;
-    for (int it = 0; it < (1 << 20); ++it)
-      if (mbar_try_wait(smem_u32(mbar), 0)) {
-        got = true;
-        break;
-      }
-    if (!got) {
-      ok = false;
-      if (err) atomicExch(err, 1);
-    } else {
-      // D f32, A and B BF16, both K-major, N = 64, M = 128
-      const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TC_NT >> 3) << 17) |
-                             ((uint32_t)(TC_M >> 4) << 24);
-      // one accumulator (64 TMEM columns) per K slice; the products Fi xj (i + j <= 5) smallest first, so the
-      // leading product is added last to the slice's sum
-      const int pa[TC_NPROD] = {1, 2, 3, 0, 1, 2, 0, 1, 0};
-      const int pb[TC_NPROD] = {2, 1, 0, 2, 1, 0, 1, 0, 0};
-      const uint32_t a0 = smem_u32(As), b0 = smem_u32(Bs);
-      for (int ks = 0; ks < KS; ++ks)
-        for (int p = 0; p < TC_NPROD; ++p) {
-          const uint64_t da = umma_desc(a0 + 2u * (uint32_t)(pa[p] * asz + ks * TC_M * 16), 128, 256);
-          const uint64_t db = umma_desc(b0 + 2u * (uint32_t)(pb[p] * bsz + ks * TC_NT * 16), 128, 256);
-          mma_bf16(tmem + (uint32_t)(ks * TC_NT), da, db, idesc, p != 0);
-        }
-    }
-    // arrive on the MMA barrier in every case (after the MMAs when they were issued)
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                     smem_u32(mbar + 1))
-                 : "memory");
-  }
-  bool done = false;
-  for (int it = 0; it < (1 << 20); ++it)
-    if (mbar_try_wait(smem_u32(mbar + 1), 0)) {
-      done = true;
-      break;
-    }
-  if (!done && err) atomicExch(err, 1);
-  ok = __syncthreads_and(ok && done) != 0;
-  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-  // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (its sub-partition's) and columns 16 (w / 4) .. + 15;
-  // the K-slice sums are combined with error-free two-sums and the rows staged in shared memory (over the
-  // constant matrix) for coalesced stores
-  float* Os = reinterpret_cast<float*>(As);  // [128][64 + 1]
-  const int n = 32 * (warp & 3) + lane;
-  {
-    const int cb = 16 * (warp >> 2);
-    float s[16], cmp[16];
-#pragma unroll
-    for (int j = 0; j < 16; ++j) s[j] = cmp[j] = 0.0f;
-#pragma unroll 1
-    for (int ks = 0; ks < KS; ++ks) {
-      uint32_t v[16];
-      const uint32_t ta = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(ks * TC_NT + cb);
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
-          "%14, %15}, [%16];\n"
-          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-            "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-          : "r"(ta));
-      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-#pragma unroll
-      for (int j = 0; j < 16; ++j) two_sum_c(s[j], __uint_as_float(v[j]), cmp[j]);
-    }
-#pragma unroll
-    for (int j = 0; j < 16; ++j) Os[n * (TC_NT + 1) + cb + j] = s[j] + cmp[j];
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-  __syncthreads();
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(512));
-  if (ok)
-    for (int i = tid; i < N * TC_NT; i += TC_THREADS) {
-      const int r = i / TC_NT, c = i - r * TC_NT;
-      if (l0 + c < nlines) out[(size_t)r * ld + l0 + c] = Os[r * (TC_NT + 1) + c];
-    }
 }
 
 }  // namespace
 
 int cheb_tc_kslices(int N) { return (N + 15) / 16; }
 
-// K slices of 16 (one 64-column TMEM accumulator each, at most 8 in the 512 columns) bound N.
-bool cheb_tc_supported(int N) { return N <= TC_M && cheb_tc_kslices(N) <= 8 && N >= 9; }
+// K slices of 16 (one 64-column TMEM accumulator each, at most 7 with the persistent kernel's shared memory:
+// constant matrix, BF16 tile and two FP32 tiles) bound N.
+bool cheb_tc_supported(int N) { return N >= 9 && cheb_tc_kslices(N) <= 7; }
 
 size_t cheb_tc_smem_bytes(int N) {
-  const int KS = cheb_tc_kslices(N);
-  const size_t KP = 16 * (size_t)KS;
-  return tc_region_a(KS) + 2 * TC_BSPLIT * TC_NT * KP + 4 * KP * TC_NT + 32;
+  const size_t KP = 16 * (size_t)cheb_tc_kslices(N);
+  return 2 * (TC_ASPLIT * TC_M * KP + TC_BSPLIT * TC_NT * KP) + 2 * 4 * KP * TC_NT + 32;
 }
 
 // Four BF16 splits of the forward matrix F (N x N, row-major FP64) in the kernel's operand layout (BF16 bits).
@@ -293,8 +309,14 @@ cudaError_t launch_cheb_tc(int N, int nlines, int ncomp, const float* in, size_t
     return true;
   }();
   (void)attr;
-  const dim3 grid((nlines + TC_NT - 1) / TC_NT, ncomp);
-  k_cheb_tc<<<grid, TC_THREADS, sm, st>>>(N, cheb_tc_kslices(N), nlines, in, ld, cs, out,
-                                          static_cast<const __nv_bfloat16*>(Ag), err);
+  static const int sms = [] {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+  }();
+  const int ntiles = ((nlines + TC_NT - 1) / TC_NT) * ncomp;
+  k_cheb_tc<<<ntiles < sms ? ntiles : sms, TC_THREADS, sm, st>>>(N, cheb_tc_kslices(N), nlines, ncomp, in, ld, cs,
+                                                                out, static_cast<const __nv_bfloat16*>(Ag), err);
   return cudaGetLastError();
 }

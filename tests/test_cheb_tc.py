@@ -24,7 +24,7 @@ CASES = [
      dict(baseflow=O.LaminarBase, constraint=O.BulkVelocity, Ubulk=2 / 3, nonlinearity=O.Rotational)),
     ("couette_conv_49", (24, 49, 18), COUETTE_BOX,
      dict(baseflow=O.LaminarBase, ulowerwall=-1.0, uupperwall=1.0, nonlinearity=O.Convection)),
-    ("poiseuille_rot_127", (16, 127, 12), POISEUILLE_BOX,
+    ("poiseuille_rot_111", (16, 111, 12), POISEUILLE_BOX,
      dict(baseflow=O.LaminarBase, constraint=O.BulkVelocity, Ubulk=2 / 3, nonlinearity=O.Rotational)),
 ]
 
