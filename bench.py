@@ -47,9 +47,10 @@ WORKLOAD = ("plane Poiseuille 128x97x128 (Lx=4pi, Lz=2pi), CNAB2 + SMRK2 start-u
             "Ubulk=2/3, Re_c=4000, rotational NL, 2/3 dealiasing, seeded perturbation L2=0.3")
 CNAB2, SMRK2, LaminarBase, BulkVelocity = 1, 3, 3, 1
 # DRAM bytes (read + write) per step of the mixed-path phases from `ncu --set full` captures of this workload
-# (the eight kernels of one step: tau solve and nonlinear pass).
-NCU_TRAFFIC = {"tau_solve": (37.94 + 0.68 + 54.39 + 0.55 + 27.11 + 0.02) * 1e6,
-               "nonlinear_pass": (16.32 + 0.0 + 16.73 + 0.42 + 25.13 + 0.0 + 12.60 + 0.0 + 8.18 + 0.0) * 1e6}
+# (one steady-state step: the tau solve's right-hand side, pressure/v and u/w kernels; the nonlinear pass's
+# curl/inverse Chebyshev, fused x/z and tensor-core forward Chebyshev kernels).
+NCU_TRAFFIC = {"tau_solve": (38.02 + 0.62 + 63.62 + 2.24 + 31.63 + 0.00) * 1e6,
+               "nonlinear_pass": (16.32 + 0.00 + 16.29 + 0.00 + 8.26 + 0.00) * 1e6}
 
 
 def peaks():
