@@ -1144,6 +1144,27 @@ int main_step(cfgpu_dns d) {
   return rk_step(d, 0);
 }
 
+// One step of an order-1 multistep start-up scheme (SBDF1 / CNFE1; MultistepDNS::advance, dnsalgo.cpp:202-251
+// with order 1): rhs = -alpha_0/dt u_n - beta_0 N(u_n), solved with lambda_t = eta/dt.
+int ms1_init_step(cfgpu_dns d) {
+  Scheme& s = d->init;
+  CKS(nonlinear(d, d->Ucur, d->fj[1], 1));
+  SolveParams sp = base_params(d);
+  sp.kind = 0;
+  sp.order = 1;
+  sp.scheme = 1;
+  sp.a[0] = -s.alpha[0] / d->fl.dt;
+  sp.b[0] = -s.beta[0];
+  SolvePtrs p = base_ptrs(d);
+  p.uin[0] = d->Ucur;  // the right-hand side is complete before the solve writes u
+  p.nin[0] = d->fj[1];
+  p.uout = d->Ucur;
+  p.qout = d->Qcur;
+  CKS(tau_solve(d, sp, p, s.tau[0]));
+  s.t += d->fl.dt;
+  return CFGPU_OK;
+}
+
 int scheme_advance(cfgpu_dns d, int which, int nsteps) {
   Scheme& s = which == 0 ? d->main : d->init;
   if (which == 0 && s.family == 0) return ms_advance(d, nsteps);
@@ -1151,7 +1172,7 @@ int scheme_advance(cfgpu_dns d, int which, int nsteps) {
     if (which == 0) {
       CKS(main_step_graph(d));
     } else {
-      CKS(s.family == 1 ? cnab_step(d, 1) : rk_step(d, 1));
+      CKS(s.family == 0 ? ms1_init_step(d) : (s.family == 1 ? cnab_step(d, 1) : rk_step(d, 1)));
     }
   }
   return CFGPU_OK;
@@ -1937,12 +1958,19 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
   if (!d->main.full && f.initstepping != f.timestepping) {
     CKS(setup_scheme(d->init, f.initstepping, f.dt));
     d->init.t = f.t0;
-    if (d->init.family == 0)
-      return fail(CFGPU_ENOTSUP, "multistep start-up schemes are not supported (use SMRK2, CNRK2 or CNAB2)");
+    // a multistep start-up scheme must start itself (DNS::DNS warns that it "needs initialization itself"
+    // otherwise, dns.cpp:34-37): order 1, SBDF1 or CNFE1
+    if (d->init.family == 0 && d->init.order > 1)
+      return fail(CFGPU_ENOTSUP, "a multistep start-up scheme must be of order 1 (SBDF1 or CNFE1)");
     d->has_init = true;
   }
   auto alloc_scheme = [&](Scheme& s, int which) -> int {
-    if (s.family == 0) {
+    if (s.family == 0 && which == 1) {
+      // order-1 multistep start-up: its nonlinear term only (u_n is the current field)
+      CKS(dalloc(&tmp, 3 * cd * rs, B));
+      d->fj[1] = tmp;
+      CK(cudaMemsetAsync(d->fj[1], 0, 3 * cd * rs, d->st));
+    } else if (s.family == 0) {
       for (int j = 0; j < s.order; ++j) {
         CKS(dalloc(&d->Uh[j], 3 * cd, B));
         CKS(dalloc(&d->Qh[j], cd, B));
@@ -2203,6 +2231,8 @@ int upload_slot(cfgpu_dns d, int f, const BaseFlow& B) {
 
 int ensure_hetero(cfgpu_dns d) {
   if (d->hetero) return CFGPU_OK;
+  if (d->has_init && d->init.family == 0)
+    return fail(CFGPU_ENOTSUP, "per-field parameters with a multistep start-up scheme");
   const size_t N = d->N, nb = d->nb;
   CKS(dalloc(&d->dslot, nb, d->bytes));
   CKS(dalloc(&d->dbaseS, 4 * nb * N, d->bytes));
