@@ -20,17 +20,25 @@
 #include "kernels.h"
 
 
-// Exact FP32 -> FP64 conversion by integer operations for zero and normal numbers (the conversion
-// instruction runs on the FP64 pipe, 64 cycles per warp instruction on GB300); subnormals, infinities and
-// NaNs take the conversion instruction.  FP64 values pass through.
+// Exact FP32 -> FP64 conversion by integer operations only (the conversion instruction runs on the FP64 pipe,
+// 64 cycles per warp instruction on GB300, and a conversion kept for rare lanes still takes the whole warp's
+// slot).  Normal numbers re-bias the exponent; a subnormal m 2^-149 with its leading one at bit p becomes
+// 1.f 2^(p-149); infinities and NaNs keep their payload.  FP64 values pass through.
 __device__ __forceinline__ double widen(double x) { return x; }
 __device__ __forceinline__ double widen(float f) {
   const unsigned u = __float_as_uint(f);
   const unsigned long long sgn = (unsigned long long)(u & 0x80000000u) << 32;
   const unsigned e = (u >> 23) & 0xFFu;
-  if ((u & 0x7FFFFFFFu) == 0) return __longlong_as_double((long long)sgn);
-  if (e == 0 || e == 0xFFu) return (double)f;
-  const unsigned long long bits = sgn | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7FFFFFu) << 29);
+  unsigned mant = u & 0x7FFFFFu;
+  unsigned ex = e + 896u;
+  if (e == 0xFFu) {
+    ex = 0x7FFu;
+  } else if (e == 0) {
+    const int p = 31 - __clz(mant | 1u);  // mant = 0 (zero): p = 0, mant stays 0, exponent field 0
+    ex = mant ? (unsigned)(p + 874) : 0u;
+    mant = (mant << (23 - p)) & 0x7FFFFFu;
+  }
+  const unsigned long long bits = sgn | ((unsigned long long)ex << 52) | ((unsigned long long)mant << 29);
   return __longlong_as_double((long long)bits);
 }
 
@@ -929,8 +937,11 @@ __global__ void __launch_bounds__(32) k_tau_rhs(GridDev g, int N, SolveParams sp
     const double e0L = sp.constraint == 0 ? dP : wall + sp.baseShear[c == 0 ? 0 : 1];
     const double e0 = aL * e0L + (sp.constraint == 0 ? dP : 0.0);
     const double* Byy = c == 0 ? P.Ubaseyy + fb : P.Wbaseyy + fb;
-    auto sweep = [&](auto KIND) {
+    // The (0,0) mode's terms are compiled only into the sweep of the warp that holds that mode: lanes whose
+    // predicate is off still take the warp's FP64 slot of a predicated instruction.
+    auto sweep = [&](auto KIND, auto EXTRA) {
       constexpr int kind = decltype(KIND)::value;
+      constexpr bool has_extra = decltype(EXTRA)::value;
       double d2n2 = 0.0, dqn2 = 0.0;
       for (int i0 = M - 1; i0 >= 0; i0 -= RB) {
         double uv[RB], qv[RB];
@@ -970,15 +981,23 @@ __global__ void __launch_bounds__(32) k_tau_rhs(GridDev g, int N, SolveParams sp
           }
           const bool n0 = n == 0;
           double rhs = fma(cu, uv[k], fma(n0 ? cd0 : cd, d2, fma(n0 ? cg0 : cg, gv, Nc)));
-          if (extra) rhs += (aL + 1.0) * (nu * Byy[n]) - (n0 ? e0 : 0.0);
+          if (has_extra && extra) rhs += (aL + 1.0) * (nu * Byy[n]) - (n0 ? e0 : 0.0);
           if (act) out[i] = rhs;
         }
       }
     };
-    if (sp.kind == 1)
-      sweep(std::integral_constant<int, 1>{});
-    else
-      sweep(std::integral_constant<int, 2>{});
+    const bool warp_extra = __any_sync(0xffffffffu, extra);
+    if (sp.kind == 1) {
+      if (warp_extra)
+        sweep(std::integral_constant<int, 1>{}, std::true_type{});
+      else
+        sweep(std::integral_constant<int, 1>{}, std::false_type{});
+    } else {
+      if (warp_extra)
+        sweep(std::integral_constant<int, 2>{}, std::true_type{});
+      else
+        sweep(std::integral_constant<int, 2>{}, std::false_type{});
+    }
   }
   __syncwarp(gmask);
   __threadfence_block();

@@ -210,9 +210,11 @@ __global__ void __launch_bounds__(32, 12) k_tau_pv_seg(GridDev g, int N, SolvePa
   const int kx = mode_kx(g, m), kz = mode_kz(g, m);
   const bool m00 = kx == 0 && kz == 0;
   const double* ts = tt.s + m;
-  const double kxL = ts[TS_KXL * Md], kzL = ts[TS_KZL * Md];
+  // the part's sign of i k folded into the wavenumbers (one FP64 add per row below, not two and a select)
+  const double kxL = part == 0 ? -ts[TS_KXL * Md] : ts[TS_KXL * Md];
+  const double kzL = part == 0 ? -ts[TS_KZL * Md] : ts[TS_KZL * Md];
 
-  // right-hand sides: Ry (own part) and kx Rx + kz Rz of the other part
+  // right-hand sides: Ry (own part) and -/+ (kx Rx + kz Rz) of the other part
   double ry[L], x[L], w[L];
 #pragma unroll
   for (int k = 0; k < L; ++k) ry[k] = c.i0 + k < c.M ? a[2 * (c.i0 + k) + q] : 0.0;
@@ -227,7 +229,7 @@ __global__ void __launch_bounds__(32, 12) k_tau_pv_seg(GridDev g, int N, SolvePa
   // rr = diff(Ry) -/+ (kx Rx + kz Rz) of the other part
   seg_diff<L>(c, a, ct, x, full);
 #pragma unroll
-  for (int k = 0; k < L; ++k) x[k] = part == 0 ? x[k] - w[k] : x[k] + w[k];
+  for (int k = 0; k < L; ++k) x[k] += w[k];
   // P = pH^{-1} rr
   put<L>(c, b, x, full);
   const double* tf = tt.f + m;
