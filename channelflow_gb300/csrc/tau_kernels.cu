@@ -789,7 +789,7 @@ __device__ void helm_t(int M, int q, const double* __restrict__ hlo, const doubl
 // the scratch lines 0, 2 and 1 (the solve reads them back).
 // ---------------------------------------------------------------------------
 template <typename R>
-__global__ void __launch_bounds__(32) k_tau_rhs(GridDev g, int N, SolveParams sp, SolvePtrs P, TauTable tt) {
+__global__ void __launch_bounds__(32, 10) k_tau_rhs(GridDev g, int N, SolveParams sp, SolvePtrs P, TauTable tt) {
   extern __shared__ double sm[];
   const int lane = threadIdx.x;
   const int t = blockIdx.x * 32 + lane;
@@ -865,7 +865,8 @@ __global__ void __launch_bounds__(32) k_tau_rhs(GridDev g, int N, SolveParams sp
       }
     }
   } else {
-    constexpr int RB = TCH;  // loads in flight per batch of the streamed lines
+    // rows per batch of the streamed lines (two batches in registers: 6 rows when the nonlinear terms are FP64)
+    constexpr int RB = sizeof(R) == 8 ? 6 : TCH;
     // per-mode constants from the tables (no FP64 divisions here)
     const double kappa2 = tt.s[TS_KAPPA2 * Md + m];
     const double Dx = tt.s[TS_DX * Md + m];
@@ -877,6 +878,9 @@ __global__ void __launch_bounds__(32) k_tau_rhs(GridDev g, int N, SolveParams sp
     __syncwarp(gmask);
     // first derivative of this lane's parity from the other parity's coefficients (descending recurrence,
     // without the factor nu); the n = 0 coefficient is halved after the sweep
+    // Both sweeps stream their lines in batches of RB rows with the next batch's loads issued before the
+    // current batch's recurrence runs (two register buffers), so a warp waits for memory once per sweep
+    // rather than once per batch.
     {
       double dn2 = 0.0;
       int i = M - 1;
@@ -884,18 +888,28 @@ __global__ void __launch_bounds__(32) k_tau_rhs(GridDev g, int N, SolveParams sp
         d1[i] = 0.0;
         i--;
       }
-      for (; i >= 0; i -= RB) {
-        double xv[RB];
+      double xa[RB], xb[RB];
+      auto ld = [&](int i0, double(&xv)[RB]) {
 #pragma unroll
         for (int k = 0; k < RB; ++k)
-          if (i - k >= 0) xv[k] = uo[i - k + q];
+          if (i0 - k >= 0) xv[k] = uo[i0 - k + q];
+      };
+      auto run = [&](int i0, const double(&xv)[RB]) {
 #pragma unroll
         for (int k = 0; k < RB; ++k)
-          if (i - k >= 0) {
-            const double v = dn2 + ct[2 * (i - k) + q] * xv[k];
+          if (i0 - k >= 0) {
+            const double v = dn2 + ct[2 * (i0 - k) + q] * xv[k];
             dn2 = v;
-            d1[i - k] = v;
+            d1[i0 - k] = v;
           }
+      };
+      if (i >= 0) ld(i, xa);
+      for (; i >= 0; i -= 2 * RB) {
+        if (i - RB >= 0) ld(i - RB, xb);
+        run(i, xa);
+        if (i - RB < 0) break;
+        if (i - 2 * RB >= 0) ld(i - 2 * RB, xa);
+        run(i - RB, xb);
       }
       if (q == 0) d1[0] = 0.5 * d1[0];
     }
@@ -943,47 +957,65 @@ __global__ void __launch_bounds__(32) k_tau_rhs(GridDev g, int N, SolveParams sp
       constexpr int kind = decltype(KIND)::value;
       constexpr bool has_extra = decltype(EXTRA)::value;
       double d2n2 = 0.0, dqn2 = 0.0;
-      for (int i0 = M - 1; i0 >= 0; i0 -= RB) {
+      struct Batch {
         double uv[RB], qv[RB];
         R nv[RB], n1v[RB];
+      };
+      auto ld = [&](int i0, Batch& b) {
 #pragma unroll
         for (int k = 0; k < RB; ++k) {
           const int i = i0 - k;
           if (i >= 0) {
             const int n = 2 * i + q;
-            uv[k] = uc[i];
-            qv[k] = c == 1 ? ((n + 1 <= Nb) ? qo[i + q] : 0.0) : qp[i];
-            nv[k] = Nj[(size_t)i * 2 * row];
-            n1v[k] = kind == 1 ? Nj1[(size_t)i * 2 * row] : Q[(size_t)i * 2 * row];
+            b.uv[k] = uc[i];
+            b.qv[k] = c == 1 ? ((n + 1 <= Nb) ? qo[i + q] : 0.0) : qp[i];
+            b.nv[k] = Nj[(size_t)i * 2 * row];
+            b.n1v[k] = kind == 1 ? Nj1[(size_t)i * 2 * row] : Q[(size_t)i * 2 * row];
           }
         }
+      };
+      auto run = [&](int i0, const Batch& b) {
 #pragma unroll
         for (int k = 0; k < RB; ++k) {
           const int i = i0 - k;
-          if (i < 0) break;
-          const int n = 2 * i + q;
-          const double x1 = (n + 1 <= Nb) ? d1o[i + q] : 0.0;
-          const double d2 = d2n2 + ct[n] * x1;
-          d2n2 = d2;
-          double gv = qv[k];
-          if (c == 1) {
-            gv = dqn2 + ct[n] * qv[k];
-            dqn2 = gv;
+          if (i >= 0) {
+            const double* uv = b.uv;
+            const double* qv = b.qv;
+            const R* nv = b.nv;
+            const R* n1v = b.n1v;
+            const int n = 2 * i + q;
+            const double x1 = (n + 1 <= Nb) ? d1o[i + q] : 0.0;
+            const double d2 = d2n2 + ct[n] * x1;
+            d2n2 = d2;
+            double gv = qv[k];
+            if (c == 1) {
+              gv = dqn2 + ct[n] * qv[k];
+              dqn2 = gv;
+            }
+            // the nonlinear terms are combined at their own precision R (FP32 on the mixed path)
+            double Nc;
+            if (kind == 1) {
+              Nc = widen(gN * nv[k] + zN * n1v[k]);
+            } else {
+              const R Qn = n1v[k] * rA - nv[k];
+              if (act) Q[(size_t)i * 2 * row] = Qn;
+              Nc = BC * widen(Qn);
+            }
+            const bool n0 = n == 0;
+            double rhs = fma(cu, uv[k], fma(n0 ? cd0 : cd, d2, fma(n0 ? cg0 : cg, gv, Nc)));
+            if (has_extra && extra) rhs += (aL + 1.0) * (nu * Byy[n]) - (n0 ? e0 : 0.0);
+            if (act) out[i] = rhs;
           }
-          // the nonlinear terms are combined at their own precision R (FP32 on the mixed path)
-          double Nc;
-          if (kind == 1) {
-            Nc = widen(gN * nv[k] + zN * n1v[k]);
-          } else {
-            const R Qn = n1v[k] * rA - nv[k];
-            if (act) Q[(size_t)i * 2 * row] = Qn;
-            Nc = BC * widen(Qn);
-          }
-          const bool n0 = n == 0;
-          double rhs = fma(cu, uv[k], fma(n0 ? cd0 : cd, d2, fma(n0 ? cg0 : cg, gv, Nc)));
-          if (has_extra && extra) rhs += (aL + 1.0) * (nu * Byy[n]) - (n0 ? e0 : 0.0);
-          if (act) out[i] = rhs;
         }
+      };
+      Batch A, B;
+      ld(M - 1, A);
+      for (int i0 = M - 1; i0 >= 0; i0 -= 2 * RB) {
+        if (i0 - RB >= 0) ld(i0 - RB, B);
+        run(i0, A);
+        if (i0 - RB < 0) break;
+        if (i0 - 2 * RB >= 0) ld(i0 - 2 * RB, A);
+        run(i0 - RB, B);
       }
     };
     const bool warp_extra = __any_sync(0xffffffffu, extra);
