@@ -130,6 +130,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
   };
   const uint32_t tmem = *tslot;
+  // the set-up above (barriers, tensor memory, the constant matrix) overlaps the previous kernel's tail; its
+  // output is read from here on
+  pdl_wait();
+  pdl_trigger();
   if (blockIdx.x < ntiles) issue(blockIdx.x, Xs);
   asm volatile("cp.async.commit_group;\n" ::: "memory");
   bool ok = true;
@@ -316,7 +320,6 @@ cudaError_t launch_cheb_tc(int N, int nlines, int ncomp, const float* in, size_t
     return n > 0 ? n : 1;
   }();
   const int ntiles = ((nlines + TC_NT - 1) / TC_NT) * ncomp;
-  k_cheb_tc<<<ntiles < sms ? ntiles : sms, TC_THREADS, sm, st>>>(N, cheb_tc_kslices(N), nlines, ncomp, in, ld, cs,
-                                                                out, static_cast<const __nv_bfloat16*>(Ag), err);
-  return cudaGetLastError();
+  return launch_pdl(k_cheb_tc, dim3(ntiles < sms ? ntiles : sms), dim3(TC_THREADS), sm, st, N, cheb_tc_kslices(N),
+                    nlines, ncomp, in, ld, cs, out, static_cast<const __nv_bfloat16*>(Ag), err);
 }

@@ -13,6 +13,39 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <utility>
+
+// ---------------------------------------------------------------------------
+// Programmatic dependent launch between the kernels of a step.  A kernel launched by launch_pdl may be
+// scheduled while the previous kernel of its stream is still finishing (its launch latency and CTA placement
+// overlap that kernel's tail); it must call pdl_wait() before it reads or writes any global memory, which
+// returns once the previous kernel has completed and its writes are visible.  pdl_trigger() lets the next
+// kernel be scheduled as soon as every CTA of this one has issued it.  Both are no-ops for a kernel launched
+// without the attribute.  The legacy and per-thread default streams keep plain launches.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+
+inline bool pdl_stream(cudaStream_t st) {
+  return st != nullptr && st != cudaStreamLegacy && st != cudaStreamPerThread;
+}
+
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                       Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl_stream(st) ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
 // 8-byte (FP32) / 16-byte (FP64) aligned, so a complex moves with one vector load or store.
 template <typename R>
 struct alignas(2 * sizeof(R)) cpx {

@@ -640,11 +640,12 @@ INST_FORMS(double)
 
 // Advance every field's constant version after a nonlinear evaluation (one thread per field).
 __global__ void k_dither_bump(int* ver, int nb) {
+  pdl_wait();
+  pdl_trigger();
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f < nb) ver[f] = (ver[f] + 1) % DITHER_V;
 }
 
 cudaError_t launch_dither_bump(int* ver, int nb, cudaStream_t st) {
-  k_dither_bump<<<(nb + 127) / 128, 128, 0, st>>>(ver, nb);
-  return cudaGetLastError();
+  return launch_pdl(k_dither_bump, dim3((nb + 127) / 128), dim3(128), 0, st, ver, nb);
 }

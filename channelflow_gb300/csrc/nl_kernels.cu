@@ -263,6 +263,8 @@ __global__ void __launch_bounds__(256) k_curl_cheb(GridDev g, int N, const doubl
                                                    const R* __restrict__ basey, double Vsuck,
                                                    int bstride, Dither dt, int lpf) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  pdl_wait();
+  pdl_trigger();
   typedef typename Vec16<R>::T V;
   constexpr int VW = 16 / sizeof(R);
   const int P = (N + 1) / 2, KA = (N + 1) / 2, KB = (N - 1) / 2, J = (N - 1) / 2;
@@ -455,9 +457,8 @@ cudaError_t launch_curl_cheb(const GridDev& g, int N, const double* U, R* W6, co
   }();
   (void)attr_set;
   const int nf = dt.nb > 0 ? dt.nb : 1, lpf = 2 * g.Md / nf;
-  k_curl_cheb<R><<<dim3(nf * ((lpf + CC_TL - 1) / CC_TL), 2), 256, curl_cheb_smem_bytes<R>(N), st>>>(
-      g, N, U, W6, CA, CB, DA, DB, basey, Vsuck, bstride, dt, lpf);
-  return cudaGetLastError();
+  return launch_pdl(k_curl_cheb<R>, dim3(nf * ((lpf + CC_TL - 1) / CC_TL), 2), dim3(256), curl_cheb_smem_bytes<R>(N),
+                    st, g, N, U, W6, CA, CB, DA, DB, basey, Vsuck, bstride, dt, lpf);
 }
 template cudaError_t launch_curl_cheb<float>(const GridDev&, int, const double*, float*, const float*, const float*,
                                              const float*, const float*, const float*, double, cudaStream_t, int,

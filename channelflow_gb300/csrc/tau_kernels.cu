@@ -791,6 +791,8 @@ __device__ void helm_t(int M, int q, const double* __restrict__ hlo, const doubl
 template <typename R>
 __global__ void __launch_bounds__(32, 10) k_tau_rhs(GridDev g, int N, SolveParams sp, SolvePtrs P, TauTable tt) {
   extern __shared__ double sm[];
+  pdl_wait();
+  pdl_trigger();
   const int lane = threadIdx.x;
   const int t = blockIdx.x * 32 + lane;
   const int Md = g.Md;
@@ -1356,8 +1358,7 @@ cudaError_t launch_tau_solve(const GridDev& g, int N, const SolveParams& sp, con
     }();
     (void)attr;
     const size_t smem_r = sizeof(double) * (((N + 1) & ~1) + (size_t)M0 * 32);
-    k_tau_rhs<R><<<dim3((4 * g.Md + 31) / 32, 3), 32, smem_r, st>>>(g, N, sp, p, tt);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = launch_pdl(k_tau_rhs<R>, dim3((4 * g.Md + 31) / 32, 3), dim3(32), smem_r, st, g, N, sp, p, tt);
     if (e != cudaSuccess) return e;
     return launch_tau_pvuw_seg(g, N, sp, p, hb, tt, st);
   }

@@ -180,6 +180,8 @@ template <int L>
 __global__ void __launch_bounds__(32, 12) k_tau_pv_seg(GridDev g, int N, SolveParams sp, SolvePtrs P, HelmB hb,
                                                    TauTable tt) {
   extern __shared__ double sm[];
+  pdl_wait();
+  pdl_trigger();
   const int lane = threadIdx.x;
   const int ml = lane >> 4, part = (lane >> 3) & 1, q = (lane >> 2) & 1, s = lane & 3;
   const int Md = g.Md;
@@ -315,6 +317,8 @@ template <int L>
 __global__ void __launch_bounds__(32, 16) k_tau_uw_seg(GridDev g, int N, SolveParams sp, SolvePtrs P, HelmB hb,
                                                    TauTable tt) {
   extern __shared__ double sm[];
+  pdl_wait();
+  pdl_trigger();
   const int lane = threadIdx.x;
   const int cu = lane >> 4, part = (lane >> 3) & 1, q = (lane >> 2) & 1, s = lane & 3;
   const int Md = g.Md;
@@ -403,9 +407,9 @@ cudaError_t run_seg(const GridDev& g, int N, const SolveParams& sp, const SolveP
     return true;
   }();
   (void)attr;
-  k_tau_pv_seg<L><<<(g.Md + 1) / 2, 32, smem_pv, st>>>(g, N, sp, p, hb, tt);
-  k_tau_uw_seg<L><<<g.Md, 32, smem_uw, st>>>(g, N, sp, p, hb, tt);
-  return cudaGetLastError();
+  cudaError_t e = launch_pdl(k_tau_pv_seg<L>, dim3((g.Md + 1) / 2), dim3(32), smem_pv, st, g, N, sp, p, hb, tt);
+  if (e != cudaSuccess) return e;
+  return launch_pdl(k_tau_uw_seg<L>, dim3(g.Md), dim3(32), smem_uw, st, g, N, sp, p, hb, tt);
 }
 
 }  // namespace
