@@ -24,6 +24,7 @@ step is one full CNAB2 step of the 128 x 97 x 128 field.
 from __future__ import annotations
 
 import argparse
+import contextlib
 import json
 import math
 import os
@@ -201,6 +202,7 @@ def run_gpu(args, rank, world):
     import ctypes  # noqa: F401
     from channelflow_gb300 import DNS, Grid
     from channelflow_gb300 import build as b
+    from channelflow_gb300.dns import PinnedHost
     from channelflow_gb300.fields import l2norm
 
     b.build()
@@ -234,21 +236,25 @@ def run_gpu(args, rank, world):
                              tau_ms=tau_ms, tau_n=tau_n, Md=dns.num_modes(), bytes=dns.device_bytes(),
                              cheb_fft=dns.cheb_fft(), cheb_tensor=dns.cheb_tensor())
         if True:
-            # end-to-end through the public API: host buffers in, host buffers out, every step
+            # end-to-end through the public API: host buffers in, host buffers out, every step; the caller's
+            # FlowField buffers page-locked once (as a caller that keeps them does), and for comparison as plain
+            # pageable memory
             Ke = max(3, min(args.steps, 50))
-            ue, qe = u0.copy(), q0.copy()
-            dns_e = DNS(ue, grid, make_flags(), precision=prec)
-            pin_forms(args, None)
-            dns_e.advance(ue, qe, args.warmup)
-            barrier()
-            t0 = time.perf_counter()
-            for _ in range(Ke):
-                dns_e.advance(ue, qe, 1)
-            te = max_over_ranks(time.perf_counter() - t0)
-            Md = dns_e.num_modes()
-            results["e2e" if prec == "mixed" else "e2e_fp64"] = dict(s=te, K=Ke, h2d=4 * NY * Md * 16,
-                                                                       d2h=4 * NY * Md * 16)
-            dns_e.close()
+            for pinned in (True, False):
+                ue, qe = u0.copy(), q0.copy()
+                dns_e = DNS(ue, grid, make_flags(), precision=prec)
+                pin_forms(args, None)
+                with (PinnedHost(ue, qe) if pinned else contextlib.nullcontext()):
+                    dns_e.advance(ue, qe, args.warmup)
+                    barrier()
+                    t0 = time.perf_counter()
+                    for _ in range(Ke):
+                        dns_e.advance(ue, qe, 1)
+                    te = max_over_ranks(time.perf_counter() - t0)
+                Md = dns_e.num_modes()
+                key = ("e2e" if prec == "mixed" else "e2e_fp64") + ("" if pinned else "_pageable")
+                results[key] = dict(s=te, K=Ke, h2d=4 * NY * Md * 16, d2h=4 * NY * Md * 16)
+                dns_e.close()
         dns.close()
     acc = None
     if args.accuracy_steps > 0 and rank == 0:
@@ -799,7 +805,10 @@ def main():
         "e2e": {"value": world * e["K"] / e["s"], "unit": "steps/s", "h2d_bytes_per_step": e["h2d"],
                 "d2h_bytes_per_step": e["d2h"],
                 "path": "cfgpu_dns_advance(u, q, 1) per step with host FlowField buffers",
-                "fp64": world * res["e2e_fp64"]["K"] / res["e2e_fp64"]["s"]},
+                "host_memory": "page-locked once before the timed steps (cfgpu_host_register)",
+                "fp64": world * res["e2e_fp64"]["K"] / res["e2e_fp64"]["s"],
+                "pageable": {"mixed": world * res["e2e_pageable"]["K"] / res["e2e_pageable"]["s"],
+                             "fp64": world * res["e2e_fp64_pageable"]["K"] / res["e2e_fp64_pageable"]["s"]}},
         "gpu_launches": m["launches"],
         "clocks": m["clocks"],
         "cpu_baseline": cpu,

@@ -87,6 +87,8 @@ _SIGS = {
     "cfgpu_helmholtz_solve_mean_batched": [C.c_int, C.c_int, C.c_double, C.c_double, _PD, C.c_double, _PD, _PD,
                                            _PD, _PD, _PD, _PD],
     "cfgpu_dns_host_access": [C.c_void_p, C.POINTER(C.c_int)],
+    "cfgpu_host_register": [C.c_void_p, C.c_size_t],
+    "cfgpu_host_unregister": [C.c_void_p],
     "cfgpu_measure_fp64": [_PD, _PD],
     "cfgpu_dither_versions": [C.c_double, C.POINTER(C.c_float)],
     "cfgpu_timestep_adjust_for_T": [C.c_void_p, C.c_double, _PI, _PI, _PD],

@@ -175,6 +175,10 @@ bool make_fft_plan(int L, FftPlan& p, std::vector<std::complex<long double>>& tw
   while (n % 2 == 0) { rs.push_back(2); n /= 2; }
   while (n % 3 == 0) { rs.push_back(3); n /= 3; }
   while (n % 5 == 0) { rs.push_back(5); n /= 5; }
+  // any other prime factor is a direct-DFT stage (FFTW takes every length; such grids are rare, so these
+  // stages favour generality over speed)
+  for (int f = 7; n > 1 && f <= FFT_MAX_RADIX; f += 2)
+    while (n % f == 0) { rs.push_back(f); n /= f; }
   if (n != 1 || rs.empty() || (int)rs.size() > FFT_MAX_STAGES) return false;
   memset(&p, 0, sizeof(p));
   p.L = L;
@@ -195,6 +199,16 @@ bool make_fft_plan(int L, FftPlan& p, std::vector<std::complex<long double>>& tw
         tw.emplace_back(cosl(ang), sinl(ang));
       }
     off += Ns * (R - 1);
+    p.rootoff[s] = -1;
+    if (R > 5) {
+      // the stage's DFT matrix entries exp(-2 pi i e / R), e = 0 .. R-1
+      p.rootoff[s] = off;
+      for (int e = 0; e < R; ++e) {
+        const long double ang = -2.0L * PI_L * (long double)e / (long double)R;
+        tw.emplace_back(e == 0 ? 1.0L : cosl(ang), e == 0 ? 0.0L : sinl(ang));
+      }
+      off += R;
+    }
     Ns *= R;
   }
   p.twlen = off;
@@ -1811,7 +1825,7 @@ int dns_create_impl(cfgpu_dns d, const cfgpu_grid* grid, const cfgpu_flags* flag
   // FFT plans, twiddles, Chebyshev matrices
   std::vector<std::complex<long double>> twx, twz;
   if (!make_fft_plan(Nx, d->px, twx) || !make_fft_plan(Nz, d->pz, twz))
-    return fail(CFGPU_ENOTSUP, "Nx and Nz must factor into 2, 3 and 5");
+    return fail(CFGPU_ENOTSUP, "Nx and Nz must factor into primes <= " + std::to_string(FFT_MAX_RADIX));
   ChebMats cm = make_cheb_mats(Ny);
   for (auto& v : cm.derA) v *= 2.0 / (b - a);
   for (auto& v : cm.derB) v *= 2.0 / (b - a);
@@ -3069,6 +3083,31 @@ cfgpu_status cfgpu_set_host_access(int enable) {
 cfgpu_status cfgpu_dns_host_access(cfgpu_dns d, int* direct) {
   if (!d || !direct) return fail(CFGPU_EINVAL, "bad argument");
   *direct = d->direct ? 1 : 0;
+  return CFGPU_OK;
+}
+
+// Page-locking a caller's FlowField buffer maps it into every device's page tables (portable), so the
+// host-buffer kernels reach it without the host page-table walk that pageable memory needs.  Host memory only:
+// no device memory is taken.
+cfgpu_status cfgpu_host_register(void* ptr, size_t bytes) {
+  if (!ptr || bytes == 0) return fail(CFGPU_EINVAL, "null pointer or zero size");
+  const cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterPortable | cudaHostRegisterMapped);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    return fail(e == cudaErrorHostMemoryAlreadyRegistered ? CFGPU_EINVAL : CFGPU_ECUDA,
+                std::string("cudaHostRegister: ") + cudaGetErrorString(e));
+  }
+  return CFGPU_OK;
+}
+
+cfgpu_status cfgpu_host_unregister(void* ptr) {
+  if (!ptr) return fail(CFGPU_EINVAL, "null pointer");
+  const cudaError_t e = cudaHostUnregister(ptr);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    return fail(e == cudaErrorHostMemoryNotRegistered ? CFGPU_EINVAL : CFGPU_ECUDA,
+                std::string("cudaHostUnregister: ") + cudaGetErrorString(e));
+  }
   return CFGPU_OK;
 }
 

@@ -1,4 +1,4 @@
-// Batched mixed-radix (2,3,4,5) Stockham FFT on sequences held in shared memory.
+// Batched mixed-radix (2,3,4,5; other primes as direct DFTs) Stockham FFT on sequences held in shared memory.
 //
 // One thread block transforms `nseq` sequences of length L together: every
 // stage is a sweep over nseq*L/R radix-R butterflies shared by all threads,
@@ -18,6 +18,7 @@
 #include "common.cuh"
 
 #define FFT_MAX_STAGES 12
+#define FFT_MAX_RADIX 127  // largest prime factor of a length (radices above 5 run as direct DFTs)
 
 struct FftPlan {
   int L;
@@ -25,6 +26,7 @@ struct FftPlan {
   int radix[FFT_MAX_STAGES];
   int Ns[FFT_MAX_STAGES];
   int twoff[FFT_MAX_STAGES];
+  int rootoff[FFT_MAX_STAGES];  // radix > 5: offset of exp(-2 pi i e / R), e < R, in the table; else -1
   int twlen;  // total twiddle entries
 };
 
@@ -101,6 +103,40 @@ __device__ void fft_batch_generic(cpx<R>* a, cpx<R>* b, int nseq, int ss, const 
     const int LR = L / Rr;
     const int total = nseq * LR;
     const cpx<R>* twt = tw + p.twoff[s];
+    if (Rr > 5) {
+      // direct DFT of a prime radix: the butterfly's inputs (read by no other butterfly of the stage) are
+      // twiddled in place, then every output sums over them with the stage's DFT matrix entries
+      const cpx<R>* rt = tw + p.rootoff[s];
+      for (int idx = tid; idx < total; idx += nthr) {
+        const int q = idx / LR;
+        const int j = idx - q * LR;
+        const int k = j % Ns;
+        cpx<R>* sp = src + q * ss + j;
+        for (int r = 1; r < Rr; ++r) {
+          cpx<R> w = twt[k * (Rr - 1) + (r - 1)];
+          if (sign > 0) w.y = -w.y;
+          sp[r * LR] = cmul(sp[r * LR], w);
+        }
+        cpx<R>* dp = dst + q * ss + (j - k) * Rr + k;
+        for (int o = 0; o < Rr; ++o) {
+          cpx<R> acc = sp[0];
+          int e = 0;
+          for (int r = 1; r < Rr; ++r) {
+            e += o;
+            if (e >= Rr) e -= Rr;
+            cpx<R> w = rt[e];
+            if (sign > 0) w.y = -w.y;
+            acc = cadd(acc, cmul(sp[r * LR], w));
+          }
+          dp[o * Ns] = acc;
+        }
+      }
+      __syncthreads();
+      cpx<R>* t = src;
+      src = dst;
+      dst = t;
+      continue;
+    }
     for (int idx = tid; idx < total; idx += nthr) {
       const int q = idx / LR;
       const int j = idx - q * LR;

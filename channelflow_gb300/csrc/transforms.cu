@@ -255,7 +255,7 @@ cfgpu_status cfgpu_flowfield_create(const cfgpu_grid* g, int Nd, cfgpu_flowfield
   std::vector<std::complex<long double>> twx, twz;
   int st = CFGPU_OK;
   if (!cfgpu_fft_plan(g->Nx, f->px, twx) || !cfgpu_fft_plan(g->Nz, f->pz, twz))
-    st = tf_fail(CFGPU_ENOTSUP, "Nx and Nz must factor into 2, 3 and 5");
+    st = tf_fail(CFGPU_ENOTSUP, "Nx and Nz must factor into primes <= " + std::to_string(FFT_MAX_RADIX));
   if (st == CFGPU_OK && cudaStreamCreateWithFlags(&f->st, cudaStreamNonBlocking) != cudaSuccess)
     st = tf_fail(CFGPU_ECUDA, "cudaStreamCreate failed");
   if (st == CFGPU_OK) {

@@ -355,6 +355,36 @@ def set_host_access(enable: bool):
     L.check(L.load().cfgpu_set_host_access(int(bool(enable))))
 
 
+class PinnedHost:
+    """Page-locks host arrays for the lifetime of a `with` block (cfgpu_host_register / _unregister), e.g. the
+    FlowField buffers a caller passes to DNS.advance on every step; the arrays stay ordinary NumPy arrays."""
+
+    def __init__(self, *arrays: np.ndarray):
+        for a in arrays:
+            if not a.flags.c_contiguous:
+                raise ValueError("pinned arrays must be C-contiguous")
+        self._arrays = arrays
+        self._done = []
+
+    def __enter__(self):
+        lib = L.load()
+        try:
+            for a in self._arrays:
+                L.check(lib.cfgpu_host_register(C.c_void_p(a.ctypes.data), C.c_size_t(a.nbytes)))
+                self._done.append(a)
+        except BaseException:
+            self.__exit__(None, None, None)
+            raise
+        return self
+
+    def __exit__(self, *exc):
+        lib = L.load()
+        while self._done:
+            a = self._done.pop()
+            L.check(lib.cfgpu_host_unregister(C.c_void_p(a.ctypes.data)))
+        return False
+
+
 def helmholtz_solve_batched(a: float, b: float, lam, nu: float, f, ua=None, ub=None, umean=None):
     """HelmholtzSolver(N, a, b, lambda_s, nu).solve for many systems (helmholtz.cpp:18-95): f is
     [nsys][N] Chebyshev coefficients; returns u [nsys][N], or (u, mu) with umean given (the

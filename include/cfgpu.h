@@ -97,7 +97,8 @@ cfgpu_status cfgpu_dns_get_fields_device(cfgpu_dns dns, int slot, cfgpu_field u,
  * (fieldstate, cfbasics/mathdefs.h:77: Physical = 0, Spectral = 1); a transform to the current state does
  * nothing, makeSpectral runs xz then y, makePhysical y then xz.  Forward xz scales by 1/(Nx Nz); y uses the
  * chebyfft/ichebyfft scaling (chebyshev.cpp:262-303).  cfgpu_flowfield_data gives the device buffer.
- * Nx and Nz even and 2,3,5-smooth.
+ * Nx and Nz even, with no prime factor above 127 (factors 2, 3, 5 run as radix-2/3/4/5 stages, larger
+ * primes as direct DFTs: FFTW takes every length).
  */
 enum { CFGPU_PHYSICAL = 0, CFGPU_SPECTRAL = 1 };
 typedef struct cfgpu_flowfield_s* cfgpu_flowfield;
@@ -289,6 +290,13 @@ cfgpu_status cfgpu_dns_cheb_fft(cfgpu_dns dns, int* fft);
  * copies.  cfgpu_dns_host_access reports which path a DNS uses (1 direct, 0 staged). */
 cfgpu_status cfgpu_set_host_access(int enable);
 cfgpu_status cfgpu_dns_host_access(cfgpu_dns dns, int* direct);
+/* No reference counterpart (the reference's FlowField data is plain pageable memory): page-lock a caller's
+ * host buffer (e.g. a FlowField's data array kept for many advance calls) and map it for every device, so the
+ * host-buffer transfers of cfgpu_dns_advance / set_fields / get_fields read and write it through the device's
+ * own page tables; unregister before freeing the buffer.  Takes no device memory.  Registering a buffer twice,
+ * or unregistering one that was not registered, is CFGPU_EINVAL. */
+cfgpu_status cfgpu_host_register(void* ptr, size_t bytes);
+cfgpu_status cfgpu_host_unregister(void* ptr);
 cfgpu_status cfgpu_dns_set_profiling(cfgpu_dns dns, int enable);
 cfgpu_status cfgpu_dns_phase_times(cfgpu_dns dns, double* nl_ms, long long* nl_count, double* tau_ms,
                                    long long* tau_count);

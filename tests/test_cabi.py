@@ -50,3 +50,7 @@ def test_argument_errors_need_no_gpu(lib):
     assert lib.cfgpu_dns_create(C.byref(g), C.byref(f), None, None, None, 9, C.byref(h)) == L.CFGPU_EINVAL
     assert lib.cfgpu_tau_solve_batched(4, 1, None, None, 1.0, 1.0, -1.0, 1.0, 1.0, 1.0, 1,
                                        None, None, None, None, None, None, None) == L.CFGPU_EINVAL
+    assert lib.cfgpu_host_register(None, 8) == L.CFGPU_EINVAL
+    buf = C.create_string_buffer(64)
+    assert lib.cfgpu_host_register(C.cast(buf, C.c_void_p), 0) == L.CFGPU_EINVAL
+    assert lib.cfgpu_host_unregister(None) == L.CFGPU_EINVAL

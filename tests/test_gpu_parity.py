@@ -109,6 +109,10 @@ CASES = [
     ("suction_sbdf2_rotation", (12, 17, 12, *COUETTE_BOX),
      dict(nu=1 / 400, dt=0.02, timestepping=O.SBDF2, initstepping=O.SMRK2, baseflow=O.SuctionBase, Vsuck=1 / 400,
           rotation=0.5), 8),
+    # x and z lengths with prime factors 7 and 13 (direct-DFT stages of the generic FFT)
+    ("couette_sbdf3_radix7_13", (28, 17, 26, *COUETTE_BOX),
+     dict(nu=1 / 400, dt=0.02, timestepping=O.SBDF3, initstepping=O.SMRK2, baseflow=O.LaminarBase,
+          ulowerwall=-1.0, uupperwall=1.0), 10),
     ("poiseuille_48_cnab2", (48, 49, 48, *POISEUILLE_BOX),
      dict(nu=1 / 4000, dt=0.01, timestepping=O.CNAB2, initstepping=O.SMRK2, baseflow=O.LaminarBase,
           constraint=O.BulkVelocity, Ubulk=2.0 / 3.0), 5),

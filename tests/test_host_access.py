@@ -78,3 +78,34 @@ def test_direct_host_access_unaligned_buffers():
     m = np.abs(out) > 0
     assert np.array_equal(out[m], u0[m])
     d.close()
+
+
+def test_pinned_host_buffers_equal_pageable():
+    """Page-locked FlowField buffers (cfgpu_host_register) go through the same kernels: identical results; the
+    registration is undone on leaving the block, and a second registration of the same buffer is refused."""
+    from channelflow_gb300 import DNS
+    from channelflow_gb300 import _lib as L
+    from channelflow_gb300.dns import PinnedHost
+    g = O.Grid(18, 17, 12, *COUETTE_BOX)
+    fl = O.DNSFlags(nu=1 / 400, dt=0.02, baseflow=O.LaminarBase, ulowerwall=-1.0, uupperwall=1.0)
+    u0 = np.ascontiguousarray(O.random_divfree_field(g, seed=77, norm=0.2))
+    outs = []
+    for pinned in (True, False):
+        u, q = u0.copy(), np.zeros((1,) + u0.shape[1:], complex)
+        d = DNS(u.copy(), to_cgrid(g), to_cflags(fl), precision="mixed")
+        if pinned:
+            with PinnedHost(u, q):
+                with pytest.raises(L.CfgpuError):
+                    with PinnedHost(u):
+                        pass
+                for _ in range(3):
+                    d.advance(u, q, 4)
+        else:
+            for _ in range(3):
+                d.advance(u, q, 4)
+        outs.append((u, q))
+        d.close()
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+    # unregistered on exit: registering again works
+    with PinnedHost(outs[0][0]):
+        pass

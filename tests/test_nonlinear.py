@@ -27,6 +27,11 @@ CASES = [
      dict(baseflow=O.LaminarBase, ulowerwall=-1.0, uupperwall=1.0, nonlinearity=O.LinearAboutProfile)),
     ("couette_rotation", (16, 17, 16), COUETTE_BOX,
      dict(baseflow=O.LaminarBase, ulowerwall=-1.0, uupperwall=1.0, nonlinearity=O.Rotational, rotation=0.3)),
+    # x and z lengths with prime factors 7 and 11 (direct-DFT stages of the generic FFT)
+    ("couette_rotational_radix7_11", (28, 17, 22), COUETTE_BOX,
+     dict(baseflow=O.LaminarBase, ulowerwall=-1.0, uupperwall=1.0, nonlinearity=O.Rotational)),
+    ("poiseuille_skew_radix13_7", (26, 17, 14), POISEUILLE_BOX,
+     dict(baseflow=O.LaminarBase, constraint=O.BulkVelocity, Ubulk=2 / 3, nonlinearity=O.SkewSymmetric)),
 ]
 
 

@@ -14,7 +14,8 @@ from oracle import cf_oracle as O
 pytestmark = pytest.mark.gpu
 TOL = 1e-13
 
-GRIDS = [(32, 33, 32), (48, 49, 36), (24, 17, 40), (128, 97, 128), (10, 9, 6)]
+# radices 2, 3, 4, 5 and prime factors 7, 11, 13 (direct-DFT stages)
+GRIDS = [(32, 33, 32), (48, 49, 36), (24, 17, 40), (128, 97, 128), (10, 9, 6), (28, 17, 22), (14, 9, 26)]
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -112,6 +113,6 @@ def test_bad_sizes_rejected():
     from channelflow_gb300 import _lib as L
     from channelflow_gb300.flowfield import FlowField
     with pytest.raises(L.CfgpuError):
-        FlowField(14, 9, 8, 1, 1.0, 1.0)  # 14 = 2 x 7: not 2,3,5-smooth
+        FlowField(262, 9, 8, 1, 1.0, 1.0)  # 262 = 2 x 131: a prime factor above the largest radix (127)
     with pytest.raises(L.CfgpuError):
         FlowField(9, 9, 8, 1, 1.0, 1.0)  # odd Nx
