@@ -114,6 +114,7 @@ _SIGS = {
     "cfgpu_dns_set_graphs": [C.c_void_p, C.c_int],
     "cfgpu_set_autotune": [C.c_int],
     "cfgpu_set_fused_xz": [C.c_int],
+    "cfgpu_set_pdl": [C.c_int],
     "cfgpu_set_cheb_fft": [C.c_int],
     "cfgpu_set_tau_segmented": [C.c_int],
     "cfgpu_set_cheb_tensor": [C.c_int],

@@ -26,8 +26,11 @@
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
 
+// cfgpu_set_pdl: programmatic dependent launch on (the default) or off for launches made afterwards
+int pdl_enabled();
+
 inline bool pdl_stream(cudaStream_t st) {
-  return st != nullptr && st != cudaStreamLegacy && st != cudaStreamPerThread;
+  return pdl_enabled() && st != nullptr && st != cudaStreamLegacy && st != cudaStreamPerThread;
 }
 
 template <typename... KArgs, typename... Args>

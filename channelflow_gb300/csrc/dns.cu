@@ -408,6 +408,10 @@ void pinned_free(void* p) {
 
 }  // namespace
 
+// programmatic dependent launch between the kernels of a step (cfgpu_set_pdl; declared in common.cuh)
+static std::atomic<int> g_pdl_on{1};
+int pdl_enabled() { return g_pdl_on.load(std::memory_order_relaxed); }
+
 int cfgpu_record_error(int code, const std::string& msg) { return fail(code, msg); }
 
 bool cfgpu_fft_plan(int L, FftPlan& p, std::vector<std::complex<long double>>& tw) { return make_fft_plan(L, p, tw); }
@@ -1574,7 +1578,7 @@ int tune_xz(cfgpu_dns d) {
                              d->xcols);
         return e;
       });
-      if (best >= 1e30f || t3 < best) d->xzC = d->xzRC = 0;
+      if (best >= 1e30f || (t3 < best && g_fused_xz.load() != 2)) d->xzC = d->xzRC = 0;
     }
   }
   d->xzf = d->xzC > 0;
@@ -2743,6 +2747,7 @@ cfgpu_status cfgpu_dns_l2norm(cfgpu_dns d, int field, double* l2) {
 cfgpu_status cfgpu_dns_advance_timed(cfgpu_dns d, int nsteps, double* ms) {
   if (!d || nsteps < 0 || !ms) return fail(CFGPU_EINVAL, "bad argument");
   cudaEvent_t a = take_event(d), b = take_event(d);
+  CK(cudaStreamSynchronize(d->st));  // the timed region starts on an idle stream
   CK(cudaEventRecord(a, d->st));
   CKS(dns_advance_device(d, nsteps));
   CK(cudaEventRecord(b, d->st));
@@ -3025,8 +3030,19 @@ cfgpu_status cfgpu_field_symmetry(const cfgpu_grid* grid, int dealias, int Nd, c
   return st;
 }
 
+cfgpu_status cfgpu_set_pdl(int enable) {
+  g_pdl_on.store(enable ? 1 : 0);
+  return CFGPU_OK;
+}
+
 cfgpu_status cfgpu_set_fused_xz(int enable) {
-  g_fused_xz.store(enable ? 1 : 0);
+  if (enable < 0 || enable > 2) return fail(CFGPU_EINVAL, "fused x/z mode must be 0, 1 or 2");
+  {
+    // the cached choices were made under the previous mode
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_xz.clear();
+  }
+  g_fused_xz.store(enable);
   return CFGPU_OK;
 }
 

@@ -251,6 +251,7 @@ __global__ void __launch_bounds__(256) k_zphys(GridDev g, FftPlan pz, const cpx<
                                                const cpx<R>* __restrict__ X, cpx<R>* __restrict__ Z, Dither dt) {
   constexpr int NC = FormIO<FORM>::NC, NO = FormIO<FORM>::NO;
   extern __shared__ unsigned char smem_raw[];
+  pdl_wait();  // launched with launch_pdl: the previous kernel's output is read from here on
   twz = dither_ptr(twz, dither_ver(dt, blockIdx.y % dt.nb), dt.S);  // plane blockIdx.y -> its field's twiddles
   const int Nz = g.Nz, ss = Nz + 1, NKz = g.NKz;
   const int nseq = ((NC > NO ? NC : NO) * RP) / 2;
@@ -509,9 +510,8 @@ static cudaError_t launch_zphys_t(const GridDev& g, const FftPlan& pz, const cpx
     return true;
   }();
   (void)attr_set;
-  k_zphys<R, FORM><<<dim3((g.Nx + RP - 1) / RP, g.Ny), 256, zphys_smem_bytes<R>(g, FORM, RP), st>>>(g, pz, twz, RP,
-                                                                                                    X, Z, dt);
-  return cudaGetLastError();
+  return launch_pdl(k_zphys<R, FORM>, dim3((g.Nx + RP - 1) / RP, g.Ny), dim3(256), zphys_smem_bytes<R>(g, FORM, RP),
+                    st, g, pz, twz, RP, X, Z, dt);
 }
 
 template <typename R>

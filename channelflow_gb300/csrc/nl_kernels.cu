@@ -480,6 +480,7 @@ __global__ void __launch_bounds__(256) k_xinv(GridDev g, FftPlan px, const cpx<R
                                               const cpx<R>* __restrict__ W, cpx<R>* __restrict__ X, int czc,
                                               Dither dt) {
   extern __shared__ unsigned char smem_raw[];
+  pdl_wait();  // launched with launch_pdl: the previous kernel's output is read from here on
   twx = dither_ptr(twx, dither_ver(dt, blockIdx.x % dt.nb), dt.S);  // plane blockIdx.x -> its field's twiddles
   const int ss = g.Nx + 1;
   const int iz0 = blockIdx.z * czc;
@@ -519,6 +520,7 @@ __global__ void __launch_bounds__(256) k_xfwd(GridDev g, FftPlan px, const cpx<R
                                               const cpx<R>* __restrict__ Z, cpx<R>* __restrict__ F, double scale_d,
                                               int czc, Dither dt) {
   extern __shared__ unsigned char smem_raw[];
+  pdl_wait();  // launched with launch_pdl: the previous kernel's output is read from here on
   const int ver = dither_ver(dt, blockIdx.x % dt.nb);  // plane blockIdx.x -> its field's constants
   twx = dither_ptr(twx, ver, dt.S);
   const R scale = k_misc<R>(dt, ver, 0, scale_d);
@@ -657,9 +659,8 @@ cudaError_t launch_xinv(const GridDev& g, const FftPlan& px, const cpx<R>* twx, 
   }();
   (void)attr_set;
   if (czc <= 0 || czc > g.NKz) czc = xfft_cols<R>(g);
-  k_xinv<R><<<dim3(g.Ny, ncomp, (g.NKz + czc - 1) / czc), 256, xfft_smem_bytes<R>(g, czc), st>>>(g, px, twx, W, X,
-                                                                                               czc, dt);
-  return cudaGetLastError();
+  return launch_pdl(k_xinv<R>, dim3(g.Ny, ncomp, (g.NKz + czc - 1) / czc), dim3(256), xfft_smem_bytes<R>(g, czc), st,
+                    g, px, twx, W, X, czc, dt);
 }
 
 template <typename R>
@@ -673,9 +674,8 @@ cudaError_t launch_xfwd(const GridDev& g, const FftPlan& px, const cpx<R>* twx, 
   (void)attr_set;
   const double scale = 1.0 / ((double)g.Nx * (double)g.Nz);
   if (czc <= 0 || czc > g.NKz) czc = xfft_cols<R>(g);
-  k_xfwd<R><<<dim3(g.Ny, ncomp, (g.NKz + czc - 1) / czc), 256, xfft_smem_bytes<R>(g, czc), st>>>(g, px, twx, Z, F,
-                                                                                               scale, czc, dt);
-  return cudaGetLastError();
+  return launch_pdl(k_xfwd<R>, dim3(g.Ny, ncomp, (g.NKz + czc - 1) / czc), dim3(256), xfft_smem_bytes<R>(g, czc), st,
+                    g, px, twx, Z, F, scale, czc, dt);
 }
 
 #define INST_R(R)                                                                                                   \

@@ -262,8 +262,14 @@ cfgpu_status cfgpu_set_autotune(int enable);
 /* No reference counterpart: DNS objects created while enable != 0 (the default) run the rotational form's
  * x and z transforms and product as one fused kernel per step (a thread-block cluster per y-plane,
  * distributed shared memory) when the grid allows (Nx, Nz in {32, 48, 64, 96, 128}); otherwise as three
- * kernels. Both give the same results to rounding. */
+ * kernels. Both give the same results to rounding.  With enable == 1 the fused kernel's launch shapes are
+ * timed against the three kernels and the faster kept; enable == 2 keeps the fused kernel wherever the grid
+ * allows (its shapes still timed), e.g. for profiling runs, whose timings can favour the other form. */
 cfgpu_status cfgpu_set_fused_xz(int enable);
+/* No reference counterpart: programmatic dependent launch between the kernels of a step (a kernel's launch
+ * and set-up overlap the previous kernel's tail; it waits for that kernel's results before reading them).
+ * On by default; applies to launches made afterwards (a DNS captures its step graphs on its first steps). */
+cfgpu_status cfgpu_set_pdl(int enable);
 /* No reference counterpart: the Chebyshev transforms of the rotational form's nonlinear term (the inverse
  * transform of u and curl u, the forward transform of the product) run either as dense parity-split matrix
  * products or through one complex FFT of length Ny - 1 per mode (Ny - 1 in {32, 48, 64, 96, 128}).  For DNS
