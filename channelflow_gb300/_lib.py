@@ -115,6 +115,7 @@ _SIGS = {
     "cfgpu_set_autotune": [C.c_int],
     "cfgpu_set_fused_xz": [C.c_int],
     "cfgpu_set_pdl": [C.c_int],
+    "cfgpu_set_register_zpass": [C.c_int],
     "cfgpu_set_cheb_fft": [C.c_int],
     "cfgpu_set_tau_segmented": [C.c_int],
     "cfgpu_set_cheb_tensor": [C.c_int],

@@ -13,7 +13,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcfgpu.so")
 SOURCES = ["nl_kernels.cu", "nl_forms.cu", "tau_kernels.cu", "tau_seg.cu", "diag.cu", "dns.cu", "noalloc.cu", "server.cu",
-           "transforms.cu", "cheb_dct.cu", "cheb_tc.cu", "xz_fused.cu", "xz_fused_f32.cu", "xz_fused_f64.cu", "ffio.cpp"]
+           "transforms.cu", "z_reg.cu", "cheb_dct.cu", "cheb_tc.cu", "xz_fused.cu", "xz_fused_f32.cu", "xz_fused_f64.cu", "ffio.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 

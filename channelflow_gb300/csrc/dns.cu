@@ -857,7 +857,7 @@ int nonlinear_impl(cfgpu_dns d, const double* U, void* Nout, int form) {
     CK(launch_xinv<R>(gp, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)W, (cpx<R>*)d->X6, nin, d->st, d->xcols,
                       dt));
     CK(launch_zphys<R>(gp, form, d->pz, (const cpx<R>*)d->twz, d->RP, (const cpx<R>*)d->X6, (cpx<R>*)d->Z3, d->st,
-                       dt));
+                       dt, (const cpx<R>*)d->twzf));
     CK(launch_xfwd<R>(gp, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)d->Z3, (cpx<R>*)d->F3, nout, d->st,
                       d->xcols, dt));
     d->launches += 3;
@@ -1511,7 +1511,7 @@ int autotune(cfgpu_dns d, int form, int nin, int nout) {
       if (zphys_smem_bytes<R>(gp, form, rp) > 200 * 1024) continue;
       const float t = time_ms<R>(d, [&]() {
         return launch_zphys<R>(gp, form, d->pz, (const cpx<R>*)d->twz, rp, (const cpx<R>*)d->X6, (cpx<R>*)d->Z3,
-                               d->st);
+                               d->st, kNoDither, (const cpx<R>*)d->twzf);
       });
       if (t < best) {
         best = t;
@@ -1572,7 +1572,7 @@ int tune_xz(cfgpu_dns d) {
                                        d->st, d->xcols);
         if (e == cudaSuccess)
           e = launch_zphys<R>(gp, NL_ROTATIONAL, d->pz, (const cpx<R>*)d->twz, d->RP, (const cpx<R>*)d->X6,
-                              (cpx<R>*)d->Z3, d->st);
+                              (cpx<R>*)d->Z3, d->st, kNoDither, (const cpx<R>*)d->twzf);
         if (e == cudaSuccess)
           e = launch_xfwd<R>(gp, d->px, (const cpx<R>*)d->twx, (const cpx<R>*)d->Z3, (cpx<R>*)d->F3, 3, d->st,
                              d->xcols);
@@ -3030,6 +3030,11 @@ cfgpu_status cfgpu_field_symmetry(const cfgpu_grid* grid, int dealias, int Nd, c
   return st;
 }
 
+cfgpu_status cfgpu_set_register_zpass(int enable) {
+  set_zpass_register(enable);
+  return CFGPU_OK;
+}
+
 cfgpu_status cfgpu_set_pdl(int enable) {
   g_pdl_on.store(enable ? 1 : 0);
   return CFGPU_OK;
@@ -3102,9 +3107,9 @@ cfgpu_status cfgpu_dns_host_access(cfgpu_dns d, int* direct) {
   return CFGPU_OK;
 }
 
-// Page-locking a caller's FlowField buffer maps it into every device's page tables (portable), so the
-// host-buffer kernels reach it without the host page-table walk that pageable memory needs.  Host memory only:
-// no device memory is taken.
+// Page-locking a caller's FlowField buffer (portable, mapped).  The host-buffer transfers do not change path for
+// it; on GB300 the direct kernels read and write pinned and pageable buffers at the same rate.  Host memory
+// only: no device memory is taken.
 cfgpu_status cfgpu_host_register(void* ptr, size_t bytes) {
   if (!ptr || bytes == 0) return fail(CFGPU_EINVAL, "null pointer or zero size");
   const cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterPortable | cudaHostRegisterMapped);

@@ -66,9 +66,17 @@ cudaError_t launch_grad_cheb(const GridDev& g, int N, bool gradient, const doubl
                              int bstride = 0, const Dither& dt = kNoDither);
 template <typename R>
 size_t zphys_smem_bytes(const GridDev& g, int form, int RP);
+// z pass of the x/z path (c2r, the form's products, r2c).  With twzf (the full-circle twiddle table
+// exp(-2 pi i e / Nz), e < Nz) the FP32 rotational form runs with register-resident FFTs where Nz allows
+// (launch_zrot, csrc/z_reg.cu), else the generic Stockham kernel.
 template <typename R>
 cudaError_t launch_zphys(const GridDev& g, int form, const FftPlan& pz, const cpx<R>* twz, int RP, const cpx<R>* X,
-                         cpx<R>* Z, cudaStream_t st, const Dither& dt = kNoDither);
+                         cpx<R>* Z, cudaStream_t st, const Dither& dt = kNoDither, const cpx<R>* twzf = nullptr);
+// Rotational z pass with register FFTs, FP32 (Nz in {32, 48, 64, 96, 128}, RC x rows per CTA);
+// cudaErrorNotSupported, with nothing launched, for other lengths or when switched off (set_zpass_register(0)).
+cudaError_t launch_zrot(const GridDev& g, int RC, const cpx<float>* X, cpx<float>* Z, const cpx<float>* twzf,
+                        cudaStream_t st, const Dither& dt);
+void set_zpass_register(int enable);
 template <typename R>
 size_t cheb_fwd_div_smem_bytes(int N);
 template <typename R>

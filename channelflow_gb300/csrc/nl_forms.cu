@@ -516,7 +516,15 @@ static cudaError_t launch_zphys_t(const GridDev& g, const FftPlan& pz, const cpx
 
 template <typename R>
 cudaError_t launch_zphys(const GridDev& g, int form, const FftPlan& pz, const cpx<R>* twz, int RP, const cpx<R>* X,
-                         cpx<R>* Z, cudaStream_t st, const Dither& dt) {
+                         cpx<R>* Z, cudaStream_t st, const Dither& dt, const cpx<R>* twzf) {
+  // FP32 only: in FP64 the register FFTs made the step slower (1.086 against 1.055 ms at 128x97x128), the FP64
+  // pipe favouring the Stockham kernel's radix-4 stages
+  if constexpr (sizeof(R) == 4) {
+    if (form == NL_ROTATIONAL && twzf) {
+      const cudaError_t e = launch_zrot(g, RP, X, Z, twzf, st, dt);
+      if (e != cudaErrorNotSupported) return e;
+    }
+  }
   switch (form) {
     case NL_ROTATIONAL: return launch_zphys_t<R, NL_ROTATIONAL>(g, pz, twz, RP, X, Z, st, dt);
     case NL_CONVECTION: return launch_zphys_t<R, NL_CONVECTION>(g, pz, twz, RP, X, Z, st, dt);
@@ -630,7 +638,7 @@ cudaError_t launch_rotation(const GridDev& g, int N, const double* U, const doub
                                            const R*, const R*, const R*, double, cudaStream_t, int, const Dither&); \
   template size_t zphys_smem_bytes<R>(const GridDev&, int, int);                                                   \
   template cudaError_t launch_zphys<R>(const GridDev&, int, const FftPlan&, const cpx<R>*, int, const cpx<R>*,      \
-                                       cpx<R>*, cudaStream_t, const Dither&);                                      \
+                                       cpx<R>*, cudaStream_t, const Dither&, const cpx<R>*);                       \
   template size_t cheb_fwd_div_smem_bytes<R>(int);                                                                 \
   template cudaError_t launch_cheb_fwd_div<R>(const GridDev&, int, const R*, const R*, const R*, const R*, R, R, R, \
                                               R*, const R*, const R*, const R*, const R*, cudaStream_t, const Dither&);

@@ -270,6 +270,11 @@ cfgpu_status cfgpu_set_fused_xz(int enable);
  * and set-up overlap the previous kernel's tail; it waits for that kernel's results before reading them).
  * On by default; applies to launches made afterwards (a DNS captures its step graphs on its first steps). */
 cfgpu_status cfgpu_set_pdl(int enable);
+/* No reference counterpart: the mixed path's rotational z pass in the three-kernel x/z path with
+ * register-resident four-step FFTs (enable != 0, the default; Nz in {32, 48, 64, 96, 128}) or with the generic
+ * shared-memory Stockham FFT (always in FP64).  Both give the same results to rounding.  Applies to launches
+ * made afterwards. */
+cfgpu_status cfgpu_set_register_zpass(int enable);
 /* No reference counterpart: the Chebyshev transforms of the rotational form's nonlinear term (the inverse
  * transform of u and curl u, the forward transform of the product) run either as dense parity-split matrix
  * products or through one complex FFT of length Ny - 1 per mode (Ny - 1 in {32, 48, 64, 96, 128}).  For DNS
@@ -297,10 +302,11 @@ cfgpu_status cfgpu_dns_cheb_fft(cfgpu_dns dns, int* fft);
 cfgpu_status cfgpu_set_host_access(int enable);
 cfgpu_status cfgpu_dns_host_access(cfgpu_dns dns, int* direct);
 /* No reference counterpart (the reference's FlowField data is plain pageable memory): page-lock a caller's
- * host buffer (e.g. a FlowField's data array kept for many advance calls) and map it for every device, so the
- * host-buffer transfers of cfgpu_dns_advance / set_fields / get_fields read and write it through the device's
- * own page tables; unregister before freeing the buffer.  Takes no device memory.  Registering a buffer twice,
- * or unregistering one that was not registered, is CFGPU_EINVAL. */
+ * host buffer (e.g. a FlowField's data array kept for many advance calls) and map it for every device
+ * (cudaHostRegister, portable and mapped); unregister before freeing the buffer.  The host-buffer transfers of
+ * cfgpu_dns_advance / set_fields / get_fields take the same path for it (direct kernels where the device
+ * reaches pageable memory, staged copies elsewhere); on GB300 the two run at the same rate.  Takes no device
+ * memory.  Registering a buffer twice, or unregistering one that was not registered, is CFGPU_EINVAL. */
 cfgpu_status cfgpu_host_register(void* ptr, size_t bytes);
 cfgpu_status cfgpu_host_unregister(void* ptr);
 cfgpu_status cfgpu_dns_set_profiling(cfgpu_dns dns, int enable);

@@ -155,3 +155,32 @@ def test_cheb_fft_not_used_where_the_length_does_not_factor():
 def ctypes_int():
     import ctypes
     return ctypes.c_int(-1)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol,tol_pair", [("mixed", 1e-5, 3e-6)])
+@pytest.mark.parametrize("dims", FUSED_GRIDS, ids=["%dx%dx%d" % d for d in FUSED_GRIDS])
+def test_register_zpass_matches_generic_and_oracle(dims, precision, tol, tol_pair):
+    """The mixed path's three-kernel x/z path with the register-FFT z pass (csrc/z_reg.cu) against the same
+    path with the generic Stockham z pass and against the oracle's rotationalNL."""
+    from channelflow_gb300 import DNS, build
+    from channelflow_gb300 import _lib as L
+    build.build()
+    lib = L.load()
+    g = O.Grid(dims[0], dims[1], dims[2], *COUETTE_BOX)
+    fl = O.DNSFlags(nu=1 / 400, dt=0.02, baseflow=O.LaminarBase, ulowerwall=-1.0, uupperwall=1.0)
+    u = np.ascontiguousarray(O.random_divfree_field(g, seed=3 * sum(dims), norm=0.3))
+    ref, _ = O.NSE(g, fl, None, u).nonlinear(u)
+    out = {}
+    try:
+        L.check(lib.cfgpu_set_fused_xz(0))
+        for reg in (1, 0):
+            L.check(lib.cfgpu_set_register_zpass(reg))
+            d = DNS(u.copy(), to_cgrid(g), to_cflags(fl), precision=precision)
+            out[reg] = d.nonlinear(u)
+            d.close()
+    finally:
+        L.check(lib.cfgpu_set_register_zpass(1))
+        L.check(lib.cfgpu_set_fused_xz(1))
+    assert rel_l2(out[1], ref, g) <= tol
+    assert rel_l2(out[1], out[0], g) <= tol_pair
