@@ -52,7 +52,8 @@ CNAB2, SMRK2, LaminarBase, BulkVelocity = 1, 3, 3, 1
 # DRAM bytes (read + write) per step of the mixed-path phases from `ncu --set full` captures of this workload
 # (one steady-state step: the tau solve's right-hand side, pressure/v and u/w kernels; the nonlinear pass's
 # curl/inverse Chebyshev kernel, the three x/z kernels plain runs of this grid choose, and the tensor-core
-# forward Chebyshev kernel).  Cold-cache replay: in the step the x/z intermediates stay in L2.
+# forward Chebyshev kernel).  Cold-cache replay: in the step the x/z intermediates stay in L2.  The z-pass
+# figure is the Stockham kernel's; the register-FFT z pass reads and writes the same arrays.
 NCU_TRAFFIC = {"tau_solve": (38.06 + 0.59 + 63.62 + 2.34 + 31.63 + 0.07) * 1e6,
                "nonlinear_pass": (16.32 + 0.00 + 17.74 + 1.43 + 25.13 + 0.00 + 12.60 + 0.00 + 8.26 + 0.00) * 1e6}
 

@@ -54,3 +54,9 @@ def test_argument_errors_need_no_gpu(lib):
     buf = C.create_string_buffer(64)
     assert lib.cfgpu_host_register(C.cast(buf, C.c_void_p), 0) == L.CFGPU_EINVAL
     assert lib.cfgpu_host_unregister(None) == L.CFGPU_EINVAL
+    # form switches: host-side state only (no CUDA call); out-of-range modes refused
+    assert lib.cfgpu_set_fused_xz(3) == L.CFGPU_EINVAL
+    assert lib.cfgpu_set_fused_xz(-1) == L.CFGPU_EINVAL
+    for fn in ("cfgpu_set_fused_xz", "cfgpu_set_pdl", "cfgpu_set_register_zpass"):
+        assert getattr(lib, fn)(0) == L.CFGPU_OK
+        assert getattr(lib, fn)(1) == L.CFGPU_OK
