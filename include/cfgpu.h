@@ -273,7 +273,8 @@ cfgpu_status cfgpu_set_pdl(int enable);
 /* No reference counterpart: the mixed path's rotational z pass in the three-kernel x/z path with
  * register-resident four-step FFTs (enable != 0, the default; Nz in {32, 48, 64, 96, 128}) or with the generic
  * shared-memory Stockham FFT (always in FP64).  Both give the same results to rounding.  Applies to launches
- * made afterwards. */
+ * made afterwards; a DNS replays the step graphs it captured on its first steps, so set it before creating
+ * the DNS objects whose results are to be compared bit for bit. */
 cfgpu_status cfgpu_set_register_zpass(int enable);
 /* No reference counterpart: the Chebyshev transforms of the rotational form's nonlinear term (the inverse
  * transform of u and curl u, the forward transform of the product) run either as dense parity-split matrix
