@@ -466,3 +466,126 @@ def hookstep_search(dsi, x0: np.ndarray, flags: NewtonSearchFlags | None = None,
         x = x + dxH
         Gx = GxH
     return x, Gx, info
+
+
+class Arnoldi:
+    """nsolver's Arnoldi iteration (nsolver/arnoldi.cpp:24-133): eigenvalue estimates of a linear operator A
+    known only through products A q.  Q holds the orthonormal Krylov basis, H the (n+1) x n Hessenberg matrix;
+    ew() are the eigenvalues of H_n sorted by decreasing modulus (sort_by_abs, cfbasics/cfbasics.h:1261-1276),
+    ev() the Ritz vectors Q_n W, rd() the residual estimates |q_n| |W[n-1, j]| (arnoldi.cpp:108-127; q_n is a
+    unit vector, so the estimate is |W[n-1, j]|, as in the reference).  The Gram-Schmidt step is `ortho` (the
+    FP64 GPU step by default; the reference's single modified Gram-Schmidt pass differs from it by rounding).
+    A breakdown (|w| below min_condition), where the reference exits, raises RuntimeError; an iteration past
+    niter, where the reference writes past H, raises ValueError."""
+
+    def __init__(self, b: np.ndarray, niter: int, min_condition: float = 1e-13, ortho=None):
+        b = np.asarray(b, dtype=np.float64)
+        self.M, self.niter, self.cond = b.shape[0], int(niter), float(min_condition)
+        self.H = np.zeros((self.niter + 1, self.niter))
+        self.Q = [b / np.linalg.norm(b)]
+        self.n = 0
+        self.ortho = ortho or orthogonalize
+        self._eig = None
+
+    def test_vector(self) -> np.ndarray:
+        return self.Q[self.n]
+
+    def iterate(self, Aq: np.ndarray):
+        n = self.n
+        if n == self.niter:
+            raise ValueError("Arnoldi: all %d iterations done" % self.niter)
+        w, h = self.ortho(np.array(self.Q), np.asarray(Aq, dtype=np.float64))
+        if abs(h[-1]) < self.cond:
+            raise RuntimeError("Arnoldi breakdown: |w| = %.3e below %.3e after %d iterations" % (abs(h[-1]), self.cond,
+                                                                                               n))
+        self.H[: n + 1, n] = h[:-1]
+        self.H[n + 1, n] = h[-1]
+        self.Q.append(w)
+        self.n = n + 1
+        self._eig = None
+
+    def _eigencalc(self):
+        if self._eig is None:
+            n = self.n
+            lam, W = np.linalg.eig(self.H[:n, :n])
+            order = np.argsort(-np.abs(lam), kind="stable")
+            lam, W = lam[order], W[:, order]
+            V = np.array(self.Q[:n]).T @ W
+            rd = np.linalg.norm(self.Q[n]) * np.abs(W[n - 1, :])
+            self._eig = (lam, V, rd)
+        return self._eig
+
+    def ew(self) -> np.ndarray:
+        return self._eigencalc()[0]
+
+    def ev(self) -> np.ndarray:
+        return self._eigencalc()[1]
+
+    def rd(self) -> np.ndarray:
+        return self._eigencalc()[2]
+
+
+@dataclass
+class EigenvalsFlags:
+    """EigenvalsFlags (nsolver/eigenvals.h:16-44, the defaults of nsolver/eigenvals.cpp:46-59): Arnoldi
+    iterations, stable eigenvalues kept beyond the unstable and marginal ones (or exactly Nstable when
+    fixedNs), Krylov breakdown threshold, centred differences, the margin below which Re(lambda) counts as
+    stable.  The Lanczos variant for normal operators (isnormal) is not restated."""
+    Narnoldi: int = 100
+    Nstable: int = 5
+    fixedNs: bool = False
+    EPS_kry: float = 1e-10
+    centdiff: bool = False
+    EPS_stab: float = 1e-6
+
+
+def eigenvals(dsi, x: np.ndarray, dx: np.ndarray, T: float, eps: float = 1e-7,
+              flags: EigenvalsFlags | None = None, ortho=None, log=None) -> dict:
+    """Eigenvals::solve (nsolver/eigenvals.cpp:118-279), the Arnoldi iteration behind findeigenvals: the
+    eigenvalues Lambda of the linearised map Df^T at a fixed point x of f^T (G(x) = 0), from products
+        A q = (f^T(x + eps q) - f^T(x)) / eps,
+    which DSI::Jacobian gives with Gx = -eps q (G = f^T(u) - u, so G(x + eps q) + eps q = f^T(x + eps q) - x);
+    with centred differences Jacobian returns (f^T(x + eps q/2) - f^T(x - eps q/2)) / eps - q and q is added
+    back.  Each iteration is one f^T evaluation (two with centdiff, submitted together to the server when dsi
+    has one) and depends on the previous one, so the iteration itself is sequential.  Growth rates
+    lambda = log(Lambda) / T.
+
+    Returns {"Lambda", "lambda", "residual" (the last iteration's), "Nnonstable", "Nsave", "eigvecs": the
+    saved eigenfunctions as vectors (a complex pair as its real and imaginary parts, eigenvals.cpp:250-271),
+    "history": per iteration the leading Lambda and their residuals, "fcount"}."""
+    f = flags or EigenvalsFlags()
+    say = log or (lambda *a: None)
+    dx = np.asarray(dx, dtype=np.float64)
+    dx = dx / np.linalg.norm(dx)
+    arn = Arnoldi(dx, f.Narnoldi, f.EPS_kry, ortho=ortho)
+    history = []
+    fcount0 = getattr(dsi, "fcount", 0)
+    for n in range(f.Narnoldi):
+        q = arn.test_vector()
+        Gx = -eps * q
+        Aq = dsi.jacobian(x, q, Gx, eps, f.centdiff)
+        if f.centdiff:
+            Aq = Aq + q
+        arn.iterate(Aq)
+        Lam, rd = arn.ew(), arn.rd()
+        lam = np.log(Lam.astype(complex)) / T
+        nns = int(np.sum(lam.real >= -f.EPS_stab))
+        nsave = min(Lam.shape[0], f.Nstable if f.fixedNs else nns + f.Nstable)
+        history.append({"Lambda": Lam[:nsave].copy(), "residual": rd[:nsave].copy()})
+        say("Arnoldi %d: |Lambda_0| = %.12g, residual %.3e" % (n, abs(Lam[0]), rd[0]))
+    Lam, V, rd = arn.ew(), arn.ev(), arn.rd()
+    lam = np.log(Lam.astype(complex)) / T
+    nns = int(np.sum(lam.real >= -f.EPS_stab))
+    nsave = min(Lam.shape[0], f.Nstable if f.fixedNs else nns + f.Nstable)
+    eigvecs = []
+    j = 0
+    while j < nsave:
+        if Lam[j].imag == 0.0:
+            eigvecs.append((j, V[:, j].real.copy()))
+        elif j + 1 < Lam.shape[0]:
+            eigvecs.append((j, V[:, j].real.copy()))
+            eigvecs.append((j + 1, V[:, j].imag.copy()))
+            j += 1
+        j += 1
+    return {"Lambda": Lam, "lambda": lam, "residual": rd, "Nnonstable": nns, "Nsave": nsave, "eigvecs": eigvecs,
+            "history": history, "fcount": getattr(dsi, "fcount", 0) - fcount0}
