@@ -2,8 +2,9 @@
 nsolver/eigenvals.cpp:118-279, the iteration behind findeigenvals) on the host.
 
 The operator is a matrix with known eigenvalues (a complex pair among them), reached either directly or, as in
-findeigenvals, through DSI::Jacobian (nsolver/dsi.cpp:66-88) of a map f^T with a fixed point; the Gram-Schmidt
-step is the host form of the GPU step.  CPU only.
+findeigenvals, through DSI::Jacobian (nsolver/dsi.cpp:66-88) of a map f^T with a fixed point, and the DNS map
+of the reference's Orr-Sommerfeld test (the oracle's DNS) whose least stable eigenvalue is the reference's
+fixture; the Gram-Schmidt step is the host form of the GPU step.  CPU only.
 """
 
 import numpy as np
@@ -120,3 +121,58 @@ def test_eigenvals_of_a_map_at_its_fixed_point(centdiff):
     l1 = lam[1]
     w = vr + 1j * vi
     assert np.linalg.norm(A @ w - l1 * w) <= 1e-4 * np.linalg.norm(w)
+
+
+def test_eigenvals_find_the_orr_sommerfeld_mode():
+    """findeigenvals' use on a physical map: f^T of the plane-Poiseuille DNS of the reference's Orr-Sommerfeld
+    test (Re = 7500, 4 x 65 x 4, SBDF3, dt = 0.02; the oracle's DNS) on the kx = 1 coefficients, T = 2,
+    linearised about the laminar state by DSI::Jacobian's finite differences.  Started from the reference's
+    eigenfunction (tests/data/os_ueig10_65.asc) plus noise, six Arnoldi iterations give the least stable
+    mode's growth rate and frequency -i omega (os_omega10_65.cmplx) to 5e-5 (2e-5 measured; nine iterations:
+    1e-5)."""
+    from oracle import cf_oracle as O
+    from tests.test_orrsommerfeld import GOLD, os_case
+
+    d = np.load(GOLD)
+    omega = complex(d["omega"])
+    g, fl, base, _ = os_case()
+    T = 2.0
+    nsteps = int(round(T / fl.dt))
+    n = 3 * g.Ny
+
+    def field(x):
+        c = (x[:n] + 1j * x[n:]).reshape(3, g.Ny)
+        u = np.zeros((3, g.Ny, g.Nx, g.Mz), complex)
+        u[:, :, 1, 0] = c
+        u[:, :, g.Nx - 1, 0] = np.conj(c)          # kx = -1: the conjugate (real field, kz = 0)
+        return u
+
+    def vec(u):
+        c = u[:, :, 1, 0].reshape(-1)
+        return np.concatenate([c.real, c.imag])
+
+    class OSMap:
+        fcount = 0
+
+        def eval(self, x):
+            self.fcount += 1
+            u = field(x)
+            q = np.zeros((1, g.Ny, g.Nx, g.Mz), complex)
+            u, _ = O.DNS(u.copy(), q.copy(), g, fl, base=base).advance(u, q, nsteps)
+            return vec(u) - x
+
+        def jacobian(self, x, dx, Gx, epsDx=1e-7, centdiff=False):
+            m = float(np.linalg.norm(dx))
+            eps = 1.0 if m < epsDx else epsDx / m
+            return (self.eval(x + eps * dx) - Gx) / eps
+
+    dx = vec(O.basisfunc_field(d["ueig"], 1, 0, g))
+    dx = dx / np.linalg.norm(dx) + 1e-3 * np.random.default_rng(1).standard_normal(2 * n) / np.sqrt(2 * n)
+    res = eigenvals(OSMap(), np.zeros(2 * n), dx, T, eps=1e-7, flags=EigenvalsFlags(Narnoldi=6, Nstable=1),
+                    ortho=_numpy_ortho)
+    lead = res["lambda"][:2]                         # the conjugate pair of the least stable mode
+    exact = -1j * omega
+    best = lead[np.argmin(np.abs(lead - exact))]
+    assert abs(best.real - exact.real) < 5e-5 and abs(best.imag - exact.imag) < 5e-5, (best, exact)
+    assert res["Nnonstable"] == 2                    # the growing pair (Im omega > 0)
+    assert res["residual"][0] < 1e-3
