@@ -3,7 +3,7 @@ bisection round classified together in one batched GPU ensemble.
 
 Restated from the reference:
 
-* attractor (edgetracking.cpp:842-893): a field is turbulent if its cross-flow energy Ecf and/or its L2 norm
+* attractor (edgetracking.cpp:836-893): a field is turbulent if its cross-flow energy Ecf and/or its L2 norm
   are at or above the high thresholds, laminar if at or below the low ones (only the criteria whose two
   thresholds are both set count), and laminar as well once Ecf has not grown for more than tMaxDecay time
   units; both at once is an error, neither is "no attractor";
@@ -15,12 +15,16 @@ Restated from the reference:
   j >= 3, uL the candidate of j - 2.  The reference integrates the candidates one after the other; here the
   n of a round run as one ensemble (the next block of candidates only if all were laminar), which gives
   the same choice because the trajectories are independent;
-* CalcAttractor (edgetracking.cpp:766-817): integrate one time unit at a time until the attractor is known
+* CalcAttractor (edgetracking.cpp:767-818): integrate one time unit at a time until the attractor is known
   (after tMin) or tMax is reached.  The ensemble shares one dt, so each candidate runs at the flags' fixed dt
   where the reference adapts each trajectory's dt to its CFL number.
 
-Not restated: the tracking loop around the bisection (AdvanceLH, ChooseNewLH, the convergence check) and
-the output files.
+* ChooseNewLH (edgetracking.cpp:659-715), AdvanceLH (:472-657) with its equilibrium and periodic-orbit
+  checks on Ecf, and the tracking loop EdgeStateTracking (:284-327); uL and uH advance as the two slots of one
+  ensemble.
+
+Not restated: the output files (energies, saved fields, continuation) and the symmetry projection of the
+initial field.
 """
 
 from __future__ import annotations
@@ -62,7 +66,7 @@ def ecf(u: np.ndarray, Nx: int, Nz: int, a: float = -1.0, b: float = 1.0) -> flo
 
 def attractor(l2: float, ecf_value: float, flags: AttractorFlags, height: float = 2.0, tdecay: int = 0,
               last_ecf: float = 0.0):
-    """attractor(u, tDecay, lastEcf, flags) (edgetracking.cpp:848-893) from the field's L2 norm and Ecf.
+    """attractor(u, tDecay, lastEcf, flags) (edgetracking.cpp:836-893) from the field's L2 norm and Ecf.
     Returns (LAMINAR, TURBULENT or None, the updated decay counter)."""
     use_ecf = flags.EcfH > 1e-12 and flags.EcfL > 1e-12
     use_l2 = flags.L2H > 1e-12 and flags.L2L > 1e-12
@@ -210,3 +214,183 @@ def bisection(uL: np.ndarray, uH: np.ndarray, classify, Nx: int, Nz: int, flags:
         say("bisection round %d: RelL2Diff %.3e" % (info["rounds"], l2d))
     info["lambdaL"], info["lambdaH"] = lamL, lamH
     return uL, uH, info
+
+
+@dataclass
+class TrackingFlags(BisectionFlags):
+    """The remaining EdgetrackingFlags of the tracking loop (edgetracking.cpp:138-160, defaults :724-748):
+    separation at which advancing stops, lambda step of the choice of new fields, whether to keep integrating
+    after separation to verify the attractors, whether the new fields are built from uL instead of uH, and
+    the equilibrium / periodic-orbit detection on the cross-flow energy."""
+    epsilonAdvance: float = 1e-4
+    lambdaStep: float = 0.1
+    verifyLH: bool = False
+    keepUL: bool = False
+    checkConvergence: bool = False
+
+
+def choose_new_lh(u0: np.ndarray, classify, lamL: float, lamH: float, lambda_step: float):
+    """ChooseNewLH (edgetracking.cpp:659-715): raise lambdaH until lambdaH u0 is turbulent (a laminar one
+    becomes the new lambdaL), then lower lambdaL until lambdaL u0 is laminar (a turbulent one becomes the new
+    lambdaH; with lambdaL == lambdaH on entry lambdaL starts one step lower).  Returns (lambdaL, lambdaH)."""
+    if lamL > lamH:
+        raise ValueError("lambdaL > lambdaH")
+    equal = lamH == lamL
+    aH, aL = None, None
+    while aH != TURBULENT:
+        aH = classify([lamH * u0])[0]
+        if aH == LAMINAR:
+            lamL = lamH
+            lamH += lambda_step
+            aL = LAMINAR
+        elif aH is None:
+            raise RuntimeError("choose_new_lh: lambda = %g reaches no attractor" % lamH)
+    while aL != LAMINAR:
+        if equal:
+            lamL -= lambda_step
+            equal = False
+        aL = classify([lamL * u0])[0]
+        if aL == TURBULENT:
+            lamH = lamL
+            lamL -= lambda_step
+        elif aL is None:
+            raise RuntimeError("choose_new_lh: lambda = %g reaches no attractor" % lamL)
+    return lamL, lamH
+
+
+class EnsemblePair:
+    """uL and uH as the two slots of one ensemble (one set of launches for both), advanced one time unit
+    (`steps_per_unit` steps) per call; `make_ensemble(2)` as for EnsembleClassifier."""
+
+    def __init__(self, grid, flags, uL, uH, steps_per_unit: int, precision: str = "fp64", make_ensemble=None):
+        if make_ensemble is None:
+            from .dns import Ensemble
+
+            def make_ensemble(n):
+                return Ensemble(grid, flags, n, precision=precision)
+        self.ens = make_ensemble(2)
+        self.steps = int(steps_per_unit)
+        self.ens.set_field(0, np.ascontiguousarray(uL))
+        self.ens.set_field(1, np.ascontiguousarray(uH))
+        self._u = np.zeros_like(uL)
+        self._q = np.zeros((1,) + uL.shape[1:], dtype=uL.dtype)
+
+    def advance(self):
+        self.ens.advance_resident(self.steps)
+
+    def fields(self):
+        out = []
+        for i in (0, 1):
+            self.ens.get_field(i, self._u, self._q)
+            out.append(self._u.copy())
+        return out[0], out[1]
+
+    def close(self):
+        self.ens.close()
+
+
+def advance_lh(uL0: np.ndarray, uH0: np.ndarray, t: int, T: float, grid, flags: TrackingFlags,
+               aflags: AttractorFlags, pair, cd: dict | None = None, log=None):
+    """AdvanceLH (edgetracking.cpp:472-657): advance uL and uH (pair, e.g. an EnsemblePair started from them)
+    one time unit at a time while RelL2Diff(uL, uH) < epsilonAdvance, counting t; uL0, uH0 follow the last
+    states on the edge.  After the separation, with verifyLH, keep going (at most tMaxAttractor units) until uL
+    is laminar and uH turbulent; without it, either reaching its attractor is an error (the thresholds are
+    wrong), as is reaching it within two units.  With checkConvergence, a constant Ecf over 100 units (a
+    relative equilibrium) or repeating Ecf extrema (a periodic orbit) ends the call early (the states of that
+    unit are not kept, as in the reference).  Returns (uL0, uH0, t, finished: t == T or converged, cd), cd the
+    extrema record kept across calls."""
+    say = log or (lambda *a: None)
+    g = grid
+    cd = cd if cd is not None else {"EcfMax": [0.0] * 4, "EcfMin": [0.0] * 4, "tEcfMin": [0] * 4}
+
+    def push(a, b):
+        a[:] = a[1:] + [b]
+
+    t0 = t
+    t2 = float(t)
+    t_att = flags.tMaxAttractor + t
+    turbulent = laminar = False
+    on_edge = True
+    ecf0 = ecf1 = ecf2 = 0.0
+    ring = [0.0] * 100
+    try:
+        while (not turbulent or not laminar) and t <= T and (on_edge or (flags.verifyLH and t2 <= t_att)):
+            t2 += 1
+            pair.advance()
+            fL, fH = pair.fields()
+            if on_edge:
+                l2d = rel_l2_diff(fL, fH, g.Nx, g.Nz)
+                if l2d < flags.epsilonAdvance:
+                    t += 1
+                    ecf2, ecf1, ecf0 = ecf1, ecf0, ecf(fH, g.Nx, g.Nz, g.a, g.b)
+                    ecf_min = ecf1 < ecf2 and ecf1 <= ecf0
+                    ecf_max = ecf1 > ecf2 and ecf1 >= ecf0
+                    if flags.checkConvergence:
+                        ring[t % len(ring)] = ecf0
+                        if all(e >= 1e-16 and abs(e - ring[0]) / ring[0] <= flags.epsilonBisection for e in ring):
+                            say("Ecf is constant: converged to a (relative) equilibrium")
+                            return uL0, uH0, t, True, cd
+                        if ecf_max:
+                            push(cd["EcfMax"], ecf0)
+                        if ecf_min:
+                            push(cd["EcfMin"], ecf0)
+                            push(cd["tEcfMin"], t)
+                            mx, mn, tm = cd["EcfMax"], cd["EcfMin"], cd["tEcfMin"]
+                            eps = 1e-3
+                            if (abs(mx[0] - mx[2]) / ecf0 < eps and abs(mx[1] - mx[3]) / ecf0 < eps and
+                                    abs(mn[0] - mn[2]) / ecf0 < eps and abs(mn[1] - mn[3]) / ecf0 < eps and
+                                    abs((tm[3] - tm[1]) - (tm[2] - tm[0])) < 5):
+                                say("converged to a periodic orbit")
+                                return uL0, uH0, t, True, cd
+                    uL0, uH0 = fL, fH
+                else:
+                    on_edge = False
+                    say("fields separated by %.3e at t = %d" % (l2d, t))
+            if not turbulent and attractor(l2norm(fH, g.Nx, g.Nz), ecf(fH, g.Nx, g.Nz, g.a, g.b), aflags,
+                                           g.b - g.a)[0] == TURBULENT:
+                turbulent = True
+                if not flags.verifyLH:
+                    raise RuntimeError("uH is turbulent, check the thresholds")
+                if t2 - t0 <= 2:
+                    raise RuntimeError("uH turbulent within two time units, check the thresholds")
+            if not laminar and attractor(l2norm(fL, g.Nx, g.Nz), ecf(fL, g.Nx, g.Nz, g.a, g.b), aflags,
+                                         g.b - g.a)[0] == LAMINAR:
+                laminar = True
+                if not flags.verifyLH:
+                    raise RuntimeError("uL is laminar, check the thresholds")
+                if t2 - t0 <= 2:
+                    raise RuntimeError("uL laminar within two time units, check the thresholds")
+    finally:
+        pair.close()
+    if flags.verifyLH and not laminar:
+        raise RuntimeError("verifyLH: uL does not become laminar")
+    if flags.verifyLH and not turbulent:
+        raise RuntimeError("verifyLH: uH does not become turbulent")
+    return uL0, uH0, t, t == T, cd
+
+
+def edge_tracking(uL: np.ndarray, uH: np.ndarray, t0: int, T: float, grid, flags: TrackingFlags,
+                  aflags: AttractorFlags, classify, make_pair, log=None) -> dict:
+    """EdgeStateTracking (edgetracking.cpp:284-327): bisect uL, uH to the edge, advance them along it until
+    they separate, choose new fields lambda u from the last edge state (uH, or uL with keepUL), repeat until
+    t > T.  make_pair(uL, uH) builds the pair advance_lh integrates (e.g. an EnsemblePair).  As in the
+    reference, whose `finished` is redeclared inside the loop, a converged or finished advance only skips the
+    choice of new fields; the loop ends with t > T.  Returns {"uL", "uH", "t", "bisections": [(t, rounds)],
+    "lambdas": [(lambdaL, lambdaH)]}."""
+    say = log or (lambda *a: None)
+    g = grid
+    t = int(t0)
+    out = {"bisections": [], "lambdas": []}
+    cd = None
+    while t <= T:
+        uL, uH, info = bisection(uL, uH, classify, g.Nx, g.Nz, flags, log)
+        out["bisections"].append((t, info["rounds"]))
+        uL, uH, t, finished, cd = advance_lh(uL, uH, t, T, g, flags, aflags, make_pair(uL, uH), cd, log)
+        if not finished:
+            u = uL if flags.keepUL else uH
+            lamL, lamH = choose_new_lh(u, classify, 1.0, 1.0, flags.lambdaStep)
+            out["lambdas"].append((lamL, lamH))
+            say("t = %d: new lambdaL %.4g, lambdaH %.4g" % (t, lamL, lamH))
+            uL, uH = lamL * u, lamH * u
+    out.update(uL=uL, uH=uH, t=t)
+    return out

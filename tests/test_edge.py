@@ -146,3 +146,74 @@ def test_bisection_without_a_turbulent_candidate_fails():
                              make_ensemble=ToyEnsemble)
     with pytest.raises(RuntimeError):
         bisection(0.01 * e, 0.02 * e, cls, NX, NZ, BisectionFlags(nBisectTrajectories=3))
+
+
+class SlowEdgeEnsemble(ToyEnsemble):
+    """Norm a -> EDGE + G (a - EDGE) per step, clipped to [0, 1]: the edge |u| = EDGE is unstable, so a pair
+    started on it stays together for a number of steps before it separates."""
+    G = 1.5
+
+    def advance_resident(self, nsteps):
+        self.steps += nsteps
+        for i, u in enumerate(self.u):
+            for _ in range(nsteps):
+                a = l2norm(u, NX, NZ)
+                a2 = min(1.0, max(0.0, EDGE + self.G * (a - EDGE)))
+                u = u * (a2 / a) if a > 0 else u
+            self.u[i] = u
+
+
+def slow_classifier(tmax=400):
+    return EnsembleClassifier(ToyGrid(), None, AttractorFlags(L2H=0.5, L2L=0.01), steps_per_unit=1, tmax=tmax,
+                              make_ensemble=SlowEdgeEnsemble)
+
+
+def test_choose_new_lh_brackets_the_edge():
+    from channelflow_gb300.edge import choose_new_lh
+    e = unit_field(21)
+    # u0 on the turbulent side: lambdaH = 1 is turbulent, lambdaL steps down to the first laminar value
+    lamL, lamH = choose_new_lh(0.15 * e, slow_classifier(), 1.0, 1.0, 0.1)
+    assert math.isclose(lamH, 1.0 - 0.3, abs_tol=1e-12) and math.isclose(lamL, 1.0 - 0.4, abs_tol=1e-12)
+    # u0 on the laminar side: lambdaH steps up until turbulent, the last laminar one becomes lambdaL
+    lamL, lamH = choose_new_lh(0.07 * e, slow_classifier(), 1.0, 1.0, 0.1)
+    assert math.isclose(lamL, 1.4, abs_tol=1e-12) and math.isclose(lamH, 1.5, abs_tol=1e-12)
+    with pytest.raises(ValueError):
+        choose_new_lh(e, slow_classifier(), 2.0, 1.0, 0.1)
+
+
+def test_edge_tracking_follows_the_edge():
+    from channelflow_gb300.edge import EnsemblePair, TrackingFlags, edge_tracking
+    e1, e2 = unit_field(31), unit_field(32)
+    fl = TrackingFlags(epsilonBisection=1e-7, epsilonAdvance=1e-4, lambdaStep=0.1)
+
+    def make_pair(uL, uH):
+        return EnsemblePair(ToyGrid(), None, uL, uH, 1, make_ensemble=SlowEdgeEnsemble)
+
+    out = edge_tracking(0.05 * e1, 0.3 * e2, 0, 40, ToyGrid(), fl, AttractorFlags(L2H=0.5, L2L=0.01),
+                        slow_classifier(), make_pair)
+    assert out["t"] > 40
+    assert len(out["bisections"]) >= 2 and len(out["lambdas"]) >= 1
+    # every cycle ends near the edge: the last states bracket it
+    assert l2norm(out["uL"], NX, NZ) < EDGE < l2norm(out["uH"], NX, NZ) + 1e-9
+    assert abs(l2norm(out["uH"], NX, NZ) - EDGE) < 1e-3
+    for lamL, lamH in out["lambdas"]:
+        assert lamL < lamH
+
+
+def test_advance_lh_detects_a_relative_equilibrium_and_misplaced_thresholds():
+    from channelflow_gb300.edge import EnsemblePair, TrackingFlags, advance_lh
+
+    class Still(SlowEdgeEnsemble):
+        G = 1.05
+
+    e = unit_field(41)
+    uH = EDGE * e                       # exactly on the edge: stays there, Ecf constant
+    uL = EDGE * (1 - 1e-10) * e
+    fl = TrackingFlags(epsilonBisection=1e-6, epsilonAdvance=1e-4, checkConvergence=True)
+    pair = EnsemblePair(ToyGrid(), None, uL, uH, 1, make_ensemble=Still)
+    _, _, t, finished, _ = advance_lh(uL, uH, 0, 1000, ToyGrid(), fl, AttractorFlags(L2H=0.5, L2L=0.01), pair)
+    assert finished and 100 <= t <= 101
+    # thresholds that call the edge state turbulent are an error without verifyLH
+    pair = EnsemblePair(ToyGrid(), None, uL, uH, 1, make_ensemble=Still)
+    with pytest.raises(RuntimeError):
+        advance_lh(uL, uH, 0, 1000, ToyGrid(), TrackingFlags(), AttractorFlags(L2H=0.05, L2L=0.01), pair)
