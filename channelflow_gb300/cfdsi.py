@@ -525,12 +525,51 @@ class Arnoldi:
         return self._eigencalc()[2]
 
 
+class Lanczos(Arnoldi):
+    """nsolver's Lanczos iteration for normal (self-adjoint) operators (nsolver/lanczos.cpp:23-93): the
+    tridiagonal T with T[n, n] = <q_n, A q_n - T[n-1, n] q_{n-1}> and T[n+1, n] = T[n, n+1] = |w|, w
+    reorthogonalised against every earlier q (the reference's full modified Gram-Schmidt pass); ew() from the
+    symmetric eigenproblem of T_n, sorted by decreasing modulus; ev() and rd() as for Arnoldi."""
+
+    def iterate(self, Aq: np.ndarray):
+        n = self.n
+        if n == self.niter:
+            raise ValueError("Lanczos: all %d iterations done" % self.niter)
+        v = np.array(Aq, dtype=np.float64, copy=True)
+        if n != 0:
+            v -= self.H[n - 1, n] * self.Q[n - 1]
+        self.H[n, n] = float(self.Q[n] @ v)
+        for q in self.Q:
+            v -= float(q @ v) * q
+        vnorm = float(np.linalg.norm(v))
+        if vnorm < self.cond:
+            raise RuntimeError("Lanczos breakdown: |w| = %.3e below %.3e after %d iterations" % (vnorm, self.cond, n))
+        if n + 1 < self.niter:
+            self.H[n, n + 1] = vnorm
+        self.H[n + 1, n] = vnorm
+        self.Q.append(v / vnorm)
+        self.n = n + 1
+        self._eig = None
+
+    def _eigencalc(self):
+        if self._eig is None:
+            n = self.n
+            lam, W = np.linalg.eigh(self.H[:n, :n])
+            order = np.argsort(-np.abs(lam), kind="stable")
+            lam, W = lam[order].astype(complex), W[:, order]
+            V = (np.array(self.Q[:n]).T @ W).astype(complex)
+            rd = np.linalg.norm(self.Q[n]) * np.abs(W[n - 1, :])
+            self._eig = (lam, V, rd)
+        return self._eig
+
+
 @dataclass
 class EigenvalsFlags:
     """EigenvalsFlags (nsolver/eigenvals.h:16-44, the defaults of nsolver/eigenvals.cpp:46-59): Arnoldi
     iterations, stable eigenvalues kept beyond the unstable and marginal ones (or exactly Nstable when
     fixedNs), Krylov breakdown threshold, centred differences, the margin below which Re(lambda) counts as
-    stable.  The Lanczos variant for normal operators (isnormal) is not restated."""
+    stable; isnormal selects the Lanczos iteration (self-adjoint operators)."""
+    isnormal: bool = False
     Narnoldi: int = 100
     Nstable: int = 5
     fixedNs: bool = False
@@ -557,7 +596,7 @@ def eigenvals(dsi, x: np.ndarray, dx: np.ndarray, T: float, eps: float = 1e-7,
     say = log or (lambda *a: None)
     dx = np.asarray(dx, dtype=np.float64)
     dx = dx / np.linalg.norm(dx)
-    arn = Arnoldi(dx, f.Narnoldi, f.EPS_kry, ortho=ortho)
+    arn = Lanczos(dx, f.Narnoldi, f.EPS_kry) if f.isnormal else Arnoldi(dx, f.Narnoldi, f.EPS_kry, ortho=ortho)
     history = []
     fcount0 = getattr(dsi, "fcount", 0)
     for n in range(f.Narnoldi):

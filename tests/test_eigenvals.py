@@ -176,3 +176,28 @@ def test_eigenvals_find_the_orr_sommerfeld_mode():
     assert abs(best.real - exact.real) < 5e-5 and abs(best.imag - exact.imag) < 5e-5, (best, exact)
     assert res["Nnonstable"] == 2                    # the growing pair (Im omega > 0)
     assert res["residual"][0] < 1e-3
+
+
+def test_lanczos_for_a_self_adjoint_operator():
+    """Lanczos (nsolver/lanczos.cpp): the extreme eigenvalues of a symmetric matrix, through eigenvals with
+    isnormal as findeigenvals selects it."""
+    from channelflow_gb300.cfdsi import Lanczos
+    n = 70
+    rng = np.random.default_rng(7)
+    Qm, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    ev = np.concatenate([[1.8, -1.5, 1.2], rng.uniform(-0.3, 0.3, n - 3)])
+    A = (Qm * ev) @ Qm.T
+    lz = Lanczos(rng.standard_normal(n), 30, 1e-13)
+    for _ in range(30):
+        lz.iterate(A @ lz.test_vector())
+    lam = lz.ew()
+    assert np.allclose(lam[:3].real, [1.8, -1.5, 1.2], atol=1e-10) and np.all(lam.imag == 0)
+    v = lz.ev()[:, 0].real
+    assert np.linalg.norm(A @ v - 1.8 * v) < 1e-8 * np.linalg.norm(v)
+    # the tridiagonal matrix is symmetric
+    T = lz.H[:30, :30]
+    assert np.allclose(T, T.T)
+    dsi = LinearMap(A, 8)
+    res = eigenvals(dsi, dsi.xs, rng.standard_normal(n), 1.0, eps=1e-7,
+                    flags=EigenvalsFlags(isnormal=True, Narnoldi=30, Nstable=1, centdiff=True))
+    assert np.allclose(res["Lambda"][:3].real, [1.8, -1.5, 1.2], atol=1e-6)
