@@ -217,3 +217,23 @@ def test_advance_lh_detects_a_relative_equilibrium_and_misplaced_thresholds():
     pair = EnsemblePair(ToyGrid(), None, uL, uH, 1, make_ensemble=Still)
     with pytest.raises(RuntimeError):
         advance_lh(uL, uH, 0, 1000, ToyGrid(), TrackingFlags(), AttractorFlags(L2H=0.05, L2L=0.01), pair)
+
+
+def test_advance_lh_detects_a_periodic_orbit():
+    """Ecf of uH oscillating with period 10 on the edge: after four maxima and four minima at equal spacing
+    AdvanceLH's periodic-orbit check ends the advance (edgetracking.cpp:562-580)."""
+    from channelflow_gb300.edge import EnsemblePair, TrackingFlags, advance_lh
+
+    class Periodic(ToyEnsemble):
+        def advance_resident(self, nsteps):
+            self.steps += nsteps
+            a = EDGE * (1.0 + 0.05 * math.sin(2 * math.pi * self.steps / 10.0))
+            self.u = [u * (a / l2norm(u, NX, NZ)) for u in self.u]
+
+    e = unit_field(51)
+    fl = TrackingFlags(checkConvergence=True)
+    pair = EnsemblePair(ToyGrid(), None, EDGE * e, EDGE * e, 1, make_ensemble=Periodic)
+    _, _, t, finished, cd = advance_lh(EDGE * e, EDGE * e, 0, 1000, ToyGrid(), fl,
+                                       AttractorFlags(L2H=0.5, L2L=0.01), pair)
+    assert finished and t < 60
+    assert all(x > 0 for x in cd["EcfMin"]) and cd["tEcfMin"][3] - cd["tEcfMin"][2] == 10
